@@ -1,0 +1,1168 @@
+/* g4oracle.c — plain-C FP64 restatement of the GENESIS 1.3 v4 undulator step.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker and the timed CPU baseline); the product
+ * never calls it. Compile with -ffp-contract=off so that every floating-point
+ * operation rounds as the reference's (no fused multiply-add), and with C99
+ * complex arithmetic, which GCC lowers exactly as it lowers std::complex<double>.
+ * Citations are file:line in GENESIS 1.3 v4.6.14.
+ */
+#include "g4oracle.h"
+
+#define _GNU_SOURCE
+#include <complex.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef double complex cplx;
+
+/* physical constants, GenMain.cpp:63-68 */
+static const double kVacimp = 376.73;
+static const double kEev = 510998.95069;
+static const double kCe = 4.8032045e-11;
+static const double kPi = 3.14159265358979323846;
+
+/* ------------------------------------------------------------------------- */
+/* host thread pool: a parallel-for over [0, n)                              */
+/* ------------------------------------------------------------------------- */
+typedef void (*range_fn)(void *ctx, int i0, int i1);
+struct pf_arg {
+  range_fn fn;
+  void *ctx;
+  int i0, i1;
+};
+static void *pf_thread(void *p) {
+  struct pf_arg *a = (struct pf_arg *)p;
+  a->fn(a->ctx, a->i0, a->i1);
+  return NULL;
+}
+static void parallel_for(int n, int nthreads, range_fn fn, void *ctx) {
+  if (nthreads <= 1 || n <= 1) {
+    fn(ctx, 0, n);
+    return;
+  }
+  if (nthreads > n) nthreads = n;
+  pthread_t th[256];
+  struct pf_arg args[256];
+  if (nthreads > 256) nthreads = 256;
+  for (int t = 0; t < nthreads; t++) {
+    args[t].fn = fn;
+    args[t].ctx = ctx;
+    args[t].i0 = (int)((long long)n * t / nthreads);
+    args[t].i1 = (int)((long long)n * (t + 1) / nthreads);
+    pthread_create(&th[t], NULL, pf_thread, &args[t]);
+  }
+  for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+}
+
+/* ------------------------------------------------------------------------- */
+/* random streams                                                            */
+/* ------------------------------------------------------------------------- */
+/* ran2 with Bays-Durham shuffle, RandomU.cpp:17-33 (seeding) and :46-73 (draw) */
+typedef struct {
+  int iv[32], iy, iseed, iseed2;
+} ran2_t;
+
+static void ran2_init(ran2_t *r, unsigned int istart) {
+  const int ia1 = 40014, im1 = 2147483563, iq1 = 53668, ir1 = 12211, ntab = 32;
+  /* RandomU.cpp:28: the comparison is unsigned, the stored seed an int */
+  r->iseed = (1u < istart) ? (int)istart : 1;
+  r->iseed2 = r->iseed;
+  for (int i = ntab + 7; i >= 0; i--) {
+    int k = r->iseed / iq1;
+    r->iseed = ia1 * (r->iseed - k * iq1) - k * ir1;
+    if (r->iseed < 0) r->iseed += im1;
+    if (i < ntab) r->iv[i] = r->iseed;
+  }
+  r->iy = r->iv[0];
+}
+
+static double ran2_next(ran2_t *r) {
+  const int ia1 = 40014, ia2 = 40692, im1 = 2147483563, im2 = 2147483399;
+  const int imm1 = 2147483562, iq1 = 53668, iq2 = 52774, ir1 = 12211, ir2 = 3791;
+  const int ndiv = 67108862;
+  const double am = 1. / 2147483563;
+  const double rnmx = 1. - 1.2e-40;
+  int k = r->iseed / iq1;
+  r->iseed = ia1 * (r->iseed - k * iq1) - k * ir1;
+  if (r->iseed < 0) r->iseed = r->iseed + im1;
+  k = r->iseed2 / iq2;
+  r->iseed2 = ia2 * (r->iseed2 - k * iq2) - k * ir2;
+  if (r->iseed2 < 0) r->iseed2 = r->iseed2 + im2;
+  int j = r->iy / ndiv;
+  r->iy = r->iv[j] - r->iseed2;
+  r->iv[j] = r->iseed;
+  if (r->iy < 1) r->iy = r->iy + imm1;
+  return (am * r->iy < rnmx) ? am * r->iy : rnmx;
+}
+
+void orc_ran2(int seed, int n, double *out) {
+  ran2_t r;
+  ran2_init(&r, (unsigned int)seed);
+  for (int i = 0; i < n; i++) out[i] = ran2_next(&r);
+}
+
+/* radical-inverse (Hammersley) sequence, Hammerslay.cpp:15-49 */
+static const double kHamBases[26] = {2,  3,  5,  7,  11, 13, 17, 19, 23, 29, 31, 37, 41,
+                                     43, 47, 53, 59, 61, 67, 71, 73, 79, 83, 89, 97, 101};
+typedef struct {
+  double base;
+  unsigned int idx;
+} ham_t;
+
+static double ham_next(ham_t *h) {
+  double xs = 0, xsi = 1.0;
+  unsigned int i1, i2 = ++h->idx;
+  do {
+    xsi = xsi / h->base;
+    i1 = i2 / (unsigned int)h->base;
+    xs += (i2 - h->base * i1) * xsi;
+    i2 = i1;
+  } while (i2 > 0);
+  return xs;
+}
+
+void orc_hammersley(int base_index, int start, int n, double *out) {
+  ham_t h = {kHamBases[base_index], (unsigned int)start};
+  for (int i = 0; i < n; i++) out[i] = ham_next(&h);
+}
+
+/* inverse erfc after T. Ooura, Inverfc.cpp:16-65 */
+static double inverfc(double y) {
+  double z = y;
+  if (y > 1) z = 2 - y;
+  double w = 0.916461398268964 - log(z);
+  double u = sqrt(w);
+  double s = (log(u) + 0.488826640273108) / w;
+  double t = 1 / (u + 0.231729200323405);
+  double x = u * (1 - s * (s * 0.124610454613712 + 0.5)) -
+             ((((-0.0728846765585675 * t + 0.269999308670029) * t + 0.150689047360223) * t +
+               0.116065025341614) * t + 0.499999303439796) * t;
+  t = 3.97886080735226 / (x + 3.97886080735226);
+  u = t - 0.5;
+  s = (((((((((0.00112648096188977922 * u + 1.05739299623423047e-4) * u -
+              0.00351287146129100025) * u - 7.71708358954120939e-4) * u +
+            0.00685649426074558612) * u + 0.00339721910367775861) * u -
+          0.011274916933250487) * u - 0.0118598117047771104) * u +
+        0.0142961988697898018) * u + 0.0346494207789099922) * u + 0.00220995927012179067;
+  s = ((((((((((((s * u - 0.0743424357241784861) * u - 0.105872177941595488) * u +
+                0.0147297938331485121) * u + 0.316847638520135944) * u +
+              0.713657635868730364) * u + 1.05375024970847138) * u +
+            1.21448730779995237) * u + 1.16374581931560831) * u +
+          0.956464974744799006) * u + 0.686265948274097816) * u +
+        0.434397492331430115) * u + 0.244044510593190935) * t -
+      z * exp(x * x - 0.120782237635245222);
+  x = x + s * (x * s + 1);
+  if (y > 1) x = -x;
+  return x;
+}
+
+void orc_inverfc(int n, const double *in, double *out) {
+  for (int i = 0; i < n; i++) out[i] = inverfc(in[i]);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Bessel functions and coupling, BesselJ.cpp and Undulator.cpp:141-167      */
+/* ------------------------------------------------------------------------- */
+static double bessj0(double x) {
+  if (fabs(x) < 8) {
+    double y = x * x;
+    return (57568490574.e0 + y * (-13362590354.e0 + y * (651619640.7e0 + y * (-11214424.18e0 + y * (77392.33017e0 + y * -184.9052456e0))))) /
+           (57568490411.e0 + y * (1029532985.e0 + y * (9494680.718e0 + y * (59272.64853e0 + y * (267.8532712e0 + y * 1.e0)))));
+  }
+  double ax = fabs(x), z = 8 / ax, y = z * z, xx = ax - 0.785398164;
+  return sqrt(0.636619772 / ax) *
+         (cos(xx) * (1.e0 + y * (-.1098628627e-2 + y * (.2734510407e-4 + y * (-.2073370639e-5 + y * .2093887211e-6)))) -
+          z * sin(xx) * (-.1562499995e-1 + y * (.1430488765e-3 + y * (-.6911147651e-5 + y * (.7621095161e-6 + y * -.934945152e-7)))));
+}
+
+static double bessj1(double x) {
+  if (fabs(x) < 8) {
+    double y = x * x;
+    return x * (72362614232.e0 + y * (-7895059235.e0 + y * (242396853.1e0 + y * (-2972611.439e0 + y * (15704.48260e0 + y * -30.16036606e0))))) /
+           (144725228442.e0 + y * (2300535178.e0 + y * (18583304.74e0 + y * (99447.43394e0 + y * (376.9991397e0 + y * 1.e0)))));
+  }
+  double ax = fabs(x), z = 8 / ax, y = z * z, xx = ax - 2.356194491;
+  return sqrt(0.636619772 / ax) *
+         (cos(xx) * (1.e0 + y * (.183105e-2 + y * (-.3516396496e-4 + y * (.2457520174e-5 + y * -.240337019e-6)))) -
+          z * sin(xx) * (.04687499995e0 + y * (-.2002690873e-3 + y * (.8449199096e-5 + y * (-.88228987e-6 + y * .105787412e-6)))));
+}
+
+double orc_besselj(int n, double x) {
+  if (n == 0) return bessj0(x);
+  if (n == 1) return bessj1(x);
+  if (x == 0) return 0;
+  double bessj = 0, ax = fabs(x);
+  if (ax > (double)n) {
+    /* upward recurrence */
+    double tox = 2 / ax, bjm = bessj0(ax), bj = bessj1(ax);
+    for (int j = 1; j < n; j++) {
+      double bjp = j * tox * bj - bjm;
+      bjm = bj;
+      bj = bjp;
+    }
+    bessj = bj;
+  } else {
+    /* Miller's downward recurrence */
+    double tox = 2. / ax;
+    int m = (int)(2 * (n + floor(sqrt((double)(40 * n))) / 2));
+    int jsum = 0;
+    double sum = 0, bjp = 0, bj = 1;
+    for (int j = m; j > 0; j--) {
+      double bjm = j * tox * bj - bjp;
+      bjp = bj;
+      bj = bjm;
+      if (fabs(bj) > 1e10) {
+        bj *= 1e-10;
+        bjp *= 1e-10;
+        bessj *= 1e-10;
+        sum *= 1e-10;
+      }
+      if (jsum != 0) sum += bj;
+      jsum = 1 - jsum;
+      if (j == n) bessj = bjp;
+    }
+    sum = 2 * sum - bj;
+    bessj = bessj / sum;
+  }
+  if ((x < 0) && ((n % 2) == 1)) bessj = -bessj;
+  return bessj;
+}
+
+double orc_fc(double aw, int helical, int h) {
+  double coup = aw;
+  if (helical) return (h == 1) ? coup : 0;
+  double xi = aw * aw;
+  xi = 0.5 * xi / (1 + xi) * (double)h;
+  if ((h % 2) == 1) {
+    int h0 = (h - 1) / 2, h1 = h0 + 1;
+    return coup * (orc_besselj(h0, xi) - orc_besselj(h1, xi)) * pow(-1., h0);
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* beam loading, QuietLoading.cpp:50-260 and ShotNoise.cpp:16-68             */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  double gamma, theta, x, y, px, py;
+} part_t;
+
+static void load_quiet(part_t *b, const double *sp, int npart, int nbins, double theta0,
+                       int islice) {
+  const double gamma0 = sp[0], delgam = sp[1], ex = sp[2], ey = sp[3], betax = sp[4],
+               betay = sp[5], alphax = sp[6], alphay = sp[7], xcen = sp[8], ycen = sp[9],
+               pxcen = sp[10], pycen = sp[11], bunch = sp[12], bunchphase = sp[13],
+               emod = sp[14], emodphase = sp[15];
+  ran2_t rs;
+  ran2_init(&rs, (unsigned int)islice);
+  int iseed = (int)round(ran2_next(&rs) * 1e9);
+  ham_t st = {kHamBases[0], (unsigned)iseed}, sg = {kHamBases[1], (unsigned)iseed},
+        sx = {kHamBases[2], (unsigned)iseed}, sy = {kHamBases[3], (unsigned)iseed},
+        spx = {kHamBases[4], (unsigned)iseed}, spy = {kHamBases[5], (unsigned)iseed};
+  int mpart = npart / nbins;
+  double dtheta = 1. / (double)nbins;
+  for (int i = 0; i < mpart; i++) {
+    b[i].theta = ham_next(&st) * dtheta;
+    b[i].gamma = inverfc(2 * ham_next(&sg));
+    b[i].x = inverfc(2 * ham_next(&sx));
+    b[i].y = inverfc(2 * ham_next(&sy));
+    b[i].px = inverfc(2 * ham_next(&spx));
+    b[i].py = inverfc(2 * ham_next(&spy));
+  }
+  double z = 0, zz = 0, norm = 0;
+  if (mpart > 0) norm = 1. / (double)mpart;
+  for (int i = 0; i < mpart; i++) {
+    z += b[i].gamma;
+    zz += b[i].gamma * b[i].gamma;
+  }
+  z *= norm;
+  zz = sqrt(fabs(zz * norm - z * z));
+  if (zz > 0) zz = 1 / zz;
+  zz *= delgam;
+  for (int i = 0; i < mpart; i++) b[i].gamma = (b[i].gamma - z) * zz + gamma0;
+
+  /* x-px and y-py decorrelation, QuietLoading.cpp:110-156 */
+  for (int plane = 0; plane < 2; plane++) {
+    double p = 0, zp = 0;
+    z = 0;
+    zz = 0;
+    for (int i = 0; i < mpart; i++) {
+      double q = plane ? b[i].y : b[i].x, pq = plane ? b[i].py : b[i].px;
+      z += q;
+      zz += q * q;
+      p += pq;
+      zp += q * pq;
+    }
+    z *= norm;
+    p *= norm;
+    zz = sqrt(fabs(zz * norm - z * z));
+    if (zz > 0) zz = 1. / zz;
+    zp = (zp * norm - z * p) * zz * zz;
+    for (int i = 0; i < mpart; i++) {
+      double *q = plane ? &b[i].y : &b[i].x, *pq = plane ? &b[i].py : &b[i].px;
+      *pq = *pq - p;
+      *pq -= zp * *q;
+      *q = (*q - z) * zz;
+    }
+  }
+  double p = 0, pp = 0;
+  z = 0;
+  zz = 0;
+  for (int i = 0; i < mpart; i++) {
+    z += b[i].px;
+    zz += b[i].px * b[i].px;
+    p += b[i].py;
+    pp += b[i].py * b[i].py;
+  }
+  z *= norm;
+  p *= norm;
+  zz = sqrt(fabs(zz * norm - z * z));
+  if (zz > 0) zz = 1. / zz;
+  pp = sqrt(fabs(pp * norm - p * p));
+  if (pp > 0) pp = 1. / pp;
+  for (int i = 0; i < mpart; i++) {
+    b[i].px = (b[i].px - z) * zz;
+    b[i].py = (b[i].py - p) * pp;
+  }
+
+  /* Twiss scaling, QuietLoading.cpp:185-203 */
+  double sigx = sqrt(ex * betax / gamma0), sigy = sqrt(ey * betay / gamma0);
+  double sigpx = sqrt(ex / betax / gamma0), sigpy = sqrt(ey / betay / gamma0);
+  double corx = -alphax / betax, cory = -alphay / betay;
+  for (int i = 0; i < mpart; i++) {
+    b[i].x *= sigx;
+    b[i].y *= sigy;
+    b[i].px = sigpx * b[i].px + corx * b[i].x;
+    b[i].py = sigpy * b[i].py + cory * b[i].y;
+    b[i].px *= b[i].gamma;
+    b[i].py *= b[i].gamma;
+    b[i].x += xcen;
+    b[i].y += ycen;
+    b[i].px += pxcen;
+    b[i].py += pycen;
+  }
+  /* beamlet mirroring, QuietLoading.cpp:207-218 */
+  for (int i = mpart; i > 0; i--) {
+    int i1 = i - 1, i2 = nbins * i1;
+    for (int j = 0; j < nbins; j++) {
+      b[i2 + j].gamma = b[i1].gamma;
+      b[i2 + j].x = b[i1].x;
+      b[i2 + j].y = b[i1].y;
+      b[i2 + j].px = b[i1].px;
+      b[i2 + j].py = b[i1].py;
+      b[i2 + j].theta = b[i1].theta + j * dtheta;
+    }
+  }
+  for (int i = 0; i < npart; i++) b[i].theta *= theta0;
+
+  /* optional bunching / energy modulation, QuietLoading.cpp:227-259 */
+  double pi = 2 * asin(1.);
+  double blocal = bunch;
+  if (blocal != 0) {
+    double btar = blocal, blow = 0, bupp = 0.9999, bmid = 0;
+    while ((bupp - blow) > 1e-6) {
+      bmid = 0.5 * (blow + bupp);
+      double bprobe = sin((1 - bmid) * pi) / ((1 - bmid) * pi);
+      if (btar < bprobe)
+        bupp = bmid;
+      else
+        blow = bmid;
+    }
+    blocal = bmid;
+  }
+  if ((blocal != 0) || (emod != 0)) {
+    if (bunch > 0.1) {
+      for (int i = 0; i < npart; i++) {
+        b[i].gamma -= emod * sin(b[i].theta - emodphase);
+        b[i].theta += -blocal * b[i].theta + blocal * pi + bunchphase + pi;
+      }
+    } else {
+      for (int i = 0; i < npart; i++) {
+        b[i].gamma -= emod * sin(b[i].theta - emodphase);
+        b[i].theta -= 2 * bunch * sin(b[i].theta - bunchphase);
+      }
+    }
+  }
+}
+
+static void shot_noise(part_t *b, int npart, int nbins, double ne, ran2_t *sran, double *work) {
+  if (ne <= 0) return;
+  int mpart = npart / nbins;
+  double nbl = ne / (double)mpart;
+  if (nbl < 1) nbl = 1;
+  for (int i = 0; i < npart; i++) work[i] = 0;
+  double twopi = 4 * asin(1.);
+  for (int ih = 0; ih < (nbins - 1) / 2; ih++) {
+    for (int i1 = 0; i1 < mpart; i1++) {
+      double phi = 4 * asin(1) * ran2_next(sran);
+      double an = sqrt(-log(ran2_next(sran)) / nbl) * 2 / (double)(ih + 1);
+      if (an > twopi) an = fmod(an, twopi);
+      for (int i2 = 0; i2 < nbins; i2++) {
+        int idx = i1 * nbins + i2;
+        work[idx] -= an * sin(b[idx].theta * (ih + 1) + phi);
+      }
+    }
+  }
+  for (int i = 0; i < npart; i++) b[i].theta += work[i];
+}
+
+void orc_load_beam(int nslice, int islice0, int npart, int nbins, int seed, int shotnoise,
+                   double lambda, double sample, const double *slicepar, double *out) {
+  /* ShotNoise::init for rank 0: one draw from ran2(seed), ShotNoise.cpp:16-27 */
+  ran2_t rseed, sran;
+  ran2_init(&rseed, (unsigned int)seed);
+  double val = ran2_next(&rseed) * 1e9;
+  ran2_init(&sran, (unsigned int)(int)round(val));
+  part_t *b = (part_t *)malloc(sizeof(part_t) * (size_t)npart);
+  double *work = (double *)malloc(sizeof(double) * (size_t)npart);
+  for (int j = 0; j < nslice; j++) {
+    const double *sp = slicepar + (size_t)j * 17;
+    double ne = sp[16] * lambda * sample / kCe;
+    load_quiet(b, sp, npart, nbins, 4. * asin(1.), islice0 + j);
+    if (shotnoise) shot_noise(b, npart, nbins, ne, &sran, work);
+    memcpy(out + (size_t)j * npart * 6, b, sizeof(part_t) * (size_t)npart);
+  }
+  free(work);
+  free(b);
+}
+
+/* Gauss-Hermite mode, GaussHermite.cpp:20-85 */
+static double hn(double x, int n) {
+  if (n <= 0) return 1;
+  if (n == 1) return 2 * x;
+  return 2. * x * hn(x, n - 1) - 2 * (n - 1) * hn(x, n - 2);
+}
+static int fac(int n) { return n <= 1 ? 1 : n * fac(n - 1); }
+
+void orc_gauss_hermite(const double *par, double gridmax, int ngrid, double *out) {
+  double lambda = par[0], power = par[1], phase = par[2], z0in = par[3], w0 = par[4];
+  double xcen = par[5], ycen = par[6], xangle = par[7], yangle = par[8];
+  int nx = (int)par[9], ny = (int)par[10], harm = (int)par[11];
+  double k = 4. * asin(1) / lambda * (double)harm;
+  double z0 = -z0in;
+  double zr = w0 * w0 * k * 0.5;
+  double f0 = sqrt(k * zr / (zr * zr + z0 * z0));
+  cplx qz = CMPLX(-z0, zr);
+  cplx coef = CMPLX(0, 1) * 0.5 * k / qz;
+  double unit = sqrt(power * kVacimp) * k / kEev;
+  double norm = f0 / sqrt(2. * asin(1.) * fac(nx) * fac(ny) * (1 << (nx + ny)));
+  cplx zscale = unit * norm * CMPLX(cos(phase), sin(phase));
+  double xmid = gridmax + xcen, ymid = gridmax + ycen;
+  double dxy = 2. * gridmax / (ngrid - 1.);
+  double kx = k * xangle, ky = k * yangle;
+  cplx *f = (cplx *)out;
+  for (int iy = 0; iy < ngrid; iy++) {
+    double y = iy * dxy - ymid;
+    double hy = hn(f0 * y, ny);
+    double y2 = y * y;
+    double phiy = ky * y;
+    for (int ix = 0; ix < ngrid; ix++) {
+      double x = ix * dxy - xmid;
+      double hx = hn(f0 * x, nx);
+      double r2 = y2 + x * x;
+      cplx phi = CMPLX(0, phiy + kx * x);
+      f[iy * ngrid + ix] = zscale * cexp(-coef * r2 + phi) * hx * hy;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------- */
+/* the integration step                                                      */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  double aw, ax, ay, ku, kx, ky, gradx, grady, qf, qx, qy, cx, cy, dz, slip, phase, z;
+  int helical;
+} step_t;
+
+static step_t get_step(const double *lat, int i) {
+  const double *r = lat + (size_t)i * G4_LAT_NCOL;
+  step_t s;
+  s.aw = r[G4_LAT_AW]; s.ax = r[G4_LAT_AX]; s.ay = r[G4_LAT_AY]; s.ku = r[G4_LAT_KU];
+  s.kx = r[G4_LAT_KX]; s.ky = r[G4_LAT_KY]; s.gradx = r[G4_LAT_GRADX];
+  s.grady = r[G4_LAT_GRADY]; s.qf = r[G4_LAT_QF]; s.qx = r[G4_LAT_QX]; s.qy = r[G4_LAT_QY];
+  s.cx = r[G4_LAT_CX]; s.cy = r[G4_LAT_CY]; s.dz = r[G4_LAT_DZ]; s.slip = r[G4_LAT_SLIP];
+  s.phase = r[G4_LAT_PHASE]; s.z = r[G4_LAT_Z];
+  s.helical = r[G4_LAT_HELICAL] != 0;
+  return s;
+}
+
+/* Undulator::faw / faw2, Undulator.cpp:170-182 */
+static double faw(const step_t *u, double x, double y) {
+  double dx = x - u->ax, dy = y - u->ay;
+  return (1 + 0.5 * (u->kx * dx * dx + u->ky * dy * dy) + u->gradx * dx + u->grady * dy);
+}
+static double faw2(const step_t *u, double x, double y) {
+  double dx = x - u->ax, dy = y - u->ay;
+  return (1 + u->kx * dx * dx + u->ky * dy * dy + 2 * (u->gradx * dx + u->grady * dy));
+}
+
+/* Field::getLLGridpoint, Field.cpp:160-174 */
+static int ll_gridpoint(double gridmax, double dgrid, int ngrid, double x, double y,
+                        double *wx, double *wy, int *idx) {
+  if ((x > -gridmax) && (x < gridmax) && (y > -gridmax) && (y < gridmax)) {
+    *wx = (x + gridmax) / dgrid;
+    *wy = (y + gridmax) / dgrid;
+    int ix = (int)floor(*wx), iy = (int)floor(*wy);
+    *wx = 1 + floor(*wx) - *wx;
+    *wy = 1 + floor(*wy) - *wy;
+    *idx = ix + iy * ngrid;
+    return 1;
+  }
+  return 0;
+}
+
+typedef struct {
+  int ns, npart, nfld, ngrid;
+  part_t *beam;
+  const double *current;
+  cplx *fields;
+  const int *harm;
+  const int *first;
+  const double *gridmax;
+  double reflength;
+  double gammaref;
+  step_t st;
+  double delz;
+  /* push */
+  double xks_fund, xku, rtmp[8], rharm[8];
+  /* field solve */
+  int ifld;
+  int solver;
+  double filt[3];
+  cplx *cbet, *cwet, *cc, cstep;
+  cplx *k2, *sigm;
+} step_ctx;
+
+/* TrackBeam::track, TrackBeam.cpp:8-116 (no chicane: the lattice has none) */
+typedef struct {
+  double q, off;
+  int kind; /* 0 drift, 1 focusing, 2 defocusing */
+} plane_t;
+
+static void transverse_setup(const step_t *u, double gamma0, plane_t *px, plane_t *py,
+                             double *aw_out) {
+  int inund = u->aw > 0;
+  double aw = inund ? u->aw : 0, dax = inund ? u->ax : 0, day = inund ? u->ay : 0;
+  double kx = inund ? u->kx : 0, ky = inund ? u->ky : 0;
+  double qf = u->qf, dqx = qf == 0 ? 0 : u->qx, dqy = qf == 0 ? 0 : u->qy;
+  double betpar0 = sqrt(1 - (1 + aw * aw) / gamma0 / gamma0);
+  double qquad = qf * gamma0;
+  double qnatx = kx * aw * aw / gamma0 / betpar0;
+  double qnaty = ky * aw * aw / gamma0 / betpar0;
+  double qx = qquad + qnatx, qy = -qquad + qnaty;
+  double xoff = qquad * dqx + qnatx * dax;
+  double yoff = -qquad * dqy + qnaty * day;
+  px->q = qx;
+  py->q = qy;
+  if (qx == 0) {
+    px->kind = 0;
+    px->off = xoff;
+  } else {
+    px->off = xoff / qx;
+    px->kind = qx > 0 ? 1 : 2;
+  }
+  if (qy == 0) {
+    py->kind = 0;
+    py->off = yoff;
+  } else {
+    py->off = yoff / qy;
+    py->kind = qy > 0 ? 1 : 2;
+  }
+  *aw_out = aw;
+}
+
+static void apply_plane(const plane_t *pl, double delz, double *x, double *p, double gammaz) {
+  if (pl->kind == 0) {
+    *x += (*p) * delz / gammaz;
+  } else if (pl->kind == 1) {
+    double foc = sqrt(pl->q / gammaz), omg = foc * delz;
+    double a1 = cos(omg), a2 = sin(omg) / foc, a3 = -a2 * foc * foc;
+    double xtmp = *x - pl->off;
+    *x = a1 * xtmp + a2 * (*p) / gammaz + pl->off;
+    *p = a3 * xtmp * gammaz + a1 * (*p);
+  } else {
+    double foc = sqrt(-pl->q / gammaz), omg = foc * delz;
+    double a1 = cosh(omg), a2 = sinh(omg) / foc, a3 = a2 * foc * foc;
+    double xtmp = *x - pl->off;
+    *x = a1 * xtmp + a2 * (*p) / gammaz + pl->off;
+    *p = a3 * xtmp * gammaz + a1 * (*p);
+  }
+}
+
+static void transverse_slices(step_ctx *c, int is0, int is1, int last) {
+  plane_t pxp, pyp;
+  double aw;
+  transverse_setup(&c->st, c->gammaref, &pxp, &pyp, &aw);
+  double delz = c->delz * 0.5;
+  double cxk = c->st.cx * c->gammaref, cyk = c->st.cy * c->gammaref;
+  int corr = last && ((c->st.cx != 0) || (c->st.cy != 0));
+  for (int is = is0; is < is1; is++) {
+    part_t *b = c->beam + (size_t)is * c->npart;
+    for (int j = 0; j < c->npart; j++) {
+      part_t *p = b + j;
+      if (corr) {
+        p->px += cxk;
+        p->py += cyk;
+      }
+      double gammaz = sqrt(p->gamma * p->gamma - 1 - aw * aw - p->px * p->px - p->py * p->py);
+      apply_plane(&pxp, delz, &p->x, &p->px, gammaz);
+      apply_plane(&pyp, delz, &p->y, &p->py, gammaz);
+    }
+  }
+}
+
+/* BeamSolver::ODE, BeamSolver.cpp:144-163 */
+static void ode(const step_ctx *c, int nf, const cplx *rpart, double btpar, double ez,
+                double tgam, double tthet, double *k2gg, double *k2pp) {
+  double ztemp1 = -2. / c->xks_fund;
+  cplx ctmp = 0;
+  for (int i = 0; i < nf; i++)
+    ctmp += rpart[i] * CMPLX(cos(c->rharm[i] * tthet), -sin(c->rharm[i] * tthet));
+  double btper0 = btpar + ztemp1 * creal(ctmp);
+  double btpar0 = sqrt(1. - btper0 / (tgam * tgam));
+  *k2pp += c->xks_fund * (1. - 1. / btpar0) + c->xku;
+  *k2gg += cimag(ctmp) / btpar0 / tgam - ez;
+}
+
+/* BeamSolver::advance + RungeKutta, BeamSolver.cpp:13-141 */
+static void push_slices(step_ctx *c, int is0, int is1) {
+  const step_t *u = &c->st;
+  double aw = u->aw, autophase = u->phase, delz = c->delz;
+  size_t ncell = (size_t)c->ngrid * c->ngrid;
+  for (int is = is0; is < is1; is++) {
+    part_t *b = c->beam + (size_t)is * c->npart;
+    for (int ip = 0; ip < c->npart; ip++) {
+      part_t *p = b + ip;
+      double gamma = p->gamma, theta = p->theta + autophase;
+      double x = p->x, y = p->y, px = p->px, py = p->py;
+      double awloc = faw(u, x, y);
+      double btpar = 1 + px * px + py * py + aw * aw * awloc * awloc;
+      double ez = 0;
+      cplx rpart[8];
+      for (int k = 0; k < c->nfld; k++) {
+        int ns = c->ns;
+        size_t islice = (size_t)((is + c->first[k]) % ns);
+        const cplx *f = c->fields + ((size_t)k * ns + islice) * ncell;
+        double gm = c->gridmax[k], dg = 2 * gm / (double)(c->ngrid - 1);
+        double wx, wy;
+        int idx;
+        if (ll_gridpoint(gm, dg, c->ngrid, x, y, &wx, &wy, &idx)) {
+          cplx cpart = f[idx] * wx * wy;
+          idx++;
+          cpart += f[idx] * (1 - wx) * wy;
+          idx += c->ngrid - 1;
+          cpart += f[idx] * wx * (1 - wy);
+          idx++;
+          cpart += f[idx] * (1 - wx) * (1 - wy);
+          rpart[k] = c->rtmp[k] * awloc * conj(cpart);
+        } else {
+          rpart[k] = 0;
+        }
+      }
+      /* RungeKutta, BeamSolver.cpp:89-141 */
+      double k2gg = 0, k2pp = 0, k3gg, k3pp;
+      ode(c, c->nfld, rpart, btpar, ez, gamma, theta, &k2gg, &k2pp);
+      double stpz = 0.5 * delz;
+      gamma += stpz * k2gg;
+      theta += stpz * k2pp;
+      k3gg = k2gg;
+      k3pp = k2pp;
+      k2gg = 0;
+      k2pp = 0;
+      ode(c, c->nfld, rpart, btpar, ez, gamma, theta, &k2gg, &k2pp);
+      gamma += stpz * (k2gg - k3gg);
+      theta += stpz * (k2pp - k3pp);
+      k3gg /= 6;
+      k3pp /= 6;
+      k2gg *= -0.5;
+      k2pp *= -0.5;
+      ode(c, c->nfld, rpart, btpar, ez, gamma, theta, &k2gg, &k2pp);
+      stpz = delz;
+      gamma += stpz * k2gg;
+      theta += stpz * k2pp;
+      k3gg -= k2gg;
+      k3pp -= k2pp;
+      k2gg *= 2;
+      k2pp *= 2;
+      ode(c, c->nfld, rpart, btpar, ez, gamma, theta, &k2gg, &k2pp);
+      gamma += stpz * (k3gg + k2gg / 6.0);
+      theta += stpz * (k3pp + k2pp / 6.0);
+      p->gamma = gamma;
+      p->theta = theta;
+    }
+  }
+}
+
+/* source deposition, FieldSolverADI.cpp:13-52 (identical in FieldSolverFFT.cpp:13-52) */
+static void deposit(const step_ctx *c, int ii, cplx *src) {
+  int ng = c->ngrid;
+  size_t ncell = (size_t)ng * ng;
+  for (size_t i = 0; i < ncell; i++) src[i] = 0;
+  int harm = c->harm[c->ifld];
+  if (!(c->st.aw > 0) || (harm % 2 != 1)) return;
+  double gm = c->gridmax[c->ifld], dgrid = 2 * gm / (double)(ng - 1);
+  double xks = 4. * asin(1) / (c->reflength / (double)harm);
+  double scl = orc_fc(c->st.aw, c->st.helical, harm) * kVacimp * c->current[ii] * xks * c->delz;
+  scl /= 4 * kEev * (double)c->npart * dgrid * dgrid;
+  const part_t *b = c->beam + (size_t)ii * c->npart;
+  for (int ip = 0; ip < c->npart; ip++) {
+    double x = b[ip].x, y = b[ip].y, theta = (double)harm * b[ip].theta, gamma = b[ip].gamma;
+    double wx, wy;
+    int idx;
+    if (ll_gridpoint(gm, dgrid, ng, x, y, &wx, &wy, &idx)) {
+      double part = sqrt(faw2(&c->st, x, y)) * scl / gamma;
+      cplx cpart = CMPLX(sin(theta), cos(theta)) * part;
+      double weight = wx * wy;
+      src[idx] += weight * cpart;
+      weight = (1 - wx) * wy;
+      idx++;
+      src[idx] += weight * cpart;
+      weight = wx * (1 - wy);
+      idx += ng - 1;
+      src[idx] += weight * cpart;
+      weight = (1 - wx) * (1 - wy);
+      idx++;
+      src[idx] += weight * cpart;
+    }
+  }
+}
+
+/* Crank-Nicolson ADI, FieldSolverADI.cpp:60-122 */
+static void adi(const step_ctx *c, cplx *u, const cplx *src, cplx *r) {
+  int ng = c->ngrid;
+  cplx cstep = c->cstep;
+  const cplx *cc = c->cc, *cbet = c->cbet, *cwet = c->cwet;
+  int idx;
+  for (idx = 0; idx < ng; idx++)
+    r[idx] = src[idx] + u[idx] + cstep * (u[idx + ng] - 2.0 * u[idx]);
+  for (idx = ng; idx < ng * (ng - 1); idx++)
+    r[idx] = src[idx] + u[idx] + cstep * (u[idx + ng] - 2.0 * u[idx] + u[idx - ng]);
+  for (idx = ng * (ng - 1); idx < ng * ng; idx++)
+    r[idx] = src[idx] + u[idx] + cstep * (u[idx - ng] - 2.0 * u[idx]);
+  /* tridagx */
+  for (int i = 0; i < ng * ng; i += ng) {
+    u[i] = r[i] * cbet[0];
+    for (int k = 1; k < ng; k++) u[k + i] = (r[k + i] - cc[k] * u[k + i - 1]) * cbet[k];
+    for (int k = ng - 2; k >= 0; k--) u[k + i] -= cwet[k + 1] * u[k + i + 1];
+  }
+  for (int ix = 0; ix < ng * ng; ix += ng) {
+    idx = ix;
+    r[idx] = src[idx] + u[idx] + cstep * (u[idx + 1] - 2.0 * u[idx]);
+    for (idx = ix + 1; idx < ix + ng - 1; idx++)
+      r[idx] = src[idx] + u[idx] + cstep * (u[idx + 1] - 2.0 * u[idx] + u[idx - 1]);
+    idx = ix + ng - 1;
+    r[idx] = src[idx] + u[idx] + cstep * (u[idx - 1] - 2.0 * u[idx]);
+  }
+  /* tridagy */
+  for (int i = 0; i < ng; i++) u[i] = r[i] * cbet[0];
+  for (int k = 1; k < ng; k++) {
+    int n = k * ng;
+    for (int i = 0; i < ng; i++) u[n + i] = (r[n + i] - cc[k] * u[n + i - ng]) * cbet[k];
+  }
+  for (int k = ng - 2; k >= 0; k--) {
+    int n = k * ng;
+    for (int i = 0; i < ng; i++) u[n + i] -= cwet[k + 1] * u[n + i + ng];
+  }
+}
+
+/* FieldSolverADI::init coefficients, FieldSolverADI.cpp:125-182 */
+static void adi_init(step_ctx *c, double delz, double dgrid, double xks) {
+  int ng = c->ngrid;
+  double rtmp = 0.25 * delz / (xks * dgrid * dgrid);
+  c->cstep = CMPLX(0, rtmp);
+  double *mupp = malloc(sizeof(double) * ng), *mmid = malloc(sizeof(double) * ng),
+         *mlow = malloc(sizeof(double) * ng);
+  cplx *w1 = malloc(sizeof(cplx) * ng), *w2 = malloc(sizeof(cplx) * ng);
+  mupp[0] = rtmp;
+  mmid[0] = -2 * rtmp;
+  mlow[0] = 0;
+  for (int i = 1; i < ng - 1; i++) {
+    mupp[i] = rtmp;
+    mmid[i] = -2 * rtmp;
+    mlow[i] = rtmp;
+  }
+  mupp[ng - 1] = 0;
+  mmid[ng - 1] = -2 * rtmp;
+  mlow[ng - 1] = rtmp;
+  for (int i = 0; i < ng; i++) {
+    w1[i] = CMPLX(0, -mupp[i]);
+    w2[i] = CMPLX(1, -mmid[i]);
+    c->cc[i] = CMPLX(0, -mlow[i]);
+  }
+  c->cbet[0] = 1. / w2[0];
+  c->cwet[0] = 0.;
+  for (int i = 1; i < ng; i++) {
+    c->cwet[i] = w1[i - 1] * c->cbet[i - 1];
+    c->cbet[i] = 1. / (w2[i] - c->cc[i] * c->cwet[i]);
+  }
+  free(mupp);
+  free(mmid);
+  free(mlow);
+  free(w1);
+  free(w2);
+}
+
+/* ---- FFT (mixed radix, any length) used by the FFT field solver -------- */
+/* out[k] = sum_j in[j*stride] exp(sign*2*pi*i*j*k/n); recursive decimation in time */
+static void fft_rec(const cplx *in, cplx *out, int n, int stride, int sign, cplx *scratch) {
+  if (n == 1) {
+    out[0] = in[0];
+    return;
+  }
+  int p = 2;
+  while (p * p <= n && n % p) p++;
+  if (n % p) p = n; /* prime length: direct DFT */
+  int m = n / p;
+  if (p == n) {
+    for (int k = 0; k < n; k++) {
+      cplx s = 0;
+      for (int j = 0; j < n; j++) {
+        double ang = sign * 2.0 * kPi * (double)(((long long)j * k) % n) / (double)n;
+        s += in[(size_t)j * stride] * CMPLX(cos(ang), sin(ang));
+      }
+      out[k] = s;
+    }
+    return;
+  }
+  /* p sub-transforms of length m on decimated inputs, stored contiguously in scratch */
+  for (int r = 0; r < p; r++) fft_rec(in + (size_t)r * stride, scratch + (size_t)r * m, m, stride * p, sign, out);
+  for (int k = 0; k < m; k++) {
+    for (int q = 0; q < p; q++) {
+      cplx s = 0;
+      int kk = k + q * m;
+      for (int r = 0; r < p; r++) {
+        double ang = sign * 2.0 * kPi * (double)(((long long)r * kk) % n) / (double)n;
+        s += scratch[(size_t)r * m + k] * CMPLX(cos(ang), sin(ang));
+      }
+      out[kk] = s;
+    }
+  }
+}
+
+/* 2-D transform of an ngrid x ngrid row-major array (FFTW sign convention) */
+static void fft2(cplx *a, int ng, int sign, cplx *tmp, cplx *tmp2) {
+  cplx *line = tmp, *res = tmp + ng;
+  for (int iy = 0; iy < ng; iy++) {
+    fft_rec(a + (size_t)iy * ng, res, ng, 1, sign, tmp2);
+    memcpy(a + (size_t)iy * ng, res, sizeof(cplx) * ng);
+  }
+  for (int ix = 0; ix < ng; ix++) {
+    for (int iy = 0; iy < ng; iy++) line[iy] = a[(size_t)iy * ng + ix];
+    fft_rec(line, res, ng, 1, sign, tmp2);
+    for (int iy = 0; iy < ng; iy++) a[(size_t)iy * ng + ix] = res[iy];
+  }
+}
+
+/* FieldSolverFFT::init tables, FieldSolverFFT.cpp:117-155 */
+static void fft_init(step_ctx *c, double dgrid, double xks) {
+  int ng = c->ngrid;
+  double dk = 4. * asin(1.) / ((double)ng * dgrid);
+  double xc = c->filt[0], yc = c->filt[1], sig = c->filt[2];
+  double shift = -0.5 * (double)(ng - 1);
+  for (int iy = 0; iy < ng; iy++) {
+    double dy = (double)iy + shift;
+    double y = dy / (double)ng / yc;
+    for (int ix = 0; ix < ng; ix++) {
+      double dx = (double)ix + shift;
+      double x = dx / (double)ng / xc;
+      int iiy = (iy + (ng + 1) / 2) % ng, iix = (ix + (ng + 1) / 2) % ng;
+      int ii = iiy * ng + iix;
+      c->k2[ii] = CMPLX(0, -(dx * dx + dy * dy) * dk * dk / 2. / xks);
+      double r = (sqrt(x * x + y * y) - 1) / sig;
+      c->sigm[ii] = 1. / (1 + exp(r));
+    }
+  }
+}
+
+/* FieldSolverFFT::FFT, FieldSolverFFT.cpp:64-114 */
+static void fft_solve(const step_ctx *c, cplx *u, const cplx *src, cplx *work) {
+  int ng = c->ngrid;
+  size_t n2 = (size_t)ng * ng;
+  cplx *uf = work, *sf = work + n2, *t1 = work + 2 * n2, *t2 = t1 + 2 * (size_t)ng;
+  memcpy(uf, u, sizeof(cplx) * n2);
+  fft2(uf, ng, -1, t1, t2);
+  if (c->solver == 2) {
+    memcpy(sf, src, sizeof(cplx) * n2);
+    fft2(sf, ng, -1, t1, t2);
+    for (size_t i = 0; i < n2; i++) sf[i] = sf[i] * c->sigm[i];
+    for (size_t i = 0; i < n2; i++) uf[i] = uf[i] * cexp(c->k2[i] * c->delz) + 2. * sf[i];
+  } else {
+    for (size_t i = 0; i < n2; i++) uf[i] = uf[i] * cexp(c->k2[i] * c->delz);
+  }
+  fft2(uf, ng, +1, t1, t2);
+  double norm = 1. / (double)(ng * ng);
+  if (c->solver == 2) {
+    for (size_t i = 0; i < n2; i++) u[i] = uf[i] * norm;
+  } else {
+    for (size_t i = 0; i < n2; i++) u[i] = uf[i] * norm + 2. * src[i];
+  }
+}
+
+static void field_slices(step_ctx *c, int ii0, int ii1) {
+  int ng = c->ngrid;
+  size_t n2 = (size_t)ng * ng;
+  cplx *src = malloc(sizeof(cplx) * n2);
+  cplx *work = malloc(sizeof(cplx) * (3 * n2 + 4 * (size_t)ng));
+  int k = c->ifld;
+  for (int ii = ii0; ii < ii1; ii++) {
+    deposit(c, ii, src);
+    size_t i = (size_t)((ii + c->first[k]) % c->ns);
+    cplx *u = c->fields + ((size_t)k * c->ns + i) * n2;
+    if (c->solver == 0)
+      adi(c, u, src, work);
+    else
+      fft_solve(c, u, src, work);
+  }
+  free(work);
+  free(src);
+}
+
+static void run_push(void *ctx, int i0, int i1) {
+  step_ctx *c = (step_ctx *)ctx;
+  transverse_slices(c, i0, i1, 0);
+  push_slices(c, i0, i1);
+  transverse_slices(c, i0, i1, 1);
+}
+static void run_field(void *ctx, int i0, int i1) { field_slices((step_ctx *)ctx, i0, i1); }
+
+/* Control::applySlippage for one rank, Control.cpp:158-276 */
+static void apply_slippage(double slippage, double sample, int periodic, int ns, size_t n2,
+                           cplx *field, int *first, double *accuslip) {
+  *accuslip += slippage;
+  int direction = 1;
+  while (fabs(*accuslip) > (sample * 0.8)) {
+    if (*accuslip < 0) direction = -1;
+    *accuslip -= sample * direction;
+    int last = (*first + ns - 1) % ns;
+    if (direction < 0) last = (last + 1) % ns;
+    if (!periodic) {
+      /* rank 0 zero-fills for forward slippage, the last rank for backward */
+      cplx *f = field + (size_t)last * n2;
+      for (size_t i = 0; i < n2; i++) f[i] = 0;
+    }
+    *first = last;
+    if (direction < 0) *first = (last + 1) % ns;
+  }
+}
+
+int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int npart,
+                  double *particles, const double *current, double reflength,
+                  double sample, int nfld, const int *harm, int ngrid,
+                  const double *gridmax, double *fields, int *first, double *accuslip,
+                  int time_run, int periodic, int stages, int solver, const double *filt,
+                  int nthreads) {
+  if (nfld > 8 || ngrid < 3) return 1;
+  step_ctx c;
+  memset(&c, 0, sizeof(c));
+  c.ns = ns;
+  c.npart = npart;
+  c.nfld = nfld;
+  c.ngrid = ngrid;
+  c.beam = (part_t *)particles;
+  c.current = current;
+  c.fields = (cplx *)fields;
+  c.harm = harm;
+  c.first = first;
+  c.gridmax = gridmax;
+  c.reflength = reflength;
+  c.gammaref = gammaref;
+  c.solver = solver;
+  if (filt) {
+    c.filt[0] = filt[0];
+    c.filt[1] = filt[1];
+    c.filt[2] = filt[2];
+  } else {
+    c.filt[0] = c.filt[1] = c.filt[2] = 1;
+  }
+  /* FieldSolverFFT::initSourceFilter disables the filter for bad input */
+  if (c.solver == 2 && (c.filt[2] <= 0 || c.filt[0] <= 0 || c.filt[1] <= 0)) c.solver = 1;
+  size_t n2 = (size_t)ngrid * ngrid;
+  cplx *coef = malloc(sizeof(cplx) * 3 * ngrid);
+  c.cc = coef;
+  c.cbet = coef + ngrid;
+  c.cwet = coef + 2 * ngrid;
+  int fft_ready[8] = {0};
+  cplx *fft_tabs = NULL;
+  if (solver) fft_tabs = malloc(sizeof(cplx) * 2 * n2 * nfld);
+
+  for (int istep = 0; istep < nsteps; istep++) {
+    c.st = get_step(lat, istep);
+    c.delz = c.st.dz;
+    if (stages & ORC_STAGE_PUSH) {
+      /* BeamSolver::advance field-dependent constants, BeamSolver.cpp:19-38 */
+      double xks = 1;
+      for (int k = 0; k < nfld; k++) {
+        double fxks = 4. * asin(1) / (reflength / (double)harm[k]);
+        xks = fxks / (double)harm[k];
+        c.rtmp[k] = orc_fc(c.st.aw, c.st.helical, harm[k]) / fxks;
+        c.rharm[k] = (double)harm[k];
+      }
+      c.xks_fund = xks;
+      c.xku = c.st.ku;
+      if (c.xku == 0) c.xku = xks * 0.5 / gammaref / gammaref;
+      parallel_for(ns, nthreads, run_push, &c);
+    }
+    if (stages & ORC_STAGE_FIELD) {
+      for (int k = 0; k < nfld; k++) {
+        c.ifld = k;
+        double gm = gridmax[k], dgrid = 2 * gm / (double)(ngrid - 1);
+        double fxks = 4. * asin(1) / (reflength / (double)harm[k]);
+        if (solver == 0) {
+          /* FieldSolverADI.cpp:127 caches these per field and delz; they are a
+           * pure function of (delz, dgrid, xks), so recomputing is identical */
+          adi_init(&c, c.delz, dgrid, fxks);
+        } else {
+          c.k2 = fft_tabs + 2 * n2 * k;
+          c.sigm = c.k2 + n2;
+          if (!fft_ready[k]) fft_init(&c, dgrid, fxks);
+          fft_ready[k] = 1;
+        }
+        parallel_for(ns, nthreads, run_field, &c);
+      }
+    }
+    if ((stages & ORC_STAGE_SLIP) && time_run) {
+      for (int k = 0; k < nfld; k++)
+        apply_slippage(c.st.slip, sample, periodic, ns, n2, c.fields + (size_t)k * ns * n2,
+                       &first[k], &accuslip[k]);
+    }
+  }
+  free(coef);
+  free(fft_tabs);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* diagnostics                                                               */
+/* ------------------------------------------------------------------------- */
+void orc_diag_beam(int ns, int npart, const double *particles, int nharm, double *out) {
+  int ncol = ORC_DB_NCOL + 2 * nharm;
+  cplx b[64];
+  for (int is = 0; is < ns; is++) {
+    const part_t *s = (const part_t *)particles + (size_t)is * npart;
+    double g1 = 0, g2 = 0, x1 = 0, x2 = 0, y1 = 0, y2 = 0, px1 = 0, py1 = 0, px2 = 0, py2 = 0;
+    double xpx = 0, ypy = 0, xmin = 1e5, xmax = -1e5, pxmin = 1e5, pxmax = -1e5, ymin = 1e5;
+    double ymax = -1e5, pymin = 1e5, pymax = -1e5, gmin = 1e7, gmax = 1;
+    for (int h = 0; h < nharm; h++) b[h] = 0;
+    for (int i = 0; i < npart; i++) {
+      const part_t *p = s + i;
+      x1 += p->x;
+      x2 += p->x * p->x;
+      y1 += p->y;
+      y2 += p->y * p->y;
+      g1 += p->gamma;
+      g2 += p->gamma * p->gamma;
+      px1 += p->px;
+      py1 += p->py;
+      px2 += p->px * p->px;
+      py2 += p->py * p->py;
+      xpx += p->x * p->px;
+      ypy += p->y * p->py;
+      for (int h = 0; h < nharm; h++) b[h] += CMPLX(cos((h + 1) * p->theta), sin((h + 1) * p->theta));
+    }
+    for (int i = 0; i < npart; i++) {
+      const part_t *p = s + i;
+      if (p->x < xmin) xmin = p->x;
+      if (p->x > xmax) xmax = p->x;
+      if (p->px < pxmin) pxmin = p->px;
+      if (p->px > pxmax) pxmax = p->px;
+      if (p->y < ymin) ymin = p->y;
+      if (p->y > ymax) ymax = p->y;
+      if (p->py < pymin) pymin = p->py;
+      if (p->py > pymax) pymax = p->py;
+      if (p->gamma < gmin) gmin = p->gamma;
+      if (p->gamma > gmax) gmax = p->gamma;
+    }
+    double norm = 1.;
+    if (npart > 0) norm = 1. / (double)npart;
+    x1 *= norm; x2 *= norm; y1 *= norm; y2 *= norm; px1 *= norm; px2 *= norm;
+    py1 *= norm; py2 *= norm; g1 *= norm; g2 *= norm; xpx *= norm; ypy *= norm;
+    for (int h = 0; h < nharm; h++) b[h] *= norm;
+    double *o = out + (size_t)is * ncol;
+    o[ORC_DB_ENERGY] = g1;
+    o[ORC_DB_ENERGYSPREAD] = sqrt(fabs(g2 - g1 * g1));
+    o[ORC_DB_XPOS] = x1;
+    o[ORC_DB_XSIZE] = sqrt(fabs(x2 - x1 * x1));
+    o[ORC_DB_YPOS] = y1;
+    o[ORC_DB_YSIZE] = sqrt(fabs(y2 - y1 * y1));
+    o[ORC_DB_PXPOS] = px1;
+    o[ORC_DB_PYPOS] = py1;
+    double ex = sqrt(fabs((x2 - x1 * x1) * (px2 - px1 * px1) - (xpx - x1 * px1) * (xpx - x1 * px1)));
+    double ey = sqrt(fabs((y2 - y1 * y1) * (py2 - py1 * py1) - (ypy - y1 * py1) * (ypy - y1 * py1)));
+    o[ORC_DB_EMITX] = ex;
+    o[ORC_DB_EMITY] = ey;
+    o[ORC_DB_BETAX] = (x2 - x1 * x1) / ex * g1;
+    o[ORC_DB_BETAY] = (y2 - y1 * y1) / ey * g1;
+    o[ORC_DB_ALPHAX] = -(xpx - x1 * px1) / ex;
+    o[ORC_DB_ALPHAY] = -(ypy - y1 * py1) / ey;
+    o[ORC_DB_XMIN] = xmin; o[ORC_DB_XMAX] = xmax; o[ORC_DB_PXMIN] = pxmin; o[ORC_DB_PXMAX] = pxmax;
+    o[ORC_DB_YMIN] = ymin; o[ORC_DB_YMAX] = ymax; o[ORC_DB_PYMIN] = pymin; o[ORC_DB_PYMAX] = pymax;
+    o[ORC_DB_EMIN] = gmin; o[ORC_DB_EMAX] = gmax;
+    for (int h = 0; h < nharm; h++) {
+      o[ORC_DB_NCOL + 2 * h] = cabs(b[h]);
+      o[ORC_DB_NCOL + 2 * h + 1] = atan2(cimag(b[h]), creal(b[h]));
+    }
+  }
+}
+
+void orc_diag_field(int ns, int ngrid, double gridmax, double lambda0, int harm,
+                    const double *field, int first, double *out) {
+  const cplx *f = (const cplx *)field;
+  double xlambda = lambda0 / (double)harm;
+  double dgrid = 2 * gridmax / (double)(ngrid - 1);
+  double ks = 4. * asin(1) / xlambda;
+  double scl = dgrid * kEev / ks;
+  double shift = -0.5 * (double)(ngrid - 1);
+  for (int is0 = 0; is0 < ns; is0++) {
+    int is = (ns + is0 - first) % ns;
+    const cplx *sl = f + (size_t)is0 * ngrid * ngrid;
+    double power = 0, x1 = 0, x2 = 0, y1 = 0, y2 = 0;
+    cplx ff = 0;
+    for (int iy = 0; iy < ngrid; iy++) {
+      double dy = (double)iy + shift;
+      for (int ix = 0; ix < ngrid; ix++) {
+        double dx = (double)ix + shift;
+        cplx loc = sl[iy * ngrid + ix];
+        double wei = creal(loc) * creal(loc) + cimag(loc) * cimag(loc);
+        ff += loc;
+        power += wei;
+        x1 += dx * wei;
+        x2 += dx * dx * wei;
+        y1 += dy * wei;
+        y2 += dy * dy * wei;
+      }
+    }
+    if (power > 0) {
+      x1 /= power;
+      x2 /= power;
+      y1 /= power;
+      y2 /= power;
+    }
+    x2 = sqrt(fabs(x2 - x1 * x1));
+    y2 = sqrt(fabs(y2 - y1 * y1));
+    int i = (ngrid / 2) * ngrid + (ngrid / 2);
+    cplx loc = sl[i];
+    double inten = creal(loc) * creal(loc) + cimag(loc) * cimag(loc);
+    double intenphi = atan2(cimag(loc), creal(loc));
+    double farfield = creal(ff) * creal(ff) + cimag(ff) * cimag(ff);
+    double farfieldphi = atan2(cimag(ff), creal(ff));
+    farfield *= dgrid * dgrid;
+    power *= scl * scl / kVacimp;
+    x1 *= dgrid;
+    x2 *= dgrid;
+    y1 *= dgrid;
+    y2 *= dgrid;
+    inten *= kEev * kEev / ks / ks / kVacimp;
+    double *o = out + (size_t)is * ORC_DF_NCOL;
+    o[ORC_DF_POWER] = power;
+    o[ORC_DF_XPOS] = x1;
+    o[ORC_DF_XSIZE] = x2;
+    o[ORC_DF_YPOS] = y1;
+    o[ORC_DF_YSIZE] = y2;
+    o[ORC_DF_NF_INT] = inten;
+    o[ORC_DF_NF_PHI] = intenphi;
+    o[ORC_DF_FF_INT] = farfield;
+    o[ORC_DF_FF_PHI] = farfieldphi;
+  }
+}

@@ -1,0 +1,93 @@
+/* g4oracle — plain-C FP64 restatement of the GENESIS 1.3 v4 undulator step.
+ *
+ * TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / --impl reference legs of bench.py may load this library, and
+ * only as the checker or as the timed CPU baseline. The product (the CUDA path
+ * behind include/g4gpu.h) never calls it.
+ *
+ * Every function restates the reference algorithm at the cited file:line in
+ * GENESIS 1.3 v4.6.14 (svenreiche/Genesis-1.3-Version4). Parity is pinned against
+ * the reference itself, compiled from its own sources by oracle/ref_build/ into
+ * oracle/_ref/libg4ref.so, and against the fixtures in tests/golden/.
+ *
+ * Array conventions (shared with oracle/ref_build/g4ref_harness.cpp):
+ *   particles  [ns][npart][6] doubles: gamma, theta, x, y, px, py
+ *   fields     [nfld][ns][ngrid*ngrid] complex doubles (re, im), storage order;
+ *              window slice j lives in storage slot (j + first) % ns
+ *   lattice    [nsteps][G4_LAT_NCOL] doubles, one row per integration step
+ */
+#ifndef G4ORACLE_H
+#define G4ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  G4_LAT_AW, G4_LAT_AX, G4_LAT_AY, G4_LAT_KU, G4_LAT_KX, G4_LAT_KY, G4_LAT_GRADX,
+  G4_LAT_GRADY, G4_LAT_QF, G4_LAT_QX, G4_LAT_QY, G4_LAT_CX, G4_LAT_CY, G4_LAT_DZ,
+  G4_LAT_SLIP, G4_LAT_PHASE, G4_LAT_HELICAL, G4_LAT_Z, G4_LAT_NCOL
+};
+
+/* stage bits for orc_run_steps */
+#define ORC_STAGE_PUSH 1
+#define ORC_STAGE_FIELD 2
+#define ORC_STAGE_SLIP 4
+
+/* Runs nsteps integration steps in place (Gencore.cpp:102-147 without markers,
+ * sorting or diagnostics). solver: 0 = ADI, 1 = FFT (unfiltered), 2 = FFT with the
+ * sigmoid source filter (xcut, ycut, sigmoid in filt[0..2]). accuslip[nfld] is the
+ * accumulated slippage per field (Field::accuslip), carried in and out.
+ * nthreads >= 1 splits every per-slice loop over that many host threads. */
+int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int npart,
+                  double *particles, const double *current, double reflength,
+                  double sample, int nfld, const int *harm, int ngrid,
+                  const double *gridmax, double *fields, int *first, double *accuslip,
+                  int time_run, int periodic, int stages, int solver, const double *filt,
+                  int nthreads);
+
+/* Random and quasi-random streams (RandomU.cpp:17-73, Hammerslay.cpp:15-49). */
+void orc_ran2(int seed, int n, double *out);
+void orc_hammersley(int base_index, int start, int n, double *out);
+/* Inverse complementary error function (Inverfc.cpp:16-65). */
+void orc_inverfc(int n, const double *in, double *out);
+/* Bessel J_n (BesselJ.cpp) and undulator coupling fc(h) (Undulator.cpp:141-167). */
+double orc_besselj(int n, double x);
+double orc_fc(double aw, int helical, int h);
+
+/* Quiet loading + shot noise for nslice consecutive slices of one rank
+ * (LoadBeam.cpp:157-212, QuietLoading.cpp:50-260, ShotNoise.cpp:16-68).
+ * slicepar[nslice][17]: gamma, delgam, ex, ey, betax, betay, alphax, alphay,
+ * xcen, ycen, pxcen, pycen, bunch, bunchphase, emod, emodphase, current. */
+void orc_load_beam(int nslice, int islice0, int npart, int nbins, int seed, int shotnoise,
+                   double lambda, double sample, const double *slicepar, double *out);
+
+/* Gauss-Hermite seed field of one slice (GaussHermite.cpp:20-85).
+ * par: lambda, power, phase, z0, w0, xcen, ycen, xangle, yangle, nx, ny, harm */
+void orc_gauss_hermite(const double *par, double gridmax, int ngrid, double *out);
+
+/* Per-slice beam diagnostics (Diagnostic.cpp:373-563) for nharm bunching
+ * harmonics. out[ns][ORC_DB_NCOL + 2*nharm]: the columns below, then
+ * |b_h| and arg(b_h) for h = 1..nharm. */
+enum {
+  ORC_DB_ENERGY, ORC_DB_ENERGYSPREAD, ORC_DB_XPOS, ORC_DB_XSIZE, ORC_DB_YPOS, ORC_DB_YSIZE,
+  ORC_DB_PXPOS, ORC_DB_PYPOS, ORC_DB_EMITX, ORC_DB_EMITY, ORC_DB_BETAX, ORC_DB_BETAY,
+  ORC_DB_ALPHAX, ORC_DB_ALPHAY, ORC_DB_XMIN, ORC_DB_XMAX, ORC_DB_PXMIN, ORC_DB_PXMAX,
+  ORC_DB_YMIN, ORC_DB_YMAX, ORC_DB_PYMIN, ORC_DB_PYMAX, ORC_DB_EMIN, ORC_DB_EMAX,
+  ORC_DB_NCOL
+};
+void orc_diag_beam(int ns, int npart, const double *particles, int nharm, double *out);
+
+/* Per-slice field diagnostics (Diagnostic.cpp:718-902, without the FFTW part),
+ * indexed by window slice. out[ns][ORC_DF_NCOL]. */
+enum {
+  ORC_DF_POWER, ORC_DF_XPOS, ORC_DF_XSIZE, ORC_DF_YPOS, ORC_DF_YSIZE, ORC_DF_NF_INT,
+  ORC_DF_NF_PHI, ORC_DF_FF_INT, ORC_DF_FF_PHI, ORC_DF_NCOL
+};
+void orc_diag_field(int ns, int ngrid, double gridmax, double lambda0, int harm,
+                    const double *field, int first, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

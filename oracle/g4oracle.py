@@ -1,0 +1,179 @@
+"""ctypes bindings for the CPU checker libraries.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+cpu_baseline / --impl reference legs of bench.py, never by the product path.
+
+Two libraries share one calling convention:
+  * liborc   — oracle/g4oracle.c, the plain-C FP64 restatement (built by
+               oracle/build_oracle.py; travels to every machine);
+  * libg4ref — the GENESIS 1.3 v4 reference compiled from its own sources by
+               oracle/ref_build/Makefile (only where the reference is present).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liborc.so")
+REF_SO = os.path.join(HERE, "_ref", "libg4ref.so")
+
+# lattice table columns (oracle/g4oracle.h G4_LAT_*)
+LAT_COLS = ["aw", "ax", "ay", "ku", "kx", "ky", "gradx", "grady", "qf", "qx", "qy",
+            "cx", "cy", "dz", "slip", "phase", "helical", "z"]
+LAT_NCOL = len(LAT_COLS)
+LAT = {k: i for i, k in enumerate(LAT_COLS)}
+
+DB_COLS = ["energy", "energyspread", "xposition", "xsize", "yposition", "ysize",
+           "pxposition", "pyposition", "emitx", "emity", "betax", "betay", "alphax",
+           "alphay", "xmin", "xmax", "pxmin", "pxmax", "ymin", "ymax", "pymin", "pymax",
+           "emin", "emax"]
+DF_COLS = ["power", "xposition", "xsize", "yposition", "ysize", "intensity-nearfield",
+           "phase-nearfield", "intensity-farfield", "phase-farfield"]
+
+_P = ctypes.POINTER
+_d = ctypes.c_double
+_i = ctypes.c_int
+_pd = _P(ctypes.c_double)
+_pi = _P(ctypes.c_int)
+
+
+def _ptr(a, t=_pd):
+    return a.ctypes.data_as(t)
+
+
+class _Lib:
+    def __init__(self, path, prefix):
+        self.path = path
+        self.lib = ctypes.CDLL(path)
+        self.p = prefix
+        L = self.lib
+        f = getattr(L, prefix + "run_steps")
+        f.restype = _i
+        self.has_accuslip = prefix == "orc_"
+        if self.has_accuslip:
+            f.argtypes = [_i, _pd, _d, _i, _i, _pd, _pd, _d, _d, _i, _pi, _i, _pd, _pd, _pi,
+                          _pd, _i, _i, _i, _i, _pd, _i]
+        else:
+            f.argtypes = [_i, _pd, _d, _i, _i, _pd, _pd, _d, _d, _i, _pi, _i, _pd, _pd, _pi,
+                          _i, _i, _i]
+        getattr(L, prefix + "ran2").argtypes = [_i, _i, _pd]
+        getattr(L, prefix + "hammersley").argtypes = [_i, _i, _i, _pd]
+        getattr(L, prefix + "inverfc").argtypes = [_i, _pd, _pd]
+        getattr(L, prefix + "besselj").argtypes = [_i, _d]
+        getattr(L, prefix + "besselj").restype = _d
+        getattr(L, prefix + "fc").argtypes = [_d, _i, _i]
+        getattr(L, prefix + "fc").restype = _d
+        getattr(L, prefix + "load_beam").argtypes = [_i, _i, _i, _i, _i, _i, _d, _d, _pd, _pd]
+        getattr(L, prefix + "gauss_hermite").argtypes = [_pd, _d, _i, _pd]
+        if prefix == "orc_":
+            L.orc_diag_beam.argtypes = [_i, _i, _pd, _i, _pd]
+            L.orc_diag_field.argtypes = [_i, _i, _d, _d, _i, _pd, _i, _pd]
+
+    def ran2(self, seed, n):
+        out = np.zeros(n)
+        getattr(self.lib, self.p + "ran2")(seed, n, _ptr(out))
+        return out
+
+    def hammersley(self, base_index, start, n):
+        out = np.zeros(n)
+        getattr(self.lib, self.p + "hammersley")(base_index, start, n, _ptr(out))
+        return out
+
+    def inverfc(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros_like(x)
+        getattr(self.lib, self.p + "inverfc")(x.size, _ptr(x), _ptr(out))
+        return out
+
+    def besselj(self, n, x):
+        return getattr(self.lib, self.p + "besselj")(n, x)
+
+    def fc(self, aw, helical, h):
+        return getattr(self.lib, self.p + "fc")(aw, int(helical), h)
+
+    def load_beam(self, slicepar, islice0, npart, nbins, seed, shotnoise, lam, sample):
+        slicepar = np.ascontiguousarray(slicepar, dtype=np.float64).reshape(-1, 17)
+        ns = slicepar.shape[0]
+        out = np.zeros((ns, npart, 6))
+        getattr(self.lib, self.p + "load_beam")(ns, islice0, npart, nbins, seed, int(shotnoise),
+                                                lam, sample, _ptr(slicepar), _ptr(out))
+        return out
+
+    def gauss_hermite(self, par, gridmax, ngrid):
+        par = np.ascontiguousarray(par, dtype=np.float64)
+        out = np.zeros((ngrid * ngrid, 2))
+        getattr(self.lib, self.p + "gauss_hermite")(_ptr(par), gridmax, ngrid, _ptr(out))
+        return out[:, 0] + 1j * out[:, 1]
+
+    def run_steps(self, lat, gammaref, particles, current, reflength, sample, harm, gridmax,
+                  fields, first, time_run=True, periodic=False, stages=7, solver=0,
+                  filt=None, nthreads=1, accuslip=None):
+        """Runs the steps of `lat` in place on copies; returns (particles, fields, first, accuslip)."""
+        lat = np.ascontiguousarray(lat, dtype=np.float64).reshape(-1, LAT_NCOL)
+        part = np.array(particles, dtype=np.float64, order="C", copy=True)
+        ns, npart = part.shape[0], part.shape[1]
+        cur = np.ascontiguousarray(current, dtype=np.float64)
+        harm = np.ascontiguousarray(harm, dtype=np.int32)
+        nfld = harm.size
+        gm = np.ascontiguousarray(gridmax, dtype=np.float64).reshape(nfld)
+        f = np.array(fields, dtype=np.complex128, order="C", copy=True).reshape(nfld, ns, -1)
+        ngrid = int(round(np.sqrt(f.shape[2])))
+        fv = f.view(np.float64)
+        fst = np.ascontiguousarray(first, dtype=np.int32).reshape(nfld).copy()
+        fn = getattr(self.lib, self.p + "run_steps")
+        if self.has_accuslip:
+            acc = np.zeros(nfld) if accuslip is None else np.array(accuslip, dtype=np.float64)
+            fl = np.ones(3) if filt is None else np.ascontiguousarray(filt, dtype=np.float64)
+            rc = fn(lat.shape[0], _ptr(lat), gammaref, ns, npart, _ptr(part), _ptr(cur),
+                    reflength, sample, nfld, _ptr(harm, _pi), ngrid, _ptr(gm), _ptr(fv),
+                    _ptr(fst, _pi), _ptr(acc), int(time_run), int(periodic), stages, solver,
+                    _ptr(fl), nthreads)
+        else:
+            if solver != 0:
+                raise ValueError("the reference build has no FFT solver (no FFTW)")
+            acc = None
+            rc = fn(lat.shape[0], _ptr(lat), gammaref, ns, npart, _ptr(part), _ptr(cur),
+                    reflength, sample, nfld, _ptr(harm, _pi), ngrid, _ptr(gm), _ptr(fv),
+                    _ptr(fst, _pi), int(time_run), int(periodic), stages)
+        if rc != 0:
+            raise RuntimeError(f"{self.p}run_steps failed: {rc}")
+        return part, f, fst, acc
+
+    def diag_beam(self, particles, nharm):
+        part = np.ascontiguousarray(particles, dtype=np.float64)
+        ns, npart = part.shape[0], part.shape[1]
+        out = np.zeros((ns, len(DB_COLS) + 2 * nharm))
+        self.lib.orc_diag_beam(ns, npart, _ptr(part), nharm, _ptr(out))
+        return out
+
+    def diag_field(self, field, gridmax, lambda0, harm, first):
+        f = np.ascontiguousarray(field, dtype=np.complex128)
+        ns = f.shape[0]
+        ngrid = int(round(np.sqrt(f.shape[1])))
+        out = np.zeros((ns, len(DF_COLS)))
+        self.lib.orc_diag_field(ns, ngrid, gridmax, lambda0, harm, _ptr(f.view(np.float64)),
+                                int(first), _ptr(out))
+        return out
+
+
+_oracle = None
+_ref = None
+
+
+def oracle(path=None):
+    global _oracle
+    if _oracle is None or (path and _oracle.path != path):
+        _oracle = _Lib(path or ORACLE_SO, "orc_")
+    return _oracle
+
+
+def reference(path=None):
+    """The compiled reference checker, or None where it was not built."""
+    global _ref
+    p = path or REF_SO
+    if _ref is None:
+        if not os.path.exists(p):
+            return None
+        _ref = _Lib(p, "g4ref_")
+    return _ref

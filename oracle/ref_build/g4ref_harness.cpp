@@ -1,0 +1,208 @@
+// C entry points into the compiled GENESIS 1.3 v4 reference, used only to produce
+// known-answer vectors for the tests (tests/golden/) and to validate the C
+// restatement in oracle/g4oracle.c. It builds the reference's own Beam, Field,
+// Undulator and Control objects from flat arrays and runs the reference's step
+// sequence (Gencore.cpp:102-147): Beam::track, Field::track for every field and
+// Control::applySlippage, without diagnostics or markers.
+//
+// Test infrastructure only; the product never links or loads it.
+
+#include <cstring>
+#include <string>
+#include <vector>
+#include <complex>
+
+#include "Beam.h"
+#include "Field.h"
+#include "Undulator.h"
+#include "Control.h"
+#include "QuietLoading.h"
+#include "ShotNoise.h"
+#include "GaussHermite.h"
+#include "Inverfc.h"
+#include "RandomU.h"
+#include "Hammerslay.h"
+#include "BesselJ.h"
+
+// Electron charge as in GenMain.cpp:68 (ce), used for the electrons per slice.
+static const double kCe = 4.8032045e-11;
+
+// Column order of the per-step lattice table (one row per integration step).
+enum {
+  T_AW, T_AX, T_AY, T_KU, T_KX, T_KY, T_GRADX, T_GRADY, T_QF, T_QX, T_QY,
+  T_CX, T_CY, T_DZ, T_SLIP, T_PHASE, T_HELICAL, T_Z, T_NCOL
+};
+
+static void fill_undulator(Undulator *und, int nsteps, const double *tab, double gammaref) {
+  auto col = [&](std::vector<double> &v, int c) {
+    v.resize(nsteps);
+    for (int i = 0; i < nsteps; i++) v[i] = tab[i * T_NCOL + c];
+  };
+  col(und->aw, T_AW); col(und->ax, T_AX); col(und->ay, T_AY); col(und->ku, T_KU);
+  col(und->kx, T_KX); col(und->ky, T_KY); col(und->gradx, T_GRADX); col(und->grady, T_GRADY);
+  col(und->qf, T_QF); col(und->qx, T_QX); col(und->qy, T_QY); col(und->cx, T_CX);
+  col(und->cy, T_CY); col(und->dz, T_DZ); col(und->slip, T_SLIP); col(und->phaseshift, T_PHASE);
+  col(und->z, T_Z);
+  und->helical.resize(nsteps);
+  for (int i = 0; i < nsteps; i++) und->helical[i] = tab[i * T_NCOL + T_HELICAL] != 0 ? 1 : 0;
+  und->chic_angle.assign(nsteps, 0.0);
+  und->chic_lb.assign(nsteps, 0.0);
+  und->chic_ld.assign(nsteps, 0.0);
+  und->chic_lt.assign(nsteps, 0.0);
+  und->marker.assign(nsteps + 1, 0);
+  und->setGammaRef(gammaref);
+  und->updateMarker(0, 0, 0, 1e9);
+  und->updateOutput(1);
+}
+
+extern "C" {
+
+// Runs `nsteps` reference integration steps in place.
+//   particles: [ns][npart][6] (gamma, theta, x, y, px, py)
+//   fields:    [nfld][ns][ngrid*ngrid][2] in storage order; first[nfld] is the ring start
+//   stages:    bit 1 beam push, bit 2 field solve, bit 4 slippage
+// Returns 0 on success.
+int g4ref_run_steps(int nsteps, const double *tab, double gammaref, int ns, int npart,
+                    double *particles, const double *current, double reflength, double sample,
+                    int nfld, const int *harm, int ngrid, const double *gridmax, double *fields,
+                    int *first, int time_run, int periodic, int stages) {
+  Undulator und;
+  fill_undulator(&und, nsteps, tab, gammaref);
+
+  Beam beam;
+  beam.init(ns, 1, reflength, reflength * sample, 0.0, false);
+  for (int is = 0; is < ns; is++) {
+    beam.current[is] = current[is];
+    beam.beam[is].resize(npart);
+    for (int ip = 0; ip < npart; ip++) {
+      const double *p = particles + (static_cast<size_t>(is) * npart + ip) * 6;
+      Particle &q = beam.beam[is][ip];
+      q.gamma = p[0]; q.theta = p[1]; q.x = p[2]; q.y = p[3]; q.px = p[4]; q.py = p[5];
+    }
+  }
+
+  std::vector<Field *> fld;
+  size_t ncell = static_cast<size_t>(ngrid) * ngrid;
+  for (int k = 0; k < nfld; k++) {
+    Field *f = new Field;
+    f->init(ns, ngrid, gridmax[k], reflength, reflength * sample, 0.0, harm[k]);
+    f->initSolver(false, false, 1, 1, 1);
+    for (int is = 0; is < ns; is++)
+      for (size_t c = 0; c < ncell; c++) {
+        const double *v = fields + ((static_cast<size_t>(k) * ns + is) * ncell + c) * 2;
+        f->field[is][c] = std::complex<double>(v[0], v[1]);
+      }
+    f->first = first[k];
+    fld.push_back(f);
+  }
+
+  Control control;
+  control.init(0, 1, "g4ref", &beam, &fld, &und, time_run != 0, false, periodic != 0);
+  while (und.advance(0)) {
+    double delz = und.steplength();
+    if (stages & 1) beam.track(delz, &fld, &und);
+    if (stages & 2)
+      for (auto *f : fld) f->track(delz, &beam, &und);
+    if (stages & 4)
+      for (auto *f : fld) control.applySlippage(und.slippage(), f);
+  }
+
+  for (int is = 0; is < ns; is++)
+    for (int ip = 0; ip < npart; ip++) {
+      double *p = particles + (static_cast<size_t>(is) * npart + ip) * 6;
+      const Particle &q = beam.beam[is][ip];
+      p[0] = q.gamma; p[1] = q.theta; p[2] = q.x; p[3] = q.y; p[4] = q.px; p[5] = q.py;
+    }
+  for (int k = 0; k < nfld; k++) {
+    for (int is = 0; is < ns; is++)
+      for (size_t c = 0; c < ncell; c++) {
+        double *v = fields + ((static_cast<size_t>(k) * ns + is) * ncell + c) * 2;
+        v[0] = fld[k]->field[is][c].real();
+        v[1] = fld[k]->field[is][c].imag();
+      }
+    first[k] = static_cast<int>(fld[k]->first);
+    delete fld[k];
+  }
+  return 0;
+}
+
+// Reference random streams, for known-answer vectors.
+void g4ref_ran2(int seed, int n, double *out) {
+  RandomU r(seed);
+  for (int i = 0; i < n; i++) out[i] = r.getElement();
+}
+void g4ref_hammersley(int base_index, int start, int n, double *out) {
+  Hammerslay h(base_index);
+  h.set(start);
+  for (int i = 0; i < n; i++) out[i] = h.getElement();
+}
+void g4ref_inverfc(int n, const double *in, double *out) {
+  Inverfc e;
+  for (int i = 0; i < n; i++) out[i] = e.value(in[i]);
+}
+double g4ref_besselj(int n, double x) {
+  BesselJ b;
+  return b.value(n, x);
+}
+// Coupling factor fc(h) of Undulator.cpp:141-167 for one step.
+double g4ref_fc(double aw, int helical, int h) {
+  Undulator und;
+  double tab[T_NCOL] = {0};
+  tab[T_AW] = aw;
+  tab[T_HELICAL] = helical;
+  tab[T_DZ] = 1;
+  fill_undulator(&und, 1, tab, 1000.0);
+  und.advance(0);
+  return und.fc(h);
+}
+
+// One quiet-loaded slice (QuietLoading.cpp:50-260) plus optional shot noise
+// (ShotNoise.cpp:29-68), as LoadBeam.cpp:157-200 drives them for a single rank.
+// slicepar: gamma, delgam, ex, ey, betax, betay, alphax, alphay, xcen, ycen,
+//           pxcen, pycen, bunch, bunchphase, emod, emodphase, current
+// Slices islice0 .. islice0+nslice-1 are loaded in order with one shot-noise
+// stream seeded from `seed`, exactly as a single rank does.
+void g4ref_load_beam(int nslice, int islice0, int npart, int nbins, int seed, int shotnoise,
+                     double lambda, double sample, const double *slicepar, double *out) {
+  QuietLoading ql;
+  int base[6] = {0, 1, 2, 3, 4, 5};
+  ql.init(false, base);
+  ShotNoise sn;
+  sn.init(seed, 0);
+  std::vector<Particle> buf(npart);
+  for (int j = 0; j < nslice; j++) {
+    const double *sp = slicepar + static_cast<size_t>(j) * 17;
+    BeamSlice s;
+    s.gamma = sp[0]; s.delgam = sp[1]; s.ex = sp[2]; s.ey = sp[3];
+    s.betax = sp[4]; s.betay = sp[5]; s.alphax = sp[6]; s.alphay = sp[7];
+    s.xcen = sp[8]; s.ycen = sp[9]; s.pxcen = sp[10]; s.pycen = sp[11];
+    s.bunch = sp[12]; s.bunchphase = sp[13]; s.emod = sp[14]; s.emodphase = sp[15];
+    s.current = sp[16];
+    double ne = s.current * lambda * sample / kCe;
+    ql.loadQuiet(buf.data(), &s, npart, nbins, 4. * asin(1.), islice0 + j);
+    if (shotnoise) sn.applyShotNoise(buf.data(), npart, nbins, ne);
+    for (int k = 0; k < npart; k++) {
+      double *p = out + (static_cast<size_t>(j) * npart + k) * 6;
+      p[0] = buf[k].gamma; p[1] = buf[k].theta; p[2] = buf[k].x;
+      p[3] = buf[k].y; p[4] = buf[k].px; p[5] = buf[k].py;
+    }
+  }
+}
+
+// Gauss-Hermite seed field for one slice (GaussHermite.cpp:20-63).
+// par: lambda, power, phase, z0, w0, xcen, ycen, xangle, yangle, nx, ny, harm
+void g4ref_gauss_hermite(const double *par, double gridmax, int ngrid, double *out) {
+  FieldSlice s;
+  s.lambda = par[0]; s.power = par[1]; s.phase = par[2]; s.z0 = par[3]; s.w0 = par[4];
+  s.xcen = par[5]; s.ycen = par[6]; s.xangle = par[7]; s.yangle = par[8];
+  s.nx = static_cast<int>(par[9]); s.ny = static_cast<int>(par[10]); s.harm = static_cast<int>(par[11]);
+  std::vector<std::complex<double> > f(static_cast<size_t>(ngrid) * ngrid);
+  GaussHermite gh;
+  gh.loadGauss(f.data(), &s, gridmax, ngrid);
+  for (size_t i = 0; i < f.size(); i++) {
+    out[2 * i] = f[i].real();
+    out[2 * i + 1] = f[i].imag();
+  }
+}
+
+}  // extern "C"
