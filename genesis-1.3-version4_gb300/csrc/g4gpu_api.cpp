@@ -1,0 +1,774 @@
+// Host implementation of the C ABI in include/g4gpu.h: handle lifetime, device
+// memory, per-step constants, the step sequence and the slippage bookkeeping.
+//
+// The step sequence replaces the body of the reference's step loop
+// (src/Core/Gencore.cpp:102-147) for one time window held in GPU memory:
+//   push      Beam::track                      -> one fused kernel (+ deposition)
+//   field     Field::track of every field       -> deposition + ADI (or FFT) kernels
+//   slippage  Control::applySlippage            -> ring-start bookkeeping on the host
+//                                                  and a clear of the entering slice
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "g4gpu.h"
+#include "g4gpu_internal.h"
+
+using g4::StepConst;
+
+namespace g4 {
+// kernels_util.cu
+void launch_aos_to_soa(void *stream, const double *aos, void *const *soa, int mixed, double gref,
+                       size_t n);
+void launch_soa_to_aos(void *stream, const void *const *soa, double *aos, int mixed, double gref,
+                       size_t n);
+void launch_convert_field(void *stream, const void *in, void *out, size_t n, int to_float);
+}
+
+struct g4gpu_ctx {
+  g4gpu_config cfg{};
+  cudaStream_t stream = nullptr;
+  std::string err;
+  bool mixed = false;
+  size_t csize = 16;  // bytes per complex field value
+  size_t rsize = 8;   // bytes per particle coordinate other than theta
+
+  g4::DeviceBeam beam{};
+  void *field[G4GPU_MAX_FIELDS] = {};
+  void *src[G4GPU_MAX_FIELDS] = {};
+  void *tmp = nullptr;
+  void *coef = nullptr;      // [nset][3][ngrid] complex of the field type
+  size_t coef_bytes = 0;
+  void *fftk2 = nullptr;     // FFT propagator and filter tables
+  int *derr = nullptr;
+  double *ddiag = nullptr;
+  size_t ddiag_bytes = 0;
+  void *stage = nullptr;     // AoS staging buffer for host transfers
+  size_t stage_bytes = 0;
+  size_t bytes = 0;
+
+  int nsteps = 0;
+  std::vector<StepConst> steps;
+  std::vector<double> slip;
+  int first[G4GPU_MAX_FIELDS] = {};
+  double accuslip[G4GPU_MAX_FIELDS] = {};
+  bool beam_loaded = false;
+  bool field_loaded[G4GPU_MAX_FIELDS] = {};
+
+  bool prof = false;
+  long long launches[G4GPU_K_NCLASS] = {};
+  double ms[G4GPU_K_NCLASS] = {};
+  struct Pending {
+    int cls;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> pool;
+};
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_create_err;
+
+int fail(g4gpu_handle h, int code, const std::string &msg) {
+  if (h) {
+    h->err = msg;
+  } else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_create_err = msg;
+  }
+  return code;
+}
+
+int cuda_fail(g4gpu_handle h, cudaError_t e, const char *what) {
+  return fail(h, e == cudaErrorMemoryAllocation ? G4GPU_ERR_NOMEM : G4GPU_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define G4_CUDA(h, call)                            \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+cudaEvent_t take_event(g4gpu_handle h) {
+  if (!h->pool.empty()) {
+    cudaEvent_t e = h->pool.back();
+    h->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Brackets one kernel launch for accounting.
+struct Timed {
+  g4gpu_handle h;
+  int cls;
+  cudaEvent_t a = nullptr, b = nullptr;
+  Timed(g4gpu_handle h_, int cls_) : h(h_), cls(cls_) {
+    h->launches[cls]++;
+    if (h->prof) {
+      a = take_event(h);
+      b = take_event(h);
+      cudaEventRecord(a, h->stream);
+    }
+  }
+  ~Timed() {
+    if (h->prof) {
+      cudaEventRecord(b, h->stream);
+      h->pending.push_back({cls, a, b});
+    }
+  }
+};
+
+void collect_events(g4gpu_handle h) {
+  if (h->pending.empty()) return;
+  cudaStreamSynchronize(h->stream);
+  for (auto &p : h->pending) {
+    float t = 0;
+    cudaEventElapsedTime(&t, p.a, p.b);
+    h->ms[p.cls] += t;
+    h->pool.push_back(p.a);
+    h->pool.push_back(p.b);
+  }
+  h->pending.clear();
+}
+
+int check_device_flag(g4gpu_handle h) {
+  int v = 0;
+  G4_CUDA(h, cudaMemcpyAsync(&v, h->derr, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  G4_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (v != 0) {
+    char buf[128];
+    snprintf(buf, sizeof(buf), "device error flag raised (code %d)", v);
+    return fail(h, G4GPU_ERR_DEVICE, buf);
+  }
+  return G4GPU_OK;
+}
+
+int alloc(g4gpu_handle h, void **p, size_t n) {
+  cudaError_t e = cudaMalloc(p, n);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc");
+  h->bytes += n;
+  return G4GPU_OK;
+}
+
+// ADI coefficients of FieldSolverADI::init (src/Core/FieldSolverADI.cpp:125-182),
+// computed with std::complex<double> exactly as the reference does.
+void adi_coefficients(double delz, double dgrid, double xks, int ngrid, std::vector<std::complex<double>> &c,
+                      std::vector<std::complex<double>> &cbet, std::vector<std::complex<double>> &cwet,
+                      double *cstep_im) {
+  typedef std::complex<double> cd;
+  double rtmp = 0.25 * delz / (xks * dgrid * dgrid);
+  *cstep_im = rtmp;
+  std::vector<double> mupp(ngrid), mmid(ngrid), mlow(ngrid);
+  std::vector<cd> w1(ngrid), w2(ngrid);
+  c.assign(ngrid, 0);
+  cbet.assign(ngrid, 0);
+  cwet.assign(ngrid, 0);
+  mupp[0] = rtmp;
+  mmid[0] = -2 * rtmp;
+  mlow[0] = 0;
+  for (int i = 1; i < ngrid - 1; i++) {
+    mupp[i] = rtmp;
+    mmid[i] = -2 * rtmp;
+    mlow[i] = rtmp;
+  }
+  mupp[ngrid - 1] = 0;
+  mmid[ngrid - 1] = -2 * rtmp;
+  mlow[ngrid - 1] = rtmp;
+  for (int i = 0; i < ngrid; i++) {
+    w1[i] = cd(0, -mupp[i]);
+    w2[i] = cd(1, -mmid[i]);
+    c[i] = cd(0, -mlow[i]);
+  }
+  cbet[0] = 1. / w2[0];
+  cwet[0] = 0.;
+  for (int i = 1; i < ngrid; i++) {
+    cwet[i] = w1[i - 1] * cbet[i - 1];
+    cbet[i] = 1. / (w2[i] - c[i] * cwet[i]);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void g4gpu_config_defaults(g4gpu_config *cfg) {
+  if (!cfg) return;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->nslice = 1;
+  cfg->npart = 8192;  // Setup.cpp: npart
+  cfg->ngrid = 151;   // LoadField.cpp: ngrid
+  cfg->nfield = 1;
+  cfg->harm[0] = 1;
+  cfg->gridmax[0] = 1e-3;  // LoadField.cpp: dgrid
+  cfg->lambda0 = 1e-10;    // Setup.cpp: lambda0
+  cfg->sample = 1;
+  cfg->gammaref = 5800 / 0.511;  // Setup.cpp:19 gamma0
+  cfg->precision = G4GPU_PLAIN;
+  cfg->solver = G4GPU_SOLVER_ADI;
+  cfg->xcut = cfg->ycut = cfg->sigmoid = 1;  // Track.cpp:73-75
+  cfg->time_run = 0;
+  cfg->periodic = 0;
+  cfg->device = 0;
+}
+
+const char *g4gpu_last_error(g4gpu_handle h) {
+  if (h) return h->err.c_str();
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  return g_create_err.c_str();
+}
+
+int g4gpu_create(const g4gpu_config *cfg, g4gpu_handle *out) {
+  if (!cfg || !out) return fail(nullptr, G4GPU_ERR_ARG, "null argument");
+  *out = nullptr;
+  const g4gpu_config &c = *cfg;
+  if (c.nslice < 1 || c.npart < 1 || c.ngrid < 3 || c.nfield < 1 || c.nfield > G4GPU_MAX_FIELDS)
+    return fail(nullptr, G4GPU_ERR_ARG, "nslice, npart >= 1, ngrid >= 3, 1 <= nfield <= 8 required");
+  if (c.precision != G4GPU_PLAIN && c.precision != G4GPU_MIXED)
+    return fail(nullptr, G4GPU_ERR_ARG, "unknown precision");
+  if (c.solver != G4GPU_SOLVER_ADI && c.solver != G4GPU_SOLVER_FFT)
+    return fail(nullptr, G4GPU_ERR_ARG, "unknown solver");
+  for (int k = 0; k < c.nfield; k++)
+    if (c.harm[k] < 1 || !(c.gridmax[k] > 0))
+      return fail(nullptr, G4GPU_ERR_ARG, "harm >= 1 and gridmax > 0 required for every field");
+  if (!(c.lambda0 > 0) || !(c.sample > 0) || !(c.gammaref > 1))
+    return fail(nullptr, G4GPU_ERR_ARG, "lambda0 > 0, sample > 0 and gammaref > 1 required");
+  if ((long long)c.ngrid * c.ngrid > (1LL << 30))
+    return fail(nullptr, G4GPU_ERR_ARG, "ngrid too large");
+
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(nullptr, G4GPU_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  if (c.device < 0 || c.device >= ndev) return fail(nullptr, G4GPU_ERR_ARG, "device ordinal out of range");
+
+  g4gpu_handle h = new g4gpu_ctx;
+  h->cfg = c;
+  h->mixed = c.precision == G4GPU_MIXED;
+  h->csize = h->mixed ? 8 : 16;
+  h->rsize = h->mixed ? 4 : 8;
+  int rc = G4GPU_OK;
+  auto bail = [&](int code) {
+    g_create_err = h->err;
+    g4gpu_destroy(h);
+    return code;
+  };
+  if ((e = cudaSetDevice(c.device)) != cudaSuccess) return bail(cuda_fail(h, e, "cudaSetDevice"));
+  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(cuda_fail(h, e, "cudaStreamCreate"));
+
+  size_t np = (size_t)c.nslice * c.npart;
+  size_t ncell = (size_t)c.ngrid * c.ngrid;
+  void **coords[5] = {&h->beam.gamma, &h->beam.x, &h->beam.y, &h->beam.px, &h->beam.py};
+  for (auto p : coords)
+    if ((rc = alloc(h, p, np * h->rsize))) return bail(rc);
+  if ((rc = alloc(h, &h->beam.theta, np * sizeof(double)))) return bail(rc);
+  if ((rc = alloc(h, (void **)&h->beam.current, c.nslice * sizeof(double)))) return bail(rc);
+  for (int k = 0; k < c.nfield; k++) {
+    if ((rc = alloc(h, &h->field[k], (size_t)c.nslice * ncell * h->csize))) return bail(rc);
+    if ((rc = alloc(h, &h->src[k], (size_t)c.nslice * ncell * h->csize))) return bail(rc);
+    cudaMemsetAsync(h->field[k], 0, (size_t)c.nslice * ncell * h->csize, h->stream);
+    cudaMemsetAsync(h->src[k], 0, (size_t)c.nslice * ncell * h->csize, h->stream);
+  }
+  if ((rc = alloc(h, &h->tmp, (size_t)c.nslice * ncell * h->csize))) return bail(rc);
+  if ((rc = alloc(h, (void **)&h->derr, sizeof(int)))) return bail(rc);
+  cudaMemsetAsync(h->derr, 0, sizeof(int), h->stream);
+  if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(cuda_fail(h, e, "init"));
+  *out = h;
+  return G4GPU_OK;
+}
+
+void g4gpu_destroy(g4gpu_handle h) {
+  if (!h) return;
+  cudaSetDevice(h->cfg.device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  void *ptrs[] = {h->beam.gamma, h->beam.theta, h->beam.x, h->beam.y, h->beam.px, h->beam.py,
+                  h->beam.current, h->tmp, h->coef, h->fftk2, h->derr, h->ddiag, h->stage};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
+    if (h->field[k]) cudaFree(h->field[k]);
+    if (h->src[k]) cudaFree(h->src[k]);
+  }
+  for (auto &p : h->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (auto ev : h->pool) cudaEventDestroy(ev);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *tab) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (nsteps < 0 || (nsteps > 0 && !tab)) return fail(h, G4GPU_ERR_ARG, "bad lattice table");
+  cudaSetDevice(h->cfg.device);
+  const g4gpu_config &c = h->cfg;
+  int ng = c.ngrid;
+  h->steps.assign(nsteps, StepConst{});
+  h->slip.assign(nsteps, 0.0);
+  typedef std::complex<double> cd;
+  std::map<std::pair<int, double>, int> sets;  // (field, delz) -> set
+  std::vector<cd> coefs;                       // [nset][3][ng]
+  for (int i = 0; i < nsteps; i++) {
+    const double *r = tab + (size_t)i * G4GPU_LAT_NCOL;
+    StepConst &s = h->steps[i];
+    double aw = r[G4GPU_LAT_AW];
+    bool inund = aw > 0;  // Undulator::inUndulator, Undulator.h:141-146
+    double gamma0 = c.gammaref;
+    // TrackBeam::track, TrackBeam.cpp:17-64
+    double awt = inund ? aw : 0, dax = inund ? r[G4GPU_LAT_AX] : 0, day = inund ? r[G4GPU_LAT_AY] : 0;
+    double kxt = inund ? r[G4GPU_LAT_KX] : 0, kyt = inund ? r[G4GPU_LAT_KY] : 0;
+    double qf = r[G4GPU_LAT_QF];
+    double dqx = qf == 0 ? 0 : r[G4GPU_LAT_QX], dqy = qf == 0 ? 0 : r[G4GPU_LAT_QY];
+    double betpar0 = std::sqrt(1 - (1 + awt * awt) / gamma0 / gamma0);
+    double qquad = qf * gamma0;
+    double qnatx = kxt * awt * awt / gamma0 / betpar0;
+    double qnaty = kyt * awt * awt / gamma0 / betpar0;
+    double qx = qquad + qnatx, qy = -qquad + qnaty;
+    double xoff = qquad * dqx + qnatx * dax, yoff = -qquad * dqy + qnaty * day;
+    s.aw_t = awt;
+    s.qx = qx;
+    s.qy = qy;
+    if (qx == 0) {
+      s.kindx = 0;
+      s.xoff = xoff;
+    } else {
+      s.xoff = xoff / qx;
+      s.kindx = qx > 0 ? 1 : 2;
+    }
+    if (qy == 0) {
+      s.kindy = 0;
+      s.yoff = yoff;
+    } else {
+      s.yoff = yoff / qy;
+      s.kindy = qy > 0 ? 1 : 2;
+    }
+    double cx = r[G4GPU_LAT_CX], cy = r[G4GPU_LAT_CY];
+    s.cxk = cx * gamma0;
+    s.cyk = cy * gamma0;
+    s.corr = (cx != 0) || (cy != 0);
+    // BeamSolver::advance, BeamSolver.cpp:19-41
+    s.aw = aw;
+    s.ax = r[G4GPU_LAT_AX];
+    s.ay = r[G4GPU_LAT_AY];
+    s.kx = r[G4GPU_LAT_KX];
+    s.ky = r[G4GPU_LAT_KY];
+    s.gradx = r[G4GPU_LAT_GRADX];
+    s.grady = r[G4GPU_LAT_GRADY];
+    s.autophase = r[G4GPU_LAT_PHASE];
+    s.delz = r[G4GPU_LAT_DZ];
+    s.gammaref = gamma0;
+    s.nfld = c.nfield;
+    int helical = r[G4GPU_LAT_HELICAL] != 0;
+    double xks = 1;
+    for (int k = 0; k < c.nfield; k++) {
+      int harm = c.harm[k];
+      double xlambda = c.lambda0 / static_cast<double>(harm);  // Field.cpp:42
+      double fxks = 4. * std::asin(1) / xlambda;                // Field.cpp:65
+      double fc = g4::host_fc(aw, helical, harm);
+      xks = fxks / static_cast<double>(harm);
+      g4::FieldStep &f = s.f[k];
+      f.rtmp = fc / fxks;
+      f.rharm = static_cast<double>(harm);
+      f.fc = fc;
+      f.xks = fxks;
+      f.gridmax = c.gridmax[k];
+      f.dgrid = 2 * c.gridmax[k] / static_cast<double>(ng - 1);  // Field.cpp:46
+      f.dep_on = inund && (harm % 2 == 1);
+      double dk = 4. * std::asin(1.) / (static_cast<double>(ng) * f.dgrid);
+      f.k2scale = dk * dk / 2. / fxks;
+      auto key = std::make_pair(k, s.delz);
+      auto it = sets.find(key);
+      if (it == sets.end()) {
+        std::vector<cd> cc, cb, cw;
+        double cs;
+        adi_coefficients(s.delz, f.dgrid, fxks, ng, cc, cb, cw, &cs);
+        int id = static_cast<int>(sets.size());
+        sets[key] = id;
+        coefs.insert(coefs.end(), cc.begin(), cc.end());
+        coefs.insert(coefs.end(), cb.begin(), cb.end());
+        coefs.insert(coefs.end(), cw.begin(), cw.end());
+        it = sets.find(key);
+      }
+      f.coef = it->second;
+      f.cstep = 0.25 * s.delz / (fxks * f.dgrid * f.dgrid);
+    }
+    s.xks = xks;
+    s.xku = r[G4GPU_LAT_KU];
+    if (s.xku == 0) s.xku = xks * 0.5 / gamma0 / gamma0;  // BeamSolver.cpp:34-38
+    h->slip[i] = r[G4GPU_LAT_SLIP];
+  }
+  h->nsteps = nsteps;
+  if (h->coef) {
+    cudaFree(h->coef);
+    h->bytes -= h->coef_bytes;
+    h->coef = nullptr;
+    h->coef_bytes = 0;
+  }
+  if (!coefs.empty()) {
+    size_t n = coefs.size();
+    int rc = alloc(h, &h->coef, n * h->csize);
+    if (rc) return rc;
+    h->coef_bytes = n * h->csize;
+    if (h->mixed) {
+      std::vector<float> fl(2 * n);
+      for (size_t i = 0; i < n; i++) {
+        fl[2 * i] = static_cast<float>(coefs[i].real());
+        fl[2 * i + 1] = static_cast<float>(coefs[i].imag());
+      }
+      G4_CUDA(h, cudaMemcpy(h->coef, fl.data(), fl.size() * sizeof(float), cudaMemcpyHostToDevice));
+    } else {
+      G4_CUDA(h, cudaMemcpy(h->coef, coefs.data(), n * sizeof(cd), cudaMemcpyHostToDevice));
+    }
+  }
+  return G4GPU_OK;
+}
+
+static int ensure_stage(g4gpu_handle h, size_t n) {
+  if (h->stage_bytes >= n) return G4GPU_OK;
+  if (h->stage) {
+    cudaFree(h->stage);
+    h->bytes -= h->stage_bytes;
+    h->stage = nullptr;
+    h->stage_bytes = 0;
+  }
+  int rc = alloc(h, &h->stage, n);
+  if (rc == G4GPU_OK) h->stage_bytes = n;
+  return rc;
+}
+
+int g4gpu_load_beam(g4gpu_handle h, const double *particles, const double *current) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (!particles || !current) return fail(h, G4GPU_ERR_ARG, "null particles or current");
+  cudaSetDevice(h->cfg.device);
+  size_t n = (size_t)h->cfg.nslice * h->cfg.npart;
+  int rc = ensure_stage(h, n * 6 * sizeof(double));
+  if (rc) return rc;
+  G4_CUDA(h, cudaMemcpyAsync(h->stage, particles, n * 6 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  G4_CUDA(h, cudaMemcpyAsync(h->beam.current, current, h->cfg.nslice * sizeof(double),
+                             cudaMemcpyHostToDevice, h->stream));
+  void *soa[6] = {h->beam.gamma, h->beam.theta, h->beam.x, h->beam.y, h->beam.px, h->beam.py};
+  {
+    Timed t(h, G4GPU_K_MISC);
+    g4::launch_aos_to_soa(h->stream, (const double *)h->stage, soa, h->mixed, h->cfg.gammaref, n);
+  }
+  G4_CUDA(h, cudaGetLastError());
+  h->beam_loaded = true;
+  return G4GPU_OK;
+}
+
+int g4gpu_get_beam(g4gpu_handle h, double *particles) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (!particles) return fail(h, G4GPU_ERR_ARG, "null particles");
+  if (!h->beam_loaded) return fail(h, G4GPU_ERR_STATE, "no beam loaded");
+  cudaSetDevice(h->cfg.device);
+  size_t n = (size_t)h->cfg.nslice * h->cfg.npart;
+  int rc = ensure_stage(h, n * 6 * sizeof(double));
+  if (rc) return rc;
+  const void *soa[6] = {h->beam.gamma, h->beam.theta, h->beam.x, h->beam.y, h->beam.px, h->beam.py};
+  {
+    Timed t(h, G4GPU_K_MISC);
+    g4::launch_soa_to_aos(h->stream, soa, (double *)h->stage, h->mixed, h->cfg.gammaref, n);
+  }
+  G4_CUDA(h, cudaGetLastError());
+  G4_CUDA(h, cudaMemcpyAsync(particles, h->stage, n * 6 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return check_device_flag(h);
+}
+
+int g4gpu_load_field(g4gpu_handle h, int ifld, const double *field, int first, double accuslip) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (ifld < 0 || ifld >= h->cfg.nfield || !field) return fail(h, G4GPU_ERR_ARG, "bad field index or pointer");
+  if (first < 0 || first >= h->cfg.nslice) return fail(h, G4GPU_ERR_ARG, "first out of range");
+  cudaSetDevice(h->cfg.device);
+  size_t n = (size_t)h->cfg.nslice * h->cfg.ngrid * h->cfg.ngrid;
+  if (h->mixed) {
+    int rc = ensure_stage(h, n * 16);
+    if (rc) return rc;
+    G4_CUDA(h, cudaMemcpyAsync(h->stage, field, n * 16, cudaMemcpyHostToDevice, h->stream));
+    Timed t(h, G4GPU_K_MISC);
+    g4::launch_convert_field(h->stream, h->stage, h->field[ifld], n, 1);
+  } else {
+    G4_CUDA(h, cudaMemcpyAsync(h->field[ifld], field, n * 16, cudaMemcpyHostToDevice, h->stream));
+  }
+  G4_CUDA(h, cudaGetLastError());
+  h->first[ifld] = first;
+  h->accuslip[ifld] = accuslip;
+  h->field_loaded[ifld] = true;
+  return G4GPU_OK;
+}
+
+int g4gpu_get_field(g4gpu_handle h, int ifld, double *field, int *first, double *accuslip) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (ifld < 0 || ifld >= h->cfg.nfield) return fail(h, G4GPU_ERR_ARG, "bad field index");
+  cudaSetDevice(h->cfg.device);
+  size_t n = (size_t)h->cfg.nslice * h->cfg.ngrid * h->cfg.ngrid;
+  if (field) {
+    if (h->mixed) {
+      int rc = ensure_stage(h, n * 16);
+      if (rc) return rc;
+      {
+        Timed t(h, G4GPU_K_MISC);
+        g4::launch_convert_field(h->stream, h->field[ifld], h->stage, n, 0);
+      }
+      G4_CUDA(h, cudaMemcpyAsync(field, h->stage, n * 16, cudaMemcpyDeviceToHost, h->stream));
+    } else {
+      G4_CUDA(h, cudaMemcpyAsync(field, h->field[ifld], n * 16, cudaMemcpyDeviceToHost, h->stream));
+    }
+  }
+  if (first) *first = h->first[ifld];
+  if (accuslip) *accuslip = h->accuslip[ifld];
+  return check_device_flag(h);
+}
+
+int g4gpu_run(g4gpu_handle h, int istep0, int nsteps, int stages) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (istep0 < 0 || nsteps < 0 || istep0 + nsteps > h->nsteps)
+    return fail(h, G4GPU_ERR_ARG, "step range outside the lattice");
+  if (!h->beam_loaded) return fail(h, G4GPU_ERR_STATE, "no beam loaded");
+  for (int k = 0; k < h->cfg.nfield; k++)
+    if (!h->field_loaded[k]) return fail(h, G4GPU_ERR_STATE, "a field is not loaded");
+  if (h->cfg.solver == G4GPU_SOLVER_FFT && (stages & G4GPU_STAGE_FIELD))
+    return fail(h, G4GPU_ERR_ARG, "FFT solver not available in this build");
+  cudaSetDevice(h->cfg.device);
+  const g4gpu_config &c = h->cfg;
+  int ns = c.nslice, np = c.npart, ng = c.ngrid;
+  size_t ncell = (size_t)ng * ng;
+  g4::Launch L{h->stream, h->derr};
+  bool do_push = stages & G4GPU_STAGE_PUSH, do_field = stages & G4GPU_STAGE_FIELD;
+  bool do_slip = (stages & G4GPU_STAGE_SLIP) && c.time_run;
+  for (int istep = istep0; istep < istep0 + nsteps; istep++) {
+    StepConst sc = h->steps[istep];
+    for (int k = 0; k < c.nfield; k++) sc.f[k].first = h->first[k];
+    bool any_dep = false;
+    for (int k = 0; k < c.nfield; k++) any_dep = any_dep || sc.f[k].dep_on;
+    if (do_field && any_dep)
+      for (int k = 0; k < c.nfield; k++)
+        G4_CUDA(h, cudaMemsetAsync(h->src[k], 0, (size_t)ns * ncell * h->csize, h->stream));
+    g4::StepConstF scf{};
+    if (h->mixed) scf = g4::to_float(sc, np);
+    if (do_push) {
+      Timed t(h, G4GPU_K_PUSH);
+      if (h->mixed)
+        g4::launch_push_mixed(L, scf, h->beam, h->field, h->src, ns, np, ng, do_field && any_dep);
+      else
+        g4::launch_push_plain(L, sc, h->beam, h->field, h->src, ns, np, ng, do_field && any_dep);
+    } else if (do_field && any_dep) {
+      Timed t(h, G4GPU_K_PUSH);
+      if (h->mixed)
+        g4::launch_deposit_mixed(L, scf, h->beam, h->src, ns, np, ng);
+      else
+        g4::launch_deposit_plain(L, sc, h->beam, h->src, ns, np, ng);
+    }
+    if (do_field) {
+      for (int k = 0; k < c.nfield; k++) {
+        const char *cb = (const char *)h->coef + (size_t)sc.f[k].coef * 3 * ng * h->csize;
+        for (int phase = 0; phase < 2; phase++) {
+          Timed t(h, phase == 0 ? G4GPU_K_ADI_X : G4GPU_K_ADI_Y);
+          if (h->mixed)
+            g4::launch_adi_mixed(L, scf, k, phase, h->field[k], h->src[k], h->tmp, cb, ns, ng);
+          else
+            g4::launch_adi_plain(L, sc, k, phase, h->field[k], h->src[k], h->tmp, cb, ns, ng);
+        }
+      }
+    }
+    G4_CUDA(h, cudaGetLastError());
+    if (do_slip) {
+      // Control::applySlippage for a single rank (Control.cpp:158-276): the ring
+      // start moves by one slice per crossing of 0.8 sample and the slice that
+      // enters the window is cleared unless the window is periodic
+      for (int k = 0; k < c.nfield; k++) {
+        h->accuslip[k] += h->slip[istep];
+        int direction = 1;
+        while (std::fabs(h->accuslip[k]) > (c.sample * 0.8)) {
+          if (h->accuslip[k] < 0) direction = -1;
+          h->accuslip[k] -= c.sample * direction;
+          int last = (h->first[k] + ns - 1) % ns;
+          if (direction < 0) last = (last + 1) % ns;
+          if (!c.periodic) {
+            G4_CUDA(h, cudaMemsetAsync((char *)h->field[k] + (size_t)last * ncell * h->csize, 0,
+                                       ncell * h->csize, h->stream));
+          }
+          h->first[k] = last;
+          if (direction < 0) h->first[k] = (last + 1) % ns;
+        }
+      }
+    }
+  }
+  return G4GPU_OK;
+}
+
+int g4gpu_synchronize(g4gpu_handle h) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  cudaSetDevice(h->cfg.device);
+  G4_CUDA(h, cudaStreamSynchronize(h->stream));
+  G4_CUDA(h, cudaGetLastError());
+  return check_device_flag(h);
+}
+
+int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (nharm < 1 || nharm > G4GPU_MAX_HARM) return fail(h, G4GPU_ERR_ARG, "nharm must be 1..16");
+  cudaSetDevice(h->cfg.device);
+  const g4gpu_config &c = h->cfg;
+  int ns = c.nslice, np = c.npart, ng = c.ngrid;
+  int bw = g4::beam_diag_width(nharm), fw = g4::kFieldSums + 2;
+  size_t need = ((size_t)ns * bw + (size_t)c.nfield * ns * fw) * sizeof(double);
+  if (need > h->ddiag_bytes) {
+    if (h->ddiag) cudaFree(h->ddiag);
+    h->ddiag = nullptr;
+    h->ddiag_bytes = 0;
+    int rc = alloc(h, (void **)&h->ddiag, need);
+    if (rc) return rc;
+    h->ddiag_bytes = need;
+  }
+  g4::Launch L{h->stream, h->derr};
+  double *db = h->ddiag, *dfd = h->ddiag + (size_t)ns * bw;
+  if (beam_out) {
+    if (!h->beam_loaded) return fail(h, G4GPU_ERR_STATE, "no beam loaded");
+    Timed t(h, G4GPU_K_DIAG);
+    if (h->mixed)
+      g4::launch_diag_beam_mixed(L, h->beam, c.gammaref, ns, np, nharm, db);
+    else
+      g4::launch_diag_beam_plain(L, h->beam, ns, np, nharm, db);
+  }
+  if (field_out) {
+    for (int k = 0; k < c.nfield; k++) {
+      Timed t(h, G4GPU_K_DIAG);
+      if (h->mixed)
+        g4::launch_diag_field_mixed(L, h->field[k], ns, ng, dfd + (size_t)k * ns * fw);
+      else
+        g4::launch_diag_field_plain(L, h->field[k], ns, ng, dfd + (size_t)k * ns * fw);
+    }
+  }
+  G4_CUDA(h, cudaGetLastError());
+  std::vector<double> raw(need / sizeof(double));
+  G4_CUDA(h, cudaMemcpyAsync(raw.data(), h->ddiag, need, cudaMemcpyDeviceToHost, h->stream));
+  int rc = check_device_flag(h);
+  if (rc) return rc;
+
+  if (beam_out) {
+    // DiagBeam::getValues, Diagnostic.cpp:457-531
+    int ow = G4GPU_DB_NCOL + 2 * nharm;
+    double norm = np > 0 ? 1. / static_cast<double>(np) : 1.;
+    for (int is = 0; is < ns; is++) {
+      const double *s = raw.data() + (size_t)is * bw;
+      double g1 = s[0] * norm, g2 = s[1] * norm, x1 = s[2] * norm, x2 = s[3] * norm;
+      double y1 = s[4] * norm, y2 = s[5] * norm, px1 = s[6] * norm, px2 = s[7] * norm;
+      double py1 = s[8] * norm, py2 = s[9] * norm, xpx = s[10] * norm, ypy = s[11] * norm;
+      double *o = beam_out + (size_t)is * ow;
+      o[G4GPU_DB_ENERGY] = g1;
+      o[G4GPU_DB_ENERGYSPREAD] = std::sqrt(std::fabs(g2 - g1 * g1));
+      o[G4GPU_DB_XPOS] = x1;
+      o[G4GPU_DB_XSIZE] = std::sqrt(std::fabs(x2 - x1 * x1));
+      o[G4GPU_DB_YPOS] = y1;
+      o[G4GPU_DB_YSIZE] = std::sqrt(std::fabs(y2 - y1 * y1));
+      o[G4GPU_DB_PXPOS] = px1;
+      o[G4GPU_DB_PYPOS] = py1;
+      double ex = std::sqrt(std::fabs((x2 - x1 * x1) * (px2 - px1 * px1) - (xpx - x1 * px1) * (xpx - x1 * px1)));
+      double ey = std::sqrt(std::fabs((y2 - y1 * y1) * (py2 - py1 * py1) - (ypy - y1 * py1) * (ypy - y1 * py1)));
+      o[G4GPU_DB_EMITX] = ex;
+      o[G4GPU_DB_EMITY] = ey;
+      o[G4GPU_DB_BETAX] = (x2 - x1 * x1) / ex * g1;
+      o[G4GPU_DB_BETAY] = (y2 - y1 * y1) / ey * g1;
+      o[G4GPU_DB_ALPHAX] = -(xpx - x1 * px1) / ex;
+      o[G4GPU_DB_ALPHAY] = -(ypy - y1 * py1) / ey;
+      for (int k = 0; k < 10; k++) o[G4GPU_DB_XMIN + k] = s[g4::kBeamSums + k];
+      for (int hh = 0; hh < nharm; hh++) {
+        double br = s[g4::kBeamSums + g4::kBeamMinMax + 2 * hh] * norm;
+        double bi = s[g4::kBeamSums + g4::kBeamMinMax + 2 * hh + 1] * norm;
+        o[G4GPU_DB_NCOL + 2 * hh] = std::abs(std::complex<double>(br, bi));
+        o[G4GPU_DB_NCOL + 2 * hh + 1] = std::atan2(bi, br);
+      }
+    }
+  }
+  if (field_out) {
+    // DiagField::getValues, Diagnostic.cpp:796-866
+    for (int k = 0; k < c.nfield; k++) {
+      double xlambda = c.lambda0 / static_cast<double>(c.harm[k]);
+      double dgrid = 2 * c.gridmax[k] / static_cast<double>(ng - 1);
+      double ks = 4. * std::asin(1) / xlambda;
+      double scl = dgrid * g4::kEev / ks;
+      for (int is0 = 0; is0 < ns; is0++) {
+        const double *s = raw.data() + (size_t)ns * bw + ((size_t)k * ns + is0) * fw;
+        int is = (ns + is0 - h->first[k]) % ns;
+        double power = s[0], x1 = s[1], x2 = s[2], y1 = s[3], y2 = s[4];
+        if (power > 0) {
+          x1 /= power;
+          x2 /= power;
+          y1 /= power;
+          y2 /= power;
+        }
+        x2 = std::sqrt(std::fabs(x2 - x1 * x1));
+        y2 = std::sqrt(std::fabs(y2 - y1 * y1));
+        double inten = s[7] * s[7] + s[8] * s[8];
+        double intenphi = std::atan2(s[8], s[7]);
+        double farfield = (s[5] * s[5] + s[6] * s[6]) * dgrid * dgrid;
+        double farphi = std::atan2(s[6], s[5]);
+        double *o = field_out + ((size_t)k * ns + is) * G4GPU_DF_NCOL;
+        o[G4GPU_DF_POWER] = power * scl * scl / g4::kVacimp;
+        o[G4GPU_DF_XPOS] = x1 * dgrid;
+        o[G4GPU_DF_XSIZE] = x2 * dgrid;
+        o[G4GPU_DF_YPOS] = y1 * dgrid;
+        o[G4GPU_DF_YSIZE] = y2 * dgrid;
+        o[G4GPU_DF_NF_INT] = inten * g4::kEev * g4::kEev / ks / ks / g4::kVacimp;
+        o[G4GPU_DF_NF_PHI] = intenphi;
+        o[G4GPU_DF_FF_INT] = farfield;
+        o[G4GPU_DF_FF_PHI] = farphi;
+      }
+    }
+  }
+  return G4GPU_OK;
+}
+
+int g4gpu_get_stream(g4gpu_handle h, void **stream) {
+  if (!h || !stream) return fail(h, G4GPU_ERR_ARG, "null argument");
+  *stream = h->stream;
+  return G4GPU_OK;
+}
+
+int g4gpu_set_profiling(g4gpu_handle h, int on) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  collect_events(h);
+  h->prof = on != 0;
+  return G4GPU_OK;
+}
+
+int g4gpu_kernel_stats(g4gpu_handle h, long long *launches, double *ms) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  cudaSetDevice(h->cfg.device);
+  collect_events(h);
+  for (int k = 0; k < G4GPU_K_NCLASS; k++) {
+    if (launches) launches[k] = h->launches[k];
+    if (ms) ms[k] = h->ms[k];
+  }
+  return G4GPU_OK;
+}
+
+int g4gpu_reset_stats(g4gpu_handle h) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  collect_events(h);
+  for (int k = 0; k < G4GPU_K_NCLASS; k++) {
+    h->launches[k] = 0;
+    h->ms[k] = 0;
+  }
+  return G4GPU_OK;
+}
+
+size_t g4gpu_device_bytes(g4gpu_handle h) { return h ? h->bytes : 0; }
+
+}  // extern "C"

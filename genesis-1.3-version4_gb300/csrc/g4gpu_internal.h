@@ -1,0 +1,122 @@
+// Internal declarations shared by the host API (g4gpu_api.cpp) and the CUDA
+// kernels (step_*.cu). Not part of the ABI.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include "g4gpu.h"
+
+namespace g4 {
+
+// physical constants of the reference (src/Main/GenMain.cpp:63-68)
+constexpr double kVacimp = 376.73;
+constexpr double kEev = 510998.95069;
+constexpr double kCe = 4.8032045e-11;
+
+// Per field, per integration step constants.
+struct FieldStep {
+  double rtmp;    // fc(h) / xks of this field (BeamSolver.cpp:28)
+  double rharm;   // harmonic number as a double (BeamSolver.cpp:30)
+  double fc;      // fc(h) (Undulator.cpp:141-167), used by the deposition
+  double xks;     // field wavenumber 2 pi h / lambda0 (Field.cpp:65)
+  double gridmax; // half width of the grid (Field::gridmax)
+  double dgrid;   // grid spacing 2 gridmax / (ngrid - 1) (Field.cpp:46)
+  double cstep;   // imaginary part of the ADI step factor i dz / (4 xks dgrid^2)
+  double k2scale; // FFT propagator: dk^2 dz / (2 xks)
+  int dep_on;     // deposition active: in undulator and odd harmonic (FieldSolverADI.cpp:20)
+  int coef;       // index of the ADI coefficient set of this (field, delz)
+  int first;      // ring start of the field when the step runs (filled at launch)
+  int pad;
+};
+
+// Per integration step constants (Undulator accessors, Undulator.h:82-204).
+struct StepConst {
+  // transverse optics, TrackBeam::track (TrackBeam.cpp:17-64)
+  double aw_t;        // aw inside an undulator, else 0
+  double qx, qy;      // focusing strengths
+  double xoff, yoff;  // focusing centres (already divided by qx, qy)
+  double cxk, cyk;    // corrector kicks times gamma0
+  int kindx, kindy;   // 0 drift, 1 focusing, 2 defocusing
+  int corr;           // corrector active at the end of the step
+  int nfld;
+  // longitudinal push, BeamSolver::advance (BeamSolver.cpp:13-87)
+  double aw;          // aw[istepz] as BeamSolver reads it
+  double ax, ay, kx, ky, gradx, grady;  // faw / faw2 (Undulator.cpp:170-182)
+  double autophase;
+  double xks;         // fundamental wavenumber
+  double xku;         // undulator wavenumber, or xks/(2 gamma0^2) in drifts
+  double delz;
+  double gammaref;
+  FieldStep f[G4GPU_MAX_FIELDS];
+};
+
+// FP32 copy of the per-step constants for the mixed-precision kernels, prepared on
+// the host so that no kernel converts FP64 constants per particle.
+struct FieldStepF {
+  float rtmp, rharm, gridmax, dgrid, cstep;
+  float dep_scl;  // fc vacimp xks delz / (4 eev npart dgrid^2): times the slice current
+  int dep_on, coef, first, harm;
+};
+struct StepConstF {
+  float aw_t, qx, qy, xoff, yoff, cxk, cyk;
+  int kindx, kindy, corr, nfld;
+  float aw, ax, ay, kx, ky, gradx, grady;
+  float xks, xku, delz, ztemp1;
+  double autophase;
+  double gammaref;
+  FieldStepF f[G4GPU_MAX_FIELDS];
+};
+StepConstF to_float(const StepConst &s, int npart);
+
+// Device arrays of one time window.
+struct DeviceBeam {
+  void *gamma, *theta, *x, *y, *px, *py;  // theta is always double
+  double *current;
+};
+
+struct Launch {
+  void *stream;
+  int *err;  // device error flag
+};
+
+// kernels_plain.cu (FP64, the reference's arithmetic)
+void launch_push_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,
+                       void *const *field, void *const *src, int ns, int np, int ngrid,
+                       int deposit);
+void launch_deposit_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,
+                          void *const *src, int ns, int np, int ngrid);
+// phase 0: implicit along x into tmp; phase 1: implicit along y back into the field
+void launch_adi_plain(const Launch &L, const StepConst &sc, int k, int phase, void *field,
+                      const void *src, void *tmp, const void *coef, int ns, int ngrid);
+void launch_diag_beam_plain(const Launch &L, const DeviceBeam &b, int ns, int np, int nharm,
+                            double *out);
+void launch_diag_field_plain(const Launch &L, const void *field, int ns, int ngrid,
+                             double *out);
+
+// kernels_mixed.cu (FP32 field, FP64 phase)
+void launch_push_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,
+                       void *const *field, void *const *src, int ns, int np, int ngrid,
+                       int deposit);
+void launch_deposit_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,
+                          void *const *src, int ns, int np, int ngrid);
+void launch_adi_mixed(const Launch &L, const StepConstF &sc, int k, int phase, void *field,
+                      const void *src, void *tmp, const void *coef, int ns, int ngrid);
+void launch_diag_beam_mixed(const Launch &L, const DeviceBeam &b, double gammaref, int ns, int np,
+                            int nharm, double *out);
+void launch_diag_field_mixed(const Launch &L, const void *field, int ns, int ngrid,
+                             double *out);
+
+// number of raw sums per slice written by the diagnostic kernels
+constexpr int kBeamSums = 12;   // g1 g2 x1 x2 y1 y2 px1 px2 py1 py2 xpx ypy
+constexpr int kBeamMinMax = 10; // xmin xmax pxmin pxmax ymin ymax pymin pymax gmin gmax
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline int beam_diag_width(int nharm) { return kBeamSums + kBeamMinMax + 2 * nharm; }
+constexpr int kFieldSums = 7;   // power x1 x2 y1 y2 ff.re ff.im
+
+// host_loading.cpp
+double host_fc(double aw, int helical, int h);
+
+}  // namespace g4

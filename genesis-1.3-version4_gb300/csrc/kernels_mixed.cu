@@ -1,0 +1,549 @@
+// Mixed-precision kernels of the undulator step: FP32 field, ADI solve,
+// deposition and transverse optics; FP64 accumulated ponderomotive phase.
+//
+// Storage: theta FP64; gamma as the FP32 offset from gammaref (|offset| is a few
+// units, so FP32 resolves it to ~1e-7); x, y, px, py FP32; fields float2.
+// Numerics that differ in form (not in value) from the reference's FP64 code:
+//  * the phase is reduced to [-pi, pi] in FP64 once per step; the RK4 stages and
+//    the deposition work on FP32 offsets from it, and the step's FP32 increment is
+//    added to the FP64 phase;
+//  * 1 - 1/beta_par is evaluated as -eps / (s (1 + s)), s = sqrt(1 - eps), which
+//    has no cancellation in FP32 (eps ~ 1e-8);
+//  * RK4 is written in its classic form, algebraically identical to the reference's
+//    "pushp" sequence (BeamSolver.cpp:89-141).
+#include <cuda_runtime.h>
+
+#include "g4gpu_internal.h"
+
+namespace g4 {
+
+StepConstF to_float(const StepConst &s, int npart) {
+  StepConstF f{};
+  f.aw_t = (float)s.aw_t;
+  f.qx = (float)s.qx;
+  f.qy = (float)s.qy;
+  f.xoff = (float)s.xoff;
+  f.yoff = (float)s.yoff;
+  f.cxk = (float)s.cxk;
+  f.cyk = (float)s.cyk;
+  f.kindx = s.kindx;
+  f.kindy = s.kindy;
+  f.corr = s.corr;
+  f.nfld = s.nfld;
+  f.aw = (float)s.aw;
+  f.ax = (float)s.ax;
+  f.ay = (float)s.ay;
+  f.kx = (float)s.kx;
+  f.ky = (float)s.ky;
+  f.gradx = (float)s.gradx;
+  f.grady = (float)s.grady;
+  f.xks = (float)s.xks;
+  f.xku = (float)s.xku;
+  f.delz = (float)s.delz;
+  f.ztemp1 = (float)(-2. / s.xks);
+  f.autophase = s.autophase;
+  f.gammaref = s.gammaref;
+  for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
+    const FieldStep &a = s.f[k];
+    FieldStepF &b = f.f[k];
+    b.rtmp = (float)a.rtmp;
+    b.rharm = (float)a.rharm;
+    b.gridmax = (float)a.gridmax;
+    b.dgrid = (float)a.dgrid;
+    b.cstep = (float)a.cstep;
+    b.dep_scl = a.dgrid > 0 ? (float)(a.fc * kVacimp * a.xks * s.delz /
+                                      (4 * kEev * (double)npart * a.dgrid * a.dgrid))
+                            : 0.f;
+    b.dep_on = a.dep_on;
+    b.coef = a.coef;
+    b.first = a.first;
+    b.harm = (int)a.rharm;
+  }
+  return f;
+}
+
+namespace {
+
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+constexpr float kTwoPiF = 6.283185307f;
+constexpr float kInvTwoPiF = 0.159154943f;
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// reduces an FP32 angle of moderate size (|a| < ~1e3) to [-pi, pi]
+__device__ __forceinline__ float wrapf(float a) { return fmaf(-kTwoPiF, rintf(a * kInvTwoPiF), a); }
+
+__device__ __forceinline__ void plane_step_f(int kind, float q, float off, float delz, float &x,
+                                             float &p, float gz) {
+  if (kind == 0) {
+    x += p * delz / gz;
+  } else if (kind == 1) {
+    float foc = sqrtf(q / gz), omg = foc * delz, s, c;
+    sincosf(omg, &s, &c);
+    float a2 = s / foc, a3 = -a2 * foc * foc, xt = x - off;
+    x = c * xt + a2 * p / gz + off;
+    p = a3 * xt * gz + c * p;
+  } else {
+    float foc = sqrtf(-q / gz), omg = foc * delz;
+    float a1 = coshf(omg), a2 = sinhf(omg) / foc, a3 = a2 * foc * foc, xt = x - off;
+    x = a1 * xt + a2 * p / gz + off;
+    p = a3 * xt * gz + a1 * p;
+  }
+}
+
+// TrackBeam::track over half a step in FP32; g is the full Lorentz factor.
+__device__ __forceinline__ void transverse_f(const StepConstF &sc, bool last, float g, float &x,
+                                             float &y, float &px, float &py) {
+  if (last && sc.corr) {
+    px += sc.cxk;
+    py += sc.cyk;
+  }
+  float a = 1.f + sc.aw_t * sc.aw_t + px * px + py * py;
+  float gz = g * sqrtf(1.f - a / (g * g));
+  float dz = 0.5f * sc.delz;
+  plane_step_f(sc.kindx, sc.qx, sc.xoff, dz, x, px, gz);
+  plane_step_f(sc.kindy, sc.qy, sc.yoff, dz, y, py, gz);
+}
+
+struct CellF {
+  int i00, i10, i01, i11;
+  float wx, wy;
+};
+__device__ __forceinline__ bool ll_gridpoint_f(float gm, float dg, int ng, float x, float y, CellF &c) {
+  if ((x > -gm) && (x < gm) && (y > -gm) && (y < gm)) {
+    float wx = (x + gm) / dg, wy = (y + gm) / dg;
+    float fx = floorf(wx), fy = floorf(wy);
+    int ix = min((int)fx, ng - 1), iy = min((int)fy, ng - 1);
+    c.wx = 1.f + fx - wx;
+    c.wy = 1.f + fy - wy;
+    int ix1 = ix + 1 < ng ? ix + 1 : ix;
+    int iy1 = iy + 1 < ng ? iy + 1 : iy;
+    c.i00 = ix + iy * ng;
+    c.i10 = ix1 + iy * ng;
+    c.i01 = ix + iy1 * ng;
+    c.i11 = ix1 + iy1 * ng;
+    return true;
+  }
+  return false;
+}
+
+// e^{-i h a} for the harmonics of one ODE evaluation, a in [-pi, pi] + small
+template <int NF>
+__device__ __forceinline__ void ode_f(const StepConstF &sc, const float2 *rpart, float btpar,
+                                      float g, float a, float &dgam, float &dth) {
+  float2 ctmp = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int i = 0; i < NF; i++) {
+    if (i >= sc.nfld) break;
+    float s, c;
+    __sincosf(wrapf(sc.f[i].rharm * a), &s, &c);
+    ctmp.x += rpart[i].x * c + rpart[i].y * s;
+    ctmp.y += rpart[i].y * c - rpart[i].x * s;
+  }
+  float btper0 = btpar + sc.ztemp1 * ctmp.x;
+  float eps = btper0 / (g * g);
+  float s = sqrtf(1.f - eps);
+  dth = -sc.xks * eps / (s * (1.f + s)) + sc.xku;
+  dgam = ctmp.y / (s * g);
+}
+
+struct PtrsF {
+  float *dg, *x, *y, *px, *py;
+  double *theta;
+  const double *current;
+  const float2 *field[G4GPU_MAX_FIELDS];
+  float2 *src[G4GPU_MAX_FIELDS];
+};
+
+template <int NF>
+__device__ __forceinline__ void deposit_f(const StepConstF &sc, const PtrsF &p, size_t off, int ng,
+                                          float cur, float g, float a, float x, float y) {
+  float dx = x - sc.ax, dy = y - sc.ay;
+  float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
+  float base = sqrtf(faw2) / g;
+#pragma unroll
+  for (int k = 0; k < NF; k++) {
+    if (k >= sc.nfld) break;
+    const FieldStepF &fs = sc.f[k];
+    if (!fs.dep_on) continue;
+    CellF c;
+    if (!ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x, y, c)) continue;
+    float part = base * fs.dep_scl * cur;
+    float s, co;
+    __sincosf(wrapf(fs.rharm * a), &s, &co);
+    float2 cp = make_float2(s * part, co * part);
+    float2 *d = p.src[k] + off;
+    float w = c.wx * c.wy;
+    atomicAdd(d + c.i00, make_float2(w * cp.x, w * cp.y));
+    w = (1.f - c.wx) * c.wy;
+    atomicAdd(d + c.i10, make_float2(w * cp.x, w * cp.y));
+    w = c.wx * (1.f - c.wy);
+    atomicAdd(d + c.i01, make_float2(w * cp.x, w * cp.y));
+    w = (1.f - c.wx) * (1.f - c.wy);
+    atomicAdd(d + c.i11, make_float2(w * cp.x, w * cp.y));
+  }
+}
+
+template <int NF>
+__global__ void __launch_bounds__(256) k_push_f(StepConstF sc, PtrsF p, int ns, int np, int ng,
+                                                int deposit) {
+  int is = blockIdx.y;
+  int ip = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ip >= np) return;
+  size_t o = (size_t)is * np + ip;
+  const float g0 = (float)sc.gammaref;
+  float dg = p.dg[o], x = p.x[o], y = p.y[o], px = p.px[o], py = p.py[o];
+  double th = p.theta[o] + sc.autophase;
+  size_t ncell = (size_t)ng * ng;
+
+  transverse_f(sc, false, g0 + dg, x, y, px, py);
+
+  // phase reduced once in FP64; the step works on FP32 offsets from it
+  double nturn = rint(th * (1.0 / kTwoPi));
+  float a0 = (float)fma(-nturn, kTwoPi, th);
+
+  float ddx = x - sc.ax, ddy = y - sc.ay;
+  float awloc = 1.f + 0.5f * (sc.kx * ddx * ddx + sc.ky * ddy * ddy) + sc.gradx * ddx + sc.grady * ddy;
+  float btpar = 1.f + px * px + py * py + sc.aw * sc.aw * awloc * awloc;
+  float2 rpart[NF];
+#pragma unroll
+  for (int k = 0; k < NF; k++) {
+    if (k >= sc.nfld) break;
+    const FieldStepF &fs = sc.f[k];
+    int islice = (is + fs.first) % ns;
+    const float2 *f = p.field[k] + (size_t)islice * ncell;
+    CellF c;
+    if (ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x, y, c)) {
+      float2 v00 = f[c.i00], v10 = f[c.i10], v01 = f[c.i01], v11 = f[c.i11];
+      float w00 = c.wx * c.wy, w10 = (1.f - c.wx) * c.wy, w01 = c.wx * (1.f - c.wy),
+            w11 = (1.f - c.wx) * (1.f - c.wy);
+      float cr = v00.x * w00 + v10.x * w10 + v01.x * w01 + v11.x * w11;
+      float ci = v00.y * w00 + v10.y * w10 + v01.y * w01 + v11.y * w11;
+      float r = fs.rtmp * awloc;
+      rpart[k] = make_float2(r * cr, -r * ci);
+    } else {
+      rpart[k] = make_float2(0.f, 0.f);
+    }
+  }
+
+  // classic RK4 on (gamma offset, phase offset)
+  const float h = sc.delz, h2 = 0.5f * sc.delz;
+  float k1g, k1t, k2g, k2t, k3g, k3t, k4g, k4t;
+  ode_f<NF>(sc, rpart, btpar, g0 + dg, a0, k1g, k1t);
+  ode_f<NF>(sc, rpart, btpar, g0 + (dg + h2 * k1g), a0 + h2 * k1t, k2g, k2t);
+  ode_f<NF>(sc, rpart, btpar, g0 + (dg + h2 * k2g), a0 + h2 * k2t, k3g, k3t);
+  ode_f<NF>(sc, rpart, btpar, g0 + (dg + h * k3g), a0 + h * k3t, k4g, k4t);
+  const float h6 = sc.delz * (1.f / 6.f);
+  float dgam = h6 * (k1g + 2.f * k2g + 2.f * k3g + k4g);
+  float dth = h6 * (k1t + 2.f * k2t + 2.f * k3t + k4t);
+  dg += dgam;
+  th += (double)dth;
+  float a1 = a0 + dth;
+  float g = g0 + dg;
+
+  transverse_f(sc, true, g, x, y, px, py);
+
+  p.dg[o] = dg;
+  p.theta[o] = th;
+  p.x[o] = x;
+  p.y[o] = y;
+  p.px[o] = px;
+  p.py[o] = py;
+  if (deposit) deposit_f<NF>(sc, p, (size_t)is * ncell, ng, (float)p.current[is], g, wrapf(a1), x, y);
+}
+
+template <int NF>
+__global__ void __launch_bounds__(256) k_deposit_f(StepConstF sc, PtrsF p, int ns, int np, int ng) {
+  int is = blockIdx.y;
+  int ip = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ip >= np) return;
+  size_t o = (size_t)is * np + ip;
+  double th = p.theta[o];
+  float a = (float)fma(-rint(th * (1.0 / kTwoPi)), kTwoPi, th);
+  deposit_f<NF>(sc, p, (size_t)is * (size_t)ng * ng, ng, (float)p.current[is],
+                (float)sc.gammaref + p.dg[o], a, p.x[o], p.y[o]);
+}
+
+struct CoefF {
+  const float2 *c, *cbet, *cwet;
+};
+__device__ __forceinline__ float2 lapf(bool hp, bool hn, float2 pv, float2 u, float2 nx) {
+  float2 r;
+  if (!hp) {
+    r.x = nx.x - 2.f * u.x;
+    r.y = nx.y - 2.f * u.y;
+  } else if (!hn) {
+    r.x = pv.x - 2.f * u.x;
+    r.y = pv.y - 2.f * u.y;
+  } else {
+    r.x = nx.x - 2.f * u.x + pv.x;
+    r.y = nx.y - 2.f * u.y + pv.y;
+  }
+  return r;
+}
+
+// ADI implicit in x (FieldSolverADI.cpp:63-75, 94-104), FP32; thread per (slice, row)
+__global__ void __launch_bounds__(128) k_adi_x_f(const float2 *__restrict__ field,
+                                                 const float2 *__restrict__ src,
+                                                 float2 *__restrict__ tmp, CoefF cf, float cstep,
+                                                 int ns, int ng, int first) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)ns * ng) return;
+  int ii = (int)(t / ng), iy = (int)(t % ng);
+  size_t ncell = (size_t)ng * ng;
+  int i = (ii + first) % ns;
+  const float2 *u = field + (size_t)i * ncell + (size_t)iy * ng;
+  const float2 *s = src + (size_t)ii * ncell + (size_t)iy * ng;
+  float2 *w = tmp + (size_t)i * ncell + (size_t)iy * ng;
+  bool hp = iy > 0, hn = iy < ng - 1;
+  float2 prev = make_float2(0.f, 0.f);
+  for (int k = 0; k < ng; k++) {
+    float2 uc = u[k];
+    float2 un = hn ? u[k + ng] : make_float2(0.f, 0.f);
+    float2 us = hp ? u[k - ng] : make_float2(0.f, 0.f);
+    float2 l = lapf(hp, hn, us, uc, un);
+    float2 sv = s[k];
+    float2 r = make_float2(sv.x + uc.x - cstep * l.y, sv.y + uc.y + cstep * l.x);
+    float2 v;
+    if (k == 0) {
+      v = cmulf(r, cf.cbet[0]);
+    } else {
+      float2 cp = cmulf(cf.c[k], prev);
+      v = cmulf(make_float2(r.x - cp.x, r.y - cp.y), cf.cbet[k]);
+    }
+    w[k] = v;
+    prev = v;
+  }
+  float2 next = prev;
+  for (int k = ng - 2; k >= 0; k--) {
+    float2 cw = cmulf(cf.cwet[k + 1], next);
+    float2 v = w[k];
+    v.x -= cw.x;
+    v.y -= cw.y;
+    w[k] = v;
+    next = v;
+  }
+}
+
+// ADI implicit in y (FieldSolverADI.cpp:77-89, 106-122), FP32; thread per (slice, column)
+__global__ void __launch_bounds__(128) k_adi_y_f(float2 *__restrict__ field,
+                                                 const float2 *__restrict__ src,
+                                                 const float2 *__restrict__ tmp, CoefF cf,
+                                                 float cstep, int ns, int ng, int first) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)ns * ng) return;
+  int ii = (int)(t / ng), ix = (int)(t % ng);
+  size_t ncell = (size_t)ng * ng;
+  int i = (ii + first) % ns;
+  float2 *u = field + (size_t)i * ncell + ix;
+  const float2 *s = src + (size_t)ii * ncell + ix;
+  const float2 *w = tmp + (size_t)i * ncell + ix;
+  bool hp = ix > 0, hn = ix < ng - 1;
+  float2 prev = make_float2(0.f, 0.f);
+  for (int k = 0; k < ng; k++) {
+    size_t o = (size_t)k * ng;
+    float2 wc = w[o];
+    float2 wn = hn ? w[o + 1] : make_float2(0.f, 0.f);
+    float2 wp = hp ? w[o - 1] : make_float2(0.f, 0.f);
+    float2 l = lapf(hp, hn, wp, wc, wn);
+    float2 sv = s[o];
+    float2 r = make_float2(sv.x + wc.x - cstep * l.y, sv.y + wc.y + cstep * l.x);
+    float2 v;
+    if (k == 0) {
+      v = cmulf(r, cf.cbet[0]);
+    } else {
+      float2 cp = cmulf(cf.c[k], prev);
+      v = cmulf(make_float2(r.x - cp.x, r.y - cp.y), cf.cbet[k]);
+    }
+    u[o] = v;
+    prev = v;
+  }
+  float2 next = prev;
+  for (int k = ng - 2; k >= 0; k--) {
+    size_t o = (size_t)k * ng;
+    float2 cw = cmulf(cf.cwet[k + 1], next);
+    float2 v = u[o];
+    v.x -= cw.x;
+    v.y -= cw.y;
+    u[o] = v;
+    next = v;
+  }
+}
+
+template <int BS>
+__device__ __forceinline__ double bsum(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < BS / 32; i++) r += sh[i];
+  return r;
+}
+template <int BS, bool MAX>
+__device__ __forceinline__ double bext(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double w = __shfl_down_sync(0xffffffffu, v, o);
+    v = MAX ? fmax(v, w) : fmin(v, w);
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = sh[0];
+  if (threadIdx.x == 0)
+    for (int i = 1; i < BS / 32; i++) r = MAX ? fmax(r, sh[i]) : fmin(r, sh[i]);
+  return r;
+}
+
+// DiagBeam sums with FP64 accumulation (Diagnostic.cpp:415-456); one block per slice
+template <int BS>
+__global__ void __launch_bounds__(BS) k_diag_beam_f(PtrsF p, double gref, int np, int nharm, double *out) {
+  __shared__ double sh[BS / 32];
+  int is = blockIdx.x;
+  size_t base = (size_t)is * np;
+  double s[kBeamSums] = {0};
+  double mn[5] = {1e5, 1e5, 1e5, 1e5, 1e7}, mx[5] = {-1e5, -1e5, -1e5, -1e5, 1};
+  double br[G4GPU_MAX_HARM], bi[G4GPU_MAX_HARM];
+  for (int h = 0; h < G4GPU_MAX_HARM; h++) br[h] = bi[h] = 0;
+  for (int ip = threadIdx.x; ip < np; ip += BS) {
+    double x = p.x[base + ip], y = p.y[base + ip], g = gref + (double)p.dg[base + ip];
+    double px = p.px[base + ip], py = p.py[base + ip], th = p.theta[base + ip];
+    s[0] += g; s[1] += g * g; s[2] += x; s[3] += x * x; s[4] += y; s[5] += y * y;
+    s[6] += px; s[7] += px * px; s[8] += py; s[9] += py * py; s[10] += x * px; s[11] += y * py;
+    mn[0] = fmin(mn[0], x); mx[0] = fmax(mx[0], x);
+    mn[1] = fmin(mn[1], px); mx[1] = fmax(mx[1], px);
+    mn[2] = fmin(mn[2], y); mx[2] = fmax(mx[2], y);
+    mn[3] = fmin(mn[3], py); mx[3] = fmax(mx[3], py);
+    mn[4] = fmin(mn[4], g); mx[4] = fmax(mx[4], g);
+    for (int h = 0; h < nharm && h < G4GPU_MAX_HARM; h++) {
+      double sn, cs;
+      sincos((h + 1) * th, &sn, &cs);
+      br[h] += cs;
+      bi[h] += sn;
+    }
+  }
+  int w = beam_diag_width(nharm);
+  double *o = out + (size_t)is * w;
+  for (int k = 0; k < kBeamSums; k++) {
+    double r = bsum<BS>(s[k], sh);
+    if (threadIdx.x == 0) o[k] = r;
+  }
+  for (int k = 0; k < 5; k++) {
+    double a = bext<BS, false>(mn[k], sh);
+    if (threadIdx.x == 0) o[kBeamSums + 2 * k] = a;
+    double b = bext<BS, true>(mx[k], sh);
+    if (threadIdx.x == 0) o[kBeamSums + 2 * k + 1] = b;
+  }
+  for (int h = 0; h < nharm && h < G4GPU_MAX_HARM; h++) {
+    double a = bsum<BS>(br[h], sh);
+    double b = bsum<BS>(bi[h], sh);
+    if (threadIdx.x == 0) {
+      o[kBeamSums + kBeamMinMax + 2 * h] = a;
+      o[kBeamSums + kBeamMinMax + 2 * h + 1] = b;
+    }
+  }
+}
+
+template <int BS>
+__global__ void __launch_bounds__(BS) k_diag_field_f(const float2 *field, int ng, double *out) {
+  __shared__ double sh[BS / 32];
+  int is0 = blockIdx.x;
+  size_t ncell = (size_t)ng * ng;
+  const float2 *f = field + (size_t)is0 * ncell;
+  double shift = -0.5 * (double)(ng - 1);
+  double s[7] = {0};
+  for (size_t i = threadIdx.x; i < ncell; i += BS) {
+    int iy = (int)(i / ng), ix = (int)(i % ng);
+    double dx = (double)ix + shift, dy = (double)iy + shift;
+    float2 v = f[i];
+    double wei = (double)v.x * v.x + (double)v.y * v.y;
+    s[0] += wei; s[1] += dx * wei; s[2] += dx * dx * wei; s[3] += dy * wei; s[4] += dy * dy * wei;
+    s[5] += v.x; s[6] += v.y;
+  }
+  double *o = out + (size_t)is0 * (kFieldSums + 2);
+  for (int k = 0; k < 7; k++) {
+    double r = bsum<BS>(s[k], sh);
+    if (threadIdx.x == 0) o[k] = r;
+  }
+  if (threadIdx.x == 0) {
+    float2 v = f[(size_t)(ng / 2) * ng + ng / 2];
+    o[7] = v.x;
+    o[8] = v.y;
+  }
+}
+
+PtrsF make_ptrs_f(const DeviceBeam &b, void *const *field, void *const *src, int nfld) {
+  PtrsF p{};
+  p.dg = (float *)b.gamma;
+  p.theta = (double *)b.theta;
+  p.x = (float *)b.x;
+  p.y = (float *)b.y;
+  p.px = (float *)b.px;
+  p.py = (float *)b.py;
+  p.current = b.current;
+  for (int k = 0; k < nfld && k < G4GPU_MAX_FIELDS; k++) {
+    p.field[k] = field ? (const float2 *)field[k] : nullptr;
+    p.src[k] = src ? (float2 *)src[k] : nullptr;
+  }
+  return p;
+}
+
+}  // namespace
+
+void launch_push_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,
+                       void *const *field, void *const *src, int ns, int np, int ngrid,
+                       int deposit) {
+  PtrsF p = make_ptrs_f(b, field, src, sc.nfld);
+  dim3 grid((np + 255) / 256, ns);
+  cudaStream_t s = (cudaStream_t)L.stream;
+  switch (sc.nfld) {
+    case 1: k_push_f<1><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    case 2: k_push_f<2><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    case 3: k_push_f<3><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    default: k_push_f<G4GPU_MAX_FIELDS><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+  }
+}
+
+void launch_deposit_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,
+                          void *const *src, int ns, int np, int ngrid) {
+  PtrsF p = make_ptrs_f(b, nullptr, src, sc.nfld);
+  dim3 grid((np + 255) / 256, ns);
+  cudaStream_t s = (cudaStream_t)L.stream;
+  switch (sc.nfld) {
+    case 1: k_deposit_f<1><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid); break;
+    case 2: k_deposit_f<2><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid); break;
+    case 3: k_deposit_f<3><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid); break;
+    default: k_deposit_f<G4GPU_MAX_FIELDS><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid); break;
+  }
+}
+
+void launch_adi_mixed(const Launch &L, const StepConstF &sc, int k, int phase, void *field,
+                      const void *src, void *tmp, const void *coef, int ns, int ngrid) {
+  const float2 *cb = (const float2 *)coef;
+  CoefF cf{cb, cb + ngrid, cb + 2 * ngrid};
+  long long n = (long long)ns * ngrid;
+  unsigned blocks = (unsigned)((n + 127) / 128);
+  cudaStream_t s = (cudaStream_t)L.stream;
+  if (phase == 0)
+    k_adi_x_f<<<blocks, 128, 0, s>>>((const float2 *)field, (const float2 *)src, (float2 *)tmp, cf,
+                                     sc.f[k].cstep, ns, ngrid, sc.f[k].first);
+  else
+    k_adi_y_f<<<blocks, 128, 0, s>>>((float2 *)field, (const float2 *)src, (const float2 *)tmp, cf,
+                                     sc.f[k].cstep, ns, ngrid, sc.f[k].first);
+}
+
+void launch_diag_beam_mixed(const Launch &L, const DeviceBeam &b, double gammaref, int ns, int np,
+                            int nharm, double *out) {
+  PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
+  k_diag_beam_f<256><<<ns, 256, 0, (cudaStream_t)L.stream>>>(p, gammaref, np, nharm, out);
+}
+
+void launch_diag_field_mixed(const Launch &L, const void *field, int ns, int ngrid, double *out) {
+  k_diag_field_f<256><<<ns, 256, 0, (cudaStream_t)L.stream>>>((const float2 *)field, ngrid, out);
+}
+
+}  // namespace g4

@@ -1,0 +1,527 @@
+// FP64 kernels of the undulator step with the reference's arithmetic.
+//
+// This translation unit is compiled with --fmad=false so that every product and
+// sum rounds separately, as the reference's x86-64 build does; together with the
+// IEEE-rounded division and square root of CUDA, only the transcendental
+// functions (sin, cos, sinh, cosh of the CUDA math library) differ in the last
+// bits from the reference. Operation order follows the cited reference lines.
+//
+// Layout: particles are structure-of-arrays, slice-major (index is*np + ip);
+// fields are [nslice][ngrid*ngrid] double2, storage order with the ring start
+// `first`; the deposited source is [nslice][ngrid*ngrid] double2 indexed by
+// beam slice.
+#include <cuda_runtime.h>
+
+#include "g4gpu_internal.h"
+
+namespace g4 {
+namespace {
+
+struct C2 {
+  double x, y;
+};
+__device__ __forceinline__ C2 ld(const double2 *p) {
+  double2 v = *p;
+  return {v.x, v.y};
+}
+__device__ __forceinline__ void st(double2 *p, C2 v) { *p = make_double2(v.x, v.y); }
+__device__ __forceinline__ C2 cadd(C2 a, C2 b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ C2 csub(C2 a, C2 b) { return {a.x - b.x, a.y - b.y}; }
+// std::complex<double> product as GCC evaluates it: (ac - bd, ad + bc)
+__device__ __forceinline__ C2 cmul(C2 a, C2 b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+// real * complex
+__device__ __forceinline__ C2 rmul(double s, C2 a) { return {s * a.x, s * a.y}; }
+// complex * real
+__device__ __forceinline__ C2 mulr(C2 a, double s) { return {a.x * s, a.y * s}; }
+
+// TrackBeam::applyDrift / applyFQuad / applyDQuad (TrackBeam.cpp:84-116)
+__device__ __forceinline__ void plane_step(int kind, double q, double off, double delz, double &x,
+                                           double &p, double gammaz) {
+  if (kind == 0) {
+    x += p * delz / gammaz;
+  } else if (kind == 1) {
+    double foc = sqrt(q / gammaz);
+    double omg = foc * delz;
+    double a1 = cos(omg);
+    double a2 = sin(omg) / foc;
+    double a3 = -a2 * foc * foc;
+    double xtmp = x - off;
+    x = a1 * xtmp + a2 * p / gammaz + off;
+    p = a3 * xtmp * gammaz + a1 * p;
+  } else {
+    double foc = sqrt(-q / gammaz);
+    double omg = foc * delz;
+    double a1 = cosh(omg);
+    double a2 = sinh(omg) / foc;
+    double a3 = a2 * foc * foc;
+    double xtmp = x - off;
+    x = a1 * xtmp + a2 * p / gammaz + off;
+    p = a3 * xtmp * gammaz + a1 * p;
+  }
+}
+
+// TrackBeam::track over half a step (TrackBeam.cpp:66-76); `last` applies the
+// corrector kick first (TrackBeam.cpp:37-38, 118-128).
+__device__ __forceinline__ void transverse(const StepConst &sc, bool last, double g, double &x,
+                                           double &y, double &px, double &py) {
+  if (last && sc.corr) {
+    px += sc.cxk;
+    py += sc.cyk;
+  }
+  double delz = sc.delz * 0.5;
+  double gammaz = sqrt(g * g - 1 - sc.aw_t * sc.aw_t - px * px - py * py);
+  plane_step(sc.kindx, sc.qx, sc.xoff, delz, x, px, gammaz);
+  plane_step(sc.kindy, sc.qy, sc.yoff, delz, y, py, gammaz);
+}
+
+// Field::getLLGridpoint (Field.cpp:160-174). Returns the lower-left cell and the
+// weights. A particle within rounding of the upper edge can land on index
+// ngrid-1, where the reference's right/upper neighbour carries weight exactly 0;
+// the neighbour index is then clamped so that no access leaves the grid.
+struct Cell {
+  int i00, i10, i01, i11;
+  double wx, wy;
+};
+__device__ __forceinline__ bool ll_gridpoint(double gm, double dg, int ng, double x, double y,
+                                             Cell &c) {
+  if ((x > -gm) && (x < gm) && (y > -gm) && (y < gm)) {
+    double wx = (x + gm) / dg;
+    double wy = (y + gm) / dg;
+    double fx = floor(wx), fy = floor(wy);
+    int ix = (int)fx, iy = (int)fy;
+    c.wx = 1 + fx - wx;
+    c.wy = 1 + fy - wy;
+    int ix1 = ix + 1 < ng ? ix + 1 : ix;
+    int iy1 = iy + 1 < ng ? iy + 1 : iy;
+    c.i00 = ix + iy * ng;
+    c.i10 = ix1 + iy * ng;
+    c.i01 = ix + iy1 * ng;
+    c.i11 = ix1 + iy1 * ng;
+    return true;
+  }
+  return false;
+}
+
+// BeamSolver::ODE (BeamSolver.cpp:144-163) for NF fields
+template <int NF>
+__device__ __forceinline__ void ode(const StepConst &sc, const C2 *rpart, double btpar,
+                                    double tgam, double tthet, double &k2gg, double &k2pp) {
+  double ztemp1 = -2. / sc.xks;
+  C2 ctmp = {0, 0};
+#pragma unroll
+  for (int i = 0; i < NF; i++) {
+    if (i >= sc.nfld) break;
+    double s, c;
+    sincos(sc.f[i].rharm * tthet, &s, &c);
+    ctmp = cadd(ctmp, cmul(rpart[i], C2{c, -s}));
+  }
+  double btper0 = btpar + ztemp1 * ctmp.x;
+  double btpar0 = sqrt(1. - btper0 / (tgam * tgam));
+  k2pp += sc.xks * (1. - 1. / btpar0) + sc.xku;
+  k2gg += ctmp.y / btpar0 / tgam;  // the space-charge field ez is zero here
+}
+
+// Deposition of one particle into the source of every field
+// (FieldSolverADI.cpp:19-51; FieldSolverFFT.cpp:19-51 is identical).
+template <int NF>
+__device__ __forceinline__ void deposit_particle(const StepConst &sc, double2 *const *src,
+                                                 size_t slice_off, int ng, double cur,
+                                                 double npd, double g, double th, double x,
+                                                 double y) {
+#pragma unroll
+  for (int k = 0; k < NF; k++) {
+    if (k >= sc.nfld) break;
+    const FieldStep &fs = sc.f[k];
+    if (!fs.dep_on) continue;
+    Cell c;
+    if (!ll_gridpoint(fs.gridmax, fs.dgrid, ng, x, y, c)) continue;
+    double scl = fs.fc * kVacimp * cur * fs.xks * sc.delz;
+    scl /= 4 * kEev * npd * fs.dgrid * fs.dgrid;
+    double dx = x - sc.ax, dy = y - sc.ay;
+    double faw2 = (1 + sc.kx * dx * dx + sc.ky * dy * dy + 2 * (sc.gradx * dx + sc.grady * dy));
+    double part = sqrt(faw2) * scl / g;
+    double s, co;
+    sincos(fs.rharm * th, &s, &co);
+    C2 cpart = mulr(C2{s, co}, part);
+    double2 *d = src[k] + slice_off;
+    double w = c.wx * c.wy;
+    atomicAdd(&d[c.i00].x, w * cpart.x);
+    atomicAdd(&d[c.i00].y, w * cpart.y);
+    w = (1 - c.wx) * c.wy;
+    atomicAdd(&d[c.i10].x, w * cpart.x);
+    atomicAdd(&d[c.i10].y, w * cpart.y);
+    w = c.wx * (1 - c.wy);
+    atomicAdd(&d[c.i01].x, w * cpart.x);
+    atomicAdd(&d[c.i01].y, w * cpart.y);
+    w = (1 - c.wx) * (1 - c.wy);
+    atomicAdd(&d[c.i11].x, w * cpart.x);
+    atomicAdd(&d[c.i11].y, w * cpart.y);
+  }
+}
+
+struct Ptrs {
+  double *gamma, *theta, *x, *y, *px, *py;
+  const double *current;
+  const double2 *field[G4GPU_MAX_FIELDS];
+  double2 *src[G4GPU_MAX_FIELDS];
+};
+
+// Beam::track (Beam.cpp:296-311): half transverse step, BeamSolver::advance with
+// the bilinear field gather and RK4 (BeamSolver.cpp:48-141), half transverse step
+// with the corrector; then, with `deposit`, the source deposition of the
+// following Field::track. One thread per particle; blockIdx.y is the slice.
+template <int NF>
+__global__ void __launch_bounds__(256) k_push(StepConst sc, Ptrs p, int ns, int np, int ng,
+                                              int deposit) {
+  int is = blockIdx.y;
+  int ip = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ip >= np) return;
+  size_t o = (size_t)is * np + ip;
+  double g = p.gamma[o], th = p.theta[o], x = p.x[o], y = p.y[o], px = p.px[o], py = p.py[o];
+  size_t ncell = (size_t)ng * ng;
+
+  transverse(sc, false, g, x, y, px, py);
+
+  // BeamSolver::advance, BeamSolver.cpp:53-80
+  double gamma = g, theta = th + sc.autophase;
+  double dx = x - sc.ax, dy = y - sc.ay;
+  double awloc = (1 + 0.5 * (sc.kx * dx * dx + sc.ky * dy * dy) + sc.gradx * dx + sc.grady * dy);
+  double btpar = 1 + px * px + py * py + sc.aw * sc.aw * awloc * awloc;
+  C2 rpart[NF];
+#pragma unroll
+  for (int k = 0; k < NF; k++) {
+    if (k >= sc.nfld) break;
+    const FieldStep &fs = sc.f[k];
+    int islice = (is + fs.first) % ns;
+    const double2 *f = p.field[k] + (size_t)islice * ncell;
+    Cell c;
+    if (ll_gridpoint(fs.gridmax, fs.dgrid, ng, x, y, c)) {
+      C2 cpart = mulr(mulr(ld(f + c.i00), c.wx), c.wy);
+      cpart = cadd(cpart, mulr(mulr(ld(f + c.i10), 1 - c.wx), c.wy));
+      cpart = cadd(cpart, mulr(mulr(ld(f + c.i01), c.wx), 1 - c.wy));
+      cpart = cadd(cpart, mulr(mulr(ld(f + c.i11), 1 - c.wx), 1 - c.wy));
+      rpart[k] = rmul(fs.rtmp * awloc, C2{cpart.x, -cpart.y});
+    } else {
+      rpart[k] = C2{0, 0};
+    }
+  }
+
+  // BeamSolver::RungeKutta, BeamSolver.cpp:89-141
+  double k2gg = 0, k2pp = 0, k3gg, k3pp;
+  ode<NF>(sc, rpart, btpar, gamma, theta, k2gg, k2pp);
+  double stpz = 0.5 * sc.delz;
+  gamma += stpz * k2gg;
+  theta += stpz * k2pp;
+  k3gg = k2gg;
+  k3pp = k2pp;
+  k2gg = 0;
+  k2pp = 0;
+  ode<NF>(sc, rpart, btpar, gamma, theta, k2gg, k2pp);
+  gamma += stpz * (k2gg - k3gg);
+  theta += stpz * (k2pp - k3pp);
+  k3gg /= 6;
+  k3pp /= 6;
+  k2gg *= -0.5;
+  k2pp *= -0.5;
+  ode<NF>(sc, rpart, btpar, gamma, theta, k2gg, k2pp);
+  stpz = sc.delz;
+  gamma += stpz * k2gg;
+  theta += stpz * k2pp;
+  k3gg -= k2gg;
+  k3pp -= k2pp;
+  k2gg *= 2;
+  k2pp *= 2;
+  ode<NF>(sc, rpart, btpar, gamma, theta, k2gg, k2pp);
+  gamma += stpz * (k3gg + k2gg / 6.0);
+  theta += stpz * (k3pp + k2pp / 6.0);
+
+  transverse(sc, true, gamma, x, y, px, py);
+
+  p.gamma[o] = gamma;
+  p.theta[o] = theta;
+  p.x[o] = x;
+  p.y[o] = y;
+  p.px[o] = px;
+  p.py[o] = py;
+
+  if (deposit)
+    deposit_particle<NF>(sc, p.src, (size_t)is * ncell, ng, p.current[is], (double)np, gamma,
+                         theta, x, y);
+}
+
+// Deposition alone, for a Field::track without a preceding push.
+template <int NF>
+__global__ void __launch_bounds__(256) k_deposit(StepConst sc, Ptrs p, int ns, int np, int ng) {
+  int is = blockIdx.y;
+  int ip = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ip >= np) return;
+  size_t o = (size_t)is * np + ip;
+  size_t ncell = (size_t)ng * ng;
+  deposit_particle<NF>(sc, p.src, (size_t)is * ncell, ng, p.current[is], (double)np, p.gamma[o],
+                       p.theta[o], p.x[o], p.y[o]);
+}
+
+// ADI coefficient set: c[ng], cbet[ng], cwet[ng] (FieldSolverADI.cpp:125-182)
+struct Coef {
+  const double2 *c, *cbet, *cwet;
+};
+
+// Right-hand side term cstep * (second difference) with the reference's operand
+// order (FieldSolverADI.cpp:64-86): (next - 2 u) + prev, one-sided at the edges.
+__device__ __forceinline__ C2 lap(bool has_prev, bool has_next, C2 prev, C2 u, C2 next) {
+  if (!has_prev) return csub(next, rmul(2.0, u));
+  if (!has_next) return csub(prev, rmul(2.0, u));
+  return cadd(csub(next, rmul(2.0, u)), prev);
+}
+
+// First ADI half step: implicit along x (tridagx, FieldSolverADI.cpp:63-75, 94-104).
+// One thread per (slice, row); writes the intermediate field to tmp.
+__global__ void __launch_bounds__(128) k_adi_x(const double2 *__restrict__ field,
+                                               const double2 *__restrict__ src,
+                                               double2 *__restrict__ tmp, Coef cf, double cstep,
+                                               int ns, int ng, int first) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)ns * ng) return;
+  int ii = (int)(t / ng), iy = (int)(t % ng);
+  size_t ncell = (size_t)ng * ng;
+  int i = (ii + first) % ns;
+  const double2 *u = field + (size_t)i * ncell + (size_t)iy * ng;
+  const double2 *s = src + (size_t)ii * ncell + (size_t)iy * ng;
+  double2 *w = tmp + (size_t)i * ncell + (size_t)iy * ng;
+  bool hp = iy > 0, hn = iy < ng - 1;
+  C2 cs = {0.0, cstep};
+  C2 prev = {0, 0};
+  for (int k = 0; k < ng; k++) {
+    C2 uc = ld(u + k);
+    C2 un = hn ? ld(u + k + ng) : C2{0, 0};
+    C2 us = hp ? ld(u + k - ng) : C2{0, 0};
+    C2 r = cadd(cadd(ld(s + k), uc), cmul(cs, lap(hp, hn, us, uc, un)));
+    C2 v = (k == 0) ? cmul(r, ld(cf.cbet)) : cmul(csub(r, cmul(ld(cf.c + k), prev)), ld(cf.cbet + k));
+    st(w + k, v);
+    prev = v;
+  }
+  C2 next = prev;
+  for (int k = ng - 2; k >= 0; k--) {
+    C2 v = csub(ld(w + k), cmul(ld(cf.cwet + k + 1), next));
+    st(w + k, v);
+    next = v;
+  }
+}
+
+// Second ADI half step: implicit along y (tridagy, FieldSolverADI.cpp:77-89, 106-122).
+// One thread per (slice, column); reads tmp, writes the field.
+__global__ void __launch_bounds__(128) k_adi_y(double2 *__restrict__ field,
+                                               const double2 *__restrict__ src,
+                                               const double2 *__restrict__ tmp, Coef cf,
+                                               double cstep, int ns, int ng, int first) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)ns * ng) return;
+  int ii = (int)(t / ng), ix = (int)(t % ng);
+  size_t ncell = (size_t)ng * ng;
+  int i = (ii + first) % ns;
+  double2 *u = field + (size_t)i * ncell + ix;
+  const double2 *s = src + (size_t)ii * ncell + ix;
+  const double2 *w = tmp + (size_t)i * ncell + ix;
+  bool hp = ix > 0, hn = ix < ng - 1;
+  C2 cs = {0.0, cstep};
+  C2 prev = {0, 0};
+  for (int k = 0; k < ng; k++) {
+    size_t o = (size_t)k * ng;
+    C2 wc = ld(w + o);
+    C2 wn = hn ? ld(w + o + 1) : C2{0, 0};
+    C2 wp = hp ? ld(w + o - 1) : C2{0, 0};
+    C2 r = cadd(cadd(ld(s + o), wc), cmul(cs, lap(hp, hn, wp, wc, wn)));
+    C2 v = (k == 0) ? cmul(r, ld(cf.cbet)) : cmul(csub(r, cmul(ld(cf.c + k), prev)), ld(cf.cbet + k));
+    st(u + o, v);
+    prev = v;
+  }
+  C2 next = prev;
+  for (int k = ng - 2; k >= 0; k--) {
+    size_t o = (size_t)k * ng;
+    C2 v = csub(ld(u + o), cmul(ld(cf.cwet + k + 1), next));
+    st(u + o, v);
+    next = v;
+  }
+}
+
+// ---- diagnostics: per-slice FP64 sums, finished on the host -----------------
+template <int BS>
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < BS / 32; i++) r += sh[i];
+  return r;
+}
+template <int BS, bool MAX>
+__device__ __forceinline__ double block_ext(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double w = __shfl_down_sync(0xffffffffu, v, o);
+    v = MAX ? fmax(v, w) : fmin(v, w);
+  }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = sh[0];
+  if (threadIdx.x == 0)
+    for (int i = 1; i < BS / 32; i++) r = MAX ? fmax(r, sh[i]) : fmin(r, sh[i]);
+  return r;
+}
+
+// DiagBeam::getValues sums (Diagnostic.cpp:415-456): one block per slice.
+template <int BS>
+__global__ void __launch_bounds__(BS) k_diag_beam(Ptrs p, int np, int nharm, double *out) {
+  __shared__ double sh[BS / 32];
+  int is = blockIdx.x;
+  size_t base = (size_t)is * np;
+  double s[kBeamSums] = {0};
+  double mn[5] = {1e5, 1e5, 1e5, 1e5, 1e7}, mx[5] = {-1e5, -1e5, -1e5, -1e5, 1};
+  double br[G4GPU_MAX_HARM], bi[G4GPU_MAX_HARM];
+  for (int h = 0; h < G4GPU_MAX_HARM; h++) br[h] = bi[h] = 0;
+  for (int ip = threadIdx.x; ip < np; ip += BS) {
+    double x = p.x[base + ip], y = p.y[base + ip], g = p.gamma[base + ip];
+    double px = p.px[base + ip], py = p.py[base + ip], th = p.theta[base + ip];
+    s[0] += g; s[1] += g * g; s[2] += x; s[3] += x * x; s[4] += y; s[5] += y * y;
+    s[6] += px; s[7] += px * px; s[8] += py; s[9] += py * py; s[10] += x * px; s[11] += y * py;
+    mn[0] = fmin(mn[0], x); mx[0] = fmax(mx[0], x);
+    mn[1] = fmin(mn[1], px); mx[1] = fmax(mx[1], px);
+    mn[2] = fmin(mn[2], y); mx[2] = fmax(mx[2], y);
+    mn[3] = fmin(mn[3], py); mx[3] = fmax(mx[3], py);
+    mn[4] = fmin(mn[4], g); mx[4] = fmax(mx[4], g);
+    for (int h = 0; h < nharm && h < G4GPU_MAX_HARM; h++) {
+      double sn, cs;
+      sincos((h + 1) * th, &sn, &cs);
+      br[h] += cs;
+      bi[h] += sn;
+    }
+  }
+  int w = beam_diag_width(nharm);
+  double *o = out + (size_t)is * w;
+  for (int k = 0; k < kBeamSums; k++) {
+    double r = block_sum<BS>(s[k], sh);
+    if (threadIdx.x == 0) o[k] = r;
+  }
+  for (int k = 0; k < 5; k++) {
+    double a = block_ext<BS, false>(mn[k], sh);
+    if (threadIdx.x == 0) o[kBeamSums + 2 * k] = a;
+    double b = block_ext<BS, true>(mx[k], sh);
+    if (threadIdx.x == 0) o[kBeamSums + 2 * k + 1] = b;
+  }
+  for (int h = 0; h < nharm && h < G4GPU_MAX_HARM; h++) {
+    double a = block_sum<BS>(br[h], sh);
+    double b = block_sum<BS>(bi[h], sh);
+    if (threadIdx.x == 0) {
+      o[kBeamSums + kBeamMinMax + 2 * h] = a;
+      o[kBeamSums + kBeamMinMax + 2 * h + 1] = b;
+    }
+  }
+}
+
+// DiagField::getValues sums (Diagnostic.cpp:754-776): one block per storage slot.
+template <int BS>
+__global__ void __launch_bounds__(BS) k_diag_field(const double2 *field, int ng, double *out) {
+  __shared__ double sh[BS / 32];
+  int is0 = blockIdx.x;
+  size_t ncell = (size_t)ng * ng;
+  const double2 *f = field + (size_t)is0 * ncell;
+  double shift = -0.5 * (double)(ng - 1);
+  double s[7] = {0};
+  for (size_t i = threadIdx.x; i < ncell; i += BS) {
+    int iy = (int)(i / ng), ix = (int)(i % ng);
+    double dx = (double)ix + shift, dy = (double)iy + shift;
+    double2 v = f[i];
+    double wei = v.x * v.x + v.y * v.y;
+    s[0] += wei; s[1] += dx * wei; s[2] += dx * dx * wei; s[3] += dy * wei; s[4] += dy * dy * wei;
+    s[5] += v.x; s[6] += v.y;
+  }
+  double *o = out + (size_t)is0 * (kFieldSums + 2);
+  for (int k = 0; k < 7; k++) {
+    double r = block_sum<BS>(s[k], sh);
+    if (threadIdx.x == 0) o[k] = r;
+  }
+  if (threadIdx.x == 0) {
+    double2 v = f[(size_t)(ng / 2) * ng + ng / 2];
+    o[7] = v.x;
+    o[8] = v.y;
+  }
+}
+
+Ptrs make_ptrs(const DeviceBeam &b, void *const *field, void *const *src, int nfld) {
+  Ptrs p{};
+  p.gamma = (double *)b.gamma;
+  p.theta = (double *)b.theta;
+  p.x = (double *)b.x;
+  p.y = (double *)b.y;
+  p.px = (double *)b.px;
+  p.py = (double *)b.py;
+  p.current = b.current;
+  for (int k = 0; k < nfld && k < G4GPU_MAX_FIELDS; k++) {
+    p.field[k] = field ? (const double2 *)field[k] : nullptr;
+    p.src[k] = src ? (double2 *)src[k] : nullptr;
+  }
+  return p;
+}
+
+}  // namespace
+
+void launch_push_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,
+                       void *const *field, void *const *src, int ns, int np, int ngrid,
+                       int deposit) {
+  Ptrs p = make_ptrs(b, field, src, sc.nfld);
+  dim3 grid((np + 255) / 256, ns);
+  cudaStream_t s = (cudaStream_t)L.stream;
+  switch (sc.nfld) {
+    case 1: k_push<1><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    case 2: k_push<2><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    case 3: k_push<3><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    default: k_push<G4GPU_MAX_FIELDS><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+  }
+}
+
+void launch_deposit_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,
+                          void *const *src, int ns, int np, int ngrid) {
+  Ptrs p = make_ptrs(b, nullptr, src, sc.nfld);
+  dim3 grid((np + 255) / 256, ns);
+  cudaStream_t s = (cudaStream_t)L.stream;
+  switch (sc.nfld) {
+    case 1: k_deposit<1><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid); break;
+    case 2: k_deposit<2><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid); break;
+    case 3: k_deposit<3><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid); break;
+    default: k_deposit<G4GPU_MAX_FIELDS><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid); break;
+  }
+}
+
+void launch_adi_plain(const Launch &L, const StepConst &sc, int k, int phase, void *field,
+                      const void *src, void *tmp, const void *coef, int ns, int ngrid) {
+  const double2 *cb = (const double2 *)coef;
+  Coef cf{cb, cb + ngrid, cb + 2 * ngrid};
+  long long n = (long long)ns * ngrid;
+  unsigned blocks = (unsigned)((n + 127) / 128);
+  cudaStream_t s = (cudaStream_t)L.stream;
+  if (phase == 0)
+    k_adi_x<<<blocks, 128, 0, s>>>((const double2 *)field, (const double2 *)src, (double2 *)tmp,
+                                   cf, sc.f[k].cstep, ns, ngrid, sc.f[k].first);
+  else
+    k_adi_y<<<blocks, 128, 0, s>>>((double2 *)field, (const double2 *)src, (const double2 *)tmp,
+                                   cf, sc.f[k].cstep, ns, ngrid, sc.f[k].first);
+}
+
+void launch_diag_beam_plain(const Launch &L, const DeviceBeam &b, int ns, int np, int nharm,
+                            double *out) {
+  Ptrs p = make_ptrs(b, nullptr, nullptr, 0);
+  k_diag_beam<256><<<ns, 256, 0, (cudaStream_t)L.stream>>>(p, np, nharm, out);
+}
+
+void launch_diag_field_plain(const Launch &L, const void *field, int ns, int ngrid,
+                             double *out) {
+  k_diag_field<256><<<ns, 256, 0, (cudaStream_t)L.stream>>>((const double2 *)field, ngrid, out);
+}
+
+}  // namespace g4

@@ -1,0 +1,295 @@
+"""Python binding of the GB300 engine's C ABI (include/g4gpu.h) via ctypes.
+
+This module is a thin wrapper: every call goes to lib/libg4gpu.so, which runs
+the undulator step as CUDA kernels on the GPU. There is no CPU fallback; if the
+library is missing, load_library() raises.
+
+Usage:
+    import g4gpu
+    cfg = g4gpu.Config(nslice=..., npart=..., ngrid=..., ...)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(table)              # [nsteps][LAT_NCOL]
+        h.load_beam(particles, current)   # [ns][np][6], [ns]
+        h.load_field(0, field, first=0)   # [ns][ngrid*ngrid] complex
+        h.run(0, nsteps)
+        beam_diag, field_diag = h.diag(nharm=1)
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libg4gpu.so")
+
+MAX_FIELDS = 8
+MAX_HARM = 16
+PLAIN, MIXED = 0, 1
+SOLVER_ADI, SOLVER_FFT = 0, 1
+STAGE_PUSH, STAGE_FIELD, STAGE_SLIP, STAGE_ALL = 1, 2, 4, 7
+
+LAT_COLS = ["aw", "ax", "ay", "ku", "kx", "ky", "gradx", "grady", "qf", "qx", "qy",
+            "cx", "cy", "dz", "slip", "phase", "helical", "z"]
+LAT_NCOL = len(LAT_COLS)
+DB_COLS = ["energy", "energyspread", "xposition", "xsize", "yposition", "ysize",
+           "pxposition", "pyposition", "emitx", "emity", "betax", "betay", "alphax",
+           "alphay", "xmin", "xmax", "pxmin", "pxmax", "ymin", "ymax", "pymin", "pymax",
+           "emin", "emax"]
+DF_COLS = ["power", "xposition", "xsize", "yposition", "ysize", "intensity-nearfield",
+           "phase-nearfield", "intensity-farfield", "phase-farfield"]
+KERNEL_CLASSES = ["push", "adi_x", "adi_y", "fft", "slip", "diag", "misc"]
+
+# exported symbols of include/g4gpu.h
+ABI_SYMBOLS = [
+    "g4gpu_config_defaults", "g4gpu_create", "g4gpu_destroy", "g4gpu_last_error",
+    "g4gpu_set_lattice", "g4gpu_load_beam", "g4gpu_get_beam", "g4gpu_load_field",
+    "g4gpu_get_field", "g4gpu_run", "g4gpu_synchronize", "g4gpu_diag", "g4gpu_get_stream",
+    "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
+    "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc",
+]
+
+
+class G4Error(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"g4gpu error {code}: {msg}")
+        self.code = code
+
+
+class Config(ctypes.Structure):
+    _fields_ = [
+        ("nslice", ctypes.c_int), ("npart", ctypes.c_int), ("ngrid", ctypes.c_int),
+        ("nfield", ctypes.c_int), ("harm", ctypes.c_int * MAX_FIELDS),
+        ("gridmax", ctypes.c_double * MAX_FIELDS), ("lambda0", ctypes.c_double),
+        ("sample", ctypes.c_double), ("gammaref", ctypes.c_double),
+        ("precision", ctypes.c_int), ("solver", ctypes.c_int), ("source_filter", ctypes.c_int),
+        ("xcut", ctypes.c_double), ("ycut", ctypes.c_double), ("sigmoid", ctypes.c_double),
+        ("time_run", ctypes.c_int), ("periodic", ctypes.c_int), ("device", ctypes.c_int),
+    ]
+
+    def __init__(self, **kw):
+        super().__init__()
+        _lib().g4gpu_config_defaults(ctypes.byref(self))
+        harm = kw.pop("harm", None)
+        gridmax = kw.pop("gridmax", None)
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise TypeError(f"unknown config field {k}")
+            setattr(self, k, v)
+        if harm is not None:
+            harm = list(np.atleast_1d(harm))
+            self.nfield = len(harm)
+            for i, h in enumerate(harm):
+                self.harm[i] = int(h)
+        if gridmax is not None:
+            gm = list(np.atleast_1d(gridmax))
+            if len(gm) == 1 and self.nfield > 1:
+                gm = gm * self.nfield
+            for i, g in enumerate(gm):
+                self.gridmax[i] = float(g)
+
+
+_LIB = None
+
+
+def load_library(path=None):
+    """Loads lib/libg4gpu.so; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError(f"{p} is missing: build it with genesis-1.3-version4_gb300/build.py")
+    L = ctypes.CDLL(p)
+    P = ctypes.POINTER
+    d, i, vp, pd = ctypes.c_double, ctypes.c_int, ctypes.c_void_p, P(ctypes.c_double)
+    L.g4gpu_config_defaults.argtypes = [P(Config)]
+    L.g4gpu_config_defaults.restype = None
+    L.g4gpu_create.argtypes = [P(Config), P(vp)]
+    L.g4gpu_destroy.argtypes = [vp]
+    L.g4gpu_destroy.restype = None
+    L.g4gpu_last_error.argtypes = [vp]
+    L.g4gpu_last_error.restype = ctypes.c_char_p
+    L.g4gpu_set_lattice.argtypes = [vp, i, pd]
+    L.g4gpu_load_beam.argtypes = [vp, vp, vp]
+    L.g4gpu_get_beam.argtypes = [vp, vp]
+    L.g4gpu_load_field.argtypes = [vp, i, vp, i, d]
+    L.g4gpu_get_field.argtypes = [vp, i, vp, P(i), pd]
+    L.g4gpu_run.argtypes = [vp, i, i, i]
+    L.g4gpu_synchronize.argtypes = [vp]
+    L.g4gpu_diag.argtypes = [vp, i, vp, vp]
+    L.g4gpu_get_stream.argtypes = [vp, P(vp)]
+    L.g4gpu_set_profiling.argtypes = [vp, i]
+    L.g4gpu_kernel_stats.argtypes = [vp, P(ctypes.c_longlong), pd]
+    L.g4gpu_reset_stats.argtypes = [vp]
+    L.g4gpu_device_bytes.argtypes = [vp]
+    L.g4gpu_device_bytes.restype = ctypes.c_size_t
+    L.g4gpu_host_load_beam.argtypes = [i, i, i, i, i, i, d, d, pd, pd]
+    L.g4gpu_host_gauss_hermite.argtypes = [pd, d, i, pd]
+    L.g4gpu_host_fc.argtypes = [d, i, i]
+    L.g4gpu_host_fc.restype = d
+    for name in ABI_SYMBOLS:
+        if not hasattr(L, name):
+            raise ImportError(f"{p} does not export {name}")
+    _LIB = L
+    return L
+
+
+def _lib():
+    return load_library()
+
+
+def _pd(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _vp(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def host_load_beam(slicepar, islice0, npart, nbins, seed, shotnoise, lambda0, sample, out=None):
+    """Quiet loading + shot noise on the host, bit-exact with the reference.
+    `out` may be a preallocated C-contiguous float64 array [ns][npart][6]."""
+    sp = np.ascontiguousarray(slicepar, dtype=np.float64).reshape(-1, 17)
+    if out is None:
+        out = np.zeros((sp.shape[0], npart, 6))
+    elif out.shape != (sp.shape[0], npart, 6) or out.dtype != np.float64 or not out.flags.c_contiguous:
+        raise ValueError("out must be a C-contiguous float64 array [ns][npart][6]")
+    rc = _lib().g4gpu_host_load_beam(sp.shape[0], islice0, npart, nbins, seed, int(shotnoise),
+                                     lambda0, sample, _pd(sp), _pd(out))
+    if rc:
+        raise G4Error(rc, "host_load_beam: invalid arguments")
+    return out
+
+
+def host_gauss_hermite(par, gridmax, ngrid):
+    par = np.ascontiguousarray(par, dtype=np.float64)
+    out = np.zeros((ngrid * ngrid, 2))
+    rc = _lib().g4gpu_host_gauss_hermite(_pd(par), gridmax, ngrid, _pd(out))
+    if rc:
+        raise G4Error(rc, "host_gauss_hermite: invalid arguments")
+    return out[:, 0] + 1j * out[:, 1]
+
+
+def host_fc(aw, helical, h):
+    return _lib().g4gpu_host_fc(aw, int(helical), h)
+
+
+class Handle:
+    """One time window resident on the GPU (g4gpu_handle)."""
+
+    def __init__(self, cfg):
+        self.L = _lib()
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        rc = self.L.g4gpu_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc:
+            raise G4Error(rc, self.L.g4gpu_last_error(None).decode())
+        self.h = h
+
+    def _check(self, rc):
+        if rc:
+            raise G4Error(rc, self.L.g4gpu_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.g4gpu_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def ncell(self):
+        return self.cfg.ngrid * self.cfg.ngrid
+
+    def set_lattice(self, table):
+        t = np.ascontiguousarray(table, dtype=np.float64).reshape(-1, LAT_NCOL)
+        self._check(self.L.g4gpu_set_lattice(self.h, t.shape[0], _pd(t)))
+        self.nsteps = t.shape[0]
+
+    def load_beam(self, particles, current):
+        """particles: host array [ns][np][6] (any memory, pinned is fastest)."""
+        p = particles if (isinstance(particles, np.ndarray) and particles.flags.c_contiguous and
+                          particles.dtype == np.float64) else np.ascontiguousarray(particles, np.float64)
+        c = np.ascontiguousarray(current, dtype=np.float64)
+        if p.size != self.cfg.nslice * self.cfg.npart * 6 or c.size != self.cfg.nslice:
+            raise ValueError("particle or current array has the wrong size")
+        self._check(self.L.g4gpu_load_beam(self.h, _vp(p), _vp(c)))
+
+    def load_beam_ptr(self, particles_ptr, current_ptr):
+        """Same as load_beam with raw host pointers (e.g. pinned torch tensors)."""
+        self._check(self.L.g4gpu_load_beam(self.h, ctypes.c_void_p(particles_ptr),
+                                           ctypes.c_void_p(current_ptr)))
+
+    def get_beam(self, out=None):
+        if out is None:
+            out = np.empty((self.cfg.nslice, self.cfg.npart, 6))
+        self._check(self.L.g4gpu_get_beam(self.h, _vp(out)))
+        return out
+
+    def load_field(self, ifld, field, first=0, accuslip=0.0):
+        f = np.ascontiguousarray(field, dtype=np.complex128)
+        if f.size != self.cfg.nslice * self.ncell:
+            raise ValueError("field array has the wrong size")
+        self._check(self.L.g4gpu_load_field(self.h, ifld, _vp(f), int(first), float(accuslip)))
+
+    def load_field_ptr(self, ifld, ptr, first=0, accuslip=0.0):
+        self._check(self.L.g4gpu_load_field(self.h, ifld, ctypes.c_void_p(ptr), int(first), float(accuslip)))
+
+    def get_field(self, ifld, out=None):
+        if out is None:
+            out = np.empty((self.cfg.nslice, self.ncell), dtype=np.complex128)
+        first = ctypes.c_int()
+        acc = ctypes.c_double()
+        self._check(self.L.g4gpu_get_field(self.h, ifld, _vp(out), ctypes.byref(first), ctypes.byref(acc)))
+        return out, first.value, acc.value
+
+    def slippage_state(self, ifld):
+        first = ctypes.c_int()
+        acc = ctypes.c_double()
+        self._check(self.L.g4gpu_get_field(self.h, ifld, None, ctypes.byref(first), ctypes.byref(acc)))
+        return first.value, acc.value
+
+    def run(self, istep0, nsteps, stages=STAGE_ALL):
+        self._check(self.L.g4gpu_run(self.h, istep0, nsteps, stages))
+
+    def synchronize(self):
+        self._check(self.L.g4gpu_synchronize(self.h))
+
+    def diag(self, nharm=1, beam=True, field=True):
+        ns = self.cfg.nslice
+        b = np.zeros((ns, len(DB_COLS) + 2 * nharm)) if beam else None
+        f = np.zeros((self.cfg.nfield, ns, len(DF_COLS))) if field else None
+        self._check(self.L.g4gpu_diag(self.h, nharm, _vp(b) if beam else None,
+                                      _vp(f) if field else None))
+        return b, f
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        self._check(self.L.g4gpu_get_stream(self.h, ctypes.byref(s)))
+        return s.value
+
+    def set_profiling(self, on):
+        self._check(self.L.g4gpu_set_profiling(self.h, int(on)))
+
+    def kernel_stats(self):
+        n = len(KERNEL_CLASSES)
+        la = (ctypes.c_longlong * n)()
+        ms = (ctypes.c_double * n)()
+        self._check(self.L.g4gpu_kernel_stats(self.h, la, ms))
+        return {k: (int(la[i]), float(ms[i])) for i, k in enumerate(KERNEL_CLASSES)}
+
+    def reset_stats(self):
+        self._check(self.L.g4gpu_reset_stats(self.h))
+
+    def device_bytes(self):
+        return int(self.L.g4gpu_device_bytes(self.h))

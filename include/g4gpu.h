@@ -1,0 +1,195 @@
+/* g4gpu.h — C ABI of the GB300 engine for the GENESIS 1.3 v4 undulator step.
+ *
+ * One handle owns one time window (or, with the batch entry points, an ensemble of
+ * independent runs) resident in GPU memory: particles in structure-of-arrays form,
+ * the complex radiation field of every harmonic, and the per-step lattice tables.
+ * Every call returns 0 on success or a G4GPU_ERR_* code; g4gpu_last_error() gives
+ * the message. No call traps the device: kernels that detect an inconsistency
+ * (an index outside the grid) set a device flag that the next synchronising call
+ * reports as G4GPU_ERR_DEVICE.
+ *
+ * What each entry point replaces in the reference (GENESIS 1.3 v4.6.14, paths
+ * within svenreiche/Genesis-1.3-Version4) is cited beside it. The integration step
+ * g4gpu_run() replaces the body of the step loop in src/Core/Gencore.cpp:102-147:
+ * Beam::track (src/Core/Beam.cpp:296-311), Field::track for every field
+ * (src/Core/Field.cpp:177-185 → FieldSolver::advance, include/FieldSolver.h:20-26)
+ * and Control::applySlippage (src/Core/Control.cpp:158-276).
+ *
+ * Array conventions:
+ *   particles  [nslice][npart][6] doubles (gamma, theta, x, y, px, py) — the
+ *              reference's Particle record (include/Particle.h:6-13) per slice
+ *   current    [nslice] doubles, Beam::current (include/Beam.h)
+ *   field      [nslice][ngrid*ngrid][2] doubles (re, im) in storage order; window
+ *              slice j sits in storage slot (j + first) % nslice (include/Field.h:57-59)
+ *   lattice    [nsteps][G4GPU_LAT_NCOL] doubles, one row per integration step, the
+ *              per-step vectors of the reference's Undulator (include/Undulator.h:58-62)
+ */
+#ifndef G4GPU_H
+#define G4GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define G4GPU_ABI_VERSION 1
+#define G4GPU_MAX_FIELDS 8
+#define G4GPU_MAX_HARM 16
+
+/* status codes */
+#define G4GPU_OK 0
+#define G4GPU_ERR_ARG 1     /* invalid argument or configuration */
+#define G4GPU_ERR_CUDA 2    /* a CUDA runtime call failed */
+#define G4GPU_ERR_STATE 3   /* call out of order (e.g. run before load) */
+#define G4GPU_ERR_DEVICE 4  /* a kernel raised the device error flag */
+#define G4GPU_ERR_NOMEM 5   /* device allocation failed */
+
+/* arithmetic of the step */
+#define G4GPU_PLAIN 0 /* FP64 everywhere, the reference's arithmetic */
+#define G4GPU_MIXED 1 /* FP32 field, solver, deposition and transverse optics; FP64
+                         accumulated phase and FP64 diagnostic reductions */
+
+/* field solver (Field::initSolver, src/Core/Field.cpp:72-83) */
+#define G4GPU_SOLVER_ADI 0 /* FieldSolverADI, src/Core/FieldSolverADI.cpp */
+#define G4GPU_SOLVER_FFT 1 /* FieldSolverFFT, src/Core/FieldSolverFFT.cpp */
+
+/* stage bits for g4gpu_run */
+#define G4GPU_STAGE_PUSH 1  /* Beam::track */
+#define G4GPU_STAGE_FIELD 2 /* Field::track of every field */
+#define G4GPU_STAGE_SLIP 4  /* Control::applySlippage of every field */
+#define G4GPU_STAGE_ALL 7
+
+/* lattice table columns: Undulator per-step vectors (include/Undulator.h:58-62);
+ * the column set and order are also those of oracle/g4oracle.h */
+enum {
+  G4GPU_LAT_AW, G4GPU_LAT_AX, G4GPU_LAT_AY, G4GPU_LAT_KU, G4GPU_LAT_KX, G4GPU_LAT_KY,
+  G4GPU_LAT_GRADX, G4GPU_LAT_GRADY, G4GPU_LAT_QF, G4GPU_LAT_QX, G4GPU_LAT_QY,
+  G4GPU_LAT_CX, G4GPU_LAT_CY, G4GPU_LAT_DZ, G4GPU_LAT_SLIP, G4GPU_LAT_PHASE,
+  G4GPU_LAT_HELICAL, G4GPU_LAT_Z, G4GPU_LAT_NCOL
+};
+
+/* per-slice beam diagnostic columns (DiagBeam::getValues, src/Core/Diagnostic.cpp:373-563);
+ * g4gpu_diag writes these, then |b_h| and arg(b_h) for h = 1..nharm */
+enum {
+  G4GPU_DB_ENERGY, G4GPU_DB_ENERGYSPREAD, G4GPU_DB_XPOS, G4GPU_DB_XSIZE, G4GPU_DB_YPOS,
+  G4GPU_DB_YSIZE, G4GPU_DB_PXPOS, G4GPU_DB_PYPOS, G4GPU_DB_EMITX, G4GPU_DB_EMITY,
+  G4GPU_DB_BETAX, G4GPU_DB_BETAY, G4GPU_DB_ALPHAX, G4GPU_DB_ALPHAY, G4GPU_DB_XMIN,
+  G4GPU_DB_XMAX, G4GPU_DB_PXMIN, G4GPU_DB_PXMAX, G4GPU_DB_YMIN, G4GPU_DB_YMAX,
+  G4GPU_DB_PYMIN, G4GPU_DB_PYMAX, G4GPU_DB_EMIN, G4GPU_DB_EMAX, G4GPU_DB_NCOL
+};
+/* per-slice field diagnostic columns (DiagField::getValues, src/Core/Diagnostic.cpp:718-902),
+ * indexed by window slice */
+enum {
+  G4GPU_DF_POWER, G4GPU_DF_XPOS, G4GPU_DF_XSIZE, G4GPU_DF_YPOS, G4GPU_DF_YSIZE,
+  G4GPU_DF_NF_INT, G4GPU_DF_NF_PHI, G4GPU_DF_FF_INT, G4GPU_DF_FF_PHI, G4GPU_DF_NCOL
+};
+
+typedef struct {
+  int nslice;    /* slices in the time window (Time::getNodeNSlice, src/Main/GenTime.cpp:64-86) */
+  int npart;     /* macro particles per slice (&setup npart) */
+  int ngrid;     /* transverse grid points per dimension (&field ngrid), >= 3 */
+  int nfield;    /* number of radiation fields (harmonics), 1..G4GPU_MAX_FIELDS */
+  int harm[G4GPU_MAX_FIELDS];       /* harmonic of each field (Field::harm) */
+  double gridmax[G4GPU_MAX_FIELDS]; /* half width of each grid (&field dgrid, Field::gridmax) */
+  double lambda0;  /* reference wavelength (&setup lambda0) */
+  double sample;   /* slice spacing in units of lambda0 (&time sample) */
+  double gammaref; /* reference energy (&setup gamma0, Undulator::getGammaRef) */
+  int precision;   /* G4GPU_PLAIN or G4GPU_MIXED */
+  int solver;      /* G4GPU_SOLVER_ADI or G4GPU_SOLVER_FFT (&track fft_fieldsolver) */
+  int source_filter;    /* &track source_filter (FFT solver only) */
+  double xcut, ycut, sigmoid; /* &track xcut, ycut, sigmoid */
+  int time_run;    /* time-dependent run: slippage is applied (Control::timerun) */
+  int periodic;    /* &track periodic: the window wraps instead of zero-filling */
+  int device;      /* CUDA device ordinal */
+} g4gpu_config;
+
+typedef struct g4gpu_ctx *g4gpu_handle;
+
+/* Fills *cfg with the reference's defaults (Setup.cpp:7-47, Track.cpp:4-15). */
+void g4gpu_config_defaults(g4gpu_config *cfg);
+
+/* Creates a handle and allocates the device arrays for cfg.
+ * Replaces the allocation in Beam::init (src/Core/Beam.cpp:221-238) and
+ * Field::init (src/Core/Field.cpp:34-70) plus Field::initSolver (Field.cpp:72-83). */
+int g4gpu_create(const g4gpu_config *cfg, g4gpu_handle *out);
+
+/* Releases the handle and its device memory. */
+void g4gpu_destroy(g4gpu_handle h);
+
+/* Message of the last failed call on h (or of the last failed g4gpu_create when h
+ * is NULL); never NULL. */
+const char *g4gpu_last_error(g4gpu_handle h);
+
+/* Uploads the per-step lattice tables and precomputes the per-step constants
+ * (coupling fc(h) of Undulator::fc, src/Core/Undulator.cpp:141-167; transverse
+ * focusing of TrackBeam::track, src/Core/TrackBeam.cpp:17-64; ADI coefficients of
+ * FieldSolverADI::init, src/Core/FieldSolverADI.cpp:125-182). Replaces the
+ * Undulator produced by Lattice::generateLattice (src/Lattice/Lattice.cpp:53-149). */
+int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *table);
+
+/* Copies particles (host, AoS) and slice currents to the device. */
+int g4gpu_load_beam(g4gpu_handle h, const double *particles, const double *current);
+/* Copies the particles of the device back (host, AoS). */
+int g4gpu_get_beam(g4gpu_handle h, double *particles);
+
+/* Copies field ifld (host, storage order) to the device with ring start `first`
+ * and accumulated slippage `accuslip` (Field::first, Field::accuslip). */
+int g4gpu_load_field(g4gpu_handle h, int ifld, const double *field, int first, double accuslip);
+/* Copies field ifld back (storage order) with its ring start and slippage. */
+int g4gpu_get_field(g4gpu_handle h, int ifld, double *field, int *first, double *accuslip);
+
+/* Runs integration steps istep0 .. istep0+nsteps-1 of the lattice on the device,
+ * each made of the stages selected by `stages` in the order of Gencore.cpp:118-147.
+ * Asynchronous: returns once the work is queued on the handle's stream. */
+int g4gpu_run(g4gpu_handle h, int istep0, int nsteps, int stages);
+
+/* Waits for the handle's stream and reports any device error flag. */
+int g4gpu_synchronize(g4gpu_handle h);
+
+/* Per-slice diagnostics of the current state, reduced on the device in FP64.
+ * beam_out [nslice][G4GPU_DB_NCOL + 2*nharm] (may be NULL),
+ * field_out [nfield][nslice][G4GPU_DF_NCOL] indexed by window slice (may be NULL).
+ * Replaces Diagnostic::calc (src/Core/Diagnostic.cpp:262-277) for these columns. */
+int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out);
+
+/* The CUDA stream (cudaStream_t) every kernel of h is queued on. */
+int g4gpu_get_stream(g4gpu_handle h, void **stream);
+
+/* Kernel accounting. With profiling on, every launch is bracketed by CUDA events
+ * on the handle's stream; g4gpu_kernel_stats returns per kernel class
+ * (G4GPU_K_*) the launch count and the summed device time in milliseconds of the
+ * launches since the last reset. The launch counter runs always. */
+enum { G4GPU_K_PUSH, G4GPU_K_ADI_X, G4GPU_K_ADI_Y, G4GPU_K_FFT, G4GPU_K_SLIP, G4GPU_K_DIAG,
+       G4GPU_K_MISC, G4GPU_K_NCLASS };
+int g4gpu_set_profiling(g4gpu_handle h, int on);
+int g4gpu_kernel_stats(g4gpu_handle h, long long *launches, double *ms);
+int g4gpu_reset_stats(g4gpu_handle h);
+
+/* Bytes of device memory held by h. */
+size_t g4gpu_device_bytes(g4gpu_handle h);
+
+/* ---- host-side loading (bit-exact with the reference, run on the CPU) ------ */
+
+/* Quiet loading plus shot noise of nslice consecutive slices for one rank, as
+ * LoadBeam::init drives QuietLoading::loadQuiet and ShotNoise::applyShotNoise
+ * (src/Loading/LoadBeam.cpp:157-212, src/Loading/QuietLoading.cpp:50-260,
+ * src/Loading/ShotNoise.cpp:16-68). slicepar[nslice][17]: gamma, delgam, ex, ey,
+ * betax, betay, alphax, alphay, xcen, ycen, pxcen, pycen, bunch, bunchphase, emod,
+ * emodphase, current. out: particles [nslice][npart][6]. */
+int g4gpu_host_load_beam(int nslice, int islice0, int npart, int nbins, int seed,
+                         int shotnoise, double lambda0, double sample, const double *slicepar,
+                         double *out);
+
+/* Gauss-Hermite seed field of one slice (src/Util/GaussHermite.cpp:20-85).
+ * par: lambda, power, phase, z0, w0, xcen, ycen, xangle, yangle, nx, ny, harm.
+ * out: [ngrid*ngrid][2]. */
+int g4gpu_host_gauss_hermite(const double *par, double gridmax, int ngrid, double *out);
+
+/* Undulator coupling fc(h) (src/Core/Undulator.cpp:141-167). */
+double g4gpu_host_fc(double aw, int helical, int h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,274 @@
+"""Generates the golden fixtures of tests/golden/ from the GENESIS 1.3 v4 reference
+itself, compiled from its own sources (oracle/ref_build/Makefile -> oracle/_ref/).
+
+Run where the reference tree is present:
+    python oracle/build_oracle.py && python tests/golden/gen_golden.py
+
+Fixtures (numpy .npz):
+  streams.npz    ran2, Hammersley, inverse erfc, Bessel J_n and fc(h) values
+  loading.npz    quiet-loaded / shot-noise slices and Gauss-Hermite seed fields
+  steps.npz      integration steps of small windows: input state, lattice table and
+                 the reference's output state for single stages and full steps
+  example1.npz   the reference's Example1 deck (examples/Example1-SteadyState):
+                 lattice table, loaded beam, per-step power / bunching / energy
+  config0.npz    the 443-step steady-state deck of the planar FODO configuration:
+                 lattice table, loaded beam, per-step power / bunching / energy
+
+The reference's CI check of Example1 (examples/Example1-SteadyState/TEST_power.py)
+expects a final power of 0.932785e9 W within 30 %; example1.npz records what the
+compiled reference produces here.
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+import g4cases as T  # noqa: E402
+import g4oracle as G  # noqa: E402
+from rawio import read_raw  # noqa: E402
+
+REF_DIR = os.environ.get("G4_REFERENCE_DIR", "/root/reference")
+GENESIS = os.path.join(ROOT, "oracle", "_ref", "genesis4")
+
+
+def gen_streams(r):
+    d = {}
+    for s in (1, 7, 11, 123456789):
+        d[f"ran2_{s}"] = r.ran2(s, 64)
+    for b in range(6):
+        for st in (0, 12345, 987654321):
+            d[f"ham_{b}_{st}"] = r.hammersley(b, st, 64)
+    x = np.linspace(1e-12, 2 - 1e-12, 1001)
+    d["inverfc_x"] = x
+    d["inverfc_y"] = r.inverfc(x)
+    xs = np.array([-9.0, -3.0, 0.0, 0.1, 0.3, 1.0, 2.5, 7.9, 8.1, 15.0])
+    d["bessel_x"] = xs
+    d["bessel_j"] = np.array([[r.besselj(n, v) for v in xs] for n in range(5)])
+    aws = np.array([0.5, 0.84853, 1.7, 3.0])
+    d["fc_aw"] = aws
+    d["fc"] = np.array([[[r.fc(a, hel, h) for h in range(1, 8)] for hel in (0, 1)] for a in aws])
+    np.savez_compressed(os.path.join(HERE, "streams.npz"), **d)
+
+
+def loading_cases():
+    sp0 = T.slice_params(4, 11357.8, 2.0, 0.4e-6, 15.0)
+    sp1 = T.slice_params(4, 11357.8, 1.0, 0.4e-6, 15.0, alpha=0.3)
+    sp2 = T.slice_params(3, 11357.8, 2.0, 0.4e-6, 12.0)
+    sp2[:, 8] = 1e-6
+    sp2[:, 11] = 0.1
+    sp2[:, 12] = [0.05, 0.2, 0.0]    # bunch (both branches of QuietLoading.cpp:248-258)
+    sp2[:, 13] = 0.4
+    sp2[:, 14] = [0.5, 0.0, 1.0]     # emod
+    sp2[:, 15] = 0.1
+    cur = T.flat_top_current(4, 1e-10, 1.0, 3000.0, 0.8e-10)
+    sp3 = T.slice_params(4, 11357.8, 2.0, 0.4e-6, 15.0, currents=cur)
+    return [
+        dict(name="quiet_nb4", sp=sp0, islice0=0, npart=64, nbins=4, seed=1, sn=0),
+        dict(name="shot_nb4", sp=sp0, islice0=0, npart=64, nbins=4, seed=7, sn=1),
+        dict(name="shot_nb8", sp=sp1, islice0=10, npart=128, nbins=8, seed=11, sn=1),
+        dict(name="bunch_emod", sp=sp2, islice0=3, npart=32, nbins=4, seed=5, sn=0),
+        dict(name="shot_profile", sp=sp3, islice0=100, npart=64, nbins=4, seed=7, sn=1),
+    ]
+
+
+def gh_cases():
+    return [
+        dict(name="gh_fund", par=T.gauss_field_par(1e-10, 1e3, 30e-6), gridmax=1e-4, ngrid=21),
+        dict(name="gh_h3", par=np.array([1e-10, 2e2, 0.3, 0.5, 20e-6, 1e-6, -2e-6, 1e-5, 0, 1, 2, 3.0]),
+             gridmax=1.5e-4, ngrid=17),
+    ]
+
+
+def gen_loading(r):
+    d = {}
+    for c in loading_cases():
+        d[c["name"] + "_sp"] = c["sp"]
+        d[c["name"] + "_args"] = np.array([c["islice0"], c["npart"], c["nbins"], c["seed"], c["sn"]])
+        d[c["name"]] = r.load_beam(c["sp"], c["islice0"], c["npart"], c["nbins"], c["seed"], c["sn"], 1e-10, 1.0)
+    for c in gh_cases():
+        d[c["name"] + "_par"] = c["par"]
+        d[c["name"] + "_grid"] = np.array([c["gridmax"], c["ngrid"]])
+        d[c["name"]] = r.gauss_hermite(c["par"], c["gridmax"], c["ngrid"])
+    np.savez_compressed(os.path.join(HERE, "loading.npz"), **d)
+
+
+def step_cases(r):
+    """Small windows that exercise every branch of the step."""
+    cases = []
+    # planar FODO, time dependent, shot noise
+    lat = T.undulator_lattice(1.7, 0.015, 8, 2, 1e-10, 11357.8, quad_k1=1.5, quad_l=0.08)
+    cur = np.array([3000.0, 2500.0, 1000.0, 3000.0])
+    part = r.load_beam(T.slice_params(4, 11357.8, 2.0, 0.4e-6, 15.0, currents=cur), 0, 64, 4, 7, 1, 1e-10, 1.0)
+    gh = r.gauss_hermite(T.gauss_field_par(1e-10, 1e5, 20e-6), 6e-5, 25)
+    fld = np.stack([gh * (1 + 0.2j * k) for k in range(4)])[None]
+    cases.append(dict(name="planar", lat=lat, gammaref=11357.8, part=part, cur=cur, harm=[1],
+                      gridmax=[6e-5], fields=fld, first=[0], time_run=1, periodic=0))
+    # helical undulator with corrector kicks, a phase shift and an offset/gradient
+    lat = T.undulator_lattice(0.84853, 0.015, 6, 2, 1e-10, 11357.82, helical=True, quad_k1=2.0, quad_l=0.08)
+    lat[3, T.C["cx"]] = 2e-6
+    lat[5, T.C["cy"]] = -1e-6
+    lat[2, T.C["phase"]] = 0.7
+    lat[:6, T.C["ax"]] = 2e-6
+    lat[:6, T.C["gradx"]] = 3.0
+    lat[6, T.C["qx"]] = 1e-5
+    part = r.load_beam(T.slice_params(3, 11357.82, 1.0, 0.4e-6, 10.0), 2, 64, 8, 3, 1, 1e-10, 1.0)
+    gh = r.gauss_hermite(T.gauss_field_par(1e-10, 5e3, 30e-6), 8e-5, 21)
+    fld = np.stack([gh * (1 - 0.1j * k) for k in range(3)])[None]
+    cases.append(dict(name="helical", lat=lat, gammaref=11357.82, part=part, cur=np.full(3, 3000.0),
+                      harm=[1], gridmax=[8e-5], fields=fld, first=[1], time_run=1, periodic=0))
+    # two harmonics (1 and 3) with their own grids; periodic window
+    lat = T.undulator_lattice(1.7, 0.015, 6, 2, 1e-10, 11357.8, quad_k1=1.5, quad_l=0.08)
+    part = r.load_beam(T.slice_params(5, 11357.8, 2.0, 0.4e-6, 15.0), 0, 48, 4, 9, 1, 1e-10, 1.0)
+    g1 = r.gauss_hermite(T.gauss_field_par(1e-10, 1e5, 20e-6), 6e-5, 19)
+    g3 = r.gauss_hermite(T.gauss_field_par(1e-10, 1e3, 12e-6, harm=3), 4e-5, 19)
+    fld = np.stack([np.stack([g1 * (1 + 0.3j * k) for k in range(5)]),
+                    np.stack([g3 * (1 - 0.2j * k) for k in range(5)])])
+    cases.append(dict(name="harm13", lat=lat, gammaref=11357.8, part=part, cur=np.full(5, 2000.0),
+                      harm=[1, 3], gridmax=[6e-5, 4e-5], fields=fld, first=[0, 2], time_run=1,
+                      periodic=1))
+    # steady state single slice, particles partly off the grid
+    lat = T.undulator_lattice(1.7, 0.015, 10, 1, 1e-10, 11357.8)
+    part = r.load_beam(T.slice_params(1, 11357.8, 2.0, 4e-6, 15.0), 0, 96, 4, 1, 0, 1e-10, 1.0)
+    gh = r.gauss_hermite(T.gauss_field_par(1e-10, 1e6, 15e-6), 3e-5, 15)
+    cases.append(dict(name="steady", lat=lat, gammaref=11357.8, part=part, cur=np.array([3000.0]),
+                      harm=[1], gridmax=[3e-5], fields=gh[None, None], first=[0], time_run=0,
+                      periodic=0))
+    return cases
+
+
+def gen_steps(r):
+    d = {}
+    for c in step_cases(r):
+        n = c["name"]
+        for k in ("lat", "part", "cur", "harm", "gridmax", "fields", "first"):
+            d[f"{n}_{k}"] = np.asarray(c[k])
+        d[f"{n}_args"] = np.array([c["gammaref"], c["time_run"], c["periodic"]])
+        for stages in (1, 2, 4, 7):
+            # single stages over the first step, the full step over the whole lattice
+            lat = c["lat"][:1] if stages != 7 else c["lat"]
+            out = r.run_steps(lat, c["gammaref"], c["part"], c["cur"], 1e-10, 1.0, c["harm"],
+                              c["gridmax"], c["fields"], c["first"], time_run=c["time_run"],
+                              periodic=c["periodic"], stages=stages)
+            d[f"{n}_s{stages}_part"] = out[0]
+            d[f"{n}_s{stages}_fields"] = out[1]
+            d[f"{n}_s{stages}_first"] = out[2]
+    np.savez_compressed(os.path.join(HERE, "steps.npz"), **d)
+
+
+LAT_FROM_OUT = {"aw": "aw", "ax": "ax", "ay": "ay", "ku": "ku", "kx": "kx", "ky": "ky",
+                "gradx": "gradx", "grady": "grady", "qf": "qf", "qx": "qx", "qy": "qy",
+                "cx": "cx", "cy": "cy", "dz": "dz", "slip": "slippage", "phase": "phaseshift",
+                "z": "z"}
+
+
+def run_deck(name, deck, lattice, helical):
+    """Runs the reference's genesis4 on a deck; returns lattice table, loaded beam, outputs."""
+    with tempfile.TemporaryDirectory() as tmp:
+        with open(os.path.join(tmp, name + ".in"), "w") as f:
+            f.write(deck)
+        with open(os.path.join(tmp, name + ".lat"), "w") as f:
+            f.write(lattice)
+        subprocess.run([GENESIS, name + ".in"], cwd=tmp, check=True, stdout=subprocess.DEVNULL)
+        out = read_raw(os.path.join(tmp, name + ".out.h5.raw"))
+        par = read_raw(os.path.join(tmp, name + "_init.par.h5.raw"))
+    latg = out["Lattice"]
+    nz = latg["aw"].size
+    tab = np.zeros((nz, len(T.LAT_COLS)))
+    for k, src in LAT_FROM_OUT.items():
+        tab[:, T.C[k]] = latg[src][:nz]
+    tab[:, T.C["helical"]] = np.where(tab[:, T.C["aw"]] > 0, float(helical), 0.0)
+    beam = np.stack([par[k]["particles"].reshape(-1, 6) for k in sorted(par)])
+    cur = np.array([par[k]["current"][0] for k in sorted(par)])
+    return tab, beam, cur, out
+
+
+def gen_example1():
+    ex = os.path.join(REF_DIR, "examples", "Example1-SteadyState")
+    deck = open(os.path.join(ex, "Example1.in")).read()
+    lattice = open(os.path.join(ex, "Example1.lat")).read()
+    # dump the loaded beam before tracking: &write after &beam
+    deck = deck.replace("&track", "&write\nbeam=Example1_init\n&end\n\n&track", 1)
+    tab, beam, cur, out = run_deck("Example1", deck, lattice, helical=True)
+    np.savez_compressed(os.path.join(HERE, "example1.npz"), lat=tab, beam=beam, current=cur,
+                        gammaref=11357.82, lambda0=1e-10, gridmax=2e-4, ngrid=255, power0=5e3,
+                        waist=30e-6, power=out["Field"]["power"], bunching=out["Beam"]["bunching"],
+                        energy=out["Beam"]["energy"], xsize=out["Beam"]["xsize"],
+                        fieldxsize=out["Field"]["xsize"])
+
+
+CONFIG0_DECK = """&setup
+rootname=cfg0
+lattice=cfg0.lat
+beamline=FEL
+lambda0=1e-10
+gamma0=11357.8
+delz=0.015
+shotnoise=0
+nbins=4
+npart=8192
+seed=1
+&end
+
+&field
+power=1e3
+dgrid=1e-4
+ngrid=151
+waist_size=30e-6
+&end
+
+&beam
+current=3000
+delgam=2.0
+ex=0.4e-6
+ey=0.4e-6
+betax=15
+betay=15
+alphax=0
+alphay=0
+&end
+
+&write
+beam=cfg0_init
+&end
+
+&track
+&end
+"""
+CONFIG0_LAT = """UND: UNDULATOR = {lambdau=0.015, nwig=110, aw=1.7};
+QF: QUADRUPOLE = {l=0.08, k1=1.5};
+QD: QUADRUPOLE = {l=0.08, k1=-1.5};
+FEL: LINE = {UND,QF,UND,QD,UND,QF,UND};
+"""
+
+
+def gen_config0():
+    tab, beam, cur, out = run_deck("cfg0", CONFIG0_DECK, CONFIG0_LAT, helical=False)
+    np.savez_compressed(os.path.join(HERE, "config0.npz"), lat=tab, beam=beam, current=cur,
+                        gammaref=11357.8, lambda0=1e-10, gridmax=1e-4, ngrid=151, power0=1e3,
+                        waist=30e-6, power=out["Field"]["power"], bunching=out["Beam"]["bunching"],
+                        energy=out["Beam"]["energy"])
+
+
+def main():
+    r = G.reference()
+    if r is None or not os.path.exists(GENESIS):
+        sys.exit("the reference checker is not built: run oracle/build_oracle.py with the reference present")
+    gen_streams(r)
+    gen_loading(r)
+    gen_steps(r)
+    gen_example1()
+    gen_config0()
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

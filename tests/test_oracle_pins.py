@@ -1,0 +1,112 @@
+"""Pins the C restatement (oracle/g4oracle.c) to the GENESIS 1.3 v4 reference.
+
+The fixtures in tests/golden/ were produced by the reference itself, compiled from
+its own sources (tests/golden/gen_golden.py). The oracle is bit-exact with them on
+x86-64 (same C library, no fused multiply-add); elsewhere a 1e-14 relative bound
+covers last-bit differences of the platform's log/exp/sin.
+"""
+import platform
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+EXACT = platform.machine() in ("x86_64", "AMD64")
+
+
+def same(a, b, rtol=1e-14):
+    if EXACT:
+        return np.array_equal(a, b)
+    return np.allclose(a, b, rtol=rtol, atol=0)
+
+
+def test_ran2_and_hammersley_streams(oracle):
+    d = golden("streams.npz")
+    for s in (1, 7, 11, 123456789):
+        assert np.array_equal(oracle.ran2(s, 64), d[f"ran2_{s}"]), s  # integer arithmetic: exact
+    for b in range(6):
+        for st in (0, 12345, 987654321):
+            assert np.array_equal(oracle.hammersley(b, st, 64), d[f"ham_{b}_{st}"]), (b, st)
+
+
+def test_inverfc_bessel_fc(oracle):
+    d = golden("streams.npz")
+    assert same(oracle.inverfc(d["inverfc_x"]), d["inverfc_y"])
+    xs = d["bessel_x"]
+    got = np.array([[oracle.besselj(n, v) for v in xs] for n in range(5)])
+    assert same(got, d["bessel_j"])
+    fc = np.array([[[oracle.fc(a, hel, h) for h in range(1, 8)] for hel in (0, 1)] for a in d["fc_aw"]])
+    assert same(fc, d["fc"])
+    # even harmonics of a planar undulator and harmonics > 1 of a helical one couple to 0
+    assert np.all(d["fc"][:, 0, 1::2] == 0) and np.all(d["fc"][:, 1, 1:] == 0)
+
+
+@pytest.mark.parametrize("name", ["quiet_nb4", "shot_nb4", "shot_nb8", "bunch_emod", "shot_profile"])
+def test_quiet_loading_and_shot_noise(oracle, name):
+    d = golden("loading.npz")
+    islice0, npart, nbins, seed, sn = (int(v) for v in d[name + "_args"])
+    got = oracle.load_beam(d[name + "_sp"], islice0, npart, nbins, seed, sn, 1e-10, 1.0)
+    assert same(got, d[name])
+
+
+@pytest.mark.parametrize("name", ["gh_fund", "gh_h3"])
+def test_gauss_hermite(oracle, name):
+    d = golden("loading.npz")
+    gm, ng = d[name + "_grid"]
+    assert same(oracle.gauss_hermite(d[name + "_par"], gm, int(ng)), d[name])
+
+
+@pytest.mark.parametrize("case", ["planar", "helical", "harm13", "steady"])
+@pytest.mark.parametrize("stages", [1, 2, 4, 7])
+def test_integration_steps(oracle, case, stages):
+    d = golden("steps.npz")
+    g = lambda k: d[f"{case}_{k}"]
+    gammaref, time_run, periodic = g("args")
+    lat = g("lat")[:1] if stages != 7 else g("lat")
+    part, fld, first, _ = oracle.run_steps(lat, gammaref, g("part"), g("cur"), 1e-10, 1.0, g("harm"),
+                                           g("gridmax"), g("fields"), g("first"),
+                                           time_run=int(time_run), periodic=int(periodic),
+                                           stages=stages)
+    assert same(part, g(f"s{stages}_part"), rtol=1e-12)
+    assert same(fld, g(f"s{stages}_fields"), rtol=1e-12)
+    assert np.array_equal(first, g(f"s{stages}_first"))
+
+
+def test_threads_do_not_change_results(oracle):
+    d = golden("steps.npz")
+    g = lambda k: d[f"harm13_{k}"]
+    args = (g("lat"), 11357.8, g("part"), g("cur"), 1e-10, 1.0, g("harm"), g("gridmax"), g("fields"), g("first"))
+    a = oracle.run_steps(*args, periodic=1, nthreads=1)
+    b = oracle.run_steps(*args, periodic=1, nthreads=3)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def _gauss_field(oracle, d):
+    ng = int(d["ngrid"])
+    par = np.array([d["lambda0"], d["power0"], 0, 0, d["waist"], 0, 0, 0, 0, 0, 0, 1.0])
+    return oracle.gauss_hermite(par, float(d["gridmax"]), ng)
+
+
+def test_config0_deck_final_power(oracle):
+    """The 443-step planar FODO deck, steady state (the reference's genesis4 output)."""
+    d = golden("config0.npz")
+    fld = _gauss_field(oracle, d)[None, None]
+    part, f, first, _ = oracle.run_steps(d["lat"], float(d["gammaref"]), d["beam"], d["current"], 1e-10,
+                                         1.0, [1], [float(d["gridmax"])], fld, [0], time_run=0)
+    df = oracle.diag_field(f[0], float(d["gridmax"]), 1e-10, 1, 0)
+    db = oracle.diag_beam(part, 1)
+    assert same(df[0, 0], d["power"][-1], rtol=1e-12)
+    assert same(db[0, 24], d["bunching"][-1], rtol=1e-9)
+
+
+def test_example1_deck_final_power(oracle):
+    """Example1 of the reference (helical, lasing): 1104 steps, ngrid 255."""
+    d = golden("example1.npz")
+    fld = _gauss_field(oracle, d)[None, None]
+    part, f, first, _ = oracle.run_steps(d["lat"], float(d["gammaref"]), d["beam"], d["current"], 1e-10,
+                                         1.0, [1], [float(d["gridmax"])], fld, [0], time_run=0)
+    df = oracle.diag_field(f[0], float(d["gridmax"]), 1e-10, 1, 0)
+    assert same(df[0, 0], d["power"][-1], rtol=1e-12)
+    # the reference's CI golden value (examples/Example1-SteadyState/TEST_power.py:14,17)
+    assert abs(df[0, 0] / 0.932785e9 - 1) < 0.3
