@@ -63,8 +63,8 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def workload_inputs(ns=NS, npart=NPART):
-    import g4gpu
+def workload_inputs(ns=None):
+    ns = ns or NS
     cur = flat_top(ns)
     sp = T.slice_params(ns, GAMMA0, 2.0, 0.4e-6, 15.0, currents=cur)
     lat = T.undulator_lattice(1.7, 0.015, 110, 4, LAMBDA0, GAMMA0, quad_k1=1.5, quad_l=0.08)
@@ -170,12 +170,29 @@ def alg_bytes_per_slice_step(mixed):
     return (56 * NPART + 16 * ncell) if mixed else (96 * NPART + 32 * ncell)
 
 
-def push_alg_bytes(mixed, ns):
-    """Algorithmic bytes of one push launch over the window: particles read and
-    written (plain 96 B, mixed 56 B per particle), the field slice gathered once
-    and the source written once (plain 16 + 16, mixed 8 + 8 B per cell)."""
+def kernel_alg_bytes(kernel, mixed, ns=None):
+    """Algorithmic bytes of one launch of a kernel class over the whole window:
+    what the kernel must read and write at least, per slice:
+      push        particles read + written (plain 96 B, mixed 56 B per particle) and
+                  the field slice gathered once (16 / 8 B per cell); in the plain form
+                  the push also deposits, writing the source once (16 B per cell)
+      adi_x       (plain, and mixed for ngrid > 168) field + source read, intermediate
+                  written: 3 x 16 / 3 x 8 B per cell
+      adi_y       intermediate + source read, field written: same
+      field       (fused mixed kernel) field read + written (16 B per cell) and the
+                  particle coordinates the deposition needs (x, y, gamma FP32, theta
+                  FP64: 20 B per particle)"""
+    ns = ns or NS
     ncell = NGRID * NGRID
-    return ns * ((56 * NPART + 16 * ncell) if mixed else (96 * NPART + 32 * ncell))
+    if kernel == "push":
+        per = (56 * NPART + 8 * ncell) if mixed else (96 * NPART + 32 * ncell)
+    elif kernel in ("adi_x", "adi_y"):
+        per = (24 if mixed else 48) * ncell
+    elif kernel == "field":
+        per = 16 * ncell + 20 * NPART
+    else:
+        return None
+    return ns * per
 
 
 def time_form(g4gpu, torch, precision, beam, cur, lat, steps, warmup, profile=True):
@@ -330,7 +347,13 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=None, help="timed steps of the plain form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--nslice", type=int, default=None,
+                    help="slices of the window (default 4096); smaller values are for profiling only")
+    ap.add_argument("--forms", default="mixed,plain", help="forms to time: mixed, plain or both")
     args = ap.parse_args()
+    global NS
+    if args.nslice:
+        NS = args.nslice
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -356,11 +379,13 @@ def main():
     ms_m = max_over_ranks(ws, ms_m)
     # plain FP64 form, same initial state and steps
     psteps = args.plain_steps if args.plain_steps is not None else args.steps
-    hp, ms_p, st_p = time_form(g4gpu, torch, g4gpu.PLAIN, beam, cur, lat, psteps, args.warmup)
-    ms_p = max_over_ranks(ws, ms_p)
+    do_plain = "plain" in args.forms
+    if do_plain:
+        hp, ms_p, st_p = time_form(g4gpu, torch, g4gpu.PLAIN, beam, cur, lat, psteps, args.warmup)
+        ms_p = max_over_ranks(ws, ms_p)
     # error of the mixed form against the plain one after the same steps
     err = None
-    if psteps == args.steps:
+    if do_plain and psteps == args.steps:
         bm, fm = hm.diag(1)
         bp, fp = hp.diag(1)
         pw_m, pw_p = fm[0][:, 0], fp[0][:, 0]
@@ -369,18 +394,37 @@ def main():
                "bunching_max_rel": float(np.max(np.abs(bm[:, 24] - bp[:, 24])) / np.max(np.abs(bp[:, 24]))),
                "after_steps": args.warmup + args.steps}
     hm.close()
-    hp.close()
+    if do_plain:
+        hp.close()
 
     value = NS * ws / (ms_m / args.steps / 1e3)
-    plain_value = NS * ws / (ms_p / psteps / 1e3)
+    plain_value = NS * ws / (ms_p / psteps / 1e3) if do_plain else None
     launches = sum(v[0] for v in st_m.values())
-    push_n, push_ms = st_m["push"]
-    push_avg = push_ms / max(push_n, 1)
-    achieved = push_alg_bytes(True, NS) / (push_avg / 1e3) / 1e9
-    kernels = {k: {"launches": v[0], "ms_total": v[1], "share": v[1] / max(sum(x[1] for x in st_m.values()), 1e-12)}
-               for k, v in st_m.items() if v[0] > 0}
-    pp_n, pp_ms = st_p["push"]
-    plain_push_avg = pp_ms / max(pp_n, 1)
+
+    def kernel_table(st, mixed):
+        # the mixed form's deposition + ADI runs as one fused kernel when the slice
+        # fits in shared memory; it is accounted under the adi_x class
+        fused = mixed and NGRID <= 168
+        tot = max(sum(x[1] for x in st.values()), 1e-12)
+        out = {}
+        for k, (n, ms) in st.items():
+            if n == 0:
+                continue
+            name = "field" if (fused and k == "adi_x") else k
+            avg = ms / n
+            ab = kernel_alg_bytes(name, mixed)
+            row = {"launches": n, "ms_total": ms, "ms_avg": avg, "share": ms / tot}
+            if ab is not None:
+                row["alg_bytes"] = ab
+                row["achieved_gbs"] = ab / (avg / 1e3) / 1e9
+                row["frac_hbm"] = row["achieved_gbs"] / peak
+            out[name] = row
+        return out
+
+    kernels = kernel_table(st_m, True)
+    kernels_plain = kernel_table(st_p, False) if do_plain else None
+    dom = max(kernels, key=lambda k: kernels[k]["ms_total"])
+    dk = kernels[dom]
 
     line = {"metric": METRIC, "value": value, "unit": "slice-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_m / args.steps,
@@ -391,14 +435,13 @@ def main():
                        "form": "mixed (FP32 field/solver/deposition, FP64 phase)",
                        "cache": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{ws}"},
             "forms": {"mixed": {"value": value, "ms_per_step": ms_m / args.steps},
-                      "plain_fp64": {"value": plain_value, "ms_per_step": ms_p / psteps,
-                                     "steps": psteps, "push_ms_avg": plain_push_avg,
-                                     "push_achieved_gbs": push_alg_bytes(False, NS) / (plain_push_avg / 1e3) / 1e9}},
+                      "plain_fp64": ({"value": plain_value, "ms_per_step": ms_p / psteps,
+                                      "steps": psteps, "kernels": kernels_plain} if do_plain else None)},
             "mixed_error_vs_plain": err,
-            "roofline": {"bound": "hbm", "kernel": "push (k_push_f)", "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                         "peak_source": peak_kind,
-                         "alg_bytes_per_launch": push_alg_bytes(True, NS)},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": dk.get("achieved_gbs"), "peak": peak,
+                         "unit": "GB/s", "frac": dk.get("frac_hbm"), "traffic": None,
+                         "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                         "alg_bytes_per_launch": dk.get("alg_bytes"), "ms_per_launch": dk["ms_avg"]},
             "kernels": kernels, "gpu_launches": launches, "clocks": clocks}
 
     if rank == 0 and not args.no_e2e:

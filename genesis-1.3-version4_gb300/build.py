@@ -6,6 +6,7 @@ and g++. The library is built in-tree and is what include/g4gpu.h describes.
   kernels_plain.cu   FP64 kernels, compiled with --fmad=false (reference rounding)
   kernels_mixed.cu   mixed-precision kernels
   kernels_util.cu    layout conversions
+  kernels_fft.cu     FFT field solver (mixed-radix Stockham, FP64 and FP32)
   g4gpu_api.cpp      C ABI, host bookkeeping (-ffp-contract=off)
   host_loading.cpp   bit-exact host loading (-ffp-contract=off)
 """
@@ -38,8 +39,11 @@ def _units():
                   "-I", os.path.join(_cuda_home(), "include")]
     return [
         ("kernels_plain.cu", cu_common + ["--fmad=false"]),
-        ("kernels_mixed.cu", cu_common),
+        # the mixed form tolerates approximate FP32 division, square root and
+        # sin/cos (errors ~1e-7 relative, far below its 1 % target)
+        ("kernels_mixed.cu", cu_common + ["-use_fast_math"]),
         ("kernels_util.cu", cu_common),
+        ("kernels_fft.cu", cu_common),
         ("g4gpu_api.cpp", cxx_common),
         ("host_loading.cpp", cxx_common + ["-pthread"]),
     ]

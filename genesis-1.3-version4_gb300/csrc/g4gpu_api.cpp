@@ -48,7 +48,11 @@ struct g4gpu_ctx {
   void *tmp = nullptr;
   void *coef = nullptr;      // [nset][3][ngrid] complex of the field type
   size_t coef_bytes = 0;
-  void *fftk2 = nullptr;     // FFT propagator and filter tables
+  // FFT solver tables per field: roots of unity [n], Im(K2) and the sigmoid [n^2]
+  void *fft_roots[G4GPU_MAX_FIELDS] = {};
+  void *fft_k2[G4GPU_MAX_FIELDS] = {};
+  void *fft_sig[G4GPU_MAX_FIELDS] = {};
+  g4::FFTPlan fft_plan{};
   int *derr = nullptr;
   double *ddiag = nullptr;
   size_t ddiag_bytes = 0;
@@ -117,8 +121,8 @@ struct Timed {
   g4gpu_handle h;
   int cls;
   cudaEvent_t a = nullptr, b = nullptr;
-  Timed(g4gpu_handle h_, int cls_) : h(h_), cls(cls_) {
-    h->launches[cls]++;
+  Timed(g4gpu_handle h_, int cls_, int kernels = 1) : h(h_), cls(cls_) {
+    h->launches[cls] += kernels;
     if (h->prof) {
       a = take_event(h);
       b = take_event(h);
@@ -200,6 +204,67 @@ void adi_coefficients(double delz, double dgrid, double xks, int ngrid, std::vec
     cwet[i] = w1[i - 1] * cbet[i - 1];
     cbet[i] = 1. / (w2[i] - c[i] * cwet[i]);
   }
+}
+
+// FieldSolverFFT::init (src/Core/FieldSolverFFT.cpp:117-155): the propagator
+// exponent Im(K2) and the source filter on the shifted frequency map, per field,
+// plus the n-th roots of unity and the prime factors of ngrid for the kernels.
+int fft_tables(g4gpu_handle h) {
+  const g4gpu_config &c = h->cfg;
+  int n = c.ngrid;
+  g4::FFTPlan &pl = h->fft_plan;
+  pl.n = n;
+  pl.nstage = 0;
+  int m = n;
+  for (int p = 2; p * p <= m; p++)
+    while (m % p == 0 && pl.nstage < 31) {
+      pl.radix[pl.nstage++] = p;
+      m /= p;
+    }
+  if (m > 1) pl.radix[pl.nstage++] = m;
+  std::vector<double> roots(2 * n);
+  for (int i = 0; i < n; i++) {
+    double a = 2.0 * 3.14159265358979323846 * (double)i / (double)n;
+    roots[2 * i] = std::cos(a);
+    roots[2 * i + 1] = -std::sin(a);
+  }
+  double xc = c.xcut, yc = c.ycut, sig = c.sigmoid;
+  for (int k = 0; k < c.nfield; k++) {
+    double xlambda = c.lambda0 / static_cast<double>(c.harm[k]);
+    double xks = 4. * std::asin(1) / xlambda;
+    double dgrid = 2 * c.gridmax[k] / static_cast<double>(n - 1);
+    double dk = 4. * std::asin(1.) / (static_cast<double>(n) * dgrid);
+    std::vector<double> k2((size_t)n * n), sg((size_t)n * n);
+    double shift = -0.5 * static_cast<double>(n - 1);
+    for (int iy = 0; iy < n; iy++) {
+      double dy = static_cast<double>(iy) + shift;
+      double y = dy / static_cast<double>(n) / yc;
+      for (int ix = 0; ix < n; ix++) {
+        double dx = static_cast<double>(ix) + shift;
+        double x = dx / static_cast<double>(n) / xc;
+        int iiy = (iy + (n + 1) / 2) % n, iix = (ix + (n + 1) / 2) % n;
+        size_t ii = (size_t)iiy * n + iix;
+        k2[ii] = -(dx * dx + dy * dy) * dk * dk / 2. / xks;
+        double r = (std::sqrt(x * x + y * y) - 1) / sig;
+        sg[ii] = 1. / (1 + std::exp(r));
+      }
+    }
+    size_t es = h->mixed ? sizeof(float) : sizeof(double);
+    int rc;
+    if ((rc = alloc(h, &h->fft_roots[k], (size_t)n * 2 * es))) return rc;
+    if ((rc = alloc(h, &h->fft_k2[k], (size_t)n * n * es))) return rc;
+    if ((rc = alloc(h, &h->fft_sig[k], (size_t)n * n * es))) return rc;
+    auto put = [&](void *dst, const std::vector<double> &v) -> int {
+      if (h->mixed) {
+        std::vector<float> f(v.begin(), v.end());
+        return cudaMemcpy(dst, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice);
+      }
+      return cudaMemcpy(dst, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice);
+    };
+    if (put(h->fft_roots[k], roots) || put(h->fft_k2[k], k2) || put(h->fft_sig[k], sg))
+      return fail(h, G4GPU_ERR_CUDA, "copy of the FFT tables failed");
+  }
+  return G4GPU_OK;
 }
 
 }  // namespace
@@ -285,6 +350,11 @@ int g4gpu_create(const g4gpu_config *cfg, g4gpu_handle *out) {
     cudaMemsetAsync(h->src[k], 0, (size_t)c.nslice * ncell * h->csize, h->stream);
   }
   if ((rc = alloc(h, &h->tmp, (size_t)c.nslice * ncell * h->csize))) return bail(rc);
+  if (c.solver == G4GPU_SOLVER_FFT) {
+    if (c.ngrid > g4::fft_max_ngrid(h->mixed))
+      return bail(fail(h, G4GPU_ERR_ARG, "ngrid too large for the FFT solver"));
+    if ((rc = fft_tables(h))) return bail(rc);
+  }
   if ((rc = alloc(h, (void **)&h->derr, sizeof(int)))) return bail(rc);
   cudaMemsetAsync(h->derr, 0, sizeof(int), h->stream);
   if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(cuda_fail(h, e, "init"));
@@ -297,12 +367,13 @@ void g4gpu_destroy(g4gpu_handle h) {
   cudaSetDevice(h->cfg.device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   void *ptrs[] = {h->beam.gamma, h->beam.theta, h->beam.x, h->beam.y, h->beam.px, h->beam.py,
-                  h->beam.current, h->tmp, h->coef, h->fftk2, h->derr, h->ddiag, h->stage};
+                  h->beam.current, h->tmp, h->coef, h->derr, h->ddiag, h->stage};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
-    if (h->field[k]) cudaFree(h->field[k]);
-    if (h->src[k]) cudaFree(h->src[k]);
+    void *fp[] = {h->field[k], h->src[k], h->fft_roots[k], h->fft_k2[k], h->fft_sig[k]};
+    for (void *p : fp)
+      if (p) cudaFree(p);
   }
   for (auto &p : h->pending) {
     cudaEventDestroy(p.a);
@@ -542,8 +613,6 @@ int g4gpu_run(g4gpu_handle h, int istep0, int nsteps, int stages) {
   if (!h->beam_loaded) return fail(h, G4GPU_ERR_STATE, "no beam loaded");
   for (int k = 0; k < h->cfg.nfield; k++)
     if (!h->field_loaded[k]) return fail(h, G4GPU_ERR_STATE, "a field is not loaded");
-  if (h->cfg.solver == G4GPU_SOLVER_FFT && (stages & G4GPU_STAGE_FIELD))
-    return fail(h, G4GPU_ERR_ARG, "FFT solver not available in this build");
   cudaSetDevice(h->cfg.device);
   const g4gpu_config &c = h->cfg;
   int ns = c.nslice, np = c.npart, ng = c.ngrid;
@@ -556,6 +625,22 @@ int g4gpu_run(g4gpu_handle h, int istep0, int nsteps, int stages) {
     for (int k = 0; k < c.nfield; k++) sc.f[k].first = h->first[k];
     bool any_dep = false;
     for (int k = 0; k < c.nfield; k++) any_dep = any_dep || sc.f[k].dep_on;
+    // mixed form with the slice in shared memory: deposition and ADI in one kernel
+    bool fused = h->mixed && c.solver == G4GPU_SOLVER_ADI && ng <= g4::fused_max_ngrid();
+    if (fused) {
+      g4::StepConstF scf = g4::to_float(sc, np);
+      if (do_push) {
+        Timed t(h, G4GPU_K_PUSH);
+        g4::launch_push_mixed(L, scf, h->beam, h->field, nullptr, ns, np, ng, 0);
+      }
+      if (do_field) {
+        for (int k = 0; k < c.nfield; k++) {
+          const char *cb = (const char *)h->coef + (size_t)sc.f[k].coef * 3 * ng * h->csize;
+          Timed t(h, G4GPU_K_ADI_X);
+          g4::launch_field_fused_mixed(L, scf, k, h->beam, h->field[k], cb, ns, np, ng, sc.f[k].dep_on);
+        }
+      }
+    } else {
     if (do_field && any_dep)
       for (int k = 0; k < c.nfield; k++)
         G4_CUDA(h, cudaMemsetAsync(h->src[k], 0, (size_t)ns * ncell * h->csize, h->stream));
@@ -574,17 +659,30 @@ int g4gpu_run(g4gpu_handle h, int istep0, int nsteps, int stages) {
       else
         g4::launch_deposit_plain(L, sc, h->beam, h->src, ns, np, ng);
     }
-    if (do_field) {
+    if (do_field && c.solver == G4GPU_SOLVER_FFT) {
+      for (int k = 0; k < c.nfield; k++) {
+        const void *srck = any_dep ? h->src[k] : nullptr;
+        // a zero source makes the filtered term vanish (FieldSolverFFT.cpp:74-90)
+        int filtered = c.source_filter && srck && c.sigmoid > 0 && c.xcut > 0 && c.ycut > 0;
+        Timed t(h, G4GPU_K_FFT, 3);
+        g4::launch_fft_solve(h->stream, h->mixed, h->field[k], srck, h->tmp, h->fft_roots[k],
+                             h->fft_k2[k], h->fft_sig[k], filtered, sc.delz, h->fft_plan, ns,
+                             sc.f[k].first);
+      }
+    } else if (do_field) {
       for (int k = 0; k < c.nfield; k++) {
         const char *cb = (const char *)h->coef + (size_t)sc.f[k].coef * 3 * ng * h->csize;
+        // the source was cleared and deposited only when some field deposits
+        const void *srck = any_dep ? h->src[k] : nullptr;
         for (int phase = 0; phase < 2; phase++) {
           Timed t(h, phase == 0 ? G4GPU_K_ADI_X : G4GPU_K_ADI_Y);
           if (h->mixed)
-            g4::launch_adi_mixed(L, scf, k, phase, h->field[k], h->src[k], h->tmp, cb, ns, ng);
+            g4::launch_adi_mixed(L, scf, k, phase, h->field[k], srck, h->tmp, cb, ns, ng);
           else
-            g4::launch_adi_plain(L, sc, k, phase, h->field[k], h->src[k], h->tmp, cb, ns, ng);
+            g4::launch_adi_plain(L, sc, k, phase, h->field[k], srck, h->tmp, cb, ns, ng);
         }
       }
+    }
     }
     G4_CUDA(h, cudaGetLastError());
     if (do_slip) {

@@ -106,6 +106,24 @@ void launch_diag_beam_mixed(const Launch &L, const DeviceBeam &b, double gammare
                             int nharm, double *out);
 void launch_diag_field_mixed(const Launch &L, const void *field, int ns, int ngrid,
                              double *out);
+// Fused deposition + ADI of one field in shared memory, one CTA per slice; usable
+// for ngrid <= fused_max_ngrid() (168: the FP32 slice must fit in 227 KB).
+int fused_max_ngrid();
+void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b,
+                              void *field, const void *coef, int ns, int np, int ngrid,
+                              int deposit);
+
+// kernels_fft.cu: FFT field solver (FieldSolverFFT::FFT)
+struct FFTPlan {
+  int n, nstage;
+  int radix[32];  // prime factors of n
+};
+int fft_max_ngrid(int mixed);
+// roots: n complex exp(-2 pi i m / n); k2, sig: Im(K2) and the sigmoid filter on the
+// FFT index (real, n^2); work: n^2 * nslice complex scratch, used when filtered
+void launch_fft_solve(void *stream, int mixed, void *field, const void *src, void *work,
+                      const void *roots, const void *k2, const void *sig, int filtered, double delz,
+                      const FFTPlan &pl, int ns, int first);
 
 // number of raw sums per slice written by the diagnostic kernels
 constexpr int kBeamSums = 12;   // g1 g2 x1 x2 y1 y2 px1 px2 py1 py2 xpx ypy

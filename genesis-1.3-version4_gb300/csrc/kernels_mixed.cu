@@ -13,6 +13,8 @@
 //    "pushp" sequence (BeamSolver.cpp:89-141).
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 #include "g4gpu_internal.h"
 
 namespace g4 {
@@ -294,7 +296,7 @@ __global__ void __launch_bounds__(128) k_adi_x_f(const float2 *__restrict__ fiel
   size_t ncell = (size_t)ng * ng;
   int i = (ii + first) % ns;
   const float2 *u = field + (size_t)i * ncell + (size_t)iy * ng;
-  const float2 *s = src + (size_t)ii * ncell + (size_t)iy * ng;
+  const float2 *s = src ? src + (size_t)ii * ncell + (size_t)iy * ng : nullptr;
   float2 *w = tmp + (size_t)i * ncell + (size_t)iy * ng;
   bool hp = iy > 0, hn = iy < ng - 1;
   float2 prev = make_float2(0.f, 0.f);
@@ -303,7 +305,7 @@ __global__ void __launch_bounds__(128) k_adi_x_f(const float2 *__restrict__ fiel
     float2 un = hn ? u[k + ng] : make_float2(0.f, 0.f);
     float2 us = hp ? u[k - ng] : make_float2(0.f, 0.f);
     float2 l = lapf(hp, hn, us, uc, un);
-    float2 sv = s[k];
+    float2 sv = s ? s[k] : make_float2(0.f, 0.f);
     float2 r = make_float2(sv.x + uc.x - cstep * l.y, sv.y + uc.y + cstep * l.x);
     float2 v;
     if (k == 0) {
@@ -337,7 +339,7 @@ __global__ void __launch_bounds__(128) k_adi_y_f(float2 *__restrict__ field,
   size_t ncell = (size_t)ng * ng;
   int i = (ii + first) % ns;
   float2 *u = field + (size_t)i * ncell + ix;
-  const float2 *s = src + (size_t)ii * ncell + ix;
+  const float2 *s = src ? src + (size_t)ii * ncell + ix : nullptr;
   const float2 *w = tmp + (size_t)i * ncell + ix;
   bool hp = ix > 0, hn = ix < ng - 1;
   float2 prev = make_float2(0.f, 0.f);
@@ -347,7 +349,7 @@ __global__ void __launch_bounds__(128) k_adi_y_f(float2 *__restrict__ field,
     float2 wn = hn ? w[o + 1] : make_float2(0.f, 0.f);
     float2 wp = hp ? w[o - 1] : make_float2(0.f, 0.f);
     float2 l = lapf(hp, hn, wp, wc, wn);
-    float2 sv = s[o];
+    float2 sv = s ? s[o] : make_float2(0.f, 0.f);
     float2 r = make_float2(sv.x + wc.x - cstep * l.y, sv.y + wc.y + cstep * l.x);
     float2 v;
     if (k == 0) {
@@ -369,6 +371,220 @@ __global__ void __launch_bounds__(128) k_adi_y_f(float2 *__restrict__ field,
     u[o] = v;
     next = v;
   }
+}
+
+// ---- fused field step: deposition + ADI of one slice in shared memory --------
+//
+// One CTA per (field, slice). The slice's FP32 field (ngrid^2 float2, 182 KB at
+// ngrid 151) lives in shared memory for the whole solve, so the field is read and
+// written once and the source never touches global memory:
+//   S = u                                   load
+//   S = (I + c Dy) S  + src                  column pass, then deposition (pass 1)
+//   S = Thomas_x(S)                          row sweeps           -> u'
+//   S = (I + c Dx) S  + src                  row pass, then deposition (pass 2)
+//   S = Thomas_y(S)                          column sweeps        -> u''
+//   u = S                                   store
+// This is the reference's ADI (FieldSolverADI.cpp:60-122) with its source
+// (FieldSolverADI.cpp:19-51) added after, instead of before, the stencil term;
+// the deposition is recomputed from the particles for each half step instead of
+// being stored.
+constexpr int kFusedThreads = 512;
+
+__device__ __forceinline__ float2 cadd2(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+
+// c * (i * lap): cstep is purely imaginary
+__device__ __forceinline__ float2 stencil(float cs, float2 u, float2 l) {
+  return make_float2(u.x - cs * l.y, u.y + cs * l.x);
+}
+
+__device__ __forceinline__ void thomas(float2 *S, int stride, int ng, const float2 *C,
+                                       const float2 *CB, const float2 *CW) {
+  float2 prev = cmulf(S[0], CB[0]);
+  S[0] = prev;
+  for (int k = 1; k < ng; k++) {
+    float2 r = S[k * stride];
+    float2 cp = cmulf(C[k], prev);
+    prev = cmulf(make_float2(r.x - cp.x, r.y - cp.y), CB[k]);
+    S[k * stride] = prev;
+  }
+  float2 next = prev;
+  for (int k = ng - 2; k >= 0; k--) {
+    float2 v = S[k * stride];
+    float2 cw = cmulf(CW[k + 1], next);
+    v.x -= cw.x;
+    v.y -= cw.y;
+    S[k * stride] = v;
+    next = v;
+  }
+}
+
+// (I + c D) along a line of S with stride, in place, with a rolling register window
+__device__ __forceinline__ void stencil_line(float2 *S, int stride, int ng, float cs) {
+  float2 prev = make_float2(0.f, 0.f), cur = S[0];
+  for (int k = 0; k < ng; k++) {
+    float2 next = (k + 1 < ng) ? S[(k + 1) * stride] : make_float2(0.f, 0.f);
+    float2 l = lapf(k > 0, k < ng - 1, prev, cur, next);
+    S[k * stride] = stencil(cs, cur, l);
+    prev = cur;
+    cur = next;
+  }
+}
+
+// Adds the deposited source of beam slice `is` to S with shared-memory atomics.
+__device__ __forceinline__ void deposit_smem(const StepConstF &sc, const FieldStepF &fs,
+                                             const PtrsF &p, float2 *S, int is, int np, int ng) {
+  float cur = (float)p.current[is];
+  float scl = fs.dep_scl * cur;
+  size_t base = (size_t)is * np;
+  constexpr int U = 4;  // particles per thread per round: their loads are issued together
+  for (int ip0 = threadIdx.x; ip0 < np; ip0 += U * blockDim.x) {
+    float xs[U], ys[U], gs[U];
+    double ths[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      int ip = ip0 + u * blockDim.x;
+      bool in = ip < np;
+      xs[u] = in ? p.x[base + ip] : 1e30f;
+      ys[u] = in ? p.y[base + ip] : 1e30f;
+      ths[u] = in ? p.theta[base + ip] : 0.0;
+      gs[u] = in ? p.dg[base + ip] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+    float x = xs[u], y = ys[u];
+    CellF c;
+    if (!ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x, y, c)) continue;
+    double th = ths[u];
+    float a = (float)fma(-rint(th * (1.0 / kTwoPi)), kTwoPi, th);
+    float g = (float)sc.gammaref + gs[u];
+    float dx = x - sc.ax, dy = y - sc.ay;
+    float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
+    float part = sqrtf(faw2) * scl / g;
+    float sn, co;
+    __sincosf(wrapf(fs.rharm * a), &sn, &co);
+    float cpx = sn * part, cpy = co * part;
+    float w = c.wx * c.wy;
+    atomicAdd(&S[c.i00].x, w * cpx);
+    atomicAdd(&S[c.i00].y, w * cpy);
+    w = (1.f - c.wx) * c.wy;
+    atomicAdd(&S[c.i10].x, w * cpx);
+    atomicAdd(&S[c.i10].y, w * cpy);
+    w = c.wx * (1.f - c.wy);
+    atomicAdd(&S[c.i01].x, w * cpx);
+    atomicAdd(&S[c.i01].y, w * cpy);
+    w = (1.f - c.wx) * (1.f - c.wy);
+    atomicAdd(&S[c.i11].x, w * cpx);
+    atomicAdd(&S[c.i11].y, w * cpy);
+    }
+  }
+}
+
+// Bounded wait on an mbarrier phase; returns false (and raises the device error
+// flag) if the phase does not complete within the iteration limit.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err) {
+  for (long long it = 0; it < (1LL << 22); it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  if (err) atomicExch(err, 2);
+  return false;
+}
+
+// Copies `count` float2 from global g to shared s with one TMA bulk copy for the
+// 16-byte aligned middle and plain loads for an 8-byte head / tail. The shared
+// copy is laid out so that s and g agree modulo 16 bytes (see the caller).
+__device__ __forceinline__ bool bulk_load(float2 *s, const float2 *g, int count, uint32_t bar,
+                                          int *err) {
+  uintptr_t ga = reinterpret_cast<uintptr_t>(g);
+  int head = (ga & 15) ? 1 : 0;
+  int body = (count - head) & ~1;
+  int tail = count - head - body;
+  if (threadIdx.x == 0) {
+    uint32_t bytes = (uint32_t)body * 8u;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    if (bytes) {
+      uint32_t dst = (uint32_t)__cvta_generic_to_shared(s + head);
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+          ::"r"(dst), "l"(g + head), "r"(bytes), "r"(bar)
+          : "memory");
+    }
+  }
+  if (head && threadIdx.x == 32) s[0] = g[0];
+  if (tail && threadIdx.x == 64) s[count - 1] = g[count - 1];
+  bool ok = mbar_wait(bar, 0, err);
+  __syncthreads();
+  return ok;
+}
+
+__device__ __forceinline__ void bulk_store(float2 *g, const float2 *s, int count) {
+  uintptr_t ga = reinterpret_cast<uintptr_t>(g);
+  int head = (ga & 15) ? 1 : 0;
+  int body = (count - head) & ~1;
+  int tail = count - head - body;
+  // make the generic-proxy writes to s visible to the bulk copy engine
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  if (threadIdx.x == 0 && body) {
+    uint32_t src = (uint32_t)__cvta_generic_to_shared(s + head);
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(g + head), "r"(src),
+                 "r"((uint32_t)body * 8u)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+  }
+  if (head && threadIdx.x == 32) g[0] = s[0];
+  if (tail && threadIdx.x == 64) g[count - 1] = s[count - 1];
+  if (threadIdx.x == 0 && body) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kFusedThreads, 1)
+    k_field_fused_f(StepConstF sc, int k, PtrsF p, float2 *__restrict__ field,
+                    const float2 *__restrict__ coef, int ns, int np, int ng, int deposit, int *err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ncell = ng * ng;
+  const FieldStepF &fs = sc.f[k];
+  int is = blockIdx.x;
+  int i = (is + fs.first) % ns;
+  float2 *u = field + (size_t)i * ncell;
+  // layout: [mbarrier 16 B][coefficients 3 ng][pad][S: ncell] with S congruent to u mod 16
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);
+  float2 *C = reinterpret_cast<float2 *>(smem_raw + 16);
+  float2 *CB = C + ng, *CW = CB + ng;
+  size_t soff = (16 + 3 * (size_t)ng * 8 + 15) & ~(size_t)15;
+  soff += reinterpret_cast<uintptr_t>(u) & 15;
+  float2 *S = reinterpret_cast<float2 *>(smem_raw + soff);
+  uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int t = threadIdx.x; t < 3 * ng; t += blockDim.x) C[t] = coef[t];
+  __syncthreads();
+  if (!bulk_load(S, u, ncell, bar_s, err)) return;
+  const float cs = fs.cstep;
+  const int tid = threadIdx.x;
+  if (tid < ng) stencil_line(S + tid, ng, ng, cs);  // column tid: (I + c Dy)
+  __syncthreads();
+  if (deposit) {
+    deposit_smem(sc, fs, p, S, is, np, ng);
+    __syncthreads();
+  }
+  if (tid < ng) thomas(S + tid * ng, 1, ng, C, CB, CW);  // row tid
+  __syncthreads();
+  if (tid < ng) stencil_line(S + tid * ng, 1, ng, cs);  // row tid: (I + c Dx)
+  __syncthreads();
+  if (deposit) {
+    deposit_smem(sc, fs, p, S, is, np, ng);
+    __syncthreads();
+  }
+  if (tid < ng) thomas(S + tid, ng, ng, C, CB, CW);  // column tid
+  __syncthreads();
+  bulk_store(u, S, ncell);
 }
 
 template <int BS>
@@ -544,6 +760,33 @@ void launch_diag_beam_mixed(const Launch &L, const DeviceBeam &b, double gammare
 
 void launch_diag_field_mixed(const Launch &L, const void *field, int ns, int ngrid, double *out) {
   k_diag_field_f<256><<<ns, 256, 0, (cudaStream_t)L.stream>>>((const float2 *)field, ngrid, out);
+}
+
+// shared memory of the fused kernel: mbarrier, coefficients, alignment slack, slice
+size_t fused_smem_bytes(int ng) {
+  return ((16 + 3 * (size_t)ng * 8 + 15) & ~(size_t)15) + 8 + (size_t)ng * ng * 8;
+}
+
+int fused_max_ngrid() {
+  int ng = 3;
+  while (fused_smem_bytes(ng + 1) <= 227u * 1024u) ng++;
+  return ng;
+}
+
+void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b,
+                              void *field, const void *coef, int ns, int np, int ngrid,
+                              int deposit) {
+  static unsigned long long configured = 0;  // one bit per device
+  size_t smem = fused_smem_bytes(ngrid);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !(configured & (1ull << dev))) {
+    cudaFuncSetAttribute(k_field_fused_f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    configured |= 1ull << dev;
+  }
+  PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
+  k_field_fused_f<<<ns, kFusedThreads, smem, (cudaStream_t)L.stream>>>(
+      sc, k, p, (float2 *)field, (const float2 *)coef, ns, np, ngrid, deposit, L.err);
 }
 
 }  // namespace g4

@@ -286,7 +286,9 @@ __global__ void __launch_bounds__(128) k_adi_x(const double2 *__restrict__ field
   size_t ncell = (size_t)ng * ng;
   int i = (ii + first) % ns;
   const double2 *u = field + (size_t)i * ncell + (size_t)iy * ng;
-  const double2 *s = src + (size_t)ii * ncell + (size_t)iy * ng;
+  // a null source means no deposition this step (outside the undulator or an even
+  // harmonic): the reference then solves with a zero source (FieldSolverADI.cpp:14-16)
+  const double2 *s = src ? src + (size_t)ii * ncell + (size_t)iy * ng : nullptr;
   double2 *w = tmp + (size_t)i * ncell + (size_t)iy * ng;
   bool hp = iy > 0, hn = iy < ng - 1;
   C2 cs = {0.0, cstep};
@@ -295,7 +297,8 @@ __global__ void __launch_bounds__(128) k_adi_x(const double2 *__restrict__ field
     C2 uc = ld(u + k);
     C2 un = hn ? ld(u + k + ng) : C2{0, 0};
     C2 us = hp ? ld(u + k - ng) : C2{0, 0};
-    C2 r = cadd(cadd(ld(s + k), uc), cmul(cs, lap(hp, hn, us, uc, un)));
+    C2 sv = s ? ld(s + k) : C2{0, 0};
+    C2 r = cadd(cadd(sv, uc), cmul(cs, lap(hp, hn, us, uc, un)));
     C2 v = (k == 0) ? cmul(r, ld(cf.cbet)) : cmul(csub(r, cmul(ld(cf.c + k), prev)), ld(cf.cbet + k));
     st(w + k, v);
     prev = v;
@@ -320,7 +323,7 @@ __global__ void __launch_bounds__(128) k_adi_y(double2 *__restrict__ field,
   size_t ncell = (size_t)ng * ng;
   int i = (ii + first) % ns;
   double2 *u = field + (size_t)i * ncell + ix;
-  const double2 *s = src + (size_t)ii * ncell + ix;
+  const double2 *s = src ? src + (size_t)ii * ncell + ix : nullptr;
   const double2 *w = tmp + (size_t)i * ncell + ix;
   bool hp = ix > 0, hn = ix < ng - 1;
   C2 cs = {0.0, cstep};
@@ -330,7 +333,8 @@ __global__ void __launch_bounds__(128) k_adi_y(double2 *__restrict__ field,
     C2 wc = ld(w + o);
     C2 wn = hn ? ld(w + o + 1) : C2{0, 0};
     C2 wp = hp ? ld(w + o - 1) : C2{0, 0};
-    C2 r = cadd(cadd(ld(s + o), wc), cmul(cs, lap(hp, hn, wp, wc, wn)));
+    C2 sv = s ? ld(s + o) : C2{0, 0};
+    C2 r = cadd(cadd(sv, wc), cmul(cs, lap(hp, hn, wp, wc, wn)));
     C2 v = (k == 0) ? cmul(r, ld(cf.cbet)) : cmul(csub(r, cmul(ld(cf.c + k), prev)), ld(cf.cbet + k));
     st(u + o, v);
     prev = v;

@@ -29,6 +29,13 @@ def rel_err(a, b):
     return float(np.max(np.abs(a - b)) / scale) if scale > 0 else float(np.max(np.abs(a - b)))
 
 
+def bunching_ok(got, ref, rel=1e-2, floor=1e-4):
+    """Bunching (|<exp(i theta)>|, between 0 and 1) within `rel` of the largest slice
+    value, with an absolute floor below the shot-noise level 1/sqrt(npart) of these
+    windows, where a relative comparison of near-zero bunching means nothing."""
+    return float(np.max(np.abs(np.asarray(got) - ref))) <= rel * float(np.max(np.abs(ref))) + floor
+
+
 def handle_for(g4gpu, ns, npart, ngrid, harm, gridmax, gammaref, precision, time_run, periodic):
     cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ngrid, harm=list(harm), gridmax=list(gridmax),
                        lambda0=1e-10, sample=1.0, gammaref=float(gammaref), precision=precision,
@@ -80,7 +87,7 @@ def test_mixed_steps_close_to_reference(lib, oracle, case):
     ref_p = g("s7_part")
     ref_f = g("s7_fields")
     ob = oracle.diag_beam(ref_p, 1)
-    assert rel_err(bd[:, 24], ob[:, 24]) < 1e-2, case
+    assert bunching_ok(bd[:, 24], ob[:, 24]), case
     for k in range(ref_f.shape[0]):
         of = oracle.diag_field(ref_f[k], float(g("gridmax")[k]), 1e-10, int(g("harm")[k]),
                                int(g("s7_first")[k]))
@@ -117,10 +124,22 @@ def test_diagnostics_match_oracle(lib, oracle):
         bd, fd = h.diag(nharm=3)
     ob = oracle.diag_beam(part, 3)
     of = oracle.diag_field(fld[0], 6e-5, 1e-10, 1, first)
+    # The GPU sums in a tree, the reference in sequence. Columns built as
+    # sqrt(<q^2> - <q>^2) cancel (energy spread: <g^2> ~ 1.3e8 against a variance of 4),
+    # which turns the last-bit difference of the sums into ~1e-8 relative: those get 1e-6.
+    # First moments of coordinates centred on zero (x, y, px, py) cancel in the sum
+    # as well: they are compared to 1e-12 of the coordinate's extent (the min/max columns).
+    second = {1, 3, 5, 8, 9, 10, 11, 12, 13}
+    extent = {2: (14, 15), 4: (18, 19), 6: (16, 17), 7: (20, 21)}
     for col in range(ob.shape[1]):
-        assert np.allclose(bd[:, col], ob[:, col], rtol=1e-10, atol=1e-14 * np.max(np.abs(ob[:, col])) + 1e-300), col
+        rtol = 1e-6 if col in second else 1e-10
+        atol = 1e-14 * np.max(np.abs(ob[:, col])) + 1e-300
+        if col in extent:
+            atol = 1e-12 * np.max(np.abs(ob[:, list(extent[col])]))
+        assert np.allclose(bd[:, col], ob[:, col], rtol=rtol, atol=atol), col
     for col in range(of.shape[1]):
-        assert np.allclose(fd[0][:, col], of[:, col], rtol=1e-10, atol=1e-12 * np.max(np.abs(of[:, col]))), col
+        rtol = 1e-8 if col in (2, 4) else 1e-10
+        assert np.allclose(fd[0][:, col], of[:, col], rtol=rtol, atol=1e-12 * np.max(np.abs(of[:, col]))), col
 
 
 def run_deck_fixture(lib, name, precision, every=1):
@@ -159,7 +178,7 @@ def test_example1_plain_matches_reference_every_step(lib):
 def test_example1_mixed_within_one_percent(lib):
     power, bunch, d = run_deck_fixture(lib, "example1.npz", 1, every=8)
     assert abs(power[-1] / d["power"][-1] - 1) < 1e-2
-    assert abs(bunch[-1] - d["bunching"][-1]) < 1e-2 * max(d["bunching"][-1], 1e-3)
+    assert bunching_ok(bunch[-1:], d["bunching"][-1:])
 
 
 def test_config0_plain_matches_reference(lib):
@@ -205,3 +224,66 @@ def test_run_before_load_is_an_error(lib):
         with pytest.raises(g4gpu.G4Error) as e:
             h.run(0, 5)
         assert e.value.code == 1
+
+
+@pytest.mark.parametrize("solver,filt", [(1, None), (2, (0.7, 0.9, 0.3))])
+@pytest.mark.parametrize("n", [25, 45])
+def test_fft_solver_plain_matches_oracle(lib, oracle, solver, filt, n):
+    """FieldSolverFFT (src/Core/FieldSolverFFT.cpp:9-114) on a time-dependent window
+    with two harmonics, against the oracle's restatement (pinned to numpy's FFT in
+    tests/test_oracle_pins.py; the reference's own FFT path needs FFTW)."""
+    import g4gpu
+    import g4cases as T
+    ns, npart = 5, 64
+    lat = T.undulator_lattice(1.7, 0.015, 6, 2, 1e-10, 11357.8, quad_k1=1.5, quad_l=0.08)
+    part = g4gpu.host_load_beam(T.slice_params(ns, 11357.8, 2.0, 0.4e-6, 15.0), 0, npart, 4, 7, 1, 1e-10, 1.0)
+    cur = np.full(ns, 3000.0)
+    g1 = g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e5, 20e-6), 6e-5, n)
+    g3 = g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e3, 12e-6, harm=3), 4e-5, n)
+    fld = np.stack([np.stack([g1 * (1 + 0.3j * k) for k in range(ns)]),
+                    np.stack([g3 * (1 - 0.2j * k) for k in range(ns)])])
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=n, harm=[1, 3], gridmax=[6e-5, 4e-5], lambda0=1e-10,
+                       sample=1.0, gammaref=11357.8, precision=0, solver=g4gpu.SOLVER_FFT,
+                       source_filter=int(solver == 2), time_run=1)
+    if filt:
+        cfg.xcut, cfg.ycut, cfg.sigmoid = filt
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam(part, cur)
+        h.load_field(0, fld[0])
+        h.load_field(1, fld[1])
+        h.run(0, lat.shape[0])
+        p = h.get_beam()
+        f0, first0, _ = h.get_field(0)
+        f1, _, _ = h.get_field(1)
+        assert h.kernel_stats()["fft"][0] == 3 * 2 * lat.shape[0]
+    rp, rf, rfirst, _ = oracle.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, [1, 3], [6e-5, 4e-5], fld, [0, 0],
+                                         solver=solver, filt=filt)
+    assert first0 == rfirst[0]
+    assert rel_err(f0, rf[0]) < 1e-9 and rel_err(f1, rf[1]) < 1e-9
+    for col in range(6):
+        assert rel_err(p[..., col], rp[..., col]) < 1e-9
+
+
+def test_fft_solver_mixed_within_one_percent(lib, oracle):
+    import g4gpu
+    import g4cases as T
+    ns, npart, n = 6, 256, 51
+    lat = T.undulator_lattice(1.7, 0.015, 30, 1, 1e-10, 11357.8)
+    part = g4gpu.host_load_beam(T.slice_params(ns, 11357.8, 2.0, 0.4e-6, 15.0), 0, npart, 4, 7, 1, 1e-10, 1.0)
+    cur = np.full(ns, 3000.0)
+    g1 = g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e6, 20e-6), 1e-4, n)
+    fld = np.stack([g1 * (1 + 0.3j * k) for k in range(ns)])
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=n, gridmax=1e-4, lambda0=1e-10, sample=1.0,
+                       gammaref=11357.8, precision=1, solver=g4gpu.SOLVER_FFT, time_run=1)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam(part, cur)
+        h.load_field(0, fld)
+        h.run(0, lat.shape[0])
+        bd, fd = h.diag(1)
+    rp, rf, rfirst, _ = oracle.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, [1], [1e-4], fld[None], [0], solver=1)
+    of = oracle.diag_field(rf[0], 1e-4, 1e-10, 1, int(rfirst[0]))
+    ob = oracle.diag_beam(rp, 1)
+    assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-2
+    assert bunching_ok(bd[:, 24], ob[:, 24])

@@ -110,3 +110,56 @@ def test_example1_deck_final_power(oracle):
     assert same(df[0, 0], d["power"][-1], rtol=1e-12)
     # the reference's CI golden value (examples/Example1-SteadyState/TEST_power.py:14,17)
     assert abs(df[0, 0] / 0.932785e9 - 1) < 0.3
+
+
+def _k2_and_sigmoid(n, dgrid, xks, xc=1.0, yc=1.0, sig=1.0):
+    """Im(K2) and the source filter on the FFT index, FieldSolverFFT.cpp:131-145."""
+    dk = 4.0 * np.arcsin(1.0) / (n * dgrid)
+    shift = -0.5 * (n - 1)
+    k2 = np.zeros((n, n))
+    sg = np.zeros((n, n))
+    for iy in range(n):
+        dy = iy + shift
+        y = dy / n / yc
+        for ix in range(n):
+            dx = ix + shift
+            x = dx / n / xc
+            iiy, iix = (iy + (n + 1) // 2) % n, (ix + (n + 1) // 2) % n
+            k2[iiy, iix] = -(dx * dx + dy * dy) * dk * dk / 2.0 / xks
+            sg[iiy, iix] = 1.0 / (1.0 + np.exp((np.sqrt(x * x + y * y) - 1) / sig))
+    return k2, sg
+
+
+@pytest.mark.parametrize("n", [15, 16, 21])
+def test_fft_solver_matches_numpy(oracle, n):
+    """The FFT solver of the oracle (the reference's FFTW path cannot be built here:
+    no FFTW) against numpy's pocketfft: u' = IFFT(FFT(u) exp(K2 dz)) + 2 src, and the
+    filtered form IFFT(FFT(u) exp(K2 dz) + 2 FFT(src) sigmoid)."""
+    import g4cases as T
+    rng = np.random.default_rng(n)
+    ns, gm, dz = 2, 5e-5, 0.015
+    u = (rng.standard_normal((1, ns, n * n)) + 1j * rng.standard_normal((1, ns, n * n))) * 1e3
+    dgrid = 2 * gm / (n - 1)
+    xks = 4.0 * np.arcsin(1.0) / 1e-10
+    k2, sg = _k2_and_sigmoid(n, dgrid, xks, 0.7, 0.9, 0.3)
+    prop = np.exp(1j * k2 * dz)
+    # a drift step: no source
+    lat = T.undulator_lattice(1.7, 0.015, 1, 1, 1e-10, 11357.8)
+    lat[0, T.C["aw"]] = 0.0
+    part = oracle.load_beam(T.slice_params(ns, 11357.8, 2.0, 0.4e-6, 15.0), 0, 32, 4, 1, 0, 1e-10, 1.0)
+    cur = np.full(ns, 3000.0)
+    _, f1, _, _ = oracle.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, [1], [gm], u, [0], stages=2, solver=1)
+    for s in range(ns):
+        want = np.fft.ifft2(np.fft.fft2(u[0, s].reshape(n, n)) * prop).ravel()
+        assert np.allclose(f1[0, s], want, rtol=0, atol=1e-12 * np.abs(want).max())
+    # an undulator step: source deposited; the filtered solve against numpy
+    lat[0, T.C["aw"]] = 1.7
+    _, fu, _, _ = oracle.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, [1], [gm], u, [0], stages=2, solver=1)
+    _, ff, _, _ = oracle.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, [1], [gm], u, [0], stages=2, solver=2,
+                                   filt=[0.7, 0.9, 0.3])
+    for s in range(ns):
+        free = np.fft.ifft2(np.fft.fft2(u[0, s].reshape(n, n)) * prop)
+        src = (fu[0, s].reshape(n, n) - free) / 2
+        assert np.abs(src).max() > 0
+        want = np.fft.ifft2(np.fft.fft2(u[0, s].reshape(n, n)) * prop + 2 * np.fft.fft2(src) * sg).ravel()
+        assert np.allclose(ff[0, s], want, rtol=0, atol=1e-10 * np.abs(want).max())
