@@ -7,8 +7,11 @@ and g++. The library is built in-tree and is what include/g4gpu.h describes.
   kernels_mixed.cu   mixed-precision kernels
   kernels_util.cu    layout conversions
   kernels_fft.cu     FFT field solver (mixed-radix Stockham, FP64 and FP32)
+  kernels_mlp.cu     BF16 tensor-core MLP of the learned closure (training and inference)
+  kernels_closure.cu per-slice features and corrections of the learned closure
   g4gpu_api.cpp      C ABI, host bookkeeping (-ffp-contract=off)
   host_loading.cpp   bit-exact host loading (-ffp-contract=off)
+  g4gpu_learned.cpp  learned closure: MLP object, features / corrections, coarse-step driver
 """
 import concurrent.futures as cf
 import os
@@ -44,8 +47,11 @@ def _units():
         ("kernels_mixed.cu", cu_common + ["-use_fast_math"]),
         ("kernels_util.cu", cu_common),
         ("kernels_fft.cu", cu_common),
+        ("kernels_mlp.cu", cu_common),
+        ("kernels_closure.cu", cu_common + ["-use_fast_math"]),
         ("g4gpu_api.cpp", cxx_common),
         ("host_loading.cpp", cxx_common + ["-pthread"]),
+        ("g4gpu_learned.cpp", cxx_common),
     ]
 
 

@@ -16,11 +16,13 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <utility>
 #include <vector>
 
 #include "g4gpu.h"
+#include "g4gpu_ctx.h"
 #include "g4gpu_internal.h"
 
 using g4::StepConst;
@@ -33,51 +35,6 @@ void launch_soa_to_aos(void *stream, const void *const *soa, double *aos, int mi
                        size_t n);
 void launch_convert_field(void *stream, const void *in, void *out, size_t n, int to_float);
 }
-
-struct g4gpu_ctx {
-  g4gpu_config cfg{};
-  cudaStream_t stream = nullptr;
-  std::string err;
-  bool mixed = false;
-  size_t csize = 16;  // bytes per complex field value
-  size_t rsize = 8;   // bytes per particle coordinate other than theta
-
-  g4::DeviceBeam beam{};
-  void *field[G4GPU_MAX_FIELDS] = {};
-  void *src[G4GPU_MAX_FIELDS] = {};
-  void *tmp = nullptr;
-  void *coef = nullptr;      // [nset][3][ngrid] complex of the field type
-  size_t coef_bytes = 0;
-  // FFT solver tables per field: roots of unity [n], Im(K2) and the sigmoid [n^2]
-  void *fft_roots[G4GPU_MAX_FIELDS] = {};
-  void *fft_k2[G4GPU_MAX_FIELDS] = {};
-  void *fft_sig[G4GPU_MAX_FIELDS] = {};
-  g4::FFTPlan fft_plan{};
-  int *derr = nullptr;
-  double *ddiag = nullptr;
-  size_t ddiag_bytes = 0;
-  void *stage = nullptr;     // AoS staging buffer for host transfers
-  size_t stage_bytes = 0;
-  size_t bytes = 0;
-
-  int nsteps = 0;
-  std::vector<StepConst> steps;
-  std::vector<double> slip;
-  int first[G4GPU_MAX_FIELDS] = {};
-  double accuslip[G4GPU_MAX_FIELDS] = {};
-  bool beam_loaded = false;
-  bool field_loaded[G4GPU_MAX_FIELDS] = {};
-
-  bool prof = false;
-  long long launches[G4GPU_K_NCLASS] = {};
-  double ms[G4GPU_K_NCLASS] = {};
-  struct Pending {
-    int cls;
-    cudaEvent_t a, b;
-  };
-  std::vector<Pending> pending;
-  std::vector<cudaEvent_t> pool;
-};
 
 namespace {
 
@@ -123,14 +80,14 @@ struct Timed {
   cudaEvent_t a = nullptr, b = nullptr;
   Timed(g4gpu_handle h_, int cls_, int kernels = 1) : h(h_), cls(cls_) {
     h->launches[cls] += kernels;
-    if (h->prof) {
+    if (h->prof && !h->capturing) {
       a = take_event(h);
       b = take_event(h);
       cudaEventRecord(a, h->stream);
     }
   }
   ~Timed() {
-    if (h->prof) {
+    if (h->prof && a) {
       cudaEventRecord(b, h->stream);
       h->pending.push_back({cls, a, b});
     }
@@ -269,6 +226,11 @@ int fft_tables(g4gpu_handle h) {
 
 }  // namespace
 
+int g4_fail(g4gpu_handle h, int code, const std::string &msg) { return fail(h, code, msg); }
+int g4_cuda_fail(g4gpu_handle h, cudaError_t e, const char *what) { return cuda_fail(h, e, what); }
+int g4_alloc(g4gpu_handle h, void **p, size_t n) { return alloc(h, p, n); }
+int g4_check_device_flag(g4gpu_handle h) { return check_device_flag(h); }
+
 extern "C" {
 
 void g4gpu_config_defaults(g4gpu_config *cfg) {
@@ -367,7 +329,8 @@ void g4gpu_destroy(g4gpu_handle h) {
   cudaSetDevice(h->cfg.device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   void *ptrs[] = {h->beam.gamma, h->beam.theta, h->beam.x, h->beam.y, h->beam.px, h->beam.py,
-                  h->beam.current, h->tmp, h->coef, h->derr, h->ddiag, h->stage};
+                  h->beam.current, h->tmp, h->coef, h->derr, h->ddiag, h->stage,
+                  h->closure_basis, h->closure_feat, h->closure_corr};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
@@ -380,6 +343,8 @@ void g4gpu_destroy(g4gpu_handle h) {
     cudaEventDestroy(p.b);
   }
   for (auto ev : h->pool) cudaEventDestroy(ev);
+  for (auto &g : h->graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -606,14 +571,9 @@ int g4gpu_get_field(g4gpu_handle h, int ifld, double *field, int *first, double 
   return check_device_flag(h);
 }
 
-int g4gpu_run(g4gpu_handle h, int istep0, int nsteps, int stages) {
-  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
-  if (istep0 < 0 || nsteps < 0 || istep0 + nsteps > h->nsteps)
-    return fail(h, G4GPU_ERR_ARG, "step range outside the lattice");
-  if (!h->beam_loaded) return fail(h, G4GPU_ERR_STATE, "no beam loaded");
-  for (int k = 0; k < h->cfg.nfield; k++)
-    if (!h->field_loaded[k]) return fail(h, G4GPU_ERR_STATE, "a field is not loaded");
-  cudaSetDevice(h->cfg.device);
+// Queues the kernels and copies of steps istep0 .. istep0+nsteps-1 on the handle's
+// stream and advances the host-side ring state (first, accuslip) accordingly.
+static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
   const g4gpu_config &c = h->cfg;
   int ns = c.nslice, np = c.npart, ng = c.ngrid;
   size_t ncell = (size_t)ng * ng;
@@ -631,13 +591,14 @@ int g4gpu_run(g4gpu_handle h, int istep0, int nsteps, int stages) {
       g4::StepConstF scf = g4::to_float(sc, np);
       if (do_push) {
         Timed t(h, G4GPU_K_PUSH);
-        g4::launch_push_mixed(L, scf, h->beam, h->field, nullptr, ns, np, ng, 0);
+        g4::launch_push_mixed(L, scf, h->beam, h->field, nullptr, ns, np, ng, 0, h->push_block);
       }
       if (do_field) {
         for (int k = 0; k < c.nfield; k++) {
           const char *cb = (const char *)h->coef + (size_t)sc.f[k].coef * 3 * ng * h->csize;
           Timed t(h, G4GPU_K_ADI_X);
-          g4::launch_field_fused_mixed(L, scf, k, h->beam, h->field[k], cb, ns, np, ng, sc.f[k].dep_on);
+          g4::launch_field_fused_mixed(L, scf, k, h->beam, h->field[k], cb, h->tmp, ns, np, ng,
+                                       sc.f[k].dep_on, h->field_threads);
         }
       }
     } else {
@@ -649,9 +610,11 @@ int g4gpu_run(g4gpu_handle h, int istep0, int nsteps, int stages) {
     if (do_push) {
       Timed t(h, G4GPU_K_PUSH);
       if (h->mixed)
-        g4::launch_push_mixed(L, scf, h->beam, h->field, h->src, ns, np, ng, do_field && any_dep);
+        g4::launch_push_mixed(L, scf, h->beam, h->field, h->src, ns, np, ng, do_field && any_dep,
+                              h->push_block);
       else
-        g4::launch_push_plain(L, sc, h->beam, h->field, h->src, ns, np, ng, do_field && any_dep);
+        g4::launch_push_plain(L, sc, h->beam, h->field, h->src, ns, np, ng, do_field && any_dep,
+                              h->push_block);
     } else if (do_field && any_dep) {
       Timed t(h, G4GPU_K_PUSH);
       if (h->mixed)
@@ -707,6 +670,69 @@ int g4gpu_run(g4gpu_handle h, int istep0, int nsteps, int stages) {
       }
     }
   }
+  return G4GPU_OK;
+}
+
+int g4gpu_run(g4gpu_handle h, int istep0, int nsteps, int stages) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (istep0 < 0 || nsteps < 0 || istep0 + nsteps > h->nsteps)
+    return fail(h, G4GPU_ERR_ARG, "step range outside the lattice");
+  if (!h->beam_loaded) return fail(h, G4GPU_ERR_STATE, "no beam loaded");
+  for (int k = 0; k < h->cfg.nfield; k++)
+    if (!h->field_loaded[k]) return fail(h, G4GPU_ERR_STATE, "a field is not loaded");
+  cudaSetDevice(h->cfg.device);
+  if (!h->graph_mode || nsteps == 0) return enqueue_steps(h, istep0, nsteps, stages);
+
+  // Graph mode: the whole step range is one CUDA graph, captured the first time a
+  // range starts from a given ring state and replayed afterwards. The kernels take
+  // the ring start by value, so a graph is valid for exactly that starting state.
+  g4gpu_ctx::GraphKey key{istep0, nsteps, stages, h->push_block, h->field_threads, {}};
+  for (int k = 0; k < h->cfg.nfield; k++) {
+    long long bits;
+    std::memcpy(&bits, &h->accuslip[k], sizeof(bits));
+    key.state.push_back(h->first[k]);
+    key.state.push_back(bits);
+  }
+  auto it = h->graphs.find(key);
+  if (it == h->graphs.end()) {
+    long long before[G4GPU_K_NCLASS];
+    std::memcpy(before, h->launches, sizeof(before));
+    cudaGraph_t graph = nullptr;
+    G4_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    h->capturing = true;
+    int rc = enqueue_steps(h, istep0, nsteps, stages);
+    h->capturing = false;
+    cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamEndCapture");
+    g4gpu_ctx::GraphEntry ent;
+    e = cudaGraphInstantiate(&ent.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGraphInstantiate");
+    for (int k = 0; k < h->cfg.nfield; k++) {
+      ent.end_first.push_back(h->first[k]);
+      ent.end_accuslip.push_back(h->accuslip[k]);
+    }
+    for (int c = 0; c < G4GPU_K_NCLASS; c++) ent.launches[c] = h->launches[c] - before[c];
+    // the capture advanced the counters and the ring state without running anything
+    std::memcpy(h->launches, before, sizeof(before));
+    it = h->graphs.emplace(key, ent).first;
+  }
+  G4_CUDA(h, cudaGraphLaunch(it->second.exec, h->stream));
+  for (int k = 0; k < h->cfg.nfield; k++) {
+    h->first[k] = it->second.end_first[k];
+    h->accuslip[k] = it->second.end_accuslip[k];
+  }
+  for (int c = 0; c < G4GPU_K_NCLASS; c++) h->launches[c] += it->second.launches[c];
+  return G4GPU_OK;
+}
+
+int g4gpu_set_graph_mode(g4gpu_handle h, int on) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  h->graph_mode = on != 0;
   return G4GPU_OK;
 }
 
@@ -868,5 +894,222 @@ int g4gpu_reset_stats(g4gpu_handle h) {
 }
 
 size_t g4gpu_device_bytes(g4gpu_handle h) { return h ? h->bytes : 0; }
+
+// ---- launch-shape tuning -----------------------------------------------------
+
+namespace {
+struct TuneKey {
+  int device, precision, npart, ngrid, nfield, solver;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(device, precision, npart, ngrid, nfield, solver) <
+           std::tie(o.device, o.precision, o.npart, o.ngrid, o.nfield, o.solver);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int, int>> g_tune;
+
+// device copies of everything a step modifies, to undo the tuning steps
+struct StateBackup {
+  std::vector<std::pair<void *, void *>> bufs;  // (live, copy)
+  std::vector<size_t> sizes;
+  int first[G4GPU_MAX_FIELDS];
+  double accuslip[G4GPU_MAX_FIELDS];
+};
+}  // namespace
+
+static int backup_state(g4gpu_handle h, StateBackup &b) {
+  const g4gpu_config &c = h->cfg;
+  size_t np = (size_t)c.nslice * c.npart, nf = (size_t)c.nslice * c.ngrid * c.ngrid * h->csize;
+  std::vector<std::pair<void *, size_t>> live = {
+      {h->beam.gamma, np * h->rsize}, {h->beam.theta, np * 8}, {h->beam.x, np * h->rsize},
+      {h->beam.y, np * h->rsize},     {h->beam.px, np * h->rsize}, {h->beam.py, np * h->rsize}};
+  for (int k = 0; k < c.nfield; k++) live.push_back({h->field[k], nf});
+  for (auto &l : live) {
+    void *cp = nullptr;
+    cudaError_t e = cudaMalloc(&cp, l.second);
+    if (e != cudaSuccess) return cuda_fail(h, e, "autotune backup");
+    G4_CUDA(h, cudaMemcpyAsync(cp, l.first, l.second, cudaMemcpyDeviceToDevice, h->stream));
+    b.bufs.push_back({l.first, cp});
+    b.sizes.push_back(l.second);
+  }
+  std::memcpy(b.first, h->first, sizeof(b.first));
+  std::memcpy(b.accuslip, h->accuslip, sizeof(b.accuslip));
+  return G4GPU_OK;
+}
+
+static void restore_state(g4gpu_handle h, StateBackup &b, bool release) {
+  for (size_t i = 0; i < b.bufs.size(); i++) {
+    cudaMemcpyAsync(b.bufs[i].first, b.bufs[i].second, b.sizes[i], cudaMemcpyDeviceToDevice, h->stream);
+    if (release) {
+      cudaStreamSynchronize(h->stream);
+      cudaFree(b.bufs[i].second);
+    }
+  }
+  std::memcpy(h->first, b.first, sizeof(b.first));
+  std::memcpy(h->accuslip, b.accuslip, sizeof(b.accuslip));
+}
+
+extern "C" int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_threads) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (!h->beam_loaded || h->nsteps < 1) return fail(h, G4GPU_ERR_STATE, "load a lattice and a beam first");
+  for (int k = 0; k < h->cfg.nfield; k++)
+    if (!h->field_loaded[k]) return fail(h, G4GPU_ERR_STATE, "a field is not loaded");
+  cudaSetDevice(h->cfg.device);
+  const g4gpu_config &c = h->cfg;
+  TuneKey key{c.device, c.precision, c.npart, c.ngrid, c.nfield, c.solver};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      h->push_block = it->second.first;
+      h->field_threads = it->second.second;
+      if (push_block) *push_block = h->push_block;
+      if (field_threads) *field_threads = h->field_threads;
+      return G4GPU_OK;
+    }
+  }
+  // a representative step: the first one inside an undulator, if any
+  int istep = 0;
+  for (int i = 0; i < h->nsteps; i++)
+    if (h->steps[i].aw > 0) {
+      istep = i;
+      break;
+    }
+  StateBackup b;
+  int rc = backup_state(h, b);
+  if (rc) return rc;
+  bool fused = h->mixed && c.solver == G4GPU_SOLVER_ADI && c.ngrid <= g4::fused_max_ngrid();
+  std::vector<int> pushes = {128, 256, 512};
+  std::vector<int> fields = {512};
+  if (fused) {
+    fields.clear();
+    int lo = (2 * c.ngrid + 31) / 32 * 32;
+    for (int t : {lo, 512, 768, 1024})
+      if (t >= lo && std::find(fields.begin(), fields.end(), t) == fields.end()) fields.push_back(t);
+  }
+  bool saved_graph = h->graph_mode, saved_prof = h->prof;
+  h->graph_mode = false;
+  h->prof = false;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto time_step = [&](int pb, int ft, float *ms) -> int {
+    h->push_block = pb;
+    h->field_threads = ft;
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {  // first repetition warms up
+      restore_state(h, b, false);
+      cudaEventRecord(e0, h->stream);
+      int r = enqueue_steps(h, istep, 1, G4GPU_STAGE_ALL);
+      if (r) return r;
+      cudaEventRecord(e1, h->stream);
+      cudaEventSynchronize(e1);
+      float t = 0;
+      cudaEventElapsedTime(&t, e0, e1);
+      if (rep > 0 && t < best) best = t;
+    }
+    *ms = best;
+    return G4GPU_OK;
+  };
+  int best_pb = 256, best_ft = fields[0];
+  float best_ms = 1e30f;
+  for (int pb : pushes) {
+    float ms;
+    if ((rc = time_step(pb, best_ft, &ms))) break;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_pb = pb;
+    }
+  }
+  if (!rc && fields.size() > 1) {
+    best_ms = 1e30f;
+    for (int ft : fields) {
+      float ms;
+      if ((rc = time_step(best_pb, ft, &ms))) break;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_ft = ft;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  restore_state(h, b, true);
+  h->graph_mode = saved_graph;
+  h->prof = saved_prof;
+  std::memset(h->launches, 0, sizeof(h->launches));
+  if (rc) return rc;
+  h->push_block = best_pb;
+  h->field_threads = best_ft;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = {best_pb, best_ft};
+  }
+  if (push_block) *push_block = best_pb;
+  if (field_threads) *field_threads = best_ft;
+  return check_device_flag(h);
+}
+
+// ---- batched ensembles ---------------------------------------------------------
+
+struct g4gpu_batch_ctx {
+  std::vector<g4gpu_handle> members;
+};
+
+extern "C" int g4gpu_batch_create(int nrun, const g4gpu_config *cfgs, g4gpu_batch *out) {
+  if (!out || !cfgs || nrun < 1) return fail(nullptr, G4GPU_ERR_ARG, "bad batch arguments");
+  *out = nullptr;
+  g4gpu_batch b = new g4gpu_batch_ctx;
+  for (int i = 0; i < nrun; i++) {
+    g4gpu_handle h = nullptr;
+    int rc = g4gpu_create(&cfgs[i], &h);
+    if (rc) {
+      for (auto m : b->members) g4gpu_destroy(m);
+      delete b;
+      return rc;
+    }
+    h->graph_mode = true;
+    b->members.push_back(h);
+  }
+  *out = b;
+  return G4GPU_OK;
+}
+
+extern "C" void g4gpu_batch_destroy(g4gpu_batch b) {
+  if (!b) return;
+  for (auto m : b->members) g4gpu_destroy(m);
+  delete b;
+}
+
+extern "C" g4gpu_handle g4gpu_batch_member(g4gpu_batch b, int i) {
+  if (!b || i < 0 || i >= (int)b->members.size()) return nullptr;
+  return b->members[i];
+}
+
+extern "C" int g4gpu_batch_run(g4gpu_batch b, int istep0, int nsteps, int stages) {
+  if (!b || istep0 < 0 || nsteps < 0) return fail(nullptr, G4GPU_ERR_ARG, "bad batch arguments");
+  for (auto m : b->members) {
+    int n = std::min(nsteps, m->nsteps - istep0);
+    if (n <= 0) continue;
+    int rc = g4gpu_run(m, istep0, n, stages);
+    if (rc) {
+      fail(nullptr, rc, std::string("batch member: ") + m->err);
+      return rc;
+    }
+  }
+  return G4GPU_OK;
+}
+
+extern "C" int g4gpu_batch_synchronize(g4gpu_batch b) {
+  if (!b) return fail(nullptr, G4GPU_ERR_ARG, "null batch");
+  for (auto m : b->members) {
+    int rc = g4gpu_synchronize(m);
+    if (rc) {
+      fail(nullptr, rc, std::string("batch member: ") + m->err);
+      return rc;
+    }
+  }
+  return G4GPU_OK;
+}
 
 }  // extern "C"

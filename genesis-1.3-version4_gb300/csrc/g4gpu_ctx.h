@@ -1,0 +1,96 @@
+// The handle structure behind g4gpu_handle, shared by the host translation units
+// (g4gpu_api.cpp, g4gpu_learned.cpp). Not part of the ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "g4gpu.h"
+#include "g4gpu_internal.h"
+
+struct g4gpu_mlp_ctx;
+
+struct g4gpu_ctx {
+  g4gpu_config cfg{};
+  cudaStream_t stream = nullptr;
+  std::string err;
+  bool mixed = false;
+  size_t csize = 16;  // bytes per complex field value
+  size_t rsize = 8;   // bytes per particle coordinate other than theta
+
+  g4::DeviceBeam beam{};
+  void *field[G4GPU_MAX_FIELDS] = {};
+  void *src[G4GPU_MAX_FIELDS] = {};
+  void *tmp = nullptr;
+  void *coef = nullptr;      // [nset][3][ngrid] complex of the field type
+  size_t coef_bytes = 0;
+  // FFT solver tables per field: roots of unity [n], Im(K2) and the sigmoid [n^2]
+  void *fft_roots[G4GPU_MAX_FIELDS] = {};
+  void *fft_k2[G4GPU_MAX_FIELDS] = {};
+  void *fft_sig[G4GPU_MAX_FIELDS] = {};
+  g4::FFTPlan fft_plan{};
+  int *derr = nullptr;
+  double *ddiag = nullptr;
+  size_t ddiag_bytes = 0;
+  void *stage = nullptr;     // AoS staging buffer for host transfers
+  size_t stage_bytes = 0;
+  size_t bytes = 0;
+
+  int nsteps = 0;
+  std::vector<g4::StepConst> steps;
+  std::vector<double> slip;
+  int first[G4GPU_MAX_FIELDS] = {};
+  double accuslip[G4GPU_MAX_FIELDS] = {};
+  bool beam_loaded = false;
+  bool field_loaded[G4GPU_MAX_FIELDS] = {};
+
+  // launch shapes (chosen by g4gpu_autotune, defaults otherwise)
+  int push_block = 256;
+  int field_threads = 512;
+
+  // captured step sequences, keyed by the step range and the ring state they start from
+  bool graph_mode = false;
+  struct GraphKey {
+    int istep0, nsteps, stages, push_block, field_threads;
+    std::vector<long long> state;  // first[] and the bit patterns of accuslip[]
+    bool operator<(const GraphKey &o) const {
+      return std::tie(istep0, nsteps, stages, push_block, field_threads, state) <
+             std::tie(o.istep0, o.nsteps, o.stages, o.push_block, o.field_threads, o.state);
+    }
+  };
+  struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<int> end_first;
+    std::vector<double> end_accuslip;
+    long long launches[G4GPU_K_NCLASS] = {};
+  };
+  std::map<GraphKey, GraphEntry> graphs;
+  bool capturing = false;
+
+  // learned closure (g4gpu_learned.cpp)
+  g4gpu_mlp_ctx *mlp = nullptr;
+  float *closure_basis = nullptr;  // [16][ngrid^2] Gauss-Hermite modes of field 0
+  float *closure_feat = nullptr;   // [nslice][32]
+  float *closure_corr = nullptr;   // [nslice][4]
+  float closure_u0 = 1.f, closure_c0 = 1.f;
+
+  bool prof = false;
+  long long launches[G4GPU_K_NCLASS] = {};
+  double ms[G4GPU_K_NCLASS] = {};
+  struct Pending {
+    int cls;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> pool;
+};
+
+// shared helpers of the host translation units (g4gpu_api.cpp)
+int g4_fail(g4gpu_handle h, int code, const std::string &msg);
+int g4_cuda_fail(g4gpu_handle h, cudaError_t e, const char *what);
+int g4_alloc(g4gpu_handle h, void **p, size_t n);
+int g4_check_device_flag(g4gpu_handle h);

@@ -64,6 +64,7 @@ struct StepConstF {
   float aw, ax, ay, kx, ky, gradx, grady;
   float xks, xku, delz, ztemp1;
   double autophase;
+  long long autophase_q;  // autophase as a Q32.32 turn count
   double gammaref;
   FieldStepF f[G4GPU_MAX_FIELDS];
 };
@@ -81,9 +82,10 @@ struct Launch {
 };
 
 // kernels_plain.cu (FP64, the reference's arithmetic)
+// block: threads per block of the push (128, 256 or 512)
 void launch_push_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,
                        void *const *field, void *const *src, int ns, int np, int ngrid,
-                       int deposit);
+                       int deposit, int block);
 void launch_deposit_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,
                           void *const *src, int ns, int np, int ngrid);
 // phase 0: implicit along x into tmp; phase 1: implicit along y back into the field
@@ -97,7 +99,7 @@ void launch_diag_field_plain(const Launch &L, const void *field, int ns, int ngr
 // kernels_mixed.cu (FP32 field, FP64 phase)
 void launch_push_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,
                        void *const *field, void *const *src, int ns, int np, int ngrid,
-                       int deposit);
+                       int deposit, int block);
 void launch_deposit_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,
                           void *const *src, int ns, int np, int ngrid);
 void launch_adi_mixed(const Launch &L, const StepConstF &sc, int k, int phase, void *field,
@@ -109,9 +111,11 @@ void launch_diag_field_mixed(const Launch &L, const void *field, int ns, int ngr
 // Fused deposition + ADI of one field in shared memory, one CTA per slice; usable
 // for ngrid <= fused_max_ngrid() (168: the FP32 slice must fit in 227 KB).
 int fused_max_ngrid();
+// scratch: [nslice][ngrid^2] float2 holding (I + c Dy) u between the two half steps
+// threads: CTA size, a multiple of 32 in [2 ngrid, 1024]
 void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b,
-                              void *field, const void *coef, int ns, int np, int ngrid,
-                              int deposit);
+                              void *field, const void *coef, void *scratch, int ns, int np,
+                              int ngrid, int deposit, int threads);
 
 // kernels_fft.cu: FFT field solver (FieldSolverFFT::FFT)
 struct FFTPlan {
@@ -124,6 +128,34 @@ int fft_max_ngrid(int mixed);
 void launch_fft_solve(void *stream, int mixed, void *field, const void *src, void *work,
                       const void *roots, const void *k2, const void *sig, int filtered, double delz,
                       const FFTPlan &pl, int ns, int first);
+
+// kernels_mlp.cu: BF16 tensor-core MLP (mma.sync m16n8k16, FP32 accumulation)
+void mlp_gemm_nt(void *stream, const void *A, const void *B, const float *bias, float *C, void *Cb, int M,
+                 int N, int K, int relu, int accumulate);
+void mlp_transpose_bf16(void *stream, const void *in, void *out, int rows, int cols);
+void mlp_to_bf16(void *stream, const float *in, void *out, size_t n);
+void mlp_relu_backward(void *stream, const float *dA, const float *Z, float *dZ, void *dZb, size_t n);
+void mlp_colsum(void *stream, const float *dZ, float *db, int rows, int cols);
+void mlp_mse(void *stream, const float *Y, const float *T, float *dY, void *dYb, int rows, int nout, int ldy,
+             float *loss);
+void mlp_adam(void *stream, float *w, const float *g, float *m, float *v, size_t n, float lr, float b1,
+              float b2, float eps, int t);
+
+// kernels_closure.cu: per-slice features and corrections of the learned closure
+constexpr int kClosureNin = 32;
+constexpr int kClosureNout = 4;
+void closure_features(void *stream, const void *theta, const void *gam, const double *current,
+                      const void *field, const float *basis, int mixed, double gref, int ns, int np, int ng,
+                      int first, float u0, float c0, float *out);
+void closure_apply(void *stream, void *theta, void *gam, void *field, const float *corr, int mixed, int ns,
+                   int np, int ng, int first);
+void closure_targets(void *stream, const void *th_c, const void *g_c, const void *f_c, const void *th_f,
+                     const void *g_f, const void *f_f, int mixed, int ns, int np, int ng, int first_c,
+                     int first_f, float *out);
+void closure_normalize(void *stream, const float *x, const float *mean, const float *stdv, void *yb, int rows,
+                       int n, int ld);
+void closure_denormalize(void *stream, const float *y, const float *scale, const float *shift, float *out,
+                         int rows, int n, int ld);
 
 // number of raw sums per slice written by the diagnostic kernels
 constexpr int kBeamSums = 12;   // g1 g2 x1 x2 y1 y2 px1 px2 py1 py2 xpx ypy

@@ -1,23 +1,36 @@
 // Mixed-precision kernels of the undulator step: FP32 field, ADI solve,
 // deposition and transverse optics; FP64 accumulated ponderomotive phase.
 //
-// Storage: theta FP64; gamma as the FP32 offset from gammaref (|offset| is a few
-// units, so FP32 resolves it to ~1e-7); x, y, px, py FP32; fields float2.
+// Storage: the accumulated phase theta is a 64-bit fixed-point count of turns
+// (Q32.32: integer turns in the high word, 2^-32 turn = 1.5e-9 rad in the low word);
+// gamma is the FP32 offset from gammaref (|offset| is a few units, so FP32 resolves
+// it to ~1e-7); x, y, px, py FP32; fields float2.
+//
+// Why fixed point and not FP64 for the phase: GB300 executes FP64 at 1/64 of the
+// FP32 rate, and the seven FP64 operations per particle of an FP64 phase (add the
+// step increment, reduce modulo 2 pi, convert) kept the FP64 pipe 55 % busy and
+// bounded the push. The 64-bit integer accumulates without any rounding, reduces
+// modulo 2 pi by taking the low word, and gives exact harmonics (h * low word mod
+// 2^32); its 1.5e-9 rad resolution is far below the ~5e-7 rad FP32 error of one
+// step's increment, so it loses nothing an FP64 phase would keep. Host copies
+// convert to and from the reference's FP64 theta.
+//
 // Numerics that differ in form (not in value) from the reference's FP64 code:
-//  * the phase is reduced to [-pi, pi] in FP64 once per step; the RK4 stages and
-//    the deposition work on FP32 offsets from it, and the step's FP32 increment is
-//    added to the FP64 phase;
+//  * the RK4 stages and the deposition work on FP32 offsets from the reduced phase;
 //  * 1 - 1/beta_par is evaluated as -eps / (s (1 + s)), s = sqrt(1 - eps), which
 //    has no cancellation in FP32 (eps ~ 1e-8);
 //  * RK4 is written in its classic form, algebraically identical to the reference's
 //    "pushp" sequence (BeamSolver.cpp:89-141).
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 
 #include "g4gpu_internal.h"
 
 namespace g4 {
+
+constexpr double kTwoPiHost = 6.283185307179586476925286766559;
 
 StepConstF to_float(const StepConst &s, int npart) {
   StepConstF f{};
@@ -44,6 +57,7 @@ StepConstF to_float(const StepConst &s, int npart) {
   f.delz = (float)s.delz;
   f.ztemp1 = (float)(-2. / s.xks);
   f.autophase = s.autophase;
+  f.autophase_q = (long long)llrint(s.autophase * (4294967296.0 / kTwoPiHost));
   f.gammaref = s.gammaref;
   for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
     const FieldStep &a = s.f[k];
@@ -68,6 +82,22 @@ namespace {
 
 constexpr double kTwoPi = 6.283185307179586476925286766559;
 constexpr float kTwoPiF = 6.283185307f;
+// radians per unit of the low word of the fixed-point phase
+constexpr float kRadPerUnit = 6.283185307f / 4294967296.0f;
+
+// phase in [-pi, pi) of a Q32.32 turn count, optionally times a harmonic number
+__device__ __forceinline__ float phase_of(long long t, unsigned h = 1u) {
+  return (float)(int)((unsigned)t * h) * kRadPerUnit;
+}
+// adds an FP32 angle increment (radians) to a Q32.32 turn count without rounding
+// the accumulator: the integer turns and the 32-bit fraction are added separately
+__device__ __forceinline__ long long add_phase(long long t, float dth) {
+  float turns = dth * (1.0f / 6.283185307f);
+  float k = floorf(turns);
+  float f = turns - k;  // exact, in [0, 1)
+  unsigned fu = (unsigned)(f * 4294967296.0f);
+  return t + ((long long)(int)k << 32) + (long long)fu;
+}
 constexpr float kInvTwoPiF = 0.159154943f;
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
@@ -152,7 +182,7 @@ __device__ __forceinline__ void ode_f(const StepConstF &sc, const float2 *rpart,
 
 struct PtrsF {
   float *dg, *x, *y, *px, *py;
-  double *theta;
+  long long *theta;  // Q32.32 turns
   const double *current;
   const float2 *field[G4GPU_MAX_FIELDS];
   float2 *src[G4GPU_MAX_FIELDS];
@@ -160,7 +190,7 @@ struct PtrsF {
 
 template <int NF>
 __device__ __forceinline__ void deposit_f(const StepConstF &sc, const PtrsF &p, size_t off, int ng,
-                                          float cur, float g, float a, float x, float y) {
+                                          float cur, float g, long long th, float x, float y) {
   float dx = x - sc.ax, dy = y - sc.ay;
   float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
   float base = sqrtf(faw2) / g;
@@ -173,7 +203,7 @@ __device__ __forceinline__ void deposit_f(const StepConstF &sc, const PtrsF &p, 
     if (!ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x, y, c)) continue;
     float part = base * fs.dep_scl * cur;
     float s, co;
-    __sincosf(wrapf(fs.rharm * a), &s, &co);
+    __sincosf(phase_of(th, (unsigned)fs.harm), &s, &co);
     float2 cp = make_float2(s * part, co * part);
     float2 *d = p.src[k] + off;
     float w = c.wx * c.wy;
@@ -188,7 +218,7 @@ __device__ __forceinline__ void deposit_f(const StepConstF &sc, const PtrsF &p, 
 }
 
 template <int NF>
-__global__ void __launch_bounds__(256) k_push_f(StepConstF sc, PtrsF p, int ns, int np, int ng,
+__global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, int np, int ng,
                                                 int deposit) {
   int is = blockIdx.y;
   int ip = blockIdx.x * blockDim.x + threadIdx.x;
@@ -196,14 +226,13 @@ __global__ void __launch_bounds__(256) k_push_f(StepConstF sc, PtrsF p, int ns, 
   size_t o = (size_t)is * np + ip;
   const float g0 = (float)sc.gammaref;
   float dg = p.dg[o], x = p.x[o], y = p.y[o], px = p.px[o], py = p.py[o];
-  double th = p.theta[o] + sc.autophase;
+  long long th = p.theta[o] + sc.autophase_q;
   size_t ncell = (size_t)ng * ng;
 
   transverse_f(sc, false, g0 + dg, x, y, px, py);
 
-  // phase reduced once in FP64; the step works on FP32 offsets from it
-  double nturn = rint(th * (1.0 / kTwoPi));
-  float a0 = (float)fma(-nturn, kTwoPi, th);
+  // the step works on FP32 offsets from the reduced phase
+  float a0 = phase_of(th);
 
   float ddx = x - sc.ax, ddy = y - sc.ay;
   float awloc = 1.f + 0.5f * (sc.kx * ddx * ddx + sc.ky * ddy * ddy) + sc.gradx * ddx + sc.grady * ddy;
@@ -240,8 +269,7 @@ __global__ void __launch_bounds__(256) k_push_f(StepConstF sc, PtrsF p, int ns, 
   float dgam = h6 * (k1g + 2.f * k2g + 2.f * k3g + k4g);
   float dth = h6 * (k1t + 2.f * k2t + 2.f * k3t + k4t);
   dg += dgam;
-  th += (double)dth;
-  float a1 = a0 + dth;
+  th = add_phase(th, dth);
   float g = g0 + dg;
 
   transverse_f(sc, true, g, x, y, px, py);
@@ -252,7 +280,7 @@ __global__ void __launch_bounds__(256) k_push_f(StepConstF sc, PtrsF p, int ns, 
   p.y[o] = y;
   p.px[o] = px;
   p.py[o] = py;
-  if (deposit) deposit_f<NF>(sc, p, (size_t)is * ncell, ng, (float)p.current[is], g, wrapf(a1), x, y);
+  if (deposit) deposit_f<NF>(sc, p, (size_t)is * ncell, ng, (float)p.current[is], g, th, x, y);
 }
 
 template <int NF>
@@ -261,10 +289,8 @@ __global__ void __launch_bounds__(256) k_deposit_f(StepConstF sc, PtrsF p, int n
   int ip = blockIdx.x * blockDim.x + threadIdx.x;
   if (ip >= np) return;
   size_t o = (size_t)is * np + ip;
-  double th = p.theta[o];
-  float a = (float)fma(-rint(th * (1.0 / kTwoPi)), kTwoPi, th);
   deposit_f<NF>(sc, p, (size_t)is * (size_t)ng * ng, ng, (float)p.current[is],
-                (float)sc.gammaref + p.dg[o], a, p.x[o], p.y[o]);
+                (float)sc.gammaref + p.dg[o], p.theta[o], p.x[o], p.y[o]);
 }
 
 struct CoefF {
@@ -388,7 +414,7 @@ __global__ void __launch_bounds__(128) k_adi_y_f(float2 *__restrict__ field,
 // (FieldSolverADI.cpp:19-51) added after, instead of before, the stencil term;
 // the deposition is recomputed from the particles for each half step instead of
 // being stored.
-constexpr int kFusedThreads = 512;
+constexpr int kFusedMaxThreads = 1024;
 
 __device__ __forceinline__ float2 cadd2(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 
@@ -397,84 +423,152 @@ __device__ __forceinline__ float2 stencil(float cs, float2 u, float2 l) {
   return make_float2(u.x - cs * l.y, u.y + cs * l.x);
 }
 
-__device__ __forceinline__ void thomas(float2 *S, int stride, int ng, const float2 *C,
-                                       const float2 *CB, const float2 *CW) {
-  float2 prev = cmulf(S[0], CB[0]);
-  S[0] = prev;
-  for (int k = 1; k < ng; k++) {
-    float2 r = S[k * stride];
-    float2 cp = cmulf(C[k], prev);
-    prev = cmulf(make_float2(r.x - cp.x, r.y - cp.y), CB[k]);
-    S[k * stride] = prev;
+// Tridiagonal solve of one line of S (stride between elements) by two threads,
+// eliminating from both ends at once ("burn at both ends"). The matrix
+// (I - c D), D the Dirichlet second difference, is the one of tridagx / tridagy
+// (FieldSolverADI.cpp:94-122, coefficients :125-182): symmetric Toeplitz, hence
+// persymmetric, so the upward elimination uses the same cbet / cwet tables as the
+// downward one, indexed from the far end. Thread `up` == 0 eliminates rows 0..m-1,
+// thread 1 rows n-1..m+1; they exchange their last values (lanes 2l and 2l+1 of a
+// warp), both solve row m, and back-substitute outward. Half the dependent chain of
+// a one-thread sweep; the same solution up to FP32 rounding.
+// a: off-diagonal, bm: diagonal, invden: 1 / (bm - a cwet_m - a cwet_{n-1-m}).
+__device__ __forceinline__ void thomas2(float2 *S, int stride, int ng, int up, const float2 *CB,
+                                        const float2 *CW, float2 a, float2 invden, unsigned mask) {
+  const int m = ng / 2;
+  // elimination: thread 0 over rows 0..m-1, thread 1 over rows n-1..m+1
+  const int len = up ? ng - 1 - m : m;
+  const int step = up ? -stride : stride;
+  float2 *L = up ? S + (ng - 1) * stride : S;
+  float2 d = make_float2(0.f, 0.f);
+  float2 rn = L[0];
+  for (int t = 0; t < len; t++) {
+    float2 r = rn;
+    if (t + 1 < len) rn = L[(t + 1) * step];
+    float2 ad = cmulf(a, d);
+    d = cmulf(make_float2(r.x - ad.x, r.y - ad.y), CB[t]);
+    L[t * step] = d;
   }
-  float2 next = prev;
-  for (int k = ng - 2; k >= 0; k--) {
-    float2 v = S[k * stride];
-    float2 cw = cmulf(CW[k + 1], next);
-    v.x -= cw.x;
-    v.y -= cw.y;
-    S[k * stride] = v;
-    next = v;
+  // meet at row m
+  float2 d_other;
+  d_other.x = __shfl_xor_sync(mask, d.x, 1);
+  d_other.y = __shfl_xor_sync(mask, d.y, 1);
+  float2 dsum = make_float2(d.x + d_other.x, d.y + d_other.y);
+  float2 rm = S[m * stride];
+  float2 ads = cmulf(a, dsum);
+  float2 xm = cmulf(make_float2(rm.x - ads.x, rm.y - ads.y), invden);
+  // back substitution outward from m
+  float2 x = xm;
+  for (int t = len - 1; t >= 0; t--) {
+    float2 v = L[t * step];
+    float2 cw = cmulf(CW[t + 1], x);
+    x = make_float2(v.x - cw.x, v.y - cw.y);
+    L[t * step] = x;
   }
+  if (!up) S[m * stride] = xm;
 }
 
 // (I + c D) along a line of S with stride, in place, with a rolling register window
+// and the next-but-one element fetched ahead
 __device__ __forceinline__ void stencil_line(float2 *S, int stride, int ng, float cs) {
-  float2 prev = make_float2(0.f, 0.f), cur = S[0];
+  float2 prev = make_float2(0.f, 0.f), cur = S[0], next = S[stride], nn = S[2 * stride];
   for (int k = 0; k < ng; k++) {
-    float2 next = (k + 1 < ng) ? S[(k + 1) * stride] : make_float2(0.f, 0.f);
-    float2 l = lapf(k > 0, k < ng - 1, prev, cur, next);
-    S[k * stride] = stencil(cs, cur, l);
+    float2 nx = (k + 1 < ng) ? next : make_float2(0.f, 0.f);
+    float2 l = lapf(k > 0, k < ng - 1, prev, cur, nx);
+    float2 out = stencil(cs, cur, l);
     prev = cur;
     cur = next;
+    next = nn;
+    if (k + 3 < ng) nn = S[(k + 3) * stride];
+    S[k * stride] = out;
   }
 }
 
 // Adds the deposited source of beam slice `is` to S with shared-memory atomics.
+// Lanes of a warp whose particles share the lower-left cell (quiet loading stores
+// the nbins mirrored beamlet members, which share x and y, in adjacent lanes) first
+// sum their four weighted contributions with a segmented shuffle reduction over
+// runs of equal cells; only the first lane of each run issues the atomics. This cuts
+// the atomics (and their same-address conflicts) by the run length and keeps the
+// result exact up to FP32 summation order.
 __device__ __forceinline__ void deposit_smem(const StepConstF &sc, const FieldStepF &fs,
                                              const PtrsF &p, float2 *S, int is, int np, int ng) {
-  float cur = (float)p.current[is];
-  float scl = fs.dep_scl * cur;
-  size_t base = (size_t)is * np;
-  constexpr int U = 4;  // particles per thread per round: their loads are issued together
-  for (int ip0 = threadIdx.x; ip0 < np; ip0 += U * blockDim.x) {
+  const float cur = (float)p.current[is];
+  const float scl = fs.dep_scl * cur;
+  const size_t base = (size_t)is * np;
+  const unsigned lane = threadIdx.x & 31u;
+  const int warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  constexpr int U = 4;  // particles per lane per round: their loads are issued together
+  for (int w0 = warp * 32 * U; w0 < np; w0 += nwarp * 32 * U) {
     float xs[U], ys[U], gs[U];
-    double ths[U];
+    long long ths[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      int ip = ip0 + u * blockDim.x;
+      int ip = w0 + u * 32 + (int)lane;
       bool in = ip < np;
       xs[u] = in ? p.x[base + ip] : 1e30f;
       ys[u] = in ? p.y[base + ip] : 1e30f;
-      ths[u] = in ? p.theta[base + ip] : 0.0;
+      ths[u] = in ? p.theta[base + ip] : 0;
       gs[u] = in ? p.dg[base + ip] : 0.f;
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
-    float x = xs[u], y = ys[u];
-    CellF c;
-    if (!ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x, y, c)) continue;
-    double th = ths[u];
-    float a = (float)fma(-rint(th * (1.0 / kTwoPi)), kTwoPi, th);
-    float g = (float)sc.gammaref + gs[u];
-    float dx = x - sc.ax, dy = y - sc.ay;
-    float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
-    float part = sqrtf(faw2) * scl / g;
-    float sn, co;
-    __sincosf(wrapf(fs.rharm * a), &sn, &co);
-    float cpx = sn * part, cpy = co * part;
-    float w = c.wx * c.wy;
-    atomicAdd(&S[c.i00].x, w * cpx);
-    atomicAdd(&S[c.i00].y, w * cpy);
-    w = (1.f - c.wx) * c.wy;
-    atomicAdd(&S[c.i10].x, w * cpx);
-    atomicAdd(&S[c.i10].y, w * cpy);
-    w = c.wx * (1.f - c.wy);
-    atomicAdd(&S[c.i01].x, w * cpx);
-    atomicAdd(&S[c.i01].y, w * cpy);
-    w = (1.f - c.wx) * (1.f - c.wy);
-    atomicAdd(&S[c.i11].x, w * cpx);
-    atomicAdd(&S[c.i11].y, w * cpy);
+      CellF c;
+      bool on = ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, xs[u], ys[u], c);
+      float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (on) {
+        float g = (float)sc.gammaref + gs[u];
+        float dx = xs[u] - sc.ax, dy = ys[u] - sc.ay;
+        float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
+        float part = sqrtf(faw2) * scl / g;
+        float sn, co;
+        __sincosf(phase_of(ths[u], (unsigned)fs.harm), &sn, &co);
+        float cpx = sn * part, cpy = co * part;
+        float w00 = c.wx * c.wy, w10 = (1.f - c.wx) * c.wy, w01 = c.wx * (1.f - c.wy),
+              w11 = (1.f - c.wx) * (1.f - c.wy);
+        v[0] = w00 * cpx; v[1] = w00 * cpy; v[2] = w10 * cpx; v[3] = w10 * cpy;
+        v[4] = w01 * cpx; v[5] = w01 * cpy; v[6] = w11 * cpx; v[7] = w11 * cpy;
+      }
+      // runs of equal lower-left cells among adjacent lanes (off-grid lanes carry
+      // zeros and key -1; they issue no atomics)
+      int key = on ? c.i00 : -1;
+      bool run_head;
+      bool quads = __all_sync(0xffffffffu, key == __shfl_xor_sync(0xffffffffu, key, 1) &&
+                                               key == __shfl_xor_sync(0xffffffffu, key, 2));
+      if (quads) {
+        // every aligned group of four lanes shares one cell (quiet loading with nbins = 4)
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          v[q] += __shfl_xor_sync(0xffffffffu, v[q], 1);
+          v[q] += __shfl_xor_sync(0xffffffffu, v[q], 2);
+        }
+        run_head = (lane & 3u) == 0u;
+      } else {
+        int knext = __shfl_down_sync(0xffffffffu, key, 1);
+        int kprev = __shfl_up_sync(0xffffffffu, key, 1);
+        bool run_end = (lane == 31u) || (knext != key);
+        run_head = (lane == 0u) || (kprev != key);
+        unsigned ends = __ballot_sync(0xffffffffu, run_end);
+        int seg_end = __ffs(ends & (0xffffffffu << lane)) - 1;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            float o = __shfl_down_sync(0xffffffffu, v[q], off);
+            if ((int)lane + off <= seg_end) v[q] += o;
+          }
+        }
+      }
+      if (on && run_head) {
+        atomicAdd(&S[c.i00].x, v[0]);
+        atomicAdd(&S[c.i00].y, v[1]);
+        atomicAdd(&S[c.i10].x, v[2]);
+        atomicAdd(&S[c.i10].y, v[3]);
+        atomicAdd(&S[c.i01].x, v[4]);
+        atomicAdd(&S[c.i01].y, v[5]);
+        atomicAdd(&S[c.i11].x, v[6]);
+        atomicAdd(&S[c.i11].y, v[7]);
+      }
     }
   }
 }
@@ -539,20 +633,23 @@ __device__ __forceinline__ void bulk_store(float2 *g, const float2 *s, int count
   }
   if (head && threadIdx.x == 32) g[0] = s[0];
   if (tail && threadIdx.x == 64) g[count - 1] = s[count - 1];
-  if (threadIdx.x == 0 && body) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(kFusedThreads, 1)
+__global__ void __launch_bounds__(kFusedMaxThreads, 1)
     k_field_fused_f(StepConstF sc, int k, PtrsF p, float2 *__restrict__ field,
-                    const float2 *__restrict__ coef, int ns, int np, int ng, int deposit, int *err) {
+                    const float2 *__restrict__ coef, float2 *__restrict__ scratch, int ns, int np,
+                    int ng, int deposit, int *err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int ncell = ng * ng;
   const FieldStepF &fs = sc.f[k];
   int is = blockIdx.x;
   int i = (is + fs.first) % ns;
   float2 *u = field + (size_t)i * ncell;
-  // layout: [mbarrier 16 B][coefficients 3 ng][pad][S: ncell] with S congruent to u mod 16
+  float2 *s1 = scratch + (size_t)i * ncell;  // (I + c Dy) u of this slice
+  // layout: [mbarrier 16 B][solve constants 16 B][coefficients 3 ng][pad][S: ncell],
+  // S congruent to u mod 16 (the bulk copies need equal alignment on both sides)
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);
+  float2 *K = reinterpret_cast<float2 *>(smem_raw + 8);  // K[0] = 1 / den of the meeting row
   float2 *C = reinterpret_cast<float2 *>(smem_raw + 16);
   float2 *CB = C + ng, *CW = CB + ng;
   size_t soff = (16 + 3 * (size_t)ng * 8 + 15) & ~(size_t)15;
@@ -565,26 +662,52 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
   }
   for (int t = threadIdx.x; t < 3 * ng; t += blockDim.x) C[t] = coef[t];
   __syncthreads();
+  // constants of the two-ended solve: a (off-diagonal) = c[1], diagonal = 1 / cbet[0]
+  const float2 a = C[1];
+  if (threadIdx.x == 0) {
+    int m = ng / 2;
+    float2 bm = make_float2(CB[0].x, -CB[0].y);
+    float n0 = CB[0].x * CB[0].x + CB[0].y * CB[0].y;
+    bm.x /= n0;
+    bm.y /= n0;
+    float2 t1 = cmulf(a, CW[m]), t2 = cmulf(a, CW[ng - 1 - m]);
+    float2 den = make_float2(bm.x - t1.x - t2.x, bm.y - t1.y - t2.y);
+    float nd = den.x * den.x + den.y * den.y;
+    K[0] = make_float2(den.x / nd, -den.y / nd);
+  }
   if (!bulk_load(S, u, ncell, bar_s, err)) return;
   const float cs = fs.cstep;
   const int tid = threadIdx.x;
-  if (tid < ng) stencil_line(S + tid, ng, ng, cs);  // column tid: (I + c Dy)
+  if (tid < ng) stencil_line(S + tid, ng, ng, cs);  // column tid: S1 = (I + c Dy) u
+  // keep S1 for the second half step: (I + c Dx) u' + src = 2 u' - S1, because
+  // (I - c Dx) u' = S1 + src; this replaces the second deposition
+  bulk_store(s1, S, ncell);
+  if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
   __syncthreads();
   if (deposit) {
-    deposit_smem(sc, fs, p, S, is, np, ng);
+    deposit_smem(sc, fs, p, S, is, np, ng);  // S = S1 + src
     __syncthreads();
   }
-  if (tid < ng) thomas(S + tid * ng, 1, ng, C, CB, CW);  // row tid
-  __syncthreads();
-  if (tid < ng) stencil_line(S + tid * ng, 1, ng, cs);  // row tid: (I + c Dx)
-  __syncthreads();
-  if (deposit) {
-    deposit_smem(sc, fs, p, S, is, np, ng);
-    __syncthreads();
+  const float2 invden = K[0];
+  const int line = tid >> 1, up = tid & 1;
+  // lanes 2l and 2l+1 solve line l; the mask covers the lanes of the warp with a line
+  const unsigned mask = __ballot_sync(0xffffffffu, line < ng);
+  if (line < ng) thomas2(S + line * ng, 1, ng, up, CB, CW, a, invden, mask);  // rows: u'
+  // the bulk store of S1 must have landed before it is read back
+  if (threadIdx.x == 0) {
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    asm volatile("fence.proxy.async.global;" ::: "memory");
   }
-  if (tid < ng) thomas(S + tid, ng, ng, C, CB, CW);  // column tid
+  __syncthreads();
+  for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
+    float2 v = S[t], w = s1[t];
+    S[t] = make_float2(2.f * v.x - w.x, 2.f * v.y - w.y);
+  }
+  __syncthreads();
+  if (line < ng) thomas2(S + line, ng, ng, up, CB, CW, a, invden, mask);  // columns
   __syncthreads();
   bulk_store(u, S, ncell);
+  if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
 template <int BS>
@@ -627,7 +750,8 @@ __global__ void __launch_bounds__(BS) k_diag_beam_f(PtrsF p, double gref, int np
   for (int h = 0; h < G4GPU_MAX_HARM; h++) br[h] = bi[h] = 0;
   for (int ip = threadIdx.x; ip < np; ip += BS) {
     double x = p.x[base + ip], y = p.y[base + ip], g = gref + (double)p.dg[base + ip];
-    double px = p.px[base + ip], py = p.py[base + ip], th = p.theta[base + ip];
+    double px = p.px[base + ip], py = p.py[base + ip];
+    long long th = p.theta[base + ip];
     s[0] += g; s[1] += g * g; s[2] += x; s[3] += x * x; s[4] += y; s[5] += y * y;
     s[6] += px; s[7] += px * px; s[8] += py; s[9] += py * py; s[10] += x * px; s[11] += y * py;
     mn[0] = fmin(mn[0], x); mx[0] = fmax(mx[0], x);
@@ -636,8 +760,8 @@ __global__ void __launch_bounds__(BS) k_diag_beam_f(PtrsF p, double gref, int np
     mn[3] = fmin(mn[3], py); mx[3] = fmax(mx[3], py);
     mn[4] = fmin(mn[4], g); mx[4] = fmax(mx[4], g);
     for (int h = 0; h < nharm && h < G4GPU_MAX_HARM; h++) {
-      double sn, cs;
-      sincos((h + 1) * th, &sn, &cs);
+      float sn, cs;
+      sincosf(phase_of(th, (unsigned)(h + 1)), &sn, &cs);  // exact harmonic of the phase
       br[h] += cs;
       bi[h] += sn;
     }
@@ -695,7 +819,7 @@ __global__ void __launch_bounds__(BS) k_diag_field_f(const float2 *field, int ng
 PtrsF make_ptrs_f(const DeviceBeam &b, void *const *field, void *const *src, int nfld) {
   PtrsF p{};
   p.dg = (float *)b.gamma;
-  p.theta = (double *)b.theta;
+  p.theta = (long long *)b.theta;
   p.x = (float *)b.x;
   p.y = (float *)b.y;
   p.px = (float *)b.px;
@@ -712,15 +836,15 @@ PtrsF make_ptrs_f(const DeviceBeam &b, void *const *field, void *const *src, int
 
 void launch_push_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,
                        void *const *field, void *const *src, int ns, int np, int ngrid,
-                       int deposit) {
+                       int deposit, int block) {
   PtrsF p = make_ptrs_f(b, field, src, sc.nfld);
-  dim3 grid((np + 255) / 256, ns);
+  dim3 grid((np + block - 1) / block, ns);
   cudaStream_t s = (cudaStream_t)L.stream;
   switch (sc.nfld) {
-    case 1: k_push_f<1><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
-    case 2: k_push_f<2><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
-    case 3: k_push_f<3><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
-    default: k_push_f<G4GPU_MAX_FIELDS><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    case 1: k_push_f<1><<<grid, block, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    case 2: k_push_f<2><<<grid, block, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    case 3: k_push_f<3><<<grid, block, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    default: k_push_f<G4GPU_MAX_FIELDS><<<grid, block, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
   }
 }
 
@@ -774,8 +898,8 @@ int fused_max_ngrid() {
 }
 
 void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b,
-                              void *field, const void *coef, int ns, int np, int ngrid,
-                              int deposit) {
+                              void *field, const void *coef, void *scratch, int ns, int np,
+                              int ngrid, int deposit, int threads) {
   static unsigned long long configured = 0;  // one bit per device
   size_t smem = fused_smem_bytes(ngrid);
   int dev = 0;
@@ -785,8 +909,11 @@ void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, cons
     configured |= 1ull << dev;
   }
   PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
-  k_field_fused_f<<<ns, kFusedThreads, smem, (cudaStream_t)L.stream>>>(
-      sc, k, p, (float2 *)field, (const float2 *)coef, ns, np, ngrid, deposit, L.err);
+  if (threads < 2 * ngrid) threads = (2 * ngrid + 31) / 32 * 32;
+  if (threads > kFusedMaxThreads) threads = kFusedMaxThreads;
+  k_field_fused_f<<<ns, threads, smem, (cudaStream_t)L.stream>>>(
+      sc, k, p, (float2 *)field, (const float2 *)coef, (float2 *)scratch, ns, np, ngrid, deposit,
+      L.err);
 }
 
 }  // namespace g4

@@ -171,7 +171,7 @@ struct Ptrs {
 // with the corrector; then, with `deposit`, the source deposition of the
 // following Field::track. One thread per particle; blockIdx.y is the slice.
 template <int NF>
-__global__ void __launch_bounds__(256) k_push(StepConst sc, Ptrs p, int ns, int np, int ng,
+__global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int np, int ng,
                                               int deposit) {
   int is = blockIdx.y;
   int ip = blockIdx.x * blockDim.x + threadIdx.x;
@@ -477,15 +477,15 @@ Ptrs make_ptrs(const DeviceBeam &b, void *const *field, void *const *src, int nf
 
 void launch_push_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,
                        void *const *field, void *const *src, int ns, int np, int ngrid,
-                       int deposit) {
+                       int deposit, int block) {
   Ptrs p = make_ptrs(b, field, src, sc.nfld);
-  dim3 grid((np + 255) / 256, ns);
+  dim3 grid((np + block - 1) / block, ns);
   cudaStream_t s = (cudaStream_t)L.stream;
   switch (sc.nfld) {
-    case 1: k_push<1><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
-    case 2: k_push<2><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
-    case 3: k_push<3><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
-    default: k_push<G4GPU_MAX_FIELDS><<<grid, 256, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    case 1: k_push<1><<<grid, block, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    case 2: k_push<2><<<grid, block, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    case 3: k_push<3><<<grid, block, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
+    default: k_push<G4GPU_MAX_FIELDS><<<grid, block, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
   }
 }
 

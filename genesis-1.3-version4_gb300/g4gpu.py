@@ -46,7 +46,14 @@ ABI_SYMBOLS = [
     "g4gpu_get_field", "g4gpu_run", "g4gpu_synchronize", "g4gpu_diag", "g4gpu_get_stream",
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
     "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc",
+    "g4gpu_set_graph_mode", "g4gpu_autotune", "g4gpu_batch_create", "g4gpu_batch_destroy",
+    "g4gpu_batch_member", "g4gpu_batch_run", "g4gpu_batch_synchronize",
+    "g4gpu_mlp_create", "g4gpu_mlp_destroy", "g4gpu_mlp_last_error", "g4gpu_mlp_num_params",
+    "g4gpu_mlp_get_params", "g4gpu_mlp_set_params", "g4gpu_mlp_set_normalization", "g4gpu_mlp_forward",
+    "g4gpu_mlp_gradients", "g4gpu_mlp_train", "g4gpu_closure_attach", "g4gpu_closure_features",
+    "g4gpu_closure_apply", "g4gpu_closure_targets", "g4gpu_copy_state", "g4gpu_run_learned",
 ]
+CLOSURE_NIN, CLOSURE_NOUT = 32, 4
 
 
 class G4Error(RuntimeError):
@@ -127,6 +134,35 @@ def load_library(path=None):
     L.g4gpu_host_gauss_hermite.argtypes = [pd, d, i, pd]
     L.g4gpu_host_fc.argtypes = [d, i, i]
     L.g4gpu_host_fc.restype = d
+    L.g4gpu_set_graph_mode.argtypes = [vp, i]
+    L.g4gpu_autotune.argtypes = [vp, P(i), P(i)]
+    L.g4gpu_batch_create.argtypes = [i, P(Config), P(vp)]
+    L.g4gpu_batch_destroy.argtypes = [vp]
+    L.g4gpu_batch_destroy.restype = None
+    L.g4gpu_batch_member.argtypes = [vp, i]
+    L.g4gpu_batch_member.restype = vp
+    L.g4gpu_batch_run.argtypes = [vp, i, i, i]
+    L.g4gpu_batch_synchronize.argtypes = [vp]
+    pf = P(ctypes.c_float)
+    L.g4gpu_mlp_create.argtypes = [i, i, i, i, i, P(vp)]
+    L.g4gpu_mlp_destroy.argtypes = [vp]
+    L.g4gpu_mlp_destroy.restype = None
+    L.g4gpu_mlp_last_error.argtypes = [vp]
+    L.g4gpu_mlp_last_error.restype = ctypes.c_char_p
+    L.g4gpu_mlp_num_params.argtypes = [vp]
+    L.g4gpu_mlp_num_params.restype = ctypes.c_size_t
+    L.g4gpu_mlp_get_params.argtypes = [vp, pf]
+    L.g4gpu_mlp_set_params.argtypes = [vp, pf]
+    L.g4gpu_mlp_set_normalization.argtypes = [vp, pf, pf, pf, pf]
+    L.g4gpu_mlp_forward.argtypes = [vp, pf, i, pf]
+    L.g4gpu_mlp_gradients.argtypes = [vp, pf, pf, i, pf, pf]
+    L.g4gpu_mlp_train.argtypes = [vp, pf, pf, i, i, i, ctypes.c_float, i, pf]
+    L.g4gpu_closure_attach.argtypes = [vp, vp, d, d, d]
+    L.g4gpu_closure_features.argtypes = [vp, pf]
+    L.g4gpu_closure_apply.argtypes = [vp, pf]
+    L.g4gpu_closure_targets.argtypes = [vp, vp, pf]
+    L.g4gpu_copy_state.argtypes = [vp, vp]
+    L.g4gpu_run_learned.argtypes = [vp, vp, i, i, P(i), P(i), i, d, P(i), P(i), pd]
     for name in ABI_SYMBOLS:
         if not hasattr(L, name):
             raise ImportError(f"{p} does not export {name}")
@@ -293,3 +329,170 @@ class Handle:
 
     def device_bytes(self):
         return int(self.L.g4gpu_device_bytes(self.h))
+
+    def set_graph_mode(self, on):
+        self._check(self.L.g4gpu_set_graph_mode(self.h, int(on)))
+
+    def closure_attach(self, mlp, waist, u0=1.0, c0=1.0):
+        self._mlp = mlp  # keep the network alive while attached
+        self._check(self.L.g4gpu_closure_attach(self.h, mlp.m, waist, u0, c0))
+
+    def closure_features(self):
+        out = np.zeros((self.cfg.nslice, CLOSURE_NIN), dtype=np.float32)
+        self._check(self.L.g4gpu_closure_features(self.h, _pf(out)))
+        return out
+
+    def closure_apply(self, corr):
+        corr = np.ascontiguousarray(corr, dtype=np.float32)
+        self._check(self.L.g4gpu_closure_apply(self.h, _pf(corr)))
+
+    def closure_targets(self, fine):
+        out = np.zeros((self.cfg.nslice, CLOSURE_NOUT), dtype=np.float32)
+        self._check(self.L.g4gpu_closure_targets(self.h, fine.h, _pf(out)))
+        return out
+
+    def copy_state_from(self, other):
+        self._check(self.L.g4gpu_copy_state(self.h, other.h))
+
+    def run_learned(self, fine, istep0, ncoarse, fine_start, fine_count, check_every=8, tol=0.01):
+        fs = np.ascontiguousarray(fine_start, dtype=np.int32)
+        fc = np.ascontiguousarray(fine_count, dtype=np.int32)
+        nchk, nfb = ctypes.c_int(), ctypes.c_int()
+        emax = ctypes.c_double()
+        self._check(self.L.g4gpu_run_learned(self.h, fine.h, istep0, ncoarse,
+                                             fs.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                             fc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), check_every, tol,
+                                             ctypes.byref(nchk), ctypes.byref(nfb), ctypes.byref(emax)))
+        return nchk.value, nfb.value, emax.value
+
+    def autotune(self):
+        pb, ft = ctypes.c_int(), ctypes.c_int()
+        self._check(self.L.g4gpu_autotune(self.h, ctypes.byref(pb), ctypes.byref(ft)))
+        return pb.value, ft.value
+
+
+def _pf(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class MLP:
+    """BF16 tensor-core MLP of the learned closure (g4gpu_mlp)."""
+
+    def __init__(self, nin=CLOSURE_NIN, width=256, nout=CLOSURE_NOUT, seed=0, device=0):
+        self.L = _lib()
+        m = ctypes.c_void_p()
+        rc = self.L.g4gpu_mlp_create(nin, width, nout, seed, device, ctypes.byref(m))
+        if rc:
+            raise G4Error(rc, self.L.g4gpu_last_error(None).decode())
+        self.m = m
+        self.nin, self.width, self.nout = nin, width, nout
+
+    def _check(self, rc):
+        if rc:
+            raise G4Error(rc, self.L.g4gpu_mlp_last_error(self.m).decode())
+
+    @property
+    def num_params(self):
+        return int(self.L.g4gpu_mlp_num_params(self.m))
+
+    def get_params(self):
+        out = np.zeros(self.num_params, dtype=np.float32)
+        self._check(self.L.g4gpu_mlp_get_params(self.m, _pf(out)))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._check(self.L.g4gpu_mlp_set_params(self.m, _pf(p)))
+
+    def set_normalization(self, fmean, fstd, oshift, oscale):
+        a = [np.ascontiguousarray(x, dtype=np.float32) for x in (fmean, fstd, oshift, oscale)]
+        self._check(self.L.g4gpu_mlp_set_normalization(self.m, *[_pf(x) for x in a]))
+
+    def forward(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((X.shape[0], self.nout), dtype=np.float32)
+        self._check(self.L.g4gpu_mlp_forward(self.m, _pf(X), X.shape[0], _pf(Y)))
+        return Y
+
+    def gradients(self, X, T):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        g = np.zeros(self.num_params, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        self._check(self.L.g4gpu_mlp_gradients(self.m, _pf(X), _pf(T), X.shape[0], _pf(g), _pf(loss)))
+        return g, float(loss[0])
+
+    def train(self, X, T, epochs=10, batch=1024, lr=1e-3, seed=0):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        curve = np.zeros(epochs, dtype=np.float32)
+        self._check(self.L.g4gpu_mlp_train(self.m, _pf(X), _pf(T), X.shape[0], epochs, batch, lr, seed,
+                                           _pf(curve)))
+        return curve
+
+    def close(self):
+        if getattr(self, "m", None):
+            self.L.g4gpu_mlp_destroy(self.m)
+            self.m = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _Member(Handle):
+    """A handle owned by a Batch (not destroyed on its own)."""
+
+    def __init__(self, L, h, cfg):
+        self.L = L
+        self.cfg = cfg
+        self.h = ctypes.c_void_p(h)
+
+    def close(self):
+        self.h = None
+
+
+class Batch:
+    """An ensemble of independent runs (g4gpu_batch)."""
+
+    def __init__(self, cfgs):
+        self.L = _lib()
+        n = len(cfgs)
+        arr = (Config * n)(*cfgs)
+        b = ctypes.c_void_p()
+        rc = self.L.g4gpu_batch_create(n, arr, ctypes.byref(b))
+        if rc:
+            raise G4Error(rc, self.L.g4gpu_last_error(None).decode())
+        self.b = b
+        self.members = [_Member(self.L, self.L.g4gpu_batch_member(b, i), cfgs[i]) for i in range(n)]
+
+    def run(self, istep0, nsteps, stages=STAGE_ALL):
+        rc = self.L.g4gpu_batch_run(self.b, istep0, nsteps, stages)
+        if rc:
+            raise G4Error(rc, self.L.g4gpu_last_error(None).decode())
+
+    def synchronize(self):
+        rc = self.L.g4gpu_batch_synchronize(self.b)
+        if rc:
+            raise G4Error(rc, self.L.g4gpu_last_error(None).decode())
+
+    def close(self):
+        if getattr(self, "b", None):
+            for m in self.members:
+                m.h = None
+            self.L.g4gpu_batch_destroy(self.b)
+            self.b = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

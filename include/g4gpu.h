@@ -47,8 +47,9 @@ extern "C" {
 
 /* arithmetic of the step */
 #define G4GPU_PLAIN 0 /* FP64 everywhere, the reference's arithmetic */
-#define G4GPU_MIXED 1 /* FP32 field, solver, deposition and transverse optics; FP64
-                         accumulated phase and FP64 diagnostic reductions */
+#define G4GPU_MIXED 1 /* FP32 field, solver, deposition and transverse optics; the
+                         accumulated phase as a 64-bit fixed-point turn count (exact
+                         accumulation, 2 pi / 2^32 resolution); FP64 diagnostic reductions */
 
 /* field solver (Field::initSolver, src/Core/Field.cpp:72-83) */
 #define G4GPU_SOLVER_ADI 0 /* FieldSolverADI, src/Core/FieldSolverADI.cpp */
@@ -168,6 +169,85 @@ int g4gpu_reset_stats(g4gpu_handle h);
 
 /* Bytes of device memory held by h. */
 size_t g4gpu_device_bytes(g4gpu_handle h);
+
+/* ---- CUDA graphs, launch-shape tuning, batched ensembles ------------------- */
+
+/* With graph mode on, g4gpu_run captures each step range into one CUDA graph the
+ * first time it runs from a given ring state (Field::first / accuslip) and replays
+ * the graph afterwards: one launch per range instead of several per step. Results
+ * are identical to direct launches. Per-kernel event timing is not collected for
+ * graph launches (the launch counter is). No reference counterpart (the reference
+ * has no GPU path); it serves the Gencore.cpp:102-160 loop over a lattice. */
+int g4gpu_set_graph_mode(g4gpu_handle h, int on);
+
+/* Times the candidate launch shapes of the step kernels on the handle's own data
+ * (one step per candidate; beam and field are restored afterwards) and keeps the
+ * fastest: threads per block of the push, threads per CTA of the fused field
+ * kernel. Choices are cached per (precision, npart, ngrid, nfield, solver) for
+ * the life of the process. Requires the lattice, beam and fields to be loaded.
+ * *push_block and *field_threads (may be NULL) receive the choice. No reference
+ * counterpart. */
+int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_threads);
+
+/* A batch owns nrun independent handles (one time window each, with its own
+ * sizes, lattice and stream), e.g. an ensemble of runs of uneven slice counts,
+ * particle counts and grids. Members are loaded through g4gpu_batch_member and
+ * the usual calls; g4gpu_batch_run advances every member over steps
+ * istep0 .. istep0+nsteps-1 of its own lattice (clipped to its length) as one
+ * captured graph per member, launched back to back so that the members run
+ * concurrently on the GPU. Replaces running nrun separate reference jobs. */
+typedef struct g4gpu_batch_ctx *g4gpu_batch;
+int g4gpu_batch_create(int nrun, const g4gpu_config *cfgs, g4gpu_batch *out);
+void g4gpu_batch_destroy(g4gpu_batch b);
+g4gpu_handle g4gpu_batch_member(g4gpu_batch b, int i);
+int g4gpu_batch_run(g4gpu_batch b, int istep0, int nsteps, int stages);
+int g4gpu_batch_synchronize(g4gpu_batch b);
+
+/* ---- learned coarse-step closure ----------------------------------------------
+ * No reference counterpart: the reference integrates every undulator period
+ * (src/Core/Gencore.cpp:102-160). A small MLP (nin -> width -> width -> width ->
+ * nout, ReLU) with BF16 tensor-core forward and backward kernels (FP32 accumulate,
+ * FP32 master weights, Adam) corrects coarse integration steps; the non-learned
+ * fine-step solve is its fallback and its judge (g4gpu_run_learned). */
+typedef struct g4gpu_mlp_ctx *g4gpu_mlp;
+int g4gpu_mlp_create(int nin, int width, int nout, int seed, int device, g4gpu_mlp *out);
+void g4gpu_mlp_destroy(g4gpu_mlp m);
+const char *g4gpu_mlp_last_error(g4gpu_mlp m);
+/* parameter vector: per layer W [n_out_padded][n_in_padded] then b [n_out_padded],
+ * layer widths padded to multiples of 16 */
+size_t g4gpu_mlp_num_params(g4gpu_mlp m);
+int g4gpu_mlp_get_params(g4gpu_mlp m, float *out);
+int g4gpu_mlp_set_params(g4gpu_mlp m, const float *in);
+/* input normalisation (x - fmean) / fstd and output de-normalisation y * oscale + oshift */
+int g4gpu_mlp_set_normalization(g4gpu_mlp m, const float *fmean, const float *fstd, const float *oshift,
+                                const float *oscale);
+int g4gpu_mlp_forward(g4gpu_mlp m, const float *X, int n, float *Y);
+/* gradients of the mean squared error of the normalised outputs over n rows */
+int g4gpu_mlp_gradients(g4gpu_mlp m, const float *X, const float *T, int n, float *grads, float *loss);
+/* fits the normalisation to (X, T), then Adam over shuffled mini-batches */
+int g4gpu_mlp_train(g4gpu_mlp m, const float *X, const float *T, int n, int epochs, int batch, float lr,
+                    int seed, float *loss_per_epoch);
+
+/* Attaches a network (32 features -> 4 corrections) to a handle: per-slice features
+ * are the bunching at harmonics 1-3, mean and rms energy, the on-axis field, and
+ * the projections of field 0 on 16 Gauss-Hermite modes of the given waist; the
+ * corrections are a phase and an energy shift of the slice's particles and a
+ * complex factor on the slice's field. u0, c0 scale the field features. */
+int g4gpu_closure_attach(g4gpu_handle h, g4gpu_mlp m, double waist, double u0, double c0);
+int g4gpu_closure_features(g4gpu_handle h, float *out);    /* [nslice][32] */
+int g4gpu_closure_apply(g4gpu_handle h, const float *corr); /* [nslice][4] */
+/* training targets [nslice][4]: the corrections turning the coarse state of hc into
+ * the fine state of hf after the same interval (hc needs an attached closure) */
+int g4gpu_closure_targets(g4gpu_handle hc, g4gpu_handle hf, float *out);
+/* device copy of beam, fields and ring state between handles of the same shape */
+int g4gpu_copy_state(g4gpu_handle dst, g4gpu_handle src);
+/* coarse steps istep0 .. istep0+ncoarse-1 of hc with the closure; every check_every
+ * steps the fine handle hf integrates the same interval (fine steps fine_start[i],
+ * fine_count[i]) from the same state; above tol relative slice-power error the fine
+ * result replaces the coarse one and the next check_every-1 intervals run fine. */
+int g4gpu_run_learned(g4gpu_handle hc, g4gpu_handle hf, int istep0, int ncoarse, const int *fine_start,
+                      const int *fine_count, int check_every, double tol, int *nchecks, int *nfallback,
+                      double *max_err);
 
 /* ---- host-side loading (bit-exact with the reference, run on the CPU) ------ */
 

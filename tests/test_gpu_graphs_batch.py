@@ -1,0 +1,115 @@
+"""GPU tests of the captured-graph mode, the launch-shape autotuner and batched
+ensembles of uneven runs: each must reproduce the plain direct-launch results.
+
+The deposition adds with atomics, whose order varies from run to run: results of
+two executions agree to rounding (1e-12 relative in FP64, 1e-5 in the mixed form),
+not bit for bit.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_err(a, b):
+    scale = np.max(np.abs(b))
+    return float(np.max(np.abs(np.asarray(a) - b)) / scale) if scale > 0 else float(np.max(np.abs(a - b)))
+
+
+def window(ns, npart, ngrid, seed, taper=0.0, nwig=20):
+    import g4gpu
+    import g4cases as T
+    cur = T.flat_top_current(ns, 1e-10, 1.0, 3000.0, ns * 1e-10 / 8)
+    sp = T.slice_params(ns, 11357.8, 2.0, 0.4e-6, 15.0, currents=cur)
+    beam = g4gpu.host_load_beam(sp, 0, npart, 4, seed, 1, 1e-10, 1.0)
+    lat = T.undulator_lattice(1.7, 0.015, nwig, 2, 1e-10, 11357.8, quad_k1=1.5, quad_l=0.08, taper=taper)
+    gh = g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e4, 25e-6), 1e-4, ngrid)
+    fld = np.stack([gh * (1 + 0.01 * k) for k in range(ns)])
+    return lat, beam, cur, fld
+
+
+def make(lat, beam, cur, fld, precision, solver=0, graph=False):
+    import g4gpu
+    ns, npart = beam.shape[0], beam.shape[1]
+    ngrid = int(round(np.sqrt(fld.shape[1])))
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ngrid, gridmax=1e-4, lambda0=1e-10, sample=1.0,
+                       gammaref=11357.8, precision=precision, solver=solver, time_run=1)
+    h = g4gpu.Handle(cfg)
+    h.set_lattice(lat)
+    h.load_beam(beam, cur)
+    h.load_field(0, fld)
+    h.set_graph_mode(graph)
+    return h
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-12), (1, 1e-5)])
+def test_graph_mode_matches_direct_launches(lib, precision, tol):
+    lat, beam, cur, fld = window(8, 256, 41, 3)
+    with make(lat, beam, cur, fld, precision) as h:
+        h.run(0, lat.shape[0])
+        p0 = h.get_beam()
+        f0, first0, acc0 = h.get_field(0)
+    with make(lat, beam, cur, fld, precision, graph=True) as h:
+        for rep in range(2):  # capture, then replay from the same starting state
+            h.load_beam(beam, cur)
+            h.load_field(0, fld)
+            h.run(0, 10)
+            h.run(10, lat.shape[0] - 10)
+            p1 = h.get_beam()
+            f1, first1, acc1 = h.get_field(0)
+            assert first1 == first0 and acc1 == acc0
+            assert rel_err(f1, f0) < tol
+            for col in (0, 2, 3, 4, 5):
+                assert rel_err(p1[..., col], p0[..., col]) < tol
+            assert np.max(np.abs(p1[..., 1] - p0[..., 1])) < 1e-6
+        st = h.kernel_stats()
+        assert st["push"][0] == 2 * lat.shape[0]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_autotune_keeps_results(lib, precision):
+    lat, beam, cur, fld = window(16, 512, 61, 5)
+    with make(lat, beam, cur, fld, precision) as h:
+        pb, ft = h.autotune()
+        assert pb in (128, 256, 512)
+        assert ft % 32 == 0 and 2 * 61 <= ft <= 1024
+        # the tuning steps are undone
+        p = h.get_beam()
+        assert np.array_equal(p, beam) if precision == 0 else rel_err(p, beam) < 1e-6
+        h.run(0, lat.shape[0])
+        bd, fd = h.diag(1)
+    with make(lat, beam, cur, fld, precision) as h:
+        h.run(0, lat.shape[0])
+        bd0, fd0 = h.diag(1)
+    assert rel_err(fd[0][:, 0], fd0[0][:, 0]) < (1e-10 if precision == 0 else 1e-4)
+
+
+def test_batch_of_uneven_runs_matches_single_runs(lib):
+    """Ensemble members with different slice counts, particle counts, grids (one too
+    large for the shared-memory field kernel) and tapers."""
+    import g4gpu
+    specs = [(6, 256, 41, 1, 0.0, 0), (11, 512, 51, 2, -0.02, 0), (4, 128, 181, 3, -0.01, 0),
+             (7, 256, 45, 4, 0.0, 1)]
+    cases = []
+    cfgs = []
+    for ns, npart, ngrid, seed, taper, solver in specs:
+        lat, beam, cur, fld = window(ns, npart, ngrid, seed, taper=taper, nwig=12)
+        cases.append((lat, beam, cur, fld, solver))
+        cfgs.append(g4gpu.Config(nslice=ns, npart=npart, ngrid=ngrid, gridmax=1e-4, lambda0=1e-10, sample=1.0,
+                                 gammaref=11357.8, precision=1, solver=solver, time_run=1))
+    with g4gpu.Batch(cfgs) as b:
+        for m, (lat, beam, cur, fld, solver) in zip(b.members, cases):
+            m.set_lattice(lat)
+            m.load_beam(beam, cur)
+            m.load_field(0, fld)
+        n = max(c[0].shape[0] for c in cases)
+        b.run(0, 9)
+        b.run(9, n - 9)
+        b.synchronize()
+        got = [m.diag(1) for m in b.members]
+    for (lat, beam, cur, fld, solver), (bd, fd) in zip(cases, got):
+        with make(lat, beam, cur, fld, 1, solver=solver) as h:
+            h.run(0, lat.shape[0])
+            bd0, fd0 = h.diag(1)
+        assert rel_err(fd[0][:, 0], fd0[0][:, 0]) < 1e-4
+        assert np.max(np.abs(bd[:, 24] - bd0[:, 24])) < 1e-4

@@ -1,0 +1,108 @@
+"""GPU tests of the learned coarse-step closure.
+
+  * the BF16 tensor-core MLP kernels: gradients against the numpy FP64 oracle
+    (oracle/mlp_oracle.py, with the same BF16 rounding of the GEMM operands), and
+    training that lowers the loss;
+  * the closure on a SASE window: trained on fine-step runs over several shot-noise
+    seeds, it must bring coarse steps (4 periods) closer to the fine-step result on
+    a held-out seed than coarse steps without it;
+  * the judge: with a zero tolerance every checked interval falls back to the fine
+    solve, which then reproduces the all-fine run.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n", [16, 200])
+def test_mlp_gradients_match_cpu_oracle(lib, n):
+    import g4gpu
+    import mlp_oracle
+    rng = np.random.default_rng(n)
+    m = g4gpu.MLP(32, 256, 4, seed=3)
+    p = m.get_params()
+    # non-zero biases so that every parameter takes part
+    p = p + (rng.standard_normal(p.size).astype(np.float32) * 0.01) * (p == 0)
+    m.set_params(p)
+    m.set_normalization(np.zeros(32), np.ones(32), np.zeros(4), np.ones(4))
+    X = rng.standard_normal((n, 32)).astype(np.float32)
+    T = rng.standard_normal((n, 4)).astype(np.float32)
+    g, loss = m.gradients(X, T)
+    Y0, loss0, g0 = mlp_oracle.forward_backward(m.get_params(), X.astype(np.float64), T.astype(np.float64),
+                                                32, 256, 4, bf16=True)
+    assert abs(loss / loss0 - 1) < 1e-3
+    Y = m.forward(X)
+    assert np.max(np.abs(Y - Y0)) < 1e-3 * np.max(np.abs(Y0)) + 1e-6
+    # per parameter block: BF16 operands, FP32 accumulation in another order
+    layers, dims = mlp_oracle.unpack(p, 32, 256, 4)
+    o = 0
+    for (W, b) in layers:
+        for size in (W.size, b.size):
+            a, r = g[o:o + size], g0[o:o + size]
+            assert np.linalg.norm(a - r) <= 2e-3 * np.linalg.norm(r) + 1e-9, (o, size)
+            o += size
+
+
+def test_mlp_training_lowers_the_loss(lib):
+    import g4gpu
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((8192, 32)).astype(np.float32)
+    a = rng.standard_normal((32, 4))
+    T = np.tanh(X @ a / 4).astype(np.float32) + 0.1 * X[:, :4] ** 2
+    m = g4gpu.MLP(32, 256, 4, seed=1)
+    curve = m.train(X, T, epochs=12, batch=512, lr=2e-3, seed=2)
+    assert curve[-1] < 0.1 * curve[0], curve
+
+
+def sase_setup(ns=32, npart=1024, ngrid=51):
+    import g4cases as T
+    cfg = dict(nslice=ns, npart=npart, ngrid=ngrid, gridmax=1e-4, lambda0=1e-10, sample=1.0,
+               gammaref=17081.0, precision=1, time_run=1)
+    # resonant planar undulator so that the window lases within a few modules
+    lat = T.undulator_lattice(1.7, 0.015, 60, 2, 1e-10, 17081.0, quad_k1=1.5, quad_l=0.08)
+    sp = T.slice_params(ns, 17081.0, 1.0, 0.4e-6, 15.0, current=3000.0)
+    field = np.zeros((ns, ngrid * ngrid), dtype=np.complex128)
+    return cfg, lat, sp, field
+
+
+def test_closure_gains_over_coarse_steps(lib):
+    import g4gpu
+    import learned
+    cfg, lat, sp, field = sase_setup()
+    waist, u0, c0 = 30e-6, 1.0, 1.0
+    X, Tg, clat, fs, fc = learned.generate_training_data(cfg, lat, range(100, 116), sp, cfg["npart"], 4, field,
+                                                          waist, u0, c0)
+    assert X.shape[1] == 32 and Tg.shape[1] == 4 and X.shape[0] == Tg.shape[0]
+    m = g4gpu.MLP(32, 256, 4, seed=0)
+    curve = m.train(X, Tg, epochs=20, batch=256, lr=1e-3, seed=0)
+    assert curve[-1] < curve[0]
+    beam = g4gpu.host_load_beam(sp, 0, cfg["npart"], 4, 999, 1, 1e-10, 1.0)
+    res = learned.evaluate(cfg, lat, clat, fs, fc, beam, sp[:, 16], field, m, waist, u0, c0)
+    e = learned.errors(res)
+    print("coarse vs fine:", e["coarse"], "closure vs fine:", e["closure"])
+    assert e["closure"]["power_rms"] < e["coarse"]["power_rms"]
+
+
+def test_judge_falls_back_to_fine_steps(lib):
+    import g4gpu
+    import learned
+    cfg, lat, sp, field = sase_setup(ns=16, npart=512, ngrid=41)
+    clat, fs, fc = learned.coarsen_lattice(lat)
+    m = g4gpu.MLP(32, 256, 4, seed=0)
+    beam = g4gpu.host_load_beam(sp, 0, cfg["npart"], 4, 7, 1, 1e-10, 1.0)
+    n = 20
+    hf, hc = learned.make_pair(cfg, lat, clat, beam, sp[:, 16], field, m, 30e-6, 1.0, 1.0)
+    with hf, hc:
+        nchk, nfb, emax = hc.run_learned(hf, 0, n, fs, fc, check_every=1, tol=0.0)
+        assert nchk == n and nfb == n
+        bd, fd = hc.diag(1)
+    href = g4gpu.Handle(g4gpu.Config(**cfg))
+    with href:
+        href.set_lattice(lat)
+        href.load_beam(beam, sp[:, 16])
+        href.load_field(0, field)
+        href.run(0, int(fs[n - 1] + fc[n - 1]))
+        bd0, fd0 = href.diag(1)
+    scale = np.max(np.abs(fd0[0][:, 0]))
+    assert np.max(np.abs(fd[0][:, 0] - fd0[0][:, 0])) <= 1e-3 * scale
