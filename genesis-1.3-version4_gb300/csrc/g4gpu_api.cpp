@@ -1112,4 +1112,55 @@ extern "C" int g4gpu_batch_synchronize(g4gpu_batch b) {
   return G4GPU_OK;
 }
 
+// ---- ADI field step without device allocation ---------------------------------
+// For callers that cannot call cudaMalloc (their device memory belongs to another
+// allocator, or a cudaFree's device-wide synchronisation would stall their work in
+// flight). Nothing here allocates device memory: the kernel's scratch, coefficients
+// and error flag live in a static device array of the mixed-precision module, and
+// the coefficients are computed on the host exactly as g4gpu_set_lattice computes
+// them for a handle (adi_coefficients, FieldSolverADI::init).
+extern "C" int g4gpu_adi_advance_noalloc(float *field, const float *source, int nslice, int ngrid,
+                                         int first, double delz, double dgrid, double xks, int device,
+                                         void *stream) {
+  if (!field) return fail(nullptr, G4GPU_ERR_ARG, "null field");
+  if (nslice < 1) return fail(nullptr, G4GPU_ERR_ARG, "nslice must be >= 1");
+  if (ngrid < 3 || ngrid > G4GPU_NOALLOC_MAX_NGRID || ngrid > g4::fused_max_ngrid()) {
+    char buf[160];
+    snprintf(buf, sizeof(buf),
+             "ngrid %d outside [3, %d]: a slice of ngrid^2 complex floats must fit in shared memory",
+             ngrid, G4GPU_NOALLOC_MAX_NGRID);
+    return fail(nullptr, G4GPU_ERR_ARG, buf);
+  }
+  if (first < 0 || first >= nslice) return fail(nullptr, G4GPU_ERR_ARG, "first must be in [0, nslice)");
+  if (!std::isfinite(delz) || !(dgrid > 0) || !std::isfinite(dgrid) || !(xks > 0) || !std::isfinite(xks))
+    return fail(nullptr, G4GPU_ERR_ARG, "delz must be finite, dgrid and xks finite and positive");
+  if (reinterpret_cast<uintptr_t>(field) % 8 || (source && reinterpret_cast<uintptr_t>(source) % 8))
+    return fail(nullptr, G4GPU_ERR_ARG, "field and source must be 8-byte aligned (complex float)");
+  const size_t bytes = (size_t)nslice * ngrid * ngrid * 2 * sizeof(float);
+  if (source) {
+    uintptr_t f0 = reinterpret_cast<uintptr_t>(field), s0 = reinterpret_cast<uintptr_t>(source);
+    if (f0 < s0 + bytes && s0 < f0 + bytes) return fail(nullptr, G4GPU_ERR_ARG, "source overlaps field");
+  }
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+  std::vector<std::complex<double>> cc, cb, cw;
+  double cs = 0;
+  adi_coefficients(delz, dgrid, xks, ngrid, cc, cb, cw, &cs);
+  std::vector<float> coef(6 * (size_t)ngrid);
+  const std::vector<std::complex<double>> *parts[3] = {&cc, &cb, &cw};
+  for (int p = 0; p < 3; p++)
+    for (int i = 0; i < ngrid; i++) {
+      coef[2 * ((size_t)p * ngrid + i)] = static_cast<float>((*parts[p])[i].real());
+      coef[2 * ((size_t)p * ngrid + i) + 1] = static_cast<float>((*parts[p])[i].imag());
+    }
+  std::string msg;
+  int rc = g4::adi_noalloc_mixed(device, stream, field, source, coef.data(), static_cast<float>(cs), nslice,
+                                 ngrid, first, &msg);
+  if (prev >= 0 && prev != device) cudaSetDevice(prev);
+  if (rc) return fail(nullptr, rc, msg);
+  return G4GPU_OK;
+}
+
 }  // extern "C"

@@ -5,6 +5,8 @@
 #include <cstddef>
 #include <cstdint>
 
+#include <string>
+
 #include "g4gpu.h"
 
 namespace g4 {
@@ -116,6 +118,12 @@ int fused_max_ngrid();
 void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b,
                               void *field, const void *coef, void *scratch, int ns, int np,
                               int ngrid, int deposit, int threads);
+// One ADI step of ns float2 field slices with an optional source, all scratch in the
+// module's static device array (g4gpu_adi_advance_noalloc); coef: [3][ngrid] float2 of
+// c, cbet, cwet. Synchronises `stream`. Returns a G4GPU_ERR_* code with *msg set.
+size_t noalloc_scratch_bytes();
+int adi_noalloc_mixed(int device, void *stream, void *field, const void *source, const float *coef,
+                      float cstep, int ns, int ngrid, int first, std::string *msg);
 
 // kernels_fft.cu: FFT field solver (FieldSolverFFT::FFT)
 struct FFTPlan {

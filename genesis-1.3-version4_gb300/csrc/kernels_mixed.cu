@@ -25,8 +25,15 @@
 
 #include <cmath>
 #include <cstdint>
+#include <mutex>
+#include <string>
 
 #include "g4gpu_internal.h"
+
+// Scratch of g4gpu_adi_advance_noalloc: 32 MiB, shared by every call on a device and
+// held by every device that loads this module until the process exits. Host code
+// uses the name only to look up the device address (cudaGetSymbolAddress).
+static __device__ __align__(256) unsigned char g4_noalloc_scratch[32u << 20];
 
 namespace g4 {
 
@@ -832,6 +839,133 @@ PtrsF make_ptrs_f(const DeviceBeam &b, void *const *field, void *const *src, int
   return p;
 }
 
+// ---- ADI step without device allocation (g4gpu_adi_advance_noalloc) -------------
+//
+// Layout of the file-scope scratch array (g4_noalloc_scratch below):
+//   [0, 4)              device error flag, cleared by every call
+//   [256, 256 + 24 ng)  ADI coefficients c, cbet, cwet as float2, written by every call
+//   [8192, ...)         one S1 slot per CTA: (I + c Dy) u of the slice in hand, 256-byte
+//                       aligned slots of (ngrid^2 + 2) float2 rounded up
+constexpr size_t kNoallocScratchBytes = 32u << 20;
+constexpr size_t kNoallocCoefOffset = 256;
+constexpr size_t kNoallocSlotOffset = 8192;
+
+// bulk_load with the mbarrier phase parity given (a CTA that loads several slices
+// waits on phases 0, 1, 0, ...); also orders this CTA's earlier generic-proxy
+// accesses of s before the bulk copy overwrites it
+__device__ __forceinline__ bool bulk_load_parity(float2 *s, const float2 *g, int count, uint32_t bar,
+                                                 uint32_t parity, int *err) {
+  uintptr_t ga = reinterpret_cast<uintptr_t>(g);
+  int head = (ga & 15) ? 1 : 0;
+  int body = (count - head) & ~1;
+  int tail = count - head - body;
+  if (threadIdx.x == 0) {
+    uint32_t bytes = (uint32_t)body * 8u;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    if (bytes) {
+      uint32_t dst = (uint32_t)__cvta_generic_to_shared(s + head);
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+          ::"r"(dst), "l"(g + head), "r"(bytes), "r"(bar)
+          : "memory");
+    }
+  }
+  if (head && threadIdx.x == 32) s[0] = g[0];
+  if (tail && threadIdx.x == 64) s[count - 1] = g[count - 1];
+  bool ok = mbar_wait(bar, parity, err);
+  __syncthreads();
+  return ok;
+}
+
+// The ADI half steps of k_field_fused_f with the source read from a caller's array
+// instead of deposited from particles, and with a fixed number of CTAs that take
+// slices is = blockIdx.x, blockIdx.x + gridDim.x, ... so that the S1 scratch is one
+// slot per CTA rather than one per slice. Field storage slot (is + first) % ns is
+// advanced with source slice is (the ring order of FieldSolverADI::advance,
+// FieldSolverADI.cpp:9-58).
+__global__ void __launch_bounds__(kFusedMaxThreads, 1)
+    k_adi_noalloc_f(float2 *__restrict__ field, const float2 *__restrict__ source,
+                    unsigned char *__restrict__ scratch, float cs, int ns, int ng, int first,
+                    size_t slot_bytes) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int *err = reinterpret_cast<int *>(scratch);
+  const float2 *coef = reinterpret_cast<const float2 *>(scratch + kNoallocCoefOffset);
+  float2 *slot =
+      reinterpret_cast<float2 *>(scratch + kNoallocSlotOffset + (size_t)blockIdx.x * slot_bytes);
+  const int ncell = ng * ng;
+  const int tid = threadIdx.x;
+  // shared layout as in k_field_fused_f; S moves by 8 bytes per slice to stay
+  // congruent to the slice's address mod 16
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);
+  float2 *K = reinterpret_cast<float2 *>(smem_raw + 8);
+  float2 *C = reinterpret_cast<float2 *>(smem_raw + 16);
+  float2 *CB = C + ng, *CW = CB + ng;
+  const size_t soff = (16 + 3 * (size_t)ng * 8 + 15) & ~(size_t)15;
+  uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(bar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int t = tid; t < 3 * ng; t += blockDim.x) C[t] = coef[t];
+  __syncthreads();
+  const float2 a = C[1];
+  if (tid == 0) {
+    int m = ng / 2;
+    float2 bm = make_float2(CB[0].x, -CB[0].y);
+    float n0 = CB[0].x * CB[0].x + CB[0].y * CB[0].y;
+    bm.x /= n0;
+    bm.y /= n0;
+    float2 t1 = cmulf(a, CW[m]), t2 = cmulf(a, CW[ng - 1 - m]);
+    float2 den = make_float2(bm.x - t1.x - t2.x, bm.y - t1.y - t2.y);
+    float nd = den.x * den.x + den.y * den.y;
+    K[0] = make_float2(den.x / nd, -den.y / nd);
+  }
+  __syncthreads();
+  const float2 invden = K[0];
+  const int line = tid >> 1, up = tid & 1;
+  const unsigned mask = __ballot_sync(0xffffffffu, line < ng);
+  uint32_t parity = 0;
+  for (int is = blockIdx.x; is < ns; is += gridDim.x, parity ^= 1u) {
+    const int i = (is + first) % ns;
+    float2 *u = field + (size_t)i * ncell;
+    const uintptr_t mis = reinterpret_cast<uintptr_t>(u) & 15;  // 0 or 8
+    float2 *S = reinterpret_cast<float2 *>(smem_raw + soff + mis);
+    float2 *s1 = slot + (mis ? 1 : 0);
+    if (!bulk_load_parity(S, u, ncell, bar_s, parity, err)) return;
+    if (tid < ng) stencil_line(S + tid, ng, ng, cs);  // S1 = (I + c Dy) u
+    // the previous slice's generic reads of the slot precede its overwrite
+    if (tid == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
+    bulk_store(s1, S, ncell);
+    if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    __syncthreads();
+    if (source) {
+      const float2 *src = source + (size_t)is * ncell;
+      for (int t = tid; t < ncell; t += blockDim.x) {
+        float2 v = S[t], w = src[t];
+        S[t] = make_float2(v.x + w.x, v.y + w.y);
+      }
+      __syncthreads();
+    }
+    if (line < ng) thomas2(S + line * ng, 1, ng, up, CB, CW, a, invden, mask);  // rows: u'
+    if (tid == 0) {
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+    }
+    __syncthreads();
+    for (int t = tid; t < ncell; t += blockDim.x) {  // (I + c Dx) u' + src = 2 u' - S1
+      float2 v = S[t], w = s1[t];
+      S[t] = make_float2(2.f * v.x - w.x, 2.f * v.y - w.y);
+    }
+    __syncthreads();
+    if (line < ng) thomas2(S + line, ng, ng, up, CB, CW, a, invden, mask);  // columns
+    __syncthreads();
+    bulk_store(u, S, ncell);
+    if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    __syncthreads();  // the next slice's load may overwrite S
+  }
+}
+
 }  // namespace
 
 void launch_push_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,
@@ -914,6 +1048,94 @@ void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, cons
   k_field_fused_f<<<ns, threads, smem, (cudaStream_t)L.stream>>>(
       sc, k, p, (float2 *)field, (const float2 *)coef, (float2 *)scratch, ns, np, ngrid, deposit,
       L.err);
+}
+
+namespace {
+// Per-device set-up of the no-allocation path: the device address of the scratch
+// array, the kernel's shared-memory limit and the SM count, done by the first call
+// on each device.
+struct NoallocDevice {
+  bool ready = false;
+  unsigned char *scratch = nullptr;
+  int nsm = 0;
+};
+std::mutex g_noalloc_mu;
+NoallocDevice g_noalloc_dev[64];
+}  // namespace
+
+size_t noalloc_scratch_bytes() { return kNoallocScratchBytes; }
+
+int adi_noalloc_mixed(int device, void *stream, void *field, const void *source, const float *coef,
+                      float cstep, int ns, int ngrid, int first, std::string *msg) {
+  if (device < 0 || device >= 64) {
+    *msg = "device index outside [0, 64)";
+    return G4GPU_ERR_ARG;
+  }
+  unsigned char *scratch;
+  int nsm;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    NoallocDevice &d = g_noalloc_dev[device];
+    if (!d.ready) {
+      // host code names g4_noalloc_scratch only to look up its device address
+      cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&d.scratch), g4_noalloc_scratch);
+      if (e != cudaSuccess) {
+        *msg = std::string("cudaGetSymbolAddress of the scratch array: ") + cudaGetErrorString(e);
+        return G4GPU_ERR_CUDA;
+      }
+      e = cudaFuncSetAttribute(k_adi_noalloc_f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&d.nsm, cudaDevAttrMultiProcessorCount, device);
+      if (e != cudaSuccess) {
+        *msg = std::string("set-up of the no-allocation kernel: ") + cudaGetErrorString(e);
+        return G4GPU_ERR_CUDA;
+      }
+      d.ready = true;
+    }
+    scratch = d.scratch;
+    nsm = d.nsm;
+  }
+  const size_t ncell = (size_t)ngrid * ngrid;
+  const size_t slot_bytes = ((ncell + 2) * sizeof(float2) + 255) & ~(size_t)255;
+  const size_t nslot = (kNoallocScratchBytes - kNoallocSlotOffset) / slot_bytes;
+  if (nslot < 1 || 3 * (size_t)ngrid * sizeof(float2) > kNoallocSlotOffset - kNoallocCoefOffset) {
+    *msg = "ngrid too large for the scratch array";
+    return G4GPU_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  // the coefficients come from pageable host memory: the copy is staged before the
+  // call returns, so the caller's buffer may go away afterwards
+  cudaError_t e = cudaMemcpyAsync(scratch + kNoallocCoefOffset, coef, 3 * (size_t)ngrid * sizeof(float2),
+                                  cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0, sizeof(int), s);
+  if (e != cudaSuccess) {
+    *msg = std::string("scratch set-up copy: ") + cudaGetErrorString(e);
+    return G4GPU_ERR_CUDA;
+  }
+  int grid = ns;
+  if ((size_t)grid > nslot) grid = (int)nslot;
+  if (nsm > 0 && grid > nsm) grid = nsm;
+  int threads = 512;
+  if (threads < 2 * ngrid) threads = (2 * ngrid + 31) / 32 * 32;
+  if (threads > kFusedMaxThreads) threads = kFusedMaxThreads;
+  k_adi_noalloc_f<<<grid, threads, fused_smem_bytes(ngrid), s>>>(
+      (float2 *)field, (const float2 *)source, scratch, cstep, ns, ngrid, first, slot_bytes);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    *msg = std::string("k_adi_noalloc_f launch: ") + cudaGetErrorString(e);
+    return G4GPU_ERR_CUDA;
+  }
+  int flag = 0;
+  e = cudaMemcpyAsync(&flag, scratch, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    *msg = std::string("k_adi_noalloc_f: ") + cudaGetErrorString(e);
+    return G4GPU_ERR_CUDA;
+  }
+  if (flag != 0) {
+    *msg = "device error flag raised (code " + std::to_string(flag) + ")";
+    return G4GPU_ERR_DEVICE;
+  }
+  return G4GPU_OK;
 }
 
 }  // namespace g4

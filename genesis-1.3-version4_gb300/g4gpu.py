@@ -27,6 +27,7 @@ MAX_HARM = 16
 PLAIN, MIXED = 0, 1
 SOLVER_ADI, SOLVER_FFT = 0, 1
 STAGE_PUSH, STAGE_FIELD, STAGE_SLIP, STAGE_ALL = 1, 2, 4, 7
+ERR_ARG, ERR_CUDA, ERR_STATE, ERR_DEVICE, ERR_NOMEM = 1, 2, 3, 4, 5
 
 LAT_COLS = ["aw", "ax", "ay", "ku", "kx", "ky", "gradx", "grady", "qf", "qx", "qy",
             "cx", "cy", "dz", "slip", "phase", "helical", "z"]
@@ -52,8 +53,11 @@ ABI_SYMBOLS = [
     "g4gpu_mlp_get_params", "g4gpu_mlp_set_params", "g4gpu_mlp_set_normalization", "g4gpu_mlp_forward",
     "g4gpu_mlp_gradients", "g4gpu_mlp_train", "g4gpu_closure_attach", "g4gpu_closure_features",
     "g4gpu_closure_apply", "g4gpu_closure_targets", "g4gpu_copy_state", "g4gpu_run_learned",
+    "g4gpu_adi_advance_noalloc",
 ]
 CLOSURE_NIN, CLOSURE_NOUT = 32, 4
+NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
+NOALLOC_MAX_NGRID = 168
 
 
 class G4Error(RuntimeError):
@@ -163,6 +167,7 @@ def load_library(path=None):
     L.g4gpu_closure_targets.argtypes = [vp, vp, pf]
     L.g4gpu_copy_state.argtypes = [vp, vp]
     L.g4gpu_run_learned.argtypes = [vp, vp, i, i, P(i), P(i), i, d, P(i), P(i), pd]
+    L.g4gpu_adi_advance_noalloc.argtypes = [vp, vp, i, i, i, d, d, d, i, vp]
     for name in ABI_SYMBOLS:
         if not hasattr(L, name):
             raise ImportError(f"{p} does not export {name}")
@@ -369,6 +374,21 @@ class Handle:
         pb, ft = ctypes.c_int(), ctypes.c_int()
         self._check(self.L.g4gpu_autotune(self.h, ctypes.byref(pb), ctypes.byref(ft)))
         return pb.value, ft.value
+
+
+def adi_advance_noalloc(field_ptr, source_ptr, nslice, ngrid, first, delz, dgrid, xks, device=0,
+                        stream=None):
+    """One single-precision ADI step of nslice field slices at device address
+    field_ptr ([nslice][ngrid^2] complex float, in place) with the source at
+    source_ptr (beam-slice order, or None), allocating no device memory
+    (g4gpu_adi_advance_noalloc). Returns after the step has finished."""
+    L = _lib()
+    rc = L.g4gpu_adi_advance_noalloc(ctypes.c_void_p(field_ptr),
+                                     ctypes.c_void_p(source_ptr) if source_ptr else None,
+                                     nslice, ngrid, first, delz, dgrid, xks, device,
+                                     ctypes.c_void_p(stream) if stream else None)
+    if rc:
+        raise G4Error(rc, L.g4gpu_last_error(None).decode())
 
 
 def _pf(a):

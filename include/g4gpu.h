@@ -249,6 +249,42 @@ int g4gpu_run_learned(g4gpu_handle hc, g4gpu_handle hf, int istep0, int ncoarse,
                       const int *fine_count, int check_every, double tol, int *nchecks, int *nfallback,
                       double *max_err);
 
+/* ---- ADI field step without device allocation ------------------------------ */
+
+/* No counterpart in the reference: an addition of this library for callers that
+ * cannot allocate device memory. The handle API allocates its buffers with
+ * cudaMalloc; a caller whose device memory all belongs to another allocator (a
+ * framework's caching allocator that has reserved the device), or that cannot let
+ * cudaFree synchronise the device while its own work is in flight, can use this
+ * call instead. It allocates nothing: its scratch is a static device array of
+ * G4GPU_NOALLOC_SCRATCH_BYTES (32 MiB) in the library's mixed-precision module,
+ * which every device that loads that module holds until the process exits.
+ *
+ * One Crank-Nicolson ADI step (FieldSolverADI::ADI) of nslice field slices in
+ * single precision, in place:
+ *   field   device, [nslice][ngrid*ngrid] complex float (re, im), 8-byte aligned;
+ *           storage slot (is + first) % nslice is advanced with source slice is
+ *   source  device, [nslice][ngrid*ngrid] complex float in beam-slice order (the
+ *           crsource term of FieldSolverADI::advance), or NULL for none; must not
+ *           overlap field
+ *   delz, dgrid, xks   step length, grid spacing, wavenumber (FieldSolverADI::init)
+ *   device, stream     the CUDA device and a cudaStream_t on it (NULL: the default
+ *                      stream); the call returns after the step has finished.
+ * Limits: 3 <= ngrid <= G4GPU_NOALLOC_MAX_NGRID (a slice must fit in shared
+ * memory); larger grids are rejected with G4GPU_ERR_ARG, and g4gpu_last_error(NULL)
+ * gives the message. Any nslice: slices are taken in turns by at most one CTA per
+ * SM, each with one scratch slot of ngrid^2 complex floats.
+ * The first call on a device looks up the array's device address and sets the
+ * kernel's shared-memory limit; make that first call before any stream capture.
+ * Every call on a device shares the one array, which keeps the last call's
+ * contents (the call clears its error flag and rewrites its coefficients, and every
+ * slot is written before it is read): calls that overlap on the GPU, from two host
+ * threads or on two streams, race. */
+#define G4GPU_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+#define G4GPU_NOALLOC_MAX_NGRID 168
+int g4gpu_adi_advance_noalloc(float *field, const float *source, int nslice, int ngrid, int first,
+                              double delz, double dgrid, double xks, int device, void *stream);
+
 /* ---- host-side loading (bit-exact with the reference, run on the CPU) ------ */
 
 /* Quiet loading plus shot noise of nslice consecutive slices for one rank, as

@@ -1033,6 +1033,57 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
   return 0;
 }
 
+/* The source term of one field for every beam slice at lattice step istep, as
+ * FieldSolverADI::advance builds it (FieldSolverADI.cpp:13-52): out [ns][ngrid^2]
+ * complex (re, im), zero outside undulators and for even harmonics. */
+void orc_deposit_source(const double *lat, int istep, int ns, int npart, const double *particles,
+                        const double *current, double reflength, int harm, int ngrid,
+                        double gridmax, double *out) {
+  step_ctx c;
+  memset(&c, 0, sizeof(c));
+  c.ns = ns;
+  c.npart = npart;
+  c.nfld = 1;
+  c.ngrid = ngrid;
+  c.beam = (part_t *)particles;
+  c.current = current;
+  c.harm = &harm;
+  c.gridmax = &gridmax;
+  c.reflength = reflength;
+  c.ifld = 0;
+  c.st = get_step(lat, istep);
+  c.delz = c.st.dz;
+  size_t n2 = (size_t)ngrid * ngrid;
+  for (int ii = 0; ii < ns; ii++) deposit(&c, ii, (cplx *)out + (size_t)ii * n2);
+}
+
+/* One ADI step of every slice with a given source (the loop of
+ * FieldSolverADI::advance, FieldSolverADI.cpp:9-58, with the source precomputed):
+ * field storage slot (ii + first) % ns is advanced with source slice ii; source may
+ * be NULL (no source). Coefficients from FieldSolverADI::init (:125-182). */
+void orc_adi_advance(int ns, int ngrid, int first, double delz, double dgrid, double xks,
+                     double *field, const double *source) {
+  step_ctx c;
+  memset(&c, 0, sizeof(c));
+  c.ngrid = ngrid;
+  size_t n2 = (size_t)ngrid * ngrid;
+  cplx *coef = malloc(sizeof(cplx) * 3 * ngrid);
+  cplx *work = malloc(sizeof(cplx) * n2);
+  cplx *zero = calloc(n2, sizeof(cplx));
+  c.cc = coef;
+  c.cbet = coef + ngrid;
+  c.cwet = coef + 2 * ngrid;
+  adi_init(&c, delz, dgrid, xks);
+  for (int ii = 0; ii < ns; ii++) {
+    size_t i = (size_t)((ii + first) % ns);
+    const cplx *src = source ? (const cplx *)source + (size_t)ii * n2 : zero;
+    adi(&c, (cplx *)field + i * n2, src, work);
+  }
+  free(zero);
+  free(work);
+  free(coef);
+}
+
 /* ------------------------------------------------------------------------- */
 /* diagnostics                                                               */
 /* ------------------------------------------------------------------------- */

@@ -66,6 +66,16 @@ void orc_load_beam(int nslice, int islice0, int npart, int nbins, int seed, int 
  * par: lambda, power, phase, z0, w0, xcen, ycen, xangle, yangle, nx, ny, harm */
 void orc_gauss_hermite(const double *par, double gridmax, int ngrid, double *out);
 
+/* Source term of one field per beam slice at lattice step istep
+ * (FieldSolverADI.cpp:13-52): out [ns][ngrid^2][2] (re, im). */
+void orc_deposit_source(const double *lat, int istep, int ns, int npart, const double *particles,
+                        const double *current, double reflength, int harm, int ngrid,
+                        double gridmax, double *out);
+/* One ADI step of ns slices with a given source (FieldSolverADI.cpp:9-122): field
+ * storage slot (ii + first) % ns takes source slice ii; source may be NULL. */
+void orc_adi_advance(int ns, int ngrid, int first, double delz, double dgrid, double xks,
+                     double *field, const double *source);
+
 /* Per-slice beam diagnostics (Diagnostic.cpp:373-563) for nharm bunching
  * harmonics. out[ns][ORC_DB_NCOL + 2*nharm]: the columns below, then
  * |b_h| and arg(b_h) for h = 1..nharm. */

@@ -69,6 +69,8 @@ class _Lib:
         if prefix == "orc_":
             L.orc_diag_beam.argtypes = [_i, _i, _pd, _i, _pd]
             L.orc_diag_field.argtypes = [_i, _i, _d, _d, _i, _pd, _i, _pd]
+            L.orc_deposit_source.argtypes = [_pd, _i, _i, _i, _pd, _pd, _d, _i, _i, _d, _pd]
+            L.orc_adi_advance.argtypes = [_i, _i, _i, _d, _d, _d, _pd, _pd]
 
     def ran2(self, seed, n):
         out = np.zeros(n)
@@ -155,6 +157,27 @@ class _Lib:
         self.lib.orc_diag_field(ns, ngrid, gridmax, lambda0, harm, _ptr(f.view(np.float64)),
                                 int(first), _ptr(out))
         return out
+
+    def deposit_source(self, lat, istep, particles, current, reflength, harm, ngrid, gridmax):
+        """Source term [ns][ngrid^2] complex of one field at lattice step istep."""
+        lat = np.ascontiguousarray(lat, dtype=np.float64).reshape(-1, LAT_NCOL)
+        part = np.ascontiguousarray(particles, dtype=np.float64)
+        ns, npart = part.shape[0], part.shape[1]
+        cur = np.ascontiguousarray(current, dtype=np.float64)
+        out = np.zeros((ns, ngrid * ngrid), dtype=np.complex128)
+        self.lib.orc_deposit_source(_ptr(lat), istep, ns, npart, _ptr(part), _ptr(cur), reflength,
+                                    harm, ngrid, gridmax, _ptr(out.view(np.float64)))
+        return out
+
+    def adi_advance(self, field, source, first, delz, dgrid, xks):
+        """One ADI step of every slice of `field` [ns][ngrid^2] (storage order) with
+        `source` [ns][ngrid^2] in beam-slice order, or None; returns a new array."""
+        f = np.array(field, dtype=np.complex128, order="C", copy=True)
+        ns, ngrid = f.shape[0], int(round(np.sqrt(f.shape[1])))
+        src = None if source is None else np.ascontiguousarray(source, dtype=np.complex128)
+        self.lib.orc_adi_advance(ns, ngrid, int(first), delz, dgrid, xks, _ptr(f.view(np.float64)),
+                                 None if src is None else _ptr(src.view(np.float64)))
+        return f
 
 
 _oracle = None
