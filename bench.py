@@ -195,7 +195,7 @@ def kernel_alg_bytes(kernel, mixed, ns=None):
     return ns * per
 
 
-def time_form(g4gpu, torch, precision, beam, cur, lat, steps, warmup, profile=True):
+def time_form(g4gpu, torch, precision, beam, cur, lat, steps, warmup, profile=True, autotune=False):
     cfg = g4gpu.Config(nslice=NS, npart=NPART, ngrid=NGRID, gridmax=GRIDMAX, lambda0=LAMBDA0,
                        sample=1.0, gammaref=GAMMA0, precision=precision, time_run=1,
                        device=torch.cuda.current_device())
@@ -203,6 +203,8 @@ def time_form(g4gpu, torch, precision, beam, cur, lat, steps, warmup, profile=Tr
     h.set_lattice(lat)
     h.load_beam(beam, cur)
     h.load_field(0, np.zeros((NS, NGRID * NGRID), dtype=np.complex128))
+    # launch shapes picked by the library's autotuner (untimed; the state is restored)
+    h.shapes = h.autotune() if autotune else None
     nlat = lat.shape[0]
     for i in range(warmup):
         h.run(i % nlat, 1)
@@ -220,6 +222,169 @@ def time_form(g4gpu, torch, precision, beam, cur, lat, steps, warmup, profile=Tr
     stats = h.kernel_stats()
     h.set_profiling(False)
     return h, ms, stats
+
+
+ENSEMBLE_SEED, ENSEMBLE_RUNS = 11, 64
+
+
+def ensemble_runs(nrun=ENSEMBLE_RUNS, seed=ENSEMBLE_SEED):
+    """The uneven ensemble: per run (nslice, npart, ngrid, taper) drawn from `seed`:
+    nslice uniform in 64..1024, npart from {2048, 4096, 8192, 16384}, ngrid from
+    {101, 151, 201, 255}, linear aw taper uniform in [-2 %, 0] over the 4 modules."""
+    rng = np.random.default_rng(seed)
+    return [(int(rng.integers(64, 1025)), int(rng.choice([2048, 4096, 8192, 16384])),
+             int(rng.choice([101, 151, 201, 255])), float(rng.uniform(-0.02, 0.0))) for _ in range(nrun)]
+
+
+def ensemble_member(r, ns, npart, ngrid, taper, g4gpu):
+    lat = T.undulator_lattice(1.7, 0.015, 110, 4, LAMBDA0, GAMMA0, quad_k1=1.5, quad_l=0.08, taper=taper)
+    cur = flat_top(ns)
+    sp = T.slice_params(ns, GAMMA0, 2.0, 0.4e-6, 15.0, currents=cur)
+    beam = g4gpu.host_load_beam(sp, 0, npart, 4, ENSEMBLE_SEED + r, 1, LAMBDA0, 1.0)
+    return lat, beam, cur, np.zeros((ns, ngrid * ngrid), dtype=np.complex128)
+
+
+def diag_error(b, f, b0, f0):
+    """Slice-power error relative to the largest slice power, and bunching error
+    relative to the largest bunching, of (b, f) against (b0, f0)."""
+    p, p0 = f[0][:, 0], f0[0][:, 0]
+    return {"power_max_rel": float(np.max(np.abs(p - p0)) / max(np.max(np.abs(p0)), 1e-300)),
+            "bunching_max_rel": float(np.max(np.abs(b[:, 24] - b0[:, 24])) / max(np.max(np.abs(b0[:, 24])), 1e-300))}
+
+
+def batched_form(g4gpu, torch, steps, warmup, peak, nrun=ENSEMBLE_RUNS, nerr=4):
+    """The uneven ensemble as one batch (one handle and stream per run, each run's
+    steps one captured CUDA graph, launch shapes from the autotuner), mixed form.
+    Timed: `steps` steps of every run after `warmup`. Error: the nerr smallest runs
+    against the plain FP64 form over the same steps."""
+    dev = torch.cuda.current_device()
+    runs = ensemble_runs(nrun)
+    cfgs = [g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, gridmax=GRIDMAX, lambda0=LAMBDA0, sample=1.0,
+                         gammaref=GAMMA0, precision=g4gpu.MIXED, time_run=1, device=dev)
+            for (ns, npart, ng, _) in runs]
+    t_load = time.perf_counter()
+    b = g4gpu.Batch(cfgs)
+    shapes = {}
+    for r, (m, (ns, npart, ng, taper)) in enumerate(zip(b.members, runs)):
+        lat, beam, cur, fld = ensemble_member(r, ns, npart, ng, taper, g4gpu)
+        m.set_lattice(lat)
+        m.load_beam(beam, cur)
+        m.load_field(0, fld)
+        shapes[f"npart {npart} ngrid {ng}"] = list(m.autotune())
+    t_load = time.perf_counter() - t_load
+    b.run(0, warmup)
+    b.synchronize()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.run(warmup, steps)
+    b.synchronize()
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    slices = sum(x[0] for x in runs)
+    alg = sum(ns * (56 * npart + 16 * ng * ng) for (ns, npart, ng, _) in runs)
+    # error of the smallest runs against the plain FP64 form
+    order = sorted(range(nrun), key=lambda i: runs[i][0] * runs[i][1])[:nerr]
+    errs = []
+    for i in order:
+        ns, npart, ng, taper = runs[i]
+        bm, fm = b.members[i].diag(1)
+        lat, beam, cur, fld = ensemble_member(i, ns, npart, ng, taper, g4gpu)
+        cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, gridmax=GRIDMAX, lambda0=LAMBDA0, sample=1.0,
+                           gammaref=GAMMA0, precision=g4gpu.PLAIN, time_run=1, device=dev)
+        with g4gpu.Handle(cfg) as hp:
+            hp.set_lattice(lat)
+            hp.load_beam(beam, cur)
+            hp.load_field(0, fld)
+            hp.run(0, warmup + steps)
+            bp, fp = hp.diag(1)
+        errs.append(dict(run=i, nslice=ns, npart=npart, ngrid=ng, **diag_error(bm, fm, bp, fp)))
+    b.close()
+    value = slices * steps / (ms / 1e3)
+    achieved = alg * steps / (ms / 1e3) / 1e9
+    return {"value": value, "unit": "slice-steps/s", "ms_per_step": ms / steps, "runs": nrun,
+            "slices": slices, "particles": int(sum(x[0] * x[1] for x in runs)),
+            "draws": "nslice U{64..1024}, npart {2048..16384}, ngrid {101,151,201,255}, taper U[-2%,0], seed 11",
+            "launch": "one handle + stream per run; each run's timed steps one CUDA graph (captured in the "
+                      "timed region: kernels take the ring start by value, so a graph is per starting state)",
+            "launch_shapes": shapes, "setup_s": t_load,
+            "roofline_step": {"alg_bytes_per_step": alg, "achieved_gbs": achieved, "peak": peak,
+                              "frac": achieved / peak},
+            "error_vs_plain": {"runs": errs, "after_steps": warmup + steps,
+                               "power_max_rel": max(e["power_max_rel"] for e in errs),
+                               "bunching_max_rel": max(e["bunching_max_rel"] for e in errs)}}
+
+
+def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_slices=64, max_coarse=63,
+                 check_every=8, tol=0.01):
+    """The coarse-step closure on the full window. Training data: fine (one-period)
+    runs of a train_slices-slice window of the same beam over seeds 100..100+nseeds-1
+    for the first max_coarse coarse steps (4 periods each), mixed form; the network
+    (32 -> 256 -> 256 -> 256 -> 4, BF16 tensor-core GEMMs, FP32 master weights) is
+    trained with Adam on the GPU. Timed: `steps` coarse steps with the closure after
+    `warmup`, with the fine solve judging every check_every coarse steps (fallback
+    above tol relative slice-power error). Throughput counts the fine slice-steps
+    the coarse steps cover. Error: against the plain FP64 fine run."""
+    import learned
+    dev = torch.cuda.current_device()
+    waist, u0, c0 = 30e-6, 1.0, 1.0
+    base = dict(npart=NPART, ngrid=NGRID, gridmax=GRIDMAX, lambda0=LAMBDA0, sample=1.0, gammaref=GAMMA0,
+                precision=g4gpu.MIXED, time_run=1, device=dev)
+    sp = T.slice_params(train_slices, GAMMA0, 2.0, 0.4e-6, 15.0, current=3000.0)
+    t0 = time.perf_counter()
+    X, Tg, clat, fs, fc = learned.generate_training_data(
+        dict(base, nslice=train_slices), lat, range(100, 100 + nseeds), sp, NPART, 4,
+        np.zeros((train_slices, NGRID * NGRID), dtype=np.complex128), waist, u0, c0, max_coarse=max_coarse)
+    t_gen = time.perf_counter() - t0
+    fine_slice_steps = int(nseeds * train_slices * int(fs[max_coarse - 1] + fc[max_coarse - 1]))
+    t0 = time.perf_counter()
+    m = g4gpu.MLP(32, 256, 4, seed=0, device=dev)
+    curve = m.train(X, Tg, epochs=8, batch=512, lr=1e-3, seed=0)
+    t_train = time.perf_counter() - t0
+    fld = np.zeros((NS, NGRID * NGRID), dtype=np.complex128)
+    hf, hc = learned.make_pair(dict(base, nslice=NS), lat, clat, beam, cur, fld, m, waist, u0, c0)
+    hc.run_learned(hf, 0, warmup, fs, fc, check_every=check_every, tol=tol)
+    hc.synchronize()
+    hf.synchronize()
+    stream = torch.cuda.ExternalStream(hc.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    nchk, nfb, emax = hc.run_learned(hf, warmup, steps, fs, fc, check_every=check_every, tol=tol)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    nfine = int(fs[warmup + steps - 1] + fc[warmup + steps - 1])
+    covered = nfine - int(fs[warmup])
+    bl, fl = hc.diag(1)
+    hf.close()
+    hc.close()
+    # references after the same distance: the plain FP64 fine run, and coarse steps
+    # without the closure
+    cfgp = g4gpu.Config(**dict(base, nslice=NS, precision=g4gpu.PLAIN))
+    with g4gpu.Handle(cfgp) as hp:
+        hp.set_lattice(lat)
+        hp.load_beam(beam, cur)
+        hp.load_field(0, fld)
+        hp.run(0, nfine)
+        bp, fp = hp.diag(1)
+    with g4gpu.Handle(g4gpu.Config(**dict(base, nslice=NS))) as hcn:
+        hcn.set_lattice(clat)
+        hcn.load_beam(beam, cur)
+        hcn.load_field(0, fld)
+        hcn.run(0, warmup + steps)
+        bn, fn = hcn.diag(1)
+    m.close()
+    return {"value": NS * covered / (ms / 1e3), "unit": "slice-steps/s (fine steps covered)",
+            "ms_per_coarse_step": ms / steps, "coarse_steps": steps, "fine_steps_covered": covered,
+            "judge": {"check_every": check_every, "tol": tol, "checks": nchk, "fallbacks": nfb,
+                      "max_check_err": emax},
+            "error_vs_plain": dict(diag_error(bl, fl, bp, fp), after_fine_steps=nfine),
+            "coarse_without_closure_error_vs_plain": diag_error(bn, fn, bp, fp),
+            "training": {"samples": int(X.shape[0]), "fine_slice_steps": fine_slice_steps,
+                         "seeds": f"100..{99 + nseeds}", "window": f"{train_slices} slices x {NPART} particles",
+                         "epochs": len(curve), "loss_first": float(curve[0]), "loss_last": float(curve[-1]),
+                         "generate_s": t_gen, "train_s": t_train}}
 
 
 def e2e_window(g4gpu, torch, precision, beam_pinned, cur, field_pinned, lat, steps, reps):
@@ -349,7 +514,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--nslice", type=int, default=None,
                     help="slices of the window (default 4096); smaller values are for profiling only")
-    ap.add_argument("--forms", default="mixed,plain", help="forms to time: mixed, plain or both")
+    ap.add_argument("--forms", default="mixed,plain,batched,learned",
+                    help="forms to time besides the mixed headline: plain, batched, learned")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default launch shapes of the mixed form instead of autotuning them")
     args = ap.parse_args()
     global NS
     if args.nslice:
@@ -373,7 +541,9 @@ def main():
     barrier(ws)
     sampler.start()
     # headline: mixed form
-    hm, ms_m, st_m = time_form(g4gpu, torch, g4gpu.MIXED, beam, cur, lat, args.steps, args.warmup)
+    hm, ms_m, st_m = time_form(g4gpu, torch, g4gpu.MIXED, beam, cur, lat, args.steps, args.warmup,
+                               autotune=not args.no_autotune)
+    shapes = hm.shapes
     barrier(ws)
     clocks = sampler.stop()
     ms_m = max_over_ranks(ws, ms_m)
@@ -428,12 +598,14 @@ def main():
 
     line = {"metric": METRIC, "value": value, "unit": "slice-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_m / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
             "data": "synthetic",
             "config": {"workload": "time-dependent SASE, 4096 slices x 8192 particles, ngrid 151, "
                                    "ADI, 4x110-period planar undulator with FODO, shot noise seed 7",
-                       "form": "mixed (FP32 field/solver/deposition, FP64 phase)",
-                       "cache": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{ws}"},
+                       "form": "mixed (FP32 field/solver/deposition, phase as a 64-bit fixed-point turn count)",
+                       "cache": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{ws}",
+                       "launch_shapes": ({"push_block": shapes[0], "field_threads": shapes[1],
+                                          "source": "g4gpu_autotune"} if shapes else "defaults")},
             "forms": {"mixed": {"value": value, "ms_per_step": ms_m / args.steps},
                       "plain_fp64": ({"value": plain_value, "ms_per_step": ms_p / psteps,
                                       "steps": psteps, "kernels": kernels_plain} if do_plain else None)},
@@ -444,6 +616,10 @@ def main():
                          "alg_bytes_per_launch": dk.get("alg_bytes"), "ms_per_launch": dk["ms_avg"]},
             "kernels": kernels, "gpu_launches": launches, "clocks": clocks}
 
+    if "batched" in args.forms:
+        line["forms"]["batched"] = batched_form(g4gpu, torch, args.steps, args.warmup, peak)
+    if "learned" in args.forms:
+        line["forms"]["learned"] = learned_form(g4gpu, torch, lat, beam, cur, args.steps, args.warmup)
     if rank == 0 and not args.no_e2e:
         field_pinned = torch.zeros((NS, NGRID * NGRID, 2), dtype=torch.float64).pin_memory()
         t, h2d, d2h = e2e_window(g4gpu, torch, g4gpu.MIXED, beam_pinned, cur, field_pinned, lat,

@@ -540,8 +540,11 @@ __device__ __forceinline__ void deposit_smem(const StepConstF &sc, const FieldSt
       // zeros and key -1; they issue no atomics)
       int key = on ? c.i00 : -1;
       bool run_head;
-      bool quads = __all_sync(0xffffffffu, key == __shfl_xor_sync(0xffffffffu, key, 1) &&
-                                               key == __shfl_xor_sync(0xffffffffu, key, 2));
+      // both shuffles run on every lane (a short-circuit && would leave some lanes out
+      // of a full-mask shuffle)
+      const int key1 = __shfl_xor_sync(0xffffffffu, key, 1);
+      const int key2 = __shfl_xor_sync(0xffffffffu, key, 2);
+      bool quads = __all_sync(0xffffffffu, (key == key1) & (key == key2));
       if (quads) {
         // every aligned group of four lanes shares one cell (quiet loading with nbins = 4)
 #pragma unroll
