@@ -163,6 +163,26 @@ void adi_coefficients(double delz, double dgrid, double xks, int ngrid, std::vec
   }
 }
 
+// Warm-up length of the segmented tridiagonal solve for one coefficient set. Both
+// recurrences of the Thomas algorithm, d_k = (r_k - c_k d_{k-1}) cbet_k forward and
+// x_k = d_k - cwet_{k+1} x_{k+1} backward, forget their starting value by the factor
+// |c_k cbet_k| or |cwet_k| per element (about the step factor dz / (4 xks dgrid^2),
+// a few percent on the grids of these runs). A line can then be split into segments
+// solved in parallel, each started W elements early from zero: the error is below
+// alpha^W <= 2^-bits of the solution (bits = 32 for the FP32 solves), under the
+// form's rounding. Returns 0 when alpha is too large for a short warm-up (the solves
+// then run one thread per line).
+int segment_warmup(const std::vector<std::complex<double>> &c, const std::vector<std::complex<double>> &cbet,
+                   const std::vector<std::complex<double>> &cwet, int bits) {
+  double alpha = 0;
+  for (size_t k = 0; k < c.size(); k++) alpha = std::max(alpha, std::max(std::abs(c[k] * cbet[k]), std::abs(cwet[k])));
+  if (!(alpha < 0.5)) return 0;
+  if (alpha <= 0) return 1;
+  int w = (int)std::ceil(std::log(std::ldexp(1.0, -bits)) / std::log(alpha));
+  if (w < 1) w = 1;
+  return w <= 2 * bits / 3 ? w : 0;
+}
+
 // FieldSolverFFT::init (src/Core/FieldSolverFFT.cpp:117-155): the propagator
 // exponent Im(K2) and the source filter on the shifted frequency map, per field,
 // plus the n-th roots of unity and the prime factors of ngrid for the kernels.
@@ -305,13 +325,17 @@ int g4gpu_create(const g4gpu_config *cfg, g4gpu_handle *out) {
     if ((rc = alloc(h, p, np * h->rsize))) return bail(rc);
   if ((rc = alloc(h, &h->beam.theta, np * sizeof(double)))) return bail(rc);
   if ((rc = alloc(h, (void **)&h->beam.current, c.nslice * sizeof(double)))) return bail(rc);
+  // the fused mixed ADI kernel keeps the source and the intermediate on chip: no
+  // source or intermediate arrays
+  const bool fused = h->mixed && c.solver == G4GPU_SOLVER_ADI && c.ngrid <= g4::fused_max_ngrid();
   for (int k = 0; k < c.nfield; k++) {
     if ((rc = alloc(h, &h->field[k], (size_t)c.nslice * ncell * h->csize))) return bail(rc);
-    if ((rc = alloc(h, &h->src[k], (size_t)c.nslice * ncell * h->csize))) return bail(rc);
     cudaMemsetAsync(h->field[k], 0, (size_t)c.nslice * ncell * h->csize, h->stream);
+    if (fused) continue;
+    if ((rc = alloc(h, &h->src[k], (size_t)c.nslice * ncell * h->csize))) return bail(rc);
     cudaMemsetAsync(h->src[k], 0, (size_t)c.nslice * ncell * h->csize, h->stream);
   }
-  if ((rc = alloc(h, &h->tmp, (size_t)c.nslice * ncell * h->csize))) return bail(rc);
+  if (!fused && (rc = alloc(h, &h->tmp, (size_t)c.nslice * ncell * h->csize))) return bail(rc);
   if (c.solver == G4GPU_SOLVER_FFT) {
     if (c.ngrid > g4::fft_max_ngrid(h->mixed))
       return bail(fail(h, G4GPU_ERR_ARG, "ngrid too large for the FFT solver"));
@@ -360,6 +384,7 @@ int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *tab) {
   typedef std::complex<double> cd;
   std::map<std::pair<int, double>, int> sets;  // (field, delz) -> set
   std::vector<cd> coefs;                       // [nset][3][ng]
+  std::vector<int> set_tw;                     // warm-up length per coefficient set
   for (int i = 0; i < nsteps; i++) {
     const double *r = tab + (size_t)i * G4GPU_LAT_NCOL;
     StepConst &s = h->steps[i];
@@ -439,9 +464,11 @@ int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *tab) {
         coefs.insert(coefs.end(), cc.begin(), cc.end());
         coefs.insert(coefs.end(), cb.begin(), cb.end());
         coefs.insert(coefs.end(), cw.begin(), cw.end());
+        set_tw.push_back(segment_warmup(cc, cb, cw, 32));
         it = sets.find(key);
       }
       f.coef = it->second;
+      f.tw = set_tw[it->second];
       f.cstep = 0.25 * s.delz / (fxks * f.dgrid * f.dgrid);
     }
     s.xks = xks;
@@ -597,8 +624,8 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
         for (int k = 0; k < c.nfield; k++) {
           const char *cb = (const char *)h->coef + (size_t)sc.f[k].coef * 3 * ng * h->csize;
           Timed t(h, G4GPU_K_ADI_X);
-          g4::launch_field_fused_mixed(L, scf, k, h->beam, h->field[k], cb, h->tmp, ns, np, ng,
-                                       sc.f[k].dep_on, h->field_threads);
+          g4::launch_field_fused_mixed(L, scf, k, h->beam, h->field[k], cb, ns, np, ng, sc.f[k].dep_on,
+                                       h->field_threads);
         }
       }
     } else {

@@ -29,7 +29,7 @@ struct FieldStep {
   int dep_on;     // deposition active: in undulator and odd harmonic (FieldSolverADI.cpp:20)
   int coef;       // index of the ADI coefficient set of this (field, delz)
   int first;      // ring start of the field when the step runs (filled at launch)
-  int pad;
+  int tw;         // warm-up length of the segmented FP32 tridiagonal solves, 0: not applicable
 };
 
 // Per integration step constants (Undulator accessors, Undulator.h:82-204).
@@ -59,6 +59,7 @@ struct FieldStepF {
   float rtmp, rharm, gridmax, dgrid, cstep;
   float dep_scl;  // fc vacimp xks delz / (4 eev npart dgrid^2): times the slice current
   int dep_on, coef, first, harm;
+  int tw;  // FieldStep::tw
 };
 struct StepConstF {
   float aw_t, qx, qy, xoff, yoff, cxk, cyk;
@@ -74,7 +75,7 @@ StepConstF to_float(const StepConst &s, int npart);
 
 // Device arrays of one time window.
 struct DeviceBeam {
-  void *gamma, *theta, *x, *y, *px, *py;  // theta is always double
+  void *gamma, *theta, *x, *y, *px, *py;  // theta: FP64 (plain) or Q32.32 int64 (mixed), 8 B
   double *current;
 };
 
@@ -113,11 +114,10 @@ void launch_diag_field_mixed(const Launch &L, const void *field, int ns, int ngr
 // Fused deposition + ADI of one field in shared memory, one CTA per slice; usable
 // for ngrid <= fused_max_ngrid() (168: the FP32 slice must fit in 227 KB).
 int fused_max_ngrid();
-// scratch: [nslice][ngrid^2] float2 holding (I + c Dy) u between the two half steps
 // threads: CTA size, a multiple of 32 in [2 ngrid, 1024]
 void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b,
-                              void *field, const void *coef, void *scratch, int ns, int np,
-                              int ngrid, int deposit, int threads);
+                              void *field, const void *coef, int ns, int np, int ngrid, int deposit,
+                              int threads);
 // One ADI step of ns float2 field slices with an optional source, all scratch in the
 // module's static device array (g4gpu_adi_advance_noalloc); coef: [3][ngrid] float2 of
 // c, cbet, cwet. Synchronises `stream`. Returns a G4GPU_ERR_* code with *msg set.

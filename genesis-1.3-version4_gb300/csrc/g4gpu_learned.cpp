@@ -553,6 +553,10 @@ int g4gpu_copy_state(g4gpu_handle dst, g4gpu_handle src) {
 // closure: if the slice power of the coarse+closure result differs from the fine
 // one by more than tol (relative to the largest slice power), the fine result is
 // kept and the following check_every - 1 intervals run with fine steps.
+// The current state lives in one of the two handles at a time: a failed check
+// leaves it in hf, the fallback intervals advance it there, and it is copied back
+// to hc only before the next coarse step (or at the end), so a fallback block costs
+// one state copy, not two per interval.
 int g4gpu_run_learned(g4gpu_handle hc, g4gpu_handle hf, int istep0, int ncoarse, const int *fine_start,
                       const int *fine_count, int check_every, double tol, int *nchecks, int *nfallback,
                       double *max_err) {
@@ -563,20 +567,24 @@ int g4gpu_run_learned(g4gpu_handle hc, g4gpu_handle hf, int istep0, int ncoarse,
   std::vector<double> pc((size_t)nfld * ns * G4GPU_DF_NCOL), pf(pc.size());
   int checks = 0, falls = 0, fine_left = 0;
   double emax = 0;
+  bool in_fine = false;  // the current state is in hf (hc is stale)
+  int rc;
   for (int i = istep0; i < istep0 + ncoarse; i++) {
     if (i < 0 || i >= hc->nsteps) return g4_fail(hc, G4GPU_ERR_ARG, "run_learned: coarse step outside the lattice");
     int f0 = fine_start[i], nf = fine_count[i];
     if (fine_left > 0) {
-      // fallback interval: fine steps, carried back to the coarse handle
-      int rc = g4gpu_copy_state(hf, hc);
-      if (!rc) rc = g4gpu_run(hf, f0, nf, G4GPU_STAGE_ALL);
-      if (!rc) rc = g4gpu_copy_state(hc, hf);
-      if (rc) return rc;
+      // fallback interval: fine steps on hf, where the state already is
+      if (!in_fine && (rc = g4gpu_copy_state(hf, hc))) return rc;
+      in_fine = true;
+      if ((rc = g4gpu_run(hf, f0, nf, G4GPU_STAGE_ALL))) return rc;
       fine_left--;
       continue;
     }
+    if (in_fine) {
+      if ((rc = g4gpu_copy_state(hc, hf))) return rc;
+      in_fine = false;
+    }
     bool check = ((i - istep0) % check_every) == 0;
-    int rc;
     if (check && (rc = g4gpu_copy_state(hf, hc))) return rc;
     closure_features_dev(hc);
     if ((rc = g4gpu_run(hc, i, 1, G4GPU_STAGE_ALL))) return rc;
@@ -596,11 +604,12 @@ int g4gpu_run_learned(g4gpu_handle hc, g4gpu_handle hf, int istep0, int ncoarse,
       emax = std::max(emax, err);
       if (err > tol) {
         falls++;
-        if ((rc = g4gpu_copy_state(hc, hf))) return rc;
+        in_fine = true;  // keep the fine result, which hf holds
         fine_left = check_every - 1;
       }
     }
   }
+  if (in_fine && (rc = g4gpu_copy_state(hc, hf))) return rc;
   if (nchecks) *nchecks = checks;
   if (nfallback) *nfallback = falls;
   if (max_err) *max_err = emax;

@@ -81,13 +81,13 @@ StepConstF to_float(const StepConst &s, int npart) {
     b.coef = a.coef;
     b.first = a.first;
     b.harm = (int)a.rharm;
+    b.tw = a.tw;
   }
   return f;
 }
 
 namespace {
 
-constexpr double kTwoPi = 6.283185307179586476925286766559;
 constexpr float kTwoPiF = 6.283185307f;
 // radians per unit of the low word of the fixed-point phase
 constexpr float kRadPerUnit = 6.283185307f / 4294967296.0f;
@@ -411,19 +411,21 @@ __global__ void __launch_bounds__(128) k_adi_y_f(float2 *__restrict__ field,
 // One CTA per (field, slice). The slice's FP32 field (ngrid^2 float2, 182 KB at
 // ngrid 151) lives in shared memory for the whole solve, so the field is read and
 // written once and the source never touches global memory:
-//   S = u                                   load
-//   S = (I + c Dy) S  + src                  column pass, then deposition (pass 1)
-//   S = Thomas_x(S)                          row sweeps           -> u'
-//   S = (I + c Dx) S  + src                  row pass, then deposition (pass 2)
-//   S = Thomas_y(S)                          column sweeps        -> u''
-//   u = S                                   store
+//   S = u                                   bulk load
+//   S = (I + c Dy) S = S1                    column pass (column segments)
+//   S = S1 + src                             deposition
+//   S = Thomas_x(S)                          row sweeps, two-ended  -> u'
+//   S = 2 u' - S1                            = (I + c Dx) u' + src, because
+//                                              (I - c Dx) u' = S1 + src; S1 recomputed
+//                                              from u, still unmodified in global memory
+//   S = Thomas_y(S)                          column sweeps          -> u''
+//   u = S                                   bulk store
 // This is the reference's ADI (FieldSolverADI.cpp:60-122) with its source
-// (FieldSolverADI.cpp:19-51) added after, instead of before, the stencil term;
-// the deposition is recomputed from the particles for each half step instead of
-// being stored.
+// (FieldSolverADI.cpp:19-51) added after, instead of before, the stencil term, and
+// the second right-hand side formed from the first instead of from a second
+// deposition.
 constexpr int kFusedMaxThreads = 1024;
 
-__device__ __forceinline__ float2 cadd2(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 
 // c * (i * lap): cstep is purely imaginary
 __device__ __forceinline__ float2 stencil(float cs, float2 u, float2 l) {
@@ -475,6 +477,64 @@ __device__ __forceinline__ void thomas2(float2 *S, int stride, int ng, int up, c
   if (!up) S[m * stride] = xm;
 }
 
+// Tridiagonal solve (I - c D) x = r (FieldSolverADI.cpp:94-122: the Thomas recurrences
+// with the cbet / cwet tables) of the ng lines of S, nseg threads per line: thread
+// tid takes line tid % ng and the segment tid / ng of consecutive elements (element
+// k of line l at S[l * lstride + k * estride]). The recurrences forget their start
+// by a factor alpha per element (the host's segment_warmup), so each segment starts
+// W elements before its first element from zero (forward) and W elements after its
+// last one from d (backward): the carries then agree with the full sweep to within
+// alpha^W <= 2^-32. Each warm-up runs on values its neighbour has not yet overwritten
+// (a barrier separates it from the in-place pass). The first segment's forward pass
+// and the last segment's backward pass are the exact sweeps. Every thread of the
+// block must call it.
+__device__ __forceinline__ void thomas_seg(float2 *S, int lstride, int estride, int ng, int nseg, int W,
+                                           const float2 *Cc, const float2 *CB, const float2 *CW) {
+  const int tid = threadIdx.x;
+  const int line = tid % ng, seg = tid / ng;
+  const int len = (ng + nseg - 1) / nseg;
+  const int b = seg * len, e = min(b + len, ng);
+  const bool act = seg < nseg && b < e;
+  float2 *L = S + (size_t)line * lstride;
+  // forward: d_k = (r_k - c_k d_{k-1}) cbet_k
+  float2 d = make_float2(0.f, 0.f);
+  if (act)
+    for (int k = max(0, b - W); k < b; k++) {
+      float2 r = L[k * estride], cd = cmulf(Cc[k], d);
+      d = cmulf(make_float2(r.x - cd.x, r.y - cd.y), CB[k]);
+    }
+  __syncthreads();
+  if (act)
+    for (int k = b; k < e; k++) {
+      float2 r = L[k * estride], cd = cmulf(Cc[k], d);
+      d = cmulf(make_float2(r.x - cd.x, r.y - cd.y), CB[k]);
+      L[k * estride] = d;
+    }
+  __syncthreads();
+  // backward: x_k = d_k - cwet_{k+1} x_{k+1}, x_{ng-1} = d_{ng-1}
+  const int k1 = min(ng - 1, e - 1 + W);
+  float2 x = make_float2(0.f, 0.f);
+  if (act && k1 >= e) {
+    x = L[k1 * estride];
+    for (int k = k1 - 1; k >= e; k--) {
+      float2 v = L[k * estride], cw = cmulf(CW[k + 1], x);
+      x = make_float2(v.x - cw.x, v.y - cw.y);
+    }
+  }
+  __syncthreads();
+  if (act)
+    for (int k = e - 1; k >= b; k--) {
+      float2 v = L[k * estride];
+      if (k < ng - 1) {
+        float2 cw = cmulf(CW[k + 1], x);
+        v = make_float2(v.x - cw.x, v.y - cw.y);
+      }
+      x = v;
+      L[k * estride] = x;
+    }
+  __syncthreads();
+}
+
 // (I + c D) along a line of S with stride, in place, with a rolling register window
 // and the next-but-one element fetched ahead
 __device__ __forceinline__ void stencil_line(float2 *S, int stride, int ng, float cs) {
@@ -491,17 +551,145 @@ __device__ __forceinline__ void stencil_line(float2 *S, int stride, int ng, floa
   }
 }
 
-// Adds the deposited source of beam slice `is` to S with shared-memory atomics.
-// Lanes of a warp whose particles share the lower-left cell (quiet loading stores
+// (I + c Dy) on every column of S in place, each column split into nseg segments of
+// consecutive rows, one thread each (thread tid: column tid % ng, segment tid / ng),
+// so that the column pass has nseg times the threads and 1/nseg the dependent chain
+// of one thread per column. The rows just outside each segment are read before
+// anything is written; every thread of the block must call it. The outputs are the
+// same operations on the same operands as stencil_line's.
+__device__ __forceinline__ void stencil_cols_seg(float2 *S, int ng, float cs, int nseg) {
+  const int tid = threadIdx.x;
+  const int col = tid % ng, seg = tid / ng;
+  const int len = (ng + nseg - 1) / nseg;
+  const int r0 = seg * len, r1 = min(r0 + len, ng);
+  const bool act = seg < nseg && r0 < r1;
+  float2 above = make_float2(0.f, 0.f), below = make_float2(0.f, 0.f);
+  if (act) {
+    if (r0 > 0) above = S[(r0 - 1) * ng + col];
+    if (r1 < ng) below = S[r1 * ng + col];
+  }
+  __syncthreads();
+  if (act) {
+    float2 prev = above, cur = S[r0 * ng + col];
+    float2 next = (r0 + 1 < r1) ? S[(r0 + 1) * ng + col] : below;
+    for (int r = r0; r < r1; r++) {
+      float2 nx = next;
+      if (r + 2 < r1)
+        next = S[(r + 2) * ng + col];
+      else if (r + 2 == r1)
+        next = below;
+      float2 l = lapf(r > 0, r < ng - 1, prev, cur, nx);
+      float2 out = stencil(cs, cur, l);
+      prev = cur;
+      cur = nx;
+      S[r * ng + col] = out;
+    }
+  }
+}
+
+// The second right-hand side, S = 2 u' - S1 with S1 = (I + c Dy) u recomputed from
+// the slice still unmodified in global memory (read through L2, where the slice
+// load left it) instead of stored: the same column segments and the same operations
+// as stencil_cols_seg, so S1 is bitwise the value the first half step used.
+__device__ __forceinline__ void r2_cols_seg(float2 *S, const float2 *__restrict__ u, int ng, float cs,
+                                            int nseg) {
+  const int tid = threadIdx.x;
+  const int col = tid % ng, seg = tid / ng;
+  const int len = (ng + nseg - 1) / nseg;
+  const int r0 = seg * len, r1 = min(r0 + len, ng);
+  if (seg >= nseg || r0 >= r1) return;
+  float2 prev = r0 > 0 ? u[(r0 - 1) * ng + col] : make_float2(0.f, 0.f);
+  float2 cur = u[r0 * ng + col];
+  float2 next = r0 + 1 < ng ? u[(r0 + 1) * ng + col] : make_float2(0.f, 0.f);
+  for (int r = r0; r < r1; r++) {
+    float2 nx = next;
+    if (r + 2 < ng) next = u[(r + 2) * ng + col];
+    float2 l = lapf(r > 0, r < ng - 1, prev, cur, nx);
+    float2 s1 = stencil(cs, cur, l);
+    prev = cur;
+    cur = nx;
+    float2 v = S[r * ng + col];
+    S[r * ng + col] = make_float2(2.f * v.x - s1.x, 2.f * v.y - s1.y);
+  }
+}
+
+// Adds the source contribution of the 32 particles held by the lanes of a warp (one
+// each; lanes past the end carry x = 1e30, off the grid) to S with shared-memory
+// atomics. Lanes whose particles share the lower-left cell (quiet loading stores
 // the nbins mirrored beamlet members, which share x and y, in adjacent lanes) first
 // sum their four weighted contributions with a segmented shuffle reduction over
 // runs of equal cells; only the first lane of each run issues the atomics. This cuts
 // the atomics (and their same-address conflicts) by the run length and keeps the
-// result exact up to FP32 summation order.
+// result exact up to FP32 summation order. Every lane of the warp must call it.
+__device__ __forceinline__ void deposit_lanes(const StepConstF &sc, const FieldStepF &fs, float scl, float2 *S,
+                                              int ng, float x, float y, long long th, float dgam) {
+  const unsigned lane = threadIdx.x & 31u;
+  CellF c;
+  bool on = ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x, y, c);
+  float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (on) {
+    float g = (float)sc.gammaref + dgam;
+    float dx = x - sc.ax, dy = y - sc.ay;
+    float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
+    float part = sqrtf(faw2) * scl / g;
+    float sn, co;
+    __sincosf(phase_of(th, (unsigned)fs.harm), &sn, &co);
+    float cpx = sn * part, cpy = co * part;
+    float w00 = c.wx * c.wy, w10 = (1.f - c.wx) * c.wy, w01 = c.wx * (1.f - c.wy),
+          w11 = (1.f - c.wx) * (1.f - c.wy);
+    v[0] = w00 * cpx; v[1] = w00 * cpy; v[2] = w10 * cpx; v[3] = w10 * cpy;
+    v[4] = w01 * cpx; v[5] = w01 * cpy; v[6] = w11 * cpx; v[7] = w11 * cpy;
+  }
+  // runs of equal lower-left cells among adjacent lanes (off-grid lanes carry
+  // zeros and key -1; they issue no atomics)
+  int key = on ? c.i00 : -1;
+  bool run_head;
+  // both shuffles run on every lane (a short-circuit && would leave some lanes out
+  // of a full-mask shuffle)
+  const int key1 = __shfl_xor_sync(0xffffffffu, key, 1);
+  const int key2 = __shfl_xor_sync(0xffffffffu, key, 2);
+  bool quads = __all_sync(0xffffffffu, (key == key1) & (key == key2));
+  if (quads) {
+    // every aligned group of four lanes shares one cell (quiet loading with nbins = 4)
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      v[q] += __shfl_xor_sync(0xffffffffu, v[q], 1);
+      v[q] += __shfl_xor_sync(0xffffffffu, v[q], 2);
+    }
+    run_head = (lane & 3u) == 0u;
+  } else {
+    int knext = __shfl_down_sync(0xffffffffu, key, 1);
+    int kprev = __shfl_up_sync(0xffffffffu, key, 1);
+    bool run_end = (lane == 31u) || (knext != key);
+    run_head = (lane == 0u) || (kprev != key);
+    unsigned ends = __ballot_sync(0xffffffffu, run_end);
+    int seg_end = __ffs(ends & (0xffffffffu << lane)) - 1;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        float o = __shfl_down_sync(0xffffffffu, v[q], off);
+        if ((int)lane + off <= seg_end) v[q] += o;
+      }
+    }
+  }
+  if (on && run_head) {
+    atomicAdd(&S[c.i00].x, v[0]);
+    atomicAdd(&S[c.i00].y, v[1]);
+    atomicAdd(&S[c.i10].x, v[2]);
+    atomicAdd(&S[c.i10].y, v[3]);
+    atomicAdd(&S[c.i01].x, v[4]);
+    atomicAdd(&S[c.i01].y, v[5]);
+    atomicAdd(&S[c.i11].x, v[6]);
+    atomicAdd(&S[c.i11].y, v[7]);
+  }
+}
+
+// Adds the deposited source of beam slice `is` to S, the particles read from global
+// memory (used when no staging buffer fits beside the slice).
 __device__ __forceinline__ void deposit_smem(const StepConstF &sc, const FieldStepF &fs,
                                              const PtrsF &p, float2 *S, int is, int np, int ng) {
-  const float cur = (float)p.current[is];
-  const float scl = fs.dep_scl * cur;
+  const float scl = fs.dep_scl * (float)p.current[is];
   const size_t base = (size_t)is * np;
   const unsigned lane = threadIdx.x & 31u;
   const int warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
@@ -519,69 +707,102 @@ __device__ __forceinline__ void deposit_smem(const StepConstF &sc, const FieldSt
       gs[u] = in ? p.dg[base + ip] : 0.f;
     }
 #pragma unroll
-    for (int u = 0; u < U; u++) {
-      CellF c;
-      bool on = ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, xs[u], ys[u], c);
-      float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      if (on) {
-        float g = (float)sc.gammaref + gs[u];
-        float dx = xs[u] - sc.ax, dy = ys[u] - sc.ay;
-        float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
-        float part = sqrtf(faw2) * scl / g;
-        float sn, co;
-        __sincosf(phase_of(ths[u], (unsigned)fs.harm), &sn, &co);
-        float cpx = sn * part, cpy = co * part;
-        float w00 = c.wx * c.wy, w10 = (1.f - c.wx) * c.wy, w01 = c.wx * (1.f - c.wy),
-              w11 = (1.f - c.wx) * (1.f - c.wy);
-        v[0] = w00 * cpx; v[1] = w00 * cpy; v[2] = w10 * cpx; v[3] = w10 * cpy;
-        v[4] = w01 * cpx; v[5] = w01 * cpy; v[6] = w11 * cpx; v[7] = w11 * cpy;
-      }
-      // runs of equal lower-left cells among adjacent lanes (off-grid lanes carry
-      // zeros and key -1; they issue no atomics)
-      int key = on ? c.i00 : -1;
-      bool run_head;
-      // both shuffles run on every lane (a short-circuit && would leave some lanes out
-      // of a full-mask shuffle)
-      const int key1 = __shfl_xor_sync(0xffffffffu, key, 1);
-      const int key2 = __shfl_xor_sync(0xffffffffu, key, 2);
-      bool quads = __all_sync(0xffffffffu, (key == key1) & (key == key2));
-      if (quads) {
-        // every aligned group of four lanes shares one cell (quiet loading with nbins = 4)
+    for (int u = 0; u < U; u++) deposit_lanes(sc, fs, scl, S, ng, xs[u], ys[u], ths[u], gs[u]);
+  }
+}
+
+// The contribution of one particle to the four cells around it (no aggregation).
+__device__ __forceinline__ void deposit_one(const StepConstF &sc, const FieldStepF &fs, float scl, float2 *S,
+                                            int ng, float x, float y, long long th, float dgam) {
+  CellF c;
+  if (!ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x, y, c)) return;
+  float dx = x - sc.ax, dy = y - sc.ay;
+  float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
+  float part = sqrtf(faw2) * scl / ((float)sc.gammaref + dgam);
+  float sn, co;
+  __sincosf(phase_of(th, (unsigned)fs.harm), &sn, &co);
+  float cpx = sn * part, cpy = co * part;
+  float w00 = c.wx * c.wy, w10 = (1.f - c.wx) * c.wy, w01 = c.wx * (1.f - c.wy), w11 = (1.f - c.wx) * (1.f - c.wy);
+  atomicAdd(&S[c.i00].x, w00 * cpx);
+  atomicAdd(&S[c.i00].y, w00 * cpy);
+  atomicAdd(&S[c.i10].x, w10 * cpx);
+  atomicAdd(&S[c.i10].y, w10 * cpy);
+  atomicAdd(&S[c.i01].x, w01 * cpx);
+  atomicAdd(&S[c.i01].y, w01 * cpy);
+  atomicAdd(&S[c.i11].x, w11 * cpx);
+  atomicAdd(&S[c.i11].y, w11 * cpy);
+}
+
+// The summed contribution of n particles that share x and y (one cell, one set of
+// weights, one undulator factor), n = 2 or 4.
+template <int N>
+__device__ __forceinline__ void deposit_group(const StepConstF &sc, const FieldStepF &fs, float scl, float2 *S,
+                                              int ng, float x, float y, const long long *th, const float *dgam) {
+  CellF c;
+  if (!ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x, y, c)) return;
+  float dx = x - sc.ax, dy = y - sc.ay;
+  float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
+  float a = sqrtf(faw2) * scl;
+  float cpx = 0.f, cpy = 0.f;
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-          v[q] += __shfl_xor_sync(0xffffffffu, v[q], 1);
-          v[q] += __shfl_xor_sync(0xffffffffu, v[q], 2);
-        }
-        run_head = (lane & 3u) == 0u;
+  for (int m = 0; m < N; m++) {
+    float part = a / ((float)sc.gammaref + dgam[m]);
+    float sn, co;
+    __sincosf(phase_of(th[m], (unsigned)fs.harm), &sn, &co);
+    cpx += sn * part;
+    cpy += co * part;
+  }
+  float w00 = c.wx * c.wy, w10 = (1.f - c.wx) * c.wy, w01 = c.wx * (1.f - c.wy), w11 = (1.f - c.wx) * (1.f - c.wy);
+  atomicAdd(&S[c.i00].x, w00 * cpx);
+  atomicAdd(&S[c.i00].y, w00 * cpy);
+  atomicAdd(&S[c.i10].x, w10 * cpx);
+  atomicAdd(&S[c.i10].y, w10 * cpy);
+  atomicAdd(&S[c.i01].x, w01 * cpx);
+  atomicAdd(&S[c.i01].y, w01 * cpy);
+  atomicAdd(&S[c.i11].x, w11 * cpx);
+  atomicAdd(&S[c.i11].y, w11 * cpy);
+}
+
+// Adds the deposited source of beam slice `is` to S with one thread per four
+// consecutive particles. Quiet loading stores the nbins mirrored members of a
+// beamlet consecutively (nbins a multiple of 4 gives aligned groups of four sharing
+// x and y; nbins = 2, pairs): a group that shares x and y is deposited once with the
+// sum of its members' phasors, pairs likewise, anything else particle by particle.
+// No warp-level exchange is needed, and the loads are 16-byte vectors. Needs
+// npart % 4 == 0.
+__device__ __forceinline__ void deposit_quads(const StepConstF &sc, const FieldStepF &fs, const PtrsF &p,
+                                              float2 *S, int is, int np, int ng) {
+  const float scl = fs.dep_scl * (float)p.current[is];
+  const size_t base = (size_t)is * np;
+  const float4 *X = reinterpret_cast<const float4 *>(p.x + base);
+  const float4 *Y = reinterpret_cast<const float4 *>(p.y + base);
+  const float4 *G = reinterpret_cast<const float4 *>(p.dg + base);
+  const longlong2 *T = reinterpret_cast<const longlong2 *>(p.theta + base);
+  for (int q = threadIdx.x; q < (np >> 2); q += blockDim.x) {
+    const float4 x = X[q], y = Y[q], g = G[q];
+    const longlong2 t01 = T[2 * q], t23 = T[2 * q + 1];
+    const long long th[4] = {t01.x, t01.y, t23.x, t23.y};
+    const float dg[4] = {g.x, g.y, g.z, g.w};
+    const bool p01 = x.x == x.y && y.x == y.y, p23 = x.z == x.w && y.z == y.w;
+    if (p01 && p23 && x.x == x.z && y.x == y.z) {
+      deposit_group<4>(sc, fs, scl, S, ng, x.x, y.x, th, dg);
+    } else {
+      if (p01) {
+        deposit_group<2>(sc, fs, scl, S, ng, x.x, y.x, th, dg);
       } else {
-        int knext = __shfl_down_sync(0xffffffffu, key, 1);
-        int kprev = __shfl_up_sync(0xffffffffu, key, 1);
-        bool run_end = (lane == 31u) || (knext != key);
-        run_head = (lane == 0u) || (kprev != key);
-        unsigned ends = __ballot_sync(0xffffffffu, run_end);
-        int seg_end = __ffs(ends & (0xffffffffu << lane)) - 1;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-#pragma unroll
-          for (int q = 0; q < 8; q++) {
-            float o = __shfl_down_sync(0xffffffffu, v[q], off);
-            if ((int)lane + off <= seg_end) v[q] += o;
-          }
-        }
+        deposit_one(sc, fs, scl, S, ng, x.x, y.x, th[0], dg[0]);
+        deposit_one(sc, fs, scl, S, ng, x.y, y.y, th[1], dg[1]);
       }
-      if (on && run_head) {
-        atomicAdd(&S[c.i00].x, v[0]);
-        atomicAdd(&S[c.i00].y, v[1]);
-        atomicAdd(&S[c.i10].x, v[2]);
-        atomicAdd(&S[c.i10].y, v[3]);
-        atomicAdd(&S[c.i01].x, v[4]);
-        atomicAdd(&S[c.i01].y, v[5]);
-        atomicAdd(&S[c.i11].x, v[6]);
-        atomicAdd(&S[c.i11].y, v[7]);
+      if (p23) {
+        deposit_group<2>(sc, fs, scl, S, ng, x.z, y.z, th + 2, dg + 2);
+      } else {
+        deposit_one(sc, fs, scl, S, ng, x.z, y.z, th[2], dg[2]);
+        deposit_one(sc, fs, scl, S, ng, x.w, y.w, th[3], dg[3]);
       }
     }
   }
 }
+
 
 // Bounded wait on an mbarrier phase; returns false (and raises the device error
 // flag) if the phase does not complete within the iteration limit.
@@ -647,15 +868,13 @@ __device__ __forceinline__ void bulk_store(float2 *g, const float2 *s, int count
 
 __global__ void __launch_bounds__(kFusedMaxThreads, 1)
     k_field_fused_f(StepConstF sc, int k, PtrsF p, float2 *__restrict__ field,
-                    const float2 *__restrict__ coef, float2 *__restrict__ scratch, int ns, int np,
-                    int ng, int deposit, int *err) {
+                    const float2 *__restrict__ coef, int ns, int np, int ng, int deposit, int *err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int ncell = ng * ng;
   const FieldStepF &fs = sc.f[k];
   int is = blockIdx.x;
   int i = (is + fs.first) % ns;
   float2 *u = field + (size_t)i * ncell;
-  float2 *s1 = scratch + (size_t)i * ncell;  // (I + c Dy) u of this slice
   // layout: [mbarrier 16 B][solve constants 16 B][coefficients 3 ng][pad][S: ncell],
   // S congruent to u mod 16 (the bulk copies need equal alignment on both sides)
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);
@@ -688,33 +907,36 @@ __global__ void __launch_bounds__(kFusedMaxThreads, 1)
   if (!bulk_load(S, u, ncell, bar_s, err)) return;
   const float cs = fs.cstep;
   const int tid = threadIdx.x;
-  if (tid < ng) stencil_line(S + tid, ng, ng, cs);  // column tid: S1 = (I + c Dy) u
-  // keep S1 for the second half step: (I + c Dx) u' + src = 2 u' - S1, because
-  // (I - c Dx) u' = S1 + src; this replaces the second deposition
-  bulk_store(s1, S, ncell);
-  if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+  const int nseg = max(1, min((int)blockDim.x / ng, 8));
+  stencil_cols_seg(S, ng, cs, nseg);  // S1 = (I + c Dy) u
   __syncthreads();
-  if (deposit) {
-    deposit_smem(sc, fs, p, S, is, np, ng);  // S = S1 + src
+  if (deposit) {  // S = S1 + src
+    if ((np & 3) == 0)
+      deposit_quads(sc, fs, p, S, is, np, ng);
+    else
+      deposit_smem(sc, fs, p, S, is, np, ng);
     __syncthreads();
   }
   const float2 invden = K[0];
   const int line = tid >> 1, up = tid & 1;
-  // lanes 2l and 2l+1 solve line l; the mask covers the lanes of the warp with a line
+  // segmented solves when the recurrences forget fast enough (tw > 0) and a line gets
+  // at least two threads; else the two-ended solve: lanes 2l and 2l+1 on line l, the
+  // mask covering the lanes of the warp with a line
+  const bool segmented = fs.tw > 0 && nseg >= 2;
   const unsigned mask = __ballot_sync(0xffffffffu, line < ng);
-  if (line < ng) thomas2(S + line * ng, 1, ng, up, CB, CW, a, invden, mask);  // rows: u'
-  // the bulk store of S1 must have landed before it is read back
-  if (threadIdx.x == 0) {
-    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
-    asm volatile("fence.proxy.async.global;" ::: "memory");
-  }
+  if (segmented)
+    thomas_seg(S, ng, 1, ng, nseg, fs.tw, C, CB, CW);  // rows: u'
+  else if (line < ng)
+    thomas2(S + line * ng, 1, ng, up, CB, CW, a, invden, mask);
   __syncthreads();
-  for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
-    float2 v = S[t], w = s1[t];
-    S[t] = make_float2(2.f * v.x - w.x, 2.f * v.y - w.y);
-  }
+  // (I + c Dx) u' + src = 2 u' - S1, because (I - c Dx) u' = S1 + src: the second
+  // right-hand side needs neither a second deposition nor a stored S1
+  r2_cols_seg(S, u, ng, cs, nseg);
   __syncthreads();
-  if (line < ng) thomas2(S + line, ng, ng, up, CB, CW, a, invden, mask);  // columns
+  if (segmented)
+    thomas_seg(S, 1, ng, ng, nseg, fs.tw, C, CB, CW);  // columns
+  else if (line < ng)
+    thomas2(S + line, ng, ng, up, CB, CW, a, invden, mask);
   __syncthreads();
   bulk_store(u, S, ncell);
   if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
@@ -969,7 +1191,29 @@ __global__ void __launch_bounds__(kFusedMaxThreads, 1)
   }
 }
 
+// complex arithmetic of the mixed form for the tiled ADI (adi_tiled.cuh), as in
+// k_adi_x_f / k_adi_y_f
+struct MixedOps {
+  using V = float2;
+  using G = float2;
+  using R = float;
+  static __device__ __forceinline__ V ld(const G *p) { return *p; }
+  static __device__ __forceinline__ void st(G *p, V v) { *p = v; }
+  static __device__ __forceinline__ V zero() { return make_float2(0.f, 0.f); }
+  static __device__ __forceinline__ V sub(V a, V b) { return make_float2(a.x - b.x, a.y - b.y); }
+  static __device__ __forceinline__ V mul(V a, V b) { return cmulf(a, b); }
+  static __device__ __forceinline__ V lap(bool hp, bool hn, V p, V u, V n) { return lapf(hp, hn, p, u, n); }
+  static __device__ __forceinline__ V rhs(V s, V u, V l, R cs) {
+    return make_float2(s.x + u.x - cs * l.y, s.y + u.y + cs * l.x);
+  }
+};
+
 }  // namespace
+}  // namespace g4
+
+#include "adi_tiled.cuh"
+
+namespace g4 {
 
 void launch_push_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,
                        void *const *field, void *const *src, int ns, int np, int ngrid,
@@ -1001,10 +1245,33 @@ void launch_deposit_mixed(const Launch &L, const StepConstF &sc, const DeviceBea
 void launch_adi_mixed(const Launch &L, const StepConstF &sc, int k, int phase, void *field,
                       const void *src, void *tmp, const void *coef, int ns, int ngrid) {
   const float2 *cb = (const float2 *)coef;
+  cudaStream_t s = (cudaStream_t)L.stream;
+  // tiled passes (adi_tiled.cuh) when their tiles fit a CTA's shared memory
+  const int R = tiled::band_rows(ngrid, sizeof(float2)), Cw = tiled::band_cols(ngrid, sizeof(float2));
+  const size_t smx = (size_t)(2 * R + 2) * ngrid * sizeof(float2), smy = (size_t)ngrid * Cw * sizeof(float2);
+  if (smx <= 227u * 1024u && smy <= 227u * 1024u) {
+    static unsigned long long configured = 0;  // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 64 && !(configured & (1ull << dev))) {
+      cudaFuncSetAttribute(tiled::k_adi_xt<MixedOps, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      cudaFuncSetAttribute(tiled::k_adi_yt<MixedOps, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      configured |= 1ull << dev;
+    }
+    tiled::CoefP<MixedOps> cf{cb, cb + ngrid, cb + 2 * ngrid};
+    const int W = sc.f[k].tw;
+    if (phase == 0)
+      tiled::k_adi_xt<MixedOps, 256><<<dim3((ngrid + R - 1) / R, ns), 256, smx, s>>>(
+          (const float2 *)field, (const float2 *)src, (float2 *)tmp, cf, sc.f[k].cstep, ns, ngrid,
+          sc.f[k].first, R, W);
+    else
+      tiled::k_adi_yt<MixedOps, 256><<<dim3((ngrid + Cw - 1) / Cw, ns), 256, smy, s>>>(
+          (float2 *)field, (const float2 *)tmp, cf, ns, ngrid, sc.f[k].first, Cw, W);
+    return;
+  }
   CoefF cf{cb, cb + ngrid, cb + 2 * ngrid};
   long long n = (long long)ns * ngrid;
   unsigned blocks = (unsigned)((n + 127) / 128);
-  cudaStream_t s = (cudaStream_t)L.stream;
   if (phase == 0)
     k_adi_x_f<<<blocks, 128, 0, s>>>((const float2 *)field, (const float2 *)src, (float2 *)tmp, cf,
                                      sc.f[k].cstep, ns, ngrid, sc.f[k].first);
@@ -1035,8 +1302,8 @@ int fused_max_ngrid() {
 }
 
 void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b,
-                              void *field, const void *coef, void *scratch, int ns, int np,
-                              int ngrid, int deposit, int threads) {
+                              void *field, const void *coef, int ns, int np, int ngrid, int deposit,
+                              int threads) {
   static unsigned long long configured = 0;  // one bit per device
   size_t smem = fused_smem_bytes(ngrid);
   int dev = 0;
@@ -1049,8 +1316,7 @@ void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, cons
   if (threads < 2 * ngrid) threads = (2 * ngrid + 31) / 32 * 32;
   if (threads > kFusedMaxThreads) threads = kFusedMaxThreads;
   k_field_fused_f<<<ns, threads, smem, (cudaStream_t)L.stream>>>(
-      sc, k, p, (float2 *)field, (const float2 *)coef, (float2 *)scratch, ns, np, ngrid, deposit,
-      L.err);
+      sc, k, p, (float2 *)field, (const float2 *)coef, ns, np, ngrid, deposit, L.err);
 }
 
 namespace {

@@ -473,6 +473,7 @@ Ptrs make_ptrs(const DeviceBeam &b, void *const *field, void *const *src, int nf
   return p;
 }
 
+
 }  // namespace
 
 void launch_push_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,
@@ -505,10 +506,15 @@ void launch_deposit_plain(const Launch &L, const StepConst &sc, const DeviceBeam
 void launch_adi_plain(const Launch &L, const StepConst &sc, int k, int phase, void *field,
                       const void *src, void *tmp, const void *coef, int ns, int ngrid) {
   const double2 *cb = (const double2 *)coef;
+  cudaStream_t s = (cudaStream_t)L.stream;
+  // One thread per grid line over all slices. The FP64 ADI is bound by the FP64 rate
+  // (about 76 FP64 operations per cell and step; GB300 runs FP64 at 1/64 of the FP32
+  // rate), not by memory: these kernels keep every line's sweep as the reference's single
+  // sequential pass. The tiled passes of adi_tiled.cuh, which split lines into segments
+  // with redundant warm-up work, were measured slower for this form.
   Coef cf{cb, cb + ngrid, cb + 2 * ngrid};
   long long n = (long long)ns * ngrid;
   unsigned blocks = (unsigned)((n + 127) / 128);
-  cudaStream_t s = (cudaStream_t)L.stream;
   if (phase == 0)
     k_adi_x<<<blocks, 128, 0, s>>>((const double2 *)field, (const double2 *)src, (double2 *)tmp,
                                    cf, sc.f[k].cstep, ns, ngrid, sc.f[k].first);

@@ -258,6 +258,34 @@ def test_mixed_full_slices_with_split_beamlets_match_plain(lib, nbins, split):
     assert bunching_ok(bm[:, 24], bp[:, 24])
 
 
+@pytest.mark.parametrize("ng", [181, 255])
+def test_mixed_large_grid_close_to_oracle(lib, oracle, ng):
+    """Mixed form on grids too large for the fused kernel (tiled two-pass ADI, FP32):
+    slice power and bunching within 1 % of the FP64 oracle after 12 steps with a
+    seeded field."""
+    import g4gpu
+    import g4cases as T
+    ns, npart, gm, g0 = 8, 512, 1e-4, 17081.0
+    lat = T.undulator_lattice(1.7, 0.015, 12, 1, 1e-10, g0)
+    cur = np.full(ns, 3000.0)
+    beam = g4gpu.host_load_beam(T.slice_params(ns, g0, 2.0, 0.4e-6, 15.0, currents=cur), 0, npart, 4, 3, 1,
+                                1e-10, 1.0)
+    seed = g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e5, 30e-6), gm, ng)
+    fld = np.repeat(seed[None, :], ns, axis=0)
+    with handle_for(g4gpu, ns, npart, ng, [1], [gm], g0, 1, 1, 0) as h:
+        h.set_lattice(lat)
+        h.load_beam(beam, cur)
+        h.load_field(0, fld)
+        h.run(0, lat.shape[0])
+        bd, fd = h.diag(1)
+    p, f, ofirst, _ = oracle.run_steps(lat, g0, beam, cur, 1e-10, 1.0, [1], [gm], fld[None], [0], time_run=1,
+                                       nthreads=8)
+    ob = oracle.diag_beam(p, 1)
+    of = oracle.diag_field(f[0], gm, 1e-10, 1, int(ofirst[0]))
+    assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-2
+    assert bunching_ok(bd[:, 24], ob[:, 24])
+
+
 def test_run_before_load_is_an_error(lib):
     import g4gpu
     with handle_for(g4gpu, 2, 8, 11, [1], [1e-4], 11357.8, 0, 1, 0) as h:
