@@ -27,7 +27,9 @@ Arms:
                       (oracle/g4oracle.c), on a bounded sample of the workload.
 
 Under torchrun (N > 1) every rank runs its own window on its GPU (independent
-replicas, weak scaling); the slowest rank's time sets the value.
+replicas, weak scaling); the slowest rank's time sets the value. The environment
+variable G4_BENCH_GLOO selects the gloo backend for the ranks' barrier and
+reduction (CPU tests of the multi-process path); NCCL otherwise.
 """
 import argparse
 import json
@@ -141,8 +143,14 @@ def dist_setup():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl" if os.environ.get("G4_BENCH_GLOO") is None else "gloo")
+        if not dist.is_initialized():
+            dist.init_process_group("nccl" if os.environ.get("G4_BENCH_GLOO") is None else "gloo")
     return ws, rank, local
+
+
+def _on_gpu():
+    import torch.distributed as dist
+    return dist.get_backend() == "nccl"
 
 
 def barrier(ws):
@@ -150,17 +158,36 @@ def barrier(ws):
         import torch
         import torch.distributed as dist
         dist.barrier()
-        torch.cuda.synchronize()
+        if _on_gpu():
+            torch.cuda.synchronize()
 
 
 def max_over_ranks(ws, v):
+    """The largest of the ranks' values (every rank gets it): the slowest replica's
+    time sets the job's."""
     if ws == 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if _on_gpu() else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def job_value(ws, slices_per_rank, steps, ms_max):
+    """Whole-job slice-steps/s: every rank advances its own window of slices_per_rank
+    slices by `steps` steps (independent replicas), and the slowest rank's time
+    ms_max bounds the job."""
+    return slices_per_rank * ws * steps / (ms_max / 1e3)
+
+
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per slice of one launch,
+# from the ncu --set full capture of a 608-slice window of the same workload
+# (profiles/ncu_full_k_push_f_k_field_fused_f_sase608.md); the traffic of these kernels
+# grows in proportion to the slices of a launch, so a full launch's is the per-slice
+# figure times the slices.
+TRAFFIC_PER_SLICE = {"field": 448487.0, "push": 432237.0}
+TRAFFIC_SOURCE = "ncu capture of a 608-slice window, scaled to the launch's slices"
 
 
 def alg_bytes_per_slice_step(mixed):
@@ -400,25 +427,34 @@ def e2e_window(g4gpu, torch, precision, beam_pinned, cur, field_pinned, lat, ste
     cur_np = np.ascontiguousarray(cur)
     times = []
     d2h_diag = 0
-    for rep in range(reps + 1):
+    for rep in range(reps + 2):
+        # the first window is the warm-up; the last one is split into its phases
+        split = rep == reps + 1
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         h.load_beam_ptr(beam_pinned.data_ptr(), cur_np.ctypes.data)
         h.load_field_ptr(0, field_pinned.data_ptr())
+        if split:
+            h.synchronize()
+            t_up = time.perf_counter()
         d2h_diag = 0
         for i in range(steps):
             h.run(i, 1)
             bd, fd = h.diag(1)
             d2h_diag += bd.nbytes + fd.nbytes
+        if split:
+            t_steps = time.perf_counter()
         h.get_beam(out_beam.numpy())
         h.get_field(0, out_field.numpy().view(np.complex128).reshape(NS, NGRID * NGRID))
         t1 = time.perf_counter()
-        if rep > 0:  # the first window is the warm-up
+        if split:
+            phases = {"upload_s": t_up - t0, "steps_with_diag_s": t_steps - t_up, "download_s": t1 - t_steps}
+        elif rep > 0:
             times.append(t1 - t0)
     h.close()
     h2d = beam_pinned.numel() * 8 + cur_np.nbytes + field_pinned.numel() * 8
     d2h = d2h_diag + out_beam.numel() * 8 + out_field.numel() * 8
-    return min(times), h2d, d2h
+    return min(times), h2d, d2h, phases
 
 
 def cpu_baseline(nthreads, target_seconds=12.0, prefer_reference=True):
@@ -567,8 +603,8 @@ def main():
     if do_plain:
         hp.close()
 
-    value = NS * ws / (ms_m / args.steps / 1e3)
-    plain_value = NS * ws / (ms_p / psteps / 1e3) if do_plain else None
+    value = job_value(ws, NS, args.steps, ms_m)
+    plain_value = job_value(ws, NS, psteps, ms_p) if do_plain else None
     launches = sum(v[0] for v in st_m.values())
 
     def kernel_table(st, mixed):
@@ -605,13 +641,16 @@ def main():
                        "form": "mixed (FP32 field/solver/deposition, phase as a 64-bit fixed-point turn count)",
                        "cache": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{ws}",
                        "launch_shapes": ({"push_block": shapes[0], "field_threads": shapes[1],
+                                          "field_kernel": ["one CTA per slice", "cluster pair"][shapes[2]],
                                           "source": "g4gpu_autotune"} if shapes else "defaults")},
             "forms": {"mixed": {"value": value, "ms_per_step": ms_m / args.steps},
                       "plain_fp64": ({"value": plain_value, "ms_per_step": ms_p / psteps,
                                       "steps": psteps, "kernels": kernels_plain} if do_plain else None)},
             "mixed_error_vs_plain": err,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": dk.get("achieved_gbs"), "peak": peak,
-                         "unit": "GB/s", "frac": dk.get("frac_hbm"), "traffic": None,
+                         "unit": "GB/s", "frac": dk.get("frac_hbm"),
+                         "traffic": (TRAFFIC_PER_SLICE[dom] * NS if dom in TRAFFIC_PER_SLICE else None),
+                         "traffic_source": TRAFFIC_SOURCE,
                          "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                          "alg_bytes_per_launch": dk.get("alg_bytes"), "ms_per_launch": dk["ms_avg"]},
             "kernels": kernels, "gpu_launches": launches, "clocks": clocks}
@@ -622,11 +661,12 @@ def main():
         line["forms"]["learned"] = learned_form(g4gpu, torch, lat, beam, cur, args.steps, args.warmup)
     if rank == 0 and not args.no_e2e:
         field_pinned = torch.zeros((NS, NGRID * NGRID, 2), dtype=torch.float64).pin_memory()
-        t, h2d, d2h = e2e_window(g4gpu, torch, g4gpu.MIXED, beam_pinned, cur, field_pinned, lat,
-                                 args.steps, 2)
+        t, h2d, d2h, phases = e2e_window(g4gpu, torch, g4gpu.MIXED, beam_pinned, cur, field_pinned, lat,
+                                         args.steps, 2)
         line["e2e"] = {"value": NS * args.steps / t, "unit": "slice-steps/s",
                        "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-                       "window": f"upload beam+field, {args.steps} steps with per-step diagnostics read-back, download"}
+                       "window": f"upload beam+field, {args.steps} steps with per-step diagnostics read-back, download",
+                       "window_s": t, "phases_of_one_window": phases}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1)
     if rank == 0:

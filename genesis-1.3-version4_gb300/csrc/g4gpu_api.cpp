@@ -367,6 +367,7 @@ void g4gpu_destroy(g4gpu_handle h) {
     cudaEventDestroy(p.b);
   }
   for (auto ev : h->pool) cudaEventDestroy(ev);
+  if (h->hdiag) cudaFreeHost(h->hdiag);
   for (auto &g : h->graphs)
     if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -612,9 +613,14 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
     for (int k = 0; k < c.nfield; k++) sc.f[k].first = h->first[k];
     bool any_dep = false;
     for (int k = 0; k < c.nfield; k++) any_dep = any_dep || sc.f[k].dep_on;
-    // mixed form with the slice in shared memory: deposition and ADI in one kernel
+    // mixed form with the slice in shared memory: deposition and ADI in one kernel,
+    // one CTA per slice or a cluster pair (chosen by the autotuner; the pair also
+    // serves grids too large for one CTA when its segmented solves apply)
     bool fused = h->mixed && c.solver == G4GPU_SOLVER_ADI && ng <= g4::fused_max_ngrid();
-    if (fused) {
+    bool pair_ok = h->mixed && c.solver == G4GPU_SOLVER_ADI && ng <= g4::pair_max_ngrid();
+    for (int k = 0; k < c.nfield; k++) pair_ok = pair_ok && sc.f[k].tw > 0;
+    bool pair = pair_ok && (h->field_kernel == 1 || !fused);
+    if (fused || pair) {
       g4::StepConstF scf = g4::to_float(sc, np);
       if (do_push) {
         Timed t(h, G4GPU_K_PUSH);
@@ -624,8 +630,11 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
         for (int k = 0; k < c.nfield; k++) {
           const char *cb = (const char *)h->coef + (size_t)sc.f[k].coef * 3 * ng * h->csize;
           Timed t(h, G4GPU_K_ADI_X);
-          g4::launch_field_fused_mixed(L, scf, k, h->beam, h->field[k], cb, ns, np, ng, sc.f[k].dep_on,
-                                       h->field_threads);
+          if (pair)
+            g4::launch_field_pair_mixed(L, scf, k, h->beam, h->field[k], cb, ns, np, ng, sc.f[k].dep_on);
+          else
+            g4::launch_field_fused_mixed(L, scf, k, h->beam, h->field[k], cb, ns, np, ng, sc.f[k].dep_on,
+                                         h->field_threads);
         }
       }
     } else {
@@ -713,7 +722,7 @@ int g4gpu_run(g4gpu_handle h, int istep0, int nsteps, int stages) {
   // Graph mode: the whole step range is one CUDA graph, captured the first time a
   // range starts from a given ring state and replayed afterwards. The kernels take
   // the ring start by value, so a graph is valid for exactly that starting state.
-  g4gpu_ctx::GraphKey key{istep0, nsteps, stages, h->push_block, h->field_threads, {}};
+  g4gpu_ctx::GraphKey key{istep0, nsteps, stages, h->push_block, h->field_threads, h->field_kernel, {}};
   for (int k = 0; k < h->cfg.nfield; k++) {
     long long bits;
     std::memcpy(&bits, &h->accuslip[k], sizeof(bits));
@@ -757,6 +766,19 @@ int g4gpu_run(g4gpu_handle h, int istep0, int nsteps, int stages) {
   return G4GPU_OK;
 }
 
+int g4gpu_set_launch_shapes(g4gpu_handle h, int push_block, int field_threads, int field_kernel) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (push_block < 32 || push_block > 512 || push_block % 32)
+    return fail(h, G4GPU_ERR_ARG, "push_block must be a multiple of 32 in [32, 512]");
+  if (field_threads < 2 * h->cfg.ngrid || field_threads > 1024 || field_threads % 32)
+    return fail(h, G4GPU_ERR_ARG, "field_threads must be a multiple of 32 in [2 ngrid, 1024]");
+  if (field_kernel != 0 && field_kernel != 1) return fail(h, G4GPU_ERR_ARG, "field_kernel must be 0 or 1");
+  h->push_block = push_block;
+  h->field_threads = field_threads;
+  h->field_kernel = field_kernel;
+  return G4GPU_OK;
+}
+
 int g4gpu_set_graph_mode(g4gpu_handle h, int on) {
   if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
   h->graph_mode = on != 0;
@@ -781,10 +803,14 @@ int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out) {
   size_t need = ((size_t)ns * bw + (size_t)c.nfield * ns * fw) * sizeof(double);
   if (need > h->ddiag_bytes) {
     if (h->ddiag) cudaFree(h->ddiag);
+    if (h->hdiag) cudaFreeHost(h->hdiag);
     h->ddiag = nullptr;
+    h->hdiag = nullptr;
     h->ddiag_bytes = 0;
     int rc = alloc(h, (void **)&h->ddiag, need);
     if (rc) return rc;
+    cudaError_t e = cudaMallocHost((void **)&h->hdiag, need);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMallocHost (diagnostics)");
     h->ddiag_bytes = need;
   }
   g4::Launch L{h->stream, h->derr};
@@ -807,17 +833,17 @@ int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out) {
     }
   }
   G4_CUDA(h, cudaGetLastError());
-  std::vector<double> raw(need / sizeof(double));
-  G4_CUDA(h, cudaMemcpyAsync(raw.data(), h->ddiag, need, cudaMemcpyDeviceToHost, h->stream));
+  G4_CUDA(h, cudaMemcpyAsync(h->hdiag, h->ddiag, need, cudaMemcpyDeviceToHost, h->stream));
   int rc = check_device_flag(h);
   if (rc) return rc;
+  const double *raw = h->hdiag;
 
   if (beam_out) {
     // DiagBeam::getValues, Diagnostic.cpp:457-531
     int ow = G4GPU_DB_NCOL + 2 * nharm;
     double norm = np > 0 ? 1. / static_cast<double>(np) : 1.;
     for (int is = 0; is < ns; is++) {
-      const double *s = raw.data() + (size_t)is * bw;
+      const double *s = raw + (size_t)is * bw;
       double g1 = s[0] * norm, g2 = s[1] * norm, x1 = s[2] * norm, x2 = s[3] * norm;
       double y1 = s[4] * norm, y2 = s[5] * norm, px1 = s[6] * norm, px2 = s[7] * norm;
       double py1 = s[8] * norm, py2 = s[9] * norm, xpx = s[10] * norm, ypy = s[11] * norm;
@@ -855,7 +881,7 @@ int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out) {
       double ks = 4. * std::asin(1) / xlambda;
       double scl = dgrid * g4::kEev / ks;
       for (int is0 = 0; is0 < ns; is0++) {
-        const double *s = raw.data() + (size_t)ns * bw + ((size_t)k * ns + is0) * fw;
+        const double *s = raw + (size_t)ns * bw + ((size_t)k * ns + is0) * fw;
         int is = (ns + is0 - h->first[k]) % ns;
         double power = s[0], x1 = s[1], x2 = s[2], y1 = s[3], y2 = s[4];
         if (power > 0) {
@@ -933,7 +959,10 @@ struct TuneKey {
   }
 };
 std::mutex g_tune_mu;
-std::map<TuneKey, std::pair<int, int>> g_tune;
+struct TuneVal {
+  int push_block, field_threads, field_kernel;
+};
+std::map<TuneKey, TuneVal> g_tune;
 
 // device copies of everything a step modifies, to undo the tuning steps
 struct StateBackup {
@@ -976,7 +1005,7 @@ static void restore_state(g4gpu_handle h, StateBackup &b, bool release) {
   std::memcpy(h->accuslip, b.accuslip, sizeof(b.accuslip));
 }
 
-extern "C" int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_threads) {
+extern "C" int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_threads, int *field_kernel) {
   if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
   if (!h->beam_loaded || h->nsteps < 1) return fail(h, G4GPU_ERR_STATE, "load a lattice and a beam first");
   for (int k = 0; k < h->cfg.nfield; k++)
@@ -988,10 +1017,12 @@ extern "C" int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_thread
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
     if (it != g_tune.end()) {
-      h->push_block = it->second.first;
-      h->field_threads = it->second.second;
+      h->push_block = it->second.push_block;
+      h->field_threads = it->second.field_threads;
+      h->field_kernel = it->second.field_kernel;
       if (push_block) *push_block = h->push_block;
       if (field_threads) *field_threads = h->field_threads;
+      if (field_kernel) *field_kernel = h->field_kernel;
       return G4GPU_OK;
     }
   }
@@ -1023,6 +1054,7 @@ extern "C" int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_thread
   auto time_step = [&](int pb, int ft, float *ms) -> int {
     h->push_block = pb;
     h->field_threads = ft;
+    h->field_kernel = 0;
     float best = 1e30f;
     for (int rep = 0; rep < 3; rep++) {  // first repetition warms up
       restore_state(h, b, false);
@@ -1059,6 +1091,30 @@ extern "C" int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_thread
       }
     }
   }
+  // the cluster-pair field kernel, where the step's segmented solves apply
+  int best_fk = 0;
+  bool pairable = fused && c.ngrid <= g4::pair_max_ngrid();
+  for (int k = 0; k < c.nfield; k++) pairable = pairable && h->steps[istep].f[k].tw > 0;
+  if (!rc && pairable) {
+    float ms;
+    if (!(rc = time_step(best_pb, best_ft, &ms))) {
+      float single = ms;
+      h->field_kernel = 1;
+      float pms = 1e30f;
+      for (int rep = 0; rep < 3 && !rc; rep++) {
+        restore_state(h, b, false);
+        cudaEventRecord(e0, h->stream);
+        rc = enqueue_steps(h, istep, 1, G4GPU_STAGE_ALL);
+        cudaEventRecord(e1, h->stream);
+        cudaEventSynchronize(e1);
+        float t = 0;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (rep > 0 && t < pms) pms = t;
+      }
+      h->field_kernel = 0;
+      if (!rc && pms < single) best_fk = 1;
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   restore_state(h, b, true);
@@ -1068,12 +1124,14 @@ extern "C" int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_thread
   if (rc) return rc;
   h->push_block = best_pb;
   h->field_threads = best_ft;
+  h->field_kernel = best_fk;
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[key] = {best_pb, best_ft};
+    g_tune[key] = {best_pb, best_ft, best_fk};
   }
   if (push_block) *push_block = best_pb;
   if (field_threads) *field_threads = best_ft;
+  if (field_kernel) *field_kernel = best_fk;
   return check_device_flag(h);
 }
 

@@ -36,6 +36,7 @@ struct g4gpu_ctx {
   int *derr = nullptr;
   double *ddiag = nullptr;
   size_t ddiag_bytes = 0;
+  double *hdiag = nullptr;  // pinned host copy of ddiag (the per-step read-back)
   void *stage = nullptr;     // AoS staging buffer for host transfers
   size_t stage_bytes = 0;
   size_t bytes = 0;
@@ -51,15 +52,16 @@ struct g4gpu_ctx {
   // launch shapes (chosen by g4gpu_autotune, defaults otherwise)
   int push_block = 256;
   int field_threads = 512;
+  int field_kernel = 0;  // mixed ADI: 0 one CTA per slice (k_field_fused_f), 1 a cluster pair (k_field_pair_f)
 
   // captured step sequences, keyed by the step range and the ring state they start from
   bool graph_mode = false;
   struct GraphKey {
-    int istep0, nsteps, stages, push_block, field_threads;
+    int istep0, nsteps, stages, push_block, field_threads, field_kernel;
     std::vector<long long> state;  // first[] and the bit patterns of accuslip[]
     bool operator<(const GraphKey &o) const {
-      return std::tie(istep0, nsteps, stages, push_block, field_threads, state) <
-             std::tie(o.istep0, o.nsteps, o.stages, o.push_block, o.field_threads, o.state);
+      return std::tie(istep0, nsteps, stages, push_block, field_threads, field_kernel, state) <
+             std::tie(o.istep0, o.nsteps, o.stages, o.push_block, o.field_threads, o.field_kernel, o.state);
     }
   };
   struct GraphEntry {

@@ -114,6 +114,12 @@ void launch_diag_field_mixed(const Launch &L, const void *field, int ns, int ngr
 // Fused deposition + ADI of one field in shared memory, one CTA per slice; usable
 // for ngrid <= fused_max_ngrid() (168: the FP32 slice must fit in 227 KB).
 int fused_max_ngrid();
+// The same step on a thread-block cluster of two CTAs per slice, each holding half the
+// rows; usable for ngrid <= pair_max_ngrid() when the step's segmented solves apply
+// (FieldStep::tw > 0).
+int pair_max_ngrid();
+void launch_field_pair_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b, void *field,
+                             const void *coef, int ns, int np, int ngrid, int deposit);
 // threads: CTA size, a multiple of 32 in [2 ngrid, 1024]
 void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b,
                               void *field, const void *coef, int ns, int np, int ngrid, int deposit,

@@ -21,6 +21,7 @@
 //    has no cancellation in FP32 (eps ~ 1e-8);
 //  * RK4 is written in its classic form, algebraically identical to the reference's
 //    "pushp" sequence (BeamSolver.cpp:89-141).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -971,76 +972,162 @@ __device__ __forceinline__ double bext(double v, double *sh) {
 }
 
 // DiagBeam sums with FP64 accumulation (Diagnostic.cpp:415-456); one block per slice
-template <int BS>
-__global__ void __launch_bounds__(BS) k_diag_beam_f(PtrsF p, double gref, int np, int nharm, double *out) {
-  __shared__ double sh[BS / 32];
-  int is = blockIdx.x;
-  size_t base = (size_t)is * np;
-  double s[kBeamSums] = {0};
-  double mn[5] = {1e5, 1e5, 1e5, 1e5, 1e7}, mx[5] = {-1e5, -1e5, -1e5, -1e5, 1};
-  double br[G4GPU_MAX_HARM], bi[G4GPU_MAX_HARM];
-  for (int h = 0; h < G4GPU_MAX_HARM; h++) br[h] = bi[h] = 0;
-  for (int ip = threadIdx.x; ip < np; ip += BS) {
-    double x = p.x[base + ip], y = p.y[base + ip], g = gref + (double)p.dg[base + ip];
-    double px = p.px[base + ip], py = p.py[base + ip];
-    long long th = p.theta[base + ip];
-    s[0] += g; s[1] += g * g; s[2] += x; s[3] += x * x; s[4] += y; s[5] += y * y;
-    s[6] += px; s[7] += px * px; s[8] += py; s[9] += py * py; s[10] += x * px; s[11] += y * py;
-    mn[0] = fmin(mn[0], x); mx[0] = fmax(mx[0], x);
-    mn[1] = fmin(mn[1], px); mx[1] = fmax(mx[1], px);
-    mn[2] = fmin(mn[2], y); mx[2] = fmax(mx[2], y);
-    mn[3] = fmin(mn[3], py); mx[3] = fmax(mx[3], py);
-    mn[4] = fmin(mn[4], g); mx[4] = fmax(mx[4], g);
-    for (int h = 0; h < nharm && h < G4GPU_MAX_HARM; h++) {
-      float sn, cs;
-      sincosf(phase_of(th, (unsigned)(h + 1)), &sn, &cs);  // exact harmonic of the phase
-      br[h] += cs;
-      bi[h] += sn;
+// Compensated (Kahan) FP32 sum: a thread's partial sum of a slice quantity keeps
+// ~FP32 relative accuracy however many terms it takes, so it can be folded into the
+// FP64 slice total once (GB300's FP64 rate is 1/64 of FP32; per-term FP64 adds would
+// bound the diagnostics).
+struct KahanF {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+// All NS sums and NX min/max pairs of a block in one pass: every warp reduces its
+// lanes' values with shuffles, lane 0 stores them, and after one barrier thread k
+// combines value k over the warps (sums in FP64). Thread 0..NS-1 return their sum in
+// *sum, threads NS..NS+2NX-1 their minimum or maximum in *ext.
+template <int BS, int NS, int NX>
+__device__ __forceinline__ void block_reduce_all(const double *s, const float *mn, const float *mx, double *sh,
+                                                 double *out) {
+  constexpr int NW = BS / 32, NV = NS + 2 * NX;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NS; k++) {
+    double v = s[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[warp * NV + k] = v;
+  }
+#pragma unroll
+  for (int k = 0; k < NX; k++) {
+    float a = mn[k], b = mx[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a = fminf(a, __shfl_down_sync(0xffffffffu, a, o));
+      b = fmaxf(b, __shfl_down_sync(0xffffffffu, b, o));
+    }
+    if (lane == 0) {
+      sh[warp * NV + NS + 2 * k] = a;
+      sh[warp * NV + NS + 2 * k + 1] = b;
     }
   }
-  int w = beam_diag_width(nharm);
-  double *o = out + (size_t)is * w;
-  for (int k = 0; k < kBeamSums; k++) {
-    double r = bsum<BS>(s[k], sh);
-    if (threadIdx.x == 0) o[k] = r;
-  }
-  for (int k = 0; k < 5; k++) {
-    double a = bext<BS, false>(mn[k], sh);
-    if (threadIdx.x == 0) o[kBeamSums + 2 * k] = a;
-    double b = bext<BS, true>(mx[k], sh);
-    if (threadIdx.x == 0) o[kBeamSums + 2 * k + 1] = b;
-  }
-  for (int h = 0; h < nharm && h < G4GPU_MAX_HARM; h++) {
-    double a = bsum<BS>(br[h], sh);
-    double b = bsum<BS>(bi[h], sh);
-    if (threadIdx.x == 0) {
-      o[kBeamSums + kBeamMinMax + 2 * h] = a;
-      o[kBeamSums + kBeamMinMax + 2 * h + 1] = b;
+  __syncthreads();
+  const int k = threadIdx.x;
+  if (k < NV) {
+    double r = sh[k];
+    for (int w = 1; w < NW; w++) {
+      const double v = sh[w * NV + k];
+      if (k < NS)
+        r += v;
+      else
+        r = ((k - NS) & 1) ? fmax(r, v) : fmin(r, v);
     }
+    out[k] = r;
   }
 }
 
+// Per-slice beam sums of the mixed form (layout of k_diag_beam in the FP64 form):
+// the coordinates are FP32 and gamma is the FP32 offset from gammaref, so every
+// particle's terms are formed in FP32; each thread sums its particles' terms with
+// compensated FP32 sums, folded into FP64 once, and the slice totals are FP64 sums
+// over the threads (the per-slice reductions, bunching and energy included, stay
+// FP64; GB300 runs FP64 at 1/64 of the FP32 rate, so per-particle FP64 arithmetic
+// would bound the kernel). The energy moments are
+// taken about gammaref: sum g = N gref + sum dg and sum g^2 = N gref^2 + 2 gref sum dg
+// + sum dg^2, without the cancellation of squaring g itself. NH: compile-time bound on
+// the number of harmonics (the arrays stay in registers).
+template <int BS, int NH>
+__global__ void __launch_bounds__(BS) k_diag_beam_f(PtrsF p, double gref, int np, int nharm, double *out) {
+  constexpr int NSUM = kBeamSums + 2 * NH;
+  __shared__ double sh[(BS / 32) * (NSUM + 10)];
+  __shared__ double res[NSUM + 10];
+  const int is = blockIdx.x;
+  const size_t base = (size_t)is * np;
+  const int nh = min(nharm, NH);
+  // dg, dg^2, x, x^2, y, y^2, px, px^2, py, py^2, x px, y py, then (Re, Im) b_h
+  KahanF c[NSUM];
+  float mn[5], mx[5];  // x, px, y, py, dg
+#pragma unroll
+  for (int k = 0; k < 5; k++) {
+    mn[k] = INFINITY;
+    mx[k] = -INFINITY;
+  }
+#pragma unroll 4
+  for (int ip = threadIdx.x; ip < np; ip += BS) {
+    const float x = p.x[base + ip], y = p.y[base + ip], dg = p.dg[base + ip];
+    const float px = p.px[base + ip], py = p.py[base + ip];
+    const long long th = p.theta[base + ip];
+    c[0].add(dg); c[1].add(dg * dg); c[2].add(x); c[3].add(x * x); c[4].add(y); c[5].add(y * y);
+    c[6].add(px); c[7].add(px * px); c[8].add(py); c[9].add(py * py); c[10].add(x * px); c[11].add(y * py);
+    mn[0] = fminf(mn[0], x); mx[0] = fmaxf(mx[0], x);
+    mn[1] = fminf(mn[1], px); mx[1] = fmaxf(mx[1], px);
+    mn[2] = fminf(mn[2], y); mx[2] = fmaxf(mx[2], y);
+    mn[3] = fminf(mn[3], py); mx[3] = fmaxf(mx[3], py);
+    mn[4] = fminf(mn[4], dg); mx[4] = fmaxf(mx[4], dg);
+#pragma unroll
+    for (int h = 0; h < NH; h++) {
+      if (h < nh) {
+        float sn, cs;
+        sincosf(phase_of(th, (unsigned)(h + 1)), &sn, &cs);  // exact harmonic of the phase
+        c[kBeamSums + 2 * h].add(cs);
+        c[kBeamSums + 2 * h + 1].add(sn);
+      }
+    }
+  }
+  double s[NSUM];
+#pragma unroll
+  for (int k = 0; k < NSUM; k++) s[k] = c[k].value();
+  block_reduce_all<BS, NSUM, 5>(s, mn, mx, sh, res);
+  __syncthreads();
+  const int w = beam_diag_width(nharm);
+  double *o = out + (size_t)is * w;
+  const int k = threadIdx.x;
+  const double n = (double)np;
+  if (k == 0) o[0] = n * gref + res[0];
+  if (k == 1) o[1] = n * gref * gref + 2.0 * gref * res[0] + res[1];
+  if (k >= 2 && k < kBeamSums) o[k] = res[k];
+  if (k >= kBeamSums && k < kBeamSums + 2 * nh) o[kBeamMinMax + k] = res[k];  // bunching after min/max
+  if (k < 10) o[kBeamSums + k] = (k >= 8 ? gref : 0.0) + res[NSUM + k];
+}
+
+// Per-slice field sums of the mixed form (layout of k_diag_field): a flat walk over
+// the cells (row and column carried along, no division per cell), each thread's
+// terms summed with compensated FP32 sums and folded into the FP64 slice totals once.
 template <int BS>
 __global__ void __launch_bounds__(BS) k_diag_field_f(const float2 *field, int ng, double *out) {
-  __shared__ double sh[BS / 32];
-  int is0 = blockIdx.x;
-  size_t ncell = (size_t)ng * ng;
+  __shared__ double sh[(BS / 32) * kFieldSums];
+  __shared__ double res[kFieldSums];
+  const int is0 = blockIdx.x;
+  const int ncell = ng * ng;
   const float2 *f = field + (size_t)is0 * ncell;
-  double shift = -0.5 * (double)(ng - 1);
-  double s[7] = {0};
-  for (size_t i = threadIdx.x; i < ncell; i += BS) {
-    int iy = (int)(i / ng), ix = (int)(i % ng);
-    double dx = (double)ix + shift, dy = (double)iy + shift;
-    float2 v = f[i];
-    double wei = (double)v.x * v.x + (double)v.y * v.y;
-    s[0] += wei; s[1] += dx * wei; s[2] += dx * dx * wei; s[3] += dy * wei; s[4] += dy * dy * wei;
-    s[5] += v.x; s[6] += v.y;
+  const float shift = -0.5f * (float)(ng - 1);
+  KahanF c[kFieldSums];
+  int row = threadIdx.x / ng, col = threadIdx.x % ng;
+#pragma unroll 4
+  for (int i = threadIdx.x; i < ncell; i += BS) {
+    const float dx = (float)col + shift, dy = (float)row + shift;
+    const float2 v = f[i];
+    const float wei = v.x * v.x + v.y * v.y;
+    c[0].add(wei); c[1].add(dx * wei); c[2].add(dx * dx * wei); c[3].add(dy * wei); c[4].add(dy * dy * wei);
+    c[5].add(v.x); c[6].add(v.y);
+    col += BS;  // the next cell of this thread, BS further on
+    while (col >= ng) {
+      col -= ng;
+      row++;
+    }
   }
+  double S[kFieldSums];
+#pragma unroll
+  for (int k = 0; k < kFieldSums; k++) S[k] = c[k].value();
+  block_reduce_all<BS, kFieldSums, 0>(S, nullptr, nullptr, sh, res);
+  __syncthreads();
   double *o = out + (size_t)is0 * (kFieldSums + 2);
-  for (int k = 0; k < 7; k++) {
-    double r = bsum<BS>(s[k], sh);
-    if (threadIdx.x == 0) o[k] = r;
-  }
+  if (threadIdx.x < kFieldSums) o[threadIdx.x] = res[threadIdx.x];
   if (threadIdx.x == 0) {
     float2 v = f[(size_t)(ng / 2) * ng + ng / 2];
     o[7] = v.x;
@@ -1062,6 +1149,348 @@ PtrsF make_ptrs_f(const DeviceBeam &b, void *const *field, void *const *src, int
     p.src[k] = src ? (float2 *)src[k] : nullptr;
   }
   return p;
+}
+
+// ---- fused field step on a pair of CTAs (a thread-block cluster of two) -------
+//
+// The slice's rows are split between the two CTAs of a cluster: rows [0, h) and
+// [h, ng), h = ceil(ng / 2). Each CTA holds its ~half slice (92 KB at ngrid 151), so
+// two CTAs fit an SM and one CTA's bulk copies, barriers and latency overlap the
+// other's arithmetic, which a single 182 KB CTA per SM cannot do. The phases are those
+// of k_field_fused_f, with what crosses the split done as follows:
+//  * the column stencils take the rows just outside a CTA's band from the slice in
+//    global memory, which stays unmodified until the final stores;
+//  * the deposition splits the particles between the two CTAs, and a contribution to
+//    the other CTA's rows is a shared-memory atomic through the cluster's distributed
+//    shared memory;
+//  * the column solves' segments next to the split take their warm-up values from
+//    the other CTA's shared memory, read between cluster barriers that order them
+//    against that CTA's in-place writes.
+// Every thread of both CTAs passes every cluster barrier (no early exit), and the
+// last distributed-shared-memory access precedes the last cluster barrier.
+namespace cg = cooperative_groups;
+
+constexpr int kPairThreads = 512;
+
+__device__ __forceinline__ void pair_rows(int ng, int q, int &r0, int &nrow) {
+  const int h = (ng + 1) / 2;
+  r0 = q ? h : 0;
+  nrow = q ? ng - h : h;
+}
+
+// thomas_seg for nline lines of n elements (the rows of a band)
+__device__ __forceinline__ void thomas_lines(float2 *S, int nline, int lstride, int estride, int n, int nseg, int W,
+                                             const float2 *Cc, const float2 *CB, const float2 *CW) {
+  const int tid = threadIdx.x;
+  const int line = tid % nline, seg = tid / nline;
+  const int len = (n + nseg - 1) / nseg;
+  const int b = seg * len, e = min(b + len, n);
+  const bool act = seg < nseg && b < e;
+  float2 *L = S + (size_t)line * lstride;
+  float2 d = make_float2(0.f, 0.f);
+  if (act)
+    for (int k = max(0, b - W); k < b; k++) {
+      float2 r = L[k * estride], cd = cmulf(Cc[k], d);
+      d = cmulf(make_float2(r.x - cd.x, r.y - cd.y), CB[k]);
+    }
+  __syncthreads();
+  if (act)
+    for (int k = b; k < e; k++) {
+      float2 r = L[k * estride], cd = cmulf(Cc[k], d);
+      d = cmulf(make_float2(r.x - cd.x, r.y - cd.y), CB[k]);
+      L[k * estride] = d;
+    }
+  __syncthreads();
+  const int k1 = min(n - 1, e - 1 + W);
+  float2 x = make_float2(0.f, 0.f);
+  if (act && k1 >= e) {
+    x = L[k1 * estride];
+    for (int k = k1 - 1; k >= e; k--) {
+      float2 v = L[k * estride], cw = cmulf(CW[k + 1], x);
+      x = make_float2(v.x - cw.x, v.y - cw.y);
+    }
+  }
+  __syncthreads();
+  if (act)
+    for (int k = e - 1; k >= b; k--) {
+      float2 v = L[k * estride];
+      if (k < n - 1) {
+        float2 cw = cmulf(CW[k + 1], x);
+        v = make_float2(v.x - cw.x, v.y - cw.y);
+      }
+      x = v;
+      L[k * estride] = x;
+    }
+  __syncthreads();
+}
+
+// S1 = (I + c Dy) u on the band's rows [r0, r0 + nrow) in place (band row k at
+// S[k * ng + col]), column segments as stencil_cols_seg; the rows just outside the
+// band are read from u in global memory.
+__device__ __forceinline__ void stencil_cols_band(float2 *S, const float2 *__restrict__ u, int ng, int r0, int nrow,
+                                                  float cs, int nseg) {
+  const int tid = threadIdx.x;
+  const int col = tid % ng, seg = tid / ng;
+  const int len = (nrow + nseg - 1) / nseg;
+  const int b = seg * len, e = min(b + len, nrow);
+  const bool act = seg < nseg && b < e;
+  float2 above = make_float2(0.f, 0.f), below = make_float2(0.f, 0.f);
+  if (act) {
+    const int ga = r0 + b - 1, gb = r0 + e;
+    if (ga >= 0) above = b > 0 ? S[(b - 1) * ng + col] : u[(size_t)ga * ng + col];
+    if (gb < ng) below = e < nrow ? S[e * ng + col] : u[(size_t)gb * ng + col];
+  }
+  __syncthreads();
+  if (act) {
+    float2 prev = above, cur = S[b * ng + col];
+    float2 next = (b + 1 < e) ? S[(b + 1) * ng + col] : below;
+    for (int k = b; k < e; k++) {
+      float2 nx = next;
+      if (k + 2 < e)
+        next = S[(k + 2) * ng + col];
+      else if (k + 2 == e)
+        next = below;
+      const int g = r0 + k;
+      float2 out = stencil(cs, cur, lapf(g > 0, g < ng - 1, prev, cur, nx));
+      prev = cur;
+      cur = nx;
+      S[k * ng + col] = out;
+    }
+  }
+}
+
+// S = 2 u' - S1 on the band's rows, S1 recomputed from u in global memory (r2_cols_seg)
+__device__ __forceinline__ void r2_cols_band(float2 *S, const float2 *__restrict__ u, int ng, int r0, int nrow,
+                                             float cs, int nseg) {
+  const int tid = threadIdx.x;
+  const int col = tid % ng, seg = tid / ng;
+  const int len = (nrow + nseg - 1) / nseg;
+  const int b = seg * len, e = min(b + len, nrow);
+  if (seg >= nseg || b >= e) return;
+  const int g0 = r0 + b;
+  float2 prev = g0 > 0 ? u[(size_t)(g0 - 1) * ng + col] : make_float2(0.f, 0.f);
+  float2 cur = u[(size_t)g0 * ng + col];
+  float2 next = g0 + 1 < ng ? u[(size_t)(g0 + 1) * ng + col] : make_float2(0.f, 0.f);
+  for (int k = b; k < e; k++) {
+    const int g = r0 + k;
+    float2 nx = next;
+    if (g + 2 < ng) next = u[(size_t)(g + 2) * ng + col];
+    float2 s1 = stencil(cs, cur, lapf(g > 0, g < ng - 1, prev, cur, nx));
+    prev = cur;
+    cur = nx;
+    float2 v = S[k * ng + col];
+    S[k * ng + col] = make_float2(2.f * v.x - s1.x, 2.f * v.y - s1.y);
+  }
+}
+
+// Column solve of the pair (thomas_seg along the columns, rows split between the
+// CTAs): band row k of this CTA is global row r0 + k; the warm-ups of the segments
+// next to the split read the peer's band P (distributed shared memory).
+__device__ __forceinline__ void thomas_cols_pair(cg::cluster_group &cl, float2 *S, const float2 *P, int ng, int r0,
+                                                 int nrow, int nrow_peer, int q, int nseg, int W, const float2 *Cc,
+                                                 const float2 *CB, const float2 *CW) {
+  const int tid = threadIdx.x;
+  const int col = tid % ng, seg = tid / ng;
+  const int len = (nrow + nseg - 1) / nseg;
+  const int b = seg * len, e = min(b + len, nrow);
+  const bool act = seg < nseg && b < e;
+  // band row k, k < 0 or k >= nrow meaning the peer's rows (above for q = 1, below for q = 0)
+  auto at = [&](int k) -> float2 {
+    if (k >= 0 && k < nrow) return S[k * ng + col];
+    return q ? P[(nrow_peer + k) * ng + col] : P[(k - nrow) * ng + col];
+  };
+  float2 d = make_float2(0.f, 0.f);
+  if (act)
+    for (int k = max(-r0, b - W); k < b; k++) {
+      const int g = r0 + k;
+      float2 r = at(k), cd = cmulf(Cc[g], d);
+      d = cmulf(make_float2(r.x - cd.x, r.y - cd.y), CB[g]);
+    }
+  cl.sync();
+  if (act)
+    for (int k = b; k < e; k++) {
+      const int g = r0 + k;
+      float2 r = S[k * ng + col], cd = cmulf(Cc[g], d);
+      d = cmulf(make_float2(r.x - cd.x, r.y - cd.y), CB[g]);
+      S[k * ng + col] = d;
+    }
+  cl.sync();
+  const int k1 = min(ng - 1 - r0, e - 1 + W);
+  float2 x = make_float2(0.f, 0.f);
+  if (act && k1 >= e) {
+    x = at(k1);
+    for (int k = k1 - 1; k >= e; k--) {
+      float2 v = at(k), cw = cmulf(CW[r0 + k + 1], x);
+      x = make_float2(v.x - cw.x, v.y - cw.y);
+    }
+  }
+  cl.sync();
+  if (act)
+    for (int k = e - 1; k >= b; k--) {
+      const int g = r0 + k;
+      float2 v = S[k * ng + col];
+      if (g < ng - 1) {
+        float2 cw = cmulf(CW[g + 1], x);
+        v = make_float2(v.x - cw.x, v.y - cw.y);
+      }
+      x = v;
+      S[k * ng + col] = x;
+    }
+  __syncthreads();
+}
+
+// Cell and weights of a particle (ll_gridpoint_f) with the row and column kept.
+struct CellRC {
+  int ix, iy, ix1, iy1;
+  float wx, wy;
+};
+__device__ __forceinline__ bool cell_rc(float gm, float dg, int ng, float x, float y, CellRC &c) {
+  if ((x > -gm) && (x < gm) && (y > -gm) && (y < gm)) {
+    float wx = (x + gm) / dg, wy = (y + gm) / dg;
+    float fx = floorf(wx), fy = floorf(wy);
+    c.ix = min((int)fx, ng - 1);
+    c.iy = min((int)fy, ng - 1);
+    c.wx = 1.f + fx - wx;
+    c.wy = 1.f + fy - wy;
+    c.ix1 = c.ix + 1 < ng ? c.ix + 1 : c.ix;
+    c.iy1 = c.iy + 1 < ng ? c.iy + 1 : c.iy;
+    return true;
+  }
+  return false;
+}
+
+// The deposition of the pair: this CTA (rank q) takes half of the slice's groups of
+// four particles (deposit_quads' grouping); each weighted contribution goes to the
+// CTA that holds its row: T[0], T[1] are the two bands (one local, one the peer's
+// through distributed shared memory), starting at global rows 0 and h.
+__device__ __forceinline__ void pair_add(float2 *const *T, int h, int ng, int ix, int iy, float w, float cpx,
+                                         float cpy) {
+  const int o = iy >= h;
+  float2 *t = T[o] + (size_t)(iy - (o ? h : 0)) * ng + ix;
+  atomicAdd(&t->x, w * cpx);
+  atomicAdd(&t->y, w * cpy);
+}
+__device__ __forceinline__ void pair_group(const StepConstF &sc, const FieldStepF &fs, float scl, float2 *const *T,
+                                           int h, int ng, float x, float y, const long long *th, const float *dgam,
+                                           int n) {
+  CellRC c;
+  if (!cell_rc(fs.gridmax, fs.dgrid, ng, x, y, c)) return;
+  float dx = x - sc.ax, dy = y - sc.ay;
+  float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
+  float a = sqrtf(faw2) * scl;
+  float cpx = 0.f, cpy = 0.f;
+  for (int m = 0; m < n; m++) {
+    float part = a / ((float)sc.gammaref + dgam[m]);
+    float sn, co;
+    __sincosf(phase_of(th[m], (unsigned)fs.harm), &sn, &co);
+    cpx += sn * part;
+    cpy += co * part;
+  }
+  pair_add(T, h, ng, c.ix, c.iy, c.wx * c.wy, cpx, cpy);
+  pair_add(T, h, ng, c.ix1, c.iy, (1.f - c.wx) * c.wy, cpx, cpy);
+  pair_add(T, h, ng, c.ix, c.iy1, c.wx * (1.f - c.wy), cpx, cpy);
+  pair_add(T, h, ng, c.ix1, c.iy1, (1.f - c.wx) * (1.f - c.wy), cpx, cpy);
+}
+__device__ __forceinline__ void deposit_pair(const StepConstF &sc, const FieldStepF &fs, const PtrsF &p,
+                                             float2 *const *T, int h, int is, int np, int ng, int q) {
+  const float scl = fs.dep_scl * (float)p.current[is];
+  const size_t base = (size_t)is * np;
+  if ((np & 3) == 0) {
+    const int nq = np >> 2, q0 = q ? nq / 2 : 0, q1 = q ? nq : nq / 2;
+    const float4 *X = reinterpret_cast<const float4 *>(p.x + base);
+    const float4 *Y = reinterpret_cast<const float4 *>(p.y + base);
+    const float4 *G = reinterpret_cast<const float4 *>(p.dg + base);
+    const longlong2 *TH = reinterpret_cast<const longlong2 *>(p.theta + base);
+    for (int g = q0 + threadIdx.x; g < q1; g += blockDim.x) {
+      const float4 x = X[g], y = Y[g], gg = G[g];
+      const longlong2 t01 = TH[2 * g], t23 = TH[2 * g + 1];
+      const long long th[4] = {t01.x, t01.y, t23.x, t23.y};
+      const float dg[4] = {gg.x, gg.y, gg.z, gg.w};
+      const bool p01 = x.x == x.y && y.x == y.y, p23 = x.z == x.w && y.z == y.w;
+      if (p01 && p23 && x.x == x.z && y.x == y.z) {
+        pair_group(sc, fs, scl, T, h, ng, x.x, y.x, th, dg, 4);
+      } else {
+        if (p01) {
+          pair_group(sc, fs, scl, T, h, ng, x.x, y.x, th, dg, 2);
+        } else {
+          pair_group(sc, fs, scl, T, h, ng, x.x, y.x, th, dg, 1);
+          pair_group(sc, fs, scl, T, h, ng, x.y, y.y, th + 1, dg + 1, 1);
+        }
+        if (p23) {
+          pair_group(sc, fs, scl, T, h, ng, x.z, y.z, th + 2, dg + 2, 2);
+        } else {
+          pair_group(sc, fs, scl, T, h, ng, x.z, y.z, th + 2, dg + 2, 1);
+          pair_group(sc, fs, scl, T, h, ng, x.w, y.w, th + 3, dg + 3, 1);
+        }
+      }
+    }
+  } else {
+    const int i0 = q ? np / 2 : 0, i1 = q ? np : np / 2;
+    for (int ip = i0 + threadIdx.x; ip < i1; ip += blockDim.x) {
+      const long long th = p.theta[base + ip];
+      const float dg = p.dg[base + ip];
+      pair_group(sc, fs, scl, T, h, ng, p.x[base + ip], p.y[base + ip], &th, &dg, 1);
+    }
+  }
+}
+
+// shared memory of one CTA of the pair: mbarrier, coefficients, slack, its band
+size_t pair_smem_bytes(int ng) {
+  return ((16 + 3 * (size_t)ng * 8 + 15) & ~(size_t)15) + 8 + (size_t)((ng + 1) / 2) * ng * 8;
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 2)
+    k_field_pair_f(StepConstF sc, int k, PtrsF p, float2 *__restrict__ field, const float2 *__restrict__ coef,
+                   int ns, int np, int ng, int deposit, int *err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cg::cluster_group cl = cg::this_cluster();
+  const int q = (int)cl.block_rank();
+  const int ncell = ng * ng;
+  const FieldStepF &fs = sc.f[k];
+  const int is = blockIdx.x >> 1;
+  const int i = (is + fs.first) % ns;
+  float2 *u = field + (size_t)i * ncell;
+  int r0, nrow, r0p, nrowp;
+  pair_rows(ng, q, r0, nrow);
+  pair_rows(ng, 1 - q, r0p, nrowp);
+  float2 *ub = u + (size_t)r0 * ng;  // this CTA's band in global memory
+  // layout as k_field_fused_f: [mbarrier][8 B][coefficients 3 ng][pad][band], the band
+  // congruent to its global rows mod 16; the peer's band at its own offset
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);
+  float2 *C = reinterpret_cast<float2 *>(smem_raw + 16);
+  float2 *CB = C + ng, *CW = CB + ng;
+  const size_t soff = (16 + 3 * (size_t)ng * 8 + 15) & ~(size_t)15;
+  float2 *S = reinterpret_cast<float2 *>(smem_raw + soff + (reinterpret_cast<uintptr_t>(ub) & 15));
+  float2 *Sp_local = reinterpret_cast<float2 *>(
+      smem_raw + soff + (reinterpret_cast<uintptr_t>(u + (size_t)r0p * ng) & 15));
+  float2 *P = cl.map_shared_rank(Sp_local, 1 - q);
+  uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int t = threadIdx.x; t < 3 * ng; t += blockDim.x) C[t] = coef[t];
+  __syncthreads();
+  // a wait that runs out raises the flag and the step goes on: leaving early would
+  // strand the peer at a cluster barrier
+  bulk_load(S, ub, nrow * ng, bar_s, err);
+  const float cs = fs.cstep;
+  const int nseg = max(1, min((int)blockDim.x / ng, 8));
+  stencil_cols_band(S, u, ng, r0, nrow, cs, nseg);  // S1 on this band
+  cl.sync();                                        // both bands hold S1 before any deposit
+  if (deposit) {
+    float2 *T[2];
+    T[q] = S;
+    T[1 - q] = P;
+    deposit_pair(sc, fs, p, T, (ng + 1) / 2, is, np, ng, q);
+  }
+  cl.sync();  // every contribution, local or remote, has landed
+  thomas_lines(S, nrow, ng, 1, ng, max(1, min((int)blockDim.x / nrow, 32)), fs.tw, C, CB, CW);  // rows
+  r2_cols_band(S, u, ng, r0, nrow, cs, nseg);
+  __syncthreads();
+  thomas_cols_pair(cl, S, P, ng, r0, nrow, nrowp, q, nseg, fs.tw, C, CB, CW);  // columns
+  bulk_store(ub, S, nrow * ng);
+  if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
 // ---- ADI step without device allocation (g4gpu_adi_advance_noalloc) -------------
@@ -1283,7 +1712,15 @@ void launch_adi_mixed(const Launch &L, const StepConstF &sc, int k, int phase, v
 void launch_diag_beam_mixed(const Launch &L, const DeviceBeam &b, double gammaref, int ns, int np,
                             int nharm, double *out) {
   PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
-  k_diag_beam_f<256><<<ns, 256, 0, (cudaStream_t)L.stream>>>(p, gammaref, np, nharm, out);
+  cudaStream_t s = (cudaStream_t)L.stream;
+  if (nharm <= 1)
+    k_diag_beam_f<256, 1><<<ns, 256, 0, s>>>(p, gammaref, np, nharm, out);
+  else if (nharm <= 3)
+    k_diag_beam_f<256, 3><<<ns, 256, 0, s>>>(p, gammaref, np, nharm, out);
+  else if (nharm <= 5)
+    k_diag_beam_f<256, 5><<<ns, 256, 0, s>>>(p, gammaref, np, nharm, out);
+  else
+    k_diag_beam_f<256, G4GPU_MAX_HARM><<<ns, 256, 0, s>>>(p, gammaref, np, nharm, out);
 }
 
 void launch_diag_field_mixed(const Launch &L, const void *field, int ns, int ngrid, double *out) {
@@ -1316,6 +1753,26 @@ void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, cons
   if (threads < 2 * ngrid) threads = (2 * ngrid + 31) / 32 * 32;
   if (threads > kFusedMaxThreads) threads = kFusedMaxThreads;
   k_field_fused_f<<<ns, threads, smem, (cudaStream_t)L.stream>>>(
+      sc, k, p, (float2 *)field, (const float2 *)coef, ns, np, ngrid, deposit, L.err);
+}
+
+int pair_max_ngrid() {
+  int ng = 3;
+  while (pair_smem_bytes(ng + 1) <= 227u * 1024u) ng++;
+  return ng;
+}
+
+void launch_field_pair_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b, void *field,
+                             const void *coef, int ns, int np, int ngrid, int deposit) {
+  static unsigned long long configured = 0;  // one bit per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !(configured & (1ull << dev))) {
+    cudaFuncSetAttribute(k_field_pair_f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    configured |= 1ull << dev;
+  }
+  PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
+  k_field_pair_f<<<2 * ns, kPairThreads, pair_smem_bytes(ngrid), (cudaStream_t)L.stream>>>(
       sc, k, p, (float2 *)field, (const float2 *)coef, ns, np, ngrid, deposit, L.err);
 }
 

@@ -53,7 +53,7 @@ ABI_SYMBOLS = [
     "g4gpu_mlp_get_params", "g4gpu_mlp_set_params", "g4gpu_mlp_set_normalization", "g4gpu_mlp_forward",
     "g4gpu_mlp_gradients", "g4gpu_mlp_train", "g4gpu_closure_attach", "g4gpu_closure_features",
     "g4gpu_closure_apply", "g4gpu_closure_targets", "g4gpu_copy_state", "g4gpu_run_learned",
-    "g4gpu_adi_advance_noalloc",
+    "g4gpu_adi_advance_noalloc", "g4gpu_set_launch_shapes",
 ]
 CLOSURE_NIN, CLOSURE_NOUT = 32, 4
 NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
@@ -139,7 +139,8 @@ def load_library(path=None):
     L.g4gpu_host_fc.argtypes = [d, i, i]
     L.g4gpu_host_fc.restype = d
     L.g4gpu_set_graph_mode.argtypes = [vp, i]
-    L.g4gpu_autotune.argtypes = [vp, P(i), P(i)]
+    L.g4gpu_autotune.argtypes = [vp, P(i), P(i), P(i)]
+    L.g4gpu_set_launch_shapes.argtypes = [vp, i, i, i]
     L.g4gpu_batch_create.argtypes = [i, P(Config), P(vp)]
     L.g4gpu_batch_destroy.argtypes = [vp]
     L.g4gpu_batch_destroy.restype = None
@@ -370,10 +371,15 @@ class Handle:
                                              ctypes.byref(nchk), ctypes.byref(nfb), ctypes.byref(emax)))
         return nchk.value, nfb.value, emax.value
 
+    def set_launch_shapes(self, push_block, field_threads, field_kernel):
+        self._check(self.L.g4gpu_set_launch_shapes(self.h, push_block, field_threads, field_kernel))
+
     def autotune(self):
-        pb, ft = ctypes.c_int(), ctypes.c_int()
-        self._check(self.L.g4gpu_autotune(self.h, ctypes.byref(pb), ctypes.byref(ft)))
-        return pb.value, ft.value
+        """(push threads per block, field kernel threads per CTA, field kernel: 0 one
+        CTA per slice, 1 a cluster pair)"""
+        pb, ft, fk = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(self.L.g4gpu_autotune(self.h, ctypes.byref(pb), ctypes.byref(ft), ctypes.byref(fk)))
+        return pb.value, ft.value, fk.value
 
 
 def adi_advance_noalloc(field_ptr, source_ptr, nslice, ngrid, first, delz, dgrid, xks, device=0,

@@ -183,11 +183,18 @@ int g4gpu_set_graph_mode(g4gpu_handle h, int on);
 /* Times the candidate launch shapes of the step kernels on the handle's own data
  * (one step per candidate; beam and field are restored afterwards) and keeps the
  * fastest: threads per block of the push, threads per CTA of the fused field
- * kernel. Choices are cached per (precision, npart, ngrid, nfield, solver) for
- * the life of the process. Requires the lattice, beam and fields to be loaded.
- * *push_block and *field_threads (may be NULL) receive the choice. No reference
- * counterpart. */
-int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_threads);
+ * kernel, and the fused field kernel itself (0: one CTA per slice, 1: a cluster of
+ * two CTAs per slice, each holding half the rows). Choices are cached per
+ * (precision, npart, ngrid, nfield, solver) for the life of the process. Requires
+ * the lattice, beam and fields to be loaded. *push_block, *field_threads and
+ * *field_kernel (each may be NULL) receive the choice. No reference counterpart. */
+int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_threads, int *field_kernel);
+/* Sets the launch shapes g4gpu_autotune would choose: push_block a multiple of 32 in
+ * [32, 512], field_threads a multiple of 32 in [2 ngrid, 1024] (mixed ADI form), and
+ * field_kernel 0 or 1; other values are rejected with G4GPU_ERR_ARG. The pair kernel
+ * runs only where its segmented solves apply; elsewhere the single-CTA kernel does. No
+ * reference counterpart. */
+int g4gpu_set_launch_shapes(g4gpu_handle h, int push_block, int field_threads, int field_kernel);
 
 /* A batch owns nrun independent handles (one time window each, with its own
  * sizes, lattice and stream), e.g. an ensemble of runs of uneven slice counts,

@@ -70,9 +70,10 @@ def test_graph_mode_matches_direct_launches(lib, precision, tol):
 def test_autotune_keeps_results(lib, precision):
     lat, beam, cur, fld = window(16, 512, 61, 5)
     with make(lat, beam, cur, fld, precision) as h:
-        pb, ft = h.autotune()
+        pb, ft, fk = h.autotune()
         assert pb in (128, 256, 512)
         assert ft % 32 == 0 and 2 * 61 <= ft <= 1024
+        assert fk in (0, 1) and (precision == 1 or fk == 0)
         # the tuning steps are undone
         p = h.get_beam()
         assert np.array_equal(p, beam) if precision == 0 else rel_err(p, beam) < 1e-6
@@ -113,3 +114,54 @@ def test_batch_of_uneven_runs_matches_single_runs(lib):
             bd0, fd0 = h.diag(1)
         assert rel_err(fd[0][:, 0], fd0[0][:, 0]) < 1e-4
         assert np.max(np.abs(bd[:, 24] - bd0[:, 24])) < 1e-4
+
+
+@pytest.mark.parametrize("ng", [51, 151, 201])
+def test_cluster_pair_field_kernel_matches_single_cta(lib, ng):
+    """The mixed form's field step on a cluster of two CTAs per slice (rows split,
+    deposition and column solves across the pair through distributed shared memory)
+    against the one-CTA-per-slice kernel (ngrid <= 168) or the tiled two-pass ADI
+    (ngrid 201, which the pair replaces by default): a lasing window over whole
+    undulator steps with slippage."""
+    import g4gpu
+    import g4cases as T
+    ns, npart = 24, 1024
+    lat = T.undulator_lattice(1.7, 0.015, 30, 1, 1e-10, 17081.0)
+    cur = np.full(ns, 3000.0)
+    beam = g4gpu.host_load_beam(T.slice_params(ns, 17081.0, 2.0, 0.4e-6, 15.0, currents=cur), 0, npart, 4, 5, 1,
+                                1e-10, 1.0)
+    seed = g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e5, 30e-6), 1e-4, ng)
+    fld = np.repeat(seed[None, :], ns, axis=0)
+    out = []
+    for fk in (1, 0):
+        cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, gridmax=1e-4, lambda0=1e-10, sample=1.0,
+                           gammaref=17081.0, precision=1, time_run=1)
+        with g4gpu.Handle(cfg) as h:
+            h.set_lattice(lat)
+            h.load_beam(beam, cur)
+            h.load_field(0, fld, first=7)
+            if ng <= 168:
+                h.set_launch_shapes(256, max(512, (2 * ng + 31) // 32 * 32), fk)
+            elif fk == 0:
+                continue
+            h.run(0, lat.shape[0])
+            out.append((h.diag(1), h.get_field(0)[0], h.get_beam()))
+    if ng > 168:
+        # the pair against the FP64 form
+        cfgp = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, gridmax=1e-4, lambda0=1e-10, sample=1.0,
+                            gammaref=17081.0, precision=0, time_run=1)
+        with g4gpu.Handle(cfgp) as h:
+            h.set_lattice(lat)
+            h.load_beam(beam, cur)
+            h.load_field(0, fld, first=7)
+            h.run(0, lat.shape[0])
+            out.append((h.diag(1), h.get_field(0)[0], h.get_beam()))
+        tol = 1e-2
+    else:
+        tol = 1e-4
+    (b1, f1), F1, P1 = out[0]
+    (b0, f0), F0, P0 = out[1]
+    assert rel_err(f1[0][:, 0], f0[0][:, 0]) < tol
+    assert rel_err(F1, F0) < (tol if ng <= 168 else 1e-2)
+    assert np.max(np.abs(b1[:, 24] - b0[:, 24])) <= tol * np.max(np.abs(b0[:, 24])) + 1e-4
+
