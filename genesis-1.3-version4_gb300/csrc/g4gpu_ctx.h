@@ -75,7 +75,7 @@ struct g4gpu_ctx {
 
   // learned closure (g4gpu_learned.cpp)
   g4gpu_mlp_ctx *mlp = nullptr;
-  float *closure_basis = nullptr;  // [16][ngrid^2] Gauss-Hermite modes of field 0
+  float *closure_basis = nullptr;  // [4][ngrid] 1-D factors of the Gauss-Hermite modes of field 0
   float *closure_feat = nullptr;   // [nslice][32]
   float *closure_corr = nullptr;   // [nslice][4]
   float closure_u0 = 1.f, closure_c0 = 1.f;

@@ -391,21 +391,20 @@ int g4gpu_closure_attach(g4gpu_handle h, g4gpu_mlp m, double waist, double u0, d
   if (!(waist > 0) || !(u0 > 0) || !(c0 > 0)) return g4_fail(h, G4GPU_ERR_ARG, "closure: waist, u0, c0 > 0");
   cudaSetDevice(h->cfg.device);
   int ng = h->cfg.ngrid;
-  size_t ncell = (size_t)ng * ng;
   double gm = h->cfg.gridmax[0], dg = 2 * gm / (ng - 1);
-  // Gauss-Hermite modes HG_mn, m, n = 0..3, on the grid of field 0 (cell area included)
-  std::vector<float> basis(16 * ncell);
-  for (int q = 0; q < 16; q++) {
-    int mm = q / 4, nn = q % 4;
-    double norm = std::sqrt(2.0 / 3.14159265358979323846) / waist /
-                  std::sqrt(std::pow(2.0, mm + nn) * std::tgamma(mm + 1.0) * std::tgamma(nn + 1.0));
-    for (int iy = 0; iy < ng; iy++)
-      for (int ix = 0; ix < ng; ix++) {
-        double x = -gm + ix * dg, y = -gm + iy * dg;
-        double sx = std::sqrt(2.0) * x / waist, sy = std::sqrt(2.0) * y / waist;
-        double v = norm * herm(mm, sx) * herm(nn, sy) * std::exp(-(x * x + y * y) / (waist * waist)) * dg * dg;
-        basis[q * ncell + (size_t)iy * ng + ix] = (float)v;
-      }
+  // Gauss-Hermite modes HG_mn(x, y) = h_m(x) h_n(y), m, n = 0..3, on the grid of field 0:
+  // the 1-D factors h_m(x_i) = sqrt(sqrt(2 / pi) / w) / sqrt(2^m m!) H_m(sqrt(2) x_i / w)
+  // exp(-x_i^2 / w^2) dg (one cell side each, so that their product carries the cell area);
+  // the grid is the same in x and y, so one table [4][ngrid] serves both
+  std::vector<float> basis(4 * (size_t)ng);
+  for (int mm = 0; mm < 4; mm++) {
+    double norm = std::sqrt(std::sqrt(2.0 / 3.14159265358979323846) / waist) /
+                  std::sqrt(std::pow(2.0, mm) * std::tgamma(mm + 1.0));
+    for (int i = 0; i < ng; i++) {
+      double x = -gm + i * dg;
+      basis[(size_t)mm * ng + i] =
+          (float)(norm * herm(mm, std::sqrt(2.0) * x / waist) * std::exp(-x * x / (waist * waist)) * dg);
+    }
   }
   if (!h->closure_basis) {
     int rc = g4_alloc(h, (void **)&h->closure_basis, basis.size() * 4);

@@ -61,11 +61,19 @@ __global__ void __launch_bounds__(BS) k_features(const void *theta, const void *
                                                  const void *field, const float *basis, int mixed,
                                                  double gref, int ns, int np, int ng, int first, float u0,
                                                  float c0, float *out) {
-  __shared__ float sh[BS / 32];
-  int is = blockIdx.x;
-  size_t base = (size_t)is * np;
+  constexpr int NW = BS / 32;
+  extern __shared__ __align__(16) float fsm[];
+  float *hb = fsm;                                         // [4][ng] 1-D Gauss-Hermite factors
+  float2 *rp = reinterpret_cast<float2 *>(fsm + 4 * ng);  // [4][ng] row projections (16 ng bytes on)
+  __shared__ float red[NW][8];
+  __shared__ float2 cm[16];
+  const int is = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int t = threadIdx.x; t < 4 * ng; t += BS) hb[t] = basis[t];
+  // particles: bunching b1..b3, mean and second moment of gamma
+  const size_t base = (size_t)is * np;
   float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int ip = threadIdx.x; ip < np; ip += BS) {
+#pragma unroll
     for (int h = 1; h <= 3; h++) {
       float s, c;
       __sincosf(phase_h(theta, base + ip, mixed, h), &s, &c);
@@ -76,30 +84,59 @@ __global__ void __launch_bounds__(BS) k_features(const void *theta, const void *
     acc[6] += g;
     acc[7] += g * g;
   }
-  float *o = out + (size_t)is * kClosureNin;
-  float res[8];
-  for (int q = 0; q < 8; q++) res[q] = bsumf<BS>(acc[q], sh);
-  // field slice: Gauss-Hermite projections
-  size_t ncell = (size_t)ng * ng;
-  int slot = (is + first) % ns;
-  size_t fb = (size_t)slot * ncell;
-  float pr[16], pi[16];
-  for (int q = 0; q < 16; q++) pr[q] = pi[q] = 0.f;
-  for (size_t i = threadIdx.x; i < ncell; i += BS) {
-    float2 u = field_at(field, fb + i, mixed);
 #pragma unroll
-    for (int q = 0; q < 16; q++) {
-      float b = basis[(size_t)q * ncell + i];
-      pr[q] += b * u.x;
-      pi[q] += b * u.y;
+  for (int q = 0; q < 8; q++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+    if (lane == 0) red[warp][q] = acc[q];
+  }
+  __syncthreads();  // hb and the particle sums
+  // field slice: HG_mn projections c_mn = sum_iy h_n(iy) sum_ix h_m(ix) u(ix, iy); each
+  // warp forms the four row projections of its rows
+  const size_t ncell = (size_t)ng * ng;
+  const size_t fb = (size_t)((is + first) % ns) * ncell;
+  for (int iy = warp; iy < ng; iy += NW) {
+    float2 r[4] = {};
+    for (int ix = lane; ix < ng; ix += 32) {
+      const float2 u = field_at(field, fb + (size_t)iy * ng + ix, mixed);
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        const float b = hb[m * ng + ix];
+        r[m].x += b * u.x;
+        r[m].y += b * u.y;
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        r[m].x += __shfl_down_sync(0xffffffffu, r[m].x, o);
+        r[m].y += __shfl_down_sync(0xffffffffu, r[m].y, o);
+      }
+      if (lane == 0) rp[m * ng + iy] = r[m];
     }
   }
-  float cr[16], ci[16];
-  for (int q = 0; q < 16; q++) {
-    cr[q] = bsumf<BS>(pr[q], sh);
-    ci[q] = bsumf<BS>(pi[q], sh);
+  __syncthreads();
+  if (threadIdx.x < 16) {
+    const int m = threadIdx.x / 4, n = threadIdx.x % 4;
+    float2 c = make_float2(0.f, 0.f);
+    for (int iy = 0; iy < ng; iy++) {
+      const float b = hb[n * ng + iy];
+      const float2 v = rp[m * ng + iy];
+      c.x += b * v.x;
+      c.y += b * v.y;
+    }
+    cm[threadIdx.x] = c;
   }
+  __syncthreads();
   if (threadIdx.x == 0) {
+    float res[8];
+    for (int q = 0; q < 8; q++) {
+      float v = 0.f;
+      for (int w = 0; w < NW; w++) v += red[w][q];
+      res[q] = v;
+    }
+    float *o = out + (size_t)is * kClosureNin;
     float inv = 1.f / (float)np;
     for (int q = 0; q < 6; q++) o[q] = res[q] * inv;
     float mg = res[6] * inv;
@@ -111,7 +148,7 @@ __global__ void __launch_bounds__(BS) k_features(const void *theta, const void *
     float am = sqrtf(a2);
     o[9] = am > 0 ? ua.x / am : 1.f;
     o[10] = am > 0 ? ua.y / am : 0.f;
-    for (int q = 0; q < 16; q++) o[11 + q] = log1pf((cr[q] * cr[q] + ci[q] * ci[q]) / (c0 * c0));
+    for (int q = 0; q < 16; q++) o[11 + q] = log1pf((cm[q].x * cm[q].x + cm[q].y * cm[q].y) / (c0 * c0));
     o[27] = (float)(current[is] * 1e-3);
     for (int q = 28; q < kClosureNin; q++) o[q] = 0.f;
   }
@@ -238,8 +275,13 @@ __global__ void k_denormalize(const float *y, const float *scale, const float *s
 void closure_features(void *stream, const void *theta, const void *gam, const double *current,
                       const void *field, const float *basis, int mixed, double gref, int ns, int np, int ng,
                       int first, float u0, float c0, float *out) {
-  k_features<256><<<ns, 256, 0, (cudaStream_t)stream>>>(theta, gam, current, field, basis, mixed, gref, ns, np,
-                                                        ng, first, u0, c0, out);
+  // shared memory: the 1-D factors [4][ng] floats, then the row projections [4][ng]
+  // float2 (at 16 ng bytes, aligned for float2)
+  const size_t smem = (size_t)4 * ng * sizeof(float) + (size_t)4 * ng * sizeof(float2);
+  if (smem > 48u * 1024u)
+    cudaFuncSetAttribute(k_features<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_features<256><<<ns, 256, smem, (cudaStream_t)stream>>>(theta, gam, current, field, basis, mixed, gref, ns, np,
+                                                           ng, first, u0, c0, out);
 }
 
 void closure_apply(void *stream, void *theta, void *gam, void *field, const float *corr, int mixed, int ns,

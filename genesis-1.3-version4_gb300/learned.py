@@ -63,15 +63,16 @@ def make_pair(cfg_kwargs, fine_lat, coarse_lat, beam, current, field, mlp_for_ta
 
 
 def generate_training_data(cfg_kwargs, fine_lat, seeds, slice_params, npart, nbins, field, waist, u0, c0,
-                           factor=4, max_coarse=None):
-    """Features X [n][32] and targets T [n][4] from fine runs over `seeds`."""
+                           factor=4, max_coarse=None, shotnoise=1):
+    """Features X [n][32] and targets T [n][4] from fine runs over `seeds` (the loading
+    seed of each run; shotnoise 0 loads quiet beams)."""
     coarse_lat, fstart, fcount = coarsen_lattice(fine_lat, factor)
     ncoarse = coarse_lat.shape[0] if max_coarse is None else min(max_coarse, coarse_lat.shape[0])
     scratch = g4gpu.MLP()
     X, T = [], []
     lam, sample = cfg_kwargs["lambda0"], cfg_kwargs["sample"]
     for seed in seeds:
-        beam = g4gpu.host_load_beam(slice_params, 0, npart, nbins, seed, 1, lam, sample)
+        beam = g4gpu.host_load_beam(slice_params, 0, npart, nbins, seed, shotnoise, lam, sample)
         hf, hc = make_pair(cfg_kwargs, fine_lat, coarse_lat, beam, slice_params[:, 16], field, scratch, waist,
                            u0, c0)
         with hf, hc:

@@ -106,3 +106,60 @@ def test_judge_falls_back_to_fine_steps(lib):
         bd0, fd0 = href.diag(1)
     scale = np.max(np.abs(fd0[0][:, 0]))
     assert np.max(np.abs(fd[0][:, 0] - fd0[0][:, 0])) <= 1e-3 * scale
+
+
+@pytest.mark.parametrize("precision,first", [(1, 3), (0, 0)])
+def test_closure_features_match_numpy(lib, precision, first):
+    """The per-slice features against an FP64 numpy computation from the same beam and
+    field: bunching h = 1..3, mean and rms of the energy offset, the on-axis field, and
+    the projections on the 16 Gauss-Hermite modes HG_mn (m, n = 0..3) formed with the
+    full two-dimensional basis (the kernel uses its separable factors)."""
+    import math
+    import g4gpu
+    import g4cases as T
+    ns, npart, ng, gm, g0, waist, u0, c0 = 8, 512, 41, 1e-4, 17081.0, 30e-6, 2e3, 5e3
+    cur = np.linspace(1000.0, 3000.0, ns)
+    beam = g4gpu.host_load_beam(T.slice_params(ns, g0, 2.0, 0.4e-6, 15.0, currents=cur), 0, npart, 4, 9, 1,
+                                1e-10, 1.0)
+    par = T.gauss_field_par(1e-10, 1e5, 25e-6)
+    par[5], par[6] = 6e-6, -4e-6  # an off-axis seed: every mode takes part
+    seed = g4gpu.host_gauss_hermite(par, gm, ng)
+    field = seed[None, :] * np.exp(1j * np.linspace(0.0, 3.0, ns))[:, None]
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, gridmax=gm, lambda0=1e-10, sample=1.0, gammaref=g0,
+                       precision=precision, time_run=1)
+    m = g4gpu.MLP(32, 256, 4, seed=0)
+    with g4gpu.Handle(cfg) as h:
+        h.load_beam(beam, cur)
+        h.load_field(0, field, first=first)
+        h.closure_attach(m, waist, u0, c0)
+        X = h.closure_features()
+        p = h.get_beam()
+        f = h.get_field(0)[0]
+    m.close()
+    dg = 2 * gm / (ng - 1)
+    x = -gm + np.arange(ng) * dg
+
+    def herm(n, t):
+        return [np.ones_like(t), 2 * t, 4 * t * t - 2, 8 * t ** 3 - 12 * t][n]
+
+    for ib in range(ns):
+        th, g = p[ib, :, 1], p[ib, :, 0] - g0
+        for hh in range(3):
+            b = np.mean(np.exp(1j * (hh + 1) * th))
+            assert abs(X[ib, 2 * hh] - b.real) < 1e-5 and abs(X[ib, 2 * hh + 1] - b.imag) < 1e-5
+        assert abs(X[ib, 6] - g.mean()) < 1e-5 * max(1.0, abs(g.mean()))
+        assert abs(X[ib, 7] - g.std()) < 1e-3 * g.std()
+        u = f[(ib + first) % ns].reshape(ng, ng)  # [iy][ix]
+        ua = u[ng // 2, ng // 2]
+        assert abs(X[ib, 8] - math.log1p(abs(ua) ** 2 / u0 ** 2)) < 1e-4 * max(1.0, X[ib, 8])
+        for q in range(16):
+            mm, nn = q // 4, q % 4
+            norm = math.sqrt(2 / math.pi) / waist / math.sqrt(2.0 ** (mm + nn) * math.factorial(mm) * math.factorial(nn))
+            sx = math.sqrt(2) * x / waist
+            bx = herm(mm, sx) * np.exp(-x * x / waist ** 2)
+            by = herm(nn, sx) * np.exp(-x * x / waist ** 2)
+            basis = norm * np.outer(by, bx) * dg * dg  # [iy][ix]
+            cq = np.sum(basis * u)
+            want = math.log1p(abs(cq) ** 2 / c0 ** 2)
+            assert abs(X[ib, 11 + q] - want) < 1e-4 * max(1.0, want), (ib, q, X[ib, 11 + q], want)
+        assert abs(X[ib, 27] - cur[ib] * 1e-3) < 1e-6
