@@ -371,6 +371,89 @@ def batched_form(g4gpu, torch, steps, warmup, peak, nrun=ENSEMBLE_RUNS, nerr=4):
                                "bunching_max_rel": max(e["bunching_max_rel"] for e in errs)}}
 
 
+HARM_NS, HARM_NPART, HARM_NGRID, HARM_GRIDMAX, HARM_H = 2048, 16384, 255, 1.5e-4, (1, 3, 5)
+
+
+def harmonic_fft_form(g4gpu, torch, steps, warmup, peak, nsub=256):
+    """The harmonic FFT workload, mixed form: 2048 slices x 16384 particles (nbins 8,
+    shot noise seed 7, delgam 1.0, the flat-top current), fields at the 1st, 3rd and
+    5th harmonic on ngrid 255 over gridmax 1.5e-4 m, FieldSolverFFT, the undulator of
+    the headline workload. Error: power and bunching at harmonics 1..5 against the
+    plain FP64 form on the first `nsub` slices (with the field slipping towards the
+    head and zero entering at slice 0, the first slices of a window evolve exactly as
+    a window of those slices alone)."""
+    dev = torch.cuda.current_device()
+    ns, npart, ng = HARM_NS, HARM_NPART, HARM_NGRID
+    ncell = ng * ng
+    lat, _, _ = workload_inputs(ns)
+    cur = flat_top(ns)
+    sp = T.slice_params(ns, GAMMA0, 1.0, 0.4e-6, 15.0, currents=cur)
+    beam = g4gpu.host_load_beam(sp, 0, npart, 8, 7, 1, LAMBDA0, 1.0)
+    zero = np.zeros((ns, ncell), dtype=np.complex128)
+
+    def handle(precision, n):
+        cfg = g4gpu.Config(nslice=n, npart=npart, ngrid=ng, harm=list(HARM_H), gridmax=[HARM_GRIDMAX] * 3,
+                           lambda0=LAMBDA0, sample=1.0, gammaref=GAMMA0, precision=precision,
+                           solver=g4gpu.SOLVER_FFT, time_run=1, device=dev)
+        h = g4gpu.Handle(cfg)
+        h.set_lattice(lat)
+        h.load_beam(beam[:n], cur[:n])
+        for k in range(len(HARM_H)):
+            h.load_field(k, zero[:n])
+        return h
+
+    h = handle(g4gpu.MIXED, ns)
+    nlat = lat.shape[0]
+    for i in range(warmup):
+        h.run(i % nlat, 1)
+    h.synchronize()
+    stream = torch.cuda.ExternalStream(h.stream())
+    h.reset_stats()
+    h.set_profiling(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(steps):
+        h.run((warmup + i) % nlat, 1)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = h.kernel_stats()
+    h.set_profiling(False)
+    nh = 5
+    bm, fm = h.diag(nh)
+    h.close()
+    with handle(g4gpu.PLAIN, nsub) as hp:
+        hp.run(0, warmup + steps)
+        bp, fp = hp.diag(nh)
+    tot = max(sum(x[1] for x in st.values()), 1e-12)
+    kern = {k: {"launches": n, "ms_total": t, "ms_avg": t / n, "share": t / tot} for k, (n, t) in st.items() if n}
+    # FFT solve of one field over the window: at least the field read and written and
+    # the source read once (FP32 complex: 24 B per cell); the three-pass transform
+    # (rows, columns, rows through global memory) moves 56 B per cell
+    fft_alg = len(HARM_H) * ns * ncell * 24.0 * steps
+    fft_ms = st["fft"][1]
+    out = {"value": ns * steps / (ms / 1e3), "unit": "slice-steps/s", "ms_per_step": ms / steps,
+           "config": f"{ns} slices x {npart} particles (nbins 8), harmonics {list(HARM_H)}, ngrid {ng}, "
+                     f"gridmax {HARM_GRIDMAX} m, FieldSolverFFT, delgam 1.0, shot noise seed 7",
+           "kernels": kern}
+    if fft_ms > 0:
+        a = fft_alg / (fft_ms / 1e3) / 1e9
+        out["fft_roofline"] = {"bound": "hbm", "alg_bytes_per_cell": 24, "design_bytes_per_cell": 56,
+                               "achieved_gbs": a, "peak": peak, "frac": a / peak,
+                               "ms_per_field_solve": fft_ms / (steps * len(HARM_H))}
+    pw = {}
+    for k, hk in enumerate(HARM_H):
+        a, b = fm[k][:nsub, 0], fp[k][:, 0]
+        pw[f"h{hk}"] = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+    bun = {}
+    for j in range(nh):
+        a, b = bm[:nsub, 24 + 2 * j], bp[:, 24 + 2 * j]
+        bun[f"h{j + 1}"] = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+    out["error_vs_plain"] = {"slices": nsub, "after_steps": warmup + steps, "power_max_rel": pw,
+                             "bunching_max_rel": bun}
+    return out
+
+
 def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_slices=64, max_coarse=63,
                  check_every=8, tol=0.01, gamma0=GAMMA0, seed_power=0.0, time_run=1, shotnoise=1):
     """The coarse-step closure on the full window. Training data: fine (one-period)
@@ -589,8 +672,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--nslice", type=int, default=None,
                     help="slices of the window (default 4096); smaller values are for profiling only")
-    ap.add_argument("--forms", default="mixed,plain,batched,learned",
-                    help="forms to time besides the mixed headline: plain, batched, learned")
+    ap.add_argument("--forms", default="mixed,plain,batched,harmonic,learned",
+                    help="forms to time besides the mixed headline: plain, batched, harmonic, learned")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default launch shapes of the mixed form instead of autotuning them")
     ap.add_argument("--launch-shapes", default=None,
@@ -702,6 +785,8 @@ def main():
 
     if "batched" in args.forms:
         line["forms"]["batched"] = batched_form(g4gpu, torch, args.steps, args.warmup, peak)
+    if "harmonic" in args.forms:
+        line["forms"]["harmonic_fft"] = harmonic_fft_form(g4gpu, torch, args.steps, args.warmup, peak)
     if "learned" in args.forms:
         line["forms"]["learned"] = learned_form(g4gpu, torch, lat, beam, cur, args.steps, args.warmup)
         # the same closure in steady state (config 0: quiet loading, 1 kW seed, no

@@ -192,8 +192,20 @@ int fft_tables(g4gpu_handle h) {
   g4::FFTPlan &pl = h->fft_plan;
   pl.n = n;
   pl.nstage = 0;
-  int m = n;
-  for (int p = 2; p * p <= m; p++)
+  // radices of the register butterflies: the factors of two as 16s (then one 8, 4
+  // or 2), threes paired with fives (15), the other threes as 9s (then one 3), the
+  // other fives; any further prime factors in ascending order
+  int m = n, twos = 0, threes = 0, fives = 0;
+  for (; m % 2 == 0; m /= 2) twos++;
+  for (; m % 3 == 0; m /= 3) threes++;
+  for (; m % 5 == 0; m /= 5) fives++;
+  for (; twos >= 4; twos -= 4) pl.radix[pl.nstage++] = 16;
+  if (twos > 0) pl.radix[pl.nstage++] = twos == 3 ? 8 : (twos == 2 ? 4 : 2);
+  for (; threes > 0 && fives > 0; threes--, fives--) pl.radix[pl.nstage++] = 15;
+  for (; threes >= 2; threes -= 2) pl.radix[pl.nstage++] = 9;
+  if (threes > 0) pl.radix[pl.nstage++] = 3;
+  for (; fives > 0; fives--) pl.radix[pl.nstage++] = 5;
+  for (int p = 7; p * p <= m; p += 2)
     while (m % p == 0 && pl.nstage < 31) {
       pl.radix[pl.nstage++] = p;
       m /= p;
@@ -220,7 +232,8 @@ int fft_tables(g4gpu_handle h) {
         double dx = static_cast<double>(ix) + shift;
         double x = dx / static_cast<double>(n) / xc;
         int iiy = (iy + (n + 1) / 2) % n, iix = (ix + (n + 1) / 2) % n;
-        size_t ii = (size_t)iiy * n + iix;
+        // stored transposed (kx major) for the column pass
+        size_t ii = (size_t)iix * n + iiy;
         k2[ii] = -(dx * dx + dy * dy) * dk * dk / 2. / xks;
         double r = (std::sqrt(x * x + y * y) - 1) / sig;
         sg[ii] = 1. / (1 + std::exp(r));

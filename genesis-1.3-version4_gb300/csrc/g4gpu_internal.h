@@ -138,7 +138,7 @@ struct FFTPlan {
 };
 int fft_max_ngrid(int mixed);
 // roots: n complex exp(-2 pi i m / n); k2, sig: Im(K2) and the sigmoid filter on the
-// FFT index (real, n^2); work: n^2 * nslice complex scratch, used when filtered
+// FFT index (real, n^2, transposed: element kx n + ky); work: n^2 * nslice complex scratch, used when filtered
 void launch_fft_solve(void *stream, int mixed, void *field, const void *src, void *work,
                       const void *roots, const void *k2, const void *sig, int filtered, double delz,
                       const FFTPlan &pl, int ns, int first);

@@ -299,7 +299,11 @@ def test_run_before_load_is_an_error(lib):
 
 
 @pytest.mark.parametrize("solver,filt", [(1, None), (2, (0.7, 0.9, 0.3))])
-@pytest.mark.parametrize("n", [25, 45])
+# grid sizes whose plans take every stage of the transform: the register
+# butterflies of radix 2, 3, 4, 5, 7, 8, 9, 11, 13, 15, 16, 17 and the generic
+# stage (19): 25 = 5 5, 45 = 15 3, 32 = 16 2, 56 = 8 7, 22 = 2 11, 26 = 2 13,
+# 34 = 2 17, 38 = 2 19, 27 = 9 3, 100 = 4 5 5
+@pytest.mark.parametrize("n", [25, 45, 32, 56, 22, 26, 34, 38, 27, 100])
 def test_fft_solver_plain_matches_oracle(lib, oracle, solver, filt, n):
     """FieldSolverFFT (src/Core/FieldSolverFFT.cpp:9-114) on a time-dependent window
     with two harmonics, against the oracle's restatement (pinned to numpy's FFT in
@@ -359,3 +363,48 @@ def test_fft_solver_mixed_within_one_percent(lib, oracle):
     ob = oracle.diag_beam(rp, 1)
     assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-2
     assert bunching_ok(bd[:, 24], ob[:, 24])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_fft_three_harmonics_large_grid_matches_oracle(lib, oracle, precision):
+    """Config 3's field layout at a size the oracle finishes in seconds: fields at the
+    fundamental, 3rd and 5th harmonic, each on ngrid 255 over dgrid 1.5e-4 m, the FFT
+    solver (255 = 3 x 5 x 17: every radix of the mixed-radix transform), nbins 8 quiet
+    loading with shot noise (harmonic bunching), a time-dependent window with slippage.
+    Plain FP64 within 1e-9 of the oracle; the mixed form within its 1 %."""
+    import g4gpu
+    import g4cases as T
+    ns, npart, ng, gm = 3, 256, 255, 1.5e-4
+    harm = [1, 3, 5]
+    lat = T.undulator_lattice(1.7, 0.015, 5, 2, 1e-10, 11357.8, quad_k1=1.5, quad_l=0.08)
+    part = g4gpu.host_load_beam(T.slice_params(ns, 11357.8, 1.0, 0.4e-6, 15.0), 0, npart, 8, 7, 1, 1e-10, 1.0)
+    cur = np.full(ns, 3000.0)
+    fld = np.stack([np.stack([g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e5 / h ** 2, 25e-6, harm=h), gm, ng)
+                              * np.exp(1j * (0.4 * k + h)) for k in range(ns)]) for h in harm])
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, nfield=3, harm=harm, gridmax=[gm] * 3, lambda0=1e-10,
+                       sample=1.0, gammaref=11357.8, precision=precision, solver=g4gpu.SOLVER_FFT, time_run=1)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam(part, cur)
+        for k in range(3):
+            h.load_field(k, fld[k])
+        h.run(0, lat.shape[0])
+        p = h.get_beam()
+        fs = [h.get_field(k) for k in range(3)]
+        bd, fd = h.diag(5)
+    rp, rf, rfirst, _ = oracle.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, harm, [gm] * 3, fld, [0, 0, 0],
+                                         solver=1, nthreads=8)
+    for k in range(3):
+        assert fs[k][1] == rfirst[k]
+    if precision == 0:
+        for k in range(3):
+            assert rel_err(fs[k][0], rf[k]) < 1e-9, k
+        for col in range(6):
+            assert rel_err(p[..., col], rp[..., col]) < 1e-9, col
+    else:
+        ob = oracle.diag_beam(rp, 5)
+        for k in range(3):
+            of = oracle.diag_field(rf[k], gm, 1e-10, harm[k], int(rfirst[k]))
+            assert rel_err(fd[k][:, 0], of[:, 0]) < 1e-2, k
+        for hh in range(5):  # bunching at harmonics 1..5
+            assert bunching_ok(bd[:, 24 + 2 * hh], ob[:, 24 + 2 * hh])
