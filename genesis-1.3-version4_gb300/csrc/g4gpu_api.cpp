@@ -211,11 +211,32 @@ int fft_tables(g4gpu_handle h) {
       m /= p;
     }
   if (m > 1) pl.radix[pl.nstage++] = m;
-  std::vector<double> roots(2 * n);
+  // the n roots exp(-2 pi i m / n), then per stage the twiddles exp(-2 pi i q k / (ns R))
+  const double two_pi = 2.0 * 3.14159265358979323846;
+  std::vector<double> roots(2 * (2 * n - 1));
   for (int i = 0; i < n; i++) {
-    double a = 2.0 * 3.14159265358979323846 * (double)i / (double)n;
+    double a = two_pi * (double)i / (double)n;
     roots[2 * i] = std::cos(a);
     roots[2 * i + 1] = -std::sin(a);
+  }
+  int off = 0, nsp = 1;
+  auto magic = [](int d) { return d <= 1 ? 0u : (unsigned)((((unsigned long long)1 << 32) + d - 1) / d); };
+  pl.mn = magic(n);
+  for (int s = 0; s < pl.nstage; s++) {
+    const int r = pl.radix[s];
+    pl.tw_off[s] = off;
+    pl.nb[s] = n / r;
+    pl.mnb[s] = magic(n / r);
+    pl.mns[s] = magic(nsp);
+    if (nsp > 1)
+      for (int q = 1; q < r; q++)
+        for (int kk = 0; kk < nsp; kk++) {
+          double a = two_pi * (double)(q * kk) / (double)(nsp * r);
+          roots[2 * (n + off)] = std::cos(a);
+          roots[2 * (n + off) + 1] = -std::sin(a);
+          off++;
+        }
+    nsp *= r;
   }
   double xc = c.xcut, yc = c.ycut, sig = c.sigmoid;
   for (int k = 0; k < c.nfield; k++) {
@@ -223,7 +244,8 @@ int fft_tables(g4gpu_handle h) {
     double xks = 4. * std::asin(1) / xlambda;
     double dgrid = 2 * c.gridmax[k] / static_cast<double>(n - 1);
     double dk = 4. * std::asin(1.) / (static_cast<double>(n) * dgrid);
-    std::vector<double> k2((size_t)n * n), sg((size_t)n * n);
+    std::vector<double> sg((size_t)n * n);
+    h->fft_k2c[k] = -dk * dk / 2. / xks;
     double shift = -0.5 * static_cast<double>(n - 1);
     for (int iy = 0; iy < n; iy++) {
       double dy = static_cast<double>(iy) + shift;
@@ -234,15 +256,13 @@ int fft_tables(g4gpu_handle h) {
         int iiy = (iy + (n + 1) / 2) % n, iix = (ix + (n + 1) / 2) % n;
         // stored transposed (kx major) for the column pass
         size_t ii = (size_t)iix * n + iiy;
-        k2[ii] = -(dx * dx + dy * dy) * dk * dk / 2. / xks;
         double r = (std::sqrt(x * x + y * y) - 1) / sig;
         sg[ii] = 1. / (1 + std::exp(r));
       }
     }
     size_t es = h->mixed ? sizeof(float) : sizeof(double);
     int rc;
-    if ((rc = alloc(h, &h->fft_roots[k], (size_t)n * 2 * es))) return rc;
-    if ((rc = alloc(h, &h->fft_k2[k], (size_t)n * n * es))) return rc;
+    if ((rc = alloc(h, &h->fft_roots[k], roots.size() * es))) return rc;
     if ((rc = alloc(h, &h->fft_sig[k], (size_t)n * n * es))) return rc;
     auto put = [&](void *dst, const std::vector<double> &v) -> int {
       if (h->mixed) {
@@ -251,7 +271,7 @@ int fft_tables(g4gpu_handle h) {
       }
       return cudaMemcpy(dst, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice);
     };
-    if (put(h->fft_roots[k], roots) || put(h->fft_k2[k], k2) || put(h->fft_sig[k], sg))
+    if (put(h->fft_roots[k], roots) || put(h->fft_sig[k], sg))
       return fail(h, G4GPU_ERR_CUDA, "copy of the FFT tables failed");
   }
   return G4GPU_OK;
@@ -353,6 +373,10 @@ int g4gpu_create(const g4gpu_config *cfg, g4gpu_handle *out) {
     if (c.ngrid > g4::fft_max_ngrid(h->mixed))
       return bail(fail(h, G4GPU_ERR_ARG, "ngrid too large for the FFT solver"));
     if ((rc = fft_tables(h))) return bail(rc);
+    if (!g4::fft_plan_fits(h->fft_plan))
+      return bail(fail(h, G4GPU_ERR_ARG,
+                       "ngrid " + std::to_string(c.ngrid) +
+                           ": a stage of its FFT plan has more than 256 butterflies per line"));
   }
   if ((rc = alloc(h, (void **)&h->derr, sizeof(int)))) return bail(rc);
   cudaMemsetAsync(h->derr, 0, sizeof(int), h->stream);
@@ -371,7 +395,7 @@ void g4gpu_destroy(g4gpu_handle h) {
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
-    void *fp[] = {h->field[k], h->src[k], h->fft_roots[k], h->fft_k2[k], h->fft_sig[k]};
+    void *fp[] = {h->field[k], h->src[k], h->fft_roots[k], h->fft_sig[k]};
     for (void *p : fp)
       if (p) cudaFree(p);
   }
@@ -677,9 +701,8 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
         // a zero source makes the filtered term vanish (FieldSolverFFT.cpp:74-90)
         int filtered = c.source_filter && srck && c.sigmoid > 0 && c.xcut > 0 && c.ycut > 0;
         Timed t(h, G4GPU_K_FFT, 3);
-        g4::launch_fft_solve(h->stream, h->mixed, h->field[k], srck, h->tmp, h->fft_roots[k],
-                             h->fft_k2[k], h->fft_sig[k], filtered, sc.delz, h->fft_plan, ns,
-                             sc.f[k].first);
+        g4::launch_fft_solve(h->stream, h->mixed, h->field[k], srck, h->tmp, h->fft_roots[k], h->fft_k2c[k],
+                             h->fft_sig[k], filtered, sc.delz, h->fft_plan, ns, sc.f[k].first);
       }
     } else if (do_field) {
       for (int k = 0; k < c.nfield; k++) {

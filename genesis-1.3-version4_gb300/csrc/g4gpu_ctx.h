@@ -30,7 +30,7 @@ struct g4gpu_ctx {
   size_t coef_bytes = 0;
   // FFT solver tables per field: roots of unity [n], Im(K2) and the sigmoid [n^2]
   void *fft_roots[G4GPU_MAX_FIELDS] = {};
-  void *fft_k2[G4GPU_MAX_FIELDS] = {};
+  double fft_k2c[G4GPU_MAX_FIELDS] = {};  // -dk^2 / (2 xks): Im(K2) = (dx^2 + dy^2) k2c
   void *fft_sig[G4GPU_MAX_FIELDS] = {};
   g4::FFTPlan fft_plan{};
   int *derr = nullptr;

@@ -134,14 +134,30 @@ int adi_noalloc_mixed(int device, void *stream, void *field, const void *source,
 // kernels_fft.cu: FFT field solver (FieldSolverFFT::FFT)
 struct FFTPlan {
   int n, nstage;
-  int radix[32];  // prime factors of n
+  int radix[32];   // radices of the stages, whose product is n
+  int tw_off[32];  // offset of each stage's twiddles in the table after the n roots
+  int nb[32];      // n / radix
+  // ceil(2^32 / d) for d = nb and d = ns (the product of the earlier radices): the
+  // kernels divide small integers x (x d < 2^32) by them as one multiply-high
+  unsigned mnb[32], mns[32];
+  unsigned mn;  // ceil(2^32 / n)
 };
 int fft_max_ngrid(int mixed);
-// roots: n complex exp(-2 pi i m / n); k2, sig: Im(K2) and the sigmoid filter on the
-// FFT index (real, n^2, transposed: element kx n + ky); work: n^2 * nslice complex scratch, used when filtered
-void launch_fft_solve(void *stream, int mixed, void *field, const void *src, void *work,
-                      const void *roots, const void *k2, const void *sig, int filtered, double delz,
-                      const FFTPlan &pl, int ns, int first);
+// lines of a slice one CTA transforms at a time in a pass with `bufs` tile buffers
+// and `per_sm` CTAs on an SM (es: bytes of a complex element; at most maxL)
+int fft_lines_per_cta(const FFTPlan &pl, int es, int bufs, int maxL, int per_sm);
+// whether the kernels can take the plan's stages (one butterfly per thread for a
+// line of each register stage, at most 8 outputs per thread of a generic one)
+int fft_plan_fits(const FFTPlan &pl);
+// roots: n complex exp(-2 pi i m / n) followed by the stage twiddles, stage s's
+// exp(-2 pi i q k / (ns R)) at tw_off[s] + (q - 1) ns + k (ns the product of the
+// earlier radices, R the stage's, 0 < q < R, k < ns), n - 1 in all; k2c:
+// -dk^2 / (2 xks), Im(K2) = (dx^2 + dy^2) k2c; sig: the sigmoid filter on the FFT
+// index (real, n^2, transposed: element kx n + ky); work: n^2 * nslice complex
+// scratch, used when filtered
+void launch_fft_solve(void *stream, int mixed, void *field, const void *src, void *work, const void *roots,
+                      double k2c, const void *sig, int filtered, double delz, const FFTPlan &pl, int ns,
+                      int first);
 
 // kernels_mlp.cu: BF16 tensor-core MLP (mma.sync m16n8k16, FP32 accumulation)
 void mlp_gemm_nt(void *stream, const void *A, const void *B, const float *bias, float *C, void *Cb, int M,

@@ -6,16 +6,20 @@
 // shifted frequency map (FieldSolverFFT.cpp:131-145).
 //
 // The 2-D transform of each ngrid x ngrid slice is done as three passes over
-// global memory, each in shared memory:
-//   rows:    forward FFT of every row (and of the source rows when filtered)
+// global memory, each on tiles of whole lines in shared memory:
+//   rows:    forward FFT of every row (and, filtered, of the source rows)
 //   columns: forward FFT of every column, the k-space propagator (and filtered
 //            source), inverse FFT of every column
 //   rows:    inverse FFT of every row, 1/n^2, + 2 src when unfiltered
+// The passes are persistent CTAs whose next tile's loads, issued at once as
+// asynchronous copies, are in flight while the current tile is transformed.
 // Every 1-D transform is a Stockham autosort mixed-radix FFT over the factors of
-// ngrid (radices 2, 3, 4, 5, 7, 8, 9, 11, 13, 15, 16, 17 as register butterflies;
-// any other prime factor p as an O(p)-per-point stage), with the n-th roots of
-// unity in shared memory. Templated on the precision: double2 for
-// the plain form, float2 for the mixed form.
+// ngrid: radices 2, 3, 4, 5, 7, 8, 9, 11, 13, 15, 16, 17 as butterflies held in
+// registers (one butterfly per thread, their roots compile-time constants), any
+// other prime factor p as an O(p)-per-point stage. The stage twiddles come from a table laid out per stage so
+// that a warp reads consecutive entries. Templated on the precision: double2 for
+// the plain form, float2 for the mixed form, whose complex arithmetic uses the
+// paired FP32 instructions (both lanes of a float2 in one instruction).
 #include <cuda_runtime.h>
 
 #include "g4gpu_internal.h"
@@ -41,246 +45,294 @@ __device__ __forceinline__ T2 mk(typename Real<T2>::T x, typename Real<T2>::T y)
   r.y = y;
   return r;
 }
-template <typename T2>
-__device__ __forceinline__ T2 cm(T2 a, T2 b) {
-  return mk<T2>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+
+// Complex arithmetic: add, sub; axpy(c, a, y) = y + c a (c real); cm(a, w) = a w;
+// cmc(a, w) = a conj(w); addi(a, b) = a + i b; subi(a, b) = a - i b.
+__device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 axpy(float c, float2 a, float2 y) { return __ffma2_rn(make_float2(c, c), a, y); }
+__device__ __forceinline__ float2 cm(float2 a, float2 w) {
+  return __ffma2_rn(make_float2(-a.y, a.y), make_float2(w.y, w.x), __fmul2_rn(make_float2(a.x, a.x), w));
+}
+__device__ __forceinline__ float2 cmc(float2 a, float2 w) {
+  return __ffma2_rn(make_float2(a.y, -a.x), make_float2(w.y, w.y), __fmul2_rn(a, make_float2(w.x, w.x)));
+}
+__device__ __forceinline__ float2 addi(float2 a, float2 b) {
+  return __ffma2_rn(make_float2(b.y, b.x), make_float2(-1.f, 1.f), a);
+}
+__device__ __forceinline__ float2 subi(float2 a, float2 b) {
+  return __ffma2_rn(make_float2(b.y, b.x), make_float2(1.f, -1.f), a);
 }
 
-// One radix-R Stockham stage over `lines` lines (line stride `ls`) from `in` to
-// `out`, one butterfly per thread at a time, held in registers. With ns the product
-// of the earlier radices and nb = n / R, butterfly j (k = j mod ns) reads
-// in[j + q nb], q < R, multiplies input q by the twiddle W^{q k n/(ns R)}, takes the
-// R-point DFT, and writes output t to out[(j - k) R + t ns + k]:
-//   out[...] = sum_q in[j + q nb] W^{q (k n/(ns R) + t n/R)},
-// the stage of the transform with roots W[m] = exp(-2 pi i m / n) (conj(W) when
-// inverse). The R-point DFT's roots exp(-2 pi i m / R) are the table's W[m n / R],
-// read once per stage into registers.
-template <typename T2>
-__device__ __forceinline__ T2 add(T2 a, T2 b) {
-  return mk<T2>(a.x + b.x, a.y + b.y);
+__device__ __forceinline__ double2 add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 sub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 axpy(double c, double2 a, double2 y) {
+  return make_double2(y.x + c * a.x, y.y + c * a.y);
 }
-template <typename T2>
-__device__ __forceinline__ T2 sub(T2 a, T2 b) {
-  return mk<T2>(a.x - b.x, a.y - b.y);
+__device__ __forceinline__ double2 cm(double2 a, double2 w) {
+  return make_double2(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
 }
+__device__ __forceinline__ double2 cmc(double2 a, double2 w) {
+  return make_double2(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y);
+}
+__device__ __forceinline__ double2 addi(double2 a, double2 b) { return make_double2(a.x - b.y, a.y + b.x); }
+__device__ __forceinline__ double2 subi(double2 a, double2 b) { return make_double2(a.x + b.y, a.y - b.x); }
 
-// In-place R-point DFT y_t = sum_q x_q w^{q t}, w = exp(-+ 2 pi i / R), of x[0..R)
-// with the roots w^m = wr[m S] (R S = R0; the conjugate is taken when INV).
-// Odd prime R: the pairs (t, R - t) share the sums over x_m + x_{R-m} (real cosine
-// weights) and x_m - x_{R-m} (real sine weights), so that each output costs R - 1
-// real multiply-adds per component. Composite R = P M: M-point DFTs of the P
-// interleaved subsequences joined by twiddles and P-point DFTs (decimation in
-// time; for P = 2 the radix-2 split).
 __host__ __device__ constexpr int small_factor(int r) {
   for (int p = 2; p * p <= r; p++)
     if (r % p == 0) return p;
   return r;
 }
 
-template <int R, int S, bool INV, typename T2, int R0>
-__device__ __forceinline__ void dft(T2 *x, const T2 (&wr)[R0]) {
+// cos and sin of 2 pi m / R at compile time: the angle is reduced to a quadrant
+// offset a in [0, pi/2) exactly in rationals (4 m = quadrant R + rem), and cos a,
+// sin a are summed from their Taylor series (24 terms: below 1e-17 there).
+struct Root {
+  double c, s;
+};
+__host__ __device__ constexpr Root root_of(int m, int R) {
+  const double half_pi = 1.57079632679489661923;
+  const int q4 = (4 * m) / R % 4, rem = (4 * m) % R;
+  const double a = half_pi * (double)rem / (double)R;
+  double sn = a, cs = 1, ts = a, tc = 1;
+  for (int k = 1; k < 24; k++) {
+    ts *= -a * a / (double)((2 * k) * (2 * k + 1));
+    tc *= -a * a / (double)((2 * k - 1) * (2 * k));
+    sn += ts;
+    cs += tc;
+  }
+  switch (q4) {
+    case 0: return Root{cs, sn};
+    case 1: return Root{-sn, cs};
+    case 2: return Root{-cs, -sn};
+    default: return Root{sn, -cs};
+  }
+}
+// the roots w^m = exp(-+2 pi i m / R) of a transform's direction
+template <int R, bool INV>
+struct Roots {
+  double c[R], s[R];
+  __host__ __device__ constexpr Roots() : c(), s() {
+    for (int m = 0; m < R; m++) {
+      const Root r = root_of(m, R);
+      c[m] = r.c;
+      s[m] = INV ? r.s : -r.s;
+    }
+  }
+};
+
+// R-point DFT y_t = sum_q x_q w^{q t} of x[0..R), w = exp(-2 pi i / R) forward and
+// exp(+2 pi i / R) inverse (the roots are compile-time constants). OUT: y_t is
+// written to dst[t ds] as it is formed; otherwise y replaces x.
+// Odd prime R: with a_m = x_m + x_{R-m} and b_m = x_m - x_{R-m},
+//   y_t = A_t + i B_t,  y_{R-t} = A_t - i B_t,
+//   A_t = x_0 + sum_m a_m Re(w^{m t}),  B_t = sum_m b_m Im(w^{m t}),
+// so that each output costs R - 1 real multiply-adds per component.
+// Composite R = P M: the M-point DFTs of the P interleaved subsequences x[P i + s],
+// the twiddles w^{s k}, and P-point DFTs across them (decimation in time):
+//   y_{k + t M} = sum_s w^{s k} w_P^{s t} DFT_M(x_s)_k.
+#define G4_PUT(t, v)          \
+  do {                        \
+    if constexpr (OUT)        \
+      dst[(t) * ds] = (v);    \
+    else                      \
+      x[t] = (v);             \
+  } while (0)
+template <int R, bool INV, bool OUT, typename T2>
+__device__ __forceinline__ void dft(T2 *x, T2 *dst, int ds) {
   typedef typename Real<T2>::T Rt;
+  constexpr Roots<R, INV> w{};
   if constexpr (R == 1) {
-    return;
+    if (OUT) dst[0] = x[0];
   } else if constexpr (R == 2) {
-    T2 a = x[0], b = x[1];
-    x[0] = add(a, b);
-    x[1] = sub(a, b);
+    const T2 a = x[0], b = x[1];
+    G4_PUT(0, add(a, b));
+    G4_PUT(1, sub(a, b));
   } else if constexpr (R == 4) {
     // w = -i forward, +i inverse: exact
-    T2 t0 = add(x[0], x[2]), t1 = sub(x[0], x[2]), t2 = add(x[1], x[3]), t3 = sub(x[1], x[3]);
-    T2 jt3 = INV ? mk<T2>(-t3.y, t3.x) : mk<T2>(t3.y, -t3.x);  // w t3
-    x[0] = add(t0, t2);
-    x[2] = sub(t0, t2);
-    x[1] = add(t1, jt3);
-    x[3] = sub(t1, jt3);
+    const T2 t0 = add(x[0], x[2]), t1 = sub(x[0], x[2]), t2 = add(x[1], x[3]), t3 = sub(x[1], x[3]);
+    G4_PUT(0, add(t0, t2));
+    G4_PUT(2, sub(t0, t2));
+    G4_PUT(1, INV ? addi(t1, t3) : subi(t1, t3));
+    G4_PUT(3, INV ? subi(t1, t3) : addi(t1, t3));
   } else if constexpr (small_factor(R) != R) {
-    // R = P M: the P interleaved subsequences x[P i + s] of length M, their M-point
-    // DFTs, the twiddles w^{s k}, and P-point DFTs across them (decimation in time):
-    //   y_{k + t M} = sum_s w^{s k} w_P^{s t} DFT_M(x_s)_k
     constexpr int P = small_factor(R), M = R / P;
-    T2 sub[P][M];
+    T2 part[P][M];
 #pragma unroll
-    for (int sidx = 0; sidx < P; sidx++)
+    for (int s = 0; s < P; s++)
 #pragma unroll
-      for (int i = 0; i < M; i++) sub[sidx][i] = x[P * i + sidx];
+      for (int i = 0; i < M; i++) part[s][i] = x[P * i + s];
 #pragma unroll
-    for (int sidx = 0; sidx < P; sidx++) dft<M, P * S, INV>(sub[sidx], wr);
+    for (int s = 0; s < P; s++) dft<M, INV, false>(part[s], (T2 *)nullptr, 0);
 #pragma unroll
     for (int k = 0; k < M; k++) {
       T2 y[P];
 #pragma unroll
-      for (int sidx = 0; sidx < P; sidx++) {
-        if (sidx == 0 || k == 0) {
-          y[sidx] = sub[sidx][k];
-        } else {
-          T2 w = wr[sidx * k * S];
-          if (INV) w.y = -w.y;
-          y[sidx] = cm(sub[sidx][k], w);
-        }
-      }
-      dft<P, M * S, INV>(y, wr);
+      for (int s = 0; s < P; s++)
+        y[s] = (s == 0 || k == 0) ? part[s][k] : cm(part[s][k], mk<T2>((Rt)w.c[s * k], (Rt)w.s[s * k]));
+      if (OUT) {
+        dft<P, INV, true>(y, dst + k * ds, M * ds);
+      } else {
+        dft<P, INV, false>(y, (T2 *)nullptr, 0);
 #pragma unroll
-      for (int t = 0; t < P; t++) x[k + t * M] = y[t];
+        for (int t = 0; t < P; t++) x[k + t * M] = y[t];
+      }
     }
   } else {
     constexpr int H = (R - 1) / 2;
     T2 a[H + 1], b[H + 1];
-    T2 y0 = x[0];
+    const T2 x0 = x[0];
+    T2 y0 = x0;
 #pragma unroll
     for (int m = 1; m <= H; m++) {
       a[m] = add(x[m], x[R - m]);
       b[m] = sub(x[m], x[R - m]);
       y0 = add(y0, a[m]);
     }
+    G4_PUT(0, y0);
 #pragma unroll
     for (int t = 1; t <= H; t++) {
-      T2 A = x[0];
-      Rt bx = 0, by = 0;
+      T2 A = x0, B = mk<T2>(0, 0);
 #pragma unroll
       for (int m = 1; m <= H; m++) {
         const int id = (m * t) % R;
-        // w^{id} = cos(2 pi id / R) -+ i sin(2 pi id / R); wr holds the forward roots
-        const Rt c = wr[id * S].x, sn = -wr[id * S].y;
-        A.x += c * a[m].x;
-        A.y += c * a[m].y;
-        bx += sn * b[m].x;
-        by += sn * b[m].y;
+        A = axpy((Rt)w.c[id], a[m], A);
+        B = axpy((Rt)w.s[id], b[m], B);
       }
-      // forward: y_t = A - i B, y_{R-t} = A + i B; inverse: the other way round
-      if (!INV) {
-        x[t] = mk<T2>(A.x + by, A.y - bx);
-        x[R - t] = mk<T2>(A.x - by, A.y + bx);
-      } else {
-        x[t] = mk<T2>(A.x - by, A.y + bx);
-        x[R - t] = mk<T2>(A.x + by, A.y - bx);
-      }
+      G4_PUT(t, addi(A, B));
+      G4_PUT(R - t, subi(A, B));
     }
-    x[0] = y0;
   }
 }
 
+#undef G4_PUT
+
+// x / d for x d < 2^32 with m = ceil(2^32 / d) (exact there); d = 1 passes x through
+__device__ __forceinline__ int fdiv(int x, int d, unsigned m) {
+  return d == 1 ? x : (int)__umulhi((unsigned)x, m);
+}
+
+// One radix-R Stockham stage in place over lines of A, one butterfly per thread:
+// every thread loads its butterfly into registers (stage_load), the CTA
+// synchronises, and every thread writes its outputs (stage_store). With ns the
+// product of the earlier radices and nb = n / R, butterfly j (k = j mod ns) of a
+// line reads in[j + q nb], q < R, multiplies input q by the twiddle
+// exp(-+2 pi i q k / (ns R)), takes the R-point DFT, and writes output t to
+// out[(j - k) R + t ns + k]:
+//   out[...] = sum_q in[j + q nb] W^{q (k n/(ns R) + t n/R)},  W = exp(-+2 pi i / n).
+// The twiddles are tw[(q - 1) ns + k] (forward; conjugated when inverse). The
+// butterfly lives in one register array of the largest radix for every stage, so
+// that the stages' code paths share the registers held across the barrier.
+constexpr int MAX_RADIX = 17;
 template <int R, bool INV, typename T2>
-__device__ void stage_r(const T2 *in, T2 *out, int ls, int lines, int n, int ns, const T2 *W) {
-  const int nb = n / R;
-  const int tws = n / (ns * R);
-  T2 wr[R];
+__device__ __forceinline__ void stage_load(T2 *x, const T2 *src, int nb, int ns, int k, const T2 *tw) {
 #pragma unroll
-  for (int m = 0; m < R; m++) wr[m] = W[m * nb];
-  const int total = lines * nb;
-  // butterfly b = line nb + j, k = j mod ns, advanced by the CTA's stride without
-  // divisions (ns divides nb, so j wrapping past nb leaves k unchanged)
-  const int T = blockDim.x;
-  int line = threadIdx.x / nb, j = threadIdx.x - line * nb, k = j % ns;
-  const int dl = T / nb, dj = T - dl * nb, dk = dj % ns;
-  for (int b = threadIdx.x; b < total; b += T) {
-    const T2 *src = in + line * ls + j;
-    T2 x[R];
+  for (int q = 0; q < R; q++) x[q] = src[q * nb];
+  if (ns > 1) {
 #pragma unroll
-    for (int q = 0; q < R; q++) x[q] = src[q * nb];
-    if (ns > 1) {
-      const int e1 = k * tws;
-      int e = 0;
+    for (int q = 1; q < R; q++) {
+      const T2 w = tw[(q - 1) * ns + k];
+      x[q] = INV ? cmc(x[q], w) : cm(x[q], w);
+    }
+  }
+}
+
+// Stage of any radix r in place: output o of a line is the O(r) sum over its
+// butterfly's inputs with the twiddled root read from the table; a thread forms at
+// most STAGE_ANY_OUT outputs (lines n <= STAGE_ANY_OUT blockDim.x) in registers
+// before the CTA synchronises and they are written.
+constexpr int STAGE_ANY_OUT = 8;
+template <typename T2>
+__device__ __forceinline__ void any_load(T2 *acc, const T2 *A, int ls, int lines, int n, int ns, int r,
+                                         const T2 *W, bool inverse) {
+  const int nb = n / r, nsr = ns * r;
 #pragma unroll
-      for (int q = 1; q < R; q++) {
-        e += e1;  // q k tws < n
-        T2 w = W[e];
-        if (INV) w.y = -w.y;
-        x[q] = cm(x[q], w);
+  for (int u = 0; u < STAGE_ANY_OUT; u++) {
+    const int t = threadIdx.x + u * blockDim.x;
+    if (t < lines * n) {
+      const int line = t / n, o = t - line * n;
+      const int q1 = o / nsr, rem = o - q1 * nsr;
+      const int tt = rem / ns, k = rem - tt * ns;
+      const int e = k * (n / nsr) + tt * nb;  // < n
+      const T2 *src = A + line * ls + q1 * ns + k;
+      T2 v = src[0];
+      int m = 0;
+      for (int q = 1; q < r; q++) {
+        m += e;
+        if (m >= n) m -= n;
+        T2 w = W[m];
+        if (inverse) w.y = -w.y;
+        v = add(v, cm(src[q * nb], w));
       }
+      acc[u] = v;
     }
-    dft<R, 1, INV>(x, wr);
-    T2 *dst = out + line * ls + (j - k) * R + k;
+  }
+}
+template <typename T2>
+__device__ __forceinline__ void any_store(const T2 *acc, T2 *A, int ls, int lines, int n) {
 #pragma unroll
-    for (int t = 0; t < R; t++) dst[t * ns] = x[t];
-    line += dl;
-    j += dj;
-    k += dk;
-    if (k >= ns) k -= ns;
-    if (j >= nb) {
-      j -= nb;
-      line++;
+  for (int u = 0; u < STAGE_ANY_OUT; u++) {
+    const int t = threadIdx.x + u * blockDim.x;
+    if (t < lines * n) {
+      const int line = t / n;
+      A[line * ls + (t - line * n)] = acc[u];
     }
   }
 }
 
-// Stage of any radix r: each output is the O(r) sum over its butterfly's inputs
-// with the twiddled root read from the table (radices without a register DFT).
-template <typename T2>
-__device__ void stage_any(const T2 *in, T2 *out, int ls, int lines, int n, int ns, int r, const T2 *W,
-                          bool inverse) {
-  const int nb = n / r;
-  const int nsr = ns * r;
-  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-    int line = t / n, o = t - line * n;
-    int q1 = o / nsr, rem = o - q1 * nsr;
-    int tt = rem / ns, k = rem - tt * ns;
-    int j = q1 * ns + k;
-    int e = k * (n / nsr) + tt * nb;  // < n
-    const T2 *src = in + line * ls + j;
-    T2 acc = src[0];
-    int m = 0;
-    for (int q = 1; q < r; q++) {
-      m += e;
-      if (m >= n) m -= n;
-      T2 w = W[m];
-      if (inverse) w.y = -w.y;
-      T2 p = cm(src[q * nb], w);
-      acc.x += p.x;
-      acc.y += p.y;
-    }
-    out[line * ls + o] = acc;
-  }
+// Radices with a register butterfly (the others take the generic stage).
+__host__ __device__ constexpr bool register_radix(int r) {
+  return r == 2 || r == 3 || r == 4 || r == 5 || r == 7 || r == 8 || r == 9 || r == 11 || r == 13 || r == 15 ||
+         r == 16 || r == 17;
 }
 
+// One 1-D Stockham FFT of length n, in place over `lines` lines of A stored with
+// line stride `ls`, the stages of the plan's radices in turn. W: the n roots
+// exp(-2 pi i m / n), followed by the stage twiddle table (stage s's at
+// W + n + plan.tw_off[s]).
 template <bool INV, typename T2>
-__device__ __forceinline__ void stage(const T2 *in, T2 *out, int ls, int lines, int n, int ns, int r,
-                                      const T2 *W) {
-  switch (r) {
-    case 2: stage_r<2, INV>(in, out, ls, lines, n, ns, W); break;
-    case 3: stage_r<3, INV>(in, out, ls, lines, n, ns, W); break;
-    case 4: stage_r<4, INV>(in, out, ls, lines, n, ns, W); break;
-    case 5: stage_r<5, INV>(in, out, ls, lines, n, ns, W); break;
-    case 7: stage_r<7, INV>(in, out, ls, lines, n, ns, W); break;
-    case 8: stage_r<8, INV>(in, out, ls, lines, n, ns, W); break;
-    case 9: stage_r<9, INV>(in, out, ls, lines, n, ns, W); break;
-    case 11: stage_r<11, INV>(in, out, ls, lines, n, ns, W); break;
-    case 13: stage_r<13, INV>(in, out, ls, lines, n, ns, W); break;
-    case 15: stage_r<15, INV>(in, out, ls, lines, n, ns, W); break;
-    case 16: stage_r<16, INV>(in, out, ls, lines, n, ns, W); break;
-    case 17: stage_r<17, INV>(in, out, ls, lines, n, ns, W); break;
-    default: stage_any(in, out, ls, lines, n, ns, r, W, INV); break;
-  }
-}
-
-// One 1-D Stockham FFT of length n over `lines` lines stored with line stride `ls`
-// in shared memory, the stages of the plan's radices in turn; the result ends in A
-// (ping-pong through B). Roots W[m] = exp(-2 pi i m / n); the inverse uses conj(W).
-template <typename T2>
-__device__ void fft_lines(T2 *A, T2 *B, int ls, int lines, const FFTPlan &pl, const T2 *W,
-                          bool inverse) {
-  const int n = pl.n;
+__device__ __forceinline__ void fft_lines_dir(T2 *A, int ls, int lines, const FFTPlan &pl, const T2 *W) {
   int ns = 1;
-  T2 *in = A, *out = B;
   for (int s = 0; s < pl.nstage; s++) {
-    const int r = pl.radix[s];
-    if (inverse)
-      stage<true>(in, out, ls, lines, n, ns, r, W);
-    else
-      stage<false>(in, out, ls, lines, n, ns, r, W);
+    const int r = pl.radix[s], nb = pl.nb[s];
+    const T2 *tw = W + pl.n + pl.tw_off[s];
+    const bool act = (int)threadIdx.x < lines * nb;
+    const int line = fdiv(threadIdx.x, nb, pl.mnb[s]), j = threadIdx.x - line * nb;
+    const int k = j - fdiv(j, ns, pl.mns[s]) * ns;
+    const T2 *src = A + line * ls + j;
+    T2 *dst = A + line * ls + (j - k) * r + k;
+    T2 x[MAX_RADIX];
+    switch (r) {
+#define G4_LOAD(R) \
+  case R:          \
+    if (act) stage_load<R, INV>(x, src, nb, ns, k, tw); \
+    break;
+      G4_LOAD(2) G4_LOAD(3) G4_LOAD(4) G4_LOAD(5) G4_LOAD(7) G4_LOAD(8) G4_LOAD(9) G4_LOAD(11) G4_LOAD(13)
+      G4_LOAD(15) G4_LOAD(16) G4_LOAD(17)
+#undef G4_LOAD
+      default: any_load(x, A, ls, lines, pl.n, ns, r, W, INV); break;
+    }
+    __syncthreads();
+    switch (r) {
+#define G4_STORE(R) \
+  case R:           \
+    if (act) dft<R, INV, true>(x, dst, ns); \
+    break;
+      G4_STORE(2) G4_STORE(3) G4_STORE(4) G4_STORE(5) G4_STORE(7) G4_STORE(8) G4_STORE(9) G4_STORE(11)
+      G4_STORE(13) G4_STORE(15) G4_STORE(16) G4_STORE(17)
+#undef G4_STORE
+      default: any_store(x, A, ls, lines, pl.n); break;
+    }
     __syncthreads();
     ns *= r;
-    T2 *tmp = in;
-    in = out;
-    out = tmp;
   }
-  if (in != A) {
-    for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-      int line = t / n, e = t - line * n;
-      A[line * ls + e] = in[line * ls + e];
-    }
-    __syncthreads();
-  }
+}
+template <typename T2>
+__device__ __forceinline__ void fft_lines(T2 *A, int ls, int lines, const FFTPlan &pl, const T2 *W, bool inverse) {
+  if (inverse)
+    fft_lines_dir<true>(A, ls, lines, pl, W);
+  else
+    fft_lines_dir<false>(A, ls, lines, pl, W);
 }
 
 // Asynchronous copy of one complex element from global to shared memory
@@ -301,64 +353,77 @@ __device__ __forceinline__ void cp_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// Row pass over `rows_per_cta` rows of one slice. mode 0: forward FFT of the rows of
-// the field (and, with src_rows_out, of the source rows into that buffer); mode 1:
-// inverse FFT of the rows, times `scale`, plus 2 src when `src` is given. The field
-// rows go to A and the second input (the source rows) to C by asynchronous copies
-// issued together; the transform of A starts as soon as A has landed.
-// Two CTAs per SM in FP32 (at most 128 registers a thread).
-template <typename T2>
-__global__ void __launch_bounds__(256, sizeof(T2) == 8 ? 2 : 1)
-    k_fft_rows(T2 *__restrict__ field, const T2 *__restrict__ src, T2 *__restrict__ src_rows_out,
-               const T2 *__restrict__ roots, FFTPlan pl, int ns, int first, int mode, double scale,
-               int rows_per_cta) {
+// Bulk prefetch of [p, p + bytes) into L2 (the 16-byte-aligned part of it).
+__device__ __forceinline__ void prefetch_l2(const void *p, size_t bytes) {
+  const unsigned long long a = ((unsigned long long)p + 15) & ~15ull;
+  const unsigned long long e = ((unsigned long long)p + bytes) & ~15ull;
+  if (e > a) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(a), "r"((unsigned)(e - a)) : "memory");
+}
+
+// CTAs per SM the passes' launch bounds provide for (the register budget of a
+// thread is 64K / (256 x CTAs)): the row pass holds one butterfly across a barrier,
+// the column pass two transforms, the propagator and the transposed copies.
+constexpr int ROWS_CTAS_FP32 = 3, ROWS_CTAS_FP64 = 2, COLS_CTAS_FP32 = 2, COLS_CTAS_FP64 = 1;
+
+// Both passes are persistent: tile = ii nblk + blk runs over the window's slices ii
+// and each slice's blocks of L lines; CTA b takes tiles b, b + gridDim.x, ... and
+// prefetches its next tile by asynchronous copies into the second of two tile
+// buffers while it transforms the current one in place.
+
+// Row pass over tiles of L rows. MODE 0: forward FFT of the rows of `in` into `out`
+// (the same place of slice (ii + first) mod ns of each); MODE 1: inverse FFT of
+// the rows of `in`, times `scale`, plus 2 src (slice ii) when src is given, into
+// `out`. in == out transforms in place.
+template <typename T2, int MODE>
+__global__ void __launch_bounds__(256, sizeof(T2) == 8 ? ROWS_CTAS_FP32 : ROWS_CTAS_FP64)
+    k_fft_rows(const T2 *in, T2 *out, const T2 *__restrict__ src, const T2 *__restrict__ roots, FFTPlan pl,
+               int ns, int first, double scale, int L) {
   typedef typename Real<T2>::T R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T2 *W = reinterpret_cast<T2 *>(smem_raw);
   const int n = pl.n;
-  T2 *A = W + n;
-  T2 *B = A + rows_per_cta * n;
-  T2 *C = B + rows_per_cta * n;
-  const int ii = blockIdx.y;
-  const int i = (ii + first) % ns;
+  T2 *Abuf = W + 2 * n;  // two tile buffers
+  const int nblk = (n + L - 1) / L, ntiles = ns * nblk;
   const size_t ncell = (size_t)n * n;
-  const int r0 = blockIdx.x * rows_per_cta;
-  const int lines = min(rows_per_cta, n - r0);
-  const int cnt = lines * n;
-  T2 *base = field + (size_t)i * ncell + (size_t)r0 * n;
-  const T2 *sb = src ? src + (size_t)ii * ncell + (size_t)r0 * n : nullptr;
-  for (int t = threadIdx.x; t < n; t += blockDim.x) cp_elem(W + t, roots + t);
-  for (int t = threadIdx.x; t < cnt; t += blockDim.x) cp_elem(A + t, base + t);
-  cp_commit();
-  if (sb)
-    for (int t = threadIdx.x; t < cnt; t += blockDim.x) cp_elem(C + t, sb + t);
-  cp_commit();
-  cp_wait<1>();
-  __syncthreads();
-  fft_lines(A, B, n, lines, pl, W, mode == 1);
-  if (mode == 0) {
-    for (int t = threadIdx.x; t < cnt; t += blockDim.x) base[t] = A[t];
-    if (src_rows_out) {
-      cp_wait<0>();
-      __syncthreads();
-      fft_lines(C, B, n, lines, pl, W, false);
-      T2 *dst = src_rows_out + (size_t)ii * ncell + (size_t)r0 * n;
-      for (int t = threadIdx.x; t < cnt; t += blockDim.x) dst[t] = C[t];
-    }
-  } else {
-    cp_wait<0>();
-    __syncthreads();
-    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-      T2 v = A[t];
-      T2 o = mk<T2>(v.x * (R)scale, v.y * (R)scale);
-      if (sb) {
-        T2 sv = C[t];
-        o.x += (R)2. * sv.x;
-        o.y += (R)2. * sv.y;
-      }
-      base[t] = o;
-    }
+  for (int t = threadIdx.x; t < 2 * n - 1; t += blockDim.x) cp_elem(W + t, roots + t);
+  int tile = blockIdx.x;
+  if (tile < ntiles) {
+    const int ii = tile / nblk, r0 = (tile - ii * nblk) * L, cnt = min(L, n - r0) * n;
+    const T2 *g = in + (size_t)((ii + first) % ns) * ncell + (size_t)r0 * n;
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) cp_elem(Abuf + t, g + t);
   }
+  cp_commit();
+  for (int it = 0; tile < ntiles; tile += gridDim.x, it++) {
+    T2 *A = Abuf + (it & 1) * L * n;
+    const int ii = tile / nblk, r0 = (tile - ii * nblk) * L, lines = min(L, n - r0), cnt = lines * n;
+    const T2 *sb = (MODE == 1 && src) ? src + (size_t)ii * ncell + (size_t)r0 * n : nullptr;
+    // the source rows of the epilogue: into L2 while the rows are transformed
+    if (sb && threadIdx.x == 0) prefetch_l2(sb, (size_t)cnt * sizeof(T2));
+    const int nx = tile + gridDim.x;
+    if (nx < ntiles) {
+      const int jj = nx / nblk, q0 = (nx - jj * nblk) * L, qc = min(L, n - q0) * n;
+      const T2 *g = in + (size_t)((jj + first) % ns) * ncell + (size_t)q0 * n;
+      T2 *dst = Abuf + ((it + 1) & 1) * L * n;
+      for (int t = threadIdx.x; t < qc; t += blockDim.x) cp_elem(dst + t, g + t);
+    }
+    cp_commit();
+    cp_wait<1>();  // this tile's rows (committed one iteration earlier)
+    __syncthreads();
+    fft_lines(A, n, lines, pl, W, MODE == 1);
+    T2 *o = out + (size_t)((ii + first) % ns) * ncell + (size_t)r0 * n;
+    if (MODE == 0) {
+      for (int t = threadIdx.x; t < cnt; t += blockDim.x) o[t] = A[t];
+    } else {
+#pragma unroll 4
+      for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+        T2 v = axpy((R)scale, A[t], mk<T2>(0, 0));
+        if (sb) v = axpy((R)2, sb[t], v);
+        o[t] = v;
+      }
+    }
+    __syncthreads();  // A is free for the copies of the next iteration
+  }
+  cp_wait<0>();
 }
 
 // sin and cos of the propagator's phase: FP64 library sincos for the plain form;
@@ -371,126 +436,224 @@ __device__ __forceinline__ void phase_sincos(float a, float *sn, float *cs) {
   __sincosf(a, sn, cs);
 }
 
-// Column pass over `cols_per_cta` columns of one slice: forward FFT of the columns,
-// the propagator exp(K2 dz) (and the filtered source 2 FFT(src) sigmoid), inverse
-// FFT of the columns. k2t and sigt hold Im(K2) and the sigmoid transposed,
-// k2t[kx n + ky] for the FFT index (ky, kx), so that the reads of a column are
-// contiguous.
+// Transposed load of columns c0 .. c0 + lines - 1 of slice `g` (rows of n) into
+// lines of `dst` (line c = column c0 + c): thread t takes column t mod 16 of rows
+// t / 16, t / 16 + blockDim / 16, ... (lines <= 16)
 template <typename T2>
-__global__ void __launch_bounds__(256, sizeof(T2) == 8 ? 2 : 1)
-    k_fft_cols(T2 *__restrict__ field, const T2 *__restrict__ srcf, const T2 *__restrict__ roots,
-               const typename Real<T2>::T *__restrict__ k2t, const typename Real<T2>::T *__restrict__ sigt,
-               double delz, FFTPlan pl, int ns, int first, int cols_per_cta) {
+__device__ __forceinline__ void load_cols(T2 *dst, const T2 *g, int n, int c0, int lines) {
+  const int tc = threadIdx.x & 15;
+  if (tc < lines)
+    for (int row = threadIdx.x >> 4; row < n; row += blockDim.x >> 4)
+      cp_elem(dst + tc * n + row, g + (size_t)row * n + c0 + tc);
+}
+
+// Column pass over tiles of L (<= 16) columns: forward FFT of the columns, the
+// propagator exp(K2 dz) (and the filtered source 2 FFT(src) sigmoid), inverse FFT
+// of the columns, written back in place. The propagator's phase at the FFT index
+// (ky, kx) is (dx^2 + dy^2) k2dz, k2dz = -dk^2 dz / (2 xks), with dx = ix - (n-1)/2
+// and ix = (kx + n - (n+1)/2) mod n (the reference's shifted frequency map), and
+// likewise dy; sigt holds the sigmoid transposed, sigt[kx n + ky], so that the
+// reads of a column are contiguous; srcf (filtered) holds the row-transformed
+// source of slice ii, staged in a third tile buffer.
+template <typename T2>
+__global__ void __launch_bounds__(256, sizeof(T2) == 8 ? COLS_CTAS_FP32 : COLS_CTAS_FP64)
+    k_fft_cols(T2 *__restrict__ field, const T2 *__restrict__ srcf, const T2 *__restrict__ roots, double k2dz,
+               const typename Real<T2>::T *__restrict__ sigt, FFTPlan pl, int ns, int first, int L) {
   typedef typename Real<T2>::T R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T2 *W = reinterpret_cast<T2 *>(smem_raw);
   const int n = pl.n;
-  T2 *A = W + n;
-  T2 *B = A + cols_per_cta * n;
-  T2 *SA = B + cols_per_cta * n;  // filtered source columns (only with srcf)
-  const int ii = blockIdx.y;
-  const int i = (ii + first) % ns;
+  T2 *Abuf = W + 2 * n;
+  T2 *SA = Abuf + 2 * L * n;  // filtered source columns (only with srcf)
+  const int nblk = (n + L - 1) / L, ntiles = ns * nblk;
   const size_t ncell = (size_t)n * n;
-  const int c0 = blockIdx.x * cols_per_cta;
-  const int lines = min(cols_per_cta, n - c0);
-  T2 *u = field + (size_t)i * ncell;
-  const T2 *sf = srcf ? srcf + (size_t)ii * ncell : nullptr;
-  for (int t = threadIdx.x; t < n; t += blockDim.x) cp_elem(W + t, roots + t);
-  // transposed load: line c holds column c0 + c
-  for (int t = threadIdx.x; t < n * cols_per_cta; t += blockDim.x) {
-    const int row = t / cols_per_cta, c = t - row * cols_per_cta;
-    if (c < lines) cp_elem(A + c * n + row, u + (size_t)row * n + c0 + c);
+  const R kdz = (R)k2dz, half = (R)(0.5 * (n - 1));
+  const int off = n - (n + 1) / 2;
+  // element t of a tile: column t / n, ky = t mod n, advanced by the CTA's stride
+  const int c_init = fdiv(threadIdx.x, n, pl.mn), ky_init = threadIdx.x - c_init * n;
+  const int dc = fdiv(blockDim.x, n, pl.mn), dky = blockDim.x - dc * n;
+  for (int t = threadIdx.x; t < 2 * n - 1; t += blockDim.x) cp_elem(W + t, roots + t);
+  int tile = blockIdx.x;
+  if (tile < ntiles) {
+    const int ii = tile / nblk, c0 = (tile - ii * nblk) * L;
+    load_cols(Abuf, field + (size_t)((ii + first) % ns) * ncell, n, c0, min(L, n - c0));
   }
   cp_commit();
-  if (sf)
-    for (int t = threadIdx.x; t < n * cols_per_cta; t += blockDim.x) {
-      const int row = t / cols_per_cta, c = t - row * cols_per_cta;
-      if (c < lines) cp_elem(SA + c * n + row, sf + (size_t)row * n + c0 + c);
+  for (int it = 0; tile < ntiles; tile += gridDim.x, it++) {
+    T2 *A = Abuf + (it & 1) * L * n;
+    const int ii = tile / nblk, c0 = (tile - ii * nblk) * L, lines = min(L, n - c0);
+    T2 *u = field + (size_t)((ii + first) % ns) * ncell;
+    if (srcf) load_cols(SA, srcf + (size_t)ii * ncell, n, c0, lines);
+    cp_commit();
+    const int nx = tile + gridDim.x;
+    if (nx < ntiles) {
+      const int jj = nx / nblk, q0 = (nx - jj * nblk) * L;
+      load_cols(Abuf + ((it + 1) & 1) * L * n, field + (size_t)((jj + first) % ns) * ncell, n, q0,
+                min(L, n - q0));
     }
-  cp_commit();
-  cp_wait<1>();
-  __syncthreads();
-  fft_lines(A, B, n, lines, pl, W, false);
-  if (sf) {
-    cp_wait<0>();
+    cp_commit();
+    cp_wait<2>();
     __syncthreads();
-    fft_lines(SA, B, n, lines, pl, W, false);
-  }
-  const R dz = (R)delz;
-  const R *kt = k2t + (size_t)c0 * n;
-  const R *st = sigt ? sigt + (size_t)c0 * n : nullptr;
-  for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-    R sn, cs;
-    phase_sincos(kt[t] * dz, &sn, &cs);
-    T2 v = cm(A[t], mk<T2>(cs, sn));
-    if (sf) {
-      R g = (R)2. * st[t];
-      v.x += g * SA[t].x;
-      v.y += g * SA[t].y;
+    // forward transforms of the field's columns and, filtered, of the source's (one
+    // code path for both)
+    for (int job = 0; job < (srcf ? 2 : 1); job++) {
+      if (job == 1) {
+        cp_wait<1>();
+        __syncthreads();
+      }
+      fft_lines_dir<false>(job == 0 ? A : SA, n, lines, pl, W);
     }
-    A[t] = v;
+    const R *st = sigt + (size_t)c0 * n;
+    int c = c_init, ky = ky_init;
+    for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
+      int ix = c0 + c + off, iy = ky + off;
+      ix -= ix >= n ? n : 0;
+      iy -= iy >= n ? n : 0;
+      const R dx = (R)ix - half, dy = (R)iy - half;
+      R sn, cs;
+      phase_sincos((dx * dx + dy * dy) * kdz, &sn, &cs);
+      T2 v = cm(A[t], mk<T2>(cs, sn));
+      if (srcf) v = axpy((R)2 * st[t], SA[t], v);
+      A[t] = v;
+      c += dc;
+      ky += dky;
+      if (ky >= n) {
+        ky -= n;
+        c++;
+      }
+    }
+    __syncthreads();
+    fft_lines_dir<true>(A, n, lines, pl, W);
+    const int tc = threadIdx.x & 15;
+    if (tc < lines)
+      for (int row = threadIdx.x >> 4; row < n; row += blockDim.x >> 4)
+        u[(size_t)row * n + c0 + tc] = A[tc * n + row];
+    __syncthreads();
   }
-  __syncthreads();
-  fft_lines(A, B, n, lines, pl, W, true);
-  for (int t = threadIdx.x; t < n * cols_per_cta; t += blockDim.x) {
-    const int row = t / cols_per_cta, c = t - row * cols_per_cta;
-    if (c < lines) u[(size_t)row * n + c0 + c] = A[c * n + row];
-  }
+  cp_wait<0>();
 }
 
-// lines per CTA so that the column pass (roots + 3 line buffers) fits in 227 KB
-int fft_lines_per_cta(int n, int es) {
-  int lines = 16;
-  while (lines > 1 && (size_t)(n + 3 * lines * n) * es > 227u * 1024u) lines--;
-  return lines;
+constexpr int FFT_THREADS = 256;
+
+// Shared memory of a pass with `bufs` tile buffers of L lines and the roots and
+// twiddles (2 n elements).
+size_t fft_smem(int n, int L, int bufs, size_t es) { return (size_t)(2 * n + bufs * L * n) * es; }
+
+// CTAs of a pass resident on one SM: the register bound of its launch bounds,
+// fewer where the shared memory does not allow them.
+int fft_ctas_per_sm(int regs_bound, size_t smem) {
+  const size_t sm_bytes = 228u * 1024u;
+  int k = regs_bound;
+  while (k > 1 && (size_t)k * (smem + 1024) > sm_bytes) k--;
+  return k;
+}
+
+int sm_count() {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return 152;
+  if (!cached[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cached[dev] = v > 0 ? v : 152;
+  }
+  return cached[dev];
 }
 
 template <typename T2>
-void launch_fft(void *stream, void *field, const void *src, void *work, const void *roots,
-                const void *k2, const void *sig, int filtered, double delz, const FFTPlan &pl,
-                int ns, int first) {
+void launch_fft(void *stream, void *field, const void *src, void *work, const void *roots, double k2c,
+                const void *sig, int filtered, double delz, const FFTPlan &pl, int ns, int first) {
   cudaStream_t s = (cudaStream_t)stream;
   const int n = pl.n;
-  size_t es = sizeof(T2);
-  const int lines = fft_lines_per_cta(n, (int)es);
-  // roots and three line buffers (the third holds the second input)
-  size_t smem_rows = (size_t)(n + 3 * lines * n) * es;
-  size_t smem_cols = (size_t)(n + 3 * lines * n) * es;
+  const int es = (int)sizeof(T2);
   static unsigned long long configured = 0;
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 64 && !(configured & (1ull << dev))) {
-    cudaFuncSetAttribute(k_fft_rows<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_fft_rows<T2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_fft_rows<T2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_fft_cols<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     configured |= 1ull << dev;
   }
-  dim3 grid((n + lines - 1) / lines, ns);
+  const int nsm = sm_count();
+  const int rows_ctas = es == 8 ? ROWS_CTAS_FP32 : ROWS_CTAS_FP64;
+  const int cols_ctas = es == 8 ? COLS_CTAS_FP32 : COLS_CTAS_FP64;
+  auto grid = [&](int L, size_t smem, int regs_bound) {
+    const long long tiles = (long long)ns * ((n + L - 1) / L);
+    const long long cap = (long long)nsm * fft_ctas_per_sm(regs_bound, smem);
+    return (unsigned)(tiles < cap ? tiles : cap);
+  };
   T2 *f = (T2 *)field;
   const T2 *sr = (const T2 *)src;
   T2 *sfw = filtered ? (T2 *)work : nullptr;
-  k_fft_rows<T2><<<grid, 256, smem_rows, s>>>(f, sr, sfw, (const T2 *)roots, pl, ns, first, 0, 1.0, lines);
+  const T2 *rt = (const T2 *)roots;
   typedef typename Real<T2>::T R;
-  k_fft_cols<T2><<<grid, 256, smem_cols, s>>>(f, sfw, (const T2 *)roots, (const R *)k2, (const R *)sig,
-                                             delz, pl, ns, first, lines);
-  k_fft_rows<T2><<<grid, 256, smem_rows, s>>>(f, filtered ? nullptr : sr, nullptr, (const T2 *)roots, pl,
-                                             ns, first, 1, 1.0 / ((double)n * n), lines);
+  // forward rows of the field (and, filtered, of the source into the work array)
+  const int Lr = fft_lines_per_cta(pl, es, 2, 32, rows_ctas);
+  const size_t mr = fft_smem(n, Lr, 2, (size_t)es);
+  const unsigned gr = grid(Lr, mr, rows_ctas);
+  k_fft_rows<T2, 0><<<gr, FFT_THREADS, mr, s>>>(f, f, nullptr, rt, pl, ns, first, 1.0, Lr);
+  if (sfw) k_fft_rows<T2, 0><<<gr, FFT_THREADS, mr, s>>>(sr, sfw, nullptr, rt, pl, ns, 0, 1.0, Lr);
+  // columns
+  const int bc = sfw ? 3 : 2;
+  const int Lc = fft_lines_per_cta(pl, es, bc, 16, cols_ctas);
+  const size_t mc = fft_smem(n, Lc, bc, (size_t)es);
+  k_fft_cols<T2><<<grid(Lc, mc, cols_ctas), FFT_THREADS, mc, s>>>(f, sfw, rt, k2c * delz, (const R *)sig, pl,
+                                                                 ns, first, Lc);
+  // inverse rows, 1/n^2, + 2 src when unfiltered
+  k_fft_rows<T2, 1><<<gr, FFT_THREADS, mr, s>>>(f, f, filtered ? nullptr : sr, rt, pl, ns, first,
+                                                1.0 / ((double)n * n), Lr);
 }
 
 }  // namespace
 
-int fft_max_ngrid(int mixed) {
-  // one line per CTA at least: roots + 3 lines of ngrid complex values
-  int es = mixed ? (int)sizeof(float2) : (int)sizeof(double2);
-  return (int)(227u * 1024u / (4u * (unsigned)es));
+// Lines per CTA of a pass with `bufs` tile buffers: the largest L <= maxL such that
+// every register stage has a butterfly per thread for all L lines (L n / R <= T),
+// the generic stages at most 8 outputs per thread (L n <= 8 T), and the shared
+// memory of `per_sm` CTAs fits an SM (or one CTA's, in 227 KB, where not even
+// L = 1 fits that).
+int fft_lines_per_cta(const FFTPlan &pl, int es, int bufs, int maxL, int per_sm) {
+  const int n = pl.n;
+  int L = maxL;
+  for (int s = 0; s < pl.nstage; s++) {
+    const int r = pl.radix[s];
+    const int lim = register_radix(r) ? FFT_THREADS / (n / r) : STAGE_ANY_OUT * FFT_THREADS / n;
+    if (lim < L) L = lim;
+  }
+  if (L < 1) L = 1;
+  (void)es;
+  const size_t cap = 228u * 1024u / per_sm - 1024;
+  while (L > 1 && fft_smem(n, L, bufs, es) > cap) L--;
+  return L;
 }
 
-void launch_fft_solve(void *stream, int mixed, void *field, const void *src, void *work,
-                      const void *roots, const void *k2, const void *sig, int filtered, double delz,
-                      const FFTPlan &pl, int ns, int first) {
+int fft_max_ngrid(int mixed) {
+  // a register stage of one line with n / R <= 256 butterflies, the generic stages
+  // of one line with at most 8 outputs per thread (n <= 2048), and one line in
+  // each of three tile buffers plus the roots and twiddles in 227 KB
+  int es = mixed ? (int)sizeof(float2) : (int)sizeof(double2);
+  int m = (int)(227u * 1024u / (5u * (unsigned)es));
+  return m < STAGE_ANY_OUT * FFT_THREADS ? m : STAGE_ANY_OUT * FFT_THREADS;
+}
+
+// Whether every stage of the plan can take its lines (n / R butterflies of a
+// register stage per thread, n outputs of a generic stage at most 8 per thread).
+int fft_plan_fits(const FFTPlan &pl) {
+  for (int s = 0; s < pl.nstage; s++) {
+    const int r = pl.radix[s];
+    if (register_radix(r) ? pl.n / r > FFT_THREADS : pl.n > STAGE_ANY_OUT * FFT_THREADS) return 0;
+  }
+  return 1;
+}
+
+void launch_fft_solve(void *stream, int mixed, void *field, const void *src, void *work, const void *roots,
+                      double k2c, const void *sig, int filtered, double delz, const FFTPlan &pl, int ns,
+                      int first) {
   if (mixed)
-    launch_fft<float2>(stream, field, src, work, roots, k2, sig, filtered, delz, pl, ns, first);
+    launch_fft<float2>(stream, field, src, work, roots, k2c, sig, filtered, delz, pl, ns, first);
   else
-    launch_fft<double2>(stream, field, src, work, roots, k2, sig, filtered, delz, pl, ns, first);
+    launch_fft<double2>(stream, field, src, work, roots, k2c, sig, filtered, delz, pl, ns, first);
 }
 
 }  // namespace g4
