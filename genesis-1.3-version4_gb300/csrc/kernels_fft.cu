@@ -47,15 +47,12 @@ __device__ __forceinline__ T2 mk(typename Real<T2>::T x, typename Real<T2>::T y)
 }
 
 // Complex arithmetic: add, sub; axpy(c, a, y) = y + c a (c real); cm(a, w) = a w;
-// cmc(a, w) = a conj(w); addi(a, b) = a + i b; subi(a, b) = a - i b.
+// addi(a, b) = a + i b; subi(a, b) = a - i b.
 __device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 __device__ __forceinline__ float2 axpy(float c, float2 a, float2 y) { return __ffma2_rn(make_float2(c, c), a, y); }
 __device__ __forceinline__ float2 cm(float2 a, float2 w) {
   return __ffma2_rn(make_float2(-a.y, a.y), make_float2(w.y, w.x), __fmul2_rn(make_float2(a.x, a.x), w));
-}
-__device__ __forceinline__ float2 cmc(float2 a, float2 w) {
-  return __ffma2_rn(make_float2(a.y, -a.x), make_float2(w.y, w.y), __fmul2_rn(a, make_float2(w.x, w.x)));
 }
 __device__ __forceinline__ float2 addi(float2 a, float2 b) {
   return __ffma2_rn(make_float2(b.y, b.x), make_float2(-1.f, 1.f), a);
@@ -71,9 +68,6 @@ __device__ __forceinline__ double2 axpy(double c, double2 a, double2 y) {
 }
 __device__ __forceinline__ double2 cm(double2 a, double2 w) {
   return make_double2(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
-}
-__device__ __forceinline__ double2 cmc(double2 a, double2 w) {
-  return make_double2(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y);
 }
 __device__ __forceinline__ double2 addi(double2 a, double2 b) { return make_double2(a.x - b.y, a.y + b.x); }
 __device__ __forceinline__ double2 subi(double2 a, double2 b) { return make_double2(a.x + b.y, a.y - b.x); }
@@ -108,22 +102,24 @@ __host__ __device__ constexpr Root root_of(int m, int R) {
     default: return Root{sn, -cs};
   }
 }
-// the roots w^m = exp(-+2 pi i m / R) of a transform's direction
-template <int R, bool INV>
+// the forward roots w^m = exp(-2 pi i m / R)
+template <int R>
 struct Roots {
   double c[R], s[R];
   __host__ __device__ constexpr Roots() : c(), s() {
     for (int m = 0; m < R; m++) {
       const Root r = root_of(m, R);
       c[m] = r.c;
-      s[m] = INV ? r.s : -r.s;
+      s[m] = -r.s;
     }
   }
 };
 
 // R-point DFT y_t = sum_q x_q w^{q t} of x[0..R), w = exp(-2 pi i / R) forward and
-// exp(+2 pi i / R) inverse (the roots are compile-time constants). OUT: y_t is
-// written to dst[t ds] as it is formed; otherwise y replaces x.
+// exp(+2 pi i / R) inverse (sgn = +1 forward, -1 inverse: the sine of every root
+// is scaled by sgn; the roots themselves are compile-time constants). OUT 0: y
+// replaces x; 1: y_t is written to dst[t ds] as it is formed; 2: likewise through
+// the epilogue (scale, + 2 src at the same offset).
 // Odd prime R: with a_m = x_m + x_{R-m} and b_m = x_m - x_{R-m},
 //   y_t = A_t + i B_t,  y_{R-t} = A_t - i B_t,
 //   A_t = x_0 + sum_m a_m Re(w^{m t}),  B_t = sum_m b_m Im(w^{m t}),
@@ -131,30 +127,63 @@ struct Roots {
 // Composite R = P M: the M-point DFTs of the P interleaved subsequences x[P i + s],
 // the twiddles w^{s k}, and P-point DFTs across them (decimation in time):
 //   y_{k + t M} = sum_s w^{s k} w_P^{s t} DFT_M(x_s)_k.
-#define G4_PUT(t, v)          \
-  do {                        \
-    if constexpr (OUT)        \
-      dst[(t) * ds] = (v);    \
-    else                      \
-      x[t] = (v);             \
+#define G4_PUT(t, v)                       \
+  do {                                     \
+    if constexpr (OUT == 0)                \
+      x[t] = (v);                          \
+    else if constexpr (OUT == 1)           \
+      dst[(t) * ds] = (v);                 \
+    else                                   \
+      epi.put(dst + (t) * ds, (t) * ds, (v)); \
   } while (0)
-template <int R, bool INV, bool OUT, typename T2>
-__device__ __forceinline__ void dft(T2 *x, T2 *dst, int ds) {
+// Asynchronous copy of one complex element from global to shared memory
+// (cp.async: 8 bytes for float2, 16 for double2; both addresses are aligned to the
+// element's size), so that a CTA has all its loads in flight at once.
+template <typename T2>
+__device__ __forceinline__ void cp_elem(T2 *dst, const T2 *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if constexpr (sizeof(T2) == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// waits until at most N of this thread's committed groups are pending
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// What the last stage of a row pass writes to global memory: scale y (+ 2 src).
+template <typename T2>
+struct Epilogue {
+  typename Real<T2>::T scale;
+  const T2 *src;  // the source at the same place as the output, or null
+  __device__ __forceinline__ void put(T2 *g, int off, T2 v) const {
+    v = axpy(scale, v, mk<T2>(0, 0));
+    if (src) v = axpy((typename Real<T2>::T)2, src[off], v);
+    *g = v;
+  }
+};
+template <int R, int OUT, typename T2>
+__device__ __forceinline__ void dft(T2 *x, T2 *dst, int ds, typename Real<T2>::T sgn,
+                                    const Epilogue<T2> &epi = Epilogue<T2>{}) {
   typedef typename Real<T2>::T Rt;
-  constexpr Roots<R, INV> w{};
+  constexpr Roots<R> w{};
   if constexpr (R == 1) {
-    if (OUT) dst[0] = x[0];
+    G4_PUT(0, x[0]);
   } else if constexpr (R == 2) {
     const T2 a = x[0], b = x[1];
     G4_PUT(0, add(a, b));
     G4_PUT(1, sub(a, b));
   } else if constexpr (R == 4) {
-    // w = -i forward, +i inverse: exact
-    const T2 t0 = add(x[0], x[2]), t1 = sub(x[0], x[2]), t2 = add(x[1], x[3]), t3 = sub(x[1], x[3]);
+    // w = -i sgn: exact
+    const T2 t0 = add(x[0], x[2]), t1 = sub(x[0], x[2]), t2 = add(x[1], x[3]);
+    const T2 t3 = axpy(sgn, sub(x[1], x[3]), mk<T2>(0, 0));
     G4_PUT(0, add(t0, t2));
     G4_PUT(2, sub(t0, t2));
-    G4_PUT(1, INV ? addi(t1, t3) : subi(t1, t3));
-    G4_PUT(3, INV ? subi(t1, t3) : addi(t1, t3));
+    G4_PUT(1, subi(t1, t3));
+    G4_PUT(3, addi(t1, t3));
   } else if constexpr (small_factor(R) != R) {
     constexpr int P = small_factor(R), M = R / P;
     T2 part[P][M];
@@ -163,19 +192,21 @@ __device__ __forceinline__ void dft(T2 *x, T2 *dst, int ds) {
 #pragma unroll
       for (int i = 0; i < M; i++) part[s][i] = x[P * i + s];
 #pragma unroll
-    for (int s = 0; s < P; s++) dft<M, INV, false>(part[s], (T2 *)nullptr, 0);
+    for (int s = 0; s < P; s++) dft<M, 0>(part[s], (T2 *)nullptr, 0, sgn);
 #pragma unroll
     for (int k = 0; k < M; k++) {
       T2 y[P];
 #pragma unroll
       for (int s = 0; s < P; s++)
-        y[s] = (s == 0 || k == 0) ? part[s][k] : cm(part[s][k], mk<T2>((Rt)w.c[s * k], (Rt)w.s[s * k]));
-      if (OUT) {
-        dft<P, INV, true>(y, dst + k * ds, M * ds);
-      } else {
-        dft<P, INV, false>(y, (T2 *)nullptr, 0);
+        y[s] = (s == 0 || k == 0) ? part[s][k] : cm(part[s][k], mk<T2>((Rt)w.c[s * k], sgn * (Rt)w.s[s * k]));
+      if constexpr (OUT == 0) {
+        dft<P, 0>(y, (T2 *)nullptr, 0, sgn);
 #pragma unroll
         for (int t = 0; t < P; t++) x[k + t * M] = y[t];
+      } else {
+        Epilogue<T2> e2 = epi;
+        if (OUT == 2 && e2.src) e2.src += k * ds;
+        dft<P, OUT>(y, dst + k * ds, M * ds, sgn, e2);
       }
     }
   } else {
@@ -186,7 +217,7 @@ __device__ __forceinline__ void dft(T2 *x, T2 *dst, int ds) {
 #pragma unroll
     for (int m = 1; m <= H; m++) {
       a[m] = add(x[m], x[R - m]);
-      b[m] = sub(x[m], x[R - m]);
+      b[m] = axpy(sgn, sub(x[m], x[R - m]), mk<T2>(0, 0));
       y0 = add(y0, a[m]);
     }
     G4_PUT(0, y0);
@@ -204,7 +235,6 @@ __device__ __forceinline__ void dft(T2 *x, T2 *dst, int ds) {
     }
   }
 }
-
 #undef G4_PUT
 
 // x / d for x d < 2^32 with m = ceil(2^32 / d) (exact there); d = 1 passes x through
@@ -224,15 +254,16 @@ __device__ __forceinline__ int fdiv(int x, int d, unsigned m) {
 // butterfly lives in one register array of the largest radix for every stage, so
 // that the stages' code paths share the registers held across the barrier.
 constexpr int MAX_RADIX = 17;
-template <int R, bool INV, typename T2>
-__device__ __forceinline__ void stage_load(T2 *x, const T2 *src, int nb, int ns, int k, const T2 *tw) {
+template <int R, typename T2>
+__device__ __forceinline__ void stage_load(T2 *x, const T2 *src, int nb, int ns, int k, const T2 *tw,
+                                           typename Real<T2>::T sgn) {
 #pragma unroll
   for (int q = 0; q < R; q++) x[q] = src[q * nb];
   if (ns > 1) {
 #pragma unroll
     for (int q = 1; q < R; q++) {
       const T2 w = tw[(q - 1) * ns + k];
-      x[q] = INV ? cmc(x[q], w) : cm(x[q], w);
+      x[q] = cm(x[q], mk<T2>(w.x, sgn * w.y));
     }
   }
 }
@@ -269,13 +300,17 @@ __device__ __forceinline__ void any_load(T2 *acc, const T2 *A, int ls, int lines
   }
 }
 template <typename T2>
-__device__ __forceinline__ void any_store(const T2 *acc, T2 *A, int ls, int lines, int n) {
+__device__ __forceinline__ void any_store(const T2 *acc, T2 *A, int ls, int lines, int n, T2 *gout,
+                                          const Epilogue<T2> &epi) {
 #pragma unroll
   for (int u = 0; u < STAGE_ANY_OUT; u++) {
     const int t = threadIdx.x + u * blockDim.x;
     if (t < lines * n) {
-      const int line = t / n;
-      A[line * ls + (t - line * n)] = acc[u];
+      const int line = t / n, pos = line * ls + (t - line * n);
+      if (gout)
+        epi.put(gout + pos, pos, acc[u]);
+      else
+        A[pos] = acc[u];
     }
   }
 }
@@ -287,13 +322,20 @@ __host__ __device__ constexpr bool register_radix(int r) {
 }
 
 // One 1-D Stockham FFT of length n, in place over `lines` lines of A stored with
-// line stride `ls`, the stages of the plan's radices in turn. W: the n roots
-// exp(-2 pi i m / n), followed by the stage twiddle table (stage s's at
-// W + n + plan.tw_off[s]).
-template <bool INV, typename T2>
-__device__ __forceinline__ void fft_lines_dir(T2 *A, int ls, int lines, const FFTPlan &pl, const T2 *W) {
+// line stride `ls`, the stages of the plan's radices in turn, forward or inverse
+// (the direction is a run-time argument, so that a kernel with several transforms
+// holds one copy of the code). W: the n roots exp(-2 pi i m / n), followed by the
+// stage twiddle table (stage s's at W + n + plan.tw_off[s]).
+template <typename T2>
+__device__ __forceinline__ void fft_lines(T2 *A, int ls, int lines, const FFTPlan &pl, const T2 *W, bool inverse,
+                                          T2 *gout = nullptr, const Epilogue<T2> &epi = Epilogue<T2>{},
+                                          bool wait_epi_copy = false) {
+  typedef typename Real<T2>::T Rt;
+  const Rt sgn = inverse ? (Rt)-1 : (Rt)1;
   int ns = 1;
   for (int s = 0; s < pl.nstage; s++) {
+    // the last stage of a pass with a global output writes it there (line stride ls)
+    const bool to_global = gout && s == pl.nstage - 1;
     const int r = pl.radix[s], nb = pl.nb[s];
     const T2 *tw = W + pl.n + pl.tw_off[s];
     const bool act = (int)threadIdx.x < lines * nb;
@@ -305,65 +347,44 @@ __device__ __forceinline__ void fft_lines_dir(T2 *A, int ls, int lines, const FF
     switch (r) {
 #define G4_LOAD(R) \
   case R:          \
-    if (act) stage_load<R, INV>(x, src, nb, ns, k, tw); \
+    if (act) stage_load<R>(x, src, nb, ns, k, tw, sgn); \
     break;
       G4_LOAD(2) G4_LOAD(3) G4_LOAD(4) G4_LOAD(5) G4_LOAD(7) G4_LOAD(8) G4_LOAD(9) G4_LOAD(11) G4_LOAD(13)
       G4_LOAD(15) G4_LOAD(16) G4_LOAD(17)
 #undef G4_LOAD
-      default: any_load(x, A, ls, lines, pl.n, ns, r, W, INV); break;
+      default: any_load(x, A, ls, lines, pl.n, ns, r, W, inverse); break;
     }
+    // the epilogue's source, copied asynchronously by the caller, must have landed
+    // before the barrier ahead of the last stage's stores (all but the most recent
+    // copy group of this thread)
+    if (to_global && wait_epi_copy) cp_wait<1>();
     __syncthreads();
+    const int o = line * ls + (j - k) * r + k;
+    Epilogue<T2> e = epi;
+    if (e.src) e.src += o;
     switch (r) {
-#define G4_STORE(R) \
-  case R:           \
-    if (act) dft<R, INV, true>(x, dst, ns); \
+#define G4_STORE(R)                                      \
+  case R:                                                \
+    if (act) {                                           \
+      if (to_global)                                     \
+        dft<R, 2>(x, gout + o, ns, sgn, e);              \
+      else                                               \
+        dft<R, 1>(x, dst, ns, sgn);                      \
+    }                                                    \
     break;
       G4_STORE(2) G4_STORE(3) G4_STORE(4) G4_STORE(5) G4_STORE(7) G4_STORE(8) G4_STORE(9) G4_STORE(11)
       G4_STORE(13) G4_STORE(15) G4_STORE(16) G4_STORE(17)
 #undef G4_STORE
-      default: any_store(x, A, ls, lines, pl.n); break;
+      default: any_store(x, A, ls, lines, pl.n, to_global ? gout : (T2 *)nullptr, epi); break;
     }
-    __syncthreads();
+    if (!to_global) __syncthreads();
     ns *= r;
   }
 }
-template <typename T2>
-__device__ __forceinline__ void fft_lines(T2 *A, int ls, int lines, const FFTPlan &pl, const T2 *W, bool inverse) {
-  if (inverse)
-    fft_lines_dir<true>(A, ls, lines, pl, W);
-  else
-    fft_lines_dir<false>(A, ls, lines, pl, W);
-}
-
-// Asynchronous copy of one complex element from global to shared memory
-// (cp.async: 8 bytes for float2, 16 for double2; both addresses are aligned to the
-// element's size), so that a CTA has all its loads in flight at once.
-template <typename T2>
-__device__ __forceinline__ void cp_elem(T2 *dst, const T2 *src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  if constexpr (sizeof(T2) == 16)
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-// waits until at most N of this thread's committed groups are pending
-template <int N>
-__device__ __forceinline__ void cp_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-// Bulk prefetch of [p, p + bytes) into L2 (the 16-byte-aligned part of it).
-__device__ __forceinline__ void prefetch_l2(const void *p, size_t bytes) {
-  const unsigned long long a = ((unsigned long long)p + 15) & ~15ull;
-  const unsigned long long e = ((unsigned long long)p + bytes) & ~15ull;
-  if (e > a) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(a), "r"((unsigned)(e - a)) : "memory");
-}
 
 // CTAs per SM the passes' launch bounds provide for (the register budget of a
-// thread is 64K / (256 x CTAs)): the row pass holds one butterfly across a barrier,
-// the column pass two transforms, the propagator and the transposed copies.
-constexpr int ROWS_CTAS_FP32 = 3, ROWS_CTAS_FP64 = 2, COLS_CTAS_FP32 = 2, COLS_CTAS_FP64 = 1;
+// thread is 64K / (256 x CTAs): 80 registers in FP32, 128 in FP64).
+constexpr int FFT_CTAS_FP32 = 3, FFT_CTAS_FP64 = 2;
 
 // Both passes are persistent: tile = ii nblk + blk runs over the window's slices ii
 // and each slice's blocks of L lines; CTA b takes tiles b, b + gridDim.x, ... and
@@ -373,16 +394,18 @@ constexpr int ROWS_CTAS_FP32 = 3, ROWS_CTAS_FP64 = 2, COLS_CTAS_FP32 = 2, COLS_C
 // Row pass over tiles of L rows. MODE 0: forward FFT of the rows of `in` into `out`
 // (the same place of slice (ii + first) mod ns of each); MODE 1: inverse FFT of
 // the rows of `in`, times `scale`, plus 2 src (slice ii) when src is given, into
-// `out`. in == out transforms in place.
+// `out`, with the source rows in a third tile buffer and one CTA per SM fewer.
+// in == out transforms in place.
 template <typename T2, int MODE>
-__global__ void __launch_bounds__(256, sizeof(T2) == 8 ? ROWS_CTAS_FP32 : ROWS_CTAS_FP64)
+__global__ void __launch_bounds__(256, (sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTAS_FP64) - MODE)
     k_fft_rows(const T2 *in, T2 *out, const T2 *__restrict__ src, const T2 *__restrict__ roots, FFTPlan pl,
                int ns, int first, double scale, int L) {
   typedef typename Real<T2>::T R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T2 *W = reinterpret_cast<T2 *>(smem_raw);
   const int n = pl.n;
-  T2 *Abuf = W + 2 * n;  // two tile buffers
+  T2 *Abuf = W + 2 * n;      // two tile buffers
+  T2 *S = Abuf + 2 * L * n;  // MODE 1: the tile's source rows
   const int nblk = (n + L - 1) / L, ntiles = ns * nblk;
   const size_t ncell = (size_t)n * n;
   for (int t = threadIdx.x; t < 2 * n - 1; t += blockDim.x) cp_elem(W + t, roots + t);
@@ -397,8 +420,10 @@ __global__ void __launch_bounds__(256, sizeof(T2) == 8 ? ROWS_CTAS_FP32 : ROWS_C
     T2 *A = Abuf + (it & 1) * L * n;
     const int ii = tile / nblk, r0 = (tile - ii * nblk) * L, lines = min(L, n - r0), cnt = lines * n;
     const T2 *sb = (MODE == 1 && src) ? src + (size_t)ii * ncell + (size_t)r0 * n : nullptr;
-    // the source rows of the epilogue: into L2 while the rows are transformed
-    if (sb && threadIdx.x == 0) prefetch_l2(sb, (size_t)cnt * sizeof(T2));
+    // the source rows of the epilogue: copied while the rows are transformed
+    if (sb)
+      for (int t = threadIdx.x; t < cnt; t += blockDim.x) cp_elem(S + t, sb + t);
+    cp_commit();
     const int nx = tile + gridDim.x;
     if (nx < ntiles) {
       const int jj = nx / nblk, q0 = (nx - jj * nblk) * L, qc = min(L, n - q0) * n;
@@ -407,20 +432,11 @@ __global__ void __launch_bounds__(256, sizeof(T2) == 8 ? ROWS_CTAS_FP32 : ROWS_C
       for (int t = threadIdx.x; t < qc; t += blockDim.x) cp_elem(dst + t, g + t);
     }
     cp_commit();
-    cp_wait<1>();  // this tile's rows (committed one iteration earlier)
+    cp_wait<2>();  // this tile's rows (committed one iteration earlier)
     __syncthreads();
-    fft_lines(A, n, lines, pl, W, MODE == 1);
+    // the last stage writes the rows to global memory, scaled and with 2 src (MODE 1)
     T2 *o = out + (size_t)((ii + first) % ns) * ncell + (size_t)r0 * n;
-    if (MODE == 0) {
-      for (int t = threadIdx.x; t < cnt; t += blockDim.x) o[t] = A[t];
-    } else {
-#pragma unroll 4
-      for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-        T2 v = axpy((R)scale, A[t], mk<T2>(0, 0));
-        if (sb) v = axpy((R)2, sb[t], v);
-        o[t] = v;
-      }
-    }
+    fft_lines(A, n, lines, pl, W, MODE == 1, o, Epilogue<T2>{(R)scale, sb ? S : nullptr}, sb != nullptr);
     __syncthreads();  // A is free for the copies of the next iteration
   }
   cp_wait<0>();
@@ -456,7 +472,7 @@ __device__ __forceinline__ void load_cols(T2 *dst, const T2 *g, int n, int c0, i
 // reads of a column are contiguous; srcf (filtered) holds the row-transformed
 // source of slice ii, staged in a third tile buffer.
 template <typename T2>
-__global__ void __launch_bounds__(256, sizeof(T2) == 8 ? COLS_CTAS_FP32 : COLS_CTAS_FP64)
+__global__ void __launch_bounds__(256, sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTAS_FP64)
     k_fft_cols(T2 *__restrict__ field, const T2 *__restrict__ srcf, const T2 *__restrict__ roots, double k2dz,
                const typename Real<T2>::T *__restrict__ sigt, FFTPlan pl, int ns, int first, int L) {
   typedef typename Real<T2>::T R;
@@ -494,36 +510,40 @@ __global__ void __launch_bounds__(256, sizeof(T2) == 8 ? COLS_CTAS_FP32 : COLS_C
     cp_commit();
     cp_wait<2>();
     __syncthreads();
-    // forward transforms of the field's columns and, filtered, of the source's (one
-    // code path for both)
-    for (int job = 0; job < (srcf ? 2 : 1); job++) {
-      if (job == 1) {
+    // the transforms in one loop, so that the kernel holds one copy of their code:
+    // forward on the field's columns, (filtered) forward on the source's, then the
+    // propagator and the inverse on the field's
+    const int njob = srcf ? 3 : 2;
+    for (int job = 0; job < njob; job++) {
+      const bool inverse = job == njob - 1;
+      if (job == 1 && srcf) {
         cp_wait<1>();
         __syncthreads();
       }
-      fft_lines_dir<false>(job == 0 ? A : SA, n, lines, pl, W);
-    }
-    const R *st = sigt + (size_t)c0 * n;
-    int c = c_init, ky = ky_init;
-    for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-      int ix = c0 + c + off, iy = ky + off;
-      ix -= ix >= n ? n : 0;
-      iy -= iy >= n ? n : 0;
-      const R dx = (R)ix - half, dy = (R)iy - half;
-      R sn, cs;
-      phase_sincos((dx * dx + dy * dy) * kdz, &sn, &cs);
-      T2 v = cm(A[t], mk<T2>(cs, sn));
-      if (srcf) v = axpy((R)2 * st[t], SA[t], v);
-      A[t] = v;
-      c += dc;
-      ky += dky;
-      if (ky >= n) {
-        ky -= n;
-        c++;
+      if (inverse) {
+        const R *st = sigt + (size_t)c0 * n;
+        int c = c_init, ky = ky_init;
+        for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
+          int ix = c0 + c + off, iy = ky + off;
+          ix -= ix >= n ? n : 0;
+          iy -= iy >= n ? n : 0;
+          const R dx = (R)ix - half, dy = (R)iy - half;
+          R sn, cs;
+          phase_sincos((dx * dx + dy * dy) * kdz, &sn, &cs);
+          T2 v = cm(A[t], mk<T2>(cs, sn));
+          if (srcf) v = axpy((R)2 * st[t], SA[t], v);
+          A[t] = v;
+          c += dc;
+          ky += dky;
+          if (ky >= n) {
+            ky -= n;
+            c++;
+          }
+        }
+        __syncthreads();
       }
+      fft_lines(job == 1 && srcf ? SA : A, n, lines, pl, W, inverse);
     }
-    __syncthreads();
-    fft_lines_dir<true>(A, n, lines, pl, W);
     const int tc = threadIdx.x & 15;
     if (tc < lines)
       for (int row = threadIdx.x >> 4; row < n; row += blockDim.x >> 4)
@@ -577,8 +597,7 @@ void launch_fft(void *stream, void *field, const void *src, void *work, const vo
     configured |= 1ull << dev;
   }
   const int nsm = sm_count();
-  const int rows_ctas = es == 8 ? ROWS_CTAS_FP32 : ROWS_CTAS_FP64;
-  const int cols_ctas = es == 8 ? COLS_CTAS_FP32 : COLS_CTAS_FP64;
+  const int rows_ctas = es == 8 ? FFT_CTAS_FP32 : FFT_CTAS_FP64, cols_ctas = rows_ctas;
   auto grid = [&](int L, size_t smem, int regs_bound) {
     const long long tiles = (long long)ns * ((n + L - 1) / L);
     const long long cap = (long long)nsm * fft_ctas_per_sm(regs_bound, smem);
@@ -601,9 +620,14 @@ void launch_fft(void *stream, void *field, const void *src, void *work, const vo
   const size_t mc = fft_smem(n, Lc, bc, (size_t)es);
   k_fft_cols<T2><<<grid(Lc, mc, cols_ctas), FFT_THREADS, mc, s>>>(f, sfw, rt, k2c * delz, (const R *)sig, pl,
                                                                  ns, first, Lc);
-  // inverse rows, 1/n^2, + 2 src when unfiltered
-  k_fft_rows<T2, 1><<<gr, FFT_THREADS, mr, s>>>(f, f, filtered ? nullptr : sr, rt, pl, ns, first,
-                                                1.0 / ((double)n * n), Lr);
+  // inverse rows, 1/n^2, + 2 src when unfiltered (the source rows in a third tile
+  // buffer, at one CTA per SM fewer)
+  const T2 *s1 = filtered ? nullptr : sr;
+  const int c1 = rows_ctas - 1;
+  const int L1 = fft_lines_per_cta(pl, es, s1 ? 3 : 2, 32, c1);
+  const size_t m1 = fft_smem(n, L1, s1 ? 3 : 2, (size_t)es);
+  k_fft_rows<T2, 1><<<grid(L1, m1, c1), FFT_THREADS, m1, s>>>(f, f, s1, rt, pl, ns, first, 1.0 / ((double)n * n),
+                                                              L1);
 }
 
 }  // namespace
