@@ -374,7 +374,7 @@ def batched_form(g4gpu, torch, steps, warmup, peak, nrun=ENSEMBLE_RUNS, nerr=4):
 HARM_NS, HARM_NPART, HARM_NGRID, HARM_GRIDMAX, HARM_H = 2048, 16384, 255, 1.5e-4, (1, 3, 5)
 
 
-def harmonic_fft_form(g4gpu, torch, steps, warmup, peak, nsub=256):
+def harmonic_fft_form(g4gpu, torch, steps, warmup, peak, nsub=256, ns=None):
     """The harmonic FFT workload, mixed form: 2048 slices x 16384 particles (nbins 8,
     shot noise seed 7, delgam 1.0, the flat-top current), fields at the 1st, 3rd and
     5th harmonic on ngrid 255 over gridmax 1.5e-4 m, FieldSolverFFT, the undulator of
@@ -383,7 +383,8 @@ def harmonic_fft_form(g4gpu, torch, steps, warmup, peak, nsub=256):
     head and zero entering at slice 0, the first slices of a window evolve exactly as
     a window of those slices alone)."""
     dev = torch.cuda.current_device()
-    ns, npart, ng = HARM_NS, HARM_NPART, HARM_NGRID
+    ns, npart, ng = ns or HARM_NS, HARM_NPART, HARM_NGRID
+    nsub = min(nsub, ns)
     ncell = ng * ng
     lat, _, _ = workload_inputs(ns)
     cur = flat_top(ns)
@@ -674,6 +675,8 @@ def main():
                     help="slices of the window (default 4096); smaller values are for profiling only")
     ap.add_argument("--forms", default="mixed,plain,batched,harmonic,learned",
                     help="forms to time besides the mixed headline: plain, batched, harmonic, learned")
+    ap.add_argument("--harmonic-slices", type=int, default=None,
+                    help="slices of the harmonic FFT window (default 2048); smaller values are for profiling only")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default launch shapes of the mixed form instead of autotuning them")
     ap.add_argument("--launch-shapes", default=None,
@@ -786,7 +789,8 @@ def main():
     if "batched" in args.forms:
         line["forms"]["batched"] = batched_form(g4gpu, torch, args.steps, args.warmup, peak)
     if "harmonic" in args.forms:
-        line["forms"]["harmonic_fft"] = harmonic_fft_form(g4gpu, torch, args.steps, args.warmup, peak)
+        line["forms"]["harmonic_fft"] = harmonic_fft_form(g4gpu, torch, args.steps, args.warmup, peak,
+                                                          ns=args.harmonic_slices)
     if "learned" in args.forms:
         line["forms"]["learned"] = learned_form(g4gpu, torch, lat, beam, cur, args.steps, args.warmup)
         # the same closure in steady state (config 0: quiet loading, 1 kW seed, no
