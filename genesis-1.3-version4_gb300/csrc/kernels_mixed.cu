@@ -196,32 +196,66 @@ struct PtrsF {
   float2 *src[G4GPU_MAX_FIELDS];
 };
 
+// Deposition into the global source grids (FieldSolverADI.cpp:11-52) by a whole
+// warp. The particles of a beamlet (nbins consecutive particles of the quiet
+// loading) keep bit-identical x and y in FP32 for many steps, so they share the
+// cell and the bilinear weights: aligned groups of 2, 4 or 8 lanes with identical
+// positions first sum their complex amplitudes by shuffles, and one lane of the
+// group adds weight x sum to the four cells. Every shuffle is executed by all 32
+// lanes before any predicate uses its result; lanes without a particle (`valid`
+// false) take part in the shuffles and contribute nothing.
 template <int NF>
 __device__ __forceinline__ void deposit_f(const StepConstF &sc, const PtrsF &p, size_t off, int ng,
-                                          float cur, float g, long long th, float x, float y) {
+                                          float cur, float g, long long th, float x, float y, bool valid) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const float x1 = __shfl_xor_sync(full, x, 1), y1 = __shfl_xor_sync(full, y, 1);
+  const float x2 = __shfl_xor_sync(full, x, 2), y2 = __shfl_xor_sync(full, y, 2);
+  const float x4 = __shfl_xor_sync(full, x, 4), y4 = __shfl_xor_sync(full, y, 4);
+  const int v1 = __shfl_xor_sync(full, (int)valid, 1);
+  const bool e1 = valid && v1 && x == x1 && y == y1;
+  const int e1p = __shfl_xor_sync(full, (int)e1, 2);
+  const bool e2 = e1 && e1p && x == x2 && y == y2;
+  const int e2p = __shfl_xor_sync(full, (int)e2, 4);
+  const bool e4 = e2 && e2p && x == x4 && y == y4;
+  const int gsize = e4 ? 8 : (e2 ? 4 : (e1 ? 2 : 1));
+  const bool leader = valid && (lane & (gsize - 1)) == 0;
   float dx = x - sc.ax, dy = y - sc.ay;
   float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
-  float base = sqrtf(faw2) / g;
+  float base = valid ? sqrtf(faw2) / g : 0.f;
 #pragma unroll
   for (int k = 0; k < NF; k++) {
     if (k >= sc.nfld) break;
     const FieldStepF &fs = sc.f[k];
     if (!fs.dep_on) continue;
     CellF c;
-    if (!ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x, y, c)) continue;
-    float part = base * fs.dep_scl * cur;
-    float s, co;
-    __sincosf(phase_of(th, (unsigned)fs.harm), &s, &co);
-    float2 cp = make_float2(s * part, co * part);
-    float2 *d = p.src[k] + off;
-    float w = c.wx * c.wy;
-    atomicAdd(d + c.i00, make_float2(w * cp.x, w * cp.y));
-    w = (1.f - c.wx) * c.wy;
-    atomicAdd(d + c.i10, make_float2(w * cp.x, w * cp.y));
-    w = c.wx * (1.f - c.wy);
-    atomicAdd(d + c.i01, make_float2(w * cp.x, w * cp.y));
-    w = (1.f - c.wx) * (1.f - c.wy);
-    atomicAdd(d + c.i11, make_float2(w * cp.x, w * cp.y));
+    const bool on = valid && ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x, y, c);
+    float2 cp = make_float2(0.f, 0.f);
+    if (on) {
+      float part = base * fs.dep_scl * cur;
+      float s, co;
+      __sincosf(phase_of(th, (unsigned)fs.harm), &s, &co);
+      cp = make_float2(s * part, co * part);
+    }
+    float tx = __shfl_xor_sync(full, cp.x, 1), ty = __shfl_xor_sync(full, cp.y, 1);
+    if (e1) cp = make_float2(cp.x + tx, cp.y + ty);
+    tx = __shfl_xor_sync(full, cp.x, 2);
+    ty = __shfl_xor_sync(full, cp.y, 2);
+    if (e2) cp = make_float2(cp.x + tx, cp.y + ty);
+    tx = __shfl_xor_sync(full, cp.x, 4);
+    ty = __shfl_xor_sync(full, cp.y, 4);
+    if (e4) cp = make_float2(cp.x + tx, cp.y + ty);
+    if (on && leader) {
+      float2 *d = p.src[k] + off;
+      float w = c.wx * c.wy;
+      atomicAdd(d + c.i00, make_float2(w * cp.x, w * cp.y));
+      w = (1.f - c.wx) * c.wy;
+      atomicAdd(d + c.i10, make_float2(w * cp.x, w * cp.y));
+      w = c.wx * (1.f - c.wy);
+      atomicAdd(d + c.i01, make_float2(w * cp.x, w * cp.y));
+      w = (1.f - c.wx) * (1.f - c.wy);
+      atomicAdd(d + c.i11, make_float2(w * cp.x, w * cp.y));
+    }
   }
 }
 
@@ -230,8 +264,10 @@ __global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, 
                                                 int deposit) {
   int is = blockIdx.y;
   int ip = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ip >= np) return;
-  size_t o = (size_t)is * np + ip;
+  // lanes past the slice's particles stay for the deposition's warp shuffles
+  const bool valid = ip < np;
+  if (!valid && !deposit) return;
+  size_t o = (size_t)is * np + (valid ? ip : 0);
   const float g0 = (float)sc.gammaref;
   float dg = p.dg[o], x = p.x[o], y = p.y[o], px = p.px[o], py = p.py[o];
   long long th = p.theta[o] + sc.autophase_q;
@@ -282,23 +318,25 @@ __global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, 
 
   transverse_f(sc, true, g, x, y, px, py);
 
-  p.dg[o] = dg;
-  p.theta[o] = th;
-  p.x[o] = x;
-  p.y[o] = y;
-  p.px[o] = px;
-  p.py[o] = py;
-  if (deposit) deposit_f<NF>(sc, p, (size_t)is * ncell, ng, (float)p.current[is], g, th, x, y);
+  if (valid) {
+    p.dg[o] = dg;
+    p.theta[o] = th;
+    p.x[o] = x;
+    p.y[o] = y;
+    p.px[o] = px;
+    p.py[o] = py;
+  }
+  if (deposit) deposit_f<NF>(sc, p, (size_t)is * ncell, ng, (float)p.current[is], g, th, x, y, valid);
 }
 
 template <int NF>
 __global__ void __launch_bounds__(256) k_deposit_f(StepConstF sc, PtrsF p, int ns, int np, int ng) {
   int is = blockIdx.y;
   int ip = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ip >= np) return;
-  size_t o = (size_t)is * np + ip;
+  const bool valid = ip < np;
+  size_t o = (size_t)is * np + (valid ? ip : 0);
   deposit_f<NF>(sc, p, (size_t)is * (size_t)ng * ng, ng, (float)p.current[is],
-                (float)sc.gammaref + p.dg[o], p.theta[o], p.x[o], p.y[o]);
+                (float)sc.gammaref + p.dg[o], p.theta[o], p.x[o], p.y[o], valid);
 }
 
 struct CoefF {

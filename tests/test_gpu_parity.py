@@ -408,3 +408,40 @@ def test_fft_three_harmonics_large_grid_matches_oracle(lib, oracle, precision):
             assert rel_err(fd[k][:, 0], of[:, 0]) < 1e-2, k
         for hh in range(5):  # bunching at harmonics 1..5
             assert bunching_ok(bd[:, 24 + 2 * hh], ob[:, 24 + 2 * hh])
+
+
+@pytest.mark.parametrize("nbins,npart", [(8, 200), (3, 99), (4, 256)])
+@pytest.mark.parametrize("split", [False, True])
+def test_mixed_global_deposit_groups_match_oracle(lib, oracle, nbins, npart, split):
+    """The mixed form's deposition into global source grids (FFT solver here) sums the
+    amplitudes of lanes whose particles share x and y (a beamlet of the quiet loading)
+    before one atomic per cell. Particle counts that leave a warp part-filled and
+    beamlets that straddle the lane groups (nbins 3) must deposit like the oracle;
+    split runs push and field stages as separate calls, which deposits in its own
+    kernel. Slice power and bunching within 1 %."""
+    import g4gpu
+    import g4cases as T
+    ns, ng, gm = 4, 45, 1e-4
+    lat = T.undulator_lattice(1.7, 0.015, 12, 1, 1e-10, 11357.8)
+    part = g4gpu.host_load_beam(T.slice_params(ns, 11357.8, 1.0, 0.4e-6, 15.0), 0, npart, nbins, 5, 1, 1e-10, 1.0)
+    cur = np.full(ns, 3000.0)
+    g1 = g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e6, 20e-6), gm, ng)
+    fld = np.stack([g1 * (1 + 0.3j * k) for k in range(ns)])
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, gridmax=gm, lambda0=1e-10, sample=1.0,
+                       gammaref=11357.8, precision=1, solver=g4gpu.SOLVER_FFT, time_run=1)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam(part, cur)
+        h.load_field(0, fld)
+        for i in range(lat.shape[0]):
+            if split:
+                h.run(i, 1, g4gpu.STAGE_PUSH)
+                h.run(i, 1, g4gpu.STAGE_FIELD | g4gpu.STAGE_SLIP)
+            else:
+                h.run(i, 1)
+        bd, fd = h.diag(1)
+    rp, rf, rfirst, _ = oracle.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, [1], [gm], fld[None], [0], solver=1)
+    of = oracle.diag_field(rf[0], gm, 1e-10, 1, int(rfirst[0]))
+    ob = oracle.diag_beam(rp, 1)
+    assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-2
+    assert bunching_ok(bd[:, 24], ob[:, 24])
