@@ -445,3 +445,33 @@ def test_mixed_global_deposit_groups_match_oracle(lib, oracle, nbins, npart, spl
     ob = oracle.diag_beam(rp, 1)
     assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-2
     assert bunching_ok(bd[:, 24], ob[:, 24])
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_pinned_host_buffers_round_trip_like_pageable(lib, prec):
+    """Loading from and storing to pinned host arrays (through raw pointers, as the
+    benchmark's end-to-end window does) gives what pageable arrays give."""
+    import torch
+    import g4gpu
+    d = golden("steps.npz")
+    part, fld = d["harm13_part"], d["harm13_fields"]
+    ns, npart = part.shape[0], part.shape[1]
+    pin_p = torch.from_numpy(np.ascontiguousarray(part)).pin_memory()
+    pin_f = torch.from_numpy(np.ascontiguousarray(fld[1]).view(np.float64)).pin_memory()
+    with handle_for(g4gpu, ns, npart, 19, [1, 3], [6e-5, 4e-5], 11357.8, prec, 1, 0) as h:
+        h.load_beam_ptr(pin_p.data_ptr(), np.ascontiguousarray(d["harm13_cur"]).ctypes.data)
+        h.load_field_ptr(1, pin_f.data_ptr(), first=2)
+        h.load_field(0, fld[0])
+        ref_beam = h.get_beam()
+        ref_field, first, _ = h.get_field(1)
+        assert first == 2
+        out_p = torch.empty_like(pin_p).pin_memory()
+        out_f = torch.empty_like(pin_f).pin_memory()
+        h.get_beam(out_p.numpy())
+        h.get_field(1, out_f.numpy().view(np.complex128).reshape(ns, -1))
+    assert np.array_equal(out_p.numpy(), ref_beam)
+    assert np.array_equal(out_f.numpy().view(np.complex128).reshape(ns, -1), ref_field)
+    if prec == 0:
+        assert np.array_equal(ref_beam, part) and np.array_equal(ref_field, fld[1])
+    else:
+        assert rel_err(ref_beam, part) < 1e-6 and rel_err(ref_field, fld[1]) < 1e-6
