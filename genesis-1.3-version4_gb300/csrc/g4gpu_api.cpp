@@ -664,6 +664,10 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
         g4::launch_push_mixed(L, scf, h->beam, h->field, nullptr, ns, np, ng, 0, h->push_block);
       }
       if (do_field) {
+        // the diagnostic record of a step run by g4gpu_run_diag, formed by the fused
+        // kernel itself when it holds the scratch for it
+        const bool rec = h->diag_rec && !pair && g4::fused_diag_fits(ng, h->field_threads, h->diag_nharm);
+        const int bw = g4::beam_diag_width(h->diag_nharm), fw = g4::kFieldSums + 2;
         for (int k = 0; k < c.nfield; k++) {
           const char *cb = (const char *)h->coef + (size_t)sc.f[k].coef * 3 * ng * h->csize;
           Timed t(h, G4GPU_K_ADI_X);
@@ -671,8 +675,11 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
             g4::launch_field_pair_mixed(L, scf, k, h->beam, h->field[k], cb, ns, np, ng, sc.f[k].dep_on);
           else
             g4::launch_field_fused_mixed(L, scf, k, h->beam, h->field[k], cb, ns, np, ng, sc.f[k].dep_on,
-                                         h->field_threads);
+                                         h->field_threads, nullptr,
+                                         rec ? h->diag_rec + (size_t)ns * bw + (size_t)k * ns * fw : nullptr,
+                                         h->diag_nharm, c.gammaref);
         }
+        if (rec) h->diag_fields_in_step = true;
       }
     } else {
     if (do_field && any_dep)
@@ -735,6 +742,13 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
           if (!c.periodic) {
             G4_CUDA(h, cudaMemsetAsync((char *)h->field[k] + (size_t)last * ncell * h->csize, 0,
                                        ncell * h->csize, h->stream));
+            // a record formed during the step holds the slice's sums before clearing
+            if (h->diag_fields_in_step) {
+              const size_t fw = g4::kFieldSums + 2;
+              double *d = h->diag_rec + (size_t)ns * g4::beam_diag_width(h->diag_nharm) +
+                          ((size_t)k * ns + last) * fw;
+              G4_CUDA(h, cudaMemsetAsync(d, 0, fw * sizeof(double), h->stream));
+            }
           }
           h->first[k] = last;
           if (direction < 0) h->first[k] = (last + 1) % ns;
@@ -829,37 +843,47 @@ int g4gpu_synchronize(g4gpu_handle h) {
   return check_device_flag(h);
 }
 
-int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out) {
-  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
-  if (nharm < 1 || nharm > G4GPU_MAX_HARM) return fail(h, G4GPU_ERR_ARG, "nharm must be 1..16");
-  cudaSetDevice(h->cfg.device);
+}  // extern "C"
+
+namespace {
+
+// Device and pinned host buffers of the raw diagnostic sums, grown to `need` bytes.
+int diag_buffers(g4gpu_handle h, size_t need) {
+  if (need <= h->ddiag_bytes) return G4GPU_OK;
+  if (h->ddiag) cudaFree(h->ddiag);
+  if (h->hdiag) cudaFreeHost(h->hdiag);
+  h->ddiag = nullptr;
+  h->hdiag = nullptr;
+  h->ddiag_bytes = 0;
+  int rc = alloc(h, (void **)&h->ddiag, need);
+  if (rc) return rc;
+  cudaError_t e = cudaMallocHost((void **)&h->hdiag, need);
+  if (e != cudaSuccess) return cuda_fail(h, e, "cudaMallocHost (diagnostics)");
+  h->ddiag_bytes = need;
+  return G4GPU_OK;
+}
+
+// Raw sums of one diagnostic record: beam [nslice][beam_diag_width], then per field
+// [nslice][kFieldSums + 2] in storage (ring) order.
+size_t diag_record_doubles(const g4gpu_config &c, int nharm) {
+  return (size_t)c.nslice * g4::beam_diag_width(nharm) + (size_t)c.nfield * c.nslice * (g4::kFieldSums + 2);
+}
+
+// Queues the kernels of one diagnostic record of the current state into `rec`.
+void enqueue_diag(g4gpu_handle h, int nharm, double *rec, bool beam, bool field) {
   const g4gpu_config &c = h->cfg;
   int ns = c.nslice, np = c.npart, ng = c.ngrid;
   int bw = g4::beam_diag_width(nharm), fw = g4::kFieldSums + 2;
-  size_t need = ((size_t)ns * bw + (size_t)c.nfield * ns * fw) * sizeof(double);
-  if (need > h->ddiag_bytes) {
-    if (h->ddiag) cudaFree(h->ddiag);
-    if (h->hdiag) cudaFreeHost(h->hdiag);
-    h->ddiag = nullptr;
-    h->hdiag = nullptr;
-    h->ddiag_bytes = 0;
-    int rc = alloc(h, (void **)&h->ddiag, need);
-    if (rc) return rc;
-    cudaError_t e = cudaMallocHost((void **)&h->hdiag, need);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMallocHost (diagnostics)");
-    h->ddiag_bytes = need;
-  }
   g4::Launch L{h->stream, h->derr};
-  double *db = h->ddiag, *dfd = h->ddiag + (size_t)ns * bw;
-  if (beam_out) {
-    if (!h->beam_loaded) return fail(h, G4GPU_ERR_STATE, "no beam loaded");
+  double *db = rec, *dfd = rec + (size_t)ns * bw;
+  if (beam) {
     Timed t(h, G4GPU_K_DIAG);
     if (h->mixed)
       g4::launch_diag_beam_mixed(L, h->beam, c.gammaref, ns, np, nharm, db);
     else
       g4::launch_diag_beam_plain(L, h->beam, ns, np, nharm, db);
   }
-  if (field_out) {
+  if (field) {
     for (int k = 0; k < c.nfield; k++) {
       Timed t(h, G4GPU_K_DIAG);
       if (h->mixed)
@@ -868,11 +892,16 @@ int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out) {
         g4::launch_diag_field_plain(L, h->field[k], ns, ng, dfd + (size_t)k * ns * fw);
     }
   }
-  G4_CUDA(h, cudaGetLastError());
-  G4_CUDA(h, cudaMemcpyAsync(h->hdiag, h->ddiag, need, cudaMemcpyDeviceToHost, h->stream));
-  int rc = check_device_flag(h);
-  if (rc) return rc;
-  const double *raw = h->hdiag;
+}
+
+// The diagnostics of one raw record, with the fields' ring starts `first` of that
+// state: DiagBeam::getValues and DiagField::getValues finished on the host.
+void finish_diag(g4gpu_handle h, const double *raw, int nharm, const int *first, double *beam_out,
+                 double *field_out) {
+  const g4gpu_config &c = h->cfg;
+  int ns = c.nslice, np = c.npart, ng = c.ngrid;
+  int bw = g4::beam_diag_width(nharm), fw = g4::kFieldSums + 2;
+  (void)fw;
 
   if (beam_out) {
     // DiagBeam::getValues, Diagnostic.cpp:457-531
@@ -918,7 +947,7 @@ int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out) {
       double scl = dgrid * g4::kEev / ks;
       for (int is0 = 0; is0 < ns; is0++) {
         const double *s = raw + (size_t)ns * bw + ((size_t)k * ns + is0) * fw;
-        int is = (ns + is0 - h->first[k]) % ns;
+        int is = (ns + is0 - first[k]) % ns;
         double power = s[0], x1 = s[1], x2 = s[2], y1 = s[3], y2 = s[4];
         if (power > 0) {
           x1 /= power;
@@ -945,6 +974,68 @@ int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out) {
       }
     }
   }
+}
+
+}  // namespace
+
+extern "C" {
+
+int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (nharm < 1 || nharm > G4GPU_MAX_HARM) return fail(h, G4GPU_ERR_ARG, "nharm must be 1..16");
+  if (beam_out && !h->beam_loaded) return fail(h, G4GPU_ERR_STATE, "no beam loaded");
+  cudaSetDevice(h->cfg.device);
+  const size_t need = diag_record_doubles(h->cfg, nharm) * sizeof(double);
+  int rc = diag_buffers(h, need);
+  if (rc) return rc;
+  enqueue_diag(h, nharm, h->ddiag, beam_out != nullptr, field_out != nullptr);
+  G4_CUDA(h, cudaGetLastError());
+  G4_CUDA(h, cudaMemcpyAsync(h->hdiag, h->ddiag, need, cudaMemcpyDeviceToHost, h->stream));
+  rc = check_device_flag(h);
+  if (rc) return rc;
+  finish_diag(h, h->hdiag, nharm, h->first, beam_out, field_out);
+  return G4GPU_OK;
+}
+
+int g4gpu_run_diag(g4gpu_handle h, int istep0, int nsteps, int nharm, double *beam_out, double *field_out) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (nharm < 1 || nharm > G4GPU_MAX_HARM) return fail(h, G4GPU_ERR_ARG, "nharm must be 1..16");
+  if (istep0 < 0 || nsteps < 0 || istep0 + nsteps > h->nsteps)
+    return fail(h, G4GPU_ERR_ARG, "step range outside the lattice");
+  if (!h->beam_loaded) return fail(h, G4GPU_ERR_STATE, "no beam loaded");
+  for (int k = 0; k < h->cfg.nfield; k++)
+    if (!h->field_loaded[k]) return fail(h, G4GPU_ERR_STATE, "a field is not loaded");
+  if (nsteps == 0) return G4GPU_OK;
+  cudaSetDevice(h->cfg.device);
+  const g4gpu_config &c = h->cfg;
+  const size_t rec = diag_record_doubles(c, nharm);
+  int rc = diag_buffers(h, (size_t)nsteps * rec * sizeof(double));
+  if (rc) return rc;
+  std::vector<int> firsts((size_t)nsteps * G4GPU_MAX_FIELDS);
+  for (int s = 0; s < nsteps; s++) {
+    // the fused field kernel forms the fields' record during the step where it can
+    // (the slice is in its shared memory); the beam's, and the fields' elsewhere, come
+    // from the diagnostic kernels after the step
+    h->diag_rec = h->ddiag + (size_t)s * rec;
+    h->diag_nharm = nharm;
+    h->diag_fields_in_step = false;
+    rc = enqueue_steps(h, istep0 + s, 1, G4GPU_STAGE_ALL);
+    const bool fields_done = h->diag_fields_in_step;
+    h->diag_rec = nullptr;
+    h->diag_fields_in_step = false;
+    if (rc) return rc;
+    for (int k = 0; k < c.nfield; k++) firsts[(size_t)s * G4GPU_MAX_FIELDS + k] = h->first[k];
+    enqueue_diag(h, nharm, h->ddiag + (size_t)s * rec, beam_out != nullptr, field_out != nullptr && !fields_done);
+  }
+  G4_CUDA(h, cudaGetLastError());
+  G4_CUDA(h, cudaMemcpyAsync(h->hdiag, h->ddiag, (size_t)nsteps * rec * sizeof(double), cudaMemcpyDeviceToHost,
+                             h->stream));
+  if ((rc = check_device_flag(h))) return rc;
+  const size_t bstride = (size_t)c.nslice * (G4GPU_DB_NCOL + 2 * nharm);
+  const size_t fstride = (size_t)c.nfield * c.nslice * G4GPU_DF_NCOL;
+  for (int s = 0; s < nsteps; s++)
+    finish_diag(h, h->hdiag + (size_t)s * rec, nharm, &firsts[(size_t)s * G4GPU_MAX_FIELDS],
+                beam_out ? beam_out + s * bstride : nullptr, field_out ? field_out + s * fstride : nullptr);
   return G4GPU_OK;
 }
 

@@ -37,6 +37,11 @@ struct g4gpu_ctx {
   double *ddiag = nullptr;
   size_t ddiag_bytes = 0;
   double *hdiag = nullptr;  // pinned host copy of ddiag (the per-step read-back)
+  // g4gpu_run_diag: the record of the step being queued (null otherwise), its
+  // harmonics, and whether the step's kernels formed the fields' part of it
+  double *diag_rec = nullptr;
+  int diag_nharm = 0;
+  bool diag_fields_in_step = false;
   void *stage = nullptr;     // AoS staging buffer for host transfers
   size_t stage_bytes = 0;
   size_t bytes = 0;

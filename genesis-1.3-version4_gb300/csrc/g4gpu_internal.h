@@ -120,10 +120,14 @@ int fused_max_ngrid();
 int pair_max_ngrid();
 void launch_field_pair_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b, void *field,
                              const void *coef, int ns, int np, int ngrid, int deposit);
-// threads: CTA size, a multiple of 32 in [2 ngrid, 1024]
+// threads: CTA size, a multiple of 32 in [2 ngrid, 1024]. dbeam / dfield (may be
+// null): the step's diagnostic record, beam [nslice][beam_diag_width(nharm)] (formed by
+// the launch of field 0) and this field's [nslice][kFieldSums + 2] in storage order.
 void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b,
                               void *field, const void *coef, int ns, int np, int ngrid, int deposit,
-                              int threads);
+                              int threads, double *dbeam, double *dfield, int nharm, double gref);
+// whether the fused kernel can record the diagnostics (nharm bunching harmonics) too
+bool fused_diag_fits(int ngrid, int threads, int nharm);
 // One ADI step of ns float2 field slices with an optional source, all scratch in the
 // module's static device array (g4gpu_adi_advance_noalloc); coef: [3][ngrid] float2 of
 // c, cbet, cwet. Synchronises `stream`. Returns a G4GPU_ERR_* code with *msg set.

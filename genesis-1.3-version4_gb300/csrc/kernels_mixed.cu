@@ -862,8 +862,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *er
 // Copies `count` float2 from global g to shared s with one TMA bulk copy for the
 // 16-byte aligned middle and plain loads for an 8-byte head / tail. The shared
 // copy is laid out so that s and g agree modulo 16 bytes (see the caller).
-__device__ __forceinline__ bool bulk_load(float2 *s, const float2 *g, int count, uint32_t bar,
-                                          int *err) {
+__device__ __forceinline__ void bulk_load_issue(float2 *s, const float2 *g, int count, uint32_t bar) {
   uintptr_t ga = reinterpret_cast<uintptr_t>(g);
   int head = (ga & 15) ? 1 : 0;
   int body = (count - head) & ~1;
@@ -881,9 +880,16 @@ __device__ __forceinline__ bool bulk_load(float2 *s, const float2 *g, int count,
   }
   if (head && threadIdx.x == 32) s[0] = g[0];
   if (tail && threadIdx.x == 64) s[count - 1] = g[count - 1];
+}
+// Waits for bulk_load_issue's copy (bounded) and makes it visible to the CTA.
+__device__ __forceinline__ bool bulk_load_wait(uint32_t bar, int *err) {
   bool ok = mbar_wait(bar, 0, err);
   __syncthreads();
   return ok;
+}
+__device__ __forceinline__ bool bulk_load(float2 *s, const float2 *g, int count, uint32_t bar, int *err) {
+  bulk_load_issue(s, g, count, bar);
+  return bulk_load_wait(bar, err);
 }
 
 __device__ __forceinline__ void bulk_store(float2 *g, const float2 *s, int count) {
@@ -905,9 +911,144 @@ __device__ __forceinline__ void bulk_store(float2 *g, const float2 *s, int count
   if (tail && threadIdx.x == 64) g[count - 1] = s[count - 1];
 }
 
+// ---- diagnostics of a step recorded by the fused field kernel -----------------
+//
+// With the slice and its particles on chip, the fused kernel forms the per-slice sums
+// of k_diag_beam_f (first field only) and k_diag_field_f into the run's diagnostic
+// record, in the layouts of those kernels. A thread takes np / blockDim particles
+// (or ngrid^2 / blockDim cells), few enough for FP32 partial sums; the CTA folds the
+// partials in FP64.
+constexpr int kFusedDiagHarm = 2;  // bunching harmonics the fused kernel records
+constexpr int kFusedDiagValues = kBeamSums + 2 * kFusedDiagHarm + 10;
+
+// The NS sums and NX min/max pairs of the CTA: within a warp in FP32 (the lanes'
+// partials are FP32; FP64 adds run at 1/64 of the FP32 rate here and would dominate
+// the kernel), then folded over the warps in FP64 through `sh` (warps x (NS + 2 NX)
+// doubles); thread k < NS + 2 NX gets value k in *out.
+template <int NS, int NX>
+__device__ __forceinline__ void cta_reduce(const float *s, const float *mn, const float *mx, double *sh,
+                                           double *out) {
+  constexpr int NV = NS + 2 * NX;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NS; k++) {
+    float v = s[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[warp * NV + k] = v;
+  }
+#pragma unroll
+  for (int k = 0; k < NX; k++) {
+    float a = mn[k], b = mx[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a = fminf(a, __shfl_down_sync(0xffffffffu, a, o));
+      b = fmaxf(b, __shfl_down_sync(0xffffffffu, b, o));
+    }
+    if (lane == 0) {
+      sh[warp * NV + NS + 2 * k] = a;
+      sh[warp * NV + NS + 2 * k + 1] = b;
+    }
+  }
+  __syncthreads();
+  const int k = threadIdx.x;
+  if (k < NV) {
+    double r = sh[k];
+    for (int w = 1; w < nw; w++) {
+      const double v = sh[w * NV + k];
+      if (k < NS)
+        r += v;
+      else
+        r = ((k - NS) & 1) ? fmax(r, v) : fmin(r, v);
+    }
+    out[k] = r;
+  }
+  __syncthreads();
+}
+
+// Beam sums of slice `is` into o[beam_diag_width(nharm)] (k_diag_beam_f's record).
+__device__ __forceinline__ void slice_beam_sums(const PtrsF &p, double gref, int is, int np, int nharm,
+                                                double *sh, double *res, double *o) {
+  constexpr int NSUM = kBeamSums + 2 * kFusedDiagHarm;
+  const size_t base = (size_t)is * np;
+  float c[NSUM];
+#pragma unroll
+  for (int k = 0; k < NSUM; k++) c[k] = 0.f;
+  float mn[5], mx[5];  // x, px, y, py, dg
+#pragma unroll
+  for (int k = 0; k < 5; k++) {
+    mn[k] = INFINITY;
+    mx[k] = -INFINITY;
+  }
+  // unrolled so that the loads of several particles are in flight together
+#pragma unroll 8
+  for (int ip = threadIdx.x; ip < np; ip += blockDim.x) {
+    const float x = p.x[base + ip], y = p.y[base + ip], dg = p.dg[base + ip];
+    const float px = p.px[base + ip], py = p.py[base + ip];
+    const long long th = p.theta[base + ip];
+    c[0] += dg; c[1] += dg * dg; c[2] += x; c[3] += x * x; c[4] += y; c[5] += y * y;
+    c[6] += px; c[7] += px * px; c[8] += py; c[9] += py * py; c[10] += x * px; c[11] += y * py;
+    mn[0] = fminf(mn[0], x); mx[0] = fmaxf(mx[0], x);
+    mn[1] = fminf(mn[1], px); mx[1] = fmaxf(mx[1], px);
+    mn[2] = fminf(mn[2], y); mx[2] = fmaxf(mx[2], y);
+    mn[3] = fminf(mn[3], py); mx[3] = fmaxf(mx[3], py);
+    mn[4] = fminf(mn[4], dg); mx[4] = fmaxf(mx[4], dg);
+#pragma unroll
+    for (int h = 0; h < kFusedDiagHarm; h++) {
+      if (h < nharm) {
+        float sn, cs;
+        sincosf(phase_of(th, (unsigned)(h + 1)), &sn, &cs);
+        c[kBeamSums + 2 * h] += cs;
+        c[kBeamSums + 2 * h + 1] += sn;
+      }
+    }
+  }
+  cta_reduce<NSUM, 5>(c, mn, mx, sh, res);
+  const int k = threadIdx.x;
+  const double n = (double)np;
+  if (k == 0) o[0] = n * gref + res[0];
+  if (k == 1) o[1] = n * gref * gref + 2.0 * gref * res[0] + res[1];
+  if (k >= 2 && k < kBeamSums) o[k] = res[k];
+  if (k >= kBeamSums && k < kBeamSums + 2 * nharm) o[kBeamMinMax + k] = res[k];
+  if (k < 10) o[kBeamSums + k] = (k >= 8 ? gref : 0.0) + res[NSUM + k];
+}
+
+// Field sums of the slice S (ng x ng, in shared memory) into o[kFieldSums + 2]
+// (k_diag_field_f's record).
+__device__ __forceinline__ void slice_field_sums(const float2 *S, int ng, double *sh, double *res, double *o) {
+  const int ncell = ng * ng;
+  const float shift = -0.5f * (float)(ng - 1);
+  float c[kFieldSums];
+#pragma unroll
+  for (int k = 0; k < kFieldSums; k++) c[k] = 0.f;
+  int row = threadIdx.x / ng, col = threadIdx.x - row * ng;
+  const int drow = blockDim.x / ng, dcol = blockDim.x - drow * ng;
+  for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+    const float dx = (float)col + shift, dy = (float)row + shift;
+    const float2 v = S[i];
+    const float wei = v.x * v.x + v.y * v.y;
+    c[0] += wei; c[1] += dx * wei; c[2] += dx * dx * wei; c[3] += dy * wei; c[4] += dy * dy * wei;
+    c[5] += v.x; c[6] += v.y;
+    row += drow;
+    col += dcol;
+    if (col >= ng) {
+      col -= ng;
+      row++;
+    }
+  }
+  cta_reduce<kFieldSums, 0>(c, nullptr, nullptr, sh, res);
+  if (threadIdx.x < kFieldSums) o[threadIdx.x] = res[threadIdx.x];
+  if (threadIdx.x == 0) {
+    const float2 v = S[(ng / 2) * ng + ng / 2];
+    o[7] = v.x;
+    o[8] = v.y;
+  }
+}
+
 __global__ void __launch_bounds__(kFusedMaxThreads, 1)
     k_field_fused_f(StepConstF sc, int k, PtrsF p, float2 *__restrict__ field,
-                    const float2 *__restrict__ coef, int ns, int np, int ng, int deposit, int *err) {
+                    const float2 *__restrict__ coef, int ns, int np, int ng, int deposit, int *err,
+                    double *dbeam, double *dfield, int nharm, double gref) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int ncell = ng * ng;
   const FieldStepF &fs = sc.f[k];
@@ -943,7 +1084,14 @@ __global__ void __launch_bounds__(kFusedMaxThreads, 1)
     float nd = den.x * den.x + den.y * den.y;
     K[0] = make_float2(den.x / nd, -den.y / nd);
   }
-  if (!bulk_load(S, u, ncell, bar_s, err)) return;
+  // diagnostic scratch after the slice: warps x kFusedDiagValues doubles, then the
+  // folded values
+  double *dsh = reinterpret_cast<double *>(smem_raw + ((soff + (size_t)ncell * 8 + 15) & ~(size_t)15));
+  double *dres = dsh + (blockDim.x >> 5) * kFusedDiagValues;
+  bulk_load_issue(S, u, ncell, bar_s);
+  // the beam record of this slice while the field is in flight
+  if (dbeam) slice_beam_sums(p, gref, is, np, nharm, dsh, dres, dbeam + (size_t)is * beam_diag_width(nharm));
+  if (!bulk_load_wait(bar_s, err)) return;
   const float cs = fs.cstep;
   const int tid = threadIdx.x;
   const int nseg = max(1, min((int)blockDim.x / ng, 8));
@@ -978,6 +1126,8 @@ __global__ void __launch_bounds__(kFusedMaxThreads, 1)
     thomas2(S + line, ng, ng, up, CB, CW, a, invden, mask);
   __syncthreads();
   bulk_store(u, S, ncell);
+  // the field record of storage slice i, read from S alongside the store
+  if (dfield) slice_field_sums(S, ng, dsh, dres, dfield + (size_t)i * (kFieldSums + 2));
   if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
@@ -1034,12 +1184,23 @@ __device__ __forceinline__ void block_reduce_all(const double *s, const float *m
                                                  double *out) {
   constexpr int NW = BS / 32, NV = NS + 2 * NX;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // within a warp as an unevaluated pair of FP32 numbers (hi + lo, hi the FP32
+  // rounding of the lane's FP64 sum), added level by level with the exact rounding
+  // error of hi's sum (Knuth's TwoSum) carried into lo: FP32 shuffles and adds instead
+  // of FP64 ones, which run at 1/64 of the FP32 rate, to about 44 bits
 #pragma unroll
   for (int k = 0; k < NS; k++) {
-    double v = s[k];
+    float hi = (float)s[k];
+    float lo = (float)(s[k] - (double)hi);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[warp * NV + k] = v;
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_down_sync(0xffffffffu, hi, o), ol = __shfl_down_sync(0xffffffffu, lo, o);
+      const float t = hi + oh, bp = t - hi;
+      const float e = (hi - (t - bp)) + (oh - bp);
+      hi = t;
+      lo = lo + ol + e;
+    }
+    if (lane == 0) sh[warp * NV + k] = (double)hi + (double)lo;
   }
 #pragma unroll
   for (int k = 0; k < NX; k++) {
@@ -1769,6 +1930,18 @@ void launch_diag_field_mixed(const Launch &L, const void *field, int ns, int ngr
 size_t fused_smem_bytes(int ng) {
   return ((16 + 3 * (size_t)ng * 8 + 15) & ~(size_t)15) + 8 + (size_t)ng * ng * 8;
 }
+// ... and with the diagnostic scratch of `threads` threads
+size_t fused_diag_smem_bytes(int ng, int threads) {
+  return ((fused_smem_bytes(ng) + 15) & ~(size_t)15) + (size_t)(threads / 32 + 1) * kFusedDiagValues * 8;
+}
+int fused_threads(int ngrid, int threads) {
+  if (threads < 2 * ngrid) threads = (2 * ngrid + 31) / 32 * 32;
+  if (threads > kFusedMaxThreads) threads = kFusedMaxThreads;
+  return threads;
+}
+bool fused_diag_fits(int ngrid, int threads, int nharm) {
+  return nharm <= kFusedDiagHarm && fused_diag_smem_bytes(ngrid, fused_threads(ngrid, threads)) <= 227u * 1024u;
+}
 
 int fused_max_ngrid() {
   int ng = 3;
@@ -1778,9 +1951,10 @@ int fused_max_ngrid() {
 
 void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b,
                               void *field, const void *coef, int ns, int np, int ngrid, int deposit,
-                              int threads) {
+                              int threads, double *dbeam, double *dfield, int nharm, double gref) {
   static unsigned long long configured = 0;  // one bit per device
-  size_t smem = fused_smem_bytes(ngrid);
+  threads = fused_threads(ngrid, threads);
+  size_t smem = (dbeam || dfield) ? fused_diag_smem_bytes(ngrid, threads) : fused_smem_bytes(ngrid);
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 64 && !(configured & (1ull << dev))) {
@@ -1788,10 +1962,8 @@ void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, cons
     configured |= 1ull << dev;
   }
   PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
-  if (threads < 2 * ngrid) threads = (2 * ngrid + 31) / 32 * 32;
-  if (threads > kFusedMaxThreads) threads = kFusedMaxThreads;
   k_field_fused_f<<<ns, threads, smem, (cudaStream_t)L.stream>>>(
-      sc, k, p, (float2 *)field, (const float2 *)coef, ns, np, ngrid, deposit, L.err);
+      sc, k, p, (float2 *)field, (const float2 *)coef, ns, np, ngrid, deposit, L.err, dbeam, dfield, nharm, gref);
 }
 
 int pair_max_ngrid() {

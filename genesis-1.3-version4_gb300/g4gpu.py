@@ -44,7 +44,7 @@ KERNEL_CLASSES = ["push", "adi_x", "adi_y", "fft", "slip", "diag", "misc"]
 ABI_SYMBOLS = [
     "g4gpu_config_defaults", "g4gpu_create", "g4gpu_destroy", "g4gpu_last_error",
     "g4gpu_set_lattice", "g4gpu_load_beam", "g4gpu_get_beam", "g4gpu_load_field",
-    "g4gpu_get_field", "g4gpu_run", "g4gpu_synchronize", "g4gpu_diag", "g4gpu_get_stream",
+    "g4gpu_get_field", "g4gpu_run", "g4gpu_synchronize", "g4gpu_diag", "g4gpu_run_diag", "g4gpu_get_stream",
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
     "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc",
     "g4gpu_set_graph_mode", "g4gpu_autotune", "g4gpu_batch_create", "g4gpu_batch_destroy",
@@ -128,6 +128,7 @@ def load_library(path=None):
     L.g4gpu_run.argtypes = [vp, i, i, i]
     L.g4gpu_synchronize.argtypes = [vp]
     L.g4gpu_diag.argtypes = [vp, i, vp, vp]
+    L.g4gpu_run_diag.argtypes = [vp, i, i, i, vp, vp]
     L.g4gpu_get_stream.argtypes = [vp, P(vp)]
     L.g4gpu_set_profiling.argtypes = [vp, i]
     L.g4gpu_kernel_stats.argtypes = [vp, P(ctypes.c_longlong), pd]
@@ -313,6 +314,21 @@ class Handle:
         f = np.zeros((self.cfg.nfield, ns, len(DF_COLS))) if field else None
         self._check(self.L.g4gpu_diag(self.h, nharm, _vp(b) if beam else None,
                                       _vp(f) if field else None))
+        return b, f
+
+    def run_diag(self, istep0, nsteps, nharm=1, beam=True, field=True, out=None):
+        """Runs nsteps steps from istep0 and returns the per-slice diagnostics after
+        every step: beam [nsteps][nslice][cols], field [nsteps][nfield][nslice][cols]
+        (g4gpu_run_diag). `out` may pass preallocated (beam, field) arrays."""
+        ns = self.cfg.nslice
+        if out is not None:
+            b, f = out
+        else:
+            b = np.zeros((nsteps, ns, len(DB_COLS) + 2 * nharm)) if beam else None
+            f = np.zeros((nsteps, self.cfg.nfield, ns, len(DF_COLS))) if field else None
+        self._check(self.L.g4gpu_run_diag(self.h, int(istep0), int(nsteps), nharm,
+                                          _vp(b) if b is not None else None,
+                                          _vp(f) if f is not None else None))
         return b, f
 
     def stream(self):

@@ -154,6 +154,16 @@ int g4gpu_synchronize(g4gpu_handle h);
  * Replaces Diagnostic::calc (src/Core/Diagnostic.cpp:262-277) for these columns. */
 int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out);
 
+/* Runs steps istep0 .. istep0+nsteps-1 (all stages, as g4gpu_run) and records after
+ * every step the per-slice diagnostics g4gpu_diag would return at that point:
+ * beam_out [nsteps][nslice][G4GPU_DB_NCOL + 2*nharm], field_out
+ * [nsteps][nfield][nslice][G4GPU_DF_NCOL] (either may be NULL). The records stay on
+ * the device until the last step and are read back and finished once, as the
+ * reference keeps them in memory (Diagnostic::calc after every output step in
+ * Gencore::run, src/Core/Gencore.cpp:102-160; written by Output::writeGroup at the
+ * end). Synchronous: returns when the steps and the read-back are done. */
+int g4gpu_run_diag(g4gpu_handle h, int istep0, int nsteps, int nharm, double *beam_out, double *field_out);
+
 /* The CUDA stream (cudaStream_t) every kernel of h is queued on. */
 int g4gpu_get_stream(g4gpu_handle h, void **stream);
 

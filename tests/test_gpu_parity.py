@@ -475,3 +475,77 @@ def test_pinned_host_buffers_round_trip_like_pageable(lib, prec):
         assert np.array_equal(ref_beam, part) and np.array_equal(ref_field, fld[1])
     else:
         assert rel_err(ref_beam, part) < 1e-6 and rel_err(ref_field, fld[1]) < 1e-6
+
+
+@pytest.mark.parametrize("prec,nh", [(0, 3), (1, 2), (1, 3)])
+def test_run_diag_records_every_step_like_diag(lib, prec, nh):
+    """g4gpu_run_diag records after every step what g4gpu_diag gives after that step
+    of g4gpu_run (time-dependent window with slippage, two fields). A second run gives
+    the records to 1e-6 of each column's scale (the deposition's atomic adds make two
+    runs differ in the last bits; phases of small amplitudes are not compared). The
+    mixed window (ngrid 25) takes the fused field kernel, which forms the records
+    itself for up to 2 harmonics: nharm 2 there, 3 (the separate kernels) as well."""
+    import g4gpu
+    import g4cases as T
+    ns, npart, ng = 8, 128, 25
+    lat = T.undulator_lattice(1.7, 0.015, 5, 2, 1e-10, 11357.8, quad_k1=1.5, quad_l=0.08)
+    part = g4gpu.host_load_beam(T.slice_params(ns, 11357.8, 1.0, 0.4e-6, 15.0), 0, npart, 4, 3, 1, 1e-10, 1.0)
+    cur = np.full(ns, 3000.0)
+    g1 = g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e5, 20e-6), 6e-5, ng)
+    fld = np.stack([np.stack([g1 * (1 + 0.2j * k) for k in range(ns)]), np.stack([0.1 * g1] * ns)])
+    nsteps = lat.shape[0]
+
+    def handle():
+        cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, harm=[1, 3], gridmax=[6e-5, 4e-5], lambda0=1e-10,
+                           sample=1.0, gammaref=11357.8, precision=prec, time_run=1)
+        h = g4gpu.Handle(cfg)
+        h.set_lattice(lat)
+        h.load_beam(part, cur)
+        h.load_field(0, fld[0])
+        h.load_field(1, fld[1])
+        return h
+
+    with handle() as h:
+        rb, rf = h.run_diag(0, nsteps, nharm=nh)
+        b, f = h.diag(nh)
+    DB, DF = g4gpu.DB_COLS, g4gpu.DF_COLS
+    phase_b = {len(DB) + 2 * j + 1 for j in range(nh)}
+    phase_f = {DF.index("phase-nearfield"), DF.index("phase-farfield")}
+    # centroids and alphas are sums that nearly cancel: compared on the scale of the
+    # spread they sit in
+    scale_b = {DB.index("xposition"): DB.index("xsize"), DB.index("yposition"): DB.index("ysize"),
+               DB.index("pxposition"): DB.index("pxmax"), DB.index("pyposition"): DB.index("pymax")}
+    scale_f = {DF.index("xposition"): DF.index("xsize"), DF.index("yposition"): DF.index("ysize")}
+    # alphas are O(1) numbers near zero and bunching lies in [0, 1]: compared to 1e-6
+    # absolute
+    unit_b = {DB.index("alphax"), DB.index("alphay")} | {len(DB) + 2 * j for j in range(nh)}
+
+    def bad_cols(a, ref, skip, scales, unit=()):
+        bad = []
+        for col in range(ref.shape[-1]):
+            if col in skip:
+                continue
+            scale = 1.0 if col in unit else np.max(np.abs(ref[..., scales.get(col, col)]))
+            err = np.max(np.abs(a[..., col] - ref[..., col]))
+            if err > 1e-6 * scale + 1e-300:
+                bad.append((col, float(err), float(scale)))
+        return bad
+
+    def close(a, ref, skip, scales, unit=()):
+        bad = bad_cols(a, ref, skip, scales, unit)
+        assert not bad, bad
+        return True
+
+    # the last record against g4gpu_diag on the same state: identical in the plain
+    # form (the same kernels), to 1e-6 in the mixed one, whose fused field kernel forms
+    # the records with its own summation order
+    if prec == 0:
+        assert np.array_equal(rb[-1], b) and np.array_equal(rf[-1], f)
+    assert close(rb[-1], b, phase_b, scale_b, unit_b) and close(rf[-1], f, phase_f, scale_f)
+    with handle() as h:
+        for i in range(nsteps):
+            h.run(i, 1)
+            b, f = h.diag(nh)
+            assert close(rb[i], b, phase_b, scale_b, unit_b), i
+            assert close(rf[i], f, phase_f, scale_f), i
+    assert np.any(rf[-1][0][:, 0] > 0)
