@@ -390,7 +390,7 @@ void g4gpu_destroy(g4gpu_handle h) {
   cudaSetDevice(h->cfg.device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   void *ptrs[] = {h->beam.gamma, h->beam.theta, h->beam.x, h->beam.y, h->beam.px, h->beam.py,
-                  h->beam.current, h->tmp, h->coef, h->derr, h->ddiag, h->stage,
+                  h->beam.current, h->tmp, h->diag_work, h->coef, h->derr, h->ddiag, h->stage,
                   h->closure_basis, h->closure_feat, h->closure_corr};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -994,6 +994,64 @@ int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out) {
   rc = check_device_flag(h);
   if (rc) return rc;
   finish_diag(h, h->hdiag, nharm, h->first, beam_out, field_out);
+  return G4GPU_OK;
+}
+
+int g4gpu_diag_fft(g4gpu_handle h, double *out) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (!out) return fail(h, G4GPU_ERR_ARG, "null output");
+  const g4gpu_config &c = h->cfg;
+  for (int k = 0; k < c.nfield; k++)
+    if (!h->field_loaded[k]) return fail(h, G4GPU_ERR_STATE, "a field is not loaded");
+  cudaSetDevice(c.device);
+  int rc;
+  // the transform's roots and plan: the FFT solver's, else built on the first call
+  if (!h->fft_roots[0] && (rc = fft_tables(h))) return rc;
+  if (!g4::fft_plan_fits(h->fft_plan))
+    return fail(h, G4GPU_ERR_ARG, "ngrid " + std::to_string(c.ngrid) + ": no FFT plan for the far-field diagnostics");
+  const int ns = c.nslice, n = c.ngrid;
+  const size_t ncell = (size_t)n * n;
+  void *work = h->tmp;
+  if (!work) {
+    if (!h->diag_work && (rc = alloc(h, &h->diag_work, (size_t)ns * ncell * h->csize))) return rc;
+    work = h->diag_work;
+  }
+  const int L = g4::fft_diag_lines(h->fft_plan, h->mixed), nblk = (n + L - 1) / L;
+  const size_t per_field = (size_t)ns * nblk * 5;
+  if ((rc = diag_buffers(h, (size_t)c.nfield * per_field * sizeof(double)))) return rc;
+  for (int k = 0; k < c.nfield; k++) {
+    Timed t(h, G4GPU_K_DIAG, 2);
+    g4::launch_fft_diag(h->stream, h->mixed, h->field[k], work, h->fft_roots[k], h->fft_plan, ns, h->first[k],
+                        h->ddiag + k * per_field);
+  }
+  G4_CUDA(h, cudaGetLastError());
+  G4_CUDA(h, cudaMemcpyAsync(h->hdiag, h->ddiag, (size_t)c.nfield * per_field * sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream));
+  if ((rc = check_device_flag(h))) return rc;
+  // DiagField::getValues, Diagnostic.cpp:815-836 (moments) and 836-847 (scaling)
+  for (int k = 0; k < c.nfield; k++) {
+    const double xlambda = c.lambda0 / static_cast<double>(c.harm[k]);
+    const double dgrid = 2 * c.gridmax[k] / static_cast<double>(n - 1);
+    const double scltheta = xlambda / n / dgrid;
+    for (int ii = 0; ii < ns; ii++) {
+      double m[5] = {0, 0, 0, 0, 0};
+      const double *p = h->hdiag + k * per_field + (size_t)ii * nblk * 5;
+      for (int b = 0; b < nblk; b++)
+        for (int q = 0; q < 5; q++) m[q] += p[(size_t)b * 5 + q];
+      double fp = m[0], fx1 = m[1], fx2 = m[2], fy1 = m[3], fy2 = m[4];
+      if (fp > 0) {
+        fx1 /= fp;
+        fx2 /= fp;
+        fy1 /= fp;
+        fy2 /= fp;
+      }
+      double *o = out + ((size_t)k * ns + ii) * G4GPU_DFFT_NCOL;
+      o[G4GPU_DFFT_XPOINT] = fx1 * scltheta;
+      o[G4GPU_DFFT_XDIV] = std::sqrt(std::fabs(fx2 - fx1 * fx1)) * scltheta;
+      o[G4GPU_DFFT_YPOINT] = fy1 * scltheta;
+      o[G4GPU_DFFT_YDIV] = std::sqrt(std::fabs(fy2 - fy1 * fy1)) * scltheta;
+    }
+  }
   return G4GPU_OK;
 }
 

@@ -26,6 +26,7 @@ struct g4gpu_ctx {
   void *field[G4GPU_MAX_FIELDS] = {};
   void *src[G4GPU_MAX_FIELDS] = {};
   void *tmp = nullptr;
+  void *diag_work = nullptr;  // g4gpu_diag_fft's scratch where tmp is absent
   void *coef = nullptr;      // [nset][3][ngrid] complex of the field type
   size_t coef_bytes = 0;
   // FFT solver tables per field: roots of unity [n], Im(K2) and the sigmoid [n^2]

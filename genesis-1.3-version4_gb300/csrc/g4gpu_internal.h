@@ -159,6 +159,12 @@ int fft_plan_fits(const FFTPlan &pl);
 // -dk^2 / (2 xks), Im(K2) = (dx^2 + dy^2) k2c; sig: the sigmoid filter on the FFT
 // index (real, n^2, transposed: element kx n + ky); work: n^2 * nslice complex
 // scratch, used when filtered
+// Far-field moments of the field diagnostics: the row pass into `work` (n^2 nslice
+// complex scratch), then the column pass that writes one partial of 5 sums per tile of
+// fft_diag_lines columns: part[(ii nblk + blk) 5 + k], nblk = ceil(n / lines).
+int fft_diag_lines(const FFTPlan &pl, int mixed);
+void launch_fft_diag(void *stream, int mixed, const void *field, void *work, const void *roots, const FFTPlan &pl,
+                     int ns, int first, double *part);
 void launch_fft_solve(void *stream, int mixed, void *field, const void *src, void *work, const void *roots,
                       double k2c, const void *sig, int filtered, double delz, const FFTPlan &pl, int ns,
                       int first);

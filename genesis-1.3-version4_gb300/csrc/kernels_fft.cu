@@ -553,6 +553,88 @@ __global__ void __launch_bounds__(256, sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTA
   cp_wait<0>();
 }
 
+// Far-field moments of the field diagnostics (DiagField with FFTW,
+// Diagnostic.cpp:786-847): a column pass over the row-transformed field `work`
+// (k_fft_rows<T,0> into it first) that takes the forward FFT of the columns and the
+// power-weighted moments of the tile's elements on the shifted frequency map (dx, dy
+// as in k_fft_cols' propagator). One partial per tile, deterministic:
+// part[(ii nblk + blk) 5 + k] = sum |F|^2, dx |F|^2, dx^2 |F|^2, dy |F|^2, dy^2 |F|^2.
+template <typename T2>
+__global__ void __launch_bounds__(256, sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTAS_FP64)
+    k_fft_cols_moments(const T2 *__restrict__ work, const T2 *__restrict__ roots, FFTPlan pl, int ns, int first,
+                       int L, double *__restrict__ part) {
+  typedef typename Real<T2>::T R;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[8][5];
+  T2 *W = reinterpret_cast<T2 *>(smem_raw);
+  const int n = pl.n;
+  T2 *Abuf = W + 2 * n;
+  const int nblk = (n + L - 1) / L, ntiles = ns * nblk;
+  const size_t ncell = (size_t)n * n;
+  const R half = (R)(0.5 * (n - 1));
+  const int off = n - (n + 1) / 2;
+  const int c_init = fdiv(threadIdx.x, n, pl.mn), ky_init = threadIdx.x - c_init * n;
+  const int dc = fdiv(blockDim.x, n, pl.mn), dky = blockDim.x - dc * n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int t = threadIdx.x; t < 2 * n - 1; t += blockDim.x) cp_elem(W + t, roots + t);
+  int tile = blockIdx.x;
+  if (tile < ntiles) {
+    const int ii = tile / nblk, c0 = (tile - ii * nblk) * L;
+    load_cols(Abuf, work + (size_t)((ii + first) % ns) * ncell, n, c0, min(L, n - c0));
+  }
+  cp_commit();
+  for (int it = 0; tile < ntiles; tile += gridDim.x, it++) {
+    T2 *A = Abuf + (it & 1) * L * n;
+    const int ii = tile / nblk, blk = tile - ii * nblk, c0 = blk * L, lines = min(L, n - c0);
+    const int nx = tile + gridDim.x;
+    if (nx < ntiles) {
+      const int jj = nx / nblk, q0 = (nx - jj * nblk) * L;
+      load_cols(Abuf + ((it + 1) & 1) * L * n, work + (size_t)((jj + first) % ns) * ncell, n, q0,
+                min(L, n - q0));
+    }
+    cp_commit();
+    cp_wait<1>();
+    __syncthreads();
+    fft_lines(A, n, lines, pl, W, false);
+    R m[5] = {0, 0, 0, 0, 0};
+    int c = c_init, ky = ky_init;
+    for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
+      int ix = c0 + c + off, iy = ky + off;
+      ix -= ix >= n ? n : 0;
+      iy -= iy >= n ? n : 0;
+      const R dx = (R)ix - half, dy = (R)iy - half;
+      const T2 v = A[t];
+      const R w = v.x * v.x + v.y * v.y;
+      m[0] += w;
+      m[1] += dx * w;
+      m[2] += dx * dx * w;
+      m[3] += dy * w;
+      m[4] += dy * dy * w;
+      c += dc;
+      ky += dky;
+      if (ky >= n) {
+        ky -= n;
+        c++;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      R v = m[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp][k] = (double)v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+      double r = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) r += red[w][threadIdx.x];
+      part[((size_t)ii * nblk + blk) * 5 + threadIdx.x] = r;
+    }
+    __syncthreads();
+  }
+  cp_wait<0>();
+}
+
 constexpr int FFT_THREADS = 256;
 
 // Shared memory of a pass with `bufs` tile buffers of L lines and the roots and
@@ -630,6 +712,37 @@ void launch_fft(void *stream, void *field, const void *src, void *work, const vo
                                                               L1);
 }
 
+template <typename T2>
+void launch_fft_diag_t(void *stream, const void *field, void *work, const void *roots, const FFTPlan &pl, int ns,
+                       int first, double *part, int L) {
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = pl.n;
+  const int es = (int)sizeof(T2);
+  static unsigned long long configured = 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !(configured & (1ull << dev))) {
+    cudaFuncSetAttribute(k_fft_rows<T2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    // (the kernel's static reduction array counts against the 227 KB too)
+    cudaFuncSetAttribute(k_fft_cols_moments<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024);
+    configured |= 1ull << dev;
+  }
+  const int ctas = es == 8 ? FFT_CTAS_FP32 : FFT_CTAS_FP64;
+  const long long nsm = sm_count();
+  auto grid = [&](int lines, size_t smem) {
+    const long long tiles = (long long)ns * ((n + lines - 1) / lines);
+    const long long cap = nsm * fft_ctas_per_sm(ctas, smem);
+    return (unsigned)(tiles < cap ? tiles : cap);
+  };
+  const int Lr = fft_lines_per_cta(pl, es, 2, 32, ctas);
+  const size_t mr = fft_smem(n, Lr, 2, (size_t)es);
+  k_fft_rows<T2, 0><<<grid(Lr, mr), FFT_THREADS, mr, s>>>((const T2 *)field, (T2 *)work, nullptr, (const T2 *)roots,
+                                                          pl, ns, first, 1.0, Lr);
+  const size_t mc = fft_smem(n, L, 2, (size_t)es);
+  k_fft_cols_moments<T2><<<grid(L, mc), FFT_THREADS, mc, s>>>((const T2 *)work, (const T2 *)roots, pl, ns, first, L,
+                                                              part);
+}
+
 }  // namespace
 
 // Lines per CTA of a pass with `bufs` tile buffers: the largest L <= maxL such that
@@ -669,6 +782,20 @@ int fft_plan_fits(const FFTPlan &pl) {
     if (register_radix(r) ? pl.n / r > FFT_THREADS : pl.n > STAGE_ANY_OUT * FFT_THREADS) return 0;
   }
   return 1;
+}
+
+int fft_diag_lines(const FFTPlan &pl, int mixed) {
+  const int es = mixed ? (int)sizeof(float2) : (int)sizeof(double2);
+  return fft_lines_per_cta(pl, es, 2, 16, mixed ? FFT_CTAS_FP32 : FFT_CTAS_FP64);
+}
+
+void launch_fft_diag(void *stream, int mixed, const void *field, void *work, const void *roots, const FFTPlan &pl,
+                     int ns, int first, double *part) {
+  const int L = fft_diag_lines(pl, mixed);
+  if (mixed)
+    launch_fft_diag_t<float2>(stream, field, work, roots, pl, ns, first, part, L);
+  else
+    launch_fft_diag_t<double2>(stream, field, work, roots, pl, ns, first, part, L);
 }
 
 void launch_fft_solve(void *stream, int mixed, void *field, const void *src, void *work, const void *roots,

@@ -38,13 +38,14 @@ DB_COLS = ["energy", "energyspread", "xposition", "xsize", "yposition", "ysize",
            "emin", "emax"]
 DF_COLS = ["power", "xposition", "xsize", "yposition", "ysize", "intensity-nearfield",
            "phase-nearfield", "intensity-farfield", "phase-farfield"]
+DFFT_COLS = ["xpointing", "xdivergence", "ypointing", "ydivergence"]
 KERNEL_CLASSES = ["push", "adi_x", "adi_y", "fft", "slip", "diag", "misc"]
 
 # exported symbols of include/g4gpu.h
 ABI_SYMBOLS = [
     "g4gpu_config_defaults", "g4gpu_create", "g4gpu_destroy", "g4gpu_last_error",
     "g4gpu_set_lattice", "g4gpu_load_beam", "g4gpu_get_beam", "g4gpu_load_field",
-    "g4gpu_get_field", "g4gpu_run", "g4gpu_synchronize", "g4gpu_diag", "g4gpu_run_diag", "g4gpu_get_stream",
+    "g4gpu_get_field", "g4gpu_run", "g4gpu_synchronize", "g4gpu_diag", "g4gpu_run_diag", "g4gpu_diag_fft", "g4gpu_get_stream",
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
     "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc",
     "g4gpu_set_graph_mode", "g4gpu_autotune", "g4gpu_batch_create", "g4gpu_batch_destroy",
@@ -129,6 +130,7 @@ def load_library(path=None):
     L.g4gpu_synchronize.argtypes = [vp]
     L.g4gpu_diag.argtypes = [vp, i, vp, vp]
     L.g4gpu_run_diag.argtypes = [vp, i, i, i, vp, vp]
+    L.g4gpu_diag_fft.argtypes = [vp, vp]
     L.g4gpu_get_stream.argtypes = [vp, P(vp)]
     L.g4gpu_set_profiling.argtypes = [vp, i]
     L.g4gpu_kernel_stats.argtypes = [vp, P(ctypes.c_longlong), pd]
@@ -315,6 +317,13 @@ class Handle:
         self._check(self.L.g4gpu_diag(self.h, nharm, _vp(b) if beam else None,
                                       _vp(f) if field else None))
         return b, f
+
+    def diag_fft(self):
+        """Far-field xpointing, xdivergence, ypointing, ydivergence [nfield][nslice][4]
+        (g4gpu_diag_fft)."""
+        out = np.zeros((self.cfg.nfield, self.cfg.nslice, len(DFFT_COLS)))
+        self._check(self.L.g4gpu_diag_fft(self.h, _vp(out)))
+        return out
 
     def run_diag(self, istep0, nsteps, nharm=1, beam=True, field=True, out=None):
         """Runs nsteps steps from istep0 and returns the per-slice diagnostics after

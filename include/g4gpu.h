@@ -85,6 +85,11 @@ enum {
   G4GPU_DF_POWER, G4GPU_DF_XPOS, G4GPU_DF_XSIZE, G4GPU_DF_YPOS, G4GPU_DF_YSIZE,
   G4GPU_DF_NF_INT, G4GPU_DF_NF_PHI, G4GPU_DF_FF_INT, G4GPU_DF_FF_PHI, G4GPU_DF_NCOL
 };
+/* Columns of g4gpu_diag_fft: far-field pointing and divergence [rad]
+ * (DiagField with FFTW, src/Core/Diagnostic.cpp:786-847, filter "fft") */
+enum {
+  G4GPU_DFFT_XPOINT, G4GPU_DFFT_XDIV, G4GPU_DFFT_YPOINT, G4GPU_DFFT_YDIV, G4GPU_DFFT_NCOL
+};
 
 typedef struct {
   int nslice;    /* slices in the time window (Time::getNodeNSlice, src/Main/GenTime.cpp:64-86) */
@@ -153,6 +158,14 @@ int g4gpu_synchronize(g4gpu_handle h);
  * field_out [nfield][nslice][G4GPU_DF_NCOL] indexed by window slice (may be NULL).
  * Replaces Diagnostic::calc (src/Core/Diagnostic.cpp:262-277) for these columns. */
 int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out);
+
+/* Far-field pointing and divergence of every slice of every field: the forward 2-D
+ * FFT of the slice, its power-weighted moments on the shifted frequency map, scaled by
+ * xlambda / (ngrid dgrid). out [nfield][nslice][G4GPU_DFFT_NCOL] by window slice.
+ * Replaces the FFTW part of DiagField::getValues (src/Core/Diagnostic.cpp:786-847).
+ * Uses the handle's scratch field array (allocated on the first call where the
+ * handle has none). */
+int g4gpu_diag_fft(g4gpu_handle h, double *out);
 
 /* Runs steps istep0 .. istep0+nsteps-1 (all stages, as g4gpu_run) and records after
  * every step the per-slice diagnostics g4gpu_diag would return at that point:

@@ -1157,6 +1157,63 @@ void orc_diag_beam(int ns, int npart, const double *particles, int nharm, double
   }
 }
 
+/* DiagField's far-field moments, Diagnostic.cpp:786-847 (filter "fft"): the forward
+ * 2-D transform of each slice (FFTW's convention: e^{-2 pi i jk/n}, unnormalised), its
+ * power-weighted first and second moments on the shifted frequency map
+ * ii = ((iy + (n+1)/2) % n) n + (ix + (n+1)/2) % n with dx = ix - (n-1)/2 (likewise y),
+ * scaled by scltheta = xlambda / (ngrid dgrid): out[ns][4] = xpointing, xdivergence,
+ * ypointing, ydivergence, indexed by window slice. */
+void orc_diag_field_fft(int ns, int ngrid, double gridmax, double lambda0, int harm, const double *field,
+                        int first, double *out) {
+  const cplx *f = (const cplx *)field;
+  const int n = ngrid;
+  double xlambda = lambda0 / (double)harm;
+  double dgrid = 2 * gridmax / (double)(n - 1);
+  double scltheta = xlambda / n / dgrid;
+  double shift = -0.5 * (double)(n - 1);
+  cplx *a = (cplx *)malloc(sizeof(cplx) * (size_t)n * n);
+  cplx *t1 = (cplx *)malloc(sizeof(cplx) * 2 * (size_t)n);
+  cplx *t2 = (cplx *)malloc(sizeof(cplx) * (size_t)n);
+  for (int is0 = 0; is0 < ns; is0++) {
+    int is = (ns + is0 - first) % ns;
+    memcpy(a, f + (size_t)is0 * n * n, sizeof(cplx) * (size_t)n * n);
+    fft2(a, n, -1, t1, t2);
+    double fp = 0, fx1 = 0, fx2 = 0, fy1 = 0, fy2 = 0;
+    for (int iy = 0; iy < n; iy++) {
+      double dy = (double)iy + shift;
+      for (int ix = 0; ix < n; ix++) {
+        double dx = (double)ix + shift;
+        int iiy = (iy + (n + 1) / 2) % n, iix = (ix + (n + 1) / 2) % n;
+        cplx loc = a[(size_t)iiy * n + iix];
+        double wei = creal(loc) * creal(loc) + cimag(loc) * cimag(loc);
+        fp += wei;
+        fx1 += dx * wei;
+        fx2 += dx * dx * wei;
+        fy1 += dy * wei;
+        fy2 += dy * dy * wei;
+      }
+    }
+    if (fp > 0) {
+      fx1 /= fp;
+      fx2 /= fp;
+      fy1 /= fp;
+      fy2 /= fp;
+    }
+    fx2 = sqrt(fabs(fx2 - fx1 * fx1)) * scltheta;
+    fy2 = sqrt(fabs(fy2 - fy1 * fy1)) * scltheta;
+    fx1 *= scltheta;
+    fy1 *= scltheta;
+    double *o = out + (size_t)is * 4;
+    o[0] = fx1;
+    o[1] = fx2;
+    o[2] = fy1;
+    o[3] = fy2;
+  }
+  free(a);
+  free(t1);
+  free(t2);
+}
+
 void orc_diag_field(int ns, int ngrid, double gridmax, double lambda0, int harm,
                     const double *field, int first, double *out) {
   const cplx *f = (const cplx *)field;

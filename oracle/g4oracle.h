@@ -96,6 +96,10 @@ enum {
 };
 void orc_diag_field(int ns, int ngrid, double gridmax, double lambda0, int harm,
                     const double *field, int first, double *out);
+/* Far-field pointing and divergence (DiagField, Diagnostic.cpp:786-847, "fft"):
+ * out[ns][4] = xpointing, xdivergence, ypointing, ydivergence by window slice. */
+void orc_diag_field_fft(int ns, int ngrid, double gridmax, double lambda0, int harm, const double *field,
+                        int first, double *out);
 
 #ifdef __cplusplus
 }

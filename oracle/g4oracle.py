@@ -69,6 +69,7 @@ class _Lib:
         if prefix == "orc_":
             L.orc_diag_beam.argtypes = [_i, _i, _pd, _i, _pd]
             L.orc_diag_field.argtypes = [_i, _i, _d, _d, _i, _pd, _i, _pd]
+            L.orc_diag_field_fft.argtypes = [_i, _i, _d, _d, _i, _pd, _i, _pd]
             L.orc_deposit_source.argtypes = [_pd, _i, _i, _i, _pd, _pd, _d, _i, _i, _d, _pd]
             L.orc_adi_advance.argtypes = [_i, _i, _i, _d, _d, _d, _pd, _pd]
 
@@ -156,6 +157,16 @@ class _Lib:
         out = np.zeros((ns, len(DF_COLS)))
         self.lib.orc_diag_field(ns, ngrid, gridmax, lambda0, harm, _ptr(f.view(np.float64)),
                                 int(first), _ptr(out))
+        return out
+
+    def diag_field_fft(self, field, gridmax, lambda0, harm, first):
+        """Far-field xpointing, xdivergence, ypointing, ydivergence [ns][4] by window slice."""
+        f = np.ascontiguousarray(field, dtype=np.complex128)
+        ns = f.shape[0]
+        ngrid = int(round(np.sqrt(f.shape[1])))
+        out = np.zeros((ns, 4))
+        self.lib.orc_diag_field_fft(ns, ngrid, gridmax, lambda0, harm, _ptr(f.view(np.float64)),
+                                    int(first), _ptr(out))
         return out
 
     def deposit_source(self, lat, istep, particles, current, reflength, harm, ngrid, gridmax):

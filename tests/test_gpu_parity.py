@@ -549,3 +549,40 @@ def test_run_diag_records_every_step_like_diag(lib, prec, nh):
             assert close(rb[i], b, phase_b, scale_b, unit_b), i
             assert close(rf[i], f, phase_f, scale_f), i
     assert np.any(rf[-1][0][:, 0] > 0)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("ng,solver", [(45, 0), (32, 1), (51, 0)])
+def test_far_field_diagnostics_match_oracle(lib, oracle, prec, ng, solver):
+    """g4gpu_diag_fft (far-field pointing and divergence, DiagField with FFTW) against
+    the oracle's restatement, on a window after a few steps (ring start moved by
+    slippage), two fields; ADI handles (no scratch array of their own in the mixed
+    form) and an FFT one. Plain FP64 within 1e-9 of each column's scale, mixed 1e-4."""
+    import g4gpu
+    import g4cases as T
+    ns, npart = 6, 64
+    gms = [6e-5, 4e-5]
+    lat = T.undulator_lattice(1.7, 0.015, 3, 1, 1e-10, 11357.8)
+    part = g4gpu.host_load_beam(T.slice_params(ns, 11357.8, 1.0, 0.4e-6, 15.0), 0, npart, 4, 9, 1, 1e-10, 1.0)
+    x = np.arange(ng) - 0.5 * (ng - 1)
+    g = np.exp(-((x[None, :] - 2.0) ** 2 + (x[:, None] + 1.0) ** 2) / (0.05 * ng * ng))
+    fld = np.stack([np.stack([(g * np.exp(1j * (0.2 + 0.05 * s + 0.02 * k) * x[None, :]
+                                          - 1j * 0.03 * k * x[:, None])).ravel() * 1e4
+                              for s in range(ns)]) for k in range(2)])
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, harm=[1, 3], gridmax=gms, lambda0=1e-10, sample=1.0,
+                       gammaref=11357.8, precision=prec, solver=solver, time_run=1)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam(part, np.full(ns, 3000.0))
+        h.load_field(0, fld[0])
+        h.load_field(1, fld[1])
+        h.run(0, 2)
+        got = h.diag_fft()
+        fields = [h.get_field(k) for k in range(2)]
+    tol = 1e-9 if prec == 0 else 1e-4
+    for k, hk in enumerate([1, 3]):
+        f, first, _ = fields[k]
+        want = oracle.diag_field_fft(f, gms[k], 1e-10, hk, first)
+        for col in range(4):
+            scale = np.max(np.abs(want[:, col | 1]))  # pointing on the divergence's scale
+            assert np.max(np.abs(got[k][:, col] - want[:, col])) <= tol * scale, (k, col)

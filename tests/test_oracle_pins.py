@@ -163,3 +163,31 @@ def test_fft_solver_matches_numpy(oracle, n):
         assert np.abs(src).max() > 0
         want = np.fft.ifft2(np.fft.fft2(u[0, s].reshape(n, n)) * prop + 2 * np.fft.fft2(src) * sg).ravel()
         assert np.allclose(ff[0, s], want, rtol=0, atol=1e-10 * np.abs(want).max())
+
+
+@pytest.mark.parametrize("n", [15, 16, 21])
+def test_far_field_moments_match_numpy(oracle, n):
+    """The oracle's far-field pointing and divergence (DiagField with FFTW,
+    Diagnostic.cpp:786-847; FFTW is absent here) against numpy: the power-weighted
+    moments of |FFT2(u)|^2 on the shifted frequency map, scaled by
+    xlambda / (ngrid dgrid), by window slice."""
+    rng = np.random.default_rng(n + 100)
+    ns, gm, lam, harm, first = 3, 5e-5, 1e-10, 3, 1
+    x = np.arange(n) - 0.5 * (n - 1)
+    g = np.exp(-((x[None, :] - 1.3) ** 2 + (x[:, None] + 0.7) ** 2) / (0.2 * n * n))
+    u = np.stack([(g * np.exp(1j * (0.3 * s + 0.2) * x[None, :])
+                   + 0.01 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))).ravel()
+                  for s in range(ns)])
+    got = oracle.diag_field_fft(u, gm, lam, harm, first)
+    dgrid = 2 * gm / (n - 1)
+    sclt = lam / harm / n / dgrid
+    for is0 in range(ns):
+        F = np.fft.fft2(u[is0].reshape(n, n))
+        idx = (np.arange(n) + (n + 1) // 2) % n
+        w = np.abs(F[np.ix_(idx, idx)]) ** 2  # [iy, ix] on the shifted map
+        p = w.sum()
+        fx1, fx2 = (w * x[None, :]).sum() / p, (w * x[None, :] ** 2).sum() / p
+        fy1, fy2 = (w * x[:, None]).sum() / p, (w * x[:, None] ** 2).sum() / p
+        want = [fx1 * sclt, np.sqrt(abs(fx2 - fx1 * fx1)) * sclt, fy1 * sclt, np.sqrt(abs(fy2 - fy1 * fy1)) * sclt]
+        is_ = (ns + is0 - first) % ns
+        assert np.allclose(got[is_], want, rtol=1e-10, atol=1e-12 * max(abs(v) for v in want))
