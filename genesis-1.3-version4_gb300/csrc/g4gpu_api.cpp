@@ -997,6 +997,78 @@ int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out) {
   return G4GPU_OK;
 }
 
+int g4gpu_diag_global(const g4gpu_config *cfg, int nharm, const double *current, const double *beam_diag,
+                      const double *field_diag, const double *fft_diag, double *beam_global,
+                      double *field_global) {
+  if (!cfg || nharm < 1 || nharm > G4GPU_MAX_HARM) return G4GPU_ERR_ARG;
+  if ((beam_global && (!beam_diag || !current)) || (field_global && !field_diag)) return G4GPU_ERR_ARG;
+  const int ns = cfg->nslice;
+  if (beam_global) {
+    // DiagBeam, Diagnostic.cpp:551-606: per slice <g> = energy, <g^2> = spread^2 +
+    // energy^2 (likewise x, y), weighted by the current
+    const int bw = G4GPU_DB_NCOL + 2 * nharm;
+    double wc = 0, g1 = 0, g2 = 0, x1 = 0, x2 = 0, y1 = 0, y2 = 0;
+    for (int is = 0; is < ns; is++) {
+      const double *b = beam_diag + (size_t)is * bw, c = current[is];
+      wc += c;
+      g1 += c * b[G4GPU_DB_ENERGY];
+      g2 += c * (b[G4GPU_DB_ENERGYSPREAD] * b[G4GPU_DB_ENERGYSPREAD] + b[G4GPU_DB_ENERGY] * b[G4GPU_DB_ENERGY]);
+      x1 += c * b[G4GPU_DB_XPOS];
+      x2 += c * (b[G4GPU_DB_XSIZE] * b[G4GPU_DB_XSIZE] + b[G4GPU_DB_XPOS] * b[G4GPU_DB_XPOS]);
+      y1 += c * b[G4GPU_DB_YPOS];
+      y2 += c * (b[G4GPU_DB_YSIZE] * b[G4GPU_DB_YSIZE] + b[G4GPU_DB_YPOS] * b[G4GPU_DB_YPOS]);
+    }
+    const double w = wc > 0 ? 1. / wc : 1.;
+    g1 *= w, g2 *= w, x1 *= w, x2 *= w, y1 *= w, y2 *= w;
+    beam_global[G4GPU_DBG_ENERGY] = g1;
+    beam_global[G4GPU_DBG_ENERGYSPREAD] = std::sqrt(std::fabs(g2 - g1 * g1));
+    beam_global[G4GPU_DBG_XPOS] = x1;
+    beam_global[G4GPU_DBG_XSIZE] = std::sqrt(std::fabs(x2 - x1 * x1));
+    beam_global[G4GPU_DBG_YPOS] = y1;
+    beam_global[G4GPU_DBG_YSIZE] = std::sqrt(std::fabs(y2 - y1 * y1));
+  }
+  if (field_global) {
+    // DiagField, Diagnostic.cpp:902-975: centroids and sizes weighted by the slices'
+    // power; the energy is the power summed over the window times slicelength / c
+    const double slicelength = cfg->lambda0 * cfg->sample;
+    for (int k = 0; k < cfg->nfield; k++) {
+      double p = 0, x1 = 0, x2 = 0, y1 = 0, y2 = 0, ni = 0, fi = 0, fx1 = 0, fx2 = 0, fy1 = 0, fy2 = 0;
+      for (int is = 0; is < ns; is++) {
+        const double *f = field_diag + ((size_t)k * ns + is) * G4GPU_DF_NCOL, P = f[G4GPU_DF_POWER];
+        p += P;
+        x1 += P * f[G4GPU_DF_XPOS];
+        x2 += P * (f[G4GPU_DF_XSIZE] * f[G4GPU_DF_XSIZE] + f[G4GPU_DF_XPOS] * f[G4GPU_DF_XPOS]);
+        y1 += P * f[G4GPU_DF_YPOS];
+        y2 += P * (f[G4GPU_DF_YSIZE] * f[G4GPU_DF_YSIZE] + f[G4GPU_DF_YPOS] * f[G4GPU_DF_YPOS]);
+        ni += f[G4GPU_DF_NF_INT];
+        fi += f[G4GPU_DF_FF_INT];
+        if (fft_diag) {
+          const double *q = fft_diag + ((size_t)k * ns + is) * G4GPU_DFFT_NCOL;
+          fx1 += P * q[G4GPU_DFFT_XPOINT];
+          fx2 += P * (q[G4GPU_DFFT_XDIV] * q[G4GPU_DFFT_XDIV] + q[G4GPU_DFFT_XPOINT] * q[G4GPU_DFFT_XPOINT]);
+          fy1 += P * q[G4GPU_DFFT_YPOINT];
+          fy2 += P * (q[G4GPU_DFFT_YDIV] * q[G4GPU_DFFT_YDIV] + q[G4GPU_DFFT_YPOINT] * q[G4GPU_DFFT_YPOINT]);
+        }
+      }
+      const double w = p > 0 ? 1. / p : 1.;
+      x1 *= w, x2 *= w, y1 *= w, y2 *= w, fx1 *= w, fx2 *= w, fy1 *= w, fy2 *= w;
+      double *o = field_global + (size_t)k * G4GPU_DFG_NCOL;
+      o[G4GPU_DFG_ENERGY] = p * slicelength / 299792458.0;
+      o[G4GPU_DFG_XPOS] = x1;
+      o[G4GPU_DFG_XSIZE] = std::sqrt(std::fabs(x2 - x1 * x1));
+      o[G4GPU_DFG_YPOS] = y1;
+      o[G4GPU_DFG_YSIZE] = std::sqrt(std::fabs(y2 - y1 * y1));
+      o[G4GPU_DFG_NF_INT] = ns > 0 ? ni / ns : 0.;
+      o[G4GPU_DFG_FF_INT] = ns > 0 ? fi / ns : 0.;
+      o[G4GPU_DFG_XPOINT] = fft_diag ? fx1 : 0.;
+      o[G4GPU_DFG_XDIV] = fft_diag ? std::sqrt(std::fabs(fx2 - fx1 * fx1)) : 0.;
+      o[G4GPU_DFG_YPOINT] = fft_diag ? fy1 : 0.;
+      o[G4GPU_DFG_YDIV] = fft_diag ? std::sqrt(std::fabs(fy2 - fy1 * fy1)) : 0.;
+    }
+  }
+  return G4GPU_OK;
+}
+
 int g4gpu_diag_fft(g4gpu_handle h, double *out) {
   if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
   if (!out) return fail(h, G4GPU_ERR_ARG, "null output");

@@ -39,13 +39,16 @@ DB_COLS = ["energy", "energyspread", "xposition", "xsize", "yposition", "ysize",
 DF_COLS = ["power", "xposition", "xsize", "yposition", "ysize", "intensity-nearfield",
            "phase-nearfield", "intensity-farfield", "phase-farfield"]
 DFFT_COLS = ["xpointing", "xdivergence", "ypointing", "ydivergence"]
+DBG_COLS = ["energy", "energyspread", "xposition", "xsize", "yposition", "ysize"]
+DFG_COLS = ["energy", "xposition", "xsize", "yposition", "ysize", "intensity-nearfield",
+            "intensity-farfield", "xpointing", "xdivergence", "ypointing", "ydivergence"]
 KERNEL_CLASSES = ["push", "adi_x", "adi_y", "fft", "slip", "diag", "misc"]
 
 # exported symbols of include/g4gpu.h
 ABI_SYMBOLS = [
     "g4gpu_config_defaults", "g4gpu_create", "g4gpu_destroy", "g4gpu_last_error",
     "g4gpu_set_lattice", "g4gpu_load_beam", "g4gpu_get_beam", "g4gpu_load_field",
-    "g4gpu_get_field", "g4gpu_run", "g4gpu_synchronize", "g4gpu_diag", "g4gpu_run_diag", "g4gpu_diag_fft", "g4gpu_get_stream",
+    "g4gpu_get_field", "g4gpu_run", "g4gpu_synchronize", "g4gpu_diag", "g4gpu_run_diag", "g4gpu_diag_fft", "g4gpu_diag_global", "g4gpu_get_stream",
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
     "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc",
     "g4gpu_set_graph_mode", "g4gpu_autotune", "g4gpu_batch_create", "g4gpu_batch_destroy",
@@ -131,6 +134,7 @@ def load_library(path=None):
     L.g4gpu_diag.argtypes = [vp, i, vp, vp]
     L.g4gpu_run_diag.argtypes = [vp, i, i, i, vp, vp]
     L.g4gpu_diag_fft.argtypes = [vp, vp]
+    L.g4gpu_diag_global.argtypes = [P(Config), i, vp, vp, vp, vp, vp, vp]
     L.g4gpu_get_stream.argtypes = [vp, P(vp)]
     L.g4gpu_set_profiling.argtypes = [vp, i]
     L.g4gpu_kernel_stats.argtypes = [vp, P(ctypes.c_longlong), pd]
@@ -405,6 +409,25 @@ class Handle:
         pb, ft, fk = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         self._check(self.L.g4gpu_autotune(self.h, ctypes.byref(pb), ctypes.byref(ft), ctypes.byref(fk)))
         return pb.value, ft.value, fk.value
+
+
+def diag_global(cfg, nharm, current=None, beam_diag=None, field_diag=None, fft_diag=None):
+    """Window ("Global/") values from one state's per-slice diagnostics
+    (g4gpu_diag_global): (beam [6] or None, field [nfield][11] or None)."""
+    L = _lib()
+    c = np.ascontiguousarray(current, dtype=np.float64) if current is not None else None
+    bd = np.ascontiguousarray(beam_diag, dtype=np.float64) if beam_diag is not None else None
+    fd = np.ascontiguousarray(field_diag, dtype=np.float64) if field_diag is not None else None
+    qd = np.ascontiguousarray(fft_diag, dtype=np.float64) if fft_diag is not None else None
+    bg = np.zeros(len(DBG_COLS)) if bd is not None else None
+    fg = np.zeros((cfg.nfield, len(DFG_COLS))) if fd is not None else None
+    rc = L.g4gpu_diag_global(ctypes.byref(cfg), nharm, _vp(c) if c is not None else None,
+                             _vp(bd) if bd is not None else None, _vp(fd) if fd is not None else None,
+                             _vp(qd) if qd is not None else None, _vp(bg) if bg is not None else None,
+                             _vp(fg) if fg is not None else None)
+    if rc != 0:
+        raise G4Error(rc, "g4gpu_diag_global: bad arguments")
+    return bg, fg
 
 
 def adi_advance_noalloc(field_ptr, source_ptr, nslice, ngrid, first, delz, dgrid, xks, device=0,

@@ -85,6 +85,18 @@ enum {
   G4GPU_DF_POWER, G4GPU_DF_XPOS, G4GPU_DF_XSIZE, G4GPU_DF_YPOS, G4GPU_DF_YSIZE,
   G4GPU_DF_NF_INT, G4GPU_DF_NF_PHI, G4GPU_DF_FF_INT, G4GPU_DF_FF_PHI, G4GPU_DF_NCOL
 };
+/* Window ("Global/") values of g4gpu_diag_global: the beam's (DiagBeam,
+ * src/Core/Diagnostic.cpp:551-606) ... */
+enum {
+  G4GPU_DBG_ENERGY, G4GPU_DBG_ENERGYSPREAD, G4GPU_DBG_XPOS, G4GPU_DBG_XSIZE, G4GPU_DBG_YPOS, G4GPU_DBG_YSIZE,
+  G4GPU_DBG_NCOL
+};
+/* ... and a field's (DiagField, src/Core/Diagnostic.cpp:902-975): energy [J], centroid
+ * and size, mean near- and far-field intensity, far-field pointing and divergence */
+enum {
+  G4GPU_DFG_ENERGY, G4GPU_DFG_XPOS, G4GPU_DFG_XSIZE, G4GPU_DFG_YPOS, G4GPU_DFG_YSIZE, G4GPU_DFG_NF_INT,
+  G4GPU_DFG_FF_INT, G4GPU_DFG_XPOINT, G4GPU_DFG_XDIV, G4GPU_DFG_YPOINT, G4GPU_DFG_YDIV, G4GPU_DFG_NCOL
+};
 /* Columns of g4gpu_diag_fft: far-field pointing and divergence [rad]
  * (DiagField with FFTW, src/Core/Diagnostic.cpp:786-847, filter "fft") */
 enum {
@@ -166,6 +178,19 @@ int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out);
  * Uses the handle's scratch field array (allocated on the first call where the
  * handle has none). */
 int g4gpu_diag_fft(g4gpu_handle h, double *out);
+
+/* The window values from one state's per-slice diagnostics, on the host (no handle,
+ * no device): beam_diag [nslice][G4GPU_DB_NCOL + 2*nharm] with the slices' current
+ * [nslice] gives beam_global[G4GPU_DBG_NCOL] (current-weighted, as DiagBeam);
+ * field_diag [nfield][nslice][G4GPU_DF_NCOL] and fft_diag
+ * [nfield][nslice][G4GPU_DFFT_NCOL] (may be NULL: the far-field columns are then 0)
+ * give field_global[nfield][G4GPU_DFG_NCOL] (power-weighted; the far-field moments
+ * weighted by the slices' power too, which is the far field's up to the constant n^2).
+ * The sums the reference forms are rebuilt from the per-slice moments, so the values
+ * agree with it to rounding. Pairs of inputs and outputs may be NULL together. */
+int g4gpu_diag_global(const g4gpu_config *cfg, int nharm, const double *current, const double *beam_diag,
+                      const double *field_diag, const double *fft_diag, double *beam_global,
+                      double *field_global);
 
 /* Runs steps istep0 .. istep0+nsteps-1 (all stages, as g4gpu_run) and records after
  * every step the per-slice diagnostics g4gpu_diag would return at that point:

@@ -1157,6 +1157,130 @@ void orc_diag_beam(int ns, int npart, const double *particles, int nharm, double
   }
 }
 
+/* The window ("Global/") values of DiagBeam, Diagnostic.cpp:551-606: the slices'
+ * moments <g>, <g^2>, <x>, <x^2>, <y>, <y^2> weighted by the current. out[6] = energy,
+ * energyspread, xposition, xsize, yposition, ysize. */
+void orc_diag_global_beam(int ns, int npart, const double *particles, const double *current, double *out) {
+  double g_cur = 0, g_g1 = 0, g_g2 = 0, g_x1 = 0, g_x2 = 0, g_y1 = 0, g_y2 = 0;
+  double norm = npart > 0 ? 1. / (double)npart : 1.;
+  for (int is = 0; is < ns; is++) {
+    double g1 = 0, g2 = 0, x1 = 0, x2 = 0, y1 = 0, y2 = 0;
+    for (int ip = 0; ip < npart; ip++) {
+      const double *p = particles + ((size_t)is * npart + ip) * 6;
+      g1 += p[0];
+      g2 += p[0] * p[0];
+      x1 += p[2];
+      x2 += p[2] * p[2];
+      y1 += p[3];
+      y2 += p[3] * p[3];
+    }
+    g1 *= norm, g2 *= norm, x1 *= norm, x2 *= norm, y1 *= norm, y2 *= norm;
+    g_cur += current[is];
+    g_g1 += current[is] * g1;
+    g_g2 += current[is] * g2;
+    g_x1 += current[is] * x1;
+    g_x2 += current[is] * x2;
+    g_y1 += current[is] * y1;
+    g_y2 += current[is] * y2;
+  }
+  double w = g_cur > 0 ? 1. / g_cur : 1.;
+  g_g1 *= w, g_g2 *= w, g_x1 *= w, g_x2 *= w, g_y1 *= w, g_y2 *= w;
+  out[0] = g_g1;
+  out[1] = sqrt(fabs(g_g2 - g_g1 * g_g1));
+  out[2] = g_x1;
+  out[3] = sqrt(fabs(g_x2 - g_x1 * g_x1));
+  out[4] = g_y1;
+  out[5] = sqrt(fabs(g_y2 - g_y1 * g_y1));
+}
+
+/* The window values of DiagField, Diagnostic.cpp:902-975, from the raw sums over all
+ * slices: out[11] = energy [J], xposition, xsize, yposition, ysize,
+ * intensity-nearfield, intensity-farfield (means over the slices), xpointing,
+ * xdivergence, ypointing, ydivergence (from the far-field moments). */
+static void fft2(cplx *a, int ng, int sign, cplx *tmp, cplx *tmp2);
+void orc_diag_global_field(int ns, int ngrid, double gridmax, double lambda0, int harm, double sample,
+                           const double *field, double *out) {
+  const cplx *f = (const cplx *)field;
+  const int n = ngrid;
+  double xlambda = lambda0 / (double)harm;
+  double dgrid = 2 * gridmax / (double)(n - 1);
+  double ks = 4. * asin(1) / xlambda;
+  double scl = dgrid * kEev / ks;
+  double scltheta = xlambda / n / dgrid;
+  double shift = -0.5 * (double)(n - 1);
+  double g_pow = 0, g_x1 = 0, g_x2 = 0, g_y1 = 0, g_y2 = 0, g_ff = 0, g_inten = 0;
+  double f_pow = 0, f_x1 = 0, f_x2 = 0, f_y1 = 0, f_y2 = 0;
+  cplx *a = (cplx *)malloc(sizeof(cplx) * (size_t)n * n);
+  cplx *t1 = (cplx *)malloc(sizeof(cplx) * 2 * (size_t)n);
+  cplx *t2 = (cplx *)malloc(sizeof(cplx) * (size_t)n);
+  for (int is0 = 0; is0 < ns; is0++) {
+    const cplx *sl = f + (size_t)is0 * n * n;
+    cplx ff = 0;
+    for (int iy = 0; iy < n; iy++) {
+      double dy = (double)iy + shift;
+      for (int ix = 0; ix < n; ix++) {
+        double dx = (double)ix + shift;
+        cplx loc = sl[iy * n + ix];
+        double wei = creal(loc) * creal(loc) + cimag(loc) * cimag(loc);
+        ff += loc;
+        g_pow += wei;
+        g_x1 += dx * wei;
+        g_x2 += dx * dx * wei;
+        g_y1 += dy * wei;
+        g_y2 += dy * dy * wei;
+      }
+    }
+    cplx c = sl[(n / 2) * n + n / 2];
+    g_inten += creal(c) * creal(c) + cimag(c) * cimag(c);
+    g_ff += (creal(ff) * creal(ff) + cimag(ff) * cimag(ff)) * dgrid * dgrid;
+    memcpy(a, sl, sizeof(cplx) * (size_t)n * n);
+    fft2(a, n, -1, t1, t2);
+    for (int iy = 0; iy < n; iy++) {
+      double dy = (double)iy + shift;
+      for (int ix = 0; ix < n; ix++) {
+        double dx = (double)ix + shift;
+        int iiy = (iy + (n + 1) / 2) % n, iix = (ix + (n + 1) / 2) % n;
+        cplx loc = a[(size_t)iiy * n + iix];
+        double wei = creal(loc) * creal(loc) + cimag(loc) * cimag(loc);
+        f_pow += wei;
+        f_x1 += dx * wei;
+        f_x2 += dx * dx * wei;
+        f_y1 += dy * wei;
+        f_y2 += dy * dy * wei;
+      }
+    }
+  }
+  free(a);
+  free(t1);
+  free(t2);
+  double norm = g_pow > 0 ? 1. / g_pow : 1.;
+  g_x1 *= norm, g_x2 *= norm, g_y1 *= norm, g_y2 *= norm;
+  g_x2 = sqrt(fabs(g_x2 - g_x1 * g_x1)) * dgrid;
+  g_y2 = sqrt(fabs(g_y2 - g_y1 * g_y1)) * dgrid;
+  g_x1 *= dgrid;
+  g_y1 *= dgrid;
+  norm = f_pow > 0 ? 1. / f_pow : 1.;
+  f_x1 *= norm, f_x2 *= norm, f_y1 *= norm, f_y2 *= norm;
+  f_x2 = sqrt(fabs(f_x2 - f_x1 * f_x1)) * scltheta;
+  f_y2 = sqrt(fabs(f_y2 - f_y1 * f_y1)) * scltheta;
+  f_x1 *= scltheta;
+  f_y1 *= scltheta;
+  double slicelength = lambda0 * sample;
+  g_pow *= scl * scl / kVacimp * slicelength / 299792458.0;
+  norm = 1. / (double)ns;
+  out[0] = g_pow;
+  out[1] = g_x1;
+  out[2] = g_x2;
+  out[3] = g_y1;
+  out[4] = g_y2;
+  out[5] = g_inten * norm * kEev * kEev / ks / ks / kVacimp;
+  out[6] = g_ff * norm;
+  out[7] = f_x1;
+  out[8] = f_x2;
+  out[9] = f_y1;
+  out[10] = f_y2;
+}
+
 /* DiagField's far-field moments, Diagnostic.cpp:786-847 (filter "fft"): the forward
  * 2-D transform of each slice (FFTW's convention: e^{-2 pi i jk/n}, unnormalised), its
  * power-weighted first and second moments on the shifted frequency map

@@ -96,6 +96,14 @@ enum {
 };
 void orc_diag_field(int ns, int ngrid, double gridmax, double lambda0, int harm,
                     const double *field, int first, double *out);
+/* Window ("Global/") values from the raw sums: DiagBeam (Diagnostic.cpp:551-606),
+ * out[6] = energy, energyspread, xposition, xsize, yposition, ysize; DiagField
+ * (Diagnostic.cpp:902-975), out[11] = energy [J], xposition, xsize, yposition, ysize,
+ * intensity-nearfield, intensity-farfield, xpointing, xdivergence, ypointing,
+ * ydivergence. */
+void orc_diag_global_beam(int ns, int npart, const double *particles, const double *current, double *out);
+void orc_diag_global_field(int ns, int ngrid, double gridmax, double lambda0, int harm, double sample,
+                           const double *field, double *out);
 /* Far-field pointing and divergence (DiagField, Diagnostic.cpp:786-847, "fft"):
  * out[ns][4] = xpointing, xdivergence, ypointing, ydivergence by window slice. */
 void orc_diag_field_fft(int ns, int ngrid, double gridmax, double lambda0, int harm, const double *field,

@@ -70,6 +70,8 @@ class _Lib:
             L.orc_diag_beam.argtypes = [_i, _i, _pd, _i, _pd]
             L.orc_diag_field.argtypes = [_i, _i, _d, _d, _i, _pd, _i, _pd]
             L.orc_diag_field_fft.argtypes = [_i, _i, _d, _d, _i, _pd, _i, _pd]
+            L.orc_diag_global_beam.argtypes = [_i, _i, _pd, _pd, _pd]
+            L.orc_diag_global_field.argtypes = [_i, _i, _d, _d, _i, _d, _pd, _pd]
             L.orc_deposit_source.argtypes = [_pd, _i, _i, _i, _pd, _pd, _d, _i, _i, _d, _pd]
             L.orc_adi_advance.argtypes = [_i, _i, _i, _d, _d, _d, _pd, _pd]
 
@@ -157,6 +159,25 @@ class _Lib:
         out = np.zeros((ns, len(DF_COLS)))
         self.lib.orc_diag_field(ns, ngrid, gridmax, lambda0, harm, _ptr(f.view(np.float64)),
                                 int(first), _ptr(out))
+        return out
+
+    def diag_global_beam(self, particles, current):
+        """Window values of the beam [6] (energy, energyspread, x/y position and size)."""
+        part = np.ascontiguousarray(particles, dtype=np.float64)
+        out = np.zeros(6)
+        self.lib.orc_diag_global_beam(part.shape[0], part.shape[1], _ptr(part),
+                                      _ptr(np.ascontiguousarray(current, dtype=np.float64)), _ptr(out))
+        return out
+
+    def diag_global_field(self, field, gridmax, lambda0, harm, sample):
+        """Window values of one field [11] (energy J, x/y position and size, mean near-
+        and far-field intensity, far-field pointing and divergence)."""
+        f = np.ascontiguousarray(field, dtype=np.complex128)
+        ns = f.shape[0]
+        ngrid = int(round(np.sqrt(f.shape[1])))
+        out = np.zeros(11)
+        self.lib.orc_diag_global_field(ns, ngrid, gridmax, lambda0, harm, sample, _ptr(f.view(np.float64)),
+                                       _ptr(out))
         return out
 
     def diag_field_fft(self, field, gridmax, lambda0, harm, first):

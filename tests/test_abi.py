@@ -92,3 +92,41 @@ def test_large_shot_noise_window_is_sequential_in_slice_order(lib, oracle):
     a = g4gpu.host_load_beam(sp, 0, 32, 4, 7, 1, 1e-10, 1.0)
     b = oracle.load_beam(sp, 0, 32, 4, 7, 1, 1e-10, 1.0)
     assert np.array_equal(a, b)
+
+
+def test_window_values_rebuilt_from_slices_match_reference_sums(lib, oracle):
+    """g4gpu_diag_global (host only) rebuilds the window ("Global/") values from the
+    per-slice diagnostics; the oracle forms them from the raw sums over particles and
+    cells as DiagBeam / DiagField do (Diagnostic.cpp:551-606, 902-975). Uneven
+    currents, a window whose slices differ in power, two fields at harmonics 1 and 3."""
+    import g4gpu
+    import g4cases as T
+    ns, npart, ng = 5, 64, 21
+    gms, lam, sample = [6e-5, 4e-5], 1e-10, 1.0
+    part = oracle.load_beam(T.slice_params(ns, 11357.8, 2.0, 0.4e-6, 15.0), 0, npart, 4, 3, 1, lam, sample)
+    part[..., 2] += np.linspace(0, 3e-6, ns)[:, None]  # slices with different centroids
+    cur = np.array([500.0, 3000.0, 2500.0, 1200.0, 3000.0])
+    x = np.arange(ng) - 0.5 * (ng - 1)
+    g = np.exp(-((x[None, :] - 1.0) ** 2 + (x[:, None] + 0.5) ** 2) / (0.05 * ng * ng))
+    fld = np.stack([np.stack([(g * (1 + s) * np.exp(1j * (0.1 * s + 0.05 * k) * x[None, :])).ravel() * 1e4
+                              for s in range(ns)]) for k in range(2)])
+    first = 2
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, harm=[1, 3], gridmax=gms, lambda0=lam, sample=sample,
+                       gammaref=11357.8)
+    bd = oracle.diag_beam(part, 1)
+    fd = np.stack([oracle.diag_field(fld[k], gms[k], lam, h, first) for k, h in enumerate([1, 3])])
+    qd = np.stack([oracle.diag_field_fft(fld[k], gms[k], lam, h, first) for k, h in enumerate([1, 3])])
+    # the per-slice outputs are by window slice; the current too
+    cur_w = cur
+    bg, fg = g4gpu.diag_global(cfg, 1, cur_w, bd, fd, qd)
+    want_b = oracle.diag_global_beam(part, cur_w)
+    assert np.allclose(bg, want_b, rtol=1e-9, atol=1e-12 * np.abs(want_b).max())
+    for k, h in enumerate([1, 3]):
+        want_f = oracle.diag_global_field(fld[k], gms[k], lam, h, sample)
+        for col in range(len(want_f)):
+            scale = abs(want_f[col]) if col in (0, 5, 6) else np.abs(want_f[[1, 2, 3, 4]]).max() \
+                if col <= 4 else np.abs(want_f[7:]).max()
+            assert abs(fg[k][col] - want_f[col]) <= 1e-9 * scale, (k, col, fg[k][col], want_f[col])
+    # without the far-field input the far-field columns are zero
+    _, fg0 = g4gpu.diag_global(cfg, 1, None, None, fd, None)
+    assert np.all(fg0[:, 7:] == 0) and np.allclose(fg0[:, :7], fg[:, :7])
