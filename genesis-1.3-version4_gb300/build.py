@@ -12,6 +12,7 @@ and g++. The library is built in-tree and is what include/g4gpu.h describes.
   g4gpu_api.cpp      C ABI, host bookkeeping (-ffp-contract=off)
   host_loading.cpp   bit-exact host loading (-ffp-contract=off)
   g4gpu_learned.cpp  learned closure: MLP object, features / corrections, coarse-step driver
+  g4gpu_dpi.cpp      diagnostic plugins (DPI) of the reference's plugin interface, fed from the engine
 """
 import concurrent.futures as cf
 import os
@@ -52,6 +53,7 @@ def _units():
         ("g4gpu_api.cpp", cxx_common),
         ("host_loading.cpp", cxx_common + ["-pthread"]),
         ("g4gpu_learned.cpp", cxx_common),
+        ("g4gpu_dpi.cpp", cxx_common),
     ]
 
 
@@ -82,7 +84,7 @@ def build(force=False, verbose=False):
     with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:
         objs = list(ex.map(lambda u: _compile(*u), units))
     tmp = LIB + ".tmp"
-    cmd = ["nvcc", "-shared", "-o", tmp] + ARCH + objs + ["-lpthread"]
+    cmd = ["nvcc", "-shared", "-o", tmp] + ARCH + objs + ["-lpthread", "-ldl"]
     if verbose:
         print(" ".join(cmd))
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -997,6 +997,12 @@ int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out) {
   return G4GPU_OK;
 }
 
+int g4gpu_get_config(g4gpu_handle h, g4gpu_config *cfg) {
+  if (!h || !cfg) return fail(h, G4GPU_ERR_ARG, "null argument");
+  *cfg = h->cfg;
+  return G4GPU_OK;
+}
+
 int g4gpu_diag_global(const g4gpu_config *cfg, int nharm, const double *current, const double *beam_diag,
                       const double *field_diag, const double *fft_diag, double *beam_global,
                       double *field_global) {

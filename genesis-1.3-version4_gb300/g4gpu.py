@@ -39,6 +39,7 @@ DB_COLS = ["energy", "energyspread", "xposition", "xsize", "yposition", "ysize",
 DF_COLS = ["power", "xposition", "xsize", "yposition", "ysize", "intensity-nearfield",
            "phase-nearfield", "intensity-farfield", "phase-farfield"]
 DFFT_COLS = ["xpointing", "xdivergence", "ypointing", "ydivergence"]
+G4GPU_DPI_FIELD, G4GPU_DPI_BEAM = 0, 1
 DBG_COLS = ["energy", "energyspread", "xposition", "xsize", "yposition", "ysize"]
 DFG_COLS = ["energy", "xposition", "xsize", "yposition", "ysize", "intensity-nearfield",
             "intensity-farfield", "xpointing", "xdivergence", "ypointing", "ydivergence"]
@@ -48,7 +49,10 @@ KERNEL_CLASSES = ["push", "adi_x", "adi_y", "fft", "slip", "diag", "misc"]
 ABI_SYMBOLS = [
     "g4gpu_config_defaults", "g4gpu_create", "g4gpu_destroy", "g4gpu_last_error",
     "g4gpu_set_lattice", "g4gpu_load_beam", "g4gpu_get_beam", "g4gpu_load_field",
-    "g4gpu_get_field", "g4gpu_run", "g4gpu_synchronize", "g4gpu_diag", "g4gpu_run_diag", "g4gpu_diag_fft", "g4gpu_diag_global", "g4gpu_get_stream",
+    "g4gpu_get_field", "g4gpu_run", "g4gpu_synchronize", "g4gpu_diag", "g4gpu_run_diag", "g4gpu_diag_fft", "g4gpu_diag_global", "g4gpu_get_config",
+    "g4gpu_dpi_open", "g4gpu_dpi_kind", "g4gpu_dpi_nobj", "g4gpu_dpi_multi", "g4gpu_dpi_obj_name",
+    "g4gpu_dpi_info", "g4gpu_dpi_field", "g4gpu_dpi_beam", "g4gpu_dpi_field_from", "g4gpu_dpi_beam_from",
+    "g4gpu_dpi_close", "g4gpu_get_stream",
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
     "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc",
     "g4gpu_set_graph_mode", "g4gpu_autotune", "g4gpu_batch_create", "g4gpu_batch_destroy",
@@ -135,6 +139,18 @@ def load_library(path=None):
     L.g4gpu_run_diag.argtypes = [vp, i, i, i, vp, vp]
     L.g4gpu_diag_fft.argtypes = [vp, vp]
     L.g4gpu_diag_global.argtypes = [P(Config), i, vp, vp, vp, vp, vp, vp]
+    L.g4gpu_get_config.argtypes = [vp, P(Config)]
+    L.g4gpu_dpi_open.argtypes = [ctypes.c_char_p, ctypes.c_char_p, i, P(vp), ctypes.c_char_p, i]
+    for nm in ("g4gpu_dpi_kind", "g4gpu_dpi_nobj", "g4gpu_dpi_multi"):
+        getattr(L, nm).argtypes = [vp]
+    L.g4gpu_dpi_obj_name.argtypes = [vp, i, ctypes.c_char_p, i]
+    L.g4gpu_dpi_info.argtypes = [vp, ctypes.c_char_p, i]
+    L.g4gpu_dpi_field.argtypes = [vp, i, i, i, d, d, i, vp, i, vp]
+    L.g4gpu_dpi_beam.argtypes = [vp, i, i, i, vp, vp]
+    L.g4gpu_dpi_field_from.argtypes = [vp, vp, i, i, vp]
+    L.g4gpu_dpi_beam_from.argtypes = [vp, vp, i, vp]
+    L.g4gpu_dpi_close.argtypes = [vp]
+    L.g4gpu_dpi_close.restype = None
     L.g4gpu_get_stream.argtypes = [vp, P(vp)]
     L.g4gpu_set_profiling.argtypes = [vp, i]
     L.g4gpu_kernel_stats.argtypes = [vp, P(ctypes.c_longlong), pd]
@@ -428,6 +444,71 @@ def diag_global(cfg, nharm, current=None, beam_diag=None, field_diag=None, fft_d
     if rc != 0:
         raise G4Error(rc, "g4gpu_diag_global: bad arguments")
     return bg, fg
+
+
+class Plugin:
+    """A diagnostic plugin (DPI) built against the reference's plugin interface.
+    field()/beam() return {object name: [nslice] values by window slice}."""
+
+    def __init__(self, libfile, parameter="", verbose=0):
+        self.L = _lib()
+        self.p = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(512)
+        rc = self.L.g4gpu_dpi_open(os.fsencode(libfile), parameter.encode(), int(verbose), ctypes.byref(self.p),
+                                   err, 512)
+        if rc != 0:
+            raise G4Error(rc, err.value.decode())
+        self.kind = self.L.g4gpu_dpi_kind(self.p)
+        self.multi = bool(self.L.g4gpu_dpi_multi(self.p))
+        buf = ctypes.create_string_buffer(512)
+        self.names = []
+        for k in range(self.L.g4gpu_dpi_nobj(self.p)):
+            self.L.g4gpu_dpi_obj_name(self.p, k, buf, 512)
+            self.names.append(buf.value.decode())
+        self.L.g4gpu_dpi_info(self.p, buf, 512)
+        self.info = buf.value.decode()
+
+    def _named(self, out):
+        return {nm: out[k] for k, nm in enumerate(self.names)}
+
+    def field(self, field, first, iz, harm, ngrid, dgrid, xlambda):
+        f = np.ascontiguousarray(field, dtype=np.complex128)
+        ns = f.shape[0]
+        out = np.zeros((len(self.names), ns))
+        rc = self.L.g4gpu_dpi_field(self.p, int(iz), int(harm), int(ngrid), float(dgrid), float(xlambda), ns,
+                                    _vp(f), int(first), _vp(out))
+        if rc != 0:
+            raise G4Error(rc, "g4gpu_dpi_field")
+        return self._named(out)
+
+    def beam(self, particles, iz):
+        part = np.ascontiguousarray(particles, dtype=np.float64)
+        out = np.zeros((len(self.names), part.shape[0]))
+        rc = self.L.g4gpu_dpi_beam(self.p, int(iz), part.shape[0], part.shape[1], _vp(part), _vp(out))
+        if rc != 0:
+            raise G4Error(rc, "g4gpu_dpi_beam")
+        return self._named(out)
+
+    def field_from(self, handle, ifld, iz):
+        out = np.zeros((len(self.names), handle.cfg.nslice))
+        handle._check(self.L.g4gpu_dpi_field_from(self.p, handle.h, int(ifld), int(iz), _vp(out)))
+        return self._named(out)
+
+    def beam_from(self, handle, iz):
+        out = np.zeros((len(self.names), handle.cfg.nslice))
+        handle._check(self.L.g4gpu_dpi_beam_from(self.p, handle.h, int(iz), _vp(out)))
+        return self._named(out)
+
+    def close(self):
+        if self.p:
+            self.L.g4gpu_dpi_close(self.p)
+            self.p = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def adi_advance_noalloc(field_ptr, source_ptr, nslice, ngrid, first, delz, dgrid, xks, device=0,

@@ -179,6 +179,39 @@ int g4gpu_diag(g4gpu_handle h, int nharm, double *beam_out, double *field_out);
  * handle has none). */
 int g4gpu_diag_fft(g4gpu_handle h, double *out);
 
+/* The handle's configuration (as created). */
+int g4gpu_get_config(g4gpu_handle h, g4gpu_config *cfg);
+
+/* ---- diagnostic plugins (DPI) --------------------------------------------------
+ * Shared libraries built against the reference's plugin interface
+ * (include/DiagnosticPlugin.h, DiagnosticHookS.h, data version 2023092701): field
+ * plugins export factory/destroy, beam plugins factory_beamdiag/destroy_beamdiag.
+ * Replaces LibraryInterface (src/Core/DiagnosticHookLI.cpp) and the feeding of
+ * DiagFieldHook / DiagBeamHook (src/Core/DiagnosticHook.cpp:110-262,
+ * DiagnosticHookBeam.cpp) for a single rank. */
+typedef struct g4gpu_dpi_s *g4gpu_dpi;
+enum { G4GPU_DPI_FIELD = 0, G4GPU_DPI_BEAM = 1 };
+/* Loads the plugin, creates its object and reads its output names (get_infos with
+ * `parameter`); err (errlen bytes) receives a message on failure. */
+int g4gpu_dpi_open(const char *libfile, const char *parameter, int verbose, g4gpu_dpi *out, char *err,
+                   int errlen);
+int g4gpu_dpi_kind(g4gpu_dpi p);   /* G4GPU_DPI_FIELD or G4GPU_DPI_BEAM */
+int g4gpu_dpi_nobj(g4gpu_dpi p);   /* number of output objects */
+int g4gpu_dpi_multi(g4gpu_dpi p);  /* 1: a field plugin that takes all slices at once */
+int g4gpu_dpi_obj_name(g4gpu_dpi p, int i, char *buf, int n);
+int g4gpu_dpi_info(g4gpu_dpi p, char *buf, int n);
+/* A field plugin on host data: field [nslice][ngrid^2] complex in storage order with
+ * ring start `first`; out [nobj][nslice] by window slice (as the reference stores
+ * /Field/<prefix>/<object>). */
+int g4gpu_dpi_field(g4gpu_dpi p, int iz, int harm, int ngrid, double dgrid, double xlambda, int nslice,
+                    const double *field, int first, double *out);
+/* A beam plugin on host data: particles [nslice][npart][6]; out [nobj][nslice]. */
+int g4gpu_dpi_beam(g4gpu_dpi p, int iz, int nslice, int npart, const double *particles, double *out);
+/* The same on the handle's current state (field ifld, or the beam), copied from the device. */
+int g4gpu_dpi_field_from(g4gpu_dpi p, g4gpu_handle h, int ifld, int iz, double *out);
+int g4gpu_dpi_beam_from(g4gpu_dpi p, g4gpu_handle h, int iz, double *out);
+void g4gpu_dpi_close(g4gpu_dpi p);
+
 /* The window values from one state's per-slice diagnostics, on the host (no handle,
  * no device): beam_diag [nslice][G4GPU_DB_NCOL + 2*nharm] with the slices' current
  * [nslice] gives beam_global[G4GPU_DBG_NCOL] (current-weighted, as DiagBeam);

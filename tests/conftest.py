@@ -44,3 +44,21 @@ def lib():
 def golden(name):
     import numpy as np
     return np.load(os.path.join(GOLDEN, name))
+
+
+@pytest.fixture(scope="session")
+def test_plugins(tmp_path_factory):
+    """The test diagnostic plugins (tests/plugins/g4_test_plugin.cpp) built with the
+    host compiler: {"field": ..., "multi": ..., "beam": ...} paths."""
+    import subprocess
+    here = os.path.dirname(os.path.abspath(__file__))
+    src = os.path.join(here, "plugins", "g4_test_plugin.cpp")
+    inc = os.path.join(os.path.dirname(here), "include")
+    out = tmp_path_factory.mktemp("plugins")
+    libs = {}
+    for name, defs in (("field", []), ("multi", ["-DG4_TEST_MULTI"]), ("beam", ["-DG4_TEST_BEAM"])):
+        path = str(out / f"libg4test_{name}.so")
+        subprocess.check_call(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", inc] + defs +
+                              ["-o", path, src])
+        libs[name] = path
+    return libs

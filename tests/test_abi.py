@@ -130,3 +130,82 @@ def test_window_values_rebuilt_from_slices_match_reference_sums(lib, oracle):
     # without the far-field input the far-field columns are zero
     _, fg0 = g4gpu.diag_global(cfg, 1, None, None, fd, None)
     assert np.all(fg0[:, 7:] == 0) and np.allclose(fg0[:, :7], fg[:, :7])
+
+
+def _plugin_field_case(ns=5, ng=13):
+    rng = np.random.default_rng(7)
+    f = (rng.standard_normal((ns, ng * ng)) + 1j * rng.standard_normal((ns, ng * ng))) * (1 + np.arange(ns))[:, None]
+    return f
+
+
+@pytest.mark.parametrize("kind", ["field", "multi"])
+def test_plugin_runner_feeds_slices_by_window_order(lib, test_plugins, kind):
+    """The plugin runner (DiagFieldHook's feeding, DiagnosticHook.cpp:110-262) on a
+    test plugin built against include/g4gpu_dpi_abi.h: slice by slice in storage order
+    or all at once, each value stored at its window slice (is = (ns + is0 - first) % ns)."""
+    import g4gpu
+    ns, ng, first = 5, 13, 3
+    f = _plugin_field_case(ns, ng)
+    with g4gpu.Plugin(test_plugins[kind]) as p:
+        assert p.kind == g4gpu.G4GPU_DPI_FIELD and p.multi == (kind == "multi")
+        assert p.names == ["sum_abs2", "slice", "iz"] and p.info == "test field plugin"
+        out = p.field(f, first, iz=7, harm=1, ngrid=ng, dgrid=1e-6, xlambda=1e-10)
+    for is0 in range(ns):
+        is_ = (ns + is0 - first) % ns
+        assert out["sum_abs2"][is_] == pytest.approx(np.sum(np.abs(f[is0]) ** 2), rel=1e-14)
+    assert np.array_equal(out["slice"], np.arange(ns)) and np.all(out["iz"] == 7)
+
+
+def test_plugin_runner_beam(lib, test_plugins):
+    import g4gpu
+    rng = np.random.default_rng(3)
+    part = rng.standard_normal((4, 16, 6)) + 100.0
+    with g4gpu.Plugin(test_plugins["beam"]) as p:
+        assert p.kind == g4gpu.G4GPU_DPI_BEAM and p.names == ["mean_gamma", "slice"]
+        out = p.beam(part, iz=0)
+    assert np.allclose(out["mean_gamma"], part[..., 0].mean(axis=1), rtol=1e-14)
+    assert np.array_equal(out["slice"], np.arange(4))
+
+
+def test_plugin_runner_rejects_non_plugins(lib, tmp_path):
+    import g4gpu
+    with pytest.raises(g4gpu.G4Error):
+        g4gpu.Plugin(str(tmp_path / "missing.so"))
+    with pytest.raises(g4gpu.G4Error, match="factory"):
+        g4gpu.Plugin(g4gpu.LIB_PATH)  # a library that is no plugin
+
+
+def test_reference_demo_plugins_run_in_the_engine(lib):
+    """The reference's own demo plugins (misc/plugin_demo, built unmodified from their
+    sources into oracle/_ref by oracle/ref_build): the field demo's power agrees with the
+    core's power formula (with the demo's constant eev = 510999.06), the beam demo's
+    x standard deviation with numpy."""
+    import g4gpu
+    here = os.path.dirname(os.path.abspath(__file__))
+    ref = os.path.join(os.path.dirname(here), "oracle", "_ref")
+    fdemo, bdemo = os.path.join(ref, "libdemo.so"), os.path.join(ref, "libbeamdemo.so")
+    if not (os.path.exists(fdemo) and os.path.exists(bdemo)):
+        pytest.skip("the reference's demo plugins are not built here")
+    ns, ng, first, gm, lam = 5, 13, 2, 5e-5, 1e-10
+    f = _plugin_field_case(ns, ng)
+    dgrid = 2 * gm / (ng - 1)
+    try:
+        p = g4gpu.Plugin(fdemo)
+    except g4gpu.G4Error as e:  # built for another machine
+        pytest.skip(str(e))
+    with p:
+        assert p.names == ["my_power", "abc"]
+        out = p.field(f, first, iz=0, harm=1, ngrid=ng, dgrid=dgrid, xlambda=lam)
+    ks = 4 * np.arcsin(1.0) / lam
+    scl = dgrid * 510999.06 / ks
+    for is0 in range(ns):
+        want = np.sum(np.abs(f[is0]) ** 2) * scl * scl / 376.73
+        assert out["my_power"][(ns + is0 - first) % ns] == pytest.approx(want, rel=1e-13)
+    assert np.all(out["abc"] == 42.0)
+    rng = np.random.default_rng(5)
+    part = rng.standard_normal((3, 32, 6))
+    with g4gpu.Plugin(bdemo) as p:
+        assert p.names == ["xstd", "the_answer"]
+        out = p.beam(part, iz=0)
+    assert np.allclose(out["xstd"], part[..., 2].std(axis=1), rtol=1e-13)
+    assert np.all(out["the_answer"] == 42.0)

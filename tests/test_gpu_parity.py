@@ -586,3 +586,37 @@ def test_far_field_diagnostics_match_oracle(lib, oracle, prec, ng, solver):
         for col in range(4):
             scale = np.max(np.abs(want[:, col | 1]))  # pointing on the divergence's scale
             assert np.max(np.abs(got[k][:, col] - want[:, col])) <= tol * scale, (k, col)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_plugins_fed_from_the_device(lib, test_plugins, prec):
+    """Diagnostic plugins fed from a handle's state (g4gpu_dpi_field_from /
+    g4gpu_dpi_beam_from): the values a plugin computes equal those of the host arrays
+    g4gpu_get_field / g4gpu_get_beam return, by window slice, in both field modes."""
+    import g4gpu
+    import g4cases as T
+    ns, npart, ng = 6, 64, 21
+    lat = T.undulator_lattice(1.7, 0.015, 3, 1, 1e-10, 11357.8)
+    part = g4gpu.host_load_beam(T.slice_params(ns, 11357.8, 1.0, 0.4e-6, 15.0), 0, npart, 4, 9, 1, 1e-10, 1.0)
+    g1 = g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e5, 20e-6), 6e-5, ng)
+    fld = np.stack([g1 * (1 + 0.3 * k) for k in range(ns)])
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, gridmax=6e-5, lambda0=1e-10, sample=1.0,
+                       gammaref=11357.8, precision=prec, time_run=1)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam(part, np.full(ns, 3000.0))
+        h.load_field(0, fld)
+        h.run(0, 3)  # the ring start moves with slippage
+        f, first, _ = h.get_field(0)
+        beam = h.get_beam()
+        for kind in ("field", "multi"):
+            with g4gpu.Plugin(test_plugins[kind]) as p:
+                out = p.field_from(h, 0, iz=3)
+            for is0 in range(ns):
+                is_ = (ns + is0 - first) % ns
+                assert out["sum_abs2"][is_] == pytest.approx(np.sum(np.abs(f[is0]) ** 2), rel=1e-14)
+            assert np.array_equal(out["slice"], np.arange(ns)) and np.all(out["iz"] == 3)
+        assert first != 0
+        with g4gpu.Plugin(test_plugins["beam"]) as p:
+            out = p.beam_from(h, iz=3)
+        assert np.allclose(out["mean_gamma"], beam[..., 0].mean(axis=1), rtol=1e-14)
