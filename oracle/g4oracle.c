@@ -533,6 +533,9 @@ typedef struct {
   double filt[3];
   cplx *cbet, *cwet, *cc, cstep;
   cplx *k2, *sigm;
+  /* space charge: the slice's short-range field per particle and its long-range loss */
+  const double *sc_ez;
+  double sc_eloss;
 } step_ctx;
 
 /* TrackBeam::track, TrackBeam.cpp:8-116 (no chicane: the lattice has none) */
@@ -639,7 +642,9 @@ static void push_slices(step_ctx *c, int is0, int is1) {
       double x = p->x, y = p->y, px = p->px, py = p->py;
       double awloc = faw(u, x, y);
       double btpar = 1 + px * px + py * py + aw * aw * awloc * awloc;
-      double ez = 0;
+      /* BeamSolver.cpp:61: the short-range field of the particle plus the slice's
+       * long-range loss */
+      double ez = c->sc_ez ? c->sc_ez[ip] + c->sc_eloss : 0;
       cplx rpart[8];
       for (int k = 0; k < c->nfld; k++) {
         int ns = c->ns;
@@ -919,6 +924,153 @@ static void field_slices(step_ctx *c, int ii0, int ii1) {
   free(src);
 }
 
+/* ---- space charge (&efield), EFieldSolver.cpp ------------------------------ */
+static struct {
+  double rmax;
+  int ngrid, nz, nphi, longrange;
+} sc_cfg = {0, 0, 0, 0, 0};
+
+/* The &efield parameters of the following orc_run_steps calls (EField.cpp:19-39;
+ * nz = 0 and longrange = 0 switch space charge off). */
+void orc_set_efield(double rmax, int ngrid, int nz, int nphi, int longrange) {
+  sc_cfg.rmax = rmax;
+  sc_cfg.ngrid = ngrid;
+  sc_cfg.nz = nz;
+  sc_cfg.nphi = nphi;
+  sc_cfg.longrange = longrange;
+}
+
+/* Beam::getSize, Beam.cpp:42-67 */
+static double slice_size(const step_ctx *c, int is) {
+  if (c->current[is] <= 0) return 1;
+  const part_t *b = c->beam + (size_t)is * c->npart;
+  double x1 = 0, x2 = 0, y1 = 0, y2 = 0;
+  int count = 0;
+  for (int ip = 0; ip < c->npart; ip++) {
+    x1 += b[ip].x;
+    x2 += b[ip].x * b[ip].x;
+    y1 += b[ip].y;
+    y2 += b[ip].y * b[ip].y;
+    count++;
+  }
+  if (count == 0) return 1.;
+  x1 /= (double)count;
+  x2 /= (double)count;
+  y1 /= (double)count;
+  y2 /= (double)count;
+  return sqrt(fabs(x2 - x1 * x1)) * sqrt(fabs(y2 - y1 * y1));
+}
+
+/* EFieldSolver::longRange, EFieldSolver.cpp:56-118: eloss[is] = -longESC / eev */
+static void sc_long_range(const step_ctx *c, double slicelength, double *eloss) {
+  int ns = c->ns;
+  if (!sc_cfg.longrange) {
+    for (int i = 0; i < ns; i++) eloss[i] = 0;
+    return;
+  }
+  double gamma = c->gammaref / sqrt(1 + c->st.aw * c->st.aw);
+  double *fsize = malloc(sizeof(double) * ns);
+  for (int i = 0; i < ns; i++) {
+    fsize[i] = slice_size(c, i);
+    if (fsize[i] <= 0) fsize[i] = 1;
+  }
+  double scl = slicelength / 2. / asin(1) / 299792458.0 / 2 / 8.85e-12;
+  for (int i = 0; i < ns; i++) {
+    double efld = 0;
+    for (int j = 0; j < ns; j++) {
+      double ds = (double)(j - i) * slicelength * gamma;
+      double coef = 1 - sqrt(ds * ds / (ds * ds + fsize[j]));
+      double sgn = (j > i) ? -1. : ((j < i) ? 1. : 0.);
+      efld += sgn * coef * scl * c->current[j] / fsize[j];
+    }
+    eloss[i] = -efld / kEev;
+  }
+  free(fsize);
+}
+
+/* EFieldSolver::shortRange with analyseBeam, constructLaplaceOperator and tridiag,
+ * EFieldSolver.cpp:120-272: ez[npart] of slice is; *rmax carries the radial grid's
+ * extent from slice to slice (it grows to 1.5 times a slice's extreme radius) */
+static void sc_short_range(const step_ctx *c, int is, double *rmax, double *ez) {
+  int npart = c->npart, ng = sc_cfg.ngrid;
+  for (int i = 0; i < npart; i++) ez[i] = 0;
+  if (!(sc_cfg.nz > 0 && ng > 2) || npart < 1) return;
+  const part_t *b = c->beam + (size_t)is * npart;
+  double xcen = 0, ycen = 0;
+  for (int i = 0; i < npart; i++) {
+    xcen += b[i].x;
+    ycen += b[i].y;
+  }
+  xcen /= (double)npart;
+  ycen /= (double)npart;
+  double rbound = 0;
+  for (int i = 0; i < npart; i++) {
+    double tx = b[i].x - xcen, ty = b[i].y - ycen, rad2 = tx * tx + ty * ty;
+    if (rad2 > rbound) rbound = rad2;
+  }
+  rbound = sqrt(rbound);
+  if (rbound > *rmax) *rmax = rbound * 1.5;
+  double dr = *rmax / (double)(ng - 1);
+  cplx *cwork = malloc(sizeof(cplx) * npart);
+  int *idxr = malloc(sizeof(int) * npart);
+  for (int i = 0; i < npart; i++) {
+    double tx = b[i].x - xcen, ty = b[i].y - ycen, radi = sqrt(tx * tx + ty * ty);
+    cwork[i] = CMPLX(tx / radi, ty / radi);
+    idxr[i] = (int)floor(radi / dr);
+  }
+  double pi = 2 * asin(1);
+  double *vol = malloc(sizeof(double) * ng), *ldig = malloc(sizeof(double) * (ng + 1));
+  double *rlog = malloc(sizeof(double) * ng), *lmid = malloc(sizeof(double) * ng);
+  cplx *csrc = malloc(sizeof(cplx) * ng), *clow = malloc(sizeof(cplx) * ng), *cmid = malloc(sizeof(cplx) * ng);
+  cplx *cupp = malloc(sizeof(cplx) * ng), *celm = malloc(sizeof(cplx) * ng), *gam = malloc(sizeof(cplx) * ng);
+  vol[0] = pi * dr * dr;
+  rlog[0] = 0.5;
+  ldig[0] = 0;
+  for (int j = 1; j < ng; j++) {
+    vol[j] = pi * dr * dr * (2 * j + 1);
+    ldig[j] = 2 * pi * j;
+    rlog[j] = log((double)(j + 1) / (double)j);
+  }
+  ldig[ng] = 0;
+  double ks = 4 * asin(1) / c->reflength;
+  double gz2 = c->gammaref * c->gammaref / (1 + c->st.aw * c->st.aw);
+  double coef = -gz2 / ks / ks;
+  double econst = kVacimp / kEev * c->current[is] / ks / (double)npart;
+  for (int m = -sc_cfg.nphi; m <= sc_cfg.nphi; m++) {
+    for (int i = 0; i < ng; i++) lmid[i] = -ldig[i] - ldig[i + 1] - 2. * pi * m * m * rlog[i];
+    lmid[ng - 1] -= 2 * pi * ng;
+    for (int l = 1; l <= sc_cfg.nz; l++) {
+      for (int i = 0; i < ng; i++) csrc[i] = 0;
+      for (int i = 0; i < npart; i++)
+        csrc[idxr[i]] += cpow(cwork[i], -m) * CMPLX(cos(l * b[i].theta), -sin(l * b[i].theta));
+      for (int i = 0; i < ng; i++) {
+        csrc[i] *= CMPLX(0, econst / l / vol[i]);
+        clow[i] = coef * ldig[i] / l / l / vol[i];
+        cmid[i] = 1 + coef * lmid[i] / l / l / vol[i];
+        cupp[i] = coef * ldig[i + 1] / l / l / vol[i];
+      }
+      /* tridiag */
+      cplx bet = cmid[0];
+      celm[0] = csrc[0] / bet;
+      for (int i = 1; i < ng; i++) {
+        gam[i] = cupp[i - 1] / bet;
+        bet = cmid[i] - clow[i] * gam[i];
+        celm[i] = (csrc[i] - clow[i] * celm[i - 1]) / bet;
+      }
+      for (int i = ng - 2; i > -1; i--) celm[i] = celm[i] - gam[i + 1] * celm[i + 1];
+      for (int i = 0; i < npart; i++) {
+        cplx ctemp = cpow(cwork[i], m) * CMPLX(cos(l * b[i].theta), sin(l * b[i].theta));
+        ez[i] += 2 * creal(ctemp * celm[idxr[i]]);
+      }
+    }
+  }
+  free(cwork), free(idxr), free(vol), free(ldig), free(rlog), free(lmid);
+  free(csrc), free(clow), free(cmid), free(cupp), free(celm), free(gam);
+}
+
+static void run_transverse_first(void *ctx, int i0, int i1) { transverse_slices((step_ctx *)ctx, i0, i1, 0); }
+static void run_transverse_second(void *ctx, int i0, int i1) { transverse_slices((step_ctx *)ctx, i0, i1, 1); }
+
 static void run_push(void *ctx, int i0, int i1) {
   step_ctx *c = (step_ctx *)ctx;
   transverse_slices(c, i0, i1, 0);
@@ -985,6 +1137,7 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
   c.cwet = coef + 2 * ngrid;
   int fft_ready[8] = {0};
   cplx *fft_tabs = NULL;
+  double sc_rmax = sc_cfg.rmax; /* the radial grid's extent, grown over the run */
   if (solver) fft_tabs = malloc(sizeof(cplx) * 2 * n2 * nfld);
 
   for (int istep = 0; istep < nsteps; istep++) {
@@ -1002,7 +1155,26 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
       c.xks_fund = xks;
       c.xku = c.st.ku;
       if (c.xku == 0) c.xku = xks * 0.5 / gammaref / gammaref;
-      parallel_for(ns, nthreads, run_push, &c);
+      if (sc_cfg.longrange || (sc_cfg.nz > 0 && sc_cfg.ngrid > 2)) {
+        /* Beam::track with space charge (Beam.cpp:97-112, BeamSolver.cpp:43-61): the
+         * first transverse half step of every slice, the long-range loss of every
+         * slice, then slice by slice the short-range field and the push */
+        parallel_for(ns, nthreads, run_transverse_first, &c);
+        double *eloss = malloc(sizeof(double) * ns), *ez = malloc(sizeof(double) * npart);
+        sc_long_range(&c, reflength * sample, eloss);
+        for (int is = 0; is < ns; is++) {
+          sc_short_range(&c, is, &sc_rmax, ez);
+          c.sc_ez = ez;
+          c.sc_eloss = eloss[is];
+          push_slices(&c, is, is + 1);
+        }
+        c.sc_ez = NULL;
+        free(eloss);
+        free(ez);
+        parallel_for(ns, nthreads, run_transverse_second, &c);
+      } else {
+        parallel_for(ns, nthreads, run_push, &c);
+      }
     }
     if (stages & ORC_STAGE_FIELD) {
       for (int k = 0; k < nfld; k++) {

@@ -96,6 +96,11 @@ enum {
 };
 void orc_diag_field(int ns, int ngrid, double gridmax, double lambda0, int harm,
                     const double *field, int first, double *out);
+/* Space charge (&efield, EField.cpp:19-39) for the following orc_run_steps calls:
+ * radial grid extent rmax (grown as the reference does), ngrid radial points, nz
+ * longitudinal and nphi azimuthal modes of the short-range field, longrange the
+ * long-range loss. nz = 0 and longrange = 0 switch it off (the default). */
+void orc_set_efield(double rmax, int ngrid, int nz, int nphi, int longrange);
 /* Window ("Global/") values from the raw sums: DiagBeam (Diagnostic.cpp:551-606),
  * out[6] = energy, energyspread, xposition, xsize, yposition, ysize; DiagField
  * (Diagnostic.cpp:902-975), out[11] = energy [J], xposition, xsize, yposition, ysize,

@@ -75,6 +75,12 @@ class _Lib:
             L.orc_deposit_source.argtypes = [_pd, _i, _i, _i, _pd, _pd, _d, _i, _i, _d, _pd]
             L.orc_adi_advance.argtypes = [_i, _i, _i, _d, _d, _d, _pd, _pd]
 
+    def set_efield(self, rmax=0.0, ngrid=0, nz=0, nphi=0, longrange=False):
+        """Space charge (&efield) for the following run_steps calls; the defaults switch it off."""
+        f = getattr(self.lib, self.p + "set_efield")
+        f.argtypes = [_d, _i, _i, _i, _i]
+        f(float(rmax), int(ngrid), int(nz), int(nphi), int(bool(longrange)))
+
     def ran2(self, seed, n):
         out = np.zeros(n)
         getattr(self.lib, self.p + "ran2")(seed, n, _ptr(out))

@@ -55,7 +55,20 @@ static void fill_undulator(Undulator *und, int nsteps, const double *tab, double
   und->updateOutput(1);
 }
 
+// &efield parameters applied to the Beam of the following g4ref_run_steps calls
+// (EField.cpp:38: Beam::initEField); nz = 0 and longrange = 0 leave space charge off.
+static double g_sc_rmax = 0;
+static int g_sc_ngrid = 0, g_sc_nz = 0, g_sc_nphi = 0, g_sc_longrange = 0;
+
 extern "C" {
+
+void g4ref_set_efield(double rmax, int ngrid, int nz, int nphi, int longrange) {
+  g_sc_rmax = rmax;
+  g_sc_ngrid = ngrid;
+  g_sc_nz = nz;
+  g_sc_nphi = nphi;
+  g_sc_longrange = longrange;
+}
 
 // Runs `nsteps` reference integration steps in place.
 //   particles: [ns][npart][6] (gamma, theta, x, y, px, py)
@@ -71,6 +84,8 @@ int g4ref_run_steps(int nsteps, const double *tab, double gammaref, int ns, int 
 
   Beam beam;
   beam.init(ns, 1, reflength, reflength * sample, 0.0, false);
+  if (g_sc_nz > 0 || g_sc_longrange)
+    beam.initEField(g_sc_rmax, g_sc_ngrid, g_sc_nz, g_sc_nphi, reflength, g_sc_longrange != 0);
   for (int is = 0; is < ns; is++) {
     beam.current[is] = current[is];
     beam.beam[is].resize(npart);

@@ -13,6 +13,10 @@ Fixtures (numpy .npz):
                  lattice table, loaded beam, per-step power / bunching / energy
   config0.npz    the 443-step steady-state deck of the planar FODO configuration:
                  lattice table, loaded beam, per-step power / bunching / energy
+  spacecharge.npz integration steps with space charge (&efield): short-range modes,
+                 the long-range loss, both; input state, parameters and output state
+
+`python tests/golden/gen_golden.py spacecharge` regenerates only spacecharge.npz.
 
 The reference's CI check of Example1 (examples/Example1-SteadyState/TEST_power.py)
 expects a final power of 0.932785e9 W within 30 %; example1.npz records what the
@@ -162,6 +166,47 @@ def gen_steps(r):
     np.savez_compressed(os.path.join(HERE, "steps.npz"), **d)
 
 
+def sc_cases(r):
+    """Windows with space charge: the short-range field (radial grid grown from rmax 0),
+    the long-range loss, and both in steady state with a fixed radial grid."""
+    cases = []
+    lat = T.undulator_lattice(1.7, 0.015, 6, 2, 1e-10, 11357.8, quad_k1=1.5, quad_l=0.08)
+    cur = np.array([3000.0, 2500.0, 1000.0, 3000.0])
+    part = r.load_beam(T.slice_params(4, 11357.8, 2.0, 0.4e-6, 15.0, currents=cur), 0, 64, 4, 7, 1, 1e-10, 1.0)
+    gh = r.gauss_hermite(T.gauss_field_par(1e-10, 1e5, 20e-6), 6e-5, 25)
+    fld = np.stack([gh * (1 + 0.2j * k) for k in range(4)])[None]
+    base = dict(lat=lat, gammaref=11357.8, part=part, cur=cur, harm=[1], gridmax=[6e-5], fields=fld, first=[0],
+                time_run=1, periodic=0)
+    cases.append(dict(base, name="short", efield=[0.0, 24, 2, 1, 0]))
+    cases.append(dict(base, name="long", efield=[0.0, 0, 0, 0, 1]))
+    cases.append(dict(base, name="both", efield=[0.0, 16, 1, 2, 1]))
+    lat1 = T.undulator_lattice(1.7, 0.015, 10, 1, 1e-10, 11357.8)
+    part1 = r.load_beam(T.slice_params(1, 11357.8, 2.0, 0.4e-6, 15.0), 0, 96, 4, 1, 0, 1e-10, 1.0)
+    gh1 = r.gauss_hermite(T.gauss_field_par(1e-10, 1e6, 15e-6), 6e-5, 21)
+    cases.append(dict(name="steady", lat=lat1, gammaref=11357.8, part=part1, cur=np.array([3000.0]), harm=[1],
+                      gridmax=[6e-5], fields=gh1[None, None], first=[0], time_run=0, periodic=0,
+                      efield=[5e-5, 30, 3, 2, 1]))
+    return cases
+
+
+def gen_space_charge(r):
+    d = {}
+    for c in sc_cases(r):
+        n = c["name"]
+        for k in ("lat", "part", "cur", "harm", "gridmax", "fields", "first", "efield"):
+            d[f"{n}_{k}"] = np.asarray(c[k])
+        d[f"{n}_args"] = np.array([c["gammaref"], c["time_run"], c["periodic"]])
+        rmax, ngrid, nz, nphi, longrange = c["efield"]
+        r.set_efield(rmax, int(ngrid), int(nz), int(nphi), bool(longrange))
+        out = r.run_steps(c["lat"], c["gammaref"], c["part"], c["cur"], 1e-10, 1.0, c["harm"], c["gridmax"],
+                          c["fields"], c["first"], time_run=c["time_run"], periodic=c["periodic"], stages=7)
+        r.set_efield()
+        d[f"{n}_out_part"] = out[0]
+        d[f"{n}_out_fields"] = out[1]
+        d[f"{n}_out_first"] = out[2]
+    np.savez_compressed(os.path.join(HERE, "spacecharge.npz"), **d)
+
+
 LAT_FROM_OUT = {"aw": "aw", "ax": "ax", "ay": "ay", "ku": "ku", "kx": "kx", "ky": "ky",
                 "gradx": "gradx", "grady": "grady", "qf": "qf", "qx": "qx", "qy": "qy",
                 "cx": "cx", "cy": "cy", "dz": "dz", "slip": "slippage", "phase": "phaseshift",
@@ -260,6 +305,10 @@ def main():
     r = G.reference()
     if r is None or not os.path.exists(GENESIS):
         sys.exit("the reference checker is not built: run oracle/build_oracle.py with the reference present")
+    if sys.argv[1:] == ["spacecharge"]:
+        gen_space_charge(r)
+        return
+    gen_space_charge(r)
     gen_streams(r)
     gen_loading(r)
     gen_steps(r)

@@ -191,3 +191,27 @@ def test_far_field_moments_match_numpy(oracle, n):
         want = [fx1 * sclt, np.sqrt(abs(fx2 - fx1 * fx1)) * sclt, fy1 * sclt, np.sqrt(abs(fy2 - fy1 * fy1)) * sclt]
         is_ = (ns + is0 - first) % ns
         assert np.allclose(got[is_], want, rtol=1e-10, atol=1e-12 * max(abs(v) for v in want))
+
+
+@pytest.mark.parametrize("case", ["short", "long", "both", "steady"])
+def test_space_charge_steps(oracle, case):
+    """Space charge (&efield, EFieldSolver.cpp): the oracle's restatement against the
+    reference run with its own EFieldSolver (tests/golden/spacecharge.npz): the
+    short-range field of nz x (2 nphi + 1) modes on a radial grid grown from the
+    slices' extent, the long-range loss over the window, and both."""
+    d = golden("spacecharge.npz")
+    g = lambda k: d[f"{case}_{k}"]
+    gammaref, time_run, periodic = g("args")
+    rmax, ngrid, nz, nphi, longrange = g("efield")
+    oracle.set_efield(rmax, int(ngrid), int(nz), int(nphi), bool(longrange))
+    try:
+        part, fld, first, _ = oracle.run_steps(g("lat"), gammaref, g("part"), g("cur"), 1e-10, 1.0, g("harm"),
+                                               g("gridmax"), g("fields"), g("first"), time_run=int(time_run),
+                                               periodic=int(periodic), stages=7)
+    finally:
+        oracle.set_efield()
+    # the restatement raises complex powers as exp / log of C99 (cpow), the reference as
+    # C++ std::pow: they differ in the last bits, so 1e-12 even on x86-64
+    assert np.allclose(part, g("out_part"), rtol=1e-12, atol=0)
+    assert np.allclose(fld, g("out_fields"), rtol=1e-12, atol=1e-12 * np.abs(g("out_fields")).max())
+    assert np.array_equal(first, g("out_first"))
