@@ -391,7 +391,7 @@ void g4gpu_destroy(g4gpu_handle h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   void *ptrs[] = {h->beam.gamma, h->beam.theta, h->beam.x, h->beam.y, h->beam.px, h->beam.py,
                   h->beam.current, h->tmp, h->diag_work, h->coef, h->derr, h->ddiag, h->stage,
-                  h->closure_basis, h->closure_feat, h->closure_corr};
+                  h->closure_basis, h->closure_feat, h->closure_corr, h->sc.st, h->sc.state, h->sc.ez};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
@@ -638,6 +638,43 @@ int g4gpu_get_field(g4gpu_handle h, int ifld, double *field, int *first, double 
 
 // Queues the kernels and copies of steps istep0 .. istep0+nsteps-1 on the handle's
 // stream and advances the host-side ring state (first, accuslip) accordingly.
+int g4gpu_set_efield(g4gpu_handle h, double rmax, int ngrid, int nz, int nphi, int longrange) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (!(rmax >= 0) || ngrid < 0 || nz < 0 || nphi < 0)
+    return fail(h, G4GPU_ERR_ARG, "rmax, ngrid, nz and nphi must be >= 0");
+  const bool shortrange = nz > 0 && ngrid > 2;
+  if (shortrange && g4::sc_bytes_per_mode(ngrid, h->mixed) > g4::sc_max_smem())
+    return fail(h, G4GPU_ERR_ARG, "efield ngrid too large: one radial mode must fit in shared memory");
+  if (shortrange && (long long)(2 * nphi + 1) * nz > (1 << 20))
+    return fail(h, G4GPU_ERR_ARG, "too many space-charge modes");
+  cudaSetDevice(h->cfg.device);
+  const g4gpu_config &c = h->cfg;
+  int rc;
+  if (!h->sc.st) {
+    if ((rc = alloc(h, (void **)&h->sc.st, 6 * (size_t)c.nslice * sizeof(double)))) return rc;
+    // the carried grid extent (a double) and the CTA counter of the moment kernel
+    if ((rc = alloc(h, (void **)&h->sc.state, 2 * sizeof(double)))) return rc;
+    h->sc.count = reinterpret_cast<unsigned *>(h->sc.state + 1);
+  }
+  if (shortrange && !h->sc.ez &&
+      (rc = alloc(h, &h->sc.ez, (size_t)c.nslice * c.npart * h->rsize)))
+    return rc;
+  const double init[2] = {rmax, 0.0};  // the counter's bits are zero
+  G4_CUDA(h, cudaMemcpyAsync(h->sc.state, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+  G4_CUDA(h, cudaMemsetAsync(h->sc.st, 0, 6 * (size_t)c.nslice * sizeof(double), h->stream));
+  G4_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->sc_on = shortrange || longrange;
+  h->sc_ngrid = ngrid;
+  h->sc_nz = nz;
+  h->sc_nphi = nphi;
+  h->sc_longrange = longrange ? 1 : 0;
+  // captured step sequences were recorded without (or with other) space charge
+  for (auto &g : h->graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+  h->graphs.clear();
+  return G4GPU_OK;
+}
+
 static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
   const g4gpu_config &c = h->cfg;
   int ns = c.nslice, np = c.npart, ng = c.ngrid;
@@ -648,6 +685,70 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
   for (int istep = istep0; istep < istep0 + nsteps; istep++) {
     StepConst sc = h->steps[istep];
     for (int k = 0; k < c.nfield; k++) sc.f[k].first = h->first[k];
+    g4::StepConstF scf_push{};
+    if (h->mixed) scf_push = g4::to_float(sc, np);
+    // Beam::track's push (Beam.cpp:97-112). With space charge, BeamSolver::advance
+    // needs every slice after the first transverse half step (EFieldSolver::longRange
+    // reads all slices' sizes): the push runs in two launches around the space-charge
+    // kernels.
+    auto push = [&](void *const *src, int deposit) -> int {
+      if (!h->sc_on) {
+        Timed t(h, G4GPU_K_PUSH);
+        if (h->mixed)
+          g4::launch_push_mixed(L, scf_push, h->beam, h->field, src, ns, np, ng, deposit, h->push_block);
+        else
+          g4::launch_push_plain(L, sc, h->beam, h->field, src, ns, np, ng, deposit, h->push_block);
+        return G4GPU_OK;
+      }
+      const bool shortrange = h->sc_nz > 0 && h->sc_ngrid > 2;
+      const void *ez = shortrange ? h->sc.ez : nullptr;
+      const double *eloss = h->sc_longrange ? h->sc.st + 5 * (size_t)ns : nullptr;
+      {
+        Timed t(h, G4GPU_K_PUSH);
+        if (h->mixed)
+          g4::launch_push_mixed_sc(L, scf_push, h->beam, h->field, nullptr, ns, np, ng, 0, h->push_block, 1,
+                                   nullptr, nullptr);
+        else
+          g4::launch_push_plain_sc(L, sc, h->beam, h->field, nullptr, ns, np, ng, 0, h->push_block, 1,
+                                   nullptr, nullptr);
+      }
+      {
+        g4::ScConst scc{};
+        scc.ns = ns;
+        scc.np = np;
+        scc.ng = h->sc_ngrid;
+        scc.nz = h->sc_nz;
+        scc.nphi = h->sc_nphi;
+        scc.longrange = h->sc_longrange;
+        scc.shortrange = shortrange;
+        if (shortrange) {
+          const long long modes = (long long)(2 * h->sc_nphi + 1) * h->sc_nz;
+          const size_t per = g4::sc_bytes_per_mode(h->sc_ngrid, h->mixed);
+          scc.modes_per_pass = (int)std::max<long long>(1, std::min<long long>(modes, (96 << 10) / per));
+        }
+        // EFieldSolver.cpp:69, 103 and 216-218, with aw of the step (BeamSolver.cpp:40)
+        const double aw = sc.aw;
+        scc.slicelength = c.lambda0 * c.sample;
+        scc.gamma_lr = c.gammaref / std::sqrt(1 + aw * aw);
+        scc.lr_scl = scc.slicelength / 2. / std::asin(1) / 299792458.0 / 2 / 8.85e-12;
+        scc.ks = 4 * std::asin(1) / c.lambda0;
+        const double gz2 = c.gammaref * c.gammaref / (1 + aw * aw);
+        scc.coef = -gz2 / scc.ks / scc.ks;
+        Timed t(h, G4GPU_K_SC, 2);
+        if (h->mixed)
+          g4::launch_sc_mixed(L, scc, h->beam, h->sc);
+        else
+          g4::launch_sc_plain(L, scc, h->beam, h->sc);
+      }
+      Timed t(h, G4GPU_K_PUSH);
+      if (h->mixed)
+        g4::launch_push_mixed_sc(L, scf_push, h->beam, h->field, src, ns, np, ng, deposit, h->push_block, 2, ez,
+                                 eloss);
+      else
+        g4::launch_push_plain_sc(L, sc, h->beam, h->field, src, ns, np, ng, deposit, h->push_block, 2, ez,
+                                 eloss);
+      return G4GPU_OK;
+    };
     bool any_dep = false;
     for (int k = 0; k < c.nfield; k++) any_dep = any_dep || sc.f[k].dep_on;
     // mixed form with the slice in shared memory: deposition and ADI in one kernel,
@@ -658,11 +759,8 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
     for (int k = 0; k < c.nfield; k++) pair_ok = pair_ok && sc.f[k].tw > 0;
     bool pair = pair_ok && (h->field_kernel == 1 || !fused);
     if (fused || pair) {
-      g4::StepConstF scf = g4::to_float(sc, np);
-      if (do_push) {
-        Timed t(h, G4GPU_K_PUSH);
-        g4::launch_push_mixed(L, scf, h->beam, h->field, nullptr, ns, np, ng, 0, h->push_block);
-      }
+      g4::StepConstF scf = scf_push;
+      if (do_push) push(nullptr, 0);
       if (do_field) {
         // the diagnostic record of a step run by g4gpu_run_diag, formed by the fused
         // kernel itself when it holds the scratch for it
@@ -688,13 +786,7 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
     g4::StepConstF scf{};
     if (h->mixed) scf = g4::to_float(sc, np);
     if (do_push) {
-      Timed t(h, G4GPU_K_PUSH);
-      if (h->mixed)
-        g4::launch_push_mixed(L, scf, h->beam, h->field, h->src, ns, np, ng, do_field && any_dep,
-                              h->push_block);
-      else
-        g4::launch_push_plain(L, sc, h->beam, h->field, h->src, ns, np, ng, do_field && any_dep,
-                              h->push_block);
+      push(h->src, do_field && any_dep);
     } else if (do_field && any_dep) {
       Timed t(h, G4GPU_K_PUSH);
       if (h->mixed)
@@ -1243,6 +1335,8 @@ static int backup_state(g4gpu_handle h, StateBackup &b) {
       {h->beam.gamma, np * h->rsize}, {h->beam.theta, np * 8}, {h->beam.x, np * h->rsize},
       {h->beam.y, np * h->rsize},     {h->beam.px, np * h->rsize}, {h->beam.py, np * h->rsize}};
   for (int k = 0; k < c.nfield; k++) live.push_back({h->field[k], nf});
+  // the radial grid extent of the space charge, carried from step to step
+  if (h->sc.state) live.push_back({h->sc.state, 2 * sizeof(double)});
   for (auto &l : live) {
     void *cp = nullptr;
     cudaError_t e = cudaMalloc(&cp, l.second);

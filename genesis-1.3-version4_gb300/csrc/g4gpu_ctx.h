@@ -43,6 +43,10 @@ struct g4gpu_ctx {
   double *diag_rec = nullptr;
   int diag_nharm = 0;
   bool diag_fields_in_step = false;
+  // space charge (g4gpu_set_efield): its parameters and device state
+  bool sc_on = false;
+  int sc_ngrid = 0, sc_nz = 0, sc_nphi = 0, sc_longrange = 0;
+  g4::ScBuffers sc{};
   void *stage = nullptr;     // AoS staging buffer for host transfers
   size_t stage_bytes = 0;
   size_t bytes = 0;

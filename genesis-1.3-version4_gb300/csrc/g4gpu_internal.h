@@ -135,6 +135,43 @@ size_t noalloc_scratch_bytes();
 int adi_noalloc_mixed(int device, void *stream, void *field, const void *source, const float *coef,
                       float cstep, int ns, int ngrid, int first, std::string *msg);
 
+// Space charge (&efield, EFieldSolver.cpp), sc_kernels.cuh, instantiated in
+// kernels_plain.cu (FP64) and kernels_mixed.cu (FP32).
+struct ScConst {
+  int ns, np, ng, nz, nphi;
+  int longrange, shortrange;  // which parts run (EFieldSolver::hasShortRange: nz > 0, ngrid > 2)
+  int modes_per_pass;         // radial modes the short-range kernel holds in shared memory at once
+  double slicelength;         // lambda0 * sample
+  double gamma_lr;            // gammaref / sqrt(1 + aw^2) of the step (EFieldSolver.cpp:69)
+  double lr_scl;              // slicelength / (2 asin 1) / c / 2 / eps0 (EFieldSolver.cpp:103)
+  double ks;                  // 2 pi / lambda0
+  double coef;                // -gammaz^2 / ks^2 of the Laplace operator (EFieldSolver.cpp:217)
+};
+// device state of a handle's space charge
+struct ScBuffers {
+  double *st;       // [6][nslice]: xcen, ycen, size, rbound, rmax of the slice, eloss
+  double *state;    // [1]: the radial grid extent carried over steps
+  unsigned *count;  // CTAs of the moment kernel that finished (reset by the last)
+  void *ez;         // [nslice][npart] R: short-range field per particle
+};
+// shared memory of the short-range kernel per mode, and the largest it takes
+size_t sc_bytes_per_mode(int ng, int mixed);
+size_t sc_max_smem();
+// the moments and the radial grid extents (first kernel), then the long-range loss and
+// the short-range field (second kernel); the particles' x, y must be after the first
+// transverse half step
+void launch_sc_plain(const Launch &L, const ScConst &c, const DeviceBeam &b, const ScBuffers &buf);
+void launch_sc_mixed(const Launch &L, const ScConst &c, const DeviceBeam &b, const ScBuffers &buf);
+// The push in two launches around the space charge: mode 1 the first transverse half
+// step only; mode 2 the rest of the step with ez [nslice][npart] (may be null) plus
+// eloss [nslice] (may be null) in the energy equation. Mode 0 is the whole step.
+void launch_push_plain_sc(const Launch &L, const StepConst &sc, const DeviceBeam &b, void *const *field,
+                          void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
+                          const void *ez, const double *eloss);
+void launch_push_mixed_sc(const Launch &L, const StepConstF &sc, const DeviceBeam &b, void *const *field,
+                          void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
+                          const void *ez, const double *eloss);
+
 // kernels_fft.cu: FFT field solver (FieldSolverFFT::FFT)
 struct FFTPlan {
   int n, nstage;

@@ -170,7 +170,7 @@ __device__ __forceinline__ bool ll_gridpoint_f(float gm, float dg, int ng, float
 
 // e^{-i h a} for the harmonics of one ODE evaluation, a in [-pi, pi] + small
 template <int NF>
-__device__ __forceinline__ void ode_f(const StepConstF &sc, const float2 *rpart, float btpar,
+__device__ __forceinline__ void ode_f(const StepConstF &sc, const float2 *rpart, float btpar, float ez,
                                       float g, float a, float &dgam, float &dth) {
   float2 ctmp = make_float2(0.f, 0.f);
 #pragma unroll
@@ -185,7 +185,7 @@ __device__ __forceinline__ void ode_f(const StepConstF &sc, const float2 *rpart,
   float eps = btper0 / (g * g);
   float s = sqrtf(1.f - eps);
   dth = -sc.xks * eps / (s * (1.f + s)) + sc.xku;
-  dgam = ctmp.y / (s * g);
+  dgam = ctmp.y / (s * g) - ez;
 }
 
 struct PtrsF {
@@ -194,6 +194,12 @@ struct PtrsF {
   const double *current;
   const float2 *field[G4GPU_MAX_FIELDS];
   float2 *src[G4GPU_MAX_FIELDS];
+  // space charge: the short-range field per particle and the long-range loss per
+  // slice (null: zero), and which part of the step a push launch runs (0 all, 1 the
+  // first transverse half step, 2 the rest)
+  const float *ez;
+  const double *eloss;
+  int mode;
 };
 
 // Deposition into the global source grids (FieldSolverADI.cpp:11-52) by a whole
@@ -273,7 +279,18 @@ __global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, 
   long long th = p.theta[o] + sc.autophase_q;
   size_t ncell = (size_t)ng * ng;
 
-  transverse_f(sc, false, g0 + dg, x, y, px, py);
+  if (p.mode != 2) transverse_f(sc, false, g0 + dg, x, y, px, py);
+  if (p.mode == 1) {
+    if (valid) {
+      p.x[o] = x;
+      p.y[o] = y;
+      p.px[o] = px;
+      p.py[o] = py;
+    }
+    return;
+  }
+  // BeamSolver.cpp:50, 61: ez = the particle's short-range field + the slice's loss
+  const float ez = (p.ez ? p.ez[o] : 0.f) + (p.eloss ? (float)p.eloss[is] : 0.f);
 
   // the step works on FP32 offsets from the reduced phase
   float a0 = phase_of(th);
@@ -305,10 +322,10 @@ __global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, 
   // classic RK4 on (gamma offset, phase offset)
   const float h = sc.delz, h2 = 0.5f * sc.delz;
   float k1g, k1t, k2g, k2t, k3g, k3t, k4g, k4t;
-  ode_f<NF>(sc, rpart, btpar, g0 + dg, a0, k1g, k1t);
-  ode_f<NF>(sc, rpart, btpar, g0 + (dg + h2 * k1g), a0 + h2 * k1t, k2g, k2t);
-  ode_f<NF>(sc, rpart, btpar, g0 + (dg + h2 * k2g), a0 + h2 * k2t, k3g, k3t);
-  ode_f<NF>(sc, rpart, btpar, g0 + (dg + h * k3g), a0 + h * k3t, k4g, k4t);
+  ode_f<NF>(sc, rpart, btpar, ez, g0 + dg, a0, k1g, k1t);
+  ode_f<NF>(sc, rpart, btpar, ez, g0 + (dg + h2 * k1g), a0 + h2 * k1t, k2g, k2t);
+  ode_f<NF>(sc, rpart, btpar, ez, g0 + (dg + h2 * k2g), a0 + h2 * k2t, k3g, k3t);
+  ode_f<NF>(sc, rpart, btpar, ez, g0 + (dg + h * k3g), a0 + h * k3t, k4g, k4t);
   const float h6 = sc.delz * (1.f / 6.f);
   float dgam = h6 * (k1g + 2.f * k2g + 2.f * k3g + k4g);
   float dth = h6 * (k1t + 2.f * k2t + 2.f * k3t + k4t);
@@ -1836,17 +1853,47 @@ struct MixedOps {
   }
 };
 
+// FP32 space charge: e^{-i l theta} from the Q32.32 phase, whose l-th multiple is exact
+struct MixedSC {
+  using R = float;
+  using R2 = float2;
+  using Th = long long;
+  static constexpr bool kPlain = false;
+  static __device__ __forceinline__ float2 eil(long long th, int l) {
+    float s, c;
+    __sincosf(phase_of(th, (unsigned)l), &s, &c);
+    return make_float2(c, -s);
+  }
+  static __device__ __forceinline__ float2 eil_step(float2, float2, long long th, int l) { return eil(th, l); }
+};
+
 }  // namespace
 }  // namespace g4
 
 #include "adi_tiled.cuh"
+#include "sc_kernels.cuh"
 
 namespace g4 {
+
+void launch_sc_mixed(const Launch &L, const ScConst &c, const DeviceBeam &b, const ScBuffers &buf) {
+  ScBeam<MixedSC> sb{(const float *)b.x, (const float *)b.y, (const long long *)b.theta, b.current};
+  sc_launch<MixedSC>(L, c, sb, buf);
+}
 
 void launch_push_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,
                        void *const *field, void *const *src, int ns, int np, int ngrid,
                        int deposit, int block) {
+  launch_push_mixed_sc(L, sc, b, field, src, ns, np, ngrid, deposit, block, 0, nullptr, nullptr);
+}
+
+void launch_push_mixed_sc(const Launch &L, const StepConstF &sc, const DeviceBeam &b, void *const *field,
+                          void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
+                          const void *ez, const double *eloss) {
   PtrsF p = make_ptrs_f(b, field, src, sc.nfld);
+  p.mode = mode;
+  p.ez = (const float *)ez;
+  p.eloss = eloss;
+  if (mode == 1) deposit = 0;
   dim3 grid((np + block - 1) / block, ns);
   cudaStream_t s = (cudaStream_t)L.stream;
   switch (sc.nfld) {

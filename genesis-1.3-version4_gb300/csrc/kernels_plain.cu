@@ -104,7 +104,7 @@ __device__ __forceinline__ bool ll_gridpoint(double gm, double dg, int ng, doubl
 
 // BeamSolver::ODE (BeamSolver.cpp:144-163) for NF fields
 template <int NF>
-__device__ __forceinline__ void ode(const StepConst &sc, const C2 *rpart, double btpar,
+__device__ __forceinline__ void ode(const StepConst &sc, const C2 *rpart, double btpar, double ez,
                                     double tgam, double tthet, double &k2gg, double &k2pp) {
   double ztemp1 = -2. / sc.xks;
   C2 ctmp = {0, 0};
@@ -118,7 +118,7 @@ __device__ __forceinline__ void ode(const StepConst &sc, const C2 *rpart, double
   double btper0 = btpar + ztemp1 * ctmp.x;
   double btpar0 = sqrt(1. - btper0 / (tgam * tgam));
   k2pp += sc.xks * (1. - 1. / btpar0) + sc.xku;
-  k2gg += ctmp.y / btpar0 / tgam;  // the space-charge field ez is zero here
+  k2gg += ctmp.y / btpar0 / tgam - ez;
 }
 
 // Deposition of one particle into the source of every field
@@ -164,6 +164,11 @@ struct Ptrs {
   const double *current;
   const double2 *field[G4GPU_MAX_FIELDS];
   double2 *src[G4GPU_MAX_FIELDS];
+  // space charge: the short-range field per particle and the long-range loss per
+  // slice (null: zero), and which part of the step a launch runs (0 all, 1 the first
+  // transverse half step, 2 the rest)
+  const double *ez, *eloss;
+  int mode;
 };
 
 // Beam::track (Beam.cpp:296-311): half transverse step, BeamSolver::advance with
@@ -180,7 +185,16 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   double g = p.gamma[o], th = p.theta[o], x = p.x[o], y = p.y[o], px = p.px[o], py = p.py[o];
   size_t ncell = (size_t)ng * ng;
 
-  transverse(sc, false, g, x, y, px, py);
+  if (p.mode != 2) transverse(sc, false, g, x, y, px, py);
+  if (p.mode == 1) {
+    p.x[o] = x;
+    p.y[o] = y;
+    p.px[o] = px;
+    p.py[o] = py;
+    return;
+  }
+  // BeamSolver.cpp:50, 61: ez = the particle's short-range field + the slice's loss
+  const double ez = (p.ez ? p.ez[o] : 0.) + (p.eloss ? p.eloss[is] : 0.);
 
   // BeamSolver::advance, BeamSolver.cpp:53-80
   double gamma = g, theta = th + sc.autophase;
@@ -208,7 +222,7 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
 
   // BeamSolver::RungeKutta, BeamSolver.cpp:89-141
   double k2gg = 0, k2pp = 0, k3gg, k3pp;
-  ode<NF>(sc, rpart, btpar, gamma, theta, k2gg, k2pp);
+  ode<NF>(sc, rpart, btpar, ez, gamma, theta, k2gg, k2pp);
   double stpz = 0.5 * sc.delz;
   gamma += stpz * k2gg;
   theta += stpz * k2pp;
@@ -216,14 +230,14 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   k3pp = k2pp;
   k2gg = 0;
   k2pp = 0;
-  ode<NF>(sc, rpart, btpar, gamma, theta, k2gg, k2pp);
+  ode<NF>(sc, rpart, btpar, ez, gamma, theta, k2gg, k2pp);
   gamma += stpz * (k2gg - k3gg);
   theta += stpz * (k2pp - k3pp);
   k3gg /= 6;
   k3pp /= 6;
   k2gg *= -0.5;
   k2pp *= -0.5;
-  ode<NF>(sc, rpart, btpar, gamma, theta, k2gg, k2pp);
+  ode<NF>(sc, rpart, btpar, ez, gamma, theta, k2gg, k2pp);
   stpz = sc.delz;
   gamma += stpz * k2gg;
   theta += stpz * k2pp;
@@ -231,7 +245,7 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   k3pp -= k2pp;
   k2gg *= 2;
   k2pp *= 2;
-  ode<NF>(sc, rpart, btpar, gamma, theta, k2gg, k2pp);
+  ode<NF>(sc, rpart, btpar, ez, gamma, theta, k2gg, k2pp);
   gamma += stpz * (k3gg + k2gg / 6.0);
   theta += stpz * (k3pp + k2pp / 6.0);
 
@@ -473,13 +487,54 @@ Ptrs make_ptrs(const DeviceBeam &b, void *const *field, void *const *src, int nf
   return p;
 }
 
+// FP64 space charge in the reference's arithmetic: e^{-i l theta} by products of
+// e^{-i theta} (a relative difference of l ulp from the reference's cos(l theta))
+struct PlainSC {
+  using R = double;
+  using R2 = double2;
+  using Th = double;
+  static constexpr bool kPlain = true;
+  static __device__ __forceinline__ double2 eil(double th, int l) {
+    double s, c;
+    sincos((double)l * th, &s, &c);
+    return make_double2(c, -s);
+  }
+  static __device__ __forceinline__ double2 eil_step(double2 e, double2 e1, double, int) {
+    return make_double2(e.x * e1.x - e.y * e1.y, e.x * e1.y + e.y * e1.x);
+  }
+};
 
 }  // namespace
+}  // namespace g4
+
+#include "sc_kernels.cuh"
+
+namespace g4 {
+
+size_t sc_bytes_per_mode(int ng, int mixed) {
+  return (size_t)ng * (mixed ? sizeof(float2) + sizeof(float) : sizeof(double2) + sizeof(double));
+}
+size_t sc_max_smem() { return 220 * 1024; }
+
+void launch_sc_plain(const Launch &L, const ScConst &c, const DeviceBeam &b, const ScBuffers &buf) {
+  ScBeam<PlainSC> sb{(const double *)b.x, (const double *)b.y, (const double *)b.theta, b.current};
+  sc_launch<PlainSC>(L, c, sb, buf);
+}
 
 void launch_push_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,
                        void *const *field, void *const *src, int ns, int np, int ngrid,
                        int deposit, int block) {
+  launch_push_plain_sc(L, sc, b, field, src, ns, np, ngrid, deposit, block, 0, nullptr, nullptr);
+}
+
+void launch_push_plain_sc(const Launch &L, const StepConst &sc, const DeviceBeam &b, void *const *field,
+                          void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
+                          const void *ez, const double *eloss) {
   Ptrs p = make_ptrs(b, field, src, sc.nfld);
+  p.mode = mode;
+  p.ez = (const double *)ez;
+  p.eloss = eloss;
+  if (mode == 1) deposit = 0;
   dim3 grid((np + block - 1) / block, ns);
   cudaStream_t s = (cudaStream_t)L.stream;
   switch (sc.nfld) {

@@ -43,13 +43,13 @@ G4GPU_DPI_FIELD, G4GPU_DPI_BEAM = 0, 1
 DBG_COLS = ["energy", "energyspread", "xposition", "xsize", "yposition", "ysize"]
 DFG_COLS = ["energy", "xposition", "xsize", "yposition", "ysize", "intensity-nearfield",
             "intensity-farfield", "xpointing", "xdivergence", "ypointing", "ydivergence"]
-KERNEL_CLASSES = ["push", "adi_x", "adi_y", "fft", "slip", "diag", "misc"]
+KERNEL_CLASSES = ["push", "adi_x", "adi_y", "fft", "slip", "diag", "misc", "sc"]
 
 # exported symbols of include/g4gpu.h
 ABI_SYMBOLS = [
     "g4gpu_config_defaults", "g4gpu_create", "g4gpu_destroy", "g4gpu_last_error",
     "g4gpu_set_lattice", "g4gpu_load_beam", "g4gpu_get_beam", "g4gpu_load_field",
-    "g4gpu_get_field", "g4gpu_run", "g4gpu_synchronize", "g4gpu_diag", "g4gpu_run_diag", "g4gpu_diag_fft", "g4gpu_diag_global", "g4gpu_get_config",
+    "g4gpu_get_field", "g4gpu_set_efield", "g4gpu_run", "g4gpu_synchronize", "g4gpu_diag", "g4gpu_run_diag", "g4gpu_diag_fft", "g4gpu_diag_global", "g4gpu_get_config",
     "g4gpu_dpi_open", "g4gpu_dpi_kind", "g4gpu_dpi_nobj", "g4gpu_dpi_multi", "g4gpu_dpi_obj_name",
     "g4gpu_dpi_info", "g4gpu_dpi_field", "g4gpu_dpi_beam", "g4gpu_dpi_field_from", "g4gpu_dpi_beam_from",
     "g4gpu_dpi_close", "g4gpu_get_stream",
@@ -133,6 +133,7 @@ def load_library(path=None):
     L.g4gpu_get_beam.argtypes = [vp, vp]
     L.g4gpu_load_field.argtypes = [vp, i, vp, i, d]
     L.g4gpu_get_field.argtypes = [vp, i, vp, P(i), pd]
+    L.g4gpu_set_efield.argtypes = [vp, d, i, i, i, i]
     L.g4gpu_run.argtypes = [vp, i, i, i]
     L.g4gpu_synchronize.argtypes = [vp]
     L.g4gpu_diag.argtypes = [vp, i, vp, vp]
@@ -380,6 +381,13 @@ class Handle:
 
     def device_bytes(self):
         return int(self.L.g4gpu_device_bytes(self.h))
+
+    def set_efield(self, rmax=0.0, ngrid=100, nz=0, nphi=0, longrange=False):
+        """Space charge for the following steps (&efield: rmax, ngrid, nz, nphi,
+        longrange, with the namelist's defaults); nz = 0 and longrange False switch it
+        off. Resets the radial grid extent to rmax."""
+        self._check(self.L.g4gpu_set_efield(self.h, float(rmax), int(ngrid), int(nz), int(nphi),
+                                            int(bool(longrange))))
 
     def set_graph_mode(self, on):
         self._check(self.L.g4gpu_set_graph_mode(self.h, int(on)))

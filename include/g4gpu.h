@@ -157,6 +157,18 @@ int g4gpu_load_field(g4gpu_handle h, int ifld, const double *field, int first, d
 /* Copies field ifld back (storage order) with its ring start and slippage. */
 int g4gpu_get_field(g4gpu_handle h, int ifld, double *field, int *first, double *accuslip);
 
+/* Space charge for the following steps: the &efield namelist (src/Main/EField.cpp:19-39)
+ * as Beam::initEField passes it to EFieldSolver::init (src/Core/EFieldSolver.cpp:27-48).
+ * rmax: initial extent of the radial grid (it grows to 1.5 times a slice's extreme
+ * radius whenever a slice exceeds it, slice after slice and step after step, as in
+ * EFieldSolver::analyseBeam); ngrid: radial grid points; nz, nphi: longitudinal and
+ * azimuthal modes of the short-range field (l = 1..nz, m = -nphi..nphi); longrange:
+ * the long-range loss from every slice's current and size. The short-range part runs
+ * when nz > 0 and ngrid > 2; all zero switches space charge off. Each call resets the
+ * grid extent to rmax. Replaces EFieldSolver::longRange and shortRange
+ * (EFieldSolver.cpp:56-272) in BeamSolver::advance (src/Core/BeamSolver.cpp:43-61). */
+int g4gpu_set_efield(g4gpu_handle h, double rmax, int ngrid, int nz, int nphi, int longrange);
+
 /* Runs integration steps istep0 .. istep0+nsteps-1 of the lattice on the device,
  * each made of the stages selected by `stages` in the order of Gencore.cpp:118-147.
  * Asynchronous: returns once the work is queued on the handle's stream. */
@@ -243,7 +255,7 @@ int g4gpu_get_stream(g4gpu_handle h, void **stream);
  * (G4GPU_K_*) the launch count and the summed device time in milliseconds of the
  * launches since the last reset. The launch counter runs always. */
 enum { G4GPU_K_PUSH, G4GPU_K_ADI_X, G4GPU_K_ADI_Y, G4GPU_K_FFT, G4GPU_K_SLIP, G4GPU_K_DIAG,
-       G4GPU_K_MISC, G4GPU_K_NCLASS };
+       G4GPU_K_MISC, G4GPU_K_SC, G4GPU_K_NCLASS };
 int g4gpu_set_profiling(g4gpu_handle h, int on);
 int g4gpu_kernel_stats(g4gpu_handle h, long long *launches, double *ms);
 int g4gpu_reset_stats(g4gpu_handle h);

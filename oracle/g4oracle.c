@@ -926,12 +926,13 @@ static void field_slices(step_ctx *c, int ii0, int ii1) {
 
 /* ---- space charge (&efield), EFieldSolver.cpp ------------------------------ */
 static struct {
-  double rmax;
+  double rmax; /* the radial grid's extent, grown over the following runs */
   int ngrid, nz, nphi, longrange;
 } sc_cfg = {0, 0, 0, 0, 0};
 
 /* The &efield parameters of the following orc_run_steps calls (EField.cpp:19-39;
- * nz = 0 and longrange = 0 switch space charge off). */
+ * nz = 0 and longrange = 0 switch space charge off). The grid extent starts at rmax
+ * and, as the reference's EFieldSolver member, carries over from call to call. */
 void orc_set_efield(double rmax, int ngrid, int nz, int nphi, int longrange) {
   sc_cfg.rmax = rmax;
   sc_cfg.ngrid = ngrid;
@@ -988,6 +989,18 @@ static void sc_long_range(const step_ctx *c, double slicelength, double *eloss) 
   free(fsize);
 }
 
+/* std::pow(complex<double>, int) as libstdc++ forms it: binary powering, and the
+ * reciprocal of the power for a negative exponent (z^0 = 1 exactly) */
+static cplx cpow_int(cplx z, int n) {
+  unsigned u = n < 0 ? (unsigned)(-n) : (unsigned)n;
+  cplx y = (u % 2) ? z : 1;
+  while (u >>= 1) {
+    z = z * z;
+    if (u % 2) y = y * z;
+  }
+  return n < 0 ? 1 / y : y;
+}
+
 /* EFieldSolver::shortRange with analyseBeam, constructLaplaceOperator and tridiag,
  * EFieldSolver.cpp:120-272: ez[npart] of slice is; *rmax carries the radial grid's
  * extent from slice to slice (it grows to 1.5 times a slice's extreme radius) */
@@ -1042,7 +1055,7 @@ static void sc_short_range(const step_ctx *c, int is, double *rmax, double *ez) 
     for (int l = 1; l <= sc_cfg.nz; l++) {
       for (int i = 0; i < ng; i++) csrc[i] = 0;
       for (int i = 0; i < npart; i++)
-        csrc[idxr[i]] += cpow(cwork[i], -m) * CMPLX(cos(l * b[i].theta), -sin(l * b[i].theta));
+        csrc[idxr[i]] += cpow_int(cwork[i], -m) * CMPLX(cos(l * b[i].theta), -sin(l * b[i].theta));
       for (int i = 0; i < ng; i++) {
         csrc[i] *= CMPLX(0, econst / l / vol[i]);
         clow[i] = coef * ldig[i] / l / l / vol[i];
@@ -1059,7 +1072,7 @@ static void sc_short_range(const step_ctx *c, int is, double *rmax, double *ez) 
       }
       for (int i = ng - 2; i > -1; i--) celm[i] = celm[i] - gam[i + 1] * celm[i + 1];
       for (int i = 0; i < npart; i++) {
-        cplx ctemp = cpow(cwork[i], m) * CMPLX(cos(l * b[i].theta), sin(l * b[i].theta));
+        cplx ctemp = cpow_int(cwork[i], m) * CMPLX(cos(l * b[i].theta), sin(l * b[i].theta));
         ez[i] += 2 * creal(ctemp * celm[idxr[i]]);
       }
     }
@@ -1137,7 +1150,6 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
   c.cwet = coef + 2 * ngrid;
   int fft_ready[8] = {0};
   cplx *fft_tabs = NULL;
-  double sc_rmax = sc_cfg.rmax; /* the radial grid's extent, grown over the run */
   if (solver) fft_tabs = malloc(sizeof(cplx) * 2 * n2 * nfld);
 
   for (int istep = 0; istep < nsteps; istep++) {
@@ -1163,7 +1175,7 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
         double *eloss = malloc(sizeof(double) * ns), *ez = malloc(sizeof(double) * npart);
         sc_long_range(&c, reflength * sample, eloss);
         for (int is = 0; is < ns; is++) {
-          sc_short_range(&c, is, &sc_rmax, ez);
+          sc_short_range(&c, is, &sc_cfg.rmax, ez);
           c.sc_ez = ez;
           c.sc_eloss = eloss[is];
           push_slices(&c, is, is + 1);
