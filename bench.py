@@ -243,7 +243,8 @@ def kernel_alg_bytes(kernel, mixed, ns=None):
     return ns * per
 
 
-def time_form(g4gpu, torch, precision, beam, cur, lat, steps, warmup, profile=True, autotune=False, shapes=None):
+def time_form(g4gpu, torch, precision, beam, cur, lat, steps, warmup, profile=True, autotune=False, shapes=None,
+              efield=None):
     cfg = g4gpu.Config(nslice=NS, npart=NPART, ngrid=NGRID, gridmax=GRIDMAX, lambda0=LAMBDA0,
                        sample=1.0, gammaref=GAMMA0, precision=precision, time_run=1,
                        device=torch.cuda.current_device())
@@ -251,6 +252,8 @@ def time_form(g4gpu, torch, precision, beam, cur, lat, steps, warmup, profile=Tr
     h.set_lattice(lat)
     h.load_beam(beam, cur)
     h.load_field(0, np.zeros((NS, NGRID * NGRID), dtype=np.complex128))
+    if efield is not None:
+        h.set_efield(*efield)
     # launch shapes picked by the library's autotuner (untimed; the state is restored)
     h.shapes = h.autotune() if autotune else None
     if shapes is not None:
@@ -273,6 +276,80 @@ def time_form(g4gpu, torch, precision, beam, cur, lat, steps, warmup, profile=Tr
     stats = h.kernel_stats()
     h.set_profiling(False)
     return h, ms, stats
+
+
+# &efield of the space-charge form: the namelist's rmax and ngrid, the long-range loss
+# and nz x (2 nphi + 1) short-range modes: 1 (nz 1, nphi 0) and 15 (nz 3, nphi 2)
+SC_EFIELDS = ((0.0, 100, 1, 0, True), (0.0, 100, 3, 2, True))
+
+
+def spacecharge_form(g4gpu, torch, beam, cur, lat, steps, warmup, peak, ms_mixed, shapes):
+    """The headline window and form with space charge (&efield, EFieldSolver.cpp) on:
+    per setting of SC_EFIELDS the step rate and the two space-charge kernels: the
+    moments kernel (first transverse half step of the push, slice moments, radial grid
+    extents) is bound by HBM: it reads gamma, x, y, px, py and writes x, y, px, py (36 B
+    per particle); the field kernel (long-range loss, then per slice the radial-mode
+    source in shared memory, the tridiagonal solves and the gather) by instruction
+    issue: its work is counted in particle-modes (particles x modes, deposited and
+    gathered)."""
+    out = {"config": "headline window and lattice, mixed form, launch shapes of the headline",
+           "settings": []}
+    for ef in SC_EFIELDS:
+        h, ms, st = time_form(g4gpu, torch, g4gpu.MIXED, beam, cur, lat, steps, warmup, shapes=shapes, efield=ef)
+        h.close()
+        rmax, ngr, nz, nphi, lr = ef
+        modes = nz * (2 * nphi + 1) if (nz > 0 and ngr > 2) else 0
+        n_m, ms_mo = st.get("sc", (0, 0.0))
+        n_f, ms_fi = st.get("sc_field", (0, 0.0))
+        mo_avg = ms_mo / max(n_m, 1)
+        fi_avg = ms_fi / max(n_f, 1)
+        alg = 36 * NS * NPART
+        row = {"efield": {"rmax": rmax, "ngrid": ngr, "nz": nz, "nphi": nphi, "longrange": lr},
+               "modes": modes, "value": NS * steps / (ms / 1e3), "unit": "slice-steps/s",
+               "ms_per_step": ms / steps, "overhead_vs_mixed": ms / steps / ms_mixed - 1,
+               "kernels": {"sc_moments": {"ms_avg": mo_avg, "alg_bytes": alg,
+                                          "achieved_gbs": alg / (mo_avg / 1e3) / 1e9,
+                                          "frac_hbm": alg / (mo_avg / 1e3) / 1e9 / peak},
+                           "sc_field": {"ms_avg": fi_avg,
+                                        "particle_modes_per_s": (NS * NPART * modes / (fi_avg / 1e3)
+                                                                 if modes else None)}},
+               "launches_per_step": {k: v[0] / steps for k, v in st.items() if v[0]}}
+        out["settings"].append(row)
+    out["value"] = out["settings"][0]["value"]
+    out["unit"] = "slice-steps/s"
+    return out
+
+
+def cpu_baseline_sc(efield, target_seconds=8.0):
+    """The oracle port with space charge on a bounded sample of the window (slices from
+    its middle, full size: 8192 particles, ngrid 151), one host thread (the reference
+    runs the short-range field slice after slice: the radial grid extent is carried)."""
+    import g4oracle
+    import build_oracle
+    import g4gpu
+    build_oracle.build_oracle()
+    lib = g4oracle.oracle()
+    lat, _, _ = workload_inputs()
+    ns = 8
+    cur = flat_top(NS)[NS // 2 - ns // 2:NS // 2 - ns // 2 + ns]
+    sp = T.slice_params(ns, GAMMA0, 2.0, 0.4e-6, 15.0, currents=cur)
+    beam = g4gpu.host_load_beam(sp, NS // 2 - ns // 2, NPART, 4, 7, 1, LAMBDA0, 1.0)
+    fld = np.zeros((1, ns, NGRID * NGRID), dtype=np.complex128)
+    lib.set_efield(*efield)
+    try:
+        t0 = time.perf_counter()
+        lib.run_steps(lat[:1], GAMMA0, beam, cur, LAMBDA0, 1.0, [1], [GRIDMAX], fld, [0], time_run=1)
+        dt = time.perf_counter() - t0
+        nsteps = int(max(1, min(lat.shape[0], target_seconds / max(dt, 1e-6))))
+        lib.set_efield(*efield)
+        t0 = time.perf_counter()
+        lib.run_steps(lat[:nsteps], GAMMA0, beam, cur, LAMBDA0, 1.0, [1], [GRIDMAX], fld, [0], time_run=1)
+        dt = time.perf_counter() - t0
+    finally:
+        lib.set_efield()
+    return {"value": ns * nsteps / dt, "unit": "slice-steps/s", "cores": 1, "kind": "port",
+            "sample": f"{ns} slices x {nsteps} steps of the window with &efield {list(efield)}, "
+                      f"plain FP64, 1 host thread, {dt:.1f} s"}
 
 
 ENSEMBLE_SEED, ENSEMBLE_RUNS = 11, 64
@@ -676,8 +753,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--nslice", type=int, default=None,
                     help="slices of the window (default 4096); smaller values are for profiling only")
-    ap.add_argument("--forms", default="mixed,plain,batched,harmonic,learned",
-                    help="forms to time besides the mixed headline: plain, batched, harmonic, learned")
+    ap.add_argument("--forms", default="mixed,plain,batched,harmonic,learned,spacecharge",
+                    help="forms to time besides the mixed headline: plain, batched, harmonic, learned, "
+                         "spacecharge")
     ap.add_argument("--harmonic-slices", type=int, default=None,
                     help="slices of the harmonic FFT window (default 2048); smaller values are for profiling only")
     ap.add_argument("--no-autotune", action="store_true",
@@ -794,6 +872,11 @@ def main():
     if "harmonic" in args.forms:
         line["forms"]["harmonic_fft"] = harmonic_fft_form(g4gpu, torch, args.steps, args.warmup, peak,
                                                           ns=args.harmonic_slices)
+    if "spacecharge" in args.forms:
+        line["forms"]["spacecharge"] = spacecharge_form(g4gpu, torch, beam, cur, lat, args.steps, args.warmup,
+                                                        peak, ms_m / args.steps, shapes)
+        if rank == 0 and not args.no_cpu_baseline:
+            line["forms"]["spacecharge"]["cpu_baseline"] = cpu_baseline_sc(SC_EFIELDS[0])
     if "learned" in args.forms:
         line["forms"]["learned"] = learned_form(g4gpu, torch, lat, beam, cur, args.steps, args.warmup)
         # the same closure in steady state (config 0: quiet loading, 1 kW seed, no

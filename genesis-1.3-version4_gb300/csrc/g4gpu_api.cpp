@@ -651,7 +651,7 @@ int g4gpu_set_efield(g4gpu_handle h, double rmax, int ngrid, int nz, int nphi, i
   const g4gpu_config &c = h->cfg;
   int rc;
   if (!h->sc.st) {
-    if ((rc = alloc(h, (void **)&h->sc.st, 6 * (size_t)c.nslice * sizeof(double)))) return rc;
+    if ((rc = alloc(h, (void **)&h->sc.st, 7 * (size_t)c.nslice * sizeof(double)))) return rc;
     // the carried grid extent (a double) and the CTA counter of the moment kernel
     if ((rc = alloc(h, (void **)&h->sc.state, 2 * sizeof(double)))) return rc;
     h->sc.count = reinterpret_cast<unsigned *>(h->sc.state + 1);
@@ -661,7 +661,7 @@ int g4gpu_set_efield(g4gpu_handle h, double rmax, int ngrid, int nz, int nphi, i
     return rc;
   const double init[2] = {rmax, 0.0};  // the counter's bits are zero
   G4_CUDA(h, cudaMemcpyAsync(h->sc.state, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
-  G4_CUDA(h, cudaMemsetAsync(h->sc.st, 0, 6 * (size_t)c.nslice * sizeof(double), h->stream));
+  G4_CUDA(h, cudaMemsetAsync(h->sc.st, 0, 7 * (size_t)c.nslice * sizeof(double), h->stream));
   G4_CUDA(h, cudaStreamSynchronize(h->stream));
   h->sc_on = shortrange || longrange;
   h->sc_ngrid = ngrid;
@@ -689,8 +689,8 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
     if (h->mixed) scf_push = g4::to_float(sc, np);
     // Beam::track's push (Beam.cpp:97-112). With space charge, BeamSolver::advance
     // needs every slice after the first transverse half step (EFieldSolver::longRange
-    // reads all slices' sizes): the push runs in two launches around the space-charge
-    // kernels.
+    // reads all slices' sizes): the first space-charge kernel runs the half step, and
+    // the push the rest of the step.
     auto push = [&](void *const *src, int deposit) -> int {
       if (!h->sc_on) {
         Timed t(h, G4GPU_K_PUSH);
@@ -703,15 +703,6 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
       const bool shortrange = h->sc_nz > 0 && h->sc_ngrid > 2;
       const void *ez = shortrange ? h->sc.ez : nullptr;
       const double *eloss = h->sc_longrange ? h->sc.st + 5 * (size_t)ns : nullptr;
-      {
-        Timed t(h, G4GPU_K_PUSH);
-        if (h->mixed)
-          g4::launch_push_mixed_sc(L, scf_push, h->beam, h->field, nullptr, ns, np, ng, 0, h->push_block, 1,
-                                   nullptr, nullptr);
-        else
-          g4::launch_push_plain_sc(L, sc, h->beam, h->field, nullptr, ns, np, ng, 0, h->push_block, 1,
-                                   nullptr, nullptr);
-      }
       {
         g4::ScConst scc{};
         scc.ns = ns;
@@ -734,11 +725,13 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
         scc.ks = 4 * std::asin(1) / c.lambda0;
         const double gz2 = c.gammaref * c.gammaref / (1 + aw * aw);
         scc.coef = -gz2 / scc.ks / scc.ks;
-        Timed t(h, G4GPU_K_SC, 2);
-        if (h->mixed)
-          g4::launch_sc_mixed(L, scc, h->beam, h->sc);
-        else
-          g4::launch_sc_plain(L, scc, h->beam, h->sc);
+        for (int part = 0; part < 2; part++) {
+          Timed t(h, part == 0 ? G4GPU_K_SC : G4GPU_K_SC_FIELD);
+          if (h->mixed)
+            g4::launch_sc_mixed(L, scc, scf_push, h->beam, h->sc, part);
+          else
+            g4::launch_sc_plain(L, scc, sc, h->beam, h->sc, part);
+        }
       }
       Timed t(h, G4GPU_K_PUSH);
       if (h->mixed)

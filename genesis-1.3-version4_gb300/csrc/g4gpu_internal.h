@@ -149,7 +149,7 @@ struct ScConst {
 };
 // device state of a handle's space charge
 struct ScBuffers {
-  double *st;       // [6][nslice]: xcen, ycen, size, rbound, rmax of the slice, eloss
+  double *st;       // [7][nslice]: xcen, ycen, size, rbound, rmax of the slice, eloss; 2 x nslice floats
   double *state;    // [1]: the radial grid extent carried over steps
   unsigned *count;  // CTAs of the moment kernel that finished (reset by the last)
   void *ez;         // [nslice][npart] R: short-range field per particle
@@ -157,14 +157,16 @@ struct ScBuffers {
 // shared memory of the short-range kernel per mode, and the largest it takes
 size_t sc_bytes_per_mode(int ng, int mixed);
 size_t sc_max_smem();
-// the moments and the radial grid extents (first kernel), then the long-range loss and
-// the short-range field (second kernel); the particles' x, y must be after the first
-// transverse half step
-void launch_sc_plain(const Launch &L, const ScConst &c, const DeviceBeam &b, const ScBuffers &buf);
-void launch_sc_mixed(const Launch &L, const ScConst &c, const DeviceBeam &b, const ScBuffers &buf);
-// The push in two launches around the space charge: mode 1 the first transverse half
-// step only; mode 2 the rest of the step with ez [nslice][npart] (may be null) plus
-// eloss [nslice] (may be null) in the energy equation. Mode 0 is the whole step.
+// part 0: the first transverse half step of the push with the slice moments and the
+// radial grid extents; part 1: the long-range loss and the short-range field. The push
+// follows with mode 2.
+void launch_sc_plain(const Launch &L, const ScConst &c, const StepConst &step, const DeviceBeam &b,
+                     const ScBuffers &buf, int part);
+void launch_sc_mixed(const Launch &L, const ScConst &c, const StepConstF &step, const DeviceBeam &b,
+                     const ScBuffers &buf, int part);
+// The push in parts: mode 1 the first transverse half step only; mode 2 the rest of the
+// step with ez [nslice][npart] (may be null) plus eloss [nslice] (may be null) in the
+// energy equation. Mode 0 is the whole step.
 void launch_push_plain_sc(const Launch &L, const StepConst &sc, const DeviceBeam &b, void *const *field,
                           void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
                           const void *ez, const double *eloss);

@@ -1858,13 +1858,18 @@ struct MixedSC {
   using R = float;
   using R2 = float2;
   using Th = long long;
+  using Step = StepConstF;
   static constexpr bool kPlain = false;
+  static __device__ __forceinline__ float gamma(const StepConstF &s, float dg) { return (float)s.gammaref + dg; }
+  static __device__ __forceinline__ void half(const StepConstF &s, float g, float &x, float &y, float &px,
+                                              float &py) {
+    transverse_f(s, false, g, x, y, px, py);
+  }
   static __device__ __forceinline__ float2 eil(long long th, int l) {
     float s, c;
     __sincosf(phase_of(th, (unsigned)l), &s, &c);
     return make_float2(c, -s);
   }
-  static __device__ __forceinline__ float2 eil_step(float2, float2, long long th, int l) { return eil(th, l); }
 };
 
 }  // namespace
@@ -1875,9 +1880,11 @@ struct MixedSC {
 
 namespace g4 {
 
-void launch_sc_mixed(const Launch &L, const ScConst &c, const DeviceBeam &b, const ScBuffers &buf) {
-  ScBeam<MixedSC> sb{(const float *)b.x, (const float *)b.y, (const long long *)b.theta, b.current};
-  sc_launch<MixedSC>(L, c, sb, buf);
+void launch_sc_mixed(const Launch &L, const ScConst &c, const StepConstF &step, const DeviceBeam &b,
+                     const ScBuffers &buf, int part) {
+  ScBeam<MixedSC> sb{(float *)b.gamma, (float *)b.x,           (float *)b.y, (float *)b.px,
+                     (float *)b.py,    (const long long *)b.theta, b.current};
+  sc_launch<MixedSC>(L, c, step, sb, buf, part);
 }
 
 void launch_push_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,

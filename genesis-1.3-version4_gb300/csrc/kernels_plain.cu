@@ -487,20 +487,22 @@ Ptrs make_ptrs(const DeviceBeam &b, void *const *field, void *const *src, int nf
   return p;
 }
 
-// FP64 space charge in the reference's arithmetic: e^{-i l theta} by products of
-// e^{-i theta} (a relative difference of l ulp from the reference's cos(l theta))
+// FP64 space charge in the reference's arithmetic
 struct PlainSC {
   using R = double;
   using R2 = double2;
   using Th = double;
+  using Step = StepConst;
   static constexpr bool kPlain = true;
+  static __device__ __forceinline__ double gamma(const StepConst &, double g) { return g; }
+  static __device__ __forceinline__ void half(const StepConst &s, double g, double &x, double &y, double &px,
+                                              double &py) {
+    transverse(s, false, g, x, y, px, py);
+  }
   static __device__ __forceinline__ double2 eil(double th, int l) {
     double s, c;
     sincos((double)l * th, &s, &c);
     return make_double2(c, -s);
-  }
-  static __device__ __forceinline__ double2 eil_step(double2 e, double2 e1, double, int) {
-    return make_double2(e.x * e1.x - e.y * e1.y, e.x * e1.y + e.y * e1.x);
   }
 };
 
@@ -516,9 +518,11 @@ size_t sc_bytes_per_mode(int ng, int mixed) {
 }
 size_t sc_max_smem() { return 220 * 1024; }
 
-void launch_sc_plain(const Launch &L, const ScConst &c, const DeviceBeam &b, const ScBuffers &buf) {
-  ScBeam<PlainSC> sb{(const double *)b.x, (const double *)b.y, (const double *)b.theta, b.current};
-  sc_launch<PlainSC>(L, c, sb, buf);
+void launch_sc_plain(const Launch &L, const ScConst &c, const StepConst &step, const DeviceBeam &b,
+                     const ScBuffers &buf, int part) {
+  ScBeam<PlainSC> sb{(double *)b.gamma, (double *)b.x,        (double *)b.y, (double *)b.px,
+                     (double *)b.py,    (const double *)b.theta, b.current};
+  sc_launch<PlainSC>(L, c, step, sb, buf, part);
 }
 
 void launch_push_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,

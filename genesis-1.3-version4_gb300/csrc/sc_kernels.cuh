@@ -9,22 +9,26 @@
 // kernels_mixed.cu (FP32, F = MixedSC). A form F supplies
 //   R, R2            real and complex types of the arithmetic;
 //   Th               stored phase type (FP64 radians or Q32.32 turns);
+//   Step             the push's per-step constants;
+//   gamma(s, g)      gamma of a stored energy coordinate;
+//   half(s, g, x, y, px, py)  the first transverse half step (TrackBeam::track);
 //   kPlain           true for the reference's summation of the slice moments;
-//   eil(th, l)       e^{-i l theta} of a stored phase;
-//   eil_step(e, e1, th, l)  e^{-i l theta} given e = e^{-i (l-1) theta} and e1 = e^{-i theta}
-//                    (the FP64 form multiplies, the Q32.32 phase forms l theta exactly).
+//   eil(th, l)       e^{-i l theta} of a stored phase.
 //
-// Two kernels per step (one CTA per slice each):
-//   k_sc_moments  the slice's centroid, transverse size (Beam::getSize) and extreme
-//                 radius; the last CTA to finish then replays the reference's
-//                 slice-by-slice growth of the radial grid (rmax, kept across steps)
-//                 and records the extent every slice used;
+// Two kernels per step (one CTA per slice each), between which the push's first
+// transverse half step has run for every slice:
+//   k_sc_moments  the first transverse half step of the slice's particles (the push
+//                 then runs the rest of the step), the slice's centroid, transverse
+//                 size (Beam::getSize) and extreme radius; the last CTA to finish
+//                 replays the reference's slice-by-slice growth of the radial grid
+//                 (rmax, kept across steps) and records the extent every slice used;
 //   k_sc_field    the slice's long-range loss from every slice's size and current,
 //                 then its short-range field: the radial-mode source deposited in
 //                 shared memory, one tridiagonal solve per mode, gathered back per
 //                 particle into ez.
 // Buffer `st` holds, per slice, [0,ns) xcen, [ns,2ns) ycen, [2ns,3ns) size,
-// [3ns,4ns) rbound, [4ns,5ns) the grid extent rmax of the slice, [5ns,6ns) eloss.
+// [3ns,4ns) rbound, [4ns,5ns) the grid extent rmax of the slice, [5ns,6ns) eloss, then
+// (FP32 form) as floats the size and scl * current / size of every slice.
 #pragma once
 
 namespace g4 {
@@ -64,14 +68,13 @@ __device__ __forceinline__ void sc_block_sum(double (&v)[N], double (*red)[kScTh
   }
 }
 
-// Per particle: radial bin, azimuth z = e^{i phi} and e^{-i theta}
-// (EFieldSolver.cpp:166-173). A bin index outside the grid, which the reference
-// leaves undefined (a particle on the centroid of a slice with a zero grid extent),
-// is clamped into it.
+// Per particle: radial bin and azimuth z = e^{i phi} (EFieldSolver.cpp:166-173). A bin
+// index outside the grid, which the reference leaves undefined (a particle on the
+// centroid of a slice with a zero grid extent), is clamped into it.
 template <class F>
-__device__ __forceinline__ void sc_particle(typename F::R x, typename F::R y, typename F::Th th,
-                                            typename F::R xc, typename F::R yc, typename F::R dr, int ng,
-                                            int &idx, typename F::R2 &z, typename F::R2 &e1) {
+__device__ __forceinline__ void sc_particle(typename F::R x, typename F::R y, typename F::R xc,
+                                            typename F::R yc, typename F::R dr, int ng, int &idx,
+                                            typename F::R2 &z) {
   using R = typename F::R;
   const R tx = x - xc, ty = y - yc;
   const R radi = sqrt(tx * tx + ty * ty);
@@ -79,7 +82,6 @@ __device__ __forceinline__ void sc_particle(typename F::R x, typename F::R y, ty
   z.y = ty / radi;
   const R q = floor(radi / dr);
   idx = q >= 0 ? (q < (R)(ng - 1) ? (int)q : ng - 1) : 0;
-  e1 = F::eil(th, 1);
 }
 
 // z^-m as std::pow(z, -m) forms it for |z| = 1: repeated products of z (m < 0) or
@@ -93,33 +95,35 @@ __device__ __forceinline__ typename F::R2 sc_zpow_neg(typename F::R2 z, int m) {
   return r;
 }
 
-// Mode k of the slice's expansion, k = (m + nphi) nz + (l - 1): the walk over a pass's
-// modes keeps z^-m and e^{-i l theta} and steps l, then m
+// Mode k of the slice's expansion, k = (l - 1)(2 nphi + 1) + (m + nphi): the walk over
+// a pass's modes evaluates e^{-i l theta} once per l and steps z^-m by the conjugate of
+// z (the reciprocal of the unit z) from z^nphi, taking 1 exactly at m = 0
 template <class F>
 struct ScModeWalk {
   using R2 = typename F::R2;
-  R2 z, e1, zm, el;
+  R2 zc, ztop, zm, el;
   typename F::Th th;
-  int m, l, nz;
-  __device__ __forceinline__ ScModeWalk(R2 z_, R2 e1_, typename F::Th th_, int k0, int nz_, int nphi)
-      : z(z_), e1(e1_), th(th_), nz(nz_) {
-    m = k0 / nz - nphi;
-    l = k0 % nz + 1;
+  int m, l, nphi;
+  __device__ __forceinline__ ScModeWalk(R2 z, typename F::Th th_, int k0, int nphi_) : th(th_), nphi(nphi_) {
+    const int nm = 2 * nphi + 1;
+    l = k0 / nm + 1;
+    m = k0 % nm - nphi;
+    zc = R2{z.x, -z.y};
+    ztop = sc_zpow_neg<F>(z, -nphi);
     zm = sc_zpow_neg<F>(z, m);
-    el = e1;
-    for (int j = 2; j <= l; j++) el = F::eil_step(el, e1, th, j);
+    el = F::eil(th, l);
   }
   // z^-m e^{-i l theta}
   __device__ __forceinline__ R2 value() const {
     return R2{zm.x * el.x - zm.y * el.y, zm.x * el.y + zm.y * el.x};
   }
   __device__ __forceinline__ void next() {
-    if (++l > nz) {
-      l = 1;
-      zm = sc_zpow_neg<F>(z, ++m);
-      el = e1;
+    if (++m > nphi) {
+      m = -nphi;
+      el = F::eil(th, ++l);
+      zm = ztop;
     } else {
-      el = F::eil_step(el, e1, th, l);
+      zm = m == 0 ? R2{1, 0} : R2{zm.x * zc.x - zm.y * zc.y, zm.x * zc.y + zm.y * zc.x};
     }
   }
 };
@@ -169,40 +173,68 @@ __device__ void sc_solve(typename F::R2 *cs, typename F::R *gm, int ng, int m, i
 
 template <class F>
 struct ScBeam {
-  const typename F::R *x, *y;
+  typename F::R *g, *x, *y, *px, *py;
   const typename F::Th *theta;
   const double *current;
 };
 
-// Per slice moments, then (last CTA) the radial grid extent of every slice.
-// state[0]: rmax carried from slice to slice and from step to step; count: CTAs done.
+// The first transverse half step and the slice moments, then (last CTA) the radial
+// grid extent of every slice. state[0]: rmax carried from slice to slice and from step
+// to step; count: CTAs done.
 template <class F>
-__global__ void __launch_bounds__(kScThreads) k_sc_moments(ScBeam<F> b, double *st, double *state,
-                                                           unsigned *count, int ns, int np, int shortrange) {
+__global__ void __launch_bounds__(kScThreads) k_sc_moments(ScBeam<F> b, typename F::Step step, double *st,
+                                                           double *state, unsigned *count, ScConst c) {
   using R = typename F::R;
   __shared__ double red[4][kScThreads / 32];
   __shared__ double rb[kScScanChunk];
   __shared__ int last;
-  const int is = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
-  const R *xs = b.x + (size_t)is * np, *ys = b.y + (size_t)is * np;
+  const int is = blockIdx.x, tid = threadIdx.x, lane = tid & 31, ns = c.ns, np = c.np;
+  const size_t o0 = (size_t)is * np;
+  const R *xs = b.x + o0, *ys = b.y + o0;
 
-  // pass 1: sums of x, y (and, in the reference's form, of x^2, y^2), Beam.cpp:42-67
+  // pass 1: the half step (Beam.cpp:103, TrackBeam.cpp:17-64), and the sums of x, y
+  // (and, in the reference's form, of x^2, y^2), Beam.cpp:42-67; four particles per
+  // thread and round, their loads issued together
+  constexpr int U = 4;
   double s[4] = {0, 0, 0, 0};
-  if constexpr (F::kPlain) {
-    for (int i = tid; i < np; i += blockDim.x) {
-      double x = xs[i], y = ys[i];
-      s[0] += x;
-      s[1] += x * x;
-      s[2] += y;
-      s[3] += y * y;
+  R sx = 0, sy = 0;
+  for (int i0 = tid; i0 < np; i0 += U * blockDim.x) {
+    R g[U], x[U], y[U], px[U], py[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int i = i0 + u * blockDim.x;
+      if (i < np) {
+        g[u] = b.g[o0 + i];
+        x[u] = b.x[o0 + i];
+        y[u] = b.y[o0 + i];
+        px[u] = b.px[o0 + i];
+        py[u] = b.py[o0 + i];
+      }
     }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int i = i0 + u * blockDim.x;
+      if (i < np) {
+        F::half(step, F::gamma(step, g[u]), x[u], y[u], px[u], py[u]);
+        b.x[o0 + i] = x[u];
+        b.y[o0 + i] = y[u];
+        b.px[o0 + i] = px[u];
+        b.py[o0 + i] = py[u];
+        if constexpr (F::kPlain) {
+          s[0] += x[u];
+          s[1] += x[u] * x[u];
+          s[2] += y[u];
+          s[3] += y[u] * y[u];
+        } else {
+          sx += x[u];
+          sy += y[u];
+        }
+      }
+    }
+  }
+  if constexpr (F::kPlain) {
     sc_block_sum<4>(s, red);
   } else {
-    float sx = 0.f, sy = 0.f;
-    for (int i = tid; i < np; i += blockDim.x) {
-      sx += xs[i];
-      sy += ys[i];
-    }
     double t[2] = {sx, sy};
     sc_block_sum<2>(t, red);
     s[0] = t[0];
@@ -247,6 +279,13 @@ __global__ void __launch_bounds__(kScThreads) k_sc_moments(ScBeam<F> b, double *
     st[ns + is] = ycen;
     st[2 * ns + is] = size;
     st[3 * ns + is] = sqrt((double)m);
+    if constexpr (!F::kPlain) {
+      // the long-range kernel's per-slice factors in FP32 (EFieldSolver.cpp:89-93, 113)
+      const double fs = size <= 0 ? 1. : size;
+      float *sf = reinterpret_cast<float *>(st + 6 * (size_t)ns);
+      sf[is] = (float)fs;
+      sf[ns + is] = (float)(c.lr_scl * b.current[is] / fs);
+    }
     __threadfence();
     last = atomicAdd(count, 1u) == (unsigned)ns - 1;
   }
@@ -257,7 +296,7 @@ __global__ void __launch_bounds__(kScThreads) k_sc_moments(ScBeam<F> b, double *
   // exceeds it (EFieldSolver.cpp:159-163), slice after slice. Warp 0 resolves 32
   // slices at a time: a ballot finds the first slice beyond the current extent, which
   // sets the next one; at most 32 rounds per group.
-  if (shortrange) {
+  if (c.shortrange) {
     double r = state[0];
     for (int c0 = 0; c0 < ns; c0 += kScScanChunk) {
       const int nc = min(kScScanChunk, ns - c0);
@@ -303,22 +342,29 @@ __global__ void __launch_bounds__(kScThreads) k_sc_field(ScBeam<F> b, double *st
   // EFieldSolver::longRange, EFieldSolver.cpp:77-117
   if (c.longrange) {
     double e[1] = {0};
-    for (int j = tid; j < ns; j += blockDim.x) {
-      double fs = st[2 * ns + j];
-      if (fs <= 0) fs = 1;
-      const double sgn = (j > is) ? -1. : ((j < is) ? 1. : 0.);
-      if constexpr (F::kPlain) {
+    if constexpr (F::kPlain) {
+      for (int j = tid; j < ns; j += blockDim.x) {
+        double fs = st[2 * ns + j];
+        if (fs <= 0) fs = 1;
+        const double sgn = (j > is) ? -1. : ((j < is) ? 1. : 0.);
         double ds = (double)(j - is) * c.slicelength * c.gamma_lr;
         double coef = 1 - sqrt(ds * ds / (ds * ds + fs));
         e[0] += sgn * coef * c.lr_scl * b.current[j] / fs;
-      } else {
-        // 1 - sqrt(a / (a + f)) = (f / (a + f)) / (1 + sqrt(a / (a + f))), without the
-        // cancellation of the left side in FP32
-        float ds = (float)(j - is) * (float)(c.slicelength * c.gamma_lr);
-        float a = ds * ds, ff = (float)fs, q = a / (a + ff);
-        float coef = (ff / (a + ff)) / (1.f + sqrtf(q));
-        e[0] += (double)(sgn * coef * (float)(c.lr_scl * b.current[j] / fs));
       }
+    }
+    if constexpr (!F::kPlain) {
+      // 1 - sqrt(a / (a + f)) = (f / (a + f)) / (1 + sqrt(a / (a + f))), without the
+      // cancellation of the left side in FP32; w = scl current / size of the slice
+      const float *sf = reinterpret_cast<const float *>(st + 6 * (size_t)ns), *wf = sf + ns;
+      const float dsl = (float)(c.slicelength * c.gamma_lr);
+      float acc = 0.f;
+      for (int j = tid; j < ns; j += blockDim.x) {
+        const float ds = (float)(j - is) * dsl, a = ds * ds, ff = sf[j], den = a + ff;
+        const float coef = (ff / den) / (1.f + sqrtf(a / den));
+        const float sgn = (j > is) ? -1.f : ((j < is) ? 1.f : 0.f);
+        acc += sgn * coef * wf[j];
+      }
+      e[0] = acc;
     }
     sc_block_sum<1>(e, red);
     if (tid == 0) st[5 * ns + is] = -e[0] / kEev;
@@ -344,21 +390,48 @@ __global__ void __launch_bounds__(kScThreads) k_sc_field(ScBeam<F> b, double *st
     __syncthreads();
     // source: sum over the slice's particles of z^-m e^{-i l theta} in the radial bin,
     // z = e^{i phi} the particle's azimuth (EFieldSolver.cpp:228-236)
-    for (int ip = tid; ip < np; ip += blockDim.x) {
+    // Aligned groups of 2, 4 or 8 lanes whose particles fall in the same radial bin
+    // (a beamlet of the quiet loading always does) sum their terms by shuffles, and
+    // one lane adds the sum; every lane of the CTA takes part in the shuffles.
+    for (int base = 0; base < np; base += blockDim.x) {
+      const int ip = base + tid;
+      const bool valid = ip < np;
+      const int ipc = valid ? ip : np - 1;
       int idx;
-      R2 z, e1;
-      sc_particle<F>(xs[ip], ys[ip], ths[ip], xc, yc, dr, ng, idx, z, e1);
-      ScModeWalk<F> w(z, e1, ths[ip], k0, nz, nphi);
-      for (int k = k0; k < k1; k++, w.next()) {
-        const R2 d = w.value();
-        R2 *a = csrc + (size_t)(k - k0) * ng + idx;
-        atomicAdd(&a->x, d.x);
-        atomicAdd(&a->y, d.y);
+      R2 z;
+      sc_particle<F>(xs[ipc], ys[ipc], xc, yc, dr, ng, idx, z);
+      const unsigned full = 0xffffffffu;
+      const int key = valid ? idx : -1 - (threadIdx.x & 31);  // lanes without a particle match no one
+      const int key1 = __shfl_xor_sync(full, key, 1), key2 = __shfl_xor_sync(full, key, 2),
+                key4 = __shfl_xor_sync(full, key, 4);
+      const bool g1 = key == key1;
+      const int g1p = __shfl_xor_sync(full, (int)g1, 2);
+      const bool g2 = g1 && g1p && key == key2;
+      const int g2p = __shfl_xor_sync(full, (int)g2, 4);
+      const bool g4 = g2 && g2p && key == key4;
+      const int gsize = g4 ? 8 : (g2 ? 4 : (g1 ? 2 : 1));
+      const bool leader = valid && ((threadIdx.x & 31) & (gsize - 1)) == 0;
+      ScModeWalk<F> w(z, ths[ipc], k0, nphi);
+      R2 *a = csrc + idx;
+      for (int k = k0; k < k1; k++, w.next(), a += ng) {
+        R2 d = w.value();
+        R tx = __shfl_xor_sync(full, d.x, 1), ty = __shfl_xor_sync(full, d.y, 1);
+        if (g1) d = R2{d.x + tx, d.y + ty};
+        tx = __shfl_xor_sync(full, d.x, 2);
+        ty = __shfl_xor_sync(full, d.y, 2);
+        if (g2) d = R2{d.x + tx, d.y + ty};
+        tx = __shfl_xor_sync(full, d.x, 4);
+        ty = __shfl_xor_sync(full, d.y, 4);
+        if (g4) d = R2{d.x + tx, d.y + ty};
+        if (leader) {
+          atomicAdd(&a->x, d.x);
+          atomicAdd(&a->y, d.y);
+        }
       }
     }
     __syncthreads();
     for (int t = tid; t < nk; t += blockDim.x) {
-      const int k = k0 + t, m = k / nz - nphi, l = k % nz + 1;
+      const int k = k0 + t, m = k % (2 * nphi + 1) - nphi, l = k / (2 * nphi + 1) + 1;
       sc_solve<F>(csrc + (size_t)t * ng, gam + (size_t)t * ng, ng, m, l, dr, pi, coef, econst);
     }
     __syncthreads();
@@ -366,13 +439,13 @@ __global__ void __launch_bounds__(kScThreads) k_sc_field(ScBeam<F> b, double *st
     // factor is the conjugate of the deposited one
     for (int ip = tid; ip < np; ip += blockDim.x) {
       int idx;
-      R2 z, e1;
-      sc_particle<F>(xs[ip], ys[ip], ths[ip], xc, yc, dr, ng, idx, z, e1);
-      ScModeWalk<F> w(z, e1, ths[ip], k0, nz, nphi);
+      R2 z;
+      sc_particle<F>(xs[ip], ys[ip], xc, yc, dr, ng, idx, z);
+      ScModeWalk<F> w(z, ths[ip], k0, nphi);
       R acc = k0 == 0 ? (R)0 : ezs[ip];
-      for (int k = k0; k < k1; k++, w.next()) {
-        const R2 d = w.value();
-        const R2 ce = csrc[(size_t)(k - k0) * ng + idx];
+      const R2 *a = csrc + idx;
+      for (int k = k0; k < k1; k++, w.next(), a += ng) {
+        const R2 d = w.value(), ce = *a;
         acc += 2 * (d.x * ce.x + d.y * ce.y);
       }
       ezs[ip] = acc;
@@ -381,10 +454,11 @@ __global__ void __launch_bounds__(kScThreads) k_sc_field(ScBeam<F> b, double *st
   }
 }
 
-// The two launches of a step's space charge (ez: [ns][np] R, used when the
-// short-range part runs)
+// The two launches of a step's space charge, part 0 or 1 (ez: [ns][np] R, used when
+// the short-range part runs)
 template <class F>
-void sc_launch(const Launch &L, const ScConst &c, ScBeam<F> sb, const ScBuffers &buf) {
+void sc_launch(const Launch &L, const ScConst &c, const typename F::Step &step, ScBeam<F> sb,
+               const ScBuffers &buf, int part) {
   static unsigned long long configured = 0;
   int dev = 0;
   cudaGetDevice(&dev);
@@ -393,7 +467,10 @@ void sc_launch(const Launch &L, const ScConst &c, ScBeam<F> sb, const ScBuffers 
     configured |= 1ull << dev;
   }
   cudaStream_t s = (cudaStream_t)L.stream;
-  k_sc_moments<F><<<c.ns, kScThreads, 0, s>>>(sb, buf.st, buf.state, buf.count, c.ns, c.np, c.shortrange);
+  if (part == 0) {
+    k_sc_moments<F><<<c.ns, kScThreads, 0, s>>>(sb, step, buf.st, buf.state, buf.count, c);
+    return;
+  }
   const size_t smem = c.shortrange ? (size_t)c.modes_per_pass * sc_bytes_per_mode(c.ng, !F::kPlain) : 0;
   k_sc_field<F><<<c.ns, kScThreads, smem, s>>>(sb, buf.st, (typename F::R *)buf.ez, c);
 }

@@ -255,7 +255,7 @@ int g4gpu_get_stream(g4gpu_handle h, void **stream);
  * (G4GPU_K_*) the launch count and the summed device time in milliseconds of the
  * launches since the last reset. The launch counter runs always. */
 enum { G4GPU_K_PUSH, G4GPU_K_ADI_X, G4GPU_K_ADI_Y, G4GPU_K_FFT, G4GPU_K_SLIP, G4GPU_K_DIAG,
-       G4GPU_K_MISC, G4GPU_K_SC, G4GPU_K_NCLASS };
+       G4GPU_K_MISC, G4GPU_K_SC, G4GPU_K_SC_FIELD, G4GPU_K_NCLASS };
 int g4gpu_set_profiling(g4gpu_handle h, int on);
 int g4gpu_kernel_stats(g4gpu_handle h, long long *launches, double *ms);
 int g4gpu_reset_stats(g4gpu_handle h);
