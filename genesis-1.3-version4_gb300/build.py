@@ -52,6 +52,7 @@ def _units():
         ("kernels_closure.cu", cu_common + ["-use_fast_math"]),
         ("g4gpu_api.cpp", cxx_common),
         ("host_loading.cpp", cxx_common + ["-pthread"]),
+        ("host_wake.cpp", cxx_common + ["-pthread"]),
         ("g4gpu_learned.cpp", cxx_common),
         ("g4gpu_dpi.cpp", cxx_common),
     ]

@@ -391,7 +391,8 @@ void g4gpu_destroy(g4gpu_handle h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   void *ptrs[] = {h->beam.gamma, h->beam.theta, h->beam.x, h->beam.y, h->beam.px, h->beam.py,
                   h->beam.current, h->tmp, h->diag_work, h->coef, h->derr, h->ddiag, h->stage,
-                  h->closure_basis, h->closure_feat, h->closure_corr, h->sc.st, h->sc.state, h->sc.ez};
+                  h->closure_basis, h->closure_feat, h->closure_corr, h->sc.st, h->sc.state, h->sc.ez,
+                  h->wake_tab, h->wake_loss, h->wake_lossf, h->wake_scratch};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
@@ -553,6 +554,20 @@ static int ensure_stage(g4gpu_handle h, size_t n) {
   return rc;
 }
 
+// Collective::update on the device: the slices' wake loss from the current
+static int wake_update(g4gpu_handle h) {
+  const int ns = h->cfg.nslice, nw = h->wake_ns;
+  g4::Launch L{h->stream, h->derr};
+  {
+    Timed t(h, G4GPU_K_MISC, 2);
+    g4::launch_wake_update(L, h->beam.current, ns, nw, h->wake_ds, h->wake_tab + 3 * (size_t)nw, h->wake_tab,
+                           h->wake_tab + nw, h->wake_tab + 2 * (size_t)nw, h->wake_scratch, h->wake_loss,
+                           h->wake_lossf);
+  }
+  G4_CUDA(h, cudaGetLastError());
+  return G4GPU_OK;
+}
+
 int g4gpu_load_beam(g4gpu_handle h, const double *particles, const double *current) {
   if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
   if (!particles || !current) return fail(h, G4GPU_ERR_ARG, "null particles or current");
@@ -570,6 +585,8 @@ int g4gpu_load_beam(g4gpu_handle h, const double *particles, const double *curre
   }
   G4_CUDA(h, cudaGetLastError());
   h->beam_loaded = true;
+  // the wake of every slice follows the window's current
+  if (h->wake_on) return wake_update(h);
   return G4GPU_OK;
 }
 
@@ -675,6 +692,64 @@ int g4gpu_set_efield(g4gpu_handle h, double rmax, int ngrid, int nz, int nphi, i
   return G4GPU_OK;
 }
 
+int g4gpu_set_wake(g4gpu_handle h, int ns_hr, double ds, const double *ext, const double *res, const double *geo,
+                   const double *rou, double ztrans, double radius, int transient) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  cudaSetDevice(h->cfg.device);
+  auto drop_graphs = [&] {
+    // captured step sequences were recorded with other wakes
+    for (auto &g : h->graphs)
+      if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+    h->graphs.clear();
+  };
+  if (!ext) {
+    h->wake_on = false;
+    drop_graphs();
+    return G4GPU_OK;
+  }
+  const int ns = h->cfg.nslice;
+  if (!res || !geo || !rou || !(ds > 0)) return fail(h, G4GPU_ERR_ARG, "null wake table or ds <= 0");
+  // Collective::initWake / update: the fine grid covers the window, at least one fine
+  // point per slice
+  if (ns_hr < ns) return fail(h, G4GPU_ERR_ARG, "ns_hr must be at least nslice (nslice * sample)");
+  if (h->wake_ns != ns_hr) {
+    void *bufs[] = {h->wake_tab, h->wake_loss, h->wake_lossf, h->wake_scratch};
+    for (void *p : bufs)
+      if (p) cudaFree(p);
+    h->wake_tab = h->wake_loss = h->wake_scratch = nullptr;
+    h->wake_lossf = nullptr;
+    h->wake_ns = 0;
+    int rc;
+    if ((rc = alloc(h, (void **)&h->wake_tab, (3 * (size_t)ns_hr + ns) * sizeof(double))) ||
+        (rc = alloc(h, (void **)&h->wake_loss, ns * sizeof(double))) ||
+        (rc = alloc(h, (void **)&h->wake_lossf, ns * sizeof(float))) ||
+        (rc = alloc(h, (void **)&h->wake_scratch, 2 * (size_t)ns_hr * sizeof(double))))
+      return rc;
+    h->wake_ns = ns_hr;
+  }
+  std::vector<double> tab(3 * (size_t)ns_hr + ns);
+  std::copy(res, res + ns_hr, tab.begin());
+  std::copy(geo, geo + ns_hr, tab.begin() + ns_hr);
+  std::copy(rou, rou + ns_hr, tab.begin() + 2 * (size_t)ns_hr);
+  std::copy(ext, ext + ns, tab.begin() + 3 * (size_t)ns_hr);
+  // self-loading theorem (Collective.cpp:103-105)
+  tab[0] *= 0.5;
+  tab[ns_hr] *= 0.5;
+  tab[2 * (size_t)ns_hr] *= 0.5;
+  G4_CUDA(h, cudaMemcpyAsync(h->wake_tab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice,
+                             h->stream));
+  h->wake_ds = ds;
+  h->wake_ztrans = ztrans;
+  h->wake_radius = radius;
+  h->wake_transient = transient;
+  h->wake_on = true;
+  drop_graphs();
+  int rc = h->beam_loaded ? wake_update(h) : G4GPU_OK;
+  if (rc) return rc;
+  G4_CUDA(h, cudaStreamSynchronize(h->stream));
+  return G4GPU_OK;
+}
+
 static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
   const g4gpu_config &c = h->cfg;
   int ns = c.nslice, np = c.npart, ng = c.ngrid;
@@ -691,13 +766,17 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
     // needs every slice after the first transverse half step (EFieldSolver::longRange
     // reads all slices' sizes): the first space-charge kernel runs the half step, and
     // the push the rest of the step.
+    // Collective::apply after the integration (Beam.cpp:108)
+    const void *wake = !h->wake_on ? nullptr : h->mixed ? (const void *)h->wake_lossf : (const void *)h->wake_loss;
     auto push = [&](void *const *src, int deposit) -> int {
       if (!h->sc_on) {
         Timed t(h, G4GPU_K_PUSH);
         if (h->mixed)
-          g4::launch_push_mixed(L, scf_push, h->beam, h->field, src, ns, np, ng, deposit, h->push_block);
+          g4::launch_push_mixed_sc(L, scf_push, h->beam, h->field, src, ns, np, ng, deposit, h->push_block, 0,
+                                   nullptr, nullptr, wake);
         else
-          g4::launch_push_plain(L, sc, h->beam, h->field, src, ns, np, ng, deposit, h->push_block);
+          g4::launch_push_plain_sc(L, sc, h->beam, h->field, src, ns, np, ng, deposit, h->push_block, 0,
+                                   nullptr, nullptr, wake);
         return G4GPU_OK;
       }
       const bool shortrange = h->sc_nz > 0 && h->sc_ngrid > 2;
@@ -736,10 +815,10 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
       Timed t(h, G4GPU_K_PUSH);
       if (h->mixed)
         g4::launch_push_mixed_sc(L, scf_push, h->beam, h->field, src, ns, np, ng, deposit, h->push_block, 2, ez,
-                                 eloss);
+                                 eloss, wake);
       else
         g4::launch_push_plain_sc(L, sc, h->beam, h->field, src, ns, np, ng, deposit, h->push_block, 2, ez,
-                                 eloss);
+                                 eloss, wake);
       return G4GPU_OK;
     };
     bool any_dep = false;

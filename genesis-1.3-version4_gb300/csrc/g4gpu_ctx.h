@@ -47,6 +47,16 @@ struct g4gpu_ctx {
   bool sc_on = false;
   int sc_ngrid = 0, sc_nz = 0, sc_nphi = 0, sc_longrange = 0;
   g4::ScBuffers sc{};
+  // wakes (g4gpu_set_wake): fine-grid single-particle wakes, external loss, the slices'
+  // loss (FP64 eV/m and FP32 over eev) and the update's scratch, all on the device
+  bool wake_on = false;
+  int wake_ns = 0;
+  double wake_ds = 0, wake_ztrans = 0, wake_radius = 0;
+  int wake_transient = 0;
+  double *wake_tab = nullptr;  // [3][wake_ns] res, geo, rou (first points halved), then [nslice] ext
+  double *wake_loss = nullptr;  // [nslice]
+  float *wake_lossf = nullptr;  // [nslice]
+  double *wake_scratch = nullptr;  // [2][wake_ns]
   void *stage = nullptr;     // AoS staging buffer for host transfers
   size_t stage_bytes = 0;
   size_t bytes = 0;

@@ -166,13 +166,20 @@ void launch_sc_mixed(const Launch &L, const ScConst &c, const StepConstF &step, 
                      const ScBuffers &buf, int part);
 // The push in parts: mode 1 the first transverse half step only; mode 2 the rest of the
 // step with ez [nslice][npart] (may be null) plus eloss [nslice] (may be null) in the
-// energy equation. Mode 0 is the whole step.
+// energy equation. Mode 0 is the whole step. wake [nslice] (may be null): the slices'
+// wake loss added to gamma after the integration, eV/m as FP64 (plain) or divided by
+// eev as FP32 (mixed).
 void launch_push_plain_sc(const Launch &L, const StepConst &sc, const DeviceBeam &b, void *const *field,
                           void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
-                          const void *ez, const double *eloss);
+                          const void *ez, const double *eloss, const void *wake);
 void launch_push_mixed_sc(const Launch &L, const StepConstF &sc, const DeviceBeam &b, void *const *field,
                           void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
-                          const void *ez, const double *eloss);
+                          const void *ez, const double *eloss, const void *wake);
+// Wakes (Collective::update): loss [nslice] = ext + the wake of each slice from the
+// window's current cur [nslice]; lossf = loss / eev in FP32; scratch: 2 ns_hr doubles.
+void launch_wake_update(const Launch &L, const double *cur, int nslice, int ns_hr, double ds, const double *ext,
+                        const double *res, const double *geo, const double *rou, double *scratch, double *loss,
+                        float *lossf);
 
 // kernels_fft.cu: FFT field solver (FieldSolverFFT::FFT)
 struct FFTPlan {

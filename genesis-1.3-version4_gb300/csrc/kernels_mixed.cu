@@ -200,6 +200,8 @@ struct PtrsF {
   const float *ez;
   const double *eloss;
   int mode;
+  // wakes: the loss of every slice over eev (1/m, Collective::apply), null without them
+  const float *wake;
 };
 
 // Deposition into the global source grids (FieldSolverADI.cpp:11-52) by a whole
@@ -330,6 +332,8 @@ __global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, 
   float dgam = h6 * (k1g + 2.f * k2g + 2.f * k3g + k4g);
   float dth = h6 * (k1t + 2.f * k2t + 2.f * k3t + k4t);
   dg += dgam;
+  // Collective::apply (Collective.cpp:119-128), before the second half step
+  if (p.wake) dg += p.wake[is] * sc.delz;
   th = add_phase(th, dth);
   float g = g0 + dg;
 
@@ -1890,16 +1894,17 @@ void launch_sc_mixed(const Launch &L, const ScConst &c, const StepConstF &step, 
 void launch_push_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,
                        void *const *field, void *const *src, int ns, int np, int ngrid,
                        int deposit, int block) {
-  launch_push_mixed_sc(L, sc, b, field, src, ns, np, ngrid, deposit, block, 0, nullptr, nullptr);
+  launch_push_mixed_sc(L, sc, b, field, src, ns, np, ngrid, deposit, block, 0, nullptr, nullptr, nullptr);
 }
 
 void launch_push_mixed_sc(const Launch &L, const StepConstF &sc, const DeviceBeam &b, void *const *field,
                           void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
-                          const void *ez, const double *eloss) {
+                          const void *ez, const double *eloss, const void *wake) {
   PtrsF p = make_ptrs_f(b, field, src, sc.nfld);
   p.mode = mode;
   p.ez = (const float *)ez;
   p.eloss = eloss;
+  p.wake = (const float *)wake;
   if (mode == 1) deposit = 0;
   dim3 grid((np + block - 1) / block, ns);
   cudaStream_t s = (cudaStream_t)L.stream;

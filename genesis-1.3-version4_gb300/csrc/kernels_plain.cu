@@ -169,6 +169,8 @@ struct Ptrs {
   // transverse half step, 2 the rest)
   const double *ez, *eloss;
   int mode;
+  // wakes: the loss of every slice (eV/m, Collective::apply), null without them
+  const double *wake;
 };
 
 // Beam::track (Beam.cpp:296-311): half transverse step, BeamSolver::advance with
@@ -248,6 +250,9 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   ode<NF>(sc, rpart, btpar, ez, gamma, theta, k2gg, k2pp);
   gamma += stpz * (k3gg + k2gg / 6.0);
   theta += stpz * (k3pp + k2pp / 6.0);
+
+  // Collective::apply (Collective.cpp:119-128), before the second half step
+  if (p.wake) gamma += p.wake[is] * sc.delz / kEev;
 
   transverse(sc, true, gamma, x, y, px, py);
 
@@ -513,6 +518,66 @@ struct PlainSC {
 
 namespace g4 {
 
+namespace {
+
+// Collective::update for one rank (Collective.cpp:144-161): the window's current
+// interpolated to the fine grid, in electrons per fine slice, and its derivative
+__global__ void k_wake_profile(const double *cur, int ncur, int ns_hr, double ds, double dscur, double *curh,
+                               double *dcur) {
+  const int is = blockIdx.x * blockDim.x + threadIdx.x;
+  if (is >= ns_hr) return;
+  const double s = ds * (double)is;
+  unsigned idx = (unsigned)(int)floor(s / dscur);
+  if (idx > (unsigned)ncur) idx = (unsigned)ncur;  // s < ncur dscur: never taken
+  const double c0 = idx < (unsigned)ncur ? cur[idx] : 0., c1 = idx + 1 < (unsigned)ncur ? cur[idx + 1] : 0.;
+  const double wei = 1 - (s - idx * dscur) / dscur;
+  double v = wei * c0 + (1 - wei) * c1;
+  v *= ds / kCe;
+  curh[is] = v;
+  dcur[is] = -(c1 - c0) * ds / kCe / dscur;
+}
+
+// Collective.cpp:167-179: the wake of slice ic from the fine points ahead of each of
+// its `sample` fine points, averaged; loss = external + wake (eV/m), lossf = loss / eev
+// in FP32 for the mixed push. One CTA per slice.
+__global__ void __launch_bounds__(256) k_wake_slices(const double *curh, const double *dcur, const double *res,
+                                                     const double *geo, const double *rou, const double *ext,
+                                                     int ns_hr, int sample, double *loss, float *lossf) {
+  __shared__ double red[256 / 32];
+  const int ic = blockIdx.x, tid = threadIdx.x;
+  double w = 0;
+  for (int j = 0; j < sample; j++) {
+    const int is = ic * sample + j;
+    for (int i = tid; i < ns_hr - is; i += blockDim.x) {
+      w += curh[is + i] * (res[i] + rou[i]);
+      w += dcur[is + i] * geo[i];
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+  if ((tid & 31) == 0) red[tid >> 5] = w;
+  __syncthreads();
+  if (tid == 0) {
+    double t = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += red[i];
+    const double l = ext[ic] + t / (double)sample;
+    loss[ic] = l;
+    lossf[ic] = (float)(l / kEev);
+  }
+}
+
+}  // namespace
+
+void launch_wake_update(const Launch &L, const double *cur, int nslice, int ns_hr, double ds, const double *ext,
+                        const double *res, const double *geo, const double *rou, double *scratch, double *loss,
+                        float *lossf) {
+  cudaStream_t s = (cudaStream_t)L.stream;
+  const double dscur = ds * (unsigned)ns_hr / nslice;
+  int sample = (int)(dscur / ds);
+  if (sample < 1) sample = 1;
+  k_wake_profile<<<(ns_hr + 255) / 256, 256, 0, s>>>(cur, nslice, ns_hr, ds, dscur, scratch, scratch + ns_hr);
+  k_wake_slices<<<nslice, 256, 0, s>>>(scratch, scratch + ns_hr, res, geo, rou, ext, ns_hr, sample, loss, lossf);
+}
+
 size_t sc_bytes_per_mode(int ng, int mixed) {
   return (size_t)ng * (mixed ? sizeof(float2) + sizeof(float) : sizeof(double2) + sizeof(double));
 }
@@ -528,16 +593,17 @@ void launch_sc_plain(const Launch &L, const ScConst &c, const StepConst &step, c
 void launch_push_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,
                        void *const *field, void *const *src, int ns, int np, int ngrid,
                        int deposit, int block) {
-  launch_push_plain_sc(L, sc, b, field, src, ns, np, ngrid, deposit, block, 0, nullptr, nullptr);
+  launch_push_plain_sc(L, sc, b, field, src, ns, np, ngrid, deposit, block, 0, nullptr, nullptr, nullptr);
 }
 
 void launch_push_plain_sc(const Launch &L, const StepConst &sc, const DeviceBeam &b, void *const *field,
                           void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
-                          const void *ez, const double *eloss) {
+                          const void *ez, const double *eloss, const void *wake) {
   Ptrs p = make_ptrs(b, field, src, sc.nfld);
   p.mode = mode;
   p.ez = (const double *)ez;
   p.eloss = eloss;
+  p.wake = (const double *)wake;
   if (mode == 1) deposit = 0;
   dim3 grid((np + block - 1) / block, ns);
   cudaStream_t s = (cudaStream_t)L.stream;

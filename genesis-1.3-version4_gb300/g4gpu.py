@@ -54,7 +54,8 @@ ABI_SYMBOLS = [
     "g4gpu_dpi_info", "g4gpu_dpi_field", "g4gpu_dpi_beam", "g4gpu_dpi_field_from", "g4gpu_dpi_beam_from",
     "g4gpu_dpi_close", "g4gpu_get_stream",
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
-    "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc",
+    "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc", "g4gpu_host_single_wakes",
+    "g4gpu_set_wake",
     "g4gpu_set_graph_mode", "g4gpu_autotune", "g4gpu_batch_create", "g4gpu_batch_destroy",
     "g4gpu_batch_member", "g4gpu_batch_run", "g4gpu_batch_synchronize",
     "g4gpu_mlp_create", "g4gpu_mlp_destroy", "g4gpu_mlp_last_error", "g4gpu_mlp_num_params",
@@ -162,6 +163,8 @@ def load_library(path=None):
     L.g4gpu_host_gauss_hermite.argtypes = [pd, d, i, pd]
     L.g4gpu_host_fc.argtypes = [d, i, i]
     L.g4gpu_host_fc.restype = d
+    L.g4gpu_host_single_wakes.argtypes = [i, d, d, d, d, i, d, d, d, d, pd, pd, pd]
+    L.g4gpu_set_wake.argtypes = [vp, i, d, pd, pd, pd, pd, d, d, i]
     L.g4gpu_set_graph_mode.argtypes = [vp, i]
     L.g4gpu_autotune.argtypes = [vp, P(i), P(i), P(i)]
     L.g4gpu_set_launch_shapes.argtypes = [vp, i, i, i]
@@ -238,6 +241,19 @@ def host_gauss_hermite(par, gridmax, ngrid):
 
 def host_fc(aw, helical, h):
     return _lib().g4gpu_host_fc(aw, int(helical), h)
+
+
+def host_single_wakes(ns, ds, radius=2.5e-3, conductivity=0.0, relaxation=0.0, roundpipe=True, gap=0.0, lgap=1.0,
+                      hrough=0.0, lrough=1.0):
+    """Single-particle wakes (resistive, geometric, roughness) on ns points spaced ds,
+    with the &wake namelist's parameters and defaults."""
+    out = [np.zeros(int(ns)) for _ in range(3)]
+    rc = _lib().g4gpu_host_single_wakes(int(ns), float(ds), float(radius), float(conductivity), float(relaxation),
+                                        int(bool(roundpipe)), float(gap), float(lgap), float(hrough), float(lrough),
+                                        *[_pd(a) for a in out])
+    if rc:
+        raise G4Error(rc, "host_single_wakes: invalid arguments")
+    return tuple(out)
 
 
 class Handle:
@@ -381,6 +397,21 @@ class Handle:
 
     def device_bytes(self):
         return int(self.L.g4gpu_device_bytes(self.h))
+
+    def set_wake(self, ext=None, res=None, geo=None, rou=None, ds=None, ztrans=0.0, radius=2.5e-3,
+                 transient=False):
+        """Wakes for the following steps: external loss per slice (eV/m) and the
+        single-particle wakes on the fine grid (nslice * sample points spaced ds, the
+        reference length by default); ext None switches them off."""
+        if ext is None:
+            self._check(self.L.g4gpu_set_wake(self.h, 0, 0.0, None, None, None, None, 0.0, 0.0, 0))
+            return
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (ext, res, geo, rou)]
+        if arrs[0].size != self.cfg.nslice or not (arrs[1].size == arrs[2].size == arrs[3].size):
+            raise ValueError("ext needs nslice values and res, geo, rou one length")
+        ds = self.cfg.lambda0 if ds is None else ds
+        self._check(self.L.g4gpu_set_wake(self.h, int(arrs[1].size), float(ds), *[_pd(a) for a in arrs],
+                                          float(ztrans), float(radius), int(bool(transient))))
 
     def set_efield(self, rmax=0.0, ngrid=100, nz=0, nphi=0, longrange=False):
         """Space charge for the following steps (&efield: rmax, ngrid, nz, nphi,

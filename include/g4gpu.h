@@ -169,6 +169,20 @@ int g4gpu_get_field(g4gpu_handle h, int ifld, double *field, int *first, double 
  * (EFieldSolver.cpp:56-272) in BeamSolver::advance (src/Core/BeamSolver.cpp:43-61). */
 int g4gpu_set_efield(g4gpu_handle h, double rmax, int ngrid, int nz, int nphi, int longrange);
 
+/* Wakes for the following steps: Collective::initWake (src/Core/Collective.cpp:39-107)
+ * as the &wake namelist (src/Main/Wake.cpp:47-135) calls it. ns_hr fine points spaced
+ * ds cover the window (nslice * sample of them, ds the reference length); ext
+ * [nslice]: the external loss of every slice (eV/m, &wake loss); res, geo, rou
+ * [ns_hr]: the single-particle wakes (g4gpu_host_single_wakes). ztrans, radius,
+ * transient are kept as the reference keeps them; its transient cut is computed but
+ * not applied, so they do not change the result. The wake of every slice
+ * (Collective::update, Collective.cpp:132-187) is computed on the device from the
+ * window's current, here and on every later g4gpu_load_beam, and every step adds
+ * loss * dz / eev to each particle's gamma after the energy-phase integration
+ * (Collective::apply, Collective.cpp:109-129). ext = NULL switches wakes off. */
+int g4gpu_set_wake(g4gpu_handle h, int ns_hr, double ds, const double *ext, const double *res, const double *geo,
+                   const double *rou, double ztrans, double radius, int transient);
+
 /* Runs integration steps istep0 .. istep0+nsteps-1 of the lattice on the device,
  * each made of the stages selected by `stages` in the order of Gencore.cpp:118-147.
  * Asynchronous: returns once the work is queued on the handle's stream. */
@@ -404,6 +418,16 @@ int g4gpu_host_gauss_hermite(const double *par, double gridmax, int ngrid, doubl
 
 /* Undulator coupling fc(h) (src/Core/Undulator.cpp:141-167). */
 double g4gpu_host_fc(double aw, int helical, int h);
+
+/* Single-particle longitudinal wakes on ns points spaced ds, for g4gpu_set_wake:
+ * resistive wall (conductivity, relaxation c tau, round pipe of radius `radius` or
+ * parallel plates of half gap `radius`), geometric (gaps of length gap every lgap) and
+ * surface roughness (height hrough, period lrough); a zero conductivity, gap or hrough
+ * gives zeros for that wake. Replaces Wake::singleWakeResistive, singleWakeGeometric
+ * and singleWakeRoughness (src/Main/Wake.cpp:140-434) with the same numerical recipe. */
+int g4gpu_host_single_wakes(int ns, double ds, double radius, double conductivity, double relaxation,
+                            int roundpipe, double gap, double lgap, double hrough, double lrough, double *res,
+                            double *geo, double *rou);
 
 #ifdef __cplusplus
 }

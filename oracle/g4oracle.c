@@ -536,6 +536,8 @@ typedef struct {
   /* space charge: the slice's short-range field per particle and its long-range loss */
   const double *sc_ez;
   double sc_eloss;
+  /* wakes: the loss of every slice (eV/m), NULL without &wake */
+  const double *wake_loss;
 } step_ctx;
 
 /* TrackBeam::track, TrackBeam.cpp:8-116 (no chicane: the lattice has none) */
@@ -1081,6 +1083,89 @@ static void sc_short_range(const step_ctx *c, int is, double *rmax, double *ez) 
   free(csrc), free(clow), free(cmid), free(cupp), free(celm), free(gam);
 }
 
+/* ---- wakes (&wake), Collective.cpp ---------------------------------------- */
+static struct {
+  int on, ns, nslice, transient;
+  double ds, ztrans, radius;
+  double *ext, *res, *geo, *rou;
+} wk = {0, 0, 0, 0, 0, 0, 0, NULL, NULL, NULL, NULL};
+
+/* Collective::initWake (Collective.cpp:39-107) for the following orc_run_steps calls:
+ * the external loss ext[nslice] (eV/m) and the single-particle wakes res, geo, rou on
+ * ns_hr points spaced ds, whose first points are halved (self-loading theorem); on = 0
+ * switches the wake off. */
+void orc_set_wake(int on, int ns_hr, int nslice, double ds, const double *ext, const double *res,
+                  const double *geo, const double *rou, double ztrans, double radius, int transient) {
+  free(wk.ext), free(wk.res), free(wk.geo), free(wk.rou);
+  wk.ext = wk.res = wk.geo = wk.rou = NULL;
+  wk.on = on != 0;
+  if (!wk.on) return;
+  wk.ns = ns_hr;
+  wk.nslice = nslice;
+  wk.ds = ds;
+  wk.ztrans = ztrans;
+  wk.radius = radius;
+  wk.transient = transient;
+  wk.ext = malloc(sizeof(double) * nslice);
+  wk.res = malloc(sizeof(double) * ns_hr);
+  wk.geo = malloc(sizeof(double) * ns_hr);
+  wk.rou = malloc(sizeof(double) * ns_hr);
+  memcpy(wk.ext, ext, sizeof(double) * nslice);
+  memcpy(wk.res, res, sizeof(double) * ns_hr);
+  memcpy(wk.geo, geo, sizeof(double) * ns_hr);
+  memcpy(wk.rou, rou, sizeof(double) * ns_hr);
+  wk.geo[0] *= 0.5;
+  wk.res[0] *= 0.5;
+  wk.rou[0] *= 0.5;
+}
+
+/* Collective::update for a single rank (Collective.cpp:132-187): the slices' current
+ * interpolated to the fine grid (electrons per fine slice) and its derivative, then
+ * the wake of every slice from the fine points ahead of it, averaged over the slice's
+ * `sample` fine points. The transient cut is computed there but not applied. */
+static void wake_update(const double *current, int nslice, double *wakeint) {
+  const unsigned ns = (unsigned)wk.ns;
+  const int ncur = nslice;
+  const double ds = wk.ds, dscur = ds * ns / ncur;
+  double *cur = malloc(sizeof(double) * (ncur + 1));
+  double *curh = malloc(sizeof(double) * ns), *dcur = malloc(sizeof(double) * ns);
+  memcpy(cur, current, sizeof(double) * ncur);
+  cur[ncur] = 0;
+  for (int is = 0; is < (int)ns; is++) {
+    double s = ds * (double)is;
+    unsigned idx = (unsigned)(int)floor(s / dscur);
+    double wei = 1 - (s - idx * dscur) / dscur;
+    curh[is] = wei * cur[idx] + (1 - wei) * cur[idx + 1];
+    curh[is] *= ds / kCe;
+    dcur[is] = -(cur[idx + 1] - cur[idx]) * ds / kCe / dscur;
+  }
+  int sample = (int)(dscur / ds);
+  if (sample < 1) sample = 1;
+  for (int ic = 0; ic < nslice; ic++) {
+    double w = 0;
+    int is0 = ic * sample;
+    for (int j = 0; j < sample; j++) {
+      int is = is0 + j;
+      for (unsigned long i = 0; i < ns - is; i++) {
+        w += curh[is + i] * (wk.res[i] + wk.rou[i]);
+        w += dcur[is + i] * wk.geo[i];
+      }
+    }
+    wakeint[ic] = w / (double)sample;
+  }
+  free(cur), free(curh), free(dcur);
+}
+
+/* Collective::apply (Collective.cpp:109-129): every particle of a slice gains
+ * loss * delz / eev */
+static void apply_wake(step_ctx *c, int is0, int is1) {
+  for (int is = is0; is < is1; is++) {
+    double dg = c->wake_loss[is] * c->delz / kEev;
+    part_t *b = c->beam + (size_t)is * c->npart;
+    for (int ip = 0; ip < c->npart; ip++) b[ip].gamma += dg;
+  }
+}
+
 static void run_transverse_first(void *ctx, int i0, int i1) { transverse_slices((step_ctx *)ctx, i0, i1, 0); }
 static void run_transverse_second(void *ctx, int i0, int i1) { transverse_slices((step_ctx *)ctx, i0, i1, 1); }
 
@@ -1088,6 +1173,7 @@ static void run_push(void *ctx, int i0, int i1) {
   step_ctx *c = (step_ctx *)ctx;
   transverse_slices(c, i0, i1, 0);
   push_slices(c, i0, i1);
+  if (c->wake_loss) apply_wake(c, i0, i1);
   transverse_slices(c, i0, i1, 1);
 }
 static void run_field(void *ctx, int i0, int i1) { field_slices((step_ctx *)ctx, i0, i1); }
@@ -1152,6 +1238,16 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
   cplx *fft_tabs = NULL;
   if (solver) fft_tabs = malloc(sizeof(cplx) * 2 * n2 * nfld);
 
+  /* the wake of every slice: Collective::update on its first use after initWake (and,
+   * transient, on every step, with the same result); the loss adds the external one */
+  double *wake_loss = NULL;
+  if (wk.on && wk.nslice == ns) {
+    wake_loss = malloc(sizeof(double) * ns);
+    wake_update(current, ns, wake_loss);
+    for (int i = 0; i < ns; i++) wake_loss[i] = wk.ext[i] + wake_loss[i];
+  }
+  c.wake_loss = wake_loss;
+
   for (int istep = 0; istep < nsteps; istep++) {
     c.st = get_step(lat, istep);
     c.delz = c.st.dz;
@@ -1180,6 +1276,7 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
           c.sc_eloss = eloss[is];
           push_slices(&c, is, is + 1);
         }
+        if (c.wake_loss) apply_wake(&c, 0, ns);
         c.sc_ez = NULL;
         free(eloss);
         free(ez);
@@ -1214,6 +1311,7 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
   }
   free(coef);
   free(fft_tabs);
+  free(wake_loss);
   return 0;
 }
 

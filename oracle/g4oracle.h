@@ -101,6 +101,12 @@ void orc_diag_field(int ns, int ngrid, double gridmax, double lambda0, int harm,
  * longitudinal and nphi azimuthal modes of the short-range field, longrange the
  * long-range loss. nz = 0 and longrange = 0 switch it off (the default). */
 void orc_set_efield(double rmax, int ngrid, int nz, int nphi, int longrange);
+
+/* Wakes (&wake, Collective::initWake, Collective.cpp:39-107) for the following
+ * orc_run_steps calls: external loss ext[nslice] (eV/m), single-particle wakes res, geo,
+ * rou[ns_hr] on the fine grid spaced ds; on = 0 switches them off. */
+void orc_set_wake(int on, int ns_hr, int nslice, double ds, const double *ext, const double *res,
+                  const double *geo, const double *rou, double ztrans, double radius, int transient);
 /* Window ("Global/") values from the raw sums: DiagBeam (Diagnostic.cpp:551-606),
  * out[6] = energy, energyspread, xposition, xsize, yposition, ysize; DiagField
  * (Diagnostic.cpp:902-975), out[11] = energy [J], xposition, xsize, yposition, ysize,

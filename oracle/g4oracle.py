@@ -75,6 +75,31 @@ class _Lib:
             L.orc_deposit_source.argtypes = [_pd, _i, _i, _i, _pd, _pd, _d, _i, _i, _d, _pd]
             L.orc_adi_advance.argtypes = [_i, _i, _i, _d, _d, _d, _pd, _pd]
 
+    def set_wake(self, ext=None, res=None, geo=None, rou=None, ds=1e-10, ztrans=0.0, radius=2.5e-3,
+                 transient=False):
+        """Wakes (&wake) for the following run_steps calls: external loss per slice (eV/m)
+        and the single-particle wakes on the fine grid; no arguments switch them off."""
+        f = getattr(self.lib, self.p + "set_wake")
+        f.argtypes = [_i, _i, _i, _d, _pd, _pd, _pd, _pd, _d, _d, _i]
+        if ext is None:
+            f(0, 0, 0, 0.0, None, None, None, None, 0.0, 0.0, 0)
+            return
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (ext, res, geo, rou)]
+        self._wake_keep = arrs
+        f(1, int(arrs[1].size), int(arrs[0].size), float(ds), *[_ptr(a) for a in arrs], float(ztrans),
+          float(radius), int(bool(transient)))
+
+    def single_wakes(self, ns, ds, radius=2.5e-3, conductivity=0.0, relaxation=0.0, roundpipe=True, gap=0.0,
+                     lgap=1.0, hrough=0.0, lrough=1.0):
+        """The reference's single-particle wakes (resistive, geometric, roughness) on ns
+        points spaced ds; compiled reference only."""
+        f = getattr(self.lib, self.p + "single_wakes")
+        f.argtypes = [_i, _d, _d, _d, _d, _i, _d, _d, _d, _d, _pd, _pd, _pd]
+        out = [np.zeros(ns) for _ in range(3)]
+        f(int(ns), float(ds), float(radius), float(conductivity), float(relaxation), int(bool(roundpipe)),
+          float(gap), float(lgap), float(hrough), float(lrough), *[_ptr(a) for a in out])
+        return tuple(out)
+
     def set_efield(self, rmax=0.0, ngrid=0, nz=0, nphi=0, longrange=False):
         """Space charge (&efield) for the following run_steps calls; the defaults switch it off."""
         f = getattr(self.lib, self.p + "set_efield")

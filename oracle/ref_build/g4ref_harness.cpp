@@ -60,7 +60,32 @@ static void fill_undulator(Undulator *und, int nsteps, const double *tab, double
 static double g_sc_rmax = 0;
 static int g_sc_ngrid = 0, g_sc_nz = 0, g_sc_nphi = 0, g_sc_longrange = 0;
 
+// &wake of the following g4ref_run_steps calls (Wake.cpp:123: Beam::initWake): the
+// external loss per slice and the single-particle wakes on the fine grid of ns_hr
+// points spaced ds.
+static bool g_wk_on = false;
+static unsigned g_wk_ns = 0;
+static double g_wk_ds = 0, g_wk_ztrans = 0, g_wk_radius = 0;
+static bool g_wk_transient = false;
+static std::vector<double> g_wk_ext, g_wk_res, g_wk_geo, g_wk_rou;
+
 extern "C" {
+
+// on = 0 switches the wake off; ext has nslice entries, res / geo / rou ns_hr
+void g4ref_set_wake(int on, int ns_hr, int nslice, double ds, const double *ext, const double *res,
+                    const double *geo, const double *rou, double ztrans, double radius, int transient) {
+  g_wk_on = on != 0;
+  if (!g_wk_on) return;
+  g_wk_ns = static_cast<unsigned>(ns_hr);
+  g_wk_ds = ds;
+  g_wk_ext.assign(ext, ext + nslice);
+  g_wk_res.assign(res, res + ns_hr);
+  g_wk_geo.assign(geo, geo + ns_hr);
+  g_wk_rou.assign(rou, rou + ns_hr);
+  g_wk_ztrans = ztrans;
+  g_wk_radius = radius;
+  g_wk_transient = transient != 0;
+}
 
 void g4ref_set_efield(double rmax, int ngrid, int nz, int nphi, int longrange) {
   g_sc_rmax = rmax;
@@ -86,6 +111,11 @@ int g4ref_run_steps(int nsteps, const double *tab, double gammaref, int ns, int 
   beam.init(ns, 1, reflength, reflength * sample, 0.0, false);
   if (g_sc_nz > 0 || g_sc_longrange)
     beam.initEField(g_sc_rmax, g_sc_ngrid, g_sc_nz, g_sc_nphi, reflength, g_sc_longrange != 0);
+  if (g_wk_on) {
+    if (g_wk_ext.size() != static_cast<size_t>(ns)) return 2;
+    beam.initWake(g_wk_ns, static_cast<unsigned>(ns), g_wk_ds, g_wk_ext.data(), g_wk_res.data(), g_wk_geo.data(),
+                  g_wk_rou.data(), g_wk_ztrans, g_wk_radius, g_wk_transient);
+  }
   for (int is = 0; is < ns; is++) {
     beam.current[is] = current[is];
     beam.beam[is].resize(npart);

@@ -16,7 +16,11 @@ Fixtures (numpy .npz):
   spacecharge.npz integration steps with space charge (&efield): short-range modes,
                  the long-range loss, both; input state, parameters and output state
 
-`python tests/golden/gen_golden.py spacecharge` regenerates only spacecharge.npz.
+  wakes.npz      the reference's single-particle wakes (resistive round and flat pipe,
+                 geometric, roughness) for several &wake settings, and integration steps
+                 with wakes (Collective::update / apply) on windows of sample 1 and 3
+
+`python tests/golden/gen_golden.py spacecharge` (or `wakes`) regenerates only that file.
 
 The reference's CI check of Example1 (examples/Example1-SteadyState/TEST_power.py)
 expects a final power of 0.932785e9 W within 30 %; example1.npz records what the
@@ -207,6 +211,78 @@ def gen_space_charge(r):
     np.savez_compressed(os.path.join(HERE, "spacecharge.npz"), **d)
 
 
+WAKE_SETS = {
+    "cu_round": dict(radius=2.5e-3, conductivity=5.813e7, relaxation=8.1e-6, roundpipe=True),
+    "al_flat": dict(radius=3.0e-3, conductivity=3.571e7, relaxation=2.4e-6, roundpipe=False),
+    "geo_round": dict(radius=2.5e-3, gap=1e-3, lgap=0.5, roundpipe=True),
+    "geo_flat": dict(radius=2.5e-3, gap=2e-3, lgap=1.5, roundpipe=False),
+    "rough": dict(radius=2.5e-3, hrough=1e-7, lrough=1e-4),
+    "all": dict(radius=2.0e-3, conductivity=5.813e7, relaxation=8.1e-6, roundpipe=True, gap=1e-3, lgap=0.5,
+                hrough=1e-7, lrough=1e-4),
+}
+WAKE_NS, WAKE_DS = 200, 1e-10
+
+
+def wake_cases(r):
+    """Windows with wakes: the single-particle wakes of the "all" setting scaled so that
+    each changes gamma by about 1e-3 over the lattice (like the FEL interaction of these
+    windows; over a few slices the unscaled wakes are too weak to see), an external loss
+    per slice; windows of sample 1 (4 slices, 4 fine points) and sample 3 (5 slices,
+    15 fine points, current ramp), and a transient wake."""
+    res, geo, rou = r.single_wakes(64, WAKE_DS, **WAKE_SETS["all"])
+    res, geo, rou = res * 1e2, geo * 30.0, rou * 1e3
+    lat = T.undulator_lattice(1.7, 0.015, 6, 2, 1e-10, 11357.8, quad_k1=1.5, quad_l=0.08)
+    cases = []
+    cur = np.array([3000.0, 2500.0, 1000.0, 3000.0])
+    part = r.load_beam(T.slice_params(4, 11357.8, 2.0, 0.4e-6, 15.0, currents=cur), 0, 64, 4, 7, 1, 1e-10, 1.0)
+    gh = r.gauss_hermite(T.gauss_field_par(1e-10, 1e5, 20e-6), 6e-5, 25)
+    fld = np.stack([gh * (1 + 0.2j * k) for k in range(4)])[None]
+    base = dict(lat=lat, gammaref=11357.8, part=part, cur=cur, harm=[1], gridmax=[6e-5], fields=fld, first=[0],
+                time_run=1, periodic=0, sample=1.0)
+    ext = np.array([-2000.0, 500.0, 0.0, 1500.0])
+    cases.append(dict(base, name="s1", wake=dict(ext=ext, res=res[:4], geo=geo[:4], rou=rou[:4], ds=WAKE_DS,
+                                                 ztrans=0.0, radius=2.0e-3, transient=False)))
+    cases.append(dict(base, name="s1_transient", wake=dict(ext=0 * ext, res=res[:4], geo=geo[:4], rou=rou[:4],
+                                                           ds=WAKE_DS, ztrans=-1.0, radius=2.0e-3, transient=True)))
+    cur5 = np.linspace(500.0, 3500.0, 5)
+    part5 = r.load_beam(T.slice_params(5, 11357.8, 2.0, 0.4e-6, 15.0, currents=cur5), 0, 48, 4, 3, 1, 1e-10, 3.0)
+    fld5 = np.stack([gh * (1 - 0.1j * k) for k in range(5)])[None]
+    cases.append(dict(base, name="s3", part=part5, cur=cur5, fields=fld5, sample=3.0,
+                      wake=dict(ext=np.linspace(-1000.0, 1000.0, 5), res=res[:15], geo=geo[:15], rou=rou[:15],
+                                ds=WAKE_DS, ztrans=0.0, radius=2.0e-3, transient=False)))
+    return cases
+
+
+def gen_wakes(r):
+    d = {}
+    for name, kw in WAKE_SETS.items():
+        res, geo, rou = r.single_wakes(WAKE_NS, WAKE_DS, **kw)
+        d[f"single_{name}_res"], d[f"single_{name}_geo"], d[f"single_{name}_rou"] = res, geo, rou
+        d[f"single_{name}_par"] = np.array([kw.get("radius", 2.5e-3), kw.get("conductivity", 0.0),
+                                            kw.get("relaxation", 0.0), float(kw.get("roundpipe", True)),
+                                            kw.get("gap", 0.0), kw.get("lgap", 1.0), kw.get("hrough", 0.0),
+                                            kw.get("lrough", 1.0)])
+    d["single_ns_ds"] = np.array([WAKE_NS, WAKE_DS])
+    for c in wake_cases(r):
+        n = c["name"]
+        for k in ("lat", "part", "cur", "harm", "gridmax", "fields", "first"):
+            d[f"{n}_{k}"] = np.asarray(c[k])
+        w = c["wake"]
+        for k in ("ext", "res", "geo", "rou"):
+            d[f"{n}_wake_{k}"] = np.asarray(w[k])
+        d[f"{n}_wake_par"] = np.array([w["ds"], w["ztrans"], w["radius"], float(w["transient"])])
+        d[f"{n}_args"] = np.array([c["gammaref"], c["time_run"], c["periodic"], c["sample"]])
+        r.set_wake(**w)
+        out = r.run_steps(c["lat"], c["gammaref"], c["part"], c["cur"], 1e-10, c["sample"], c["harm"],
+                          c["gridmax"], c["fields"], c["first"], time_run=c["time_run"], periodic=c["periodic"],
+                          stages=7)
+        r.set_wake()
+        d[f"{n}_out_part"] = out[0]
+        d[f"{n}_out_fields"] = out[1]
+        d[f"{n}_out_first"] = out[2]
+    np.savez_compressed(os.path.join(HERE, "wakes.npz"), **d)
+
+
 LAT_FROM_OUT = {"aw": "aw", "ax": "ax", "ay": "ay", "ku": "ku", "kx": "kx", "ky": "ky",
                 "gradx": "gradx", "grady": "grady", "qf": "qf", "qx": "qx", "qy": "qy",
                 "cx": "cx", "cy": "cy", "dz": "dz", "slip": "slippage", "phase": "phaseshift",
@@ -308,7 +384,11 @@ def main():
     if sys.argv[1:] == ["spacecharge"]:
         gen_space_charge(r)
         return
+    if sys.argv[1:] == ["wakes"]:
+        gen_wakes(r)
+        return
     gen_space_charge(r)
+    gen_wakes(r)
     gen_streams(r)
     gen_loading(r)
     gen_steps(r)

@@ -1,7 +1,7 @@
 """CPU checks of the C ABI library: it loads without a GPU, exports every symbol
 that include/g4gpu.h declares, rejects bad configurations, and its host-side
-loading (quiet loading, shot noise, Gauss-Hermite seed, coupling fc) is bit-exact
-with the reference's fixtures."""
+loading (quiet loading, shot noise, Gauss-Hermite seed, coupling fc) and the
+single-particle wakes are bit-exact with the reference's fixtures."""
 import os
 import platform
 import re
@@ -74,6 +74,32 @@ def test_host_gauss_hermite_matches_reference(lib, name):
     gm, ng = d[name + "_grid"]
     got = g4gpu.host_gauss_hermite(d[name + "_par"], gm, int(ng))
     assert np.array_equal(got, d[name]) if EXACT else np.allclose(got, d[name], rtol=1e-14)
+
+
+@pytest.mark.parametrize("name", ["cu_round", "al_flat", "geo_round", "geo_flat", "rough", "all"])
+def test_host_single_wakes_match_reference(lib, name):
+    """Resistive wall (round pipe, flat chamber), geometric and roughness wakes of the
+    &wake settings of tests/golden/wakes.npz against the reference's Wake class."""
+    import g4gpu
+    d = golden("wakes.npz")
+    ns, ds = d["single_ns_ds"]
+    radius, cond, relax, roundpipe, gap, lgap, hrough, lrough = d[f"single_{name}_par"]
+    got = g4gpu.host_single_wakes(int(ns), ds, radius=radius, conductivity=cond, relaxation=relax,
+                                  roundpipe=bool(roundpipe), gap=gap, lgap=lgap, hrough=hrough, lrough=lrough)
+    for k, g in zip(("res", "geo", "rou"), got):
+        want = d[f"single_{name}_{k}"]
+        if EXACT:
+            assert np.array_equal(g, want), k
+        else:
+            assert np.allclose(g, want, rtol=1e-12, atol=1e-12 * np.abs(want).max()), k
+
+
+def test_host_single_wakes_reject_bad_arguments(lib):
+    import g4gpu
+    for kw in (dict(ns=0, ds=1e-10), dict(ns=8, ds=0.0), dict(ns=8, ds=1e-10, radius=0.0),
+               dict(ns=8, ds=1e-10, gap=1e-3, lgap=0.0), dict(ns=8, ds=1e-10, hrough=1e-7, lrough=0.0)):
+        with pytest.raises(g4gpu.G4Error):
+            g4gpu.host_single_wakes(**kw)
 
 
 def test_host_fc_matches_reference(lib):

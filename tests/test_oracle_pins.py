@@ -240,3 +240,29 @@ def test_space_charge_grid_extent_carries_over(oracle):
     finally:
         oracle.set_efield()
     assert np.array_equal(p1, p2) and np.array_equal(f1, f2)
+
+
+@pytest.mark.parametrize("case", ["s1", "s1_transient", "s3"])
+def test_wake_steps(oracle, case):
+    """Wakes (&wake, Collective.cpp): the oracle's restatement of the wake update and
+    its application against the reference run with its own Collective
+    (tests/golden/wakes.npz): windows of sample 1 and 3 with an external loss and the
+    resistive, geometric and roughness wakes, and a transient wake."""
+    d = golden("wakes.npz")
+    g = lambda k: d[f"{case}_{k}"]
+    gammaref, time_run, periodic, sample = g("args")
+    ds, ztrans, radius, transient = g("wake_par")
+    oracle.set_wake(g("wake_ext"), g("wake_res"), g("wake_geo"), g("wake_rou"), ds, ztrans, radius, bool(transient))
+    try:
+        part, fld, first, _ = oracle.run_steps(g("lat"), gammaref, g("part"), g("cur"), 1e-10, sample, g("harm"),
+                                               g("gridmax"), g("fields"), g("first"), time_run=int(time_run),
+                                               periodic=int(periodic), stages=7)
+    finally:
+        oracle.set_wake()
+    if EXACT:
+        assert np.array_equal(part, g("out_part"))
+        assert np.array_equal(fld, g("out_fields"))
+    else:
+        assert np.allclose(part, g("out_part"), rtol=1e-12, atol=0)
+        assert np.allclose(fld, g("out_fields"), rtol=1e-12, atol=1e-12 * np.abs(g("out_fields")).max())
+    assert np.array_equal(first, g("out_first"))
