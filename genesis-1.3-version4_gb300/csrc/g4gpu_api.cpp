@@ -516,6 +516,10 @@ int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *tab) {
     h->slip[i] = r[G4GPU_LAT_SLIP];
   }
   h->nsteps = nsteps;
+  // captured step sequences hold the previous lattice's constants
+  for (auto &g : h->graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+  h->graphs.clear();
   if (h->coef) {
     cudaFree(h->coef);
     h->bytes -= h->coef_bytes;
@@ -538,6 +542,78 @@ int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *tab) {
       G4_CUDA(h, cudaMemcpy(h->coef, coefs.data(), n * sizeof(cd), cudaMemcpyHostToDevice));
     }
   }
+  return G4GPU_OK;
+}
+
+namespace {
+// TrackBeam::matmul (TrackBeam.cpp:246-258): m = e m
+void chicane_matmul(double m[4][4], const double e[4][4]) {
+  double t[4][4];
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) {
+      t[i][j] = 0;
+      for (int k = 0; k < 4; k++) t[i][j] += e[i][k] * m[k][j];
+    }
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) m[i][j] = t[i][j];
+}
+
+// The transfer matrix of TrackBeam::applyChicane (TrackBeam.cpp:131-222): bend, edge,
+// drift, edge, bend, middle drift, bend, edge, drift, edge, bend, then a drift back over
+// the chicane's length, which the step's two half steps add again
+void chicane_matrix(double angle, double lb, double ld, double lt, double m[4][4]) {
+  double d1[4][4], d2[4][4], d3[4][4], bp[4][4], bn[4][4], ep[4][4], en[4][4];
+  double *all[] = {&m[0][0], &d1[0][0], &d2[0][0], &d3[0][0], &bp[0][0], &bn[0][0], &ep[0][0], &en[0][0]};
+  for (double *a : all)
+    for (int i = 0; i < 16; i++) a[i] = (i % 5 == 0) ? 1 : 0;
+  d1[0][1] = d1[2][3] = ld / std::cos(angle);
+  d2[0][1] = d2[2][3] = lt - 4 * lb - 2 * ld;
+  d3[0][1] = d3[2][3] = -lt;
+  const double R = lb / std::sin(angle), L = R * angle;
+  bp[2][3] = L;
+  bp[0][0] = std::cos(angle);
+  bp[0][1] = R * std::sin(angle);
+  bp[1][0] = -std::sin(angle) / R;
+  bp[1][1] = std::cos(angle);
+  bn[2][3] = L;
+  bn[0][0] = std::cos(-angle);
+  bn[0][1] = R * std::sin(-angle) * -1;
+  bn[1][0] = -std::sin(-angle) / R * -1;
+  bn[1][1] = std::cos(-angle);
+  const double efoc = std::tan(angle) / R;
+  ep[1][0] = efoc;
+  ep[3][2] = -efoc;
+  en[1][0] = -efoc * -1;
+  en[3][2] = efoc * -1;
+  const double(*seq[])[4] = {bp, ep, d1, en, bn, d2, bn, en, d1, ep, bp, d3};
+  for (auto e : seq) chicane_matmul(m, e);
+}
+}  // namespace
+
+int g4gpu_set_chicanes(g4gpu_handle h, int nsteps, const double *table) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (nsteps != h->nsteps || (nsteps > 0 && !table))
+    return fail(h, G4GPU_ERR_ARG, "the chicane table needs one row per lattice step");
+  for (int i = 0; i < nsteps; i++) {
+    const double *r = table + 4 * (size_t)i;
+    g4::StepConst &s = h->steps[i];
+    const double angle = r[0], lb = r[1], ld = r[2], lt = r[3];
+    s.chic = angle != 0;
+    if (!s.chic) continue;
+    if (!(lb > 0) || !std::isfinite(angle) || std::fabs(angle) >= 2 * std::asin(1.0) / 2)
+      return fail(h, G4GPU_ERR_ARG, "chicane rows need lb > 0 and |angle| below pi / 2");
+    double m[4][4];
+    chicane_matrix(angle, lb, ld, lt, m);
+    const double cm[8] = {m[0][0], m[0][1], m[1][0], m[1][1], m[2][2], m[2][3], m[3][2], m[3][3]};
+    std::copy(cm, cm + 8, s.cm);
+    // TrackBeam::applyR56 (TrackBeam.cpp:265-268)
+    double r56 = (4 * lb / std::sin(angle) * (1 - angle / std::tan(angle)) + 2 * ld * std::tan(angle) /
+                  std::cos(angle)) * angle;
+    s.r56 = r56 * 4 * std::asin(1) / h->cfg.lambda0 / h->cfg.gammaref;
+  }
+  for (auto &g : h->graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+  h->graphs.clear();
   return G4GPU_OK;
 }
 

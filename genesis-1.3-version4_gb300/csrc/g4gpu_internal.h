@@ -50,6 +50,13 @@ struct StepConst {
   double xku;         // undulator wavenumber, or xks/(2 gamma0^2) in drifts
   double delz;
   double gammaref;
+  // chicane of the step (g4gpu_set_chicanes): its transfer matrix, applied before the
+  // first half step (TrackBeam::applyChicane, TrackBeam.cpp:131-244), elements
+  // m00 m01 m10 m11 m22 m23 m32 m33, and the phase shift R56 2 pi / (lambda0 gamma0)
+  // per unit of gamma - gamma0 after the integration (TrackBeam::applyR56, :260-277)
+  int chic;
+  double cm[8];
+  double r56;
   FieldStep f[G4GPU_MAX_FIELDS];
 };
 
@@ -69,6 +76,9 @@ struct StepConstF {
   double autophase;
   long long autophase_q;  // autophase as a Q32.32 turn count
   double gammaref;
+  int chic;  // StepConst::chic, cm, r56
+  float cm[8];
+  float r56;
   FieldStepF f[G4GPU_MAX_FIELDS];
 };
 StepConstF to_float(const StepConst &s, int npart);

@@ -67,6 +67,9 @@ StepConstF to_float(const StepConst &s, int npart) {
   f.autophase = s.autophase;
   f.autophase_q = (long long)llrint(s.autophase * (4294967296.0 / kTwoPiHost));
   f.gammaref = s.gammaref;
+  f.chic = s.chic;
+  for (int i = 0; i < 8; i++) f.cm[i] = (float)s.cm[i];
+  f.r56 = (float)s.r56;
   for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
     const FieldStep &a = s.f[k];
     FieldStepF &b = f.f[k];
@@ -138,6 +141,15 @@ __device__ __forceinline__ void transverse_f(const StepConstF &sc, bool last, fl
   if (last && sc.corr) {
     px += sc.cxk;
     py += sc.cyk;
+  } else if (!last && sc.chic) {
+    // TrackBeam::applyChicane (TrackBeam.cpp:224-240)
+    const float gz = g * sqrtf(1.f - (1.f + px * px + py * py) / (g * g));
+    float tmp = x;
+    x = sc.cm[0] * tmp + sc.cm[1] * px / gz;
+    px = sc.cm[2] * tmp * gz + sc.cm[3] * px;
+    tmp = y;
+    y = sc.cm[4] * tmp + sc.cm[5] * py / gz;
+    py = sc.cm[6] * tmp * gz + sc.cm[7] * py;
   }
   float a = 1.f + sc.aw_t * sc.aw_t + px * px + py * py;
   float gz = g * sqrtf(1.f - a / (g * g));
@@ -335,6 +347,8 @@ __global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, 
   // Collective::apply (Collective.cpp:119-128), before the second half step
   if (p.wake) dg += p.wake[is] * sc.delz;
   th = add_phase(th, dth);
+  // TrackBeam::applyR56 (TrackBeam.cpp:260-277): gamma - gamma0 is the stored offset
+  if (sc.chic) th = add_phase(th, sc.r56 * dg);
   float g = g0 + dg;
 
   transverse_f(sc, true, g, x, y, px, py);

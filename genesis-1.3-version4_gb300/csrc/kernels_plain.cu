@@ -67,6 +67,16 @@ __device__ __forceinline__ void transverse(const StepConst &sc, bool last, doubl
   if (last && sc.corr) {
     px += sc.cxk;
     py += sc.cyk;
+  } else if (!last && sc.chic) {
+    // TrackBeam::applyChicane (TrackBeam.cpp:224-240): the chicane's transfer minus the
+    // drift over its length, which the two half steps then add back
+    const double gz = sqrt(g * g - 1 - px * px - py * py);
+    double tmp = x;
+    x = sc.cm[0] * tmp + sc.cm[1] * px / gz;
+    px = sc.cm[2] * tmp * gz + sc.cm[3] * px;
+    tmp = y;
+    y = sc.cm[4] * tmp + sc.cm[5] * py / gz;
+    py = sc.cm[6] * tmp * gz + sc.cm[7] * py;
   }
   double delz = sc.delz * 0.5;
   double gammaz = sqrt(g * g - 1 - sc.aw_t * sc.aw_t - px * px - py * py);
@@ -253,6 +263,8 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
 
   // Collective::apply (Collective.cpp:119-128), before the second half step
   if (p.wake) gamma += p.wake[is] * sc.delz / kEev;
+  // TrackBeam::applyR56 (TrackBeam.cpp:260-277)
+  if (sc.chic) theta += sc.r56 * (gamma - sc.gammaref);
 
   transverse(sc, true, gamma, x, y, px, py);
 

@@ -55,7 +55,7 @@ ABI_SYMBOLS = [
     "g4gpu_dpi_close", "g4gpu_get_stream",
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
     "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc", "g4gpu_host_single_wakes",
-    "g4gpu_set_wake",
+    "g4gpu_set_wake", "g4gpu_set_chicanes",
     "g4gpu_set_graph_mode", "g4gpu_autotune", "g4gpu_batch_create", "g4gpu_batch_destroy",
     "g4gpu_batch_member", "g4gpu_batch_run", "g4gpu_batch_synchronize",
     "g4gpu_mlp_create", "g4gpu_mlp_destroy", "g4gpu_mlp_last_error", "g4gpu_mlp_num_params",
@@ -165,6 +165,7 @@ def load_library(path=None):
     L.g4gpu_host_fc.restype = d
     L.g4gpu_host_single_wakes.argtypes = [i, d, d, d, d, i, d, d, d, d, pd, pd, pd]
     L.g4gpu_set_wake.argtypes = [vp, i, d, pd, pd, pd, pd, d, d, i]
+    L.g4gpu_set_chicanes.argtypes = [vp, i, pd]
     L.g4gpu_set_graph_mode.argtypes = [vp, i]
     L.g4gpu_autotune.argtypes = [vp, P(i), P(i), P(i)]
     L.g4gpu_set_launch_shapes.argtypes = [vp, i, i, i]
@@ -397,6 +398,11 @@ class Handle:
 
     def device_bytes(self):
         return int(self.L.g4gpu_device_bytes(self.h))
+
+    def set_chicanes(self, table):
+        """Chicanes of the lattice steps: [nsteps][4] angle, lb, ld, lt (zero angle: none)."""
+        t = np.ascontiguousarray(table, dtype=np.float64).reshape(-1, 4)
+        self._check(self.L.g4gpu_set_chicanes(self.h, int(t.shape[0]), _pd(t)))
 
     def set_wake(self, ext=None, res=None, geo=None, rou=None, ds=None, ztrans=0.0, radius=2.5e-3,
                  transient=False):

@@ -157,6 +157,16 @@ int g4gpu_load_field(g4gpu_handle h, int ifld, const double *field, int first, d
 /* Copies field ifld back (storage order) with its ring start and slippage. */
 int g4gpu_get_field(g4gpu_handle h, int ifld, double *field, int *first, double *accuslip);
 
+/* Chicanes of the lattice steps: table [nsteps][4] with the bend angle, dipole length lb,
+ * dipole spacing ld and total length lt of the chicane a step covers (0 angle: none), as
+ * Undulator::chic_angle, chic_lb, chic_ld, chic_lt hold them after
+ * Lattice::generateLattice converted the delay to the angle (src/Lattice/Lattice.cpp:
+ * 105-128); nsteps must be the lattice's. A chicane step applies the chicane's transfer
+ * matrix before its first half step (TrackBeam::applyChicane, src/Core/TrackBeam.cpp:
+ * 131-244) and the R56 phase shift after the integration (TrackBeam::applyR56, :260-277).
+ * g4gpu_set_lattice clears them. */
+int g4gpu_set_chicanes(g4gpu_handle h, int nsteps, const double *table);
+
 /* Space charge for the following steps: the &efield namelist (src/Main/EField.cpp:19-39)
  * as Beam::initEField passes it to EFieldSolver::init (src/Core/EFieldSolver.cpp:27-48).
  * rmax: initial extent of the radial grid (it grows to 1.5 times a slice's extreme

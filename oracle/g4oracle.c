@@ -474,11 +474,35 @@ void orc_gauss_hermite(const double *par, double gridmax, int ngrid, double *out
 typedef struct {
   double aw, ax, ay, ku, kx, ky, gradx, grady, qf, qx, qy, cx, cy, dz, slip, phase, z;
   int helical;
+  /* chicane: bend angle (0: none), dipole length, spacing, total length */
+  double angle, lb, ld, lt;
 } step_t;
+
+/* chicanes of the following orc_run_steps calls: [n][4] angle, lb, ld, lt per row of
+ * the lattice passed there */
+static double *chic_tab = NULL;
+static int chic_n = 0;
+
+void orc_set_chicanes(int nsteps, const double *tab) {
+  free(chic_tab);
+  chic_tab = NULL;
+  chic_n = 0;
+  if (nsteps <= 0 || !tab) return;
+  chic_tab = malloc(sizeof(double) * 4 * nsteps);
+  memcpy(chic_tab, tab, sizeof(double) * 4 * nsteps);
+  chic_n = nsteps;
+}
 
 static step_t get_step(const double *lat, int i) {
   const double *r = lat + (size_t)i * G4_LAT_NCOL;
   step_t s;
+  s.angle = s.lb = s.ld = s.lt = 0;
+  if (i < chic_n) {
+    s.angle = chic_tab[4 * i];
+    s.lb = chic_tab[4 * i + 1];
+    s.ld = chic_tab[4 * i + 2];
+    s.lt = chic_tab[4 * i + 3];
+  }
   s.aw = r[G4_LAT_AW]; s.ax = r[G4_LAT_AX]; s.ay = r[G4_LAT_AY]; s.ku = r[G4_LAT_KU];
   s.kx = r[G4_LAT_KX]; s.ky = r[G4_LAT_KY]; s.gradx = r[G4_LAT_GRADX];
   s.grady = r[G4_LAT_GRADY]; s.qf = r[G4_LAT_QF]; s.qx = r[G4_LAT_QX]; s.qy = r[G4_LAT_QY];
@@ -596,6 +620,52 @@ static void apply_plane(const plane_t *pl, double delz, double *x, double *p, do
   }
 }
 
+/* TrackBeam::matmul, TrackBeam.cpp:246-258: m = e m */
+static void mat4_mul(double m[4][4], double e[4][4]) {
+  double t[4][4];
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) {
+      t[i][j] = 0;
+      for (int k = 0; k < 4; k++) t[i][j] += e[i][k] * m[k][j];
+    }
+  memcpy(m, t, sizeof(t));
+}
+
+/* The chicane's transfer matrix and the drift back over its length,
+ * TrackBeam::applyChicane, TrackBeam.cpp:131-222 */
+static void chicane_transfer(const step_t *u, double m[4][4]) {
+  double d1[4][4], d2[4][4], d3[4][4], bp[4][4], bn[4][4], ep[4][4], en[4][4];
+  double(*all[8])[4] = {m, d1, d2, d3, bp, bn, ep, en};
+  for (int a = 0; a < 8; a++)
+    for (int i = 0; i < 4; i++)
+      for (int j = 0; j < 4; j++) all[a][i][j] = i == j ? 1 : 0;
+  double angle = u->angle, lb = u->lb, ld = u->ld, lt = u->lt;
+  d1[0][1] = ld / cos(angle);
+  d1[2][3] = ld / cos(angle);
+  d2[0][1] = lt - 4 * lb - 2 * ld;
+  d2[2][3] = lt - 4 * lb - 2 * ld;
+  d3[0][1] = -lt;
+  d3[2][3] = -lt;
+  double R = lb / sin(angle), Lpath = R * angle;
+  bp[2][3] = Lpath;
+  bp[0][0] = cos(angle);
+  bp[0][1] = R * sin(angle);
+  bp[1][0] = -sin(angle) / R;
+  bp[1][1] = cos(angle);
+  bn[2][3] = Lpath;
+  bn[0][0] = cos(-angle);
+  bn[0][1] = R * sin(-angle) * -1;
+  bn[1][0] = -sin(-angle) / R * -1;
+  bn[1][1] = cos(-angle);
+  double efoc = tan(angle) / R;
+  ep[1][0] = efoc;
+  ep[3][2] = -efoc;
+  en[1][0] = -efoc * -1;
+  en[3][2] = efoc * -1;
+  double(*seq[12])[4] = {bp, ep, d1, en, bn, d2, bn, en, d1, ep, bp, d3};
+  for (int a = 0; a < 12; a++) mat4_mul(m, seq[a]);
+}
+
 static void transverse_slices(step_ctx *c, int is0, int is1, int last) {
   plane_t pxp, pyp;
   double aw;
@@ -603,6 +673,9 @@ static void transverse_slices(step_ctx *c, int is0, int is1, int last) {
   double delz = c->delz * 0.5;
   double cxk = c->st.cx * c->gammaref, cyk = c->st.cy * c->gammaref;
   int corr = last && ((c->st.cx != 0) || (c->st.cy != 0));
+  int chic = !last && c->st.angle != 0;
+  double m[4][4];
+  if (chic) chicane_transfer(&c->st, m);
   for (int is = is0; is < is1; is++) {
     part_t *b = c->beam + (size_t)is * c->npart;
     for (int j = 0; j < c->npart; j++) {
@@ -610,6 +683,15 @@ static void transverse_slices(step_ctx *c, int is0, int is1, int last) {
       if (corr) {
         p->px += cxk;
         p->py += cyk;
+      }
+      if (chic) {
+        double gz = sqrt(p->gamma * p->gamma - 1 - p->px * p->px - p->py * p->py);
+        double tmp = p->x;
+        p->x = m[0][0] * tmp + m[0][1] * p->px / gz;
+        p->px = m[1][0] * tmp * gz + m[1][1] * p->px;
+        tmp = p->y;
+        p->y = m[2][2] * tmp + m[2][3] * p->py / gz;
+        p->py = m[3][2] * tmp * gz + m[3][3] * p->py;
       }
       double gammaz = sqrt(p->gamma * p->gamma - 1 - aw * aw - p->px * p->px - p->py * p->py);
       apply_plane(&pxp, delz, &p->x, &p->px, gammaz);
@@ -1166,6 +1248,19 @@ static void apply_wake(step_ctx *c, int is0, int is1) {
   }
 }
 
+/* TrackBeam::applyR56, TrackBeam.cpp:260-277 */
+static void apply_r56(step_ctx *c, int is0, int is1) {
+  const step_t *u = &c->st;
+  if (u->angle == 0) return;
+  double angle = u->angle, lb = u->lb, ld = u->ld;
+  double R56 = (4 * lb / sin(angle) * (1 - angle / tan(angle)) + 2 * ld * tan(angle) / cos(angle)) * angle;
+  R56 = R56 * 4 * asin(1) / c->reflength / c->gammaref;
+  for (int is = is0; is < is1; is++) {
+    part_t *b = c->beam + (size_t)is * c->npart;
+    for (int ip = 0; ip < c->npart; ip++) b[ip].theta += R56 * (b[ip].gamma - c->gammaref);
+  }
+}
+
 static void run_transverse_first(void *ctx, int i0, int i1) { transverse_slices((step_ctx *)ctx, i0, i1, 0); }
 static void run_transverse_second(void *ctx, int i0, int i1) { transverse_slices((step_ctx *)ctx, i0, i1, 1); }
 
@@ -1174,6 +1269,7 @@ static void run_push(void *ctx, int i0, int i1) {
   transverse_slices(c, i0, i1, 0);
   push_slices(c, i0, i1);
   if (c->wake_loss) apply_wake(c, i0, i1);
+  apply_r56(c, i0, i1);
   transverse_slices(c, i0, i1, 1);
 }
 static void run_field(void *ctx, int i0, int i1) { field_slices((step_ctx *)ctx, i0, i1); }
@@ -1277,6 +1373,7 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
           push_slices(&c, is, is + 1);
         }
         if (c.wake_loss) apply_wake(&c, 0, ns);
+        apply_r56(&c, 0, ns);
         c.sc_ez = NULL;
         free(eloss);
         free(ez);

@@ -102,6 +102,11 @@ void orc_diag_field(int ns, int ngrid, double gridmax, double lambda0, int harm,
  * long-range loss. nz = 0 and longrange = 0 switch it off (the default). */
 void orc_set_efield(double rmax, int ngrid, int nz, int nphi, int longrange);
 
+/* Chicanes (Undulator::chic_*) of the following orc_run_steps calls: tab [nsteps][4] =
+ * angle, lb, ld, lt for each row of the lattice passed there (0 angle: none); nsteps 0
+ * clears them. */
+void orc_set_chicanes(int nsteps, const double *tab);
+
 /* Wakes (&wake, Collective::initWake, Collective.cpp:39-107) for the following
  * orc_run_steps calls: external loss ext[nslice] (eV/m), single-particle wakes res, geo,
  * rou[ns_hr] on the fine grid spaced ds; on = 0 switches them off. */

@@ -75,6 +75,18 @@ class _Lib:
             L.orc_deposit_source.argtypes = [_pd, _i, _i, _i, _pd, _pd, _d, _i, _i, _d, _pd]
             L.orc_adi_advance.argtypes = [_i, _i, _i, _d, _d, _d, _pd, _pd]
 
+    def set_chicanes(self, table=None):
+        """Chicanes [nsteps][4] (angle, lb, ld, lt) of the following run_steps calls'
+        lattice rows; None clears them."""
+        f = getattr(self.lib, self.p + "set_chicanes")
+        f.argtypes = [_i, _pd]
+        if table is None:
+            f(0, None)
+            return
+        t = np.ascontiguousarray(table, dtype=np.float64).reshape(-1, 4)
+        self._chic_keep = t
+        f(int(t.shape[0]), _ptr(t))
+
     def set_wake(self, ext=None, res=None, geo=None, rou=None, ds=1e-10, ztrans=0.0, radius=2.5e-3,
                  transient=False):
         """Wakes (&wake) for the following run_steps calls: external loss per slice (eV/m)

@@ -33,6 +33,9 @@ enum {
   T_CX, T_CY, T_DZ, T_SLIP, T_PHASE, T_HELICAL, T_Z, T_NCOL
 };
 
+// chicanes of the following g4ref_run_steps calls: [nsteps][4] angle, lb, ld, lt
+static std::vector<double> g_chic;
+
 static void fill_undulator(Undulator *und, int nsteps, const double *tab, double gammaref) {
   auto col = [&](std::vector<double> &v, int c) {
     v.resize(nsteps);
@@ -49,6 +52,13 @@ static void fill_undulator(Undulator *und, int nsteps, const double *tab, double
   und->chic_lb.assign(nsteps, 0.0);
   und->chic_ld.assign(nsteps, 0.0);
   und->chic_lt.assign(nsteps, 0.0);
+  if (g_chic.size() == 4 * static_cast<size_t>(nsteps))
+    for (int i = 0; i < nsteps; i++) {
+      und->chic_angle[i] = g_chic[4 * i];
+      und->chic_lb[i] = g_chic[4 * i + 1];
+      und->chic_ld[i] = g_chic[4 * i + 2];
+      und->chic_lt[i] = g_chic[4 * i + 3];
+    }
   und->marker.assign(nsteps + 1, 0);
   und->setGammaRef(gammaref);
   und->updateMarker(0, 0, 0, 1e9);
@@ -70,6 +80,10 @@ static bool g_wk_transient = false;
 static std::vector<double> g_wk_ext, g_wk_res, g_wk_geo, g_wk_rou;
 
 extern "C" {
+
+void g4ref_set_chicanes(int nsteps, const double *tab) {
+  g_chic.assign(tab, tab + 4 * static_cast<size_t>(nsteps > 0 ? nsteps : 0));
+}
 
 // on = 0 switches the wake off; ext has nslice entries, res / geo / rou ns_hr
 void g4ref_set_wake(int on, int ns_hr, int nslice, double ds, const double *ext, const double *res,

@@ -20,7 +20,11 @@ Fixtures (numpy .npz):
                  geometric, roughness) for several &wake settings, and integration steps
                  with wakes (Collective::update / apply) on windows of sample 1 and 3
 
-`python tests/golden/gen_golden.py spacecharge` (or `wakes`) regenerates only that file.
+  chicane.npz    integration steps through a chicane between two undulator modules
+                 (TrackBeam::applyChicane and applyR56), time-dependent and steady state
+
+`python tests/golden/gen_golden.py spacecharge` (or `wakes`, `chicane`) regenerates only
+that file.
 
 The reference's CI check of Example1 (examples/Example1-SteadyState/TEST_power.py)
 expects a final power of 0.932785e9 W within 30 %; example1.npz records what the
@@ -283,6 +287,59 @@ def gen_wakes(r):
     np.savez_compressed(os.path.join(HERE, "wakes.npz"), **d)
 
 
+CHICANE = [0.01, 0.1, 0.3, 1.0]  # angle, lb, ld, lt
+
+
+def chicane_lattice(nwig):
+    """Two undulator modules of nwig periods with a chicane step between them (aw 0, the
+    chicane's length, a small slippage of its own; the table takes any values)."""
+    und = T.undulator_lattice(1.7, 0.015, nwig, 2, 1e-10, 11357.8)
+    row = np.zeros(len(T.LAT_COLS))
+    row[T.C["dz"]] = CHICANE[3]
+    row[T.C["slip"]] = 2.0
+    lat = np.vstack([und[:nwig], row, und[nwig:]])
+    z = 0.0
+    for i in range(lat.shape[0]):
+        lat[i, T.C["z"]] = z
+        z += lat[i, T.C["dz"]]
+    chic = np.zeros((lat.shape[0], 4))
+    chic[nwig] = CHICANE
+    return lat, chic
+
+
+def chicane_cases(r):
+    lat, chic = chicane_lattice(6)
+    cur = np.array([3000.0, 2500.0, 1000.0, 3000.0])
+    part = r.load_beam(T.slice_params(4, 11357.8, 2.0, 0.4e-6, 15.0, currents=cur), 0, 64, 4, 7, 1, 1e-10, 1.0)
+    gh = r.gauss_hermite(T.gauss_field_par(1e-10, 1e5, 20e-6), 6e-5, 25)
+    fld = np.stack([gh * (1 + 0.2j * k) for k in range(4)])[None]
+    cases = [dict(name="td", lat=lat, chic=chic, gammaref=11357.8, part=part, cur=cur, harm=[1], gridmax=[6e-5],
+                  fields=fld, first=[0], time_run=1, periodic=0)]
+    lat1, chic1 = chicane_lattice(5)
+    part1 = r.load_beam(T.slice_params(1, 11357.8, 2.0, 0.4e-6, 15.0), 0, 96, 4, 1, 0, 1e-10, 1.0)
+    gh1 = r.gauss_hermite(T.gauss_field_par(1e-10, 1e6, 15e-6), 6e-5, 21)
+    cases.append(dict(name="steady", lat=lat1, chic=chic1, gammaref=11357.8, part=part1, cur=np.array([3000.0]),
+                      harm=[1], gridmax=[6e-5], fields=gh1[None, None], first=[0], time_run=0, periodic=0))
+    return cases
+
+
+def gen_chicane(r):
+    d = {}
+    for c in chicane_cases(r):
+        n = c["name"]
+        for k in ("lat", "chic", "part", "cur", "harm", "gridmax", "fields", "first"):
+            d[f"{n}_{k}"] = np.asarray(c[k])
+        d[f"{n}_args"] = np.array([c["gammaref"], c["time_run"], c["periodic"]])
+        r.set_chicanes(c["chic"])
+        out = r.run_steps(c["lat"], c["gammaref"], c["part"], c["cur"], 1e-10, 1.0, c["harm"], c["gridmax"],
+                          c["fields"], c["first"], time_run=c["time_run"], periodic=c["periodic"], stages=7)
+        r.set_chicanes()
+        d[f"{n}_out_part"] = out[0]
+        d[f"{n}_out_fields"] = out[1]
+        d[f"{n}_out_first"] = out[2]
+    np.savez_compressed(os.path.join(HERE, "chicane.npz"), **d)
+
+
 LAT_FROM_OUT = {"aw": "aw", "ax": "ax", "ay": "ay", "ku": "ku", "kx": "kx", "ky": "ky",
                 "gradx": "gradx", "grady": "grady", "qf": "qf", "qx": "qx", "qy": "qy",
                 "cx": "cx", "cy": "cy", "dz": "dz", "slip": "slippage", "phase": "phaseshift",
@@ -387,8 +444,12 @@ def main():
     if sys.argv[1:] == ["wakes"]:
         gen_wakes(r)
         return
+    if sys.argv[1:] == ["chicane"]:
+        gen_chicane(r)
+        return
     gen_space_charge(r)
     gen_wakes(r)
+    gen_chicane(r)
     gen_streams(r)
     gen_loading(r)
     gen_steps(r)

@@ -266,3 +266,26 @@ def test_wake_steps(oracle, case):
         assert np.allclose(part, g("out_part"), rtol=1e-12, atol=0)
         assert np.allclose(fld, g("out_fields"), rtol=1e-12, atol=1e-12 * np.abs(g("out_fields")).max())
     assert np.array_equal(first, g("out_first"))
+
+
+@pytest.mark.parametrize("case", ["td", "steady"])
+def test_chicane_steps(oracle, case):
+    """A chicane between two undulator modules (TrackBeam::applyChicane, applyR56): the
+    oracle against the reference run (tests/golden/chicane.npz)."""
+    d = golden("chicane.npz")
+    g = lambda k: d[f"{case}_{k}"]
+    gammaref, time_run, periodic = g("args")
+    oracle.set_chicanes(g("chic"))
+    try:
+        part, fld, first, _ = oracle.run_steps(g("lat"), gammaref, g("part"), g("cur"), 1e-10, 1.0, g("harm"),
+                                               g("gridmax"), g("fields"), g("first"), time_run=int(time_run),
+                                               periodic=int(periodic), stages=7)
+    finally:
+        oracle.set_chicanes()
+    if EXACT:
+        assert np.array_equal(part, g("out_part"))
+        assert np.array_equal(fld, g("out_fields"))
+    else:
+        assert np.allclose(part, g("out_part"), rtol=1e-12, atol=0)
+        assert np.allclose(fld, g("out_fields"), rtol=1e-12, atol=1e-12 * np.abs(g("out_fields")).max())
+    assert np.array_equal(first, g("out_first"))
