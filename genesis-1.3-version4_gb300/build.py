@@ -6,6 +6,7 @@ and g++. The library is built in-tree and is what include/g4gpu.h describes.
   kernels_plain.cu   FP64 kernels, compiled with --fmad=false (reference rounding)
   kernels_mixed.cu   mixed-precision kernels
   kernels_util.cu    layout conversions
+  kernels_sort.cu    one4one sorting of a window (--fmad=false: the reference's rounding)
   kernels_fft.cu     FFT field solver (mixed-radix Stockham, FP64 and FP32)
   kernels_mlp.cu     BF16 tensor-core MLP of the learned closure (training and inference)
   kernels_closure.cu per-slice features and corrections of the learned closure
@@ -47,6 +48,7 @@ def _units():
         # sin/cos (errors ~1e-7 relative, far below its 1 % target)
         ("kernels_mixed.cu", cu_common + ["-use_fast_math"]),
         ("kernels_util.cu", cu_common),
+        ("kernels_sort.cu", cu_common + ["--fmad=false"]),
         ("kernels_fft.cu", cu_common),
         ("kernels_mlp.cu", cu_common),
         ("kernels_closure.cu", cu_common + ["-use_fast_math"]),

@@ -392,7 +392,9 @@ void g4gpu_destroy(g4gpu_handle h) {
   void *ptrs[] = {h->beam.gamma, h->beam.theta, h->beam.x, h->beam.y, h->beam.px, h->beam.py,
                   h->beam.current, h->tmp, h->diag_work, h->coef, h->derr, h->ddiag, h->stage,
                   h->closure_basis, h->closure_feat, h->closure_corr, h->sc.st, h->sc.state, h->sc.ez,
-                  h->wake_tab, h->wake_loss, h->wake_lossf, h->wake_scratch};
+                  h->wake_tab, h->wake_loss, h->wake_lossf, h->wake_scratch, h->count_buf, h->sort_iscratch,
+                  h->sort_scratch[0], h->sort_scratch[1], h->sort_scratch[2], h->sort_scratch[3],
+                  h->sort_scratch[4], h->sort_scratch[5]};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
@@ -644,10 +646,23 @@ static int wake_update(g4gpu_handle h) {
   return G4GPU_OK;
 }
 
+static void drop_graphs(g4gpu_handle h) {
+  for (auto &g : h->graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+  h->graphs.clear();
+}
+
 int g4gpu_load_beam(g4gpu_handle h, const double *particles, const double *current) {
   if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
   if (!particles || !current) return fail(h, G4GPU_ERR_ARG, "null particles or current");
   cudaSetDevice(h->cfg.device);
+  // every slice holds npart: the kernels take the fixed layout (captured graphs hold the
+  // counts' pointer)
+  if (h->beam.count) {
+    h->beam.count = nullptr;
+    h->hcount.clear();
+    drop_graphs(h);
+  }
   size_t n = (size_t)h->cfg.nslice * h->cfg.npart;
   int rc = ensure_stage(h, n * 6 * sizeof(double));
   if (rc) return rc;
@@ -663,6 +678,75 @@ int g4gpu_load_beam(g4gpu_handle h, const double *particles, const double *curre
   h->beam_loaded = true;
   // the wake of every slice follows the window's current
   if (h->wake_on) return wake_update(h);
+  return G4GPU_OK;
+}
+
+int g4gpu_load_beam_counts(g4gpu_handle h, const double *particles, const double *current, const int *counts) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (!counts) return fail(h, G4GPU_ERR_ARG, "null counts");
+  const g4gpu_config &c = h->cfg;
+  for (int is = 0; is < c.nslice; is++)
+    if (counts[is] < 0 || counts[is] > c.npart)
+      return fail(h, G4GPU_ERR_ARG, "counts must lie in [0, npart] (npart is a slice's capacity)");
+  if (h->mixed && std::fabs(c.sample - std::nearbyint(c.sample)) > 0)
+    return fail(h, G4GPU_ERR_ARG, "one4one windows in the mixed form need an integer sample");
+  int rc = g4gpu_load_beam(h, particles, current);
+  if (rc) return rc;
+  if (!h->count_buf && (rc = alloc(h, (void **)&h->count_buf, c.nslice * sizeof(int)))) return rc;
+  G4_CUDA(h, cudaMemcpyAsync(h->count_buf, counts, c.nslice * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  h->hcount.assign(counts, counts + c.nslice);
+  h->beam.count = h->count_buf;
+  drop_graphs(h);
+  // the wake follows the current (computed by g4gpu_load_beam already)
+  G4_CUDA(h, cudaStreamSynchronize(h->stream));
+  return G4GPU_OK;
+}
+
+int g4gpu_get_counts(g4gpu_handle h, int *counts) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (!counts) return fail(h, G4GPU_ERR_ARG, "null counts");
+  for (int is = 0; is < h->cfg.nslice; is++) counts[is] = h->beam.count ? h->hcount[is] : h->cfg.npart;
+  return G4GPU_OK;
+}
+
+int g4gpu_sort(g4gpu_handle h, int *shift) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (shift) *shift = 0;  // Sorting::sort leaves the centre shift off (Sorting.cpp:66-67)
+  if (!h->beam_loaded) return fail(h, G4GPU_ERR_STATE, "no beam loaded");
+  // Sorting::sort: sorting is done for one4one windows only
+  if (!h->beam.count) return G4GPU_OK;
+  cudaSetDevice(h->cfg.device);
+  const g4gpu_config &c = h->cfg;
+  const int ns = c.nslice, cap = c.npart;
+  int rc;
+  if (!h->sort_iscratch) {
+    size_t np = (size_t)ns * cap;
+    size_t es[6] = {h->rsize, 8, h->rsize, h->rsize, h->rsize, h->rsize};
+    for (int k = 0; k < 6; k++)
+      if ((rc = alloc(h, &h->sort_scratch[k], np * es[k]))) return rc;
+    if ((rc = alloc(h, (void **)&h->sort_iscratch, (3 * (size_t)ns + 1) * sizeof(int)))) return rc;
+  }
+  {
+    Timed t(h, G4GPU_K_MISC, 3);
+    g4::launch_sort(h->stream, h->mixed, h->beam, h->sort_scratch, h->sort_iscratch, ns, cap, c.lambda0, c.sample);
+  }
+  G4_CUDA(h, cudaGetLastError());
+  // the sorted window replaces the beam's arrays (their addresses stay: captured graphs
+  // hold them)
+  void *dst[6] = {h->beam.gamma, h->beam.theta, h->beam.x, h->beam.y, h->beam.px, h->beam.py};
+  size_t es[6] = {h->rsize, 8, h->rsize, h->rsize, h->rsize, h->rsize};
+  for (int k = 0; k < 6; k++)
+    G4_CUDA(h, cudaMemcpyAsync(dst[k], h->sort_scratch[k], (size_t)ns * cap * es[k], cudaMemcpyDeviceToDevice,
+                               h->stream));
+  int over = 0;
+  G4_CUDA(h, cudaMemcpyAsync(&over, h->sort_iscratch + 3 * ns, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  G4_CUDA(h, cudaMemcpyAsync(h->hcount.data(), h->count_buf, ns * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  G4_CUDA(h, cudaStreamSynchronize(h->stream));
+  // Beam::sort: the wake follows the new current (Collective::forceUpdate)
+  if (h->wake_on && (rc = wake_update(h))) return rc;
+  if (over > 0)
+    return fail(h, G4GPU_ERR_STATE,
+                std::to_string(over) + " particles found no room in their slice: npart (the slices' capacity) is too small");
   return G4GPU_OK;
 }
 
@@ -772,15 +856,10 @@ int g4gpu_set_wake(g4gpu_handle h, int ns_hr, double ds, const double *ext, cons
                    const double *rou, double ztrans, double radius, int transient) {
   if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
   cudaSetDevice(h->cfg.device);
-  auto drop_graphs = [&] {
-    // captured step sequences were recorded with other wakes
-    for (auto &g : h->graphs)
-      if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
-    h->graphs.clear();
-  };
+  // captured step sequences were recorded with other wakes
   if (!ext) {
     h->wake_on = false;
-    drop_graphs();
+    drop_graphs(h);
     return G4GPU_OK;
   }
   const int ns = h->cfg.nslice;
@@ -819,7 +898,7 @@ int g4gpu_set_wake(g4gpu_handle h, int ns_hr, double ds, const double *ext, cons
   h->wake_radius = radius;
   h->wake_transient = transient;
   h->wake_on = true;
-  drop_graphs();
+  drop_graphs(h);
   int rc = h->beam_loaded ? wake_update(h) : G4GPU_OK;
   if (rc) return rc;
   G4_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -974,24 +1053,39 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
       for (int k = 0; k < c.nfield; k++) {
         h->accuslip[k] += h->slip[istep];
         int direction = 1;
+        // the slices that enter the window are cleared; a long slip (a chicane's delay
+        // spans many windows) may enter every slice, which is then one clearing copy
+        std::vector<char> cleared;
+        int ncleared = 0;
         while (std::fabs(h->accuslip[k]) > (c.sample * 0.8)) {
           if (h->accuslip[k] < 0) direction = -1;
           h->accuslip[k] -= c.sample * direction;
           int last = (h->first[k] + ns - 1) % ns;
           if (direction < 0) last = (last + 1) % ns;
           if (!c.periodic) {
-            G4_CUDA(h, cudaMemsetAsync((char *)h->field[k] + (size_t)last * ncell * h->csize, 0,
-                                       ncell * h->csize, h->stream));
-            // a record formed during the step holds the slice's sums before clearing
-            if (h->diag_fields_in_step) {
-              const size_t fw = g4::kFieldSums + 2;
-              double *d = h->diag_rec + (size_t)ns * g4::beam_diag_width(h->diag_nharm) +
-                          ((size_t)k * ns + last) * fw;
-              G4_CUDA(h, cudaMemsetAsync(d, 0, fw * sizeof(double), h->stream));
+            if (cleared.empty()) cleared.assign(ns, 0);
+            if (!cleared[last]) {
+              cleared[last] = 1;
+              ncleared++;
             }
           }
           h->first[k] = last;
           if (direction < 0) h->first[k] = (last + 1) % ns;
+        }
+        if (ncleared == ns) {
+          G4_CUDA(h, cudaMemsetAsync(h->field[k], 0, (size_t)ns * ncell * h->csize, h->stream));
+        } else if (ncleared > 0) {
+          for (int is = 0; is < ns; is++)
+            if (cleared[is])
+              G4_CUDA(h, cudaMemsetAsync((char *)h->field[k] + (size_t)is * ncell * h->csize, 0,
+                                         ncell * h->csize, h->stream));
+        }
+        // a record formed during the step holds the slices' sums before clearing
+        if (ncleared > 0 && h->diag_fields_in_step) {
+          const size_t fw = g4::kFieldSums + 2;
+          double *d0 = h->diag_rec + (size_t)ns * g4::beam_diag_width(h->diag_nharm) + (size_t)k * ns * fw;
+          for (int is = 0; is < ns; is++)
+            if (cleared[is]) G4_CUDA(h, cudaMemsetAsync(d0 + (size_t)is * fw, 0, fw * sizeof(double), h->stream));
         }
       }
     }
@@ -1146,8 +1240,10 @@ void finish_diag(g4gpu_handle h, const double *raw, int nharm, const int *first,
   if (beam_out) {
     // DiagBeam::getValues, Diagnostic.cpp:457-531
     int ow = G4GPU_DB_NCOL + 2 * nharm;
-    double norm = np > 0 ? 1. / static_cast<double>(np) : 1.;
     for (int is = 0; is < ns; is++) {
+      // Diagnostic.cpp:452-455: 1 / the slice's particles, 1 for an empty slice
+      const int n = h->beam.count ? h->hcount[is] : np;
+      double norm = n > 0 ? 1. / static_cast<double>(n) : 1.;
       const double *s = raw + (size_t)is * bw;
       double g1 = s[0] * norm, g2 = s[1] * norm, x1 = s[2] * norm, x2 = s[3] * norm;
       double y1 = s[4] * norm, y2 = s[5] * norm, px1 = s[6] * norm, px2 = s[7] * norm;

@@ -57,6 +57,12 @@ struct g4gpu_ctx {
   double *wake_loss = nullptr;  // [nslice]
   float *wake_lossf = nullptr;  // [nslice]
   double *wake_scratch = nullptr;  // [2][wake_ns]
+  // one4one windows (g4gpu_load_beam_counts): particles per slice on the device
+  // (beam.count points at it then) and their host copy; the sort's scratch
+  int *count_buf = nullptr;
+  std::vector<int> hcount;
+  void *sort_scratch[6] = {};
+  int *sort_iscratch = nullptr;
   void *stage = nullptr;     // AoS staging buffer for host transfers
   size_t stage_bytes = 0;
   size_t bytes = 0;

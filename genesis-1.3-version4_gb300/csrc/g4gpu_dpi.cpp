@@ -41,6 +41,33 @@ void copy_out(const std::string &s, char *buf, int n) {
   buf[n - 1] = 0;
 }
 
+// DiagBeamHook::getValues: slice by slice, counts (may be null: npart each) the particles
+// of every slice of the [nslice][npart][6] array
+void beam_slices(g4gpu_dpi p, int iz, int nslice, int npart, const double *particles, const int *counts,
+                 double *out) {
+  const size_t nobj = p->names.size();
+  g4dpi::BeamData hd{};
+  hd.version = g4dpi::kDataVersion;
+  hd.verbose = p->verbose;
+  hd.mpi_rank = 0;
+  hd.mpi_size = 1;
+  hd.runid = p->runid;
+  hd.iz = iz;
+  hd.ns = nslice;
+  std::vector<g4dpi::Particle> slice;
+  for (int is = 0; is < nslice; is++) {
+    const int n = counts ? counts[is] : npart;
+    slice.resize((size_t)n);
+    std::memcpy(slice.data(), particles + (size_t)is * npart * 6, sizeof(g4dpi::Particle) * (size_t)n);
+    std::vector<double> res(nobj, -1.);
+    hd.is = is;
+    hd.datain = &slice;
+    hd.dataout = &res;
+    p->beam->doit(&hd);
+    for (size_t k = 0; k < nobj; k++) out[k * nslice + is] = res[k];
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -183,25 +210,7 @@ int g4gpu_dpi_field(g4gpu_dpi p, int iz, int harm, int ngrid, double dgrid, doub
 
 int g4gpu_dpi_beam(g4gpu_dpi p, int iz, int nslice, int npart, const double *particles, double *out) {
   if (!p || p->kind != G4GPU_DPI_BEAM || !particles || !out || nslice <= 0 || npart < 0) return G4GPU_ERR_ARG;
-  const size_t nobj = p->names.size();
-  g4dpi::BeamData hd{};
-  hd.version = g4dpi::kDataVersion;
-  hd.verbose = p->verbose;
-  hd.mpi_rank = 0;
-  hd.mpi_size = 1;
-  hd.runid = p->runid;
-  hd.iz = iz;
-  hd.ns = nslice;
-  std::vector<g4dpi::Particle> slice((size_t)npart);
-  for (int is = 0; is < nslice; is++) {
-    std::memcpy(slice.data(), particles + (size_t)is * npart * 6, sizeof(g4dpi::Particle) * (size_t)npart);
-    std::vector<double> res(nobj, -1.);
-    hd.is = is;
-    hd.datain = &slice;
-    hd.dataout = &res;
-    p->beam->doit(&hd);
-    for (size_t k = 0; k < nobj; k++) out[k * nslice + is] = res[k];
-  }
+  beam_slices(p, iz, nslice, npart, particles, nullptr, out);
   return G4GPU_OK;
 }
 
@@ -225,9 +234,13 @@ int g4gpu_dpi_beam_from(g4gpu_dpi p, g4gpu_handle h, int iz, double *out) {
   g4gpu_config c;
   int rc = g4gpu_get_config(h, &c);
   if (rc) return rc;
+  if (p->kind != G4GPU_DPI_BEAM) return G4GPU_ERR_ARG;
   std::vector<double> part(6 * (size_t)c.nslice * c.npart);
+  std::vector<int> counts(c.nslice);
   if ((rc = g4gpu_get_beam(h, part.data()))) return rc;
-  return g4gpu_dpi_beam(p, iz, c.nslice, c.npart, part.data(), out);
+  if ((rc = g4gpu_get_counts(h, counts.data()))) return rc;
+  beam_slices(p, iz, c.nslice, c.npart, part.data(), counts.data(), out);
+  return G4GPU_OK;
 }
 
 void g4gpu_dpi_close(g4gpu_dpi p) {

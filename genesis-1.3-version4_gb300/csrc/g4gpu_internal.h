@@ -87,6 +87,9 @@ StepConstF to_float(const StepConst &s, int npart);
 struct DeviceBeam {
   void *gamma, *theta, *x, *y, *px, *py;  // theta: FP64 (plain) or Q32.32 int64 (mixed), 8 B
   double *current;
+  // particles of every slice when they differ (one4one windows: npart is then the
+  // capacity of a slice), null when every slice holds npart
+  int *count;
 };
 
 struct Launch {
@@ -190,6 +193,12 @@ void launch_push_mixed_sc(const Launch &L, const StepConstF &sc, const DeviceBea
 void launch_wake_update(const Launch &L, const double *cur, int nslice, int ns_hr, double ds, const double *ext,
                         const double *res, const double *geo, const double *rou, double *scratch, double *loss,
                         float *lossf);
+
+// kernels_sort.cu: one4one sorting (Beam::sort for one rank); b.count must be set.
+// scratch: the six particle arrays' layout; iscratch: 3 ns + 1 ints, the last the number
+// of particles that found no room in their slice
+void launch_sort(void *stream, int mixed, const DeviceBeam &b, void *const *scratch, int *iscratch, int ns, int cap,
+                 double lambda0, double sample);
 
 // kernels_fft.cu: FFT field solver (FieldSolverFFT::FFT)
 struct FFTPlan {

@@ -386,6 +386,7 @@ static double herm(int n, double x) {
 
 int g4gpu_closure_attach(g4gpu_handle h, g4gpu_mlp m, double waist, double u0, double c0) {
   if (!h || !m) return g4_fail(h, G4GPU_ERR_ARG, "closure: null handle or network");
+  if (h->beam.count) return g4_fail(h, G4GPU_ERR_STATE, "closure: one4one windows are not supported");
   if (m->nin != g4::kClosureNin || m->nout != g4::kClosureNout)
     return g4_fail(h, G4GPU_ERR_ARG, "closure: the network must map 32 features to 4 corrections");
   if (!(waist > 0) || !(u0 > 0) || !(c0 > 0)) return g4_fail(h, G4GPU_ERR_ARG, "closure: waist, u0, c0 > 0");
@@ -424,6 +425,7 @@ int g4gpu_closure_attach(g4gpu_handle h, g4gpu_mlp m, double waist, double u0, d
 int g4gpu_closure_features(g4gpu_handle h, float *out) {
   if (!h || !out) return g4_fail(h, G4GPU_ERR_ARG, "closure: null argument");
   if (!h->closure_basis) return g4_fail(h, G4GPU_ERR_STATE, "closure: not attached");
+  if (h->beam.count) return g4_fail(h, G4GPU_ERR_STATE, "closure: one4one windows are not supported");
   cudaSetDevice(h->cfg.device);
   const g4gpu_config &c = h->cfg;
   g4::closure_features(h->stream, h->beam.theta, h->beam.gamma, h->beam.current, h->field[0], h->closure_basis,

@@ -214,7 +214,22 @@ struct PtrsF {
   int mode;
   // wakes: the loss of every slice over eev (1/m, Collective::apply), null without them
   const float *wake;
+  // particles per slice (one4one windows), null: np in every slice
+  const int *count;
 };
+
+// particles of slice is: np, or the slice's own count
+__device__ __forceinline__ int slice_np_f(const PtrsF &p, int is, int np) {
+  return p.count ? min(p.count[is], np) : np;
+}
+// the current the deposition scales with: dep_scl holds 1 / npart, and the reference
+// divides by the slice's own particle count (FieldSolverADI.cpp:27)
+__device__ __forceinline__ float slice_cur_f(const PtrsF &p, int is, int np) {
+  const float cur = (float)p.current[is];
+  if (!p.count) return cur;
+  const int n = min(p.count[is], np);
+  return n > 0 ? cur * ((float)np / (float)n) : 0.f;
+}
 
 // Deposition into the global source grids (FieldSolverADI.cpp:11-52) by a whole
 // warp. The particles of a beamlet (nbins consecutive particles of the quiet
@@ -285,7 +300,7 @@ __global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, 
   int is = blockIdx.y;
   int ip = blockIdx.x * blockDim.x + threadIdx.x;
   // lanes past the slice's particles stay for the deposition's warp shuffles
-  const bool valid = ip < np;
+  const bool valid = ip < slice_np_f(p, is, np);
   if (!valid && !deposit) return;
   size_t o = (size_t)is * np + (valid ? ip : 0);
   const float g0 = (float)sc.gammaref;
@@ -361,16 +376,16 @@ __global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, 
     p.px[o] = px;
     p.py[o] = py;
   }
-  if (deposit) deposit_f<NF>(sc, p, (size_t)is * ncell, ng, (float)p.current[is], g, th, x, y, valid);
+  if (deposit) deposit_f<NF>(sc, p, (size_t)is * ncell, ng, slice_cur_f(p, is, np), g, th, x, y, valid);
 }
 
 template <int NF>
 __global__ void __launch_bounds__(256) k_deposit_f(StepConstF sc, PtrsF p, int ns, int np, int ng) {
   int is = blockIdx.y;
   int ip = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = ip < np;
+  const bool valid = ip < slice_np_f(p, is, np);
   size_t o = (size_t)is * np + (valid ? ip : 0);
-  deposit_f<NF>(sc, p, (size_t)is * (size_t)ng * ng, ng, (float)p.current[is],
+  deposit_f<NF>(sc, p, (size_t)is * (size_t)ng * ng, ng, slice_cur_f(p, is, np),
                 (float)sc.gammaref + p.dg[o], p.theta[o], p.x[o], p.y[o], valid);
 }
 
@@ -763,18 +778,19 @@ __device__ __forceinline__ void deposit_lanes(const StepConstF &sc, const FieldS
 // memory (used when no staging buffer fits beside the slice).
 __device__ __forceinline__ void deposit_smem(const StepConstF &sc, const FieldStepF &fs,
                                              const PtrsF &p, float2 *S, int is, int np, int ng) {
-  const float scl = fs.dep_scl * (float)p.current[is];
+  const float scl = fs.dep_scl * slice_cur_f(p, is, np);
   const size_t base = (size_t)is * np;
+  const int n = slice_np_f(p, is, np);
   const unsigned lane = threadIdx.x & 31u;
   const int warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   constexpr int U = 4;  // particles per lane per round: their loads are issued together
-  for (int w0 = warp * 32 * U; w0 < np; w0 += nwarp * 32 * U) {
+  for (int w0 = warp * 32 * U; w0 < n; w0 += nwarp * 32 * U) {
     float xs[U], ys[U], gs[U];
     long long ths[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
       int ip = w0 + u * 32 + (int)lane;
-      bool in = ip < np;
+      bool in = ip < n;
       xs[u] = in ? p.x[base + ip] : 1e30f;
       ys[u] = in ? p.y[base + ip] : 1e30f;
       ths[u] = in ? p.theta[base + ip] : 0;
@@ -1006,6 +1022,7 @@ __device__ __forceinline__ void slice_beam_sums(const PtrsF &p, double gref, int
                                                 double *sh, double *res, double *o) {
   constexpr int NSUM = kBeamSums + 2 * kFusedDiagHarm;
   const size_t base = (size_t)is * np;
+  const int cnt = slice_np_f(p, is, np);
   float c[NSUM];
 #pragma unroll
   for (int k = 0; k < NSUM; k++) c[k] = 0.f;
@@ -1017,7 +1034,7 @@ __device__ __forceinline__ void slice_beam_sums(const PtrsF &p, double gref, int
   }
   // unrolled so that the loads of several particles are in flight together
 #pragma unroll 8
-  for (int ip = threadIdx.x; ip < np; ip += blockDim.x) {
+  for (int ip = threadIdx.x; ip < cnt; ip += blockDim.x) {
     const float x = p.x[base + ip], y = p.y[base + ip], dg = p.dg[base + ip];
     const float px = p.px[base + ip], py = p.py[base + ip];
     const long long th = p.theta[base + ip];
@@ -1040,7 +1057,7 @@ __device__ __forceinline__ void slice_beam_sums(const PtrsF &p, double gref, int
   }
   cta_reduce<NSUM, 5>(c, mn, mx, sh, res);
   const int k = threadIdx.x;
-  const double n = (double)np;
+  const double n = (double)cnt;
   if (k == 0) o[0] = n * gref + res[0];
   if (k == 1) o[1] = n * gref * gref + 2.0 * gref * res[0] + res[1];
   if (k >= 2 && k < kBeamSums) o[k] = res[k];
@@ -1133,7 +1150,8 @@ __global__ void __launch_bounds__(kFusedMaxThreads, 1)
   stencil_cols_seg(S, ng, cs, nseg);  // S1 = (I + c Dy) u
   __syncthreads();
   if (deposit) {  // S = S1 + src
-    if ((np & 3) == 0)
+    // full slices of a multiple of 4 particles take the 16-byte vector loads
+    if ((np & 3) == 0 && !p.count)
       deposit_quads(sc, fs, p, S, is, np, ng);
     else
       deposit_smem(sc, fs, p, S, is, np, ng);
@@ -1282,6 +1300,7 @@ __global__ void __launch_bounds__(BS) k_diag_beam_f(PtrsF p, double gref, int np
   __shared__ double res[NSUM + 10];
   const int is = blockIdx.x;
   const size_t base = (size_t)is * np;
+  const int cnt = slice_np_f(p, is, np);
   const int nh = min(nharm, NH);
   // dg, dg^2, x, x^2, y, y^2, px, px^2, py, py^2, x px, y py, then (Re, Im) b_h
   KahanF c[NSUM];
@@ -1292,7 +1311,7 @@ __global__ void __launch_bounds__(BS) k_diag_beam_f(PtrsF p, double gref, int np
     mx[k] = -INFINITY;
   }
 #pragma unroll 4
-  for (int ip = threadIdx.x; ip < np; ip += BS) {
+  for (int ip = threadIdx.x; ip < cnt; ip += BS) {
     const float x = p.x[base + ip], y = p.y[base + ip], dg = p.dg[base + ip];
     const float px = p.px[base + ip], py = p.py[base + ip];
     const long long th = p.theta[base + ip];
@@ -1321,7 +1340,7 @@ __global__ void __launch_bounds__(BS) k_diag_beam_f(PtrsF p, double gref, int np
   const int w = beam_diag_width(nharm);
   double *o = out + (size_t)is * w;
   const int k = threadIdx.x;
-  const double n = (double)np;
+  const double n = (double)cnt;
   if (k == 0) o[0] = n * gref + res[0];
   if (k == 1) o[1] = n * gref * gref + 2.0 * gref * res[0] + res[1];
   if (k >= 2 && k < kBeamSums) o[k] = res[k];
@@ -1378,6 +1397,7 @@ PtrsF make_ptrs_f(const DeviceBeam &b, void *const *field, void *const *src, int
   p.px = (float *)b.px;
   p.py = (float *)b.py;
   p.current = b.current;
+  p.count = b.count;
   for (int k = 0; k < nfld && k < G4GPU_MAX_FIELDS; k++) {
     p.field[k] = field ? (const float2 *)field[k] : nullptr;
     p.src[k] = src ? (float2 *)src[k] : nullptr;
@@ -1627,9 +1647,9 @@ __device__ __forceinline__ void pair_group(const StepConstF &sc, const FieldStep
 }
 __device__ __forceinline__ void deposit_pair(const StepConstF &sc, const FieldStepF &fs, const PtrsF &p,
                                              float2 *const *T, int h, int is, int np, int ng, int q) {
-  const float scl = fs.dep_scl * (float)p.current[is];
+  const float scl = fs.dep_scl * slice_cur_f(p, is, np);
   const size_t base = (size_t)is * np;
-  if ((np & 3) == 0) {
+  if ((np & 3) == 0 && !p.count) {
     const int nq = np >> 2, q0 = q ? nq / 2 : 0, q1 = q ? nq : nq / 2;
     const float4 *X = reinterpret_cast<const float4 *>(p.x + base);
     const float4 *Y = reinterpret_cast<const float4 *>(p.y + base);
@@ -1659,7 +1679,8 @@ __device__ __forceinline__ void deposit_pair(const StepConstF &sc, const FieldSt
       }
     }
   } else {
-    const int i0 = q ? np / 2 : 0, i1 = q ? np : np / 2;
+    const int n = slice_np_f(p, is, np);
+    const int i0 = q ? n / 2 : 0, i1 = q ? n : n / 2;
     for (int ip = i0 + threadIdx.x; ip < i1; ip += blockDim.x) {
       const long long th = p.theta[base + ip];
       const float dg = p.dg[base + ip];
@@ -1900,8 +1921,8 @@ namespace g4 {
 
 void launch_sc_mixed(const Launch &L, const ScConst &c, const StepConstF &step, const DeviceBeam &b,
                      const ScBuffers &buf, int part) {
-  ScBeam<MixedSC> sb{(float *)b.gamma, (float *)b.x,           (float *)b.y, (float *)b.px,
-                     (float *)b.py,    (const long long *)b.theta, b.current};
+  ScBeam<MixedSC> sb{(float *)b.gamma, (float *)b.x,              (float *)b.y, (float *)b.px,
+                     (float *)b.py,    (const long long *)b.theta, b.current,    b.count};
   sc_launch<MixedSC>(L, c, step, sb, buf, part);
 }
 

@@ -181,7 +181,14 @@ struct Ptrs {
   int mode;
   // wakes: the loss of every slice (eV/m, Collective::apply), null without them
   const double *wake;
+  // particles per slice (one4one windows), null: np in every slice
+  const int *count;
 };
+
+// particles of slice is: np, or the slice's own count
+__device__ __forceinline__ int slice_np(const Ptrs &p, int is, int np) {
+  return p.count ? min(p.count[is], np) : np;
+}
 
 // Beam::track (Beam.cpp:296-311): half transverse step, BeamSolver::advance with
 // the bilinear field gather and RK4 (BeamSolver.cpp:48-141), half transverse step
@@ -192,7 +199,8 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
                                               int deposit) {
   int is = blockIdx.y;
   int ip = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ip >= np) return;
+  const int n = slice_np(p, is, np);
+  if (ip >= n) return;
   size_t o = (size_t)is * np + ip;
   double g = p.gamma[o], th = p.theta[o], x = p.x[o], y = p.y[o], px = p.px[o], py = p.py[o];
   size_t ncell = (size_t)ng * ng;
@@ -276,7 +284,7 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   p.py[o] = py;
 
   if (deposit)
-    deposit_particle<NF>(sc, p.src, (size_t)is * ncell, ng, p.current[is], (double)np, gamma,
+    deposit_particle<NF>(sc, p.src, (size_t)is * ncell, ng, p.current[is], (double)n, gamma,
                          theta, x, y);
 }
 
@@ -285,10 +293,11 @@ template <int NF>
 __global__ void __launch_bounds__(256) k_deposit(StepConst sc, Ptrs p, int ns, int np, int ng) {
   int is = blockIdx.y;
   int ip = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ip >= np) return;
+  const int n = slice_np(p, is, np);
+  if (ip >= n) return;
   size_t o = (size_t)is * np + ip;
   size_t ncell = (size_t)ng * ng;
-  deposit_particle<NF>(sc, p.src, (size_t)is * ncell, ng, p.current[is], (double)np, p.gamma[o],
+  deposit_particle<NF>(sc, p.src, (size_t)is * ncell, ng, p.current[is], (double)n, p.gamma[o],
                        p.theta[o], p.x[o], p.y[o]);
 }
 
@@ -416,11 +425,12 @@ __global__ void __launch_bounds__(BS) k_diag_beam(Ptrs p, int np, int nharm, dou
   __shared__ double sh[BS / 32];
   int is = blockIdx.x;
   size_t base = (size_t)is * np;
+  const int n = slice_np(p, is, np);
   double s[kBeamSums] = {0};
   double mn[5] = {1e5, 1e5, 1e5, 1e5, 1e7}, mx[5] = {-1e5, -1e5, -1e5, -1e5, 1};
   double br[G4GPU_MAX_HARM], bi[G4GPU_MAX_HARM];
   for (int h = 0; h < G4GPU_MAX_HARM; h++) br[h] = bi[h] = 0;
-  for (int ip = threadIdx.x; ip < np; ip += BS) {
+  for (int ip = threadIdx.x; ip < n; ip += BS) {
     double x = p.x[base + ip], y = p.y[base + ip], g = p.gamma[base + ip];
     double px = p.px[base + ip], py = p.py[base + ip], th = p.theta[base + ip];
     s[0] += g; s[1] += g * g; s[2] += x; s[3] += x * x; s[4] += y; s[5] += y * y;
@@ -497,6 +507,7 @@ Ptrs make_ptrs(const DeviceBeam &b, void *const *field, void *const *src, int nf
   p.px = (double *)b.px;
   p.py = (double *)b.py;
   p.current = b.current;
+  p.count = b.count;
   for (int k = 0; k < nfld && k < G4GPU_MAX_FIELDS; k++) {
     p.field[k] = field ? (const double2 *)field[k] : nullptr;
     p.src[k] = src ? (double2 *)src[k] : nullptr;
@@ -597,8 +608,8 @@ size_t sc_max_smem() { return 220 * 1024; }
 
 void launch_sc_plain(const Launch &L, const ScConst &c, const StepConst &step, const DeviceBeam &b,
                      const ScBuffers &buf, int part) {
-  ScBeam<PlainSC> sb{(double *)b.gamma, (double *)b.x,        (double *)b.y, (double *)b.px,
-                     (double *)b.py,    (const double *)b.theta, b.current};
+  ScBeam<PlainSC> sb{(double *)b.gamma, (double *)b.x,           (double *)b.y, (double *)b.px,
+                     (double *)b.py,    (const double *)b.theta, b.current,    b.count};
   sc_launch<PlainSC>(L, c, step, sb, buf, part);
 }
 

@@ -176,6 +176,7 @@ struct ScBeam {
   typename F::R *g, *x, *y, *px, *py;
   const typename F::Th *theta;
   const double *current;
+  const int *count;  // particles per slice (one4one windows), null: np in every slice
 };
 
 // The first transverse half step and the slice moments, then (last CTA) the radial
@@ -188,8 +189,9 @@ __global__ void __launch_bounds__(kScThreads) k_sc_moments(ScBeam<F> b, typename
   __shared__ double red[4][kScThreads / 32];
   __shared__ double rb[kScScanChunk];
   __shared__ int last;
-  const int is = blockIdx.x, tid = threadIdx.x, lane = tid & 31, ns = c.ns, np = c.np;
-  const size_t o0 = (size_t)is * np;
+  const int is = blockIdx.x, tid = threadIdx.x, lane = tid & 31, ns = c.ns;
+  const int np = b.count ? min(b.count[is], c.np) : c.np;  // the slice's particles
+  const size_t o0 = (size_t)is * c.np;
   const R *xs = b.x + o0, *ys = b.y + o0;
 
   // pass 1: the half step (Beam.cpp:103, TrackBeam.cpp:17-64), and the sums of x, y
@@ -267,8 +269,8 @@ __global__ void __launch_bounds__(kScThreads) k_sc_moments(ScBeam<F> b, typename
     R m = 0;
     for (int i = 0; i < (int)(blockDim.x >> 5); i++) m = wmax[i] > m ? wmax[i] : m;
     double size;
-    if (b.current[is] <= 0) {
-      size = 1;  // Beam::getSize of a slice without current
+    if (b.current[is] <= 0 || np == 0) {
+      size = 1;  // Beam::getSize of a slice without current or particles
     } else if constexpr (F::kPlain) {
       double x1 = s[0] / n, x2 = s[1] / n, y1 = s[2] / n, y2 = s[3] / n;
       size = sqrt(fabs(x2 - x1 * x1)) * sqrt(fabs(y2 - y1 * y1));
@@ -337,7 +339,8 @@ __global__ void __launch_bounds__(kScThreads) k_sc_field(ScBeam<F> b, double *st
   using R2 = typename F::R2;
   __shared__ double red[4][kScThreads / 32];
   extern __shared__ __align__(16) unsigned char sc_smem[];
-  const int is = blockIdx.x, tid = threadIdx.x, ns = c.ns, np = c.np, ng = c.ng;
+  const int is = blockIdx.x, tid = threadIdx.x, ns = c.ns, ng = c.ng;
+  const int np = b.count ? min(b.count[is], c.np) : c.np;  // the slice's particles
 
   // EFieldSolver::longRange, EFieldSolver.cpp:77-117
   if (c.longrange) {
@@ -369,7 +372,7 @@ __global__ void __launch_bounds__(kScThreads) k_sc_field(ScBeam<F> b, double *st
     sc_block_sum<1>(e, red);
     if (tid == 0) st[5 * ns + is] = -e[0] / kEev;
   }
-  if (!c.shortrange) return;
+  if (!c.shortrange || np < 1) return;
 
   // EFieldSolver::shortRange, EFieldSolver.cpp:197-272
   const int nz = c.nz, nphi = c.nphi, M = (2 * nphi + 1) * nz, mp = c.modes_per_pass;
@@ -380,9 +383,9 @@ __global__ void __launch_bounds__(kScThreads) k_sc_field(ScBeam<F> b, double *st
   const R pi = (R)3.14159265358979323846;
   const R coef = (R)c.coef;
   const R econst = (R)(kVacimp / kEev * b.current[is] / c.ks / (double)np);
-  const typename F::R *xs = b.x + (size_t)is * np, *ys = b.y + (size_t)is * np;
-  const typename F::Th *ths = b.theta + (size_t)is * np;
-  R *ezs = ez + (size_t)is * np;
+  const typename F::R *xs = b.x + (size_t)is * c.np, *ys = b.y + (size_t)is * c.np;
+  const typename F::Th *ths = b.theta + (size_t)is * c.np;
+  R *ezs = ez + (size_t)is * c.np;
 
   for (int k0 = 0; k0 < M; k0 += mp) {
     const int k1 = min(M, k0 + mp), nk = k1 - k0;

@@ -55,7 +55,7 @@ ABI_SYMBOLS = [
     "g4gpu_dpi_close", "g4gpu_get_stream",
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
     "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc", "g4gpu_host_single_wakes",
-    "g4gpu_set_wake", "g4gpu_set_chicanes",
+    "g4gpu_set_wake", "g4gpu_set_chicanes", "g4gpu_load_beam_counts", "g4gpu_get_counts", "g4gpu_sort",
     "g4gpu_set_graph_mode", "g4gpu_autotune", "g4gpu_batch_create", "g4gpu_batch_destroy",
     "g4gpu_batch_member", "g4gpu_batch_run", "g4gpu_batch_synchronize",
     "g4gpu_mlp_create", "g4gpu_mlp_destroy", "g4gpu_mlp_last_error", "g4gpu_mlp_num_params",
@@ -166,6 +166,9 @@ def load_library(path=None):
     L.g4gpu_host_single_wakes.argtypes = [i, d, d, d, d, i, d, d, d, d, pd, pd, pd]
     L.g4gpu_set_wake.argtypes = [vp, i, d, pd, pd, pd, pd, d, d, i]
     L.g4gpu_set_chicanes.argtypes = [vp, i, pd]
+    L.g4gpu_load_beam_counts.argtypes = [vp, vp, vp, P(i)]
+    L.g4gpu_get_counts.argtypes = [vp, P(i)]
+    L.g4gpu_sort.argtypes = [vp, P(i)]
     L.g4gpu_set_graph_mode.argtypes = [vp, i]
     L.g4gpu_autotune.argtypes = [vp, P(i), P(i), P(i)]
     L.g4gpu_set_launch_shapes.argtypes = [vp, i, i, i]
@@ -307,6 +310,27 @@ class Handle:
         if p.size != self.cfg.nslice * self.cfg.npart * 6 or c.size != self.cfg.nslice:
             raise ValueError("particle or current array has the wrong size")
         self._check(self.L.g4gpu_load_beam(self.h, _vp(p), _vp(c)))
+
+    def load_beam_counts(self, particles, current, counts):
+        """A one4one window: particles [ns][np][6] of which the first counts[is] of every
+        slice are used (np is a slice's capacity)."""
+        p = np.ascontiguousarray(particles, np.float64)
+        c = np.ascontiguousarray(current, dtype=np.float64)
+        n = np.ascontiguousarray(counts, dtype=np.int32)
+        if p.size != self.cfg.nslice * self.cfg.npart * 6 or c.size != self.cfg.nslice or n.size != self.cfg.nslice:
+            raise ValueError("particle, current or count array has the wrong size")
+        self._check(self.L.g4gpu_load_beam_counts(self.h, _vp(p), _vp(c), n.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+
+    def get_counts(self):
+        n = np.zeros(self.cfg.nslice, dtype=np.int32)
+        self._check(self.L.g4gpu_get_counts(self.h, n.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return n
+
+    def sort(self):
+        """Beam::sort for the window (one4one); returns the field shift (0)."""
+        sh = ctypes.c_int(0)
+        self._check(self.L.g4gpu_sort(self.h, ctypes.byref(sh)))
+        return sh.value
 
     def load_beam_ptr(self, particles_ptr, current_ptr):
         """Same as load_beam with raw host pointers (e.g. pinned torch tensors)."""

@@ -151,6 +151,25 @@ int g4gpu_load_beam(g4gpu_handle h, const double *particles, const double *curre
 /* Copies the particles of the device back (host, AoS). */
 int g4gpu_get_beam(g4gpu_handle h, double *particles);
 
+/* One4one windows (&setup one4one, Beam::init with one4one, src/Core/Beam.cpp:22-40):
+ * slices hold different numbers of particles, counts[nslice] in [0, npart], npart being
+ * then a slice's capacity; particles [nslice][npart][6] with the first counts[is]
+ * records of every slice used. g4gpu_load_beam returns the handle to full slices. */
+int g4gpu_load_beam_counts(g4gpu_handle h, const double *particles, const double *current, const int *counts);
+/* Particles per slice (npart in every slice unless the window is one4one). */
+int g4gpu_get_counts(g4gpu_handle h, int *counts);
+/* Beam::sort for one rank (src/Core/Beam.cpp:81-94, Sorting::globalSort / localSort,
+ * src/Util/Sorting.cpp:55-145, 198-474): particles outside the window leave it, the
+ * others move to the slice their phase lies in, the slices' currents follow their
+ * counts, and the wake is formed again. *shift (may be NULL) receives the field shift
+ * the reference returns, always 0 (its centre shift is off). Synchronous. A full window
+ * (no counts) is left alone, as the reference skips sorting outside one4one runs.
+ * G4GPU_ERR_STATE when a slice would exceed npart (the particles without room are lost).
+ * The reference sorts at marker steps between the push and the field solve
+ * (Gencore.cpp:121-132): g4gpu_run(h, i, 1, G4GPU_STAGE_PUSH), g4gpu_sort, then
+ * g4gpu_run(h, i, 1, G4GPU_STAGE_FIELD | G4GPU_STAGE_SLIP). */
+int g4gpu_sort(g4gpu_handle h, int *shift);
+
 /* Copies field ifld (host, storage order) to the device with ring start `first`
  * and accumulated slippage `accuslip` (Field::first, Field::accuslip). */
 int g4gpu_load_field(g4gpu_handle h, int ifld, const double *field, int first, double accuslip);

@@ -562,7 +562,13 @@ typedef struct {
   double sc_eloss;
   /* wakes: the loss of every slice (eV/m), NULL without &wake */
   const double *wake_loss;
+  /* one4one windows: particles per slice (npart is then a slice's capacity), NULL when
+   * every slice holds npart */
+  const int *count;
 } step_ctx;
+
+/* the particles of slice is */
+static int np_of(const step_ctx *c, int is) { return c->count ? c->count[is] : c->npart; }
 
 /* TrackBeam::track, TrackBeam.cpp:8-116 (no chicane: the lattice has none) */
 typedef struct {
@@ -678,7 +684,7 @@ static void transverse_slices(step_ctx *c, int is0, int is1, int last) {
   if (chic) chicane_transfer(&c->st, m);
   for (int is = is0; is < is1; is++) {
     part_t *b = c->beam + (size_t)is * c->npart;
-    for (int j = 0; j < c->npart; j++) {
+    for (int j = 0; j < np_of(c, is); j++) {
       part_t *p = b + j;
       if (corr) {
         p->px += cxk;
@@ -720,7 +726,7 @@ static void push_slices(step_ctx *c, int is0, int is1) {
   size_t ncell = (size_t)c->ngrid * c->ngrid;
   for (int is = is0; is < is1; is++) {
     part_t *b = c->beam + (size_t)is * c->npart;
-    for (int ip = 0; ip < c->npart; ip++) {
+    for (int ip = 0; ip < np_of(c, is); ip++) {
       part_t *p = b + ip;
       double gamma = p->gamma, theta = p->theta + autophase;
       double x = p->x, y = p->y, px = p->px, py = p->py;
@@ -794,9 +800,10 @@ static void deposit(const step_ctx *c, int ii, cplx *src) {
   double gm = c->gridmax[c->ifld], dgrid = 2 * gm / (double)(ng - 1);
   double xks = 4. * asin(1) / (c->reflength / (double)harm);
   double scl = orc_fc(c->st.aw, c->st.helical, harm) * kVacimp * c->current[ii] * xks * c->delz;
-  scl /= 4 * kEev * (double)c->npart * dgrid * dgrid;
+  /* the slice's own particle count (FieldSolverADI.cpp:27) */
+  scl /= 4 * kEev * (double)np_of(c, ii) * dgrid * dgrid;
   const part_t *b = c->beam + (size_t)ii * c->npart;
-  for (int ip = 0; ip < c->npart; ip++) {
+  for (int ip = 0; ip < np_of(c, ii); ip++) {
     double x = b[ip].x, y = b[ip].y, theta = (double)harm * b[ip].theta, gamma = b[ip].gamma;
     double wx, wy;
     int idx;
@@ -1031,7 +1038,7 @@ static double slice_size(const step_ctx *c, int is) {
   const part_t *b = c->beam + (size_t)is * c->npart;
   double x1 = 0, x2 = 0, y1 = 0, y2 = 0;
   int count = 0;
-  for (int ip = 0; ip < c->npart; ip++) {
+  for (int ip = 0; ip < np_of(c, is); ip++) {
     x1 += b[ip].x;
     x2 += b[ip].x * b[ip].x;
     y1 += b[ip].y;
@@ -1089,10 +1096,10 @@ static cplx cpow_int(cplx z, int n) {
  * EFieldSolver.cpp:120-272: ez[npart] of slice is; *rmax carries the radial grid's
  * extent from slice to slice (it grows to 1.5 times a slice's extreme radius) */
 static void sc_short_range(const step_ctx *c, int is, double *rmax, double *ez) {
-  int npart = c->npart, ng = sc_cfg.ngrid;
+  int npart = np_of(c, is), ng = sc_cfg.ngrid;
   for (int i = 0; i < npart; i++) ez[i] = 0;
   if (!(sc_cfg.nz > 0 && ng > 2) || npart < 1) return;
-  const part_t *b = c->beam + (size_t)is * npart;
+  const part_t *b = c->beam + (size_t)is * c->npart;
   double xcen = 0, ycen = 0;
   for (int i = 0; i < npart; i++) {
     xcen += b[i].x;
@@ -1244,7 +1251,7 @@ static void apply_wake(step_ctx *c, int is0, int is1) {
   for (int is = is0; is < is1; is++) {
     double dg = c->wake_loss[is] * c->delz / kEev;
     part_t *b = c->beam + (size_t)is * c->npart;
-    for (int ip = 0; ip < c->npart; ip++) b[ip].gamma += dg;
+    for (int ip = 0; ip < np_of(c, is); ip++) b[ip].gamma += dg;
   }
 }
 
@@ -1257,7 +1264,7 @@ static void apply_r56(step_ctx *c, int is0, int is1) {
   R56 = R56 * 4 * asin(1) / c->reflength / c->gammaref;
   for (int is = is0; is < is1; is++) {
     part_t *b = c->beam + (size_t)is * c->npart;
-    for (int ip = 0; ip < c->npart; ip++) b[ip].theta += R56 * (b[ip].gamma - c->gammaref);
+    for (int ip = 0; ip < np_of(c, is); ip++) b[ip].theta += R56 * (b[ip].gamma - c->gammaref);
   }
 }
 
@@ -1294,6 +1301,83 @@ static void apply_slippage(double slippage, double sample, int periodic, int ns,
   }
 }
 
+/* one4one windows: particles per slice of the following orc_run_steps calls, and the
+ * steps after whose push the window is sorted (every sort_every-th, 0: never) */
+static int *o4o_count = NULL;
+static int o4o_ns = 0, o4o_sort_every = 0;
+
+void orc_set_counts(int nslice, const int *counts, int sort_every) {
+  free(o4o_count);
+  o4o_count = NULL;
+  o4o_ns = 0;
+  o4o_sort_every = sort_every;
+  if (nslice <= 0 || !counts) return;
+  o4o_count = malloc(sizeof(int) * nslice);
+  memcpy(o4o_count, counts, sizeof(int) * nslice);
+  o4o_ns = nslice;
+}
+
+void orc_get_counts(int nslice, int *out) {
+  for (int i = 0; i < nslice; i++) out[i] = (o4o_count && i < o4o_ns) ? o4o_count[i] : -1;
+}
+
+/* Beam::sort for one rank (Beam.cpp:81-94): Sorting::globalSort, whose single rank sends
+ * nothing and so drops the particles outside the window (fillPushVectors,
+ * Sorting.cpp:364-421), then Sorting::localSort (Sorting.cpp:74-145), which moves the
+ * others to the slice their phase lies in, removing by a swap with the slice's last
+ * particle and appending at the destination; the currents then follow the counts.
+ * particles [ns][cap][6], counts updated in place (orc_set_counts' copy too). Returns
+ * the number of particles that found no room (cap too small; 0 normally). */
+int orc_sort(int ns, int cap, double *particles, int *counts, double *current, double reflength, double sample) {
+  part_t *beam = (part_t *)particles;
+  const double slicelength = reflength * sample;
+  const double sl = 4 * asin(1.) * slicelength / reflength; /* Beam::initSorting */
+  const double keepmax = sl * (unsigned long)ns;
+  int lost = 0;
+  /* fillPushVectors with s0 = 0, sendmin = keepmin = 0, sendmax = keepmax = sl ns */
+  for (int i = 0; i < ns; i++) {
+    part_t *b = beam + (size_t)i * cap;
+    int j = 0;
+    while (j < counts[i]) {
+      double s = 0 + sl * i + b[j].theta;
+      if ((s < 0) || (s > keepmax)) {
+        b[j] = b[counts[i] - 1];
+        counts[i]--;
+      } else {
+        j++;
+      }
+    }
+  }
+  /* localSort */
+  double invslen = 1. / sl;
+  for (int a = 0; a < ns; a++) {
+    part_t *b = beam + (size_t)a * cap;
+    int k = 0;
+    while (k < counts[a]) {
+      double theta = b[k].theta;
+      int atar = (int)floor(theta * invslen);
+      if (atar != 0) {
+        part_t p = b[k];
+        p.theta = b[k].theta - sl * (atar);
+        int d = a + atar;
+        if (d >= 0 && d < ns && counts[d] < cap) {
+          beam[(size_t)d * cap + counts[d]] = p;
+          counts[d]++;
+        } else {
+          lost++;
+        }
+        b[k] = b[counts[a] - 1];
+        counts[a]--;
+      } else {
+        k++;
+      }
+    }
+  }
+  for (int i = 0; i < ns; i++) current[i] = (double)counts[i] * kCe / slicelength;
+  if (o4o_count && o4o_ns == ns) memcpy(o4o_count, counts, sizeof(int) * ns);
+  return lost;
+}
+
 int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int npart,
                   double *particles, const double *current, double reflength,
                   double sample, int nfld, const int *harm, int ngrid,
@@ -1308,7 +1392,15 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
   c.nfld = nfld;
   c.ngrid = ngrid;
   c.beam = (part_t *)particles;
+  c.count = (o4o_count && o4o_ns == ns) ? o4o_count : NULL;
   c.current = current;
+  /* sorting changes the currents: a copy of them for this call */
+  double *cur_local = NULL;
+  if (c.count && o4o_sort_every > 0) {
+    cur_local = malloc(sizeof(double) * ns);
+    memcpy(cur_local, current, sizeof(double) * ns);
+    c.current = cur_local;
+  }
   c.fields = (cplx *)fields;
   c.harm = harm;
   c.first = first;
@@ -1339,7 +1431,7 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
   double *wake_loss = NULL;
   if (wk.on && wk.nslice == ns) {
     wake_loss = malloc(sizeof(double) * ns);
-    wake_update(current, ns, wake_loss);
+    wake_update(c.current, ns, wake_loss);
     for (int i = 0; i < ns; i++) wake_loss[i] = wk.ext[i] + wake_loss[i];
   }
   c.wake_loss = wake_loss;
@@ -1382,6 +1474,15 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
         parallel_for(ns, nthreads, run_push, &c);
       }
     }
+    /* Gencore.cpp:121-132: the sort after the push, before the field solve; the wake
+     * follows the new currents (Collective::forceUpdate) */
+    if (cur_local && (istep + 1) % o4o_sort_every == 0) {
+      orc_sort(ns, npart, particles, o4o_count, cur_local, reflength, sample);
+      if (wake_loss) {
+        wake_update(c.current, ns, wake_loss);
+        for (int i = 0; i < ns; i++) wake_loss[i] = wk.ext[i] + wake_loss[i];
+      }
+    }
     if (stages & ORC_STAGE_FIELD) {
       for (int k = 0; k < nfld; k++) {
         c.ifld = k;
@@ -1409,6 +1510,7 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
   free(coef);
   free(fft_tabs);
   free(wake_loss);
+  free(cur_local);
   return 0;
 }
 

@@ -102,6 +102,17 @@ void orc_diag_field(int ns, int ngrid, double gridmax, double lambda0, int harm,
  * long-range loss. nz = 0 and longrange = 0 switch it off (the default). */
 void orc_set_efield(double rmax, int ngrid, int nz, int nphi, int longrange);
 
+/* One4one windows for the following orc_run_steps calls: particles per slice counts
+ * [nslice] (the particle array's npart is then a slice's capacity), and a sort after the
+ * push of every sort_every-th step (0: never); nslice 0 clears them. orc_get_counts
+ * reads the counts back (-1 without a one4one window). */
+void orc_set_counts(int nslice, const int *counts, int sort_every);
+void orc_get_counts(int nslice, int *out);
+/* Beam::sort for one rank (Beam.cpp:81-94, Sorting.cpp:55-145, 364-421) on particles
+ * [ns][cap][6] with counts [ns]; currents [ns] follow the counts. Returns the particles
+ * that found no room (0 when cap suffices). */
+int orc_sort(int ns, int cap, double *particles, int *counts, double *current, double reflength, double sample);
+
 /* Chicanes (Undulator::chic_*) of the following orc_run_steps calls: tab [nsteps][4] =
  * angle, lb, ld, lt for each row of the lattice passed there (0 angle: none); nsteps 0
  * clears them. */

@@ -75,6 +75,35 @@ class _Lib:
             L.orc_deposit_source.argtypes = [_pd, _i, _i, _i, _pd, _pd, _d, _i, _i, _d, _pd]
             L.orc_adi_advance.argtypes = [_i, _i, _i, _d, _d, _d, _pd, _pd]
 
+    def set_counts(self, counts=None, sort_every=0):
+        """One4one window of the following run_steps calls: particles per slice (None
+        clears), and a sort after the push of every sort_every-th step."""
+        f = getattr(self.lib, self.p + "set_one4one" if self.p == "g4ref_" else self.p + "set_counts")
+        f.argtypes = [_i, _pi, _i]
+        if counts is None:
+            f(0, None, 0)
+            return
+        c = np.ascontiguousarray(counts, dtype=np.int32)
+        f(int(c.size), _ptr(c, _pi), int(sort_every))
+
+    def get_counts(self, ns):
+        out = np.zeros(ns, dtype=np.int32)
+        f = getattr(self.lib, self.p + "get_counts")
+        f.argtypes = [_i, _pi]
+        f(int(ns), _ptr(out, _pi))
+        return out
+
+    def sort(self, particles, counts, current, reflength, sample):
+        """Beam::sort of a one4one window (oracle only): returns (particles, counts,
+        current, lost)."""
+        part = np.array(particles, dtype=np.float64, order="C", copy=True)
+        cnt = np.array(counts, dtype=np.int32, copy=True)
+        cur = np.array(current, dtype=np.float64, copy=True)
+        self.lib.orc_sort.argtypes = [_i, _i, _pd, _pi, _pd, _d, _d]
+        lost = self.lib.orc_sort(part.shape[0], part.shape[1], _ptr(part), _ptr(cnt, _pi), _ptr(cur),
+                                 float(reflength), float(sample))
+        return part, cnt, cur, lost
+
     def set_chicanes(self, table=None):
         """Chicanes [nsteps][4] (angle, lb, ld, lt) of the following run_steps calls'
         lattice rows; None clears them."""

@@ -36,6 +36,12 @@ enum {
 // chicanes of the following g4ref_run_steps calls: [nsteps][4] angle, lb, ld, lt
 static std::vector<double> g_chic;
 
+// one4one windows of the following g4ref_run_steps calls: particles per slice, and a
+// Beam::sort after the push of every sort_every-th step (Gencore.cpp:121-132); the counts
+// after the last call
+static std::vector<int> g_o4o_counts, g_o4o_out;
+static int g_o4o_sort_every = 0;
+
 static void fill_undulator(Undulator *und, int nsteps, const double *tab, double gammaref) {
   auto col = [&](std::vector<double> &v, int c) {
     v.resize(nsteps);
@@ -81,6 +87,15 @@ static std::vector<double> g_wk_ext, g_wk_res, g_wk_geo, g_wk_rou;
 
 extern "C" {
 
+void g4ref_set_one4one(int nslice, const int *counts, int sort_every) {
+  g_o4o_counts.assign(counts, counts + (nslice > 0 && counts ? nslice : 0));
+  g_o4o_sort_every = sort_every;
+}
+
+void g4ref_get_counts(int nslice, int *out) {
+  for (int i = 0; i < nslice; i++) out[i] = i < (int)g_o4o_out.size() ? g_o4o_out[i] : -1;
+}
+
 void g4ref_set_chicanes(int nsteps, const double *tab) {
   g_chic.assign(tab, tab + 4 * static_cast<size_t>(nsteps > 0 ? nsteps : 0));
 }
@@ -122,7 +137,9 @@ int g4ref_run_steps(int nsteps, const double *tab, double gammaref, int ns, int 
   fill_undulator(&und, nsteps, tab, gammaref);
 
   Beam beam;
-  beam.init(ns, 1, reflength, reflength * sample, 0.0, false);
+  const bool o4o = g_o4o_counts.size() == static_cast<size_t>(ns);
+  beam.init(ns, 1, reflength, reflength * sample, 0.0, o4o);
+  if (o4o) beam.initSorting(0, 1, false, true);
   if (g_sc_nz > 0 || g_sc_longrange)
     beam.initEField(g_sc_rmax, g_sc_ngrid, g_sc_nz, g_sc_nphi, reflength, g_sc_longrange != 0);
   if (g_wk_on) {
@@ -132,8 +149,9 @@ int g4ref_run_steps(int nsteps, const double *tab, double gammaref, int ns, int 
   }
   for (int is = 0; is < ns; is++) {
     beam.current[is] = current[is];
-    beam.beam[is].resize(npart);
-    for (int ip = 0; ip < npart; ip++) {
+    const int n = o4o ? g_o4o_counts[is] : npart;
+    beam.beam[is].resize(n);
+    for (int ip = 0; ip < n; ip++) {
       const double *p = particles + (static_cast<size_t>(is) * npart + ip) * 6;
       Particle &q = beam.beam[is][ip];
       q.gamma = p[0]; q.theta = p[1]; q.x = p[2]; q.y = p[3]; q.px = p[4]; q.py = p[5];
@@ -157,21 +175,33 @@ int g4ref_run_steps(int nsteps, const double *tab, double gammaref, int ns, int 
 
   Control control;
   control.init(0, 1, "g4ref", &beam, &fld, &und, time_run != 0, false, periodic != 0);
+  int istep = 0;
   while (und.advance(0)) {
     double delz = und.steplength();
     if (stages & 1) beam.track(delz, &fld, &und);
+    if (o4o && g_o4o_sort_every > 0 && (istep + 1) % g_o4o_sort_every == 0) {
+      int shift = beam.sort();
+      if (shift != 0)
+        for (auto *f : fld) control.applySlippage(shift, f);
+    }
+    istep++;
     if (stages & 2)
       for (auto *f : fld) f->track(delz, &beam, &und);
     if (stages & 4)
       for (auto *f : fld) control.applySlippage(und.slippage(), f);
   }
 
-  for (int is = 0; is < ns; is++)
-    for (int ip = 0; ip < npart; ip++) {
+  g_o4o_out.assign(ns, npart);
+  for (int is = 0; is < ns; is++) {
+    const int n = static_cast<int>(beam.beam[is].size());
+    if (n > npart) return 3;  // the window's capacity is too small for the sorted slice
+    g_o4o_out[is] = n;
+    for (int ip = 0; ip < n; ip++) {
       double *p = particles + (static_cast<size_t>(is) * npart + ip) * 6;
       const Particle &q = beam.beam[is][ip];
       p[0] = q.gamma; p[1] = q.theta; p[2] = q.x; p[3] = q.y; p[4] = q.px; p[5] = q.py;
     }
+  }
   for (int k = 0; k < nfld; k++) {
     for (int is = 0; is < ns; is++)
       for (size_t c = 0; c < ncell; c++) {

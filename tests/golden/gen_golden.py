@@ -22,9 +22,11 @@ Fixtures (numpy .npz):
 
   chicane.npz    integration steps through a chicane between two undulator modules
                  (TrackBeam::applyChicane and applyR56), time-dependent and steady state
+  one4one.npz    one4one windows (slices of different particle counts) sorted after the
+                 push (Beam::sort), every step and every third step with space charge
 
-`python tests/golden/gen_golden.py spacecharge` (or `wakes`, `chicane`) regenerates only
-that file.
+`python tests/golden/gen_golden.py spacecharge` (or `wakes`, `chicane`, `one4one`)
+regenerates only that file.
 
 The reference's CI check of Example1 (examples/Example1-SteadyState/TEST_power.py)
 expects a final power of 0.932785e9 W within 30 %; example1.npz records what the
@@ -340,6 +342,60 @@ def gen_chicane(r):
     np.savez_compressed(os.path.join(HERE, "chicane.npz"), **d)
 
 
+# resonant at lambda0 1e-10 with aw 1.7 and lambdau 0.015: the phases stay near their
+# slices, and sorting moves only the particles that cross a slice boundary
+O4O_GAMMA = 17081.0
+
+
+def o4o_window(r, ns=6, cap=96, seed=3):
+    """A one4one window: slices of 50..80 particles (capacity cap), uniform phases, with
+    some phases pushed outside their slice (moved by the first sort) and a few outside
+    the window (dropped by it)."""
+    rng = np.random.default_rng(seed)
+    cur = np.full(ns, 2500.0)
+    part = r.load_beam(T.slice_params(ns, O4O_GAMMA, 2.0, 0.4e-6, 15.0, currents=cur), 0, cap, 1, 5, 0, 1e-10, 1.0)
+    counts = rng.integers(50, 81, ns).astype(np.int32)
+    for i in range(ns):
+        k = rng.choice(counts[i], size=counts[i] // 8, replace=False)
+        part[i, k, 1] += rng.uniform(-7.0, 7.0, k.size)
+        part[i, counts[i]:, :] = 0.0
+    part[0, 0, 1] = -0.5                      # s < 0: leaves the window
+    part[ns - 1, 1, 1] = 2 * np.pi + 0.25     # beyond the window's end
+    return part, counts, cur
+
+
+def o4o_cases(r):
+    lat = T.undulator_lattice(1.7, 0.015, 12, 1, 1e-10, O4O_GAMMA)
+    part, counts, cur = o4o_window(r)
+    gh = r.gauss_hermite(T.gauss_field_par(1e-10, 1e5, 20e-6), 6e-5, 25)
+    fld = np.stack([gh * (1 + 0.2j * k) for k in range(part.shape[0])])[None]
+    base = dict(lat=lat, gammaref=O4O_GAMMA, part=part, cur=cur, counts=counts, harm=[1], gridmax=[6e-5],
+                fields=fld, first=[0], time_run=1, periodic=0)
+    return [dict(base, name="every", every=1, efield=[0.0, 0, 0, 0, 0]),
+            dict(base, name="third", every=3, efield=[0.0, 16, 1, 1, 1])]
+
+
+def gen_one4one(r):
+    d = {}
+    for c in o4o_cases(r):
+        n = c["name"]
+        for k in ("lat", "part", "cur", "counts", "harm", "gridmax", "fields", "first", "efield"):
+            d[f"{n}_{k}"] = np.asarray(c[k])
+        d[f"{n}_args"] = np.array([c["gammaref"], c["time_run"], c["periodic"], c["every"]])
+        r.set_counts(c["counts"], c["every"])
+        rmax, ngr, nz, nphi, lr = c["efield"]
+        r.set_efield(rmax, int(ngr), int(nz), int(nphi), bool(lr))
+        out = r.run_steps(c["lat"], c["gammaref"], c["part"], c["cur"], 1e-10, 1.0, c["harm"], c["gridmax"],
+                          c["fields"], c["first"], time_run=c["time_run"], periodic=c["periodic"], stages=7)
+        d[f"{n}_out_counts"] = r.get_counts(len(c["counts"]))
+        r.set_counts()
+        r.set_efield()
+        d[f"{n}_out_part"] = out[0]
+        d[f"{n}_out_fields"] = out[1]
+        d[f"{n}_out_first"] = out[2]
+    np.savez_compressed(os.path.join(HERE, "one4one.npz"), **d)
+
+
 LAT_FROM_OUT = {"aw": "aw", "ax": "ax", "ay": "ay", "ku": "ku", "kx": "kx", "ky": "ky",
                 "gradx": "gradx", "grady": "grady", "qf": "qf", "qx": "qx", "qy": "qy",
                 "cx": "cx", "cy": "cy", "dz": "dz", "slip": "slippage", "phase": "phaseshift",
@@ -447,9 +503,13 @@ def main():
     if sys.argv[1:] == ["chicane"]:
         gen_chicane(r)
         return
+    if sys.argv[1:] == ["one4one"]:
+        gen_one4one(r)
+        return
     gen_space_charge(r)
     gen_wakes(r)
     gen_chicane(r)
+    gen_one4one(r)
     gen_streams(r)
     gen_loading(r)
     gen_steps(r)

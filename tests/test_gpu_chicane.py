@@ -101,3 +101,33 @@ def test_set_chicanes_rejects_bad_tables(lib):
             h.set_chicanes(bad)
         h.set_chicanes(chic)
         h.set_chicanes(np.zeros_like(chic))  # none
+
+
+@pytest.mark.parametrize("slip", [10.3, 3.0, -6.2])
+def test_long_slippage_clears_like_the_oracle(lib, oracle, slip):
+    """A step whose slippage enters more slices than the window holds (a chicane's
+    delay): every slice cleared once and the ring start moved by the full count, as the
+    reference's slice-by-slice loop leaves them; also a shorter and a backward one."""
+    import g4gpu
+    g = fixture("td")
+    lat = g("lat").copy()
+    lat[6, 14] = slip  # the chicane row's slippage (column "slip")
+    gammaref, time_run, periodic = g("args")
+    oracle.set_chicanes(g("chic"))
+    try:
+        rp, rf, rfirst, _ = oracle.run_steps(lat, gammaref, g("part"), g("cur"), 1e-10, 1.0, g("harm"), g("gridmax"),
+                                             g("fields"), g("first"), time_run=1, periodic=0, stages=7)
+    finally:
+        oracle.set_chicanes()
+    part, fields = g("part"), g("fields")
+    cfg = g4gpu.Config(nslice=4, npart=part.shape[1], ngrid=25, gridmax=6e-5, lambda0=1e-10, sample=1.0,
+                       gammaref=float(gammaref), time_run=1)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.set_chicanes(g("chic"))
+        h.load_beam(part, g("cur"))
+        h.load_field(0, fields[0], first=int(g("first")[0]))
+        h.run(0, lat.shape[0])
+        p = h.get_beam()
+        f, first, _ = h.get_field(0)
+    assert_plain_like(p, [(f, first)], part, rp, rf, rfirst)

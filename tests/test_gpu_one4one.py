@@ -1,0 +1,132 @@
+"""One4one windows on the device: slices of different particle counts, and Beam::sort
+between the push and the field solve (g4gpu_sort), through the C ABI, against the
+reference run (tests/golden/one4one.npz, bit-exact with the oracle) and the oracle.
+
+The engine keeps each slice's staying particles in order and appends the arrivals; the
+reference removes by swapping with the last particle. Slices are therefore compared as
+sets (ordered by phase). Tolerances: plain FP64 1e-9 of the largest value of each
+coordinate (gamma about gammaref), counts equal; mixed form slice counts within one
+particle and slice power within 1 %.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def fixture(case):
+    d = golden("one4one.npz")
+    return lambda k: d[f"{case}_{k}"]
+
+
+def run_engine(g, precision, graph=False):
+    import g4gpu
+    gammaref, time_run, periodic, every = g("args")
+    part, fields = g("part"), g("fields")
+    ns, cap = part.shape[0], part.shape[1]
+    ngrid = int(round(np.sqrt(fields.shape[2])))
+    cfg = g4gpu.Config(nslice=ns, npart=cap, ngrid=ngrid, harm=list(g("harm")), gridmax=list(g("gridmax")),
+                       lambda0=1e-10, sample=1.0, gammaref=float(gammaref), precision=precision,
+                       time_run=int(time_run), periodic=int(periodic))
+    lat = g("lat")
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam_counts(part, g("cur"), g("counts"))
+        for k in range(fields.shape[0]):
+            h.load_field(k, fields[k], first=int(g("first")[k]))
+        rmax, ngr, nz, nphi, lr = g("efield")
+        if nz > 0 or lr:
+            h.set_efield(rmax, int(ngr), int(nz), int(nphi), bool(lr))
+        h.set_graph_mode(graph)
+        for i in range(lat.shape[0]):
+            h.run(i, 1, g4gpu.STAGE_PUSH)
+            if (i + 1) % int(every) == 0:
+                assert h.sort() == 0
+            h.run(i, 1, g4gpu.STAGE_FIELD | g4gpu.STAGE_SLIP)
+        p = h.get_beam()
+        counts = h.get_counts()
+        f, first, _ = h.get_field(0)
+        bd, fd = h.diag(1)
+    return p, counts, f, first, bd, fd
+
+
+def by_phase(p, n):
+    s = p[:n]
+    return s[np.argsort(s[:, 1], kind="stable")]
+
+
+@pytest.mark.parametrize("case,graph", [("every", False), ("third", False), ("every", True)])
+def test_plain_one4one_matches_reference(lib, case, graph):
+    g = fixture(case)
+    p, counts, f, first, bd, _ = run_engine(g, 0, graph)
+    ref_c, ref_p = g("out_counts"), g("out_part")
+    assert np.array_equal(counts, ref_c)
+    gref = float(g("args")[0])
+    got = np.concatenate([by_phase(p[i], n) for i, n in enumerate(counts)])
+    want = np.concatenate([by_phase(ref_p[i], n) for i, n in enumerate(ref_c)])
+    got[:, 0] -= gref
+    want[:, 0] -= gref
+    for col in range(6):
+        scale = np.abs(want[:, col]).max()
+        assert np.abs(got[:, col] - want[:, col]).max() <= 1e-9 * scale, col
+    ref_f = g("out_fields")[0]
+    assert np.abs(f - ref_f).max() <= 1e-9 * np.abs(ref_f).max()
+    assert first == int(g("out_first")[0])
+    # the slice diagnostics divide by each slice's own count
+    for i, n in enumerate(counts):
+        assert abs(bd[i, 0] - ref_p[i, :n, 0].mean()) <= 1e-9 * gref
+
+
+def test_mixed_one4one_within_one_percent(lib, oracle):
+    g = fixture("third")
+    _, counts, f, first, _, fd = run_engine(g, 1)
+    ref_c = g("out_counts")
+    assert np.abs(counts.astype(int) - ref_c.astype(int)).max() <= 1
+    of = oracle.diag_field(g("out_fields")[0], float(g("gridmax")[0]), 1e-10, 1, int(g("out_first")[0]))
+    assert np.abs(fd[0][:, 0] - of[:, 0]).max() <= 1e-2 * np.abs(of[:, 0]).max()
+
+
+def test_sort_of_a_full_window_is_a_no_op(lib):
+    import g4gpu
+    g = fixture("every")
+    part = g("part")
+    cfg = g4gpu.Config(nslice=part.shape[0], npart=part.shape[1], ngrid=25, gridmax=6e-5, lambda0=1e-10,
+                       sample=1.0, gammaref=17081.0)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(g("lat"))
+        h.load_beam(part, g("cur"))
+        assert h.sort() == 0
+        assert np.array_equal(h.get_beam(), part)
+        assert np.all(h.get_counts() == part.shape[1])
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_sort_reports_slices_without_room(lib, prec):
+    """Particles moving into a full slice are counted, not written, and the call
+    reports it; the kernel never writes past a slice's capacity."""
+    import g4gpu
+    ns, cap = 3, 8
+    part = np.zeros((ns, cap, 6))
+    part[:, :, 0] = 17081.0
+    part[:, :, 1] = 1.0
+    part[1, :4, 1] = -2.0  # four particles of slice 1 move into slice 0, which is full
+    counts = np.array([8, 6, 5], dtype=np.int32)
+    cfg = g4gpu.Config(nslice=ns, npart=cap, ngrid=25, gridmax=6e-5, lambda0=1e-10, sample=1.0, gammaref=17081.0,
+                       precision=prec)
+    with g4gpu.Handle(cfg) as h:
+        h.load_beam_counts(part, np.full(ns, 1000.0), counts)
+        with pytest.raises(g4gpu.G4Error, match="no room"):
+            h.sort()
+        assert list(h.get_counts()) == [8, 2, 5]
+
+
+def test_load_beam_counts_rejects_bad_counts(lib):
+    import g4gpu
+    cfg = g4gpu.Config(nslice=2, npart=8, ngrid=25, gridmax=6e-5, lambda0=1e-10, sample=1.0, gammaref=17081.0)
+    with g4gpu.Handle(cfg) as h:
+        with pytest.raises(g4gpu.G4Error):
+            h.load_beam_counts(np.zeros((2, 8, 6)), np.zeros(2), np.array([9, 1]))
+        with pytest.raises(g4gpu.G4Error):
+            h.load_beam_counts(np.zeros((2, 8, 6)), np.zeros(2), np.array([-1, 1]))

@@ -289,3 +289,58 @@ def test_chicane_steps(oracle, case):
         assert np.allclose(part, g("out_part"), rtol=1e-12, atol=0)
         assert np.allclose(fld, g("out_fields"), rtol=1e-12, atol=1e-12 * np.abs(g("out_fields")).max())
     assert np.array_equal(first, g("out_first"))
+
+
+@pytest.mark.parametrize("case", ["every", "third"])
+def test_one4one_sorting_steps(oracle, case):
+    """One4one windows (slices of different particle counts) sorted after the push
+    (Beam::sort, Sorting::globalSort / localSort for one rank): the oracle against the
+    reference run (tests/golden/one4one.npz), particles in the reference's order."""
+    d = golden("one4one.npz")
+    g = lambda k: d[f"{case}_{k}"]
+    gammaref, time_run, periodic, every = g("args")
+    rmax, ngr, nz, nphi, lr = g("efield")
+    oracle.set_counts(g("counts"), int(every))
+    oracle.set_efield(rmax, int(ngr), int(nz), int(nphi), bool(lr))
+    try:
+        part, fld, first, _ = oracle.run_steps(g("lat"), gammaref, g("part"), g("cur"), 1e-10, 1.0, g("harm"),
+                                               g("gridmax"), g("fields"), g("first"), time_run=int(time_run),
+                                               periodic=int(periodic), stages=7)
+        counts = oracle.get_counts(g("counts").size)
+    finally:
+        oracle.set_counts()
+        oracle.set_efield()
+    assert np.array_equal(counts, g("out_counts"))
+    for i, n in enumerate(counts):
+        if EXACT:
+            assert np.array_equal(part[i, :n], g("out_part")[i, :n])
+        else:
+            assert np.allclose(part[i, :n], g("out_part")[i, :n], rtol=1e-12, atol=0)
+    if EXACT:
+        assert np.array_equal(fld, g("out_fields"))
+    else:
+        assert np.allclose(fld, g("out_fields"), rtol=1e-12, atol=1e-12 * np.abs(g("out_fields")).max())
+    assert np.array_equal(first, g("out_first"))
+
+
+def test_sort_drops_and_moves_like_the_reference(oracle):
+    """orc_sort on its own: phases beyond the slice move, the window's ends drop,
+    currents follow the counts (ce / slicelength per particle)."""
+    ns, cap = 3, 8
+    part = np.zeros((ns, cap, 6))
+    counts = np.array([4, 3, 2], dtype=np.int32)
+    th = [[0.5, 7.0, -0.25, 13.0], [1.0, -7.0, 20.0], [6.0, 6.5]]
+    for i, t in enumerate(th):
+        part[i, :len(t), 1] = t
+        part[i, :len(t), 0] = 100 * i + np.arange(len(t))  # labels
+    p, c, cur, lost = oracle.sort(part, counts, np.zeros(ns), 1e-10, 1.0)
+    assert lost == 0
+    two_pi = 2 * np.pi
+    got = {i: sorted((round(p[i, k, 0]), round(p[i, k, 1], 9)) for k in range(c[i])) for i in range(ns)}
+    # slice 0: 0.5 stays, 7.0 -> slice 1, -0.25 drops (s < 0), 13.0 -> slice 2;
+    # slice 1: 1.0 stays, -7.0 drops (s < 0), 20.0 drops (s > 3 * 2 pi);
+    # slice 2: 6.0 stays, 6.5 drops (s > 3 * 2 pi)
+    assert got[0] == [(0, 0.5)]
+    assert got[1] == sorted([(1, round(7.0 - two_pi, 9)), (100, 1.0)])
+    assert got[2] == sorted([(3, round(13.0 - 2 * two_pi, 9)), (200, 6.0)])
+    assert np.allclose(cur, c * 4.8032045e-11 / 1e-10)
