@@ -905,6 +905,61 @@ int g4gpu_set_wake(g4gpu_handle h, int ns_hr, double ds, const double *ext, cons
   return G4GPU_OK;
 }
 
+// Control::applySlippage for a single rank (Control.cpp:158-276) on field k: the ring
+// start moves by one slice per crossing of 0.8 sample and the slice that enters the
+// window is cleared unless the window is periodic
+static int apply_slippage(g4gpu_handle h, int k, double slippage) {
+  const g4gpu_config &c = h->cfg;
+  const int ns = c.nslice;
+  const size_t ncell = (size_t)c.ngrid * c.ngrid;
+  h->accuslip[k] += slippage;
+  int direction = 1;
+  // the slices that enter the window are cleared; a long slip (a chicane's delay spans
+  // many windows) may enter every slice, which is then one clearing copy
+  std::vector<char> cleared;
+  int ncleared = 0;
+  while (std::fabs(h->accuslip[k]) > (c.sample * 0.8)) {
+    if (h->accuslip[k] < 0) direction = -1;
+    h->accuslip[k] -= c.sample * direction;
+    int last = (h->first[k] + ns - 1) % ns;
+    if (direction < 0) last = (last + 1) % ns;
+    if (!c.periodic) {
+      if (cleared.empty()) cleared.assign(ns, 0);
+      if (!cleared[last]) {
+        cleared[last] = 1;
+        ncleared++;
+      }
+    }
+    h->first[k] = last;
+    if (direction < 0) h->first[k] = (last + 1) % ns;
+  }
+  if (ncleared == ns) {
+    G4_CUDA(h, cudaMemsetAsync(h->field[k], 0, (size_t)ns * ncell * h->csize, h->stream));
+  } else if (ncleared > 0) {
+    for (int is = 0; is < ns; is++)
+      if (cleared[is])
+        G4_CUDA(h, cudaMemsetAsync((char *)h->field[k] + (size_t)is * ncell * h->csize, 0, ncell * h->csize,
+                                   h->stream));
+  }
+  // a record formed during the step holds the slices' sums before clearing
+  if (ncleared > 0 && h->diag_fields_in_step) {
+    const size_t fw = g4::kFieldSums + 2;
+    double *d0 = h->diag_rec + (size_t)ns * g4::beam_diag_width(h->diag_nharm) + (size_t)k * ns * fw;
+    for (int is = 0; is < ns; is++)
+      if (cleared[is]) G4_CUDA(h, cudaMemsetAsync(d0 + (size_t)is * fw, 0, fw * sizeof(double), h->stream));
+  }
+  return G4GPU_OK;
+}
+
+int g4gpu_apply_slippage(g4gpu_handle h, int ifld, double slippage) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (ifld < 0 || ifld >= h->cfg.nfield) return fail(h, G4GPU_ERR_ARG, "field index out of range");
+  if (!std::isfinite(slippage)) return fail(h, G4GPU_ERR_ARG, "slippage must be finite");
+  if (!h->cfg.time_run) return G4GPU_OK;  // Control.cpp:159
+  cudaSetDevice(h->cfg.device);
+  return apply_slippage(h, ifld, slippage);
+}
+
 static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
   const g4gpu_config &c = h->cfg;
   int ns = c.nslice, np = c.npart, ng = c.ngrid;
@@ -1046,49 +1101,11 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
     }
     }
     G4_CUDA(h, cudaGetLastError());
-    if (do_slip) {
-      // Control::applySlippage for a single rank (Control.cpp:158-276): the ring
-      // start moves by one slice per crossing of 0.8 sample and the slice that
-      // enters the window is cleared unless the window is periodic
+    if (do_slip)
       for (int k = 0; k < c.nfield; k++) {
-        h->accuslip[k] += h->slip[istep];
-        int direction = 1;
-        // the slices that enter the window are cleared; a long slip (a chicane's delay
-        // spans many windows) may enter every slice, which is then one clearing copy
-        std::vector<char> cleared;
-        int ncleared = 0;
-        while (std::fabs(h->accuslip[k]) > (c.sample * 0.8)) {
-          if (h->accuslip[k] < 0) direction = -1;
-          h->accuslip[k] -= c.sample * direction;
-          int last = (h->first[k] + ns - 1) % ns;
-          if (direction < 0) last = (last + 1) % ns;
-          if (!c.periodic) {
-            if (cleared.empty()) cleared.assign(ns, 0);
-            if (!cleared[last]) {
-              cleared[last] = 1;
-              ncleared++;
-            }
-          }
-          h->first[k] = last;
-          if (direction < 0) h->first[k] = (last + 1) % ns;
-        }
-        if (ncleared == ns) {
-          G4_CUDA(h, cudaMemsetAsync(h->field[k], 0, (size_t)ns * ncell * h->csize, h->stream));
-        } else if (ncleared > 0) {
-          for (int is = 0; is < ns; is++)
-            if (cleared[is])
-              G4_CUDA(h, cudaMemsetAsync((char *)h->field[k] + (size_t)is * ncell * h->csize, 0,
-                                         ncell * h->csize, h->stream));
-        }
-        // a record formed during the step holds the slices' sums before clearing
-        if (ncleared > 0 && h->diag_fields_in_step) {
-          const size_t fw = g4::kFieldSums + 2;
-          double *d0 = h->diag_rec + (size_t)ns * g4::beam_diag_width(h->diag_nharm) + (size_t)k * ns * fw;
-          for (int is = 0; is < ns; is++)
-            if (cleared[is]) G4_CUDA(h, cudaMemsetAsync(d0 + (size_t)is * fw, 0, fw * sizeof(double), h->stream));
-        }
+        int rc = apply_slippage(h, k, h->slip[istep]);
+        if (rc) return rc;
       }
-    }
   }
   return G4GPU_OK;
 }

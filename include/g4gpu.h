@@ -170,6 +170,12 @@ int g4gpu_get_counts(g4gpu_handle h, int *counts);
  * g4gpu_run(h, i, 1, G4GPU_STAGE_FIELD | G4GPU_STAGE_SLIP). */
 int g4gpu_sort(g4gpu_handle h, int *shift);
 
+/* Control::applySlippage (src/Core/Control.cpp:158-276) of field ifld by `slippage`
+ * wavelengths outside the step loop, as Gencore::run does after a sort that returned a
+ * shift (Gencore.cpp:125-131): the ring start moves and entering slices are cleared
+ * unless the window is periodic; nothing for a steady-state run. Asynchronous. */
+int g4gpu_apply_slippage(g4gpu_handle h, int ifld, double slippage);
+
 /* Copies field ifld (host, storage order) to the device with ring start `first`
  * and accumulated slippage `accuslip` (Field::first, Field::accuslip). */
 int g4gpu_load_field(g4gpu_handle h, int ifld, const double *field, int first, double accuslip);

@@ -130,3 +130,37 @@ def test_load_beam_counts_rejects_bad_counts(lib):
             h.load_beam_counts(np.zeros((2, 8, 6)), np.zeros(2), np.array([9, 1]))
         with pytest.raises(g4gpu.G4Error):
             h.load_beam_counts(np.zeros((2, 8, 6)), np.zeros(2), np.array([-1, 1]))
+
+
+@pytest.mark.parametrize("periodic,time_run,slip", [(0, 1, 2.3), (1, 1, -1.7), (0, 0, 3.0), (0, 1, 9.5)])
+def test_apply_slippage_outside_the_step(lib, periodic, time_run, slip):
+    """Control::applySlippage on its own (after a sort that returned a shift): the ring
+    start moves one slice per 0.8-sample crossing, entering slices are cleared unless
+    periodic, steady-state runs are left alone; restated here from Control.cpp:158-276."""
+    import g4gpu
+    ns, ng = 4, 25
+    cfg = g4gpu.Config(nslice=ns, npart=8, ngrid=ng, gridmax=6e-5, lambda0=1e-10, sample=1.0, gammaref=17081.0,
+                       time_run=time_run, periodic=periodic)
+    rng = np.random.default_rng(1)
+    fld = rng.normal(size=(ns, ng * ng)) + 1j * rng.normal(size=(ns, ng * ng))
+    with g4gpu.Handle(cfg) as h:
+        h.load_field(0, fld, first=1, accuslip=0.1)
+        h.apply_slippage(0, slip)
+        f, first, acc = h.get_field(0)
+    want = fld.copy()
+    want_first, want_acc = 1, 0.1
+    if time_run:
+        want_acc += slip
+        direction = 1
+        while abs(want_acc) > 0.8:
+            if want_acc < 0:
+                direction = -1
+            want_acc -= direction
+            last = (want_first + ns - 1) % ns
+            if direction < 0:
+                last = (last + 1) % ns
+            if not periodic:
+                want[last] = 0
+            want_first = last if direction > 0 else (last + 1) % ns
+    assert first == want_first and abs(acc - want_acc) < 1e-12
+    assert np.array_equal(f, want)
