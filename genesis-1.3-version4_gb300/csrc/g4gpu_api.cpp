@@ -394,7 +394,7 @@ void g4gpu_destroy(g4gpu_handle h) {
                   h->closure_basis, h->closure_feat, h->closure_corr, h->sc.st, h->sc.state, h->sc.ez,
                   h->wake_tab, h->wake_loss, h->wake_lossf, h->wake_scratch, h->count_buf, h->sort_iscratch,
                   h->sort_scratch[0], h->sort_scratch[1], h->sort_scratch[2], h->sort_scratch[3],
-                  h->sort_scratch[4], h->sort_scratch[5]};
+                  h->sort_scratch[4], h->sort_scratch[5], h->isr_ctr};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
@@ -474,6 +474,8 @@ int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *tab) {
     s.grady = r[G4GPU_LAT_GRADY];
     s.autophase = r[G4GPU_LAT_PHASE];
     s.delz = r[G4GPU_LAT_DZ];
+    s.ku_raw = r[G4GPU_LAT_KU];
+    s.helical = r[G4GPU_LAT_HELICAL] != 0;
     s.gammaref = gamma0;
     s.nfld = c.nfield;
     int helical = r[G4GPU_LAT_HELICAL] != 0;
@@ -591,6 +593,27 @@ void chicane_matrix(double angle, double lb, double ld, double lt, double m[4][4
   for (auto e : seq) chicane_matmul(m, e);
 }
 }  // namespace
+
+int g4gpu_set_incoherent(g4gpu_handle h, int seed, int do_loss, int do_spread, int nbins) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (nbins < 1) return fail(h, G4GPU_ERR_ARG, "nbins must be at least 1");
+  cudaSetDevice(h->cfg.device);
+  if (!h->isr_ctr) {
+    int rc = alloc(h, (void **)&h->isr_ctr, sizeof(unsigned long long));
+    if (rc) return rc;
+  }
+  // a new stream: the counter of drawing steps restarts
+  G4_CUDA(h, cudaMemsetAsync(h->isr_ctr, 0, sizeof(unsigned long long), h->stream));
+  G4_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->isr_loss = do_loss != 0;
+  h->isr_spread = do_spread != 0;
+  h->isr_seed = (unsigned)seed;
+  h->isr_nbins = nbins;
+  for (auto &g : h->graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+  h->graphs.clear();
+  return G4GPU_OK;
+}
 
 int g4gpu_set_chicanes(g4gpu_handle h, int nsteps, const double *table) {
   if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
@@ -970,6 +993,25 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
   for (int istep = istep0; istep < istep0 + nsteps; istep++) {
     StepConst sc = h->steps[istep];
     for (int k = 0; k < c.nfield; k++) sc.f[k].first = h->first[k];
+    // Incoherent::apply (Incoherent.cpp:31-63): the step's loss and spread of gamma, in
+    // undulators
+    const bool isr_step = (h->isr_loss || h->isr_spread) && sc.aw > 0;
+    if (isr_step) {
+      const double gam0 = c.gammaref, awz = sc.aw, xkw0 = sc.ku_raw, delz = sc.delz;
+      double dgamsig = 1.015e-27 * xkw0 * xkw0 * awz * awz;
+      if (sc.helical)
+        dgamsig *= 1.42 * awz + 1. / (1. + 1.5 * awz + 0.95 * awz * awz);
+      else
+        dgamsig *= 1.697 * awz + 1. / (1. + 1.88 * awz + 0.8 * awz * awz);
+      if (!h->isr_spread) dgamsig = 0;
+      dgamsig = std::sqrt(dgamsig * gam0 * gam0 * gam0 * gam0 * xkw0 * delz) * std::sqrt(3.);
+      double dgamavg = xkw0 * gam0 * awz;
+      if (!h->isr_loss) dgamavg = 0;
+      dgamavg = dgamavg * dgamavg * 1.88e-15 * delz;
+      sc.isr_avg = dgamavg;
+      sc.isr_sig = dgamsig;
+    }
+    const g4::IsrStream isr{isr_step ? h->isr_ctr : nullptr, h->isr_seed, h->beam.count ? 1 : h->isr_nbins};
     g4::StepConstF scf_push{};
     if (h->mixed) scf_push = g4::to_float(sc, np);
     // Beam::track's push (Beam.cpp:97-112). With space charge, BeamSolver::advance
@@ -983,10 +1025,11 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
         Timed t(h, G4GPU_K_PUSH);
         if (h->mixed)
           g4::launch_push_mixed_sc(L, scf_push, h->beam, h->field, src, ns, np, ng, deposit, h->push_block, 0,
-                                   nullptr, nullptr, wake);
+                                   nullptr, nullptr, wake, isr);
         else
           g4::launch_push_plain_sc(L, sc, h->beam, h->field, src, ns, np, ng, deposit, h->push_block, 0,
-                                   nullptr, nullptr, wake);
+                                   nullptr, nullptr, wake, isr);
+        if (isr.ctr) g4::launch_isr_advance(h->stream, h->isr_ctr);
         return G4GPU_OK;
       }
       const bool shortrange = h->sc_nz > 0 && h->sc_ngrid > 2;
@@ -1025,10 +1068,11 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
       Timed t(h, G4GPU_K_PUSH);
       if (h->mixed)
         g4::launch_push_mixed_sc(L, scf_push, h->beam, h->field, src, ns, np, ng, deposit, h->push_block, 2, ez,
-                                 eloss, wake);
+                                 eloss, wake, isr);
       else
         g4::launch_push_plain_sc(L, sc, h->beam, h->field, src, ns, np, ng, deposit, h->push_block, 2, ez,
-                                 eloss, wake);
+                                 eloss, wake, isr);
+      if (isr.ctr) g4::launch_isr_advance(h->stream, h->isr_ctr);
       return G4GPU_OK;
     };
     bool any_dep = false;

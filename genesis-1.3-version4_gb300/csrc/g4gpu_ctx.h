@@ -57,6 +57,12 @@ struct g4gpu_ctx {
   double *wake_loss = nullptr;  // [nslice]
   float *wake_lossf = nullptr;  // [nslice]
   double *wake_scratch = nullptr;  // [2][wake_ns]
+  // incoherent synchrotron radiation (g4gpu_set_incoherent): flags, seed, beamlet size and
+  // the device counter of the steps that drew random numbers
+  bool isr_loss = false, isr_spread = false;
+  unsigned isr_seed = 0;
+  int isr_nbins = 1;
+  unsigned long long *isr_ctr = nullptr;
   // one4one windows (g4gpu_load_beam_counts): particles per slice on the device
   // (beam.count points at it then) and their host copy; the sort's scratch
   int *count_buf = nullptr;

@@ -57,6 +57,12 @@ struct StepConst {
   int chic;
   double cm[8];
   double r56;
+  // incoherent synchrotron radiation (g4gpu_set_incoherent): the lattice's ku and helical
+  // flag of the step, and the step's mean loss and spread half-width of gamma (0 off),
+  // Incoherent::apply (Incoherent.cpp:31-63)
+  double ku_raw;
+  int helical;
+  double isr_avg, isr_sig;
   FieldStep f[G4GPU_MAX_FIELDS];
 };
 
@@ -79,6 +85,7 @@ struct StepConstF {
   int chic;  // StepConst::chic, cm, r56
   float cm[8];
   float r56;
+  float isr_avg, isr_sig;  // StepConst::isr_avg, isr_sig
   FieldStepF f[G4GPU_MAX_FIELDS];
 };
 StepConstF to_float(const StepConst &s, int npart);
@@ -148,6 +155,16 @@ size_t noalloc_scratch_bytes();
 int adi_noalloc_mixed(int device, void *stream, void *field, const void *source, const float *coef,
                       float cstep, int ns, int ngrid, int first, std::string *msg);
 
+// Incoherent synchrotron radiation: the random stream of the push. ctr: the device
+// counter of steps drawn (advanced by launch_isr_advance after each push that draws),
+// seed: &sponrad seed, nbins: particles that share a draw (a beamlet)
+struct IsrStream {
+  const unsigned long long *ctr;
+  unsigned seed;
+  int nbins;
+};
+void launch_isr_advance(void *stream, unsigned long long *ctr);
+
 // Space charge (&efield, EFieldSolver.cpp), sc_kernels.cuh, instantiated in
 // kernels_plain.cu (FP64) and kernels_mixed.cu (FP32).
 struct ScConst {
@@ -184,10 +201,10 @@ void launch_sc_mixed(const Launch &L, const ScConst &c, const StepConstF &step, 
 // eev as FP32 (mixed).
 void launch_push_plain_sc(const Launch &L, const StepConst &sc, const DeviceBeam &b, void *const *field,
                           void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
-                          const void *ez, const double *eloss, const void *wake);
+                          const void *ez, const double *eloss, const void *wake, const IsrStream &isr);
 void launch_push_mixed_sc(const Launch &L, const StepConstF &sc, const DeviceBeam &b, void *const *field,
                           void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
-                          const void *ez, const double *eloss, const void *wake);
+                          const void *ez, const double *eloss, const void *wake, const IsrStream &isr);
 // Wakes (Collective::update): loss [nslice] = ext + the wake of each slice from the
 // window's current cur [nslice]; lossf = loss / eev in FP32; scratch: 2 ns_hr doubles.
 void launch_wake_update(const Launch &L, const double *cur, int nslice, int ns_hr, double ds, const double *ext,

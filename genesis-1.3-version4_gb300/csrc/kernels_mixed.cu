@@ -30,6 +30,7 @@
 #include <string>
 
 #include "g4gpu_internal.h"
+#include "philox.cuh"
 
 // Scratch of g4gpu_adi_advance_noalloc: 32 MiB, shared by every call on a device and
 // held by every device that loads this module until the process exits. Host code
@@ -70,6 +71,8 @@ StepConstF to_float(const StepConst &s, int npart) {
   f.chic = s.chic;
   for (int i = 0; i < 8; i++) f.cm[i] = (float)s.cm[i];
   f.r56 = (float)s.r56;
+  f.isr_avg = (float)s.isr_avg;
+  f.isr_sig = (float)s.isr_sig;
   for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
     const FieldStep &a = s.f[k];
     FieldStepF &b = f.f[k];
@@ -216,6 +219,8 @@ struct PtrsF {
   const float *wake;
   // particles per slice (one4one windows), null: np in every slice
   const int *count;
+  // incoherent radiation: the stream of the step (ctr null: off)
+  IsrStream isr;
 };
 
 // particles of slice is: np, or the slice's own count
@@ -359,6 +364,11 @@ __global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, 
   float dgam = h6 * (k1g + 2.f * k2g + 2.f * k3g + k4g);
   float dth = h6 * (k1t + 2.f * k2t + 2.f * k3t + k4t);
   dg += dgam;
+  // Incoherent::apply (Incoherent.cpp:66-77): one draw per beamlet of nbins particles
+  if (p.isr.ctr) {
+    const float u = (float)isr_uniform(p.isr.seed, *p.isr.ctr, is, ip / p.isr.nbins);
+    dg += -sc.isr_avg + sc.isr_sig * (2.f * u - 1.f);
+  }
   // Collective::apply (Collective.cpp:119-128), before the second half step
   if (p.wake) dg += p.wake[is] * sc.delz;
   th = add_phase(th, dth);
@@ -1929,13 +1939,15 @@ void launch_sc_mixed(const Launch &L, const ScConst &c, const StepConstF &step, 
 void launch_push_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b,
                        void *const *field, void *const *src, int ns, int np, int ngrid,
                        int deposit, int block) {
-  launch_push_mixed_sc(L, sc, b, field, src, ns, np, ngrid, deposit, block, 0, nullptr, nullptr, nullptr);
+  launch_push_mixed_sc(L, sc, b, field, src, ns, np, ngrid, deposit, block, 0, nullptr, nullptr, nullptr,
+                       IsrStream{});
 }
 
 void launch_push_mixed_sc(const Launch &L, const StepConstF &sc, const DeviceBeam &b, void *const *field,
                           void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
-                          const void *ez, const double *eloss, const void *wake) {
+                          const void *ez, const double *eloss, const void *wake, const IsrStream &isr) {
   PtrsF p = make_ptrs_f(b, field, src, sc.nfld);
+  if (isr.ctr && (sc.isr_avg != 0 || sc.isr_sig != 0) && mode != 1) p.isr = isr;
   p.mode = mode;
   p.ez = (const float *)ez;
   p.eloss = eloss;

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include "g4gpu_internal.h"
+#include "philox.cuh"
 
 namespace g4 {
 namespace {
@@ -183,6 +184,8 @@ struct Ptrs {
   const double *wake;
   // particles per slice (one4one windows), null: np in every slice
   const int *count;
+  // incoherent radiation: the stream of the step (ctr null: off)
+  IsrStream isr;
 };
 
 // particles of slice is: np, or the slice's own count
@@ -269,6 +272,11 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   gamma += stpz * (k3gg + k2gg / 6.0);
   theta += stpz * (k3pp + k2pp / 6.0);
 
+  // Incoherent::apply (Incoherent.cpp:66-77): one draw per beamlet of nbins particles
+  if (p.isr.ctr) {
+    const double u = isr_uniform(p.isr.seed, *p.isr.ctr, is, ip / p.isr.nbins);
+    gamma += -sc.isr_avg + sc.isr_sig * (2 * u - 1);
+  }
   // Collective::apply (Collective.cpp:119-128), before the second half step
   if (p.wake) gamma += p.wake[is] * sc.delz / kEev;
   // TrackBeam::applyR56 (TrackBeam.cpp:260-277)
@@ -616,13 +624,23 @@ void launch_sc_plain(const Launch &L, const ScConst &c, const StepConst &step, c
 void launch_push_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,
                        void *const *field, void *const *src, int ns, int np, int ngrid,
                        int deposit, int block) {
-  launch_push_plain_sc(L, sc, b, field, src, ns, np, ngrid, deposit, block, 0, nullptr, nullptr, nullptr);
+  launch_push_plain_sc(L, sc, b, field, src, ns, np, ngrid, deposit, block, 0, nullptr, nullptr, nullptr,
+                       IsrStream{});
+}
+
+namespace {
+__global__ void k_isr_advance(unsigned long long *ctr) { *ctr += 1; }
+}  // namespace
+
+void launch_isr_advance(void *stream, unsigned long long *ctr) {
+  k_isr_advance<<<1, 1, 0, (cudaStream_t)stream>>>(ctr);
 }
 
 void launch_push_plain_sc(const Launch &L, const StepConst &sc, const DeviceBeam &b, void *const *field,
                           void *const *src, int ns, int np, int ngrid, int deposit, int block, int mode,
-                          const void *ez, const double *eloss, const void *wake) {
+                          const void *ez, const double *eloss, const void *wake, const IsrStream &isr) {
   Ptrs p = make_ptrs(b, field, src, sc.nfld);
+  if (isr.ctr && (sc.isr_avg != 0 || sc.isr_sig != 0) && mode != 1) p.isr = isr;
   p.mode = mode;
   p.ez = (const double *)ez;
   p.eloss = eloss;

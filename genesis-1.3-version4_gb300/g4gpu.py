@@ -56,7 +56,7 @@ ABI_SYMBOLS = [
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
     "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc", "g4gpu_host_single_wakes",
     "g4gpu_set_wake", "g4gpu_set_chicanes", "g4gpu_load_beam_counts", "g4gpu_get_counts", "g4gpu_sort",
-    "g4gpu_apply_slippage",
+    "g4gpu_apply_slippage", "g4gpu_set_incoherent",
     "g4gpu_set_graph_mode", "g4gpu_autotune", "g4gpu_batch_create", "g4gpu_batch_destroy",
     "g4gpu_batch_member", "g4gpu_batch_run", "g4gpu_batch_synchronize",
     "g4gpu_mlp_create", "g4gpu_mlp_destroy", "g4gpu_mlp_last_error", "g4gpu_mlp_num_params",
@@ -171,6 +171,7 @@ def load_library(path=None):
     L.g4gpu_get_counts.argtypes = [vp, P(i)]
     L.g4gpu_sort.argtypes = [vp, P(i)]
     L.g4gpu_apply_slippage.argtypes = [vp, i, d]
+    L.g4gpu_set_incoherent.argtypes = [vp, i, i, i, i]
     L.g4gpu_set_graph_mode.argtypes = [vp, i]
     L.g4gpu_autotune.argtypes = [vp, P(i), P(i), P(i)]
     L.g4gpu_set_launch_shapes.argtypes = [vp, i, i, i]
@@ -327,6 +328,11 @@ class Handle:
         n = np.zeros(self.cfg.nslice, dtype=np.int32)
         self._check(self.L.g4gpu_get_counts(self.h, n.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
         return n
+
+    def set_incoherent(self, seed=1234, do_loss=False, do_spread=False, nbins=1):
+        """Incoherent synchrotron radiation (&sponrad) for the following steps."""
+        self._check(self.L.g4gpu_set_incoherent(self.h, int(seed), int(bool(do_loss)), int(bool(do_spread)),
+                                                int(nbins)))
 
     def apply_slippage(self, ifld, slippage):
         """Control::applySlippage of field ifld outside the step loop."""

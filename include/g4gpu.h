@@ -182,6 +182,16 @@ int g4gpu_load_field(g4gpu_handle h, int ifld, const double *field, int first, d
 /* Copies field ifld back (storage order) with its ring start and slippage. */
 int g4gpu_get_field(g4gpu_handle h, int ifld, double *field, int *first, double *accuslip);
 
+/* Incoherent synchrotron radiation for the following steps: &sponrad (seed, doLoss,
+ * doSpread, src/Main/SponRad.cpp:19-36) with the beam's beamlet size nbins (particles
+ * sharing one random draw; one4one windows draw per particle). Every undulator step then
+ * adds -loss + spread (2u - 1) to gamma after the integration (Incoherent::apply,
+ * src/Core/Incoherent.cpp:31-80). The loss is exact; the draws u come from a counter-based
+ * generator (Philox-4x32-10 on seed, step, slice and beamlet) instead of the reference's
+ * sequential ran2 stream, which it seeds per MPI rank: the same distribution, not the same
+ * numbers. Each call restarts the stream; do_loss = do_spread = 0 switches it off. */
+int g4gpu_set_incoherent(g4gpu_handle h, int seed, int do_loss, int do_spread, int nbins);
+
 /* Chicanes of the lattice steps: table [nsteps][4] with the bend angle, dipole length lb,
  * dipole spacing ld and total length lt of the chicane a step covers (0 angle: none), as
  * Undulator::chic_angle, chic_lb, chic_ld, chic_lt hold them after

@@ -1255,6 +1255,56 @@ static void apply_wake(step_ctx *c, int is0, int is1) {
   }
 }
 
+/* ---- incoherent synchrotron radiation (&sponrad), Incoherent.cpp ---------- */
+static struct {
+  int on, loss, spread, nbins;
+  ran2_t sran;
+} isr = {0, 0, 0, 1};
+
+/* Incoherent::init (Incoherent.cpp:12-27) for rank 0: the stream is seeded with
+ * round(1e9 u), u the first draw of a stream seeded with `seed`. The stream carries over
+ * orc_run_steps calls as the reference's member does; nbins: the beamlet size, one draw
+ * per beamlet (1 for one4one windows). */
+void orc_set_incoherent(int seed, int do_loss, int do_spread, int nbins) {
+  isr.on = do_loss || do_spread;
+  isr.loss = do_loss;
+  isr.spread = do_spread;
+  isr.nbins = nbins > 0 ? nbins : 1;
+  ran2_t rseed;
+  ran2_init(&rseed, (unsigned int)seed);
+  double val = ran2_next(&rseed);
+  val *= 1e9;
+  ran2_init(&isr.sran, (unsigned int)(int)round(val));
+}
+
+/* Incoherent::apply (Incoherent.cpp:31-80): the energy loss and the spread growth of
+ * one step, slice after slice, one draw per beamlet */
+static void apply_incoherent(step_ctx *c) {
+  const step_t *u = &c->st;
+  if (!(u->aw > 0)) return;
+  if (!isr.on) return;
+  double gam0 = c->gammaref, awz = u->aw, xkw0 = u->ku, delz = c->delz;
+  double dgamsig = 1.015e-27 * xkw0 * xkw0 * awz * awz;
+  if (u->helical)
+    dgamsig *= 1.42 * awz + 1. / (1. + 1.5 * awz + 0.95 * awz * awz);
+  else
+    dgamsig *= 1.697 * awz + 1. / (1. + 1.88 * awz + 0.8 * awz * awz);
+  if (!isr.spread) dgamsig = 0;
+  dgamsig = sqrt(dgamsig * gam0 * gam0 * gam0 * gam0 * xkw0 * delz) * sqrt(3.);
+  double dgamavg = xkw0 * gam0 * awz;
+  if (!isr.loss) dgamavg = 0;
+  dgamavg = dgamavg * dgamavg * 1.88e-15 * delz;
+  int nbins = c->count ? 1 : isr.nbins;
+  double dg = 0;
+  for (int is = 0; is < c->ns; is++) {
+    part_t *b = c->beam + (size_t)is * c->npart;
+    for (int ip = 0; ip < np_of(c, is); ip++) {
+      if ((ip % nbins) == 0) dg = -dgamavg + dgamsig * (2 * ran2_next(&isr.sran) - 1);
+      b[ip].gamma += dg;
+    }
+  }
+}
+
 /* TrackBeam::applyR56, TrackBeam.cpp:260-277 */
 static void apply_r56(step_ctx *c, int is0, int is1) {
   const step_t *u = &c->st;
@@ -1275,6 +1325,21 @@ static void run_push(void *ctx, int i0, int i1) {
   step_ctx *c = (step_ctx *)ctx;
   transverse_slices(c, i0, i1, 0);
   push_slices(c, i0, i1);
+  if (c->wake_loss) apply_wake(c, i0, i1);
+  apply_r56(c, i0, i1);
+  transverse_slices(c, i0, i1, 1);
+}
+
+/* the push in Beam::track's order when a step draws random numbers (the stream runs
+ * slice after slice): first half, advance, incoherent radiation, wakes, R56, second half
+ * (Beam.cpp:103-111) */
+static void run_push_first(void *ctx, int i0, int i1) {
+  step_ctx *c = (step_ctx *)ctx;
+  transverse_slices(c, i0, i1, 0);
+  push_slices(c, i0, i1);
+}
+static void run_push_second(void *ctx, int i0, int i1) {
+  step_ctx *c = (step_ctx *)ctx;
   if (c->wake_loss) apply_wake(c, i0, i1);
   apply_r56(c, i0, i1);
   transverse_slices(c, i0, i1, 1);
@@ -1464,12 +1529,17 @@ int orc_run_steps(int nsteps, const double *lat, double gammaref, int ns, int np
           c.sc_eloss = eloss[is];
           push_slices(&c, is, is + 1);
         }
+        apply_incoherent(&c);
         if (c.wake_loss) apply_wake(&c, 0, ns);
         apply_r56(&c, 0, ns);
         c.sc_ez = NULL;
         free(eloss);
         free(ez);
         parallel_for(ns, nthreads, run_transverse_second, &c);
+      } else if (isr.on && c.st.aw > 0) {
+        parallel_for(ns, nthreads, run_push_first, &c);
+        apply_incoherent(&c);
+        parallel_for(ns, nthreads, run_push_second, &c);
       } else {
         parallel_for(ns, nthreads, run_push, &c);
       }

@@ -113,6 +113,12 @@ void orc_get_counts(int nslice, int *out);
  * that found no room (0 when cap suffices). */
 int orc_sort(int ns, int cap, double *particles, int *counts, double *current, double reflength, double sample);
 
+/* Incoherent synchrotron radiation (&sponrad, Incoherent::init for rank 0,
+ * Incoherent.cpp:12-27) for the following orc_run_steps calls; the random stream carries
+ * over calls until the next orc_set_incoherent; nbins: beamlet size (one draw per
+ * beamlet). do_loss = do_spread = 0 switches it off. */
+void orc_set_incoherent(int seed, int do_loss, int do_spread, int nbins);
+
 /* Chicanes (Undulator::chic_*) of the following orc_run_steps calls: tab [nsteps][4] =
  * angle, lb, ld, lt for each row of the lattice passed there (0 angle: none); nsteps 0
  * clears them. */

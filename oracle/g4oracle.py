@@ -75,6 +75,12 @@ class _Lib:
             L.orc_deposit_source.argtypes = [_pd, _i, _i, _i, _pd, _pd, _d, _i, _i, _d, _pd]
             L.orc_adi_advance.argtypes = [_i, _i, _i, _d, _d, _d, _pd, _pd]
 
+    def set_incoherent(self, seed=1234, do_loss=False, do_spread=False, nbins=1):
+        """Incoherent synchrotron radiation (&sponrad) of the following run_steps calls."""
+        f = getattr(self.lib, self.p + "set_incoherent")
+        f.argtypes = [_i, _i, _i, _i]
+        f(int(seed), int(bool(do_loss)), int(bool(do_spread)), int(nbins))
+
     def set_counts(self, counts=None, sort_every=0):
         """One4one window of the following run_steps calls: particles per slice (None
         clears), and a sort after the push of every sort_every-th step."""

@@ -36,6 +36,10 @@ enum {
 // chicanes of the following g4ref_run_steps calls: [nsteps][4] angle, lb, ld, lt
 static std::vector<double> g_chic;
 
+// &sponrad of the following g4ref_run_steps calls (SponRad.cpp:34: Beam::initIncoherent)
+// and the beamlet size the beam is set up with (Beam::init's nbins)
+static int g_isr_seed = 0, g_isr_loss = 0, g_isr_spread = 0, g_isr_nbins = 1;
+
 // one4one windows of the following g4ref_run_steps calls: particles per slice, and a
 // Beam::sort after the push of every sort_every-th step (Gencore.cpp:121-132); the counts
 // after the last call
@@ -86,6 +90,13 @@ static bool g_wk_transient = false;
 static std::vector<double> g_wk_ext, g_wk_res, g_wk_geo, g_wk_rou;
 
 extern "C" {
+
+void g4ref_set_incoherent(int seed, int do_loss, int do_spread, int nbins) {
+  g_isr_seed = seed;
+  g_isr_loss = do_loss;
+  g_isr_spread = do_spread;
+  g_isr_nbins = nbins > 0 ? nbins : 1;
+}
 
 void g4ref_set_one4one(int nslice, const int *counts, int sort_every) {
   g_o4o_counts.assign(counts, counts + (nslice > 0 && counts ? nslice : 0));
@@ -138,8 +149,10 @@ int g4ref_run_steps(int nsteps, const double *tab, double gammaref, int ns, int 
 
   Beam beam;
   const bool o4o = g_o4o_counts.size() == static_cast<size_t>(ns);
-  beam.init(ns, 1, reflength, reflength * sample, 0.0, o4o);
+  const bool isr = g_isr_loss || g_isr_spread;
+  beam.init(ns, isr ? g_isr_nbins : 1, reflength, reflength * sample, 0.0, o4o);
   if (o4o) beam.initSorting(0, 1, false, true);
+  if (isr) beam.initIncoherent(g_isr_seed, 0, g_isr_loss != 0, g_isr_spread != 0);
   if (g_sc_nz > 0 || g_sc_longrange)
     beam.initEField(g_sc_rmax, g_sc_ngrid, g_sc_nz, g_sc_nphi, reflength, g_sc_longrange != 0);
   if (g_wk_on) {

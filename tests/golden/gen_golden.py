@@ -24,9 +24,12 @@ Fixtures (numpy .npz):
                  (TrackBeam::applyChicane and applyR56), time-dependent and steady state
   one4one.npz    one4one windows (slices of different particle counts) sorted after the
                  push (Beam::sort), every step and every third step with space charge
+  incoherent.npz incoherent synchrotron radiation (&sponrad): the energy loss over planar
+                 and helical lattices, and loss with spread over one step of a larger
+                 window (with the same window's step without it)
 
-`python tests/golden/gen_golden.py spacecharge` (or `wakes`, `chicane`, `one4one`)
-regenerates only that file.
+`python tests/golden/gen_golden.py spacecharge` (or `wakes`, `chicane`, `one4one`,
+`incoherent`) regenerates only that file.
 
 The reference's CI check of Example1 (examples/Example1-SteadyState/TEST_power.py)
 expects a final power of 0.932785e9 W within 30 %; example1.npz records what the
@@ -396,6 +399,31 @@ def gen_one4one(r):
     np.savez_compressed(os.path.join(HERE, "one4one.npz"), **d)
 
 
+def gen_incoherent(r):
+    d = {}
+    cur = np.array([3000.0, 2500.0, 1000.0, 3000.0])
+    gh = r.gauss_hermite(T.gauss_field_par(1e-10, 1e5, 20e-6), 6e-5, 25)
+    fld = np.stack([gh * (1 + 0.2j * k) for k in range(4)])[None]
+    cases = []
+    for name, helical, npart, nwig, loss, spread in (("loss", False, 64, 6, 1, 0), ("loss_helical", True, 64, 6, 1, 0),
+                                                     ("spread", False, 1024, 1, 1, 1)):
+        lat = T.undulator_lattice(1.7, 0.015, nwig, 1, 1e-10, 11357.8, helical=helical)
+        part = r.load_beam(T.slice_params(4, 11357.8, 2.0, 0.4e-6, 15.0, currents=cur), 0, npart, 4, 7, 1, 1e-10,
+                           1.0)
+        cases.append((name, lat, part, loss, spread))
+    for name, lat, part, loss, spread in cases:
+        d[f"{name}_lat"], d[f"{name}_part"] = lat, part
+        d[f"{name}_isr"] = np.array([1234, loss, spread, 4])
+        r.set_incoherent(1234, bool(loss), bool(spread), 4)
+        out = r.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, [1], [6e-5], fld, [0], time_run=1, stages=7)
+        r.set_incoherent(1234, False, False, 4)
+        base = r.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, [1], [6e-5], fld, [0], time_run=1, stages=7)
+        d[f"{name}_out_part"], d[f"{name}_out_fields"] = out[0], out[1]
+        d[f"{name}_base_part"] = base[0]
+    d["cur"], d["fields"] = cur, fld
+    np.savez_compressed(os.path.join(HERE, "incoherent.npz"), **d)
+
+
 LAT_FROM_OUT = {"aw": "aw", "ax": "ax", "ay": "ay", "ku": "ku", "kx": "kx", "ky": "ky",
                 "gradx": "gradx", "grady": "grady", "qf": "qf", "qx": "qx", "qy": "qy",
                 "cx": "cx", "cy": "cy", "dz": "dz", "slip": "slippage", "phase": "phaseshift",
@@ -506,10 +534,14 @@ def main():
     if sys.argv[1:] == ["one4one"]:
         gen_one4one(r)
         return
+    if sys.argv[1:] == ["incoherent"]:
+        gen_incoherent(r)
+        return
     gen_space_charge(r)
     gen_wakes(r)
     gen_chicane(r)
     gen_one4one(r)
+    gen_incoherent(r)
     gen_streams(r)
     gen_loading(r)
     gen_steps(r)

@@ -1,0 +1,107 @@
+"""Incoherent synchrotron radiation (&sponrad) on the device against the reference run
+(tests/golden/incoherent.npz, bit-exact with the oracle).
+
+The mean energy loss is deterministic: plain FP64 within 1e-9 of the largest change of
+gamma over the run, mixed within 1 % of the loss. The spread draws come from a
+counter-based generator instead of the reference's sequential ran2 stream, so one step's
+energy changes are compared in distribution: every particle of a beamlet changes alike,
+every change lies within [-loss - spread, -loss + spread], and mean and variance agree
+with the uniform law (-loss, spread^2 / 3) and with the reference's own draws within their
+sampling errors.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def run(case, precision, isr=True, steps=None, reuse=None):
+    import g4gpu
+    d = golden("incoherent.npz")
+    part, lat = d[f"{case}_part"], d[f"{case}_lat"]
+    seed, loss, spread, nbins = d[f"{case}_isr"]
+    cfg = g4gpu.Config(nslice=part.shape[0], npart=part.shape[1], ngrid=25, gridmax=6e-5, lambda0=1e-10,
+                       sample=1.0, gammaref=11357.8, precision=precision, time_run=1)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam(part, d["cur"])
+        h.load_field(0, d["fields"][0])
+        if isr:
+            h.set_incoherent(int(seed), bool(loss), bool(spread), int(nbins))
+        h.run(0, lat.shape[0])
+        return h.get_beam()
+
+
+def expected(lat_row, gam0=11357.8, helical=False):
+    ku, aw, dz = lat_row[3], lat_row[0], lat_row[13]
+    sig = 1.015e-27 * ku * ku * aw * aw
+    sig *= (1.42 * aw + 1 / (1 + 1.5 * aw + 0.95 * aw * aw)) if helical else (1.697 * aw + 1 / (1 + 1.88 * aw + 0.8 * aw * aw))
+    sig = np.sqrt(sig * gam0 ** 4 * ku * dz) * np.sqrt(3.0)
+    avg = (ku * gam0 * aw) ** 2 * 1.88e-15 * dz
+    return avg, sig
+
+
+@pytest.mark.parametrize("case", ["loss", "loss_helical"])
+def test_plain_energy_loss_matches_reference(lib, case):
+    d = golden("incoherent.npz")
+    p = run(case, 0)
+    p0 = d[f"{case}_part"]
+    want = d[f"{case}_out_part"]
+    for col in range(6):
+        a, b = (p[..., col] - p0[..., col], want[..., col] - p0[..., col]) if col < 2 else (p[..., col], want[..., col])
+        assert np.abs(a - b).max() <= 1e-9 * np.abs(b).max(), col
+    q = run(case, 0, isr=False)
+    assert np.abs((p - q)[..., 0] - (want - d[f"{case}_base_part"])[..., 0]).max() < 1e-9
+
+
+def test_mixed_energy_loss_within_one_percent(lib):
+    d = golden("incoherent.npz")
+    m = run("loss", 1)
+    m0 = run("loss", 1, isr=False)
+    ref = (d["loss_out_part"] - d["loss_base_part"])[..., 0]
+    assert np.abs((m - m0)[..., 0] - ref).max() <= 1e-2 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_energy_spread_in_distribution(lib, prec):
+    d = golden("incoherent.npz")
+    avg, sig = expected(d["spread_lat"][0])
+    dg = (run("spread", prec) - run("spread", prec, isr=False))[..., 0]  # one step: the draws themselves
+    beamlets = dg.reshape(dg.shape[0], -1, 4)
+    assert np.abs(beamlets - beamlets[..., :1]).max() <= (1e-9 if prec == 0 else 1e-4) * sig
+    tol = 1e-9 * sig if prec == 0 else 2e-3 * sig
+    assert dg.min() >= -avg - sig - tol and dg.max() <= -avg + sig + tol
+    x = beamlets[..., 0].ravel()  # one value per beamlet
+    n = x.size
+    assert abs(x.mean() + avg) < 4 * sig / np.sqrt(3 * n)
+    assert abs(x.var() / (sig * sig / 3) - 1) < 4 * np.sqrt(0.8 / n)
+    ref = (d["spread_out_part"] - d["spread_base_part"])[..., 0].reshape(dg.shape[0], -1, 4)[..., 0].ravel()
+    assert abs(x.mean() - ref.mean()) < 6 * sig / np.sqrt(3 * n)
+
+
+def test_stream_advances_and_restarts(lib):
+    import g4gpu
+    d = golden("incoherent.npz")
+    part, lat = d["spread_part"], d["spread_lat"]
+    cfg = g4gpu.Config(nslice=part.shape[0], npart=part.shape[1], ngrid=25, gridmax=6e-5, lambda0=1e-10,
+                       sample=1.0, gammaref=11357.8, time_run=0)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(np.vstack([lat, lat]))
+        h.load_beam(part, d["cur"])
+        h.load_field(0, d["fields"][0])
+        h.set_incoherent(7, True, True, 4)
+        h.run(0, 1)
+        a = h.get_beam()
+        h.load_beam(part, d["cur"])
+        h.load_field(0, d["fields"][0])
+        h.run(0, 1)  # the stream has moved on
+        b = h.get_beam()
+        h.load_beam(part, d["cur"])
+        h.load_field(0, d["fields"][0])
+        h.set_incoherent(7, True, True, 4)  # restarted
+        h.run(0, 1)
+        c = h.get_beam()
+    assert not np.array_equal(a[..., 0], b[..., 0])
+    assert np.array_equal(a, c)

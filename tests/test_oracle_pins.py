@@ -344,3 +344,22 @@ def test_sort_drops_and_moves_like_the_reference(oracle):
     assert got[1] == sorted([(1, round(7.0 - two_pi, 9)), (100, 1.0)])
     assert got[2] == sorted([(3, round(13.0 - 2 * two_pi, 9)), (200, 6.0)])
     assert np.allclose(cur, c * 4.8032045e-11 / 1e-10)
+
+
+@pytest.mark.parametrize("case", ["loss", "loss_helical", "spread"])
+def test_incoherent_radiation_steps(oracle, case):
+    """Incoherent synchrotron radiation (Incoherent::init / apply): the oracle's ran2
+    stream and energy changes against the reference run (tests/golden/incoherent.npz)."""
+    d = golden("incoherent.npz")
+    seed, loss, spread, nbins = d[f"{case}_isr"]
+    oracle.set_incoherent(int(seed), bool(loss), bool(spread), int(nbins))
+    try:
+        part, fld, _, _ = oracle.run_steps(d[f"{case}_lat"], 11357.8, d[f"{case}_part"], d["cur"], 1e-10, 1.0, [1],
+                                           [6e-5], d["fields"], [0], time_run=1, stages=7)
+    finally:
+        oracle.set_incoherent()
+    if EXACT:
+        assert np.array_equal(part, d[f"{case}_out_part"])
+        assert np.array_equal(fld, d[f"{case}_out_fields"])
+    else:
+        assert np.allclose(part, d[f"{case}_out_part"], rtol=1e-12, atol=0)
