@@ -55,6 +55,7 @@ def _units():
         ("g4gpu_api.cpp", cxx_common),
         ("host_loading.cpp", cxx_common + ["-pthread"]),
         ("host_wake.cpp", cxx_common + ["-pthread"]),
+        ("h5_writer.cpp", cxx_common),
         ("g4gpu_learned.cpp", cxx_common),
         ("g4gpu_dpi.cpp", cxx_common),
     ]

@@ -56,7 +56,7 @@ ABI_SYMBOLS = [
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
     "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc", "g4gpu_host_single_wakes",
     "g4gpu_set_wake", "g4gpu_set_chicanes", "g4gpu_load_beam_counts", "g4gpu_get_counts", "g4gpu_sort",
-    "g4gpu_apply_slippage", "g4gpu_set_incoherent",
+    "g4gpu_apply_slippage", "g4gpu_set_incoherent", "g4gpu_h5_create", "g4gpu_h5_dataset", "g4gpu_h5_close",
     "g4gpu_set_graph_mode", "g4gpu_autotune", "g4gpu_batch_create", "g4gpu_batch_destroy",
     "g4gpu_batch_member", "g4gpu_batch_run", "g4gpu_batch_synchronize",
     "g4gpu_mlp_create", "g4gpu_mlp_destroy", "g4gpu_mlp_last_error", "g4gpu_mlp_num_params",
@@ -172,6 +172,9 @@ def load_library(path=None):
     L.g4gpu_sort.argtypes = [vp, P(i)]
     L.g4gpu_apply_slippage.argtypes = [vp, i, d]
     L.g4gpu_set_incoherent.argtypes = [vp, i, i, i, i]
+    L.g4gpu_h5_create.argtypes = [ctypes.c_char_p, P(vp)]
+    L.g4gpu_h5_dataset.argtypes = [vp, ctypes.c_char_p, i, P(ctypes.c_longlong), pd, ctypes.c_char_p]
+    L.g4gpu_h5_close.argtypes = [vp]
     L.g4gpu_set_graph_mode.argtypes = [vp, i]
     L.g4gpu_autotune.argtypes = [vp, P(i), P(i), P(i)]
     L.g4gpu_set_launch_shapes.argtypes = [vp, i, i, i]
@@ -248,6 +251,40 @@ def host_gauss_hermite(par, gridmax, ngrid):
 
 def host_fc(aw, helical, h):
     return _lib().g4gpu_host_fc(aw, int(helical), h)
+
+
+class H5Writer:
+    """An HDF5 file of FP64 datasets with a "unit" attribute each (the reference's output
+    layout), written at close: w.dataset("Beam/energy", array, "mc^2")."""
+
+    def __init__(self, path):
+        self.L = _lib()
+        self.f = ctypes.c_void_p()
+        rc = self.L.g4gpu_h5_create(os.fsencode(path), ctypes.byref(self.f))
+        if rc:
+            raise G4Error(rc, f"cannot create {path}")
+
+    def dataset(self, path, data, unit=" "):
+        a = np.ascontiguousarray(data, dtype=np.float64)
+        if a.ndim == 0:
+            a = a.reshape(1)
+        dims = (ctypes.c_longlong * a.ndim)(*a.shape)
+        rc = self.L.g4gpu_h5_dataset(self.f, path.encode(), a.ndim, dims, _pd(a), unit.encode())
+        if rc:
+            raise G4Error(rc, f"h5 dataset {path}: bad path, shape or a duplicate name")
+
+    def close(self):
+        if self.f:
+            rc = self.L.g4gpu_h5_close(self.f)
+            self.f = None
+            if rc:
+                raise G4Error(rc, "h5 file could not be written")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def host_single_wakes(ns, ds, radius=2.5e-3, conductivity=0.0, relaxation=0.0, roundpipe=True, gap=0.0, lgap=1.0,

@@ -464,6 +464,19 @@ int g4gpu_host_gauss_hermite(const double *par, double gridmax, int ngrid, doubl
 /* Undulator coupling fc(h) (src/Core/Undulator.cpp:141-167). */
 double g4gpu_host_fc(double aw, int helical, int h);
 
+/* HDF5 output without the HDF5 library: the reference's .out.h5 layout (groups of FP64
+ * datasets with a string attribute "unit", Output::writeGroup / writeDataset,
+ * src/IO/Output.cpp:309-340, HDF5Base::writeBuffer, src/IO/HDF5base.cpp:74-128), written
+ * by this project's own encoder of the HDF5 file format (version 0 superblock, version 1
+ * object headers, symbol-table groups, contiguous little-endian doubles). Datasets are
+ * collected in memory; g4gpu_h5_close writes the file and releases the handle. path
+ * "Beam/energy": intermediate groups are created; at most 256 members per group. */
+typedef struct g4gpu_h5_s *g4gpu_h5;
+int g4gpu_h5_create(const char *path, g4gpu_h5 *out);
+int g4gpu_h5_dataset(g4gpu_h5 f, const char *path, int rank, const long long *dims, const double *data,
+                     const char *unit);
+int g4gpu_h5_close(g4gpu_h5 f);
+
 /* Single-particle longitudinal wakes on ns points spaced ds, for g4gpu_set_wake:
  * resistive wall (conductivity, relaxation c tau, round pipe of radius `radius` or
  * parallel plates of half gap `radius`), geometric (gaps of length gap every lgap) and

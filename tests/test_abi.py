@@ -235,3 +235,41 @@ def test_reference_demo_plugins_run_in_the_engine(lib):
         out = p.beam(part, iz=0)
     assert np.allclose(out["xstd"], part[..., 2].std(axis=1), rtol=1e-13)
     assert np.all(out["the_answer"] == 42.0)
+
+
+def test_h5_writer_round_trip(lib, tmp_path):
+    """The HDF5 encoder against a reader written from the file format specification
+    (tests/h5read.py): nested groups, groups of more than one symbol table node (8
+    entries), 1-D and 2-D datasets, an empty one, the unit attributes."""
+    import g4gpu
+    import h5read
+    rng = np.random.default_rng(0)
+    path = str(tmp_path / "x.h5")
+    want = {}
+    with g4gpu.H5Writer(path) as w:
+        for i in range(40):
+            a = rng.normal(size=(3, 5))
+            w.dataset(f"Beam/d{i:02d}", a, "m")
+            want[f"d{i:02d}"] = a
+        w.dataset("Lattice/aw", np.arange(7.0), " ")
+        w.dataset("Field3/Global/energy", np.arange(3.0), "J")
+        w.dataset("Meta/empty", np.zeros((0, 4)), "x")
+    t = h5read.read(path)
+    assert sorted(t) == ["Beam", "Field3", "Lattice", "Meta"]
+    for k, a in want.items():
+        d, attrs = t["Beam"][k]
+        assert np.array_equal(d, a) and attrs == {"unit": "m"}
+    assert np.array_equal(t["Lattice"]["aw"][0], np.arange(7.0)) and t["Lattice"]["aw"][1]["unit"] == " "
+    assert np.array_equal(t["Field3"]["Global"]["energy"][0], np.arange(3.0))
+    assert t["Meta"]["empty"][0].shape == (0, 4)
+
+
+def test_h5_writer_rejects_duplicates_and_bad_paths(lib, tmp_path):
+    import g4gpu
+    w = g4gpu.H5Writer(str(tmp_path / "y.h5"))
+    w.dataset("A/b", [1.0], "m")
+    with pytest.raises(g4gpu.G4Error):
+        w.dataset("A/b", [2.0], "m")
+    with pytest.raises(g4gpu.G4Error):
+        w.dataset("A/b/c", [2.0], "m")  # b is a dataset
+    w.close()
