@@ -12,12 +12,13 @@
 //   double, layout v3 contiguous, attribute v1 "unit": fixed-length ASCII string of the
 //   unit's length, null-terminated padding, scalar dataspace); per group: local heap
 //   (names at 8-byte offsets, "" at 0), symbol table nodes of 2K = 8 entries sorted by
-//   name, one leaf B-tree node (up to 2K = 32 children), the group's object header
-//   (one symbol-table message).
-// Group leaf node K = 4, internal node K = 16 (the library's defaults): a group holds at
-// most 256 members. The local heap's free list is empty, written as the library's end
-// marker 1. Everything is 8-byte aligned; the whole file is assembled in memory and
-// written at g4gpu_h5_close.
+//   name, B-tree nodes of up to 2K = 32 children (leaves over the symbol table nodes,
+//   then as many internal levels as the group needs), the group's object header (one
+//   symbol-table message).
+// Group leaf node K = 4, internal node K = 16 (the library's defaults). The local heap's
+// free list is empty, written as the library's end marker 1. Integer datasets are 32-bit
+// signed little-endian without attributes (HDF5Base::writeSingleNodeInt). Everything is
+// 8-byte aligned; the whole file is assembled in memory and written at g4gpu_h5_close.
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
@@ -42,6 +43,9 @@ struct Obj {
   std::map<std::string, std::unique_ptr<Obj>> members;  // sorted by name (strcmp order)
   std::vector<uint64_t> dims;
   std::vector<double> data;
+  std::vector<int32_t> idata;  // integer datasets
+  bool is_int = false;
+  bool has_unit = true;
   std::string unit;
 };
 
@@ -139,23 +143,42 @@ Buf datatype_string(uint32_t n) {
   return d;
 }
 
+// datatype message, version 1: 32-bit signed integer, little endian
+Buf datatype_int32() {
+  Buf d;
+  d.u8((1 << 4) | 0);  // version 1, fixed point
+  d.u8(0x08);          // little endian, no padding, signed
+  d.u8(0);
+  d.u8(0);
+  d.u32(4);
+  d.u16(0);   // bit offset
+  d.u16(32);  // precision
+  return d;
+}
+
 uint64_t write_dataset(Buf &f, const Obj &o) {
   f.align8();
   const uint64_t raw = f.tell();
-  for (double v : o.data) {
-    uint64_t u;
-    std::memcpy(&u, &v, 8);
-    f.u64(u);
+  size_t n = o.is_int ? o.idata.size() : o.data.size();
+  if (o.is_int) {
+    for (int32_t v : o.idata) f.u32((uint32_t)v);
+  } else {
+    for (double v : o.data) {
+      uint64_t u;
+      std::memcpy(&u, &v, 8);
+      f.u64(u);
+    }
   }
   Buf m;
   message(m, 0x0001, dataspace(o.dims));
-  message(m, 0x0003, datatype_double());
+  message(m, 0x0003, o.is_int ? datatype_int32() : datatype_double());
   Buf lay;  // layout, version 3, contiguous
   lay.u8(3);
   lay.u8(1);
-  lay.u64(o.data.empty() ? kUndef : raw);
-  lay.u64(o.data.size() * 8);
+  lay.u64(n == 0 ? kUndef : raw);
+  lay.u64(n * (o.is_int ? 4 : 8));
   message(m, 0x0008, lay);
+  if (!o.has_unit) return object_header(f, m, 3);
   // attribute "unit", version 1
   const std::string unit = o.unit.empty() ? std::string(" ") : o.unit;
   const Buf dt = datatype_string((uint32_t)unit.size()), ds = dataspace({});
@@ -195,11 +218,7 @@ GroupAddr write_group(Buf &f, const Obj &g, std::string &err) {
     kids.push_back({kv.first, a});
   }
   const size_t n = kids.size();
-  const size_t nsnod = std::max<size_t>(1, (n + 2 * kLeafK - 1) / (2 * kLeafK));
-  if (nsnod > 2 * (size_t)kInternalK) {
-    err = "a group holds at most 256 members";
-    return {};
-  }
+  const size_t nsnod = n ? (n + 2 * kLeafK - 1) / (2 * kLeafK) : 0;
   // local heap: "" at offset 0, then the names
   Buf seg;
   seg.zeros(8);
@@ -218,11 +237,12 @@ GroupAddr write_group(Buf &f, const Obj &g, std::string &err) {
   f.u64(1);  // free list: none (the library's end marker)
   f.u64(heap + 32);
   f.bytes(seg.b.data(), seg.tell());
-  // symbol table nodes of up to 8 sorted entries
-  std::vector<uint64_t> snod(nsnod);
+  // symbol table nodes of up to 8 sorted entries; each child of a B-tree node carries
+  // the heap offset of the last (largest) name below it as its right key
+  std::vector<std::pair<uint64_t, uint64_t>> level;  // (address, offset of its last name)
   for (size_t s = 0; s < nsnod; s++) {
     f.align8();
-    snod[s] = f.tell();
+    const uint64_t at = f.tell();
     const size_t i0 = s * 2 * kLeafK, i1 = std::min(n, i0 + 2 * kLeafK);
     f.bytes("SNOD", 4);
     f.u8(1);
@@ -238,23 +258,37 @@ GroupAddr write_group(Buf &f, const Obj &g, std::string &err) {
       f.u64(grp ? kids[i].second.heap : 0);
     }
     f.zeros(kSnodSize - 8 - (i1 - i0) * kEntry);
+    level.push_back({at, off[i1 - 1]});
   }
-  // one leaf B-tree node: key 0 (""), child, key (last name of the child), ...
-  f.align8();
-  const uint64_t tree = f.tell();
-  f.bytes("TREE", 4);
-  f.u8(0);  // group node
-  f.u8(0);  // leaf
-  f.u16(n ? (unsigned)nsnod : 0);
-  f.u64(kUndef);
-  f.u64(kUndef);
-  f.u64(0);
-  for (size_t s = 0; s < (n ? nsnod : 0); s++) {
-    f.u64(snod[s]);
-    const size_t last = std::min(n, (s + 1) * 2 * kLeafK) - 1;
-    f.u64(off[last]);
-  }
-  f.zeros(kTreeSize - (f.tell() - tree));
+  // B-tree nodes, leaves first (level 0 over the symbol table nodes), up the levels until
+  // one node remains: key 0 (""), child, key, child, ..., key
+  uint64_t tree = 0;
+  int depth = 0;
+  do {
+    std::vector<std::pair<uint64_t, uint64_t>> up;
+    const size_t nnode = std::max<size_t>(1, (level.size() + 2 * kInternalK - 1) / (2 * kInternalK));
+    for (size_t b = 0; b < nnode; b++) {
+      const size_t c0 = b * 2 * kInternalK, c1 = std::min(level.size(), c0 + 2 * kInternalK);
+      f.align8();
+      const uint64_t at = f.tell();
+      f.bytes("TREE", 4);
+      f.u8(0);  // group node
+      f.u8((unsigned)depth);
+      f.u16((unsigned)(c1 - c0));
+      f.u64(kUndef);  // siblings: readers of symbol tables follow the children only
+      f.u64(kUndef);
+      f.u64(0);
+      for (size_t c = c0; c < c1; c++) {
+        f.u64(level[c].first);
+        f.u64(level[c].second);
+      }
+      f.zeros(kTreeSize - (f.tell() - at));
+      up.push_back({at, c1 > c0 ? level[c1 - 1].second : 0});
+    }
+    level.swap(up);
+    tree = level[0].first;
+    depth++;
+  } while (level.size() > 1);
   // the group's object header: one symbol table message
   Buf st;
   st.u64(tree);
@@ -310,6 +344,29 @@ int g4gpu_h5_dataset(g4gpu_h5 f, const char *path, int rank, const long long *di
   o->data.assign(data, data + n);
   o->unit = unit ? unit : "";
   g->members.emplace(p, std::move(o));
+  return G4GPU_OK;
+}
+
+int g4gpu_h5_dataset_int(g4gpu_h5 f, const char *path, int n, const int *data) {
+  if (!f || !path || n < 0 || (n > 0 && !data)) return G4GPU_ERR_ARG;
+  const long long dims[1] = {n};
+  // placed like a double dataset, then retyped
+  std::vector<double> tmp((size_t)n, 0.0);
+  int rc = g4gpu_h5_dataset(f, path, 1, dims, tmp.data(), nullptr);
+  if (rc) return rc;
+  std::string p(path);
+  Obj *g = &f->root;
+  size_t pos;
+  while ((pos = p.find('/')) != std::string::npos) {
+    const std::string part = p.substr(0, pos);
+    p = p.substr(pos + 1);
+    if (!part.empty()) g = g->members.at(part).get();
+  }
+  Obj &o = *g->members.at(p);
+  o.is_int = true;
+  o.has_unit = false;
+  o.data.clear();
+  o.idata.assign(data, data + n);
   return G4GPU_OK;
 }
 

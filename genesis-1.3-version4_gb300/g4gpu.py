@@ -56,7 +56,8 @@ ABI_SYMBOLS = [
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
     "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc", "g4gpu_host_single_wakes",
     "g4gpu_set_wake", "g4gpu_set_chicanes", "g4gpu_load_beam_counts", "g4gpu_get_counts", "g4gpu_sort",
-    "g4gpu_apply_slippage", "g4gpu_set_incoherent", "g4gpu_h5_create", "g4gpu_h5_dataset", "g4gpu_h5_close",
+    "g4gpu_apply_slippage", "g4gpu_set_incoherent", "g4gpu_h5_create", "g4gpu_h5_dataset", "g4gpu_h5_dataset_int",
+    "g4gpu_h5_close",
     "g4gpu_set_graph_mode", "g4gpu_autotune", "g4gpu_batch_create", "g4gpu_batch_destroy",
     "g4gpu_batch_member", "g4gpu_batch_run", "g4gpu_batch_synchronize",
     "g4gpu_mlp_create", "g4gpu_mlp_destroy", "g4gpu_mlp_last_error", "g4gpu_mlp_num_params",
@@ -174,6 +175,7 @@ def load_library(path=None):
     L.g4gpu_set_incoherent.argtypes = [vp, i, i, i, i]
     L.g4gpu_h5_create.argtypes = [ctypes.c_char_p, P(vp)]
     L.g4gpu_h5_dataset.argtypes = [vp, ctypes.c_char_p, i, P(ctypes.c_longlong), pd, ctypes.c_char_p]
+    L.g4gpu_h5_dataset_int.argtypes = [vp, ctypes.c_char_p, i, P(i)]
     L.g4gpu_h5_close.argtypes = [vp]
     L.g4gpu_set_graph_mode.argtypes = [vp, i]
     L.g4gpu_autotune.argtypes = [vp, P(i), P(i), P(i)]
@@ -272,6 +274,12 @@ class H5Writer:
         rc = self.L.g4gpu_h5_dataset(self.f, path.encode(), a.ndim, dims, _pd(a), unit.encode())
         if rc:
             raise G4Error(rc, f"h5 dataset {path}: bad path, shape or a duplicate name")
+
+    def dataset_int(self, path, data):
+        a = np.ascontiguousarray(data, dtype=np.int32).ravel()
+        rc = self.L.g4gpu_h5_dataset_int(self.f, path.encode(), a.size, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+        if rc:
+            raise G4Error(rc, f"h5 dataset {path}: bad path or a duplicate name")
 
     def close(self):
         if self.f:

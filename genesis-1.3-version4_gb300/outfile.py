@@ -123,3 +123,59 @@ _LAT = ["aw", "ax", "ay", "ku", "kx", "ky", "gradx", "grady", "qf", "qx", "qy", 
 
 def _lat_col(name):
     return _LAT.index(name)
+
+
+def write_fld(path, cfg, ifld, field, first, s0=0.0):
+    """The reference's field dump (.fld.h5, WriteFieldHDF5::writeMain,
+    src/IO/writeFieldHDF5.cpp:42-130): Meta/Version, wavelength, slicespacing, refposition,
+    gridsize (m), gridpoints and slicecount (int), and per slice in window order
+    sliceNNNNNN/field-real and field-imag, the field scaled by dgrid eev / ks / sqrt(vacimp)
+    (sqrt(W) per cell). field [nslice][ngrid^2] complex in storage order with ring start
+    `first` (g4gpu_get_field)."""
+    ns, ng = cfg.nslice, cfg.ngrid
+    h = int(cfg.harm[ifld])
+    xlambda = cfg.lambda0 / h
+    dgrid = 2 * cfg.gridmax[ifld] / (ng - 1)
+    ks = 4.0 * np.arcsin(1.0) / xlambda
+    scl = dgrid * 510998.95069 / ks / np.sqrt(376.73)
+    f = np.asarray(field).reshape(ns, ng * ng)
+    with g4gpu.H5Writer(path) as w:
+        for name, v in (("Major", 4), ("Minor", 6), ("Revision", 14), ("Beta", 0)):
+            w.dataset(f"Meta/Version/{name}", [float(v)], " ")
+        w.dataset("wavelength", [xlambda], "m")
+        w.dataset("slicespacing", [cfg.lambda0 * cfg.sample], "m")
+        w.dataset("refposition", [s0], "m")
+        w.dataset("gridsize", [dgrid], "m")
+        w.dataset_int("gridpoints", [ng])
+        w.dataset_int("slicecount", [ns])
+        for i in range(ns):
+            s = f[(i + int(first)) % ns]
+            w.dataset(f"slice{i + 1:06d}/field-real", scl * s.real, " ")
+            w.dataset(f"slice{i + 1:06d}/field-imag", scl * s.imag, " ")
+
+
+def write_par(path, cfg, particles, current, nbins, counts=None, s0=0.0):
+    """The reference's particle dump (.par.h5, WriteBeamHDF5::writeMain,
+    src/IO/writeBeamHDF5.cpp:14-188): Meta/Version, slicelength (the reference length),
+    slicespacing, refposition (m), beamletsize, slicecount, one4one (int), and per slice
+    sliceNNNNNN/current (A), gamma, theta (rad), x, y (m), px, py (rad). particles
+    [nslice][npart][6] (g4gpu_get_beam), counts per slice for one4one windows."""
+    ns = cfg.nslice
+    p = np.asarray(particles).reshape(ns, -1, 6)
+    cur = np.asarray(current, dtype=np.float64)
+    with g4gpu.H5Writer(path) as w:
+        for name, v in (("Major", 4), ("Minor", 6), ("Revision", 14), ("Beta", 0)):
+            w.dataset(f"Meta/Version/{name}", [float(v)], " ")
+        w.dataset("slicelength", [cfg.lambda0], "m")
+        w.dataset("slicespacing", [cfg.lambda0 * cfg.sample], "m")
+        w.dataset("refposition", [s0], "m")
+        w.dataset_int("beamletsize", [nbins])
+        w.dataset_int("slicecount", [ns])
+        w.dataset_int("one4one", [1 if counts is not None else 0])
+        for i in range(ns):
+            n = p.shape[1] if counts is None else int(counts[i])
+            g = f"slice{i + 1:06d}"
+            w.dataset(f"{g}/current", [cur[i]], "A")
+            for c, (name, unit) in enumerate((("gamma", " "), ("theta", "rad"), ("x", "m"), ("y", "m"),
+                                               ("px", "rad"), ("py", "rad"))):
+                w.dataset(f"{g}/{name}", p[i, :n, c], unit)

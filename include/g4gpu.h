@@ -475,6 +475,8 @@ typedef struct g4gpu_h5_s *g4gpu_h5;
 int g4gpu_h5_create(const char *path, g4gpu_h5 *out);
 int g4gpu_h5_dataset(g4gpu_h5 f, const char *path, int rank, const long long *dims, const double *data,
                      const char *unit);
+/* A 1-D dataset of 32-bit integers without attributes (HDF5Base::writeSingleNodeInt). */
+int g4gpu_h5_dataset_int(g4gpu_h5 f, const char *path, int n, const int *data);
 int g4gpu_h5_close(g4gpu_h5 f);
 
 /* Single-particle longitudinal wakes on ns points spaced ds, for g4gpu_set_wake:

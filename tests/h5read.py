@@ -78,6 +78,10 @@ class H5File:
             return ("f8", size)
         if cls == 3:
             return ("str", size)
+        if cls == 0:  # fixed point
+            if m[1] & 1 or size != 4 or not (m[1] & 8):
+                raise H5Error("only little-endian signed 4-byte integers")
+            return ("i4", size)
         raise H5Error(f"datatype class {cls}")
 
     def attribute(self, m):
@@ -120,6 +124,35 @@ class H5File:
         if level == 0:
             return kids
         return [s for k in kids for s in self.btree_children(k)]
+
+    def find(self, header, name):
+        """The member `name` of a group found as the HDF5 library finds it: down the
+        B-tree by its keys (child i holds the names in (key i, key i+1]), then a search
+        of the symbol table node. Returns the member's object header address."""
+        st = [m for t, m in self.messages(header) if t == 0x0011][0]
+        tree, heap = struct.unpack_from("<QQ", st, 0)
+        names = self.heap(heap)
+        key = lambda off: names[off:names.index(b"\x00", off)].decode()
+        b, node = self.b, tree
+        while True:
+            level, used = b[node + 5], struct.unpack_from("<H", b, node + 6)[0]
+            keys = [key(struct.unpack_from("<Q", b, node + 24 + 16 * i)[0]) for i in range(used + 1)]
+            kids = [struct.unpack_from("<Q", b, node + 32 + 16 * i)[0] for i in range(used)]
+            for i in range(used):
+                if keys[i] != keys[i + 1] and not keys[i] < keys[i + 1]:
+                    raise H5Error("B-tree keys out of order")
+            i = next((i for i in range(used) if keys[i] < name <= keys[i + 1]), None)
+            if i is None:
+                raise KeyError(name)
+            if level == 0:
+                snod = kids[i]
+                n = struct.unpack_from("<H", b, snod + 6)[0]
+                for j in range(n):
+                    noff, oh = struct.unpack_from("<QQ", b, snod + 8 + 40 * j)
+                    if key(noff) == name:
+                        return oh
+                raise KeyError(name)
+            node = kids[i]
 
     def group(self, header):
         msgs = self.messages(header)
@@ -171,9 +204,11 @@ class H5File:
             raise H5Error("a dataset without dataspace, datatype or layout")
         addr, size = layout
         n = int(np.prod(dims))
-        if size != 8 * n:
+        item = 4 if dtype[0] == "i4" else 8
+        if size != item * n:
             raise H5Error("layout size does not match the dataspace")
-        data = np.frombuffer(self.b, "<f8", count=n, offset=addr).reshape(dims) if n else np.zeros(dims)
+        fmt = "<i4" if dtype[0] == "i4" else "<f8"
+        data = np.frombuffer(self.b, fmt, count=n, offset=addr).reshape(dims) if n else np.zeros(dims)
         return data, attrs
 
     def tree(self):
@@ -183,3 +218,12 @@ class H5File:
 def read(path):
     """{name: subtree or (array, {attribute: value})}"""
     return H5File(path).tree()
+
+
+def get(path, name):
+    """One object by its path ("Beam/energy"), found through the groups' B-tree keys."""
+    f = H5File(path)
+    h = f.root_header
+    for part in name.strip("/").split("/"):
+        h = f.find(h, part)
+    return f.obj(h)

@@ -262,6 +262,38 @@ def test_h5_writer_round_trip(lib, tmp_path):
     assert np.array_equal(t["Lattice"]["aw"][0], np.arange(7.0)) and t["Lattice"]["aw"][1]["unit"] == " "
     assert np.array_equal(t["Field3"]["Global"]["energy"][0], np.arange(3.0))
     assert t["Meta"]["empty"][0].shape == (0, 4)
+    # lookups by name through the B-tree keys, as the HDF5 library finds members
+    for k, a in want.items():
+        assert np.array_equal(h5read.get(path, f"Beam/{k}")[0], a)
+    with pytest.raises(KeyError):
+        h5read.get(path, "Beam/nothing")
+
+
+def test_h5_writer_groups_of_thousands(lib, tmp_path):
+    """A dump of 3000 slices: the root group's B-tree takes an internal level above its
+    leaves; every slice is found by name; integer datasets."""
+    import g4gpu
+    import h5read
+    import outfile
+    ns, ng = 3000, 5
+    cfg = g4gpu.Config(nslice=ns, npart=8, ngrid=ng, gridmax=1e-4, lambda0=1e-10, sample=1.0, gammaref=1e4)
+    rng = np.random.default_rng(0)
+    fld = rng.normal(size=(ns, ng * ng)) + 1j * rng.normal(size=(ns, ng * ng))
+    path = str(tmp_path / "a.fld.h5")
+    outfile.write_fld(path, cfg, 0, fld, 7)
+    t = h5read.read(path)
+    assert len(t) == ns + 7 and t["gridpoints"][0].tolist() == [ng] and t["slicecount"][0].tolist() == [ns]
+    scl = (2e-4 / (ng - 1)) * 510998.95069 / (2 * np.pi / 1e-10) / np.sqrt(376.73)
+    for i in (0, 1, 777, 2999):
+        got = h5read.get(path, f"slice{i + 1:06d}/field-imag")[0]
+        assert np.allclose(got, scl * fld[(i + 7) % ns].imag, rtol=1e-15)
+    part = rng.normal(size=(4, 8, 6))
+    path = str(tmp_path / "a.par.h5")
+    cfg4 = g4gpu.Config(nslice=4, npart=8, ngrid=ng, gridmax=1e-4, lambda0=1e-10, sample=1.0, gammaref=1e4)
+    outfile.write_par(path, cfg4, part, np.arange(4.0), 4, counts=[8, 5, 0, 3])
+    assert h5read.get(path, "one4one")[0].tolist() == [1]
+    assert np.array_equal(h5read.get(path, "slice000002/theta")[0], part[1, :5, 1])
+    assert h5read.get(path, "slice000003/x")[0].shape == (0,)
 
 
 def test_h5_writer_rejects_duplicates_and_bad_paths(lib, tmp_path):
