@@ -1640,8 +1640,10 @@ static int backup_state(g4gpu_handle h, StateBackup &b) {
       {h->beam.gamma, np * h->rsize}, {h->beam.theta, np * 8}, {h->beam.x, np * h->rsize},
       {h->beam.y, np * h->rsize},     {h->beam.px, np * h->rsize}, {h->beam.py, np * h->rsize}};
   for (int k = 0; k < c.nfield; k++) live.push_back({h->field[k], nf});
-  // the radial grid extent of the space charge, carried from step to step
+  // the radial grid extent of the space charge, carried from step to step, and the
+  // incoherent radiation's counter of drawing steps: the trial steps leave neither moved
   if (h->sc.state) live.push_back({h->sc.state, 2 * sizeof(double)});
+  if (h->isr_ctr) live.push_back({h->isr_ctr, sizeof(unsigned long long)});
   for (auto &l : live) {
     void *cp = nullptr;
     cudaError_t e = cudaMalloc(&cp, l.second);

@@ -105,3 +105,25 @@ def test_stream_advances_and_restarts(lib):
         c = h.get_beam()
     assert not np.array_equal(a[..., 0], b[..., 0])
     assert np.array_equal(a, c)
+
+
+def test_autotune_leaves_the_stream_where_it_was(lib):
+    """The autotuner's trial steps restore the beam, the fields and the random stream:
+    a run after it draws what a run without it draws."""
+    import g4gpu
+    d = golden("incoherent.npz")
+    part, lat = d["spread_part"], d["spread_lat"]
+    out = []
+    for tune in (False, True):
+        cfg = g4gpu.Config(nslice=part.shape[0], npart=part.shape[1], ngrid=25, gridmax=6e-5, lambda0=1e-10,
+                           sample=1.0, gammaref=11357.8, precision=1, time_run=1)
+        with g4gpu.Handle(cfg) as h:
+            h.set_lattice(lat)
+            h.load_beam(part, d["cur"])
+            h.load_field(0, d["fields"][0])
+            h.set_incoherent(5, True, True, 4)
+            if tune:
+                h.autotune()
+            h.run(0, lat.shape[0])
+            out.append(h.get_beam())
+    assert np.array_equal(out[0], out[1])
