@@ -126,4 +126,7 @@ def test_autotune_leaves_the_stream_where_it_was(lib):
                 h.autotune()
             h.run(0, lat.shape[0])
             out.append(h.get_beam())
-    assert np.array_equal(out[0], out[1])
+    # the same draws (a moved stream changes gamma by up to the spread, ~0.02 here); the
+    # deposition's atomics may still order sums differently between runs
+    avg, sig = expected(lat[0])
+    assert np.abs(out[0][..., 0] - out[1][..., 0]).max() < 1e-3 * sig
