@@ -22,6 +22,8 @@
 // paired FP32 instructions (both lanes of a float2 in one instruction).
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "g4gpu_internal.h"
 
 namespace g4 {
@@ -669,14 +671,14 @@ void launch_fft(void *stream, void *field, const void *src, void *work, const vo
   cudaStream_t s = (cudaStream_t)stream;
   const int n = pl.n;
   const int es = (int)sizeof(T2);
-  static unsigned long long configured = 0;
+  static std::atomic<unsigned long long> configured{0};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 64 && !(configured & (1ull << dev))) {
+  if (dev < 64 && !(configured.load() & (1ull << dev))) {
     cudaFuncSetAttribute(k_fft_rows<T2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_fft_rows<T2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_fft_cols<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    configured |= 1ull << dev;
+    configured.fetch_or(1ull << dev);
   }
   const int nsm = sm_count();
   const int rows_ctas = es == 8 ? FFT_CTAS_FP32 : FFT_CTAS_FP64, cols_ctas = rows_ctas;
@@ -718,14 +720,14 @@ void launch_fft_diag_t(void *stream, const void *field, void *work, const void *
   cudaStream_t s = (cudaStream_t)stream;
   const int n = pl.n;
   const int es = (int)sizeof(T2);
-  static unsigned long long configured = 0;
+  static std::atomic<unsigned long long> configured{0};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 64 && !(configured & (1ull << dev))) {
+  if (dev < 64 && !(configured.load() & (1ull << dev))) {
     cudaFuncSetAttribute(k_fft_rows<T2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     // (the kernel's static reduction array counts against the 227 KB too)
     cudaFuncSetAttribute(k_fft_cols_moments<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 226 * 1024);
-    configured |= 1ull << dev;
+    configured.fetch_or(1ull << dev);
   }
   const int ctas = es == 8 ? FFT_CTAS_FP32 : FFT_CTAS_FP64;
   const long long nsm = sm_count();

@@ -24,6 +24,8 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <cmath>
 #include <cstdint>
 #include <mutex>
@@ -1984,13 +1986,13 @@ void launch_adi_mixed(const Launch &L, const StepConstF &sc, int k, int phase, v
   const int R = tiled::band_rows(ngrid, sizeof(float2)), Cw = tiled::band_cols(ngrid, sizeof(float2));
   const size_t smx = (size_t)(2 * R + 2) * ngrid * sizeof(float2), smy = (size_t)ngrid * Cw * sizeof(float2);
   if (smx <= 227u * 1024u && smy <= 227u * 1024u) {
-    static unsigned long long configured = 0;  // one bit per device
+    static std::atomic<unsigned long long> configured{0};  // one bit per device
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev < 64 && !(configured & (1ull << dev))) {
+    if (dev < 64 && !(configured.load() & (1ull << dev))) {
       cudaFuncSetAttribute(tiled::k_adi_xt<MixedOps, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
       cudaFuncSetAttribute(tiled::k_adi_yt<MixedOps, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-      configured |= 1ull << dev;
+      configured.fetch_or(1ull << dev);
     }
     tiled::CoefP<MixedOps> cf{cb, cb + ngrid, cb + 2 * ngrid};
     const int W = sc.f[k].tw;
@@ -2058,14 +2060,14 @@ int fused_max_ngrid() {
 void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b,
                               void *field, const void *coef, int ns, int np, int ngrid, int deposit,
                               int threads, double *dbeam, double *dfield, int nharm, double gref) {
-  static unsigned long long configured = 0;  // one bit per device
+  static std::atomic<unsigned long long> configured{0};  // one bit per device
   threads = fused_threads(ngrid, threads);
   size_t smem = (dbeam || dfield) ? fused_diag_smem_bytes(ngrid, threads) : fused_smem_bytes(ngrid);
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 64 && !(configured & (1ull << dev))) {
+  if (dev < 64 && !(configured.load() & (1ull << dev))) {
     cudaFuncSetAttribute(k_field_fused_f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    configured |= 1ull << dev;
+    configured.fetch_or(1ull << dev);
   }
   PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
   k_field_fused_f<<<ns, threads, smem, (cudaStream_t)L.stream>>>(
@@ -2080,12 +2082,12 @@ int pair_max_ngrid() {
 
 void launch_field_pair_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b, void *field,
                              const void *coef, int ns, int np, int ngrid, int deposit) {
-  static unsigned long long configured = 0;  // one bit per device
+  static std::atomic<unsigned long long> configured{0};  // one bit per device
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 64 && !(configured & (1ull << dev))) {
+  if (dev < 64 && !(configured.load() & (1ull << dev))) {
     cudaFuncSetAttribute(k_field_pair_f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    configured |= 1ull << dev;
+    configured.fetch_or(1ull << dev);
   }
   PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
   k_field_pair_f<<<2 * ns, kPairThreads, pair_smem_bytes(ngrid), (cudaStream_t)L.stream>>>(

@@ -31,6 +31,8 @@
 // (FP32 form) as floats the size and scl * current / size of every slice.
 #pragma once
 
+#include <atomic>
+
 namespace g4 {
 namespace {
 
@@ -462,12 +464,12 @@ __global__ void __launch_bounds__(kScThreads) k_sc_field(ScBeam<F> b, double *st
 template <class F>
 void sc_launch(const Launch &L, const ScConst &c, const typename F::Step &step, ScBeam<F> sb,
                const ScBuffers &buf, int part) {
-  static unsigned long long configured = 0;
+  static std::atomic<unsigned long long> configured{0};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 64 && !(configured & (1ull << dev))) {
+  if (dev < 64 && !(configured.load() & (1ull << dev))) {
     cudaFuncSetAttribute(k_sc_field<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc_max_smem());
-    configured |= 1ull << dev;
+    configured.fetch_or(1ull << dev);
   }
   cudaStream_t s = (cudaStream_t)L.stream;
   if (part == 0) {
