@@ -164,3 +164,52 @@ def test_apply_slippage_outside_the_step(lib, periodic, time_run, slip):
             want_first = last if direction > 0 else (last + 1) % ns
     assert first == want_first and abs(acc - want_acc) < 1e-12
     assert np.array_equal(f, want)
+
+
+def test_one4one_with_wakes_and_radiation_loss_matches_oracle(lib, oracle):
+    """A one4one window with wakes (formed again from the currents each sort leaves) and
+    the incoherent radiation loss (one draw per particle, none here: loss only), sorted
+    every step: plain path against the oracle."""
+    import g4gpu
+    g = fixture("every")
+    gammaref, time_run, periodic, every = g("args")
+    part, fields, lat = g("part"), g("fields"), g("lat")
+    ns, cap = part.shape[0], part.shape[1]
+    res, geo, rou = g4gpu.host_single_wakes(ns, 1e-10, radius=2e-3, conductivity=5.813e7, relaxation=8.1e-6,
+                                            gap=1e-3, lgap=0.5, hrough=1e-7, lrough=1e-4)
+    res, geo, rou = res * 1e2, geo * 30.0, rou * 1e3
+    ext = np.linspace(-500.0, 500.0, ns)
+    oracle.set_counts(g("counts"), 1)
+    oracle.set_wake(ext, res, geo, rou, 1e-10)
+    oracle.set_incoherent(3, True, False, 4)
+    try:
+        rp, rf, rfirst, _ = oracle.run_steps(lat, gammaref, part, g("cur"), 1e-10, 1.0, g("harm"), g("gridmax"),
+                                             fields, g("first"), time_run=int(time_run), periodic=int(periodic))
+        rc = oracle.get_counts(ns)
+    finally:
+        oracle.set_counts()
+        oracle.set_wake()
+        oracle.set_incoherent()
+    cfg = g4gpu.Config(nslice=ns, npart=cap, ngrid=25, harm=list(g("harm")), gridmax=list(g("gridmax")),
+                       lambda0=1e-10, sample=1.0, gammaref=float(gammaref), time_run=int(time_run),
+                       periodic=int(periodic))
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam_counts(part, g("cur"), g("counts"))
+        h.load_field(0, fields[0], first=int(g("first")[0]))
+        h.set_wake(ext, res, geo, rou)
+        h.set_incoherent(3, True, False, 4)
+        for i in range(lat.shape[0]):
+            h.run(i, 1, g4gpu.STAGE_PUSH)
+            h.sort()
+            h.run(i, 1, g4gpu.STAGE_FIELD | g4gpu.STAGE_SLIP)
+        p, counts = h.get_beam(), h.get_counts()
+        f, first, _ = h.get_field(0)
+    assert np.array_equal(counts, rc)
+    got = np.concatenate([by_phase(p[i], n) for i, n in enumerate(counts)])
+    want = np.concatenate([by_phase(rp[i], n) for i, n in enumerate(rc)])
+    got[:, 0] -= gammaref
+    want[:, 0] -= gammaref
+    for col in range(6):
+        assert np.abs(got[:, col] - want[:, col]).max() <= 1e-9 * np.abs(want[:, col]).max(), col
+    assert np.abs(f - rf[0]).max() <= 1e-9 * np.abs(rf[0]).max() and first == int(rfirst[0])
