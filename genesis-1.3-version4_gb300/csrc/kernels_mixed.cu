@@ -1243,20 +1243,21 @@ struct KahanF {
 // All NS sums and NX min/max pairs of a block in one pass: every warp reduces its
 // lanes' values with shuffles, lane 0 stores them, and after one barrier thread k
 // combines value k over the warps (sums in FP64). Thread 0..NS-1 return their sum in
-// *sum, threads NS..NS+2NX-1 their minimum or maximum in *ext.
+// *sum, threads NS..NS+2NX-1 their minimum or maximum in *ext. The lanes' compensated
+// sums enter as FP32 pairs (s, -c): no FP64 arithmetic before lane 0's store.
 template <int BS, int NS, int NX>
-__device__ __forceinline__ void block_reduce_all(const double *s, const float *mn, const float *mx, double *sh,
+__device__ __forceinline__ void block_reduce_all(const KahanF *s, const float *mn, const float *mx, double *sh,
                                                  double *out) {
   constexpr int NW = BS / 32, NV = NS + 2 * NX;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // within a warp as an unevaluated pair of FP32 numbers (hi + lo, hi the FP32
-  // rounding of the lane's FP64 sum), added level by level with the exact rounding
+  // within a warp as an unevaluated pair of FP32 numbers (hi + lo: the lane's Kahan
+  // sum and its negated compensation), added level by level with the exact rounding
   // error of hi's sum (Knuth's TwoSum) carried into lo: FP32 shuffles and adds instead
   // of FP64 ones, which run at 1/64 of the FP32 rate, to about 44 bits
 #pragma unroll
   for (int k = 0; k < NS; k++) {
-    float hi = (float)s[k];
-    float lo = (float)(s[k] - (double)hi);
+    float hi = s[k].s;
+    float lo = -s[k].c;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const float oh = __shfl_down_sync(0xffffffffu, hi, o), ol = __shfl_down_sync(0xffffffffu, lo, o);
@@ -1344,10 +1345,7 @@ __global__ void __launch_bounds__(BS) k_diag_beam_f(PtrsF p, double gref, int np
       }
     }
   }
-  double s[NSUM];
-#pragma unroll
-  for (int k = 0; k < NSUM; k++) s[k] = c[k].value();
-  block_reduce_all<BS, NSUM, 5>(s, mn, mx, sh, res);
+  block_reduce_all<BS, NSUM, 5>(c, mn, mx, sh, res);
   __syncthreads();
   const int w = beam_diag_width(nharm);
   double *o = out + (size_t)is * w;
@@ -1386,10 +1384,7 @@ __global__ void __launch_bounds__(BS) k_diag_field_f(const float2 *field, int ng
       row++;
     }
   }
-  double S[kFieldSums];
-#pragma unroll
-  for (int k = 0; k < kFieldSums; k++) S[k] = c[k].value();
-  block_reduce_all<BS, kFieldSums, 0>(S, nullptr, nullptr, sh, res);
+  block_reduce_all<BS, kFieldSums, 0>(c, nullptr, nullptr, sh, res);
   __syncthreads();
   double *o = out + (size_t)is0 * (kFieldSums + 2);
   if (threadIdx.x < kFieldSums) o[threadIdx.x] = res[threadIdx.x];
