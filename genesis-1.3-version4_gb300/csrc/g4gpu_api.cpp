@@ -1545,6 +1545,15 @@ int g4gpu_run_diag(g4gpu_handle h, int istep0, int nsteps, int nharm, double *be
   int rc = diag_buffers(h, (size_t)nsteps * rec * sizeof(double));
   if (rc) return rc;
   std::vector<int> firsts((size_t)nsteps * G4GPU_MAX_FIELDS);
+  // each step's record is copied back as soon as it is formed and finished on the host
+  // while the device runs the later steps
+  struct Events {
+    std::vector<cudaEvent_t> ev;
+    ~Events() {
+      for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    }
+  } done;
+  done.ev.reserve(nsteps);
   for (int s = 0; s < nsteps; s++) {
     // the fused field kernel forms the fields' record during the step where it can
     // (the slice is in its shared memory); the beam's, and the fields' elsewhere, come
@@ -1559,16 +1568,23 @@ int g4gpu_run_diag(g4gpu_handle h, int istep0, int nsteps, int nharm, double *be
     if (rc) return rc;
     for (int k = 0; k < c.nfield; k++) firsts[(size_t)s * G4GPU_MAX_FIELDS + k] = h->first[k];
     enqueue_diag(h, nharm, h->ddiag + (size_t)s * rec, beam_out != nullptr, field_out != nullptr && !fields_done);
+    G4_CUDA(h, cudaGetLastError());
+    G4_CUDA(h, cudaMemcpyAsync(h->hdiag + (size_t)s * rec, h->ddiag + (size_t)s * rec, rec * sizeof(double),
+                               cudaMemcpyDeviceToHost, h->stream));
+    cudaEvent_t e;
+    G4_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    done.ev.push_back(e);
+    G4_CUDA(h, cudaEventRecord(e, h->stream));
   }
-  G4_CUDA(h, cudaGetLastError());
-  G4_CUDA(h, cudaMemcpyAsync(h->hdiag, h->ddiag, (size_t)nsteps * rec * sizeof(double), cudaMemcpyDeviceToHost,
-                             h->stream));
-  if ((rc = check_device_flag(h))) return rc;
   const size_t bstride = (size_t)c.nslice * (G4GPU_DB_NCOL + 2 * nharm);
   const size_t fstride = (size_t)c.nfield * c.nslice * G4GPU_DF_NCOL;
-  for (int s = 0; s < nsteps; s++)
+  for (int s = 0; s < nsteps; s++) {
+    G4_CUDA(h, cudaEventSynchronize(done.ev[s]));
     finish_diag(h, h->hdiag + (size_t)s * rec, nharm, &firsts[(size_t)s * G4GPU_MAX_FIELDS],
                 beam_out ? beam_out + s * bstride : nullptr, field_out ? field_out + s * fstride : nullptr);
+  }
+  // a device error raised by any step fails the call (its records are then not trusted)
+  if ((rc = check_device_flag(h))) return rc;
   return G4GPU_OK;
 }
 
