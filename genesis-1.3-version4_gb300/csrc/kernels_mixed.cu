@@ -1237,7 +1237,6 @@ struct KahanF {
     c = (t - s) - y;
     s = t;
   }
-  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
 // All NS sums and NX min/max pairs of a block in one pass: every warp reduces its

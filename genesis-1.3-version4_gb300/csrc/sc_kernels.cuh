@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(kScThreads) k_sc_field(ScBeam<F> b, double *st
       R2 z;
       sc_particle<F>(xs[ipc], ys[ipc], xc, yc, dr, ng, idx, z);
       const unsigned full = 0xffffffffu;
-      const int key = valid ? idx : -1 - (threadIdx.x & 31);  // lanes without a particle match no one
+      const int key = valid ? idx : -1 - (int)(threadIdx.x & 31);  // lanes without a particle match no one
       const int key1 = __shfl_xor_sync(full, key, 1), key2 = __shfl_xor_sync(full, key, 2),
                 key4 = __shfl_xor_sync(full, key, 4);
       const bool g1 = key == key1;
