@@ -299,11 +299,13 @@ int g4gpu_diag_global(const g4gpu_config *cfg, int nharm, const double *current,
 /* Runs steps istep0 .. istep0+nsteps-1 (all stages, as g4gpu_run) and records after
  * every step the per-slice diagnostics g4gpu_diag would return at that point:
  * beam_out [nsteps][nslice][G4GPU_DB_NCOL + 2*nharm], field_out
- * [nsteps][nfield][nslice][G4GPU_DF_NCOL] (either may be NULL). The records stay on
- * the device until the last step and are read back and finished once, as the
- * reference keeps them in memory (Diagnostic::calc after every output step in
- * Gencore::run, src/Core/Gencore.cpp:102-160; written by Output::writeGroup at the
- * end). Synchronous: returns when the steps and the read-back are done. */
+ * [nsteps][nfield][nslice][G4GPU_DF_NCOL] (either may be NULL). Each step's record is
+ * formed on the device, copied back as soon as it is complete and finished on the
+ * host while the device runs the later steps; the reference keeps them in memory the
+ * same way (Diagnostic::calc after every output step in Gencore::run,
+ * src/Core/Gencore.cpp:102-160; written by Output::writeGroup at the end).
+ * Synchronous: returns when the steps and all records are done; a device error raised
+ * during any step fails the call. */
 int g4gpu_run_diag(g4gpu_handle h, int istep0, int nsteps, int nharm, double *beam_out, double *field_out);
 
 /* The CUDA stream (cudaStream_t) every kernel of h is queued on. */
