@@ -2,9 +2,9 @@
 
   * oracle/_build/liborc.so  from oracle/g4oracle.c (always; plain C, no GPU)
   * oracle/_ref/             the reference compiled from its own sources by
-                             oracle/ref_build/Makefile, only when the reference
-                             tree is present (G4_REFERENCE_DIR, default
-                             /root/reference)
+                             oracle/ref_build/Makefile, only when a reference
+                             source tree is named (argument or G4_REFERENCE_DIR)
+                             and present
 
 Test infrastructure: called by __graft_entry__.build() and the tests.
 """
@@ -34,8 +34,8 @@ def build_oracle(verbose=False):
 
 
 def build_reference(ref_dir=None, jobs=8):
-    ref_dir = ref_dir or os.environ.get("G4_REFERENCE_DIR", "/root/reference")
-    if not os.path.isdir(os.path.join(ref_dir, "src", "Core")):
+    ref_dir = ref_dir or os.environ.get("G4_REFERENCE_DIR")
+    if not ref_dir or not os.path.isdir(os.path.join(ref_dir, "src", "Core")):
         return None
     subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref_build"), f"REF={ref_dir}",
                            f"-j{jobs}"])
@@ -44,5 +44,5 @@ def build_reference(ref_dir=None, jobs=8):
 
 if __name__ == "__main__":
     print(build_oracle(verbose=True))
-    print(build_reference())
+    print(build_reference(sys.argv[1] if len(sys.argv) > 1 else None))
     sys.exit(0)

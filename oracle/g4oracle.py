@@ -66,6 +66,10 @@ class _Lib:
         getattr(L, prefix + "fc").restype = _d
         getattr(L, prefix + "load_beam").argtypes = [_i, _i, _i, _i, _i, _i, _d, _d, _pd, _pd]
         getattr(L, prefix + "gauss_hermite").argtypes = [_pd, _d, _i, _pd]
+        if prefix == "g4ref_":
+            L.g4ref_set_solver.argtypes = [_i, _pd]
+            L.g4ref_diag_field.argtypes = [_i, _i, _d, _d, _d, _i, _pd, _i, _pd, _pd]
+            L.g4ref_diag_field.restype = _i
         if prefix == "orc_":
             L.orc_diag_beam.argtypes = [_i, _i, _pd, _i, _pd]
             L.orc_diag_field.argtypes = [_i, _i, _d, _d, _i, _pd, _i, _pd]
@@ -213,15 +217,35 @@ class _Lib:
                     _ptr(fst, _pi), _ptr(acc), int(time_run), int(periodic), stages, solver,
                     _ptr(fl), nthreads)
         else:
-            if solver != 0:
-                raise ValueError("the reference build has no FFT solver (no FFTW)")
+            # the reference's FieldSolverFFT runs on the FFTW stand-in of oracle/ref_build
+            fl = np.ones(3) if filt is None else np.ascontiguousarray(filt, dtype=np.float64)
             acc = None
-            rc = fn(lat.shape[0], _ptr(lat), gammaref, ns, npart, _ptr(part), _ptr(cur),
-                    reflength, sample, nfld, _ptr(harm, _pi), ngrid, _ptr(gm), _ptr(fv),
-                    _ptr(fst, _pi), int(time_run), int(periodic), stages)
+            self.lib.g4ref_set_solver(int(solver), _ptr(fl))
+            try:
+                rc = fn(lat.shape[0], _ptr(lat), gammaref, ns, npart, _ptr(part), _ptr(cur),
+                        reflength, sample, nfld, _ptr(harm, _pi), ngrid, _ptr(gm), _ptr(fv),
+                        _ptr(fst, _pi), int(time_run), int(periodic), stages)
+            finally:
+                self.lib.g4ref_set_solver(0, None)
         if rc != 0:
             raise RuntimeError(f"{self.p}run_steps failed: {rc}")
         return part, f, fst, acc
+
+    def diag_field_all(self, field, gridmax, reflength, sample, harm, first):
+        """The reference's DiagField::getValues with every filter on (reference build
+        only): per slice [ns][13] by window slice (DF_COLS, then xpointing, xdivergence,
+        ypointing, ydivergence) and the window values [11] (energy, x/y position and
+        size, mean near- and far-field intensity, far-field pointing and divergence)."""
+        f = np.ascontiguousarray(field, dtype=np.complex128)
+        ns = f.shape[0]
+        ngrid = int(round(np.sqrt(f.shape[1])))
+        out = np.zeros((ns, 13))
+        glob = np.zeros(11)
+        rc = self.lib.g4ref_diag_field(ns, ngrid, gridmax, reflength, sample, harm, _ptr(f.view(np.float64)),
+                                       int(first), _ptr(out), _ptr(glob))
+        if rc != 0:
+            raise RuntimeError(f"g4ref_diag_field failed: {rc}")
+        return out, glob
 
     def diag_beam(self, particles, nharm):
         part = np.ascontiguousarray(particles, dtype=np.float64)

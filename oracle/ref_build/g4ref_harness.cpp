@@ -23,6 +23,7 @@
 #include "RandomU.h"
 #include "Hammerslay.h"
 #include "BesselJ.h"
+#include "Diagnostic.h"
 
 // Electron charge as in GenMain.cpp:68 (ce), used for the electrons per slice.
 static const double kCe = 4.8032045e-11;
@@ -89,7 +90,68 @@ static double g_wk_ds = 0, g_wk_ztrans = 0, g_wk_radius = 0;
 static bool g_wk_transient = false;
 static std::vector<double> g_wk_ext, g_wk_res, g_wk_geo, g_wk_rou;
 
+// field solver of the following g4ref_run_steps calls (&track fft_fieldsolver,
+// source_filter, xcut, ycut, sigmoid as Track::run passes them to Field::initSolver,
+// Track.cpp:88-112): 0 ADI, 1 FFT, 2 FFT with the source filter (xc, yc, sig)
+static int g_solver = 0;
+static double g_filt[3] = {1, 1, 1};
+
 extern "C" {
+
+void g4ref_set_solver(int solver, const double *filt) {
+  g_solver = solver;
+  for (int k = 0; k < 3; k++) g_filt[k] = filt ? filt[k] : 1.0;
+}
+
+// DiagField::getValues (Diagnostic.cpp:718-996) with every filter on (spatial,
+// intensity, fft, global) on one field of ns slices in storage order with ring start
+// `first`. out_slice [ns][13] by window slice: power, xposition, xsize, yposition,
+// ysize, intensity-nearfield, phase-nearfield, intensity-farfield, phase-farfield,
+// xpointing, xdivergence, ypointing, ydivergence. out_global [11]: energy, xposition,
+// xsize, yposition, ysize, intensity-nearfield, intensity-farfield, xpointing,
+// xdivergence, ypointing, ydivergence.
+int g4ref_diag_field(int ns, int ngrid, double gridmax, double reflength, double sample, int harm,
+                     const double *field, int first, double *out_slice, double *out_global) {
+  Field f;
+  f.init(ns, ngrid, gridmax, reflength, reflength * sample, 0.0, harm);
+  const size_t ncell = static_cast<size_t>(ngrid) * ngrid;
+  for (int is = 0; is < ns; is++)
+    for (size_t c = 0; c < ncell; c++) {
+      const double *v = field + (static_cast<size_t>(is) * ncell + c) * 2;
+      f.field[is][c] = std::complex<double>(v[0], v[1]);
+    }
+  f.first = first;
+  FilterDiagnostics filt;
+  filt.field.global = true;
+  filt.field.spatial = true;
+  filt.field.fft = true;
+  filt.field.intensity = true;
+  DiagField diag;
+  std::map<std::string, OutputInfo> tags = diag.getTags(filt);
+  std::map<std::string, std::vector<double> > val;
+  for (auto &t : tags) val[t.first].assign(t.second.global ? 1 : ns, 0.0);
+  diag.getValues(&f, val, 0);
+  static const char *slice_names[13] = {"power", "xposition", "xsize", "yposition", "ysize",
+                                        "intensity-nearfield", "phase-nearfield", "intensity-farfield",
+                                        "phase-farfield", "xpointing", "xdivergence", "ypointing",
+                                        "ydivergence"};
+  static const char *global_names[11] = {"Global/energy", "Global/xposition", "Global/xsize",
+                                         "Global/yposition", "Global/ysize", "Global/intensity-nearfield",
+                                         "Global/intensity-farfield", "Global/xpointing",
+                                         "Global/xdivergence", "Global/ypointing", "Global/ydivergence"};
+  for (int k = 0; k < 13; k++) {
+    auto it = val.find(slice_names[k]);
+    if (it == val.end()) return 1;
+    for (int is = 0; is < ns; is++) out_slice[static_cast<size_t>(is) * 13 + k] = it->second[is];
+  }
+  for (int k = 0; k < 11; k++) {
+    auto it = val.find(global_names[k]);
+    if (it == val.end()) return 2;
+    out_global[k] = it->second[0];
+  }
+  diag.cleanup_FFT_resources();
+  return 0;
+}
 
 void g4ref_set_incoherent(int seed, int do_loss, int do_spread, int nbins) {
   g_isr_seed = seed;
@@ -176,7 +238,7 @@ int g4ref_run_steps(int nsteps, const double *tab, double gammaref, int ns, int 
   for (int k = 0; k < nfld; k++) {
     Field *f = new Field;
     f->init(ns, ngrid, gridmax[k], reflength, reflength * sample, 0.0, harm[k]);
-    f->initSolver(false, false, 1, 1, 1);
+    f->initSolver(g_solver != 0, g_solver == 2, g_filt[0], g_filt[1], g_filt[2]);
     for (int is = 0; is < ns; is++)
       for (size_t c = 0; c < ncell; c++) {
         const double *v = fields + ((static_cast<size_t>(k) * ns + is) * ncell + c) * 2;

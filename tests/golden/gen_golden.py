@@ -1,8 +1,9 @@
 """Generates the golden fixtures of tests/golden/ from the GENESIS 1.3 v4 reference
 itself, compiled from its own sources (oracle/ref_build/Makefile -> oracle/_ref/).
 
-Run where the reference tree is present:
-    python oracle/build_oracle.py && python tests/golden/gen_golden.py
+Run where the reference tree is present, naming it in G4_REFERENCE_DIR:
+    G4_REFERENCE_DIR=<tree> python oracle/build_oracle.py <tree>
+    G4_REFERENCE_DIR=<tree> python tests/golden/gen_golden.py
 
 Fixtures (numpy .npz):
   streams.npz    ran2, Hammersley, inverse erfc, Bessel J_n and fc(h) values
@@ -27,9 +28,14 @@ Fixtures (numpy .npz):
   incoherent.npz incoherent synchrotron radiation (&sponrad): the energy loss over planar
                  and helical lattices, and loss with spread over one step of a larger
                  window (with the same window's step without it)
+  fft.npz        the FFT field solver (FieldSolverFFT) over whole lattices, unfiltered
+                 and filtered, odd and even grids, harmonics 1, 3, 5 on ngrid 255; the
+                 far-field pointing and divergence of DiagField (filter "fft"). The
+                 reference is built with -DFFTW on oracle/ref_build's FFTW stand-in
+                 (FFTW's documented DFT evaluated directly), as FFTW is not installed
 
 `python tests/golden/gen_golden.py spacecharge` (or `wakes`, `chicane`, `one4one`,
-`incoherent`) regenerates only that file.
+`incoherent`, `fft`) regenerates only that file.
 
 The reference's CI check of Example1 (examples/Example1-SteadyState/TEST_power.py)
 expects a final power of 0.932785e9 W within 30 %; example1.npz records what the
@@ -51,7 +57,8 @@ import g4cases as T  # noqa: E402
 import g4oracle as G  # noqa: E402
 from rawio import read_raw  # noqa: E402
 
-REF_DIR = os.environ.get("G4_REFERENCE_DIR", "/root/reference")
+# the reference source tree (its example decks are read from there)
+REF_DIR = os.environ.get("G4_REFERENCE_DIR")
 GENESIS = os.path.join(ROOT, "oracle", "_ref", "genesis4")
 
 
@@ -424,6 +431,95 @@ def gen_incoherent(r):
     np.savez_compressed(os.path.join(HERE, "incoherent.npz"), **d)
 
 
+# ngrid of the FFT-solver windows: odd and even, every register radix of the engine's
+# transform plans (25 = 5 5, 32 = 16 2, 45 = 15 3, 22 = 2 11) and a generic prime stage
+# (38 = 2 19)
+FFT_GRIDS = (25, 32, 45, 22, 38)
+FFT_FILTER = (0.7, 0.9, 0.3)
+
+
+def fft_cases(r):
+    """Windows for the reference's FieldSolverFFT (built on the FFTW stand-in): two
+    harmonics (1, 3) on their own grids, the unfiltered and the filtered source (xcut
+    0.7, ycut 0.9, sigmoid 0.3) on every grid of FFT_GRIDS; and config 3's layout at a
+    reduced size: harmonics 1, 3, 5 on ngrid 255 over gridmax 1.5e-4 m, nbins 8 shot
+    noise, delgam 1.0. The windows are periodic (the field slipping out of the head
+    re-enters at the tail): at 2.26 slices of slippage per step a zero-filled window
+    of a few slices would be emptied within two steps, and every solve would then
+    transform a zero field."""
+    cases = []
+    lat = T.undulator_lattice(1.7, 0.015, 6, 2, 1e-10, 11357.8, quad_k1=1.5, quad_l=0.08)
+    part = r.load_beam(T.slice_params(5, 11357.8, 2.0, 0.4e-6, 15.0), 0, 64, 4, 7, 1, 1e-10, 1.0)
+    for n in FFT_GRIDS:
+        g1 = r.gauss_hermite(T.gauss_field_par(1e-10, 1e5, 20e-6), 6e-5, n)
+        g3 = r.gauss_hermite(T.gauss_field_par(1e-10, 1e3, 12e-6, harm=3), 4e-5, n)
+        fld = np.stack([np.stack([g1 * (1 + 0.3j * k) for k in range(5)]),
+                        np.stack([g3 * (1 - 0.2j * k) for k in range(5)])])
+        for solver in (1, 2):
+            cases.append(dict(name=f"n{n}_s{solver}", lat=lat, part=part, cur=np.full(5, 3000.0), harm=[1, 3],
+                              gridmax=[6e-5, 4e-5], fields=fld, solver=solver,
+                              filt=FFT_FILTER if solver == 2 else (1.0, 1.0, 1.0)))
+    ns, ng, gm, harm = 3, 255, 1.5e-4, [1, 3, 5]
+    lat = T.undulator_lattice(1.7, 0.015, 5, 2, 1e-10, 11357.8, quad_k1=1.5, quad_l=0.08)
+    part = r.load_beam(T.slice_params(ns, 11357.8, 1.0, 0.4e-6, 15.0), 0, 256, 8, 7, 1, 1e-10, 1.0)
+    fld = harm255_fields(r.gauss_hermite, ns, ng, gm, harm)
+    cases.append(dict(name="harm255", lat=lat, part=part, cur=np.full(ns, 3000.0), harm=harm, gridmax=[gm] * 3,
+                      fields=fld, solver=1, filt=(1.0, 1.0, 1.0)))
+    return cases
+
+
+def harm255_fields(gauss_hermite, ns=3, ng=255, gm=1.5e-4, harm=(1, 3, 5)):
+    """Initial fields of the harm255 case from a Gauss-Hermite loader (the reference's,
+    or one bit-exact with it): they are rebuilt rather than stored."""
+    return np.stack([np.stack([gauss_hermite(T.gauss_field_par(1e-10, 1e5 / h ** 2, 25e-6, harm=h), gm, ng)
+                               * np.exp(1j * (0.4 * k + h)) for k in range(ns)]) for h in harm])
+
+
+# cells of the ngrid-255 output fields kept in fft.npz (every 29th: 2243 per slice)
+HARM255_CELLS = slice(0, None, 29)
+
+
+def far_field(ng, ns=6):
+    """A Gaussian beam off axis with a transverse tilt that changes from slice to slice
+    (rebuilt by the tests rather than stored)."""
+    x = np.arange(ng) - 0.5 * (ng - 1)
+    g = np.exp(-((x[None, :] - 2.0) ** 2 + (x[:, None] + 1.0) ** 2) / (0.05 * ng * ng))
+    return np.stack([(g * np.exp(1j * (0.2 + 0.05 * s) * x[None, :] - 1j * 0.03 * s * x[:, None])).ravel() * 1e4
+                     for s in range(ns)])
+
+
+# (ngrid, harmonic, ring start) of the far-field cases: odd and even grids
+FAR_FIELD_CASES = ((45, 1, 0), (32, 3, 2), (51, 1, 5), (21, 5, 1))
+
+
+def gen_fft(r):
+    """fft.npz: the reference's FFT field solver (FieldSolverFFT.cpp:9-167) over whole
+    lattices, and its far-field diagnostics (Diagnostic.cpp:718-996 with filter "fft"),
+    both built against the FFTW stand-in of oracle/ref_build."""
+    d = {}
+    for c in fft_cases(r):
+        n = c["name"]
+        big = n == "harm255"
+        for k in ("lat", "part", "cur", "harm", "gridmax", "filt"):
+            d[f"{n}_{k}"] = np.asarray(c[k])
+        if not big:  # one input field per grid, shared by the unfiltered and filtered case
+            d[f"{n.split('_')[0]}_fields"] = np.asarray(c["fields"])
+        d[f"{n}_solver"] = np.array(c["solver"])
+        nf = len(c["harm"])
+        out = r.run_steps(c["lat"], 11357.8, c["part"], c["cur"], 1e-10, 1.0, c["harm"], c["gridmax"],
+                          c["fields"], [0] * nf, time_run=1, periodic=1, stages=7, solver=c["solver"],
+                          filt=c["filt"])
+        d[f"{n}_out_part"], d[f"{n}_out_first"] = out[0], out[2]
+        d[f"{n}_out_fields"] = out[1][:, :, HARM255_CELLS] if big else out[1]
+        # the far-field columns of the solved fields
+        for k in range(nf):
+            sl, gl = r.diag_field_all(out[1][k], c["gridmax"][k], 1e-10, 1.0, c["harm"][k], int(out[2][k]))
+            d[f"{n}_diag{k}"], d[f"{n}_global{k}"] = sl, gl
+    for ng, harm, first in FAR_FIELD_CASES:
+        d[f"ff{ng}_diag"], d[f"ff{ng}_global"] = r.diag_field_all(far_field(ng), 6e-5, 1e-10, 1.0, harm, first)
+    np.savez_compressed(os.path.join(HERE, "fft.npz"), **d)
+
+
 LAT_FROM_OUT = {"aw": "aw", "ax": "ax", "ay": "ay", "ku": "ku", "kx": "kx", "ky": "ky",
                 "gradx": "gradx", "grady": "grady", "qf": "qf", "qx": "qx", "qy": "qy",
                 "cx": "cx", "cy": "cy", "dz": "dz", "slip": "slippage", "phase": "phaseshift",
@@ -519,6 +615,8 @@ def gen_config0():
 
 
 def main():
+    if not REF_DIR:
+        sys.exit("set G4_REFERENCE_DIR to the reference source tree")
     r = G.reference()
     if r is None or not os.path.exists(GENESIS):
         sys.exit("the reference checker is not built: run oracle/build_oracle.py with the reference present")
@@ -537,11 +635,15 @@ def main():
     if sys.argv[1:] == ["incoherent"]:
         gen_incoherent(r)
         return
+    if sys.argv[1:] == ["fft"]:
+        gen_fft(r)
+        return
     gen_space_charge(r)
     gen_wakes(r)
     gen_chicane(r)
     gen_one4one(r)
     gen_incoherent(r)
+    gen_fft(r)
     gen_streams(r)
     gen_loading(r)
     gen_steps(r)

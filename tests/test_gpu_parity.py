@@ -305,9 +305,12 @@ def test_run_before_load_is_an_error(lib):
 # 34 = 2 17, 38 = 2 19, 27 = 9 3, 100 = 4 5 5
 @pytest.mark.parametrize("n", [25, 45, 32, 56, 22, 26, 34, 38, 27, 100])
 def test_fft_solver_plain_matches_oracle(lib, oracle, solver, filt, n):
-    """FieldSolverFFT (src/Core/FieldSolverFFT.cpp:9-114) on a time-dependent window
-    with two harmonics, against the oracle's restatement (pinned to numpy's FFT in
-    tests/test_oracle_pins.py; the reference's own FFT path needs FFTW)."""
+    """FieldSolverFFT (src/Core/FieldSolverFFT.cpp:9-114) on a periodic time-dependent
+    window with two harmonics, against the oracle's restatement (pinned to the
+    reference's own FFT solver in tests/test_oracle_pins.py), on grids besides those of
+    the reference fixtures (test_fft_solver_plain_matches_reference). Periodic: at 2.26
+    slices of slippage per step a zero-filled window of 5 slices would be emptied within
+    two steps, and the solves would transform zero fields."""
     import g4gpu
     import g4cases as T
     ns, npart = 5, 64
@@ -320,7 +323,7 @@ def test_fft_solver_plain_matches_oracle(lib, oracle, solver, filt, n):
                     np.stack([g3 * (1 - 0.2j * k) for k in range(ns)])])
     cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=n, harm=[1, 3], gridmax=[6e-5, 4e-5], lambda0=1e-10,
                        sample=1.0, gammaref=11357.8, precision=0, solver=g4gpu.SOLVER_FFT,
-                       source_filter=int(solver == 2), time_run=1)
+                       source_filter=int(solver == 2), time_run=1, periodic=1)
     if filt:
         cfg.xcut, cfg.ycut, cfg.sigmoid = filt
     with g4gpu.Handle(cfg) as h:
@@ -334,8 +337,9 @@ def test_fft_solver_plain_matches_oracle(lib, oracle, solver, filt, n):
         f1, _, _ = h.get_field(1)
         assert h.kernel_stats()["fft"][0] == 3 * 2 * lat.shape[0]
     rp, rf, rfirst, _ = oracle.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, [1, 3], [6e-5, 4e-5], fld, [0, 0],
-                                         solver=solver, filt=filt)
+                                         solver=solver, filt=filt, periodic=1)
     assert first0 == rfirst[0]
+    assert np.abs(rf[0]).max() > 0 and np.abs(rf[1]).max() > 0
     assert rel_err(f0, rf[0]) < 1e-9 and rel_err(f1, rf[1]) < 1e-9
     for col in range(6):
         assert rel_err(p[..., col], rp[..., col]) < 1e-9
@@ -370,8 +374,8 @@ def test_fft_three_harmonics_large_grid_matches_oracle(lib, oracle, precision):
     """Config 3's field layout at a size the oracle finishes in seconds: fields at the
     fundamental, 3rd and 5th harmonic, each on ngrid 255 over dgrid 1.5e-4 m, the FFT
     solver (255 = 3 x 5 x 17: every radix of the mixed-radix transform), nbins 8 quiet
-    loading with shot noise (harmonic bunching), a time-dependent window with slippage.
-    Plain FP64 within 1e-9 of the oracle; the mixed form within its 1 %."""
+    loading with shot noise (harmonic bunching), a periodic time-dependent window with
+    slippage. Plain FP64 within 1e-9 of the oracle; the mixed form within its 1 %."""
     import g4gpu
     import g4cases as T
     ns, npart, ng, gm = 3, 256, 255, 1.5e-4
@@ -382,7 +386,8 @@ def test_fft_three_harmonics_large_grid_matches_oracle(lib, oracle, precision):
     fld = np.stack([np.stack([g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e5 / h ** 2, 25e-6, harm=h), gm, ng)
                               * np.exp(1j * (0.4 * k + h)) for k in range(ns)]) for h in harm])
     cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, nfield=3, harm=harm, gridmax=[gm] * 3, lambda0=1e-10,
-                       sample=1.0, gammaref=11357.8, precision=precision, solver=g4gpu.SOLVER_FFT, time_run=1)
+                       sample=1.0, gammaref=11357.8, precision=precision, solver=g4gpu.SOLVER_FFT, time_run=1,
+                       periodic=1)
     with g4gpu.Handle(cfg) as h:
         h.set_lattice(lat)
         h.load_beam(part, cur)
@@ -393,7 +398,7 @@ def test_fft_three_harmonics_large_grid_matches_oracle(lib, oracle, precision):
         fs = [h.get_field(k) for k in range(3)]
         bd, fd = h.diag(5)
     rp, rf, rfirst, _ = oracle.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, harm, [gm] * 3, fld, [0, 0, 0],
-                                         solver=1, nthreads=8)
+                                         solver=1, nthreads=8, periodic=1)
     for k in range(3):
         assert fs[k][1] == rfirst[k]
     if precision == 0:
@@ -408,6 +413,100 @@ def test_fft_three_harmonics_large_grid_matches_oracle(lib, oracle, precision):
             assert rel_err(fd[k][:, 0], of[:, 0]) < 1e-2, k
         for hh in range(5):  # bunching at harmonics 1..5
             assert bunching_ok(bd[:, 24 + 2 * hh], ob[:, 24 + 2 * hh])
+
+
+FFT_CASES = [f"n{n}_s{s}" for n in (25, 32, 45, 22, 38) for s in (1, 2)] + ["harm255"]
+
+
+def run_fft_case(g4gpu, case, precision):
+    """One window of tests/golden/fft.npz (the reference's own FieldSolverFFT, built on
+    the FFTW stand-in) through the engine: returns (particles, [(field, first)], beam
+    diagnostics, field diagnostics)."""
+    import gen_golden
+    from test_oracle_pins import fft_case_inputs
+    d = golden("fft.npz")
+    lat, part, cur, harm, gm, fld, solver, filt = fft_case_inputs(d, case, g4gpu.host_gauss_hermite)
+    ns, npart = part.shape[0], part.shape[1]
+    ng = int(round(np.sqrt(fld.shape[2])))
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, nfield=len(harm), harm=list(harm), gridmax=list(gm),
+                       lambda0=1e-10, sample=1.0, gammaref=11357.8, precision=precision,
+                       solver=g4gpu.SOLVER_FFT, source_filter=int(solver == 2), time_run=1, periodic=1)
+    cfg.xcut, cfg.ycut, cfg.sigmoid = (float(v) for v in filt)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam(part, cur)
+        for k in range(len(harm)):
+            h.load_field(k, fld[k])
+        h.run(0, lat.shape[0])
+        p = h.get_beam()
+        fs = [h.get_field(k)[:2] for k in range(len(harm))]
+        bd, fd = h.diag(1)
+    if case == "harm255":
+        fs = [(f[:, gen_golden.HARM255_CELLS], first) for f, first in fs]
+    return d, harm, p, fs, bd, fd
+
+
+@pytest.mark.parametrize("case", FFT_CASES)
+def test_fft_solver_plain_matches_reference(lib, case):
+    """The plain FP64 FFT solver against the reference's own FieldSolverFFT
+    (FieldSolverFFT.cpp:9-167, built with -DFFTW on oracle/ref_build's FFTW stand-in,
+    tests/golden/fft.npz): whole lattices of periodic windows, harmonics 1 and 3 (1, 3
+    and 5 on ngrid 255), unfiltered and filtered sources, odd and even grids and every
+    radix of the engine's transform plans. Fields and particles within 1e-9 of their
+    largest values, ring starts equal."""
+    import g4gpu
+    d, harm, p, fs, _, _ = run_fft_case(g4gpu, case, g4gpu.PLAIN)
+    want_f, want_first = d[f"{case}_out_fields"], d[f"{case}_out_first"]
+    for k in range(len(harm)):
+        assert fs[k][1] == want_first[k]
+        assert rel_err(fs[k][0], want_f[k]) < 1e-9, k
+    want_p = d[f"{case}_out_part"]
+    for col in range(6):
+        assert rel_err(p[..., col], want_p[..., col]) < 1e-9, col
+
+
+@pytest.mark.parametrize("case", ["n25_s1", "n32_s2", "n38_s1", "harm255"])
+def test_fft_solver_mixed_matches_reference(lib, case):
+    """The mixed form's FFT solver against the reference's (fft.npz): every field's
+    slice power within 1 % of the reference's DiagField power (its largest slice), the
+    ring starts equal."""
+    import g4gpu
+    d, harm, _, fs, _, fd = run_fft_case(g4gpu, case, g4gpu.MIXED)
+    for k in range(len(harm)):
+        assert fs[k][1] == d[f"{case}_out_first"][k]
+        want = d[f"{case}_diag{k}"][:, 0]
+        assert want.max() > 0
+        assert rel_err(fd[k][:, 0], want) < 1e-2, k
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("ng,harm,first", [(45, 1, 0), (32, 3, 2), (51, 1, 5), (21, 5, 1)])
+def test_field_diagnostics_match_reference(lib, prec, ng, harm, first):
+    """g4gpu_diag and g4gpu_diag_fft against the reference's DiagField::getValues with
+    every filter on (Diagnostic.cpp:718-996, far field by the FFTW stand-in;
+    tests/golden/fft.npz): per slice the power, centroid, size, near- and far-field
+    intensity and phase, far-field pointing and divergence, by window slice from a
+    moved ring start. Plain FP64 within 1e-9 of each column's scale, mixed 1e-4 (the
+    phases within 1e-4 rad)."""
+    import g4gpu
+    import gen_golden
+    u = gen_golden.far_field(ng)
+    ns = u.shape[0]
+    cfg = g4gpu.Config(nslice=ns, npart=32, ngrid=ng, harm=[harm], gridmax=6e-5, lambda0=1e-10, sample=1.0,
+                       gammaref=11357.8, precision=prec, time_run=1)
+    with g4gpu.Handle(cfg) as h:
+        h.load_field(0, u, first=first)
+        _, fd = h.diag(1, beam=False)
+        ff = h.diag_fft()
+    got = np.concatenate([fd[0], ff[0]], axis=1)
+    want = golden("fft.npz")[f"ff{ng}_diag"]
+    tol = 1e-9 if prec == 0 else 1e-4
+    for col in range(13):
+        if col in (6, 8):  # phases [rad]
+            assert np.abs(np.angle(np.exp(1j * (got[:, col] - want[:, col])))).max() <= tol, col
+            continue
+        scale = np.abs(want[:, col | 1 if col >= 9 else col]).max()
+        assert np.abs(got[:, col] - want[:, col]).max() <= tol * scale, col
 
 
 @pytest.mark.parametrize("nbins,npart", [(8, 200), (3, 99), (4, 256)])

@@ -132,9 +132,10 @@ def _k2_and_sigmoid(n, dgrid, xks, xc=1.0, yc=1.0, sig=1.0):
 
 @pytest.mark.parametrize("n", [15, 16, 21])
 def test_fft_solver_matches_numpy(oracle, n):
-    """The FFT solver of the oracle (the reference's FFTW path cannot be built here:
-    no FFTW) against numpy's pocketfft: u' = IFFT(FFT(u) exp(K2 dz)) + 2 src, and the
-    filtered form IFFT(FFT(u) exp(K2 dz) + 2 FFT(src) sigmoid)."""
+    """The FFT solver of the oracle against numpy's pocketfft, a second transform
+    besides the reference's (test_fft_solver_matches_reference): u' = IFFT(FFT(u)
+    exp(K2 dz)) + 2 src, and the filtered form IFFT(FFT(u) exp(K2 dz) + 2 FFT(src)
+    sigmoid)."""
     import g4cases as T
     rng = np.random.default_rng(n)
     ns, gm, dz = 2, 5e-5, 0.015
@@ -168,7 +169,7 @@ def test_fft_solver_matches_numpy(oracle, n):
 @pytest.mark.parametrize("n", [15, 16, 21])
 def test_far_field_moments_match_numpy(oracle, n):
     """The oracle's far-field pointing and divergence (DiagField with FFTW,
-    Diagnostic.cpp:786-847; FFTW is absent here) against numpy: the power-weighted
+    Diagnostic.cpp:786-847) against numpy, besides the reference: the power-weighted
     moments of |FFT2(u)|^2 on the shifted frequency map, scaled by
     xlambda / (ngrid dgrid), by window slice."""
     rng = np.random.default_rng(n + 100)
@@ -191,6 +192,88 @@ def test_far_field_moments_match_numpy(oracle, n):
         want = [fx1 * sclt, np.sqrt(abs(fx2 - fx1 * fx1)) * sclt, fy1 * sclt, np.sqrt(abs(fy2 - fy1 * fy1)) * sclt]
         is_ = (ns + is0 - first) % ns
         assert np.allclose(got[is_], want, rtol=1e-10, atol=1e-12 * max(abs(v) for v in want))
+
+
+FFT_CASES = [f"n{n}_s{s}" for n in (25, 32, 45, 22, 38) for s in (1, 2)] + ["harm255"]
+
+
+def fft_case_inputs(d, name, gauss_hermite):
+    """Inputs of one case of tests/golden/fft.npz: (lattice, particles, current, harm,
+    gridmax, fields, solver, filter); the ngrid-255 case's fields are rebuilt with the
+    given Gauss-Hermite loader (bit-exact with the reference's, loading.npz)."""
+    import gen_golden
+    g = lambda k: d[f"{name}_{k}"]
+    if name == "harm255":
+        fld = gen_golden.harm255_fields(gauss_hermite)
+    else:
+        fld = d[f"{name.split('_')[0]}_fields"]
+    return g("lat"), g("part"), g("cur"), g("harm"), g("gridmax"), fld, int(g("solver")), g("filt")
+
+
+@pytest.mark.parametrize("case", FFT_CASES)
+def test_fft_solver_matches_reference(oracle, case):
+    """The oracle's FFT field solver against the reference's own FieldSolverFFT
+    (FieldSolverFFT.cpp:9-167) built with -DFFTW on the FFTW stand-in of
+    oracle/ref_build (tests/golden/fft.npz): whole lattices (13 and 11 steps) of
+    periodic time-dependent windows, two or three harmonics, unfiltered and filtered
+    sources, odd and even grids and ngrid 255. The two transforms round differently
+    (FFTW's documented DFT evaluated exactly against the oracle's mixed-radix FFT):
+    within 1e-13 of the largest field value, particles within 1e-13."""
+    import gen_golden
+    d = golden("fft.npz")
+    lat, part, cur, harm, gm, fld, solver, filt = fft_case_inputs(d, case, oracle.gauss_hermite)
+    p, f, first, _ = oracle.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, harm, gm, fld, [0] * len(harm),
+                                      periodic=1, solver=solver, filt=filt, nthreads=8)
+    want_f = d[f"{case}_out_fields"]
+    if case == "harm255":
+        f = f[:, :, gen_golden.HARM255_CELLS]
+    assert np.array_equal(first, d[f"{case}_out_first"])
+    for k in range(len(harm)):
+        assert np.abs(want_f[k]).max() > 0
+        assert np.abs(f[k] - want_f[k]).max() <= 1e-13 * np.abs(want_f[k]).max(), k
+    want_p = d[f"{case}_out_part"]
+    for col in range(6):
+        assert np.abs(p[..., col] - want_p[..., col]).max() <= 1e-13 * np.abs(want_p[..., col]).max(), col
+
+
+@pytest.mark.parametrize("ng,harm,first", [(45, 1, 0), (32, 3, 2), (51, 1, 5), (21, 5, 1)])
+def test_far_field_matches_reference(oracle, ng, harm, first):
+    """The oracle's field diagnostics against the reference's DiagField::getValues
+    with every filter on, far field included (Diagnostic.cpp:718-996, FFTW stand-in):
+    per slice the power, centroid, size, near- and far-field intensity and phase,
+    far-field pointing and divergence; the window (Global/) values. Within 1e-12 of
+    each column's scale (the far-field transforms round differently)."""
+    import gen_golden
+    d = golden("fft.npz")
+    u = gen_golden.far_field(ng)
+    want, want_g = d[f"ff{ng}_diag"], d[f"ff{ng}_global"]
+    got = np.concatenate([oracle.diag_field(u, 6e-5, 1e-10, harm, first),
+                          oracle.diag_field_fft(u, 6e-5, 1e-10, harm, first)], axis=1)
+    for col in range(13):
+        scale = np.abs(want[:, col]).max()
+        if col in (9, 11):  # pointing, on the divergence's scale
+            scale = np.abs(want[:, col + 1]).max()
+        assert np.abs(got[:, col] - want[:, col]).max() <= 1e-12 * max(scale, 1e-300), col
+    got_g = oracle.diag_global_field(u, 6e-5, 1e-10, harm, 1.0)
+    for k in range(11):
+        scale = abs(want_g[k]) if k not in (7, 9) else abs(want_g[k + 1])
+        assert abs(got_g[k] - want_g[k]) <= 1e-12 * max(scale, 1e-300), k
+
+
+@pytest.mark.parametrize("case", ["n25_s1", "n32_s2"])
+def test_fft_solved_fields_far_field_matches_reference(oracle, case):
+    """The far-field columns of the reference's solved FFT fields (fft.npz), from the
+    oracle's diagnostics on the reference's own output fields."""
+    d = golden("fft.npz")
+    for k, hk in enumerate(d[f"{case}_harm"]):
+        f = d[f"{case}_out_fields"][k]
+        gm = float(d[f"{case}_gridmax"][k])
+        first = int(d[f"{case}_out_first"][k])
+        got = oracle.diag_field_fft(f, gm, 1e-10, int(hk), first)
+        want = d[f"{case}_diag{k}"][:, 9:]
+        for col in range(4):
+            scale = np.abs(want[:, col | 1]).max()
+            assert np.abs(got[:, col] - want[:, col]).max() <= 1e-12 * scale, (k, col)
 
 
 @pytest.mark.parametrize("case", ["short", "long", "both", "steady"])
