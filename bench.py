@@ -54,6 +54,12 @@ NS, NPART, NGRID, GRIDMAX = 4096, 8192, 151, 1e-4
 LAMBDA0, GAMMA0 = 1e-10, 11357.8
 EDGE_SIGMA = 0.2e-15 * 299792458.0  # 0.2 fs rms edges
 METRIC = "slice-steps/s on 1 GB300: plain FP64 vs mixed/batched/learned at <=1% power error"
+WORKLOAD = ("time-dependent SASE, 4096 slices x 8192 particles, ngrid 151, ADI, 4x110-period planar undulator "
+            "with FODO, shot noise seed 7")
+# the resonant companion of the workload: the same beam and lattice at the resonant
+# wavelength lambda_u (1 + aw^2) / (2 gamma0^2) = 2.262e-10 m (the workload's 1e-10 m is
+# off resonance and does not lase); slippage is then one slice per period
+LAMBDA_RES = 0.015 * (1 + 1.7 ** 2) / (2 * GAMMA0 ** 2)
 
 
 def measured_peaks():
@@ -193,21 +199,32 @@ TRAFFIC_SOURCE = "ncu capture of a 608-slice window, scaled to the launch's slic
 # (profiles/ncu_fp64_k_push_k_adi_plain_sase152.md); nominal GB300 FP64 rate: 1.25 TFLOP/s
 # with FMA counted as two operations, i.e. 625 G FP64 instructions/s.
 FP64_INSTR = {"push_per_particle": 762.0, "adi_per_cell": 37.8}
-FP64_PEAK_GINSTR = 625.0
+FP64_NOMINAL_GINSTR = 625.0
 
 
-def fp64_roofline(kernels_plain):
+def fp64_peak(g4gpu, device):
+    """The device's FP64 instruction rate, measured by the library's FMA-chain kernel
+    (g4gpu_measure_fp64_rate), in G instructions/s; the nominal 1.25 TFLOP/s (625 G
+    FMA/s) if the measurement fails."""
+    import ctypes
+    r = ctypes.c_double()
+    if g4gpu.load_library().g4gpu_measure_fp64_rate(device, ctypes.byref(r)) == 0 and r.value > 0:
+        return r.value / 1e9, "measured: g4gpu_measure_fp64_rate (independent DFMA chains, CUDA events)"
+    return FP64_NOMINAL_GINSTR, "nominal 1.25 TFLOP/s (measurement failed)"
+
+
+def fp64_roofline(kernels_plain, peak_ginstr, peak_source):
     """The plain form is bound by the FP64 rate: FP64 instructions per launch (ncu
     counts per particle / cell times the launch's particles / cells) over the measured
-    launch time, against the nominal FP64 instruction rate."""
-    out = {"bound": "fp64", "peak_ginstr_s": FP64_PEAK_GINSTR, "peak_source": "nominal 1.25 TFLOP/s",
+    launch time, against the device's FP64 instruction rate."""
+    out = {"bound": "fp64", "peak_ginstr_s": peak_ginstr, "peak_source": peak_source,
            "instr_source": "ncu dfma+dmul+dadd counts of a 152-slice capture"}
     for k, n in (("push", NS * NPART * FP64_INSTR["push_per_particle"]),
                  ("adi_x", NS * NGRID * NGRID * FP64_INSTR["adi_per_cell"]),
                  ("adi_y", NS * NGRID * NGRID * FP64_INSTR["adi_per_cell"])):
         if k in kernels_plain:
             g = n / (kernels_plain[k]["ms_avg"] / 1e3) / 1e9
-            out[k] = {"ginstr_s": g, "frac": g / FP64_PEAK_GINSTR}
+            out[k] = {"ginstr_s": g, "frac": g / peak_ginstr}
     return out
 
 
@@ -241,6 +258,65 @@ def kernel_alg_bytes(kernel, mixed, ns=None):
     else:
         return None
     return ns * per
+
+
+def mixed_error(hm, hp, after_steps):
+    """The mixed handle's slice power and bunching against the plain FP64 handle's
+    (both at the same step): the largest slice-power difference over the largest
+    slice power, the window energy, the largest bunching difference over the largest
+    bunching and absolute. The absolute bunching floor that matters is the shot-noise
+    level of the beam, 1/sqrt(npart) = 0.011 for 8192 particles."""
+    bm, fm = hm.diag(1)
+    bp, fp = hp.diag(1)
+    pw_m, pw_p = fm[0][:, 0], fp[0][:, 0]
+    db = float(np.max(np.abs(bm[:, 24] - bp[:, 24])))
+    return {"power_max_rel": float(np.max(np.abs(pw_m - pw_p)) / max(np.max(np.abs(pw_p)), 1e-300)),
+            "energy_rel": float(abs(pw_m.sum() / pw_p.sum() - 1)) if pw_p.sum() > 0 else None,
+            "bunching_max_rel": db / max(float(np.max(np.abs(bp[:, 24]))), 1e-300),
+            "bunching_max_abs": db, "bunching_floor_1_over_sqrt_npart": 1.0 / np.sqrt(NPART),
+            "max_slice_power_w": float(np.max(pw_p)), "max_bunching": float(np.max(bp[:, 24])),
+            "after_steps": after_steps}
+
+
+def resonant_companion(g4gpu, torch, shapes):
+    """The workload's window at the resonant wavelength LAMBDA_RES (one slice of
+    slippage per period), which lases from shot noise: the mixed form against the plain
+    FP64 form after every module of the 443-step lattice, with the window energy's
+    growth. Not timed."""
+    lat = T.undulator_lattice(1.7, 0.015, 110, 4, LAMBDA_RES, GAMMA0, quad_k1=1.5, quad_l=0.08)
+    cur = flat_top(NS)
+    sp = T.slice_params(NS, GAMMA0, 2.0, 0.4e-6, 15.0, currents=cur)
+    beam = g4gpu.host_load_beam(sp, 0, NPART, 4, 7, 1, LAMBDA_RES, 1.0)
+    hs = []
+    for prec in (g4gpu.MIXED, g4gpu.PLAIN):
+        cfg = g4gpu.Config(nslice=NS, npart=NPART, ngrid=NGRID, gridmax=GRIDMAX, lambda0=LAMBDA_RES, sample=1.0,
+                           gammaref=GAMMA0, precision=prec, time_run=1, device=torch.cuda.current_device())
+        h = g4gpu.Handle(cfg)
+        h.set_lattice(lat)
+        h.load_beam(beam, cur)
+        h.load_field(0, np.zeros((NS, NGRID * NGRID), dtype=np.complex128))
+        if prec == g4gpu.MIXED and shapes is not None:
+            h.set_launch_shapes(*shapes)
+        hs.append(h)
+    del beam
+    out = {"lambda0": LAMBDA_RES, "modules": []}
+    nlat = lat.shape[0]
+    ends = [i + 1 for i in range(nlat) if lat[i, T.C["aw"]] > 0 and (i + 1 == nlat or lat[i + 1, T.C["aw"]] == 0)]
+    done = 0
+    for e in ends:
+        for h in hs:
+            h.run(done, e - done)
+        done = e
+        row = mixed_error(hs[0], hs[1], e)
+        row["window_energy_plain"] = float(hs[1].diag(1)[1][0][:, 0].sum())
+        out["modules"].append(row)
+    for h in hs:
+        h.close()
+    e0 = out["modules"][0]["window_energy_plain"]
+    out["energy_growth_module1_to_end"] = out["modules"][-1]["window_energy_plain"] / max(e0, 1e-300)
+    out["power_max_rel"] = max(m["power_max_rel"] for m in out["modules"])
+    out["bunching_max_rel"] = max(m["bunching_max_rel"] for m in out["modules"])
+    return out
 
 
 def time_form(g4gpu, torch, precision, beam, cur, lat, steps, warmup, profile=True, autotune=False, shapes=None,
@@ -614,10 +690,15 @@ def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_s
                          "generate_s": t_gen, "train_s": t_train}}
 
 
+E2E_WINDOWS = 7
+
+
 def e2e_window(g4gpu, torch, precision, beam_pinned, cur, field_pinned, lat, steps, reps, shapes=None):
     """Track windows through the ABI with host buffers: upload, `steps` steps with the
-    per-slice diagnostics of every step (recorded on the device, read back once at the
-    end of the steps), download of beam and field."""
+    per-slice diagnostics of every step (recorded on the device, each step's record
+    read back while the later steps run), download of beam and field. One warm-up
+    window, `reps` timed windows (their wall times are returned), then one window with
+    a synchronisation between its phases to split its time."""
     cfg = g4gpu.Config(nslice=NS, npart=NPART, ngrid=NGRID, gridmax=GRIDMAX, lambda0=LAMBDA0,
                        sample=1.0, gammaref=GAMMA0, precision=precision, time_run=1,
                        device=torch.cuda.current_device())
@@ -657,43 +738,54 @@ def e2e_window(g4gpu, torch, precision, beam_pinned, cur, field_pinned, lat, ste
     h.close()
     h2d = beam_pinned.numel() * 8 + cur_np.nbytes + field_pinned.numel() * 8
     d2h = d2h_diag + out_beam.numel() * 8 + out_field.numel() * 8
-    return min(times), h2d, d2h, phases
+    return times, h2d, d2h, phases
 
 
-def cpu_baseline(nthreads, target_seconds=12.0, prefer_reference=True):
-    """Times the CPU step (oracle/_ref when built here, else the oracle port) on a
-    bounded sample: full-size slices (8192 particles, ngrid 151) of the workload."""
+def cpu_sample(lib, ns):
+    """ns full-size slices (8192 particles, ngrid 151) from the middle of the
+    workload's window, loaded by the checker library's own bit-exact loader (the
+    quiet loading and shot-noise stream of the window's slices), with zero field."""
+    cur = flat_top(NS)[NS // 2 - ns // 2:NS // 2 - ns // 2 + ns]
+    sp = T.slice_params(ns, GAMMA0, 2.0, 0.4e-6, 15.0, currents=cur)
+    beam = lib.load_beam(sp, NS // 2 - ns // 2, NPART, 4, 7, 1, LAMBDA0, 1.0)
+    return beam, cur, np.zeros((1, ns, NGRID * NGRID), dtype=np.complex128)
+
+
+def cpu_baseline(nthreads, target_seconds=15.0):
+    """Times the oracle port (oracle/g4oracle.c, bit-exact with the reference) on a
+    bounded sample of the workload: full-size slices (8192 particles, ngrid 151), as
+    many steps of the lattice as fit and then as many slices (a multiple of the
+    threads) as fill about target_seconds, on all host threads."""
     import g4oracle
     import build_oracle
     build_oracle.build_oracle()
-    ref = g4oracle.reference() if prefer_reference else None
-    kind = "reference" if ref is not None else "port"
-    lib = ref if ref is not None else g4oracle.oracle()
-    threads = 1 if ref is not None else nthreads
+    lib = g4oracle.oracle()
     lat, _, _ = workload_inputs()
-    import g4gpu
-    ns = max(threads, 1)
-    cur = flat_top(NS)[NS // 2 - ns // 2:NS // 2 - ns // 2 + ns]
-    sp = T.slice_params(ns, GAMMA0, 2.0, 0.4e-6, 15.0, currents=cur)
-    beam = g4gpu.host_load_beam(sp, NS // 2 - ns // 2, NPART, 4, 7, 1, LAMBDA0, 1.0)
-    fld = np.zeros((1, ns, NGRID * NGRID), dtype=np.complex128)
-    # one step first to size the sample
+    threads = max(nthreads, 1)
+    ns = threads
+    beam, cur, fld = cpu_sample(lib, ns)
+    kw = dict(time_run=1, nthreads=threads)
     t0 = time.perf_counter()
-    kw = dict(time_run=1)
-    if kind == "port":
-        kw["nthreads"] = threads
     lib.run_steps(lat[:1], GAMMA0, beam, cur, LAMBDA0, 1.0, [1], [GRIDMAX], fld, [0], **kw)
-    dt = time.perf_counter() - t0
-    nsteps = int(max(1, min(lat.shape[0], target_seconds / max(dt, 1e-6))))
+    dt1 = time.perf_counter() - t0
+    nsteps = int(max(1, min(lat.shape[0], target_seconds / max(dt1, 1e-6))))
+    ns = threads * int(max(1, round(target_seconds / max(dt1 * nsteps, 1e-6))))
+    beam, cur, fld = cpu_sample(lib, ns)
     t0 = time.perf_counter()
     lib.run_steps(lat[:nsteps], GAMMA0, beam, cur, LAMBDA0, 1.0, [1], [GRIDMAX], fld, [0], **kw)
     dt = time.perf_counter() - t0
-    return {"value": ns * nsteps / dt, "unit": "slice-steps/s", "cores": threads, "kind": kind,
+    return {"value": ns * nsteps / dt, "unit": "slice-steps/s", "cores": threads, "kind": "port",
             "sample": f"{ns} slices x {nsteps} steps of the workload (8192 particles, ngrid 151, "
-                      f"plain FP64), {threads} host thread(s), {dt:.1f} s"}
+                      f"plain FP64), {threads} host threads, {dt:.1f} s"}
 
 
 def run_reference_arm(args):
+    """The CPU implementation of the step on the host cores, on the workload's
+    metric and config: the C restatement of the reference (oracle/g4oracle.c, which is
+    bit-exact with the reference compiled from its own sources), all host threads,
+    each step a bounded sample of the window (full-size slices, one per thread times
+    REF_SLICES_PER_THREAD). The reference itself is x86 code built where its source
+    tree is; that tree is not present where this arm runs, so the port stands in."""
     ws, rank, _ = dist_setup()
     if rank != 0:
         return 0
@@ -701,19 +793,11 @@ def run_reference_arm(args):
     import build_oracle
     build_oracle.build_oracle()
     nthreads = os.cpu_count() or 1
-    ref = g4oracle.reference()
-    kind = "reference" if ref is not None else "port"
-    lib = ref if ref is not None else g4oracle.oracle()
+    lib = g4oracle.oracle()
     lat, _, _ = workload_inputs()
-    import g4gpu
-    ns = nthreads if kind == "port" else 2
-    cur = flat_top(NS)[NS // 2 - ns // 2:NS // 2 - ns // 2 + ns]
-    sp = T.slice_params(ns, GAMMA0, 2.0, 0.4e-6, 15.0, currents=cur)
-    beam = g4gpu.host_load_beam(sp, NS // 2 - ns // 2, NPART, 4, 7, 1, LAMBDA0, 1.0)
-    fld = np.zeros((1, ns, NGRID * NGRID), dtype=np.complex128)
-    kw = dict(time_run=1)
-    if kind == "port":
-        kw["nthreads"] = nthreads
+    ns = nthreads * REF_SLICES_PER_THREAD
+    beam, cur, fld = cpu_sample(lib, ns)
+    kw = dict(time_run=1, nthreads=nthreads)
     times = []
     state = (beam, fld, [0])
     for i in range(args.warmup + args.steps):
@@ -726,20 +810,23 @@ def run_reference_arm(args):
             times.append(dt)
     tot = sum(times)
     value = ns * args.steps / tot
+    sample = f"{ns} full-size slices of the window per step (8192 particles, ngrid 151), {args.steps} timed steps"
     line = {"metric": METRIC, "value": value, "unit": "slice-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": "time-dependent SASE, 4096 slices x 8192 particles, ngrid 151, ADI",
-                       "sample_per_step": f"{ns} slices x 1 integration step",
-                       "cache": "inputs larger than L2"},
-            "cpu_baseline": {"value": value, "unit": "slice-steps/s",
-                             "cores": nthreads if kind == "port" else 1, "kind": kind,
-                             "sample": f"{ns} full-size slices per step, {args.steps} timed steps"},
+            "config": {"workload": WORKLOAD, "form": "plain FP64 (the reference's arithmetic)",
+                       "cache": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{ws}",
+                       "sample_per_step": sample},
+            "cpu_baseline": {"value": value, "unit": "slice-steps/s", "cores": nthreads, "kind": "port",
+                             "sample": sample},
             "e2e": {"value": value, "unit": "slice-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+REF_SLICES_PER_THREAD = 2
 
 
 def main():
@@ -751,6 +838,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=None, help="timed steps of the plain form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-full-lattice", action="store_true",
+                    help="skip the mixed form's error after the whole 443-step lattice and its resonant companion")
     ap.add_argument("--nslice", type=int, default=None,
                     help="slices of the window (default 4096); smaller values are for profiling only")
     ap.add_argument("--forms", default="mixed,plain,batched,harmonic,learned,spacecharge",
@@ -799,19 +888,23 @@ def main():
     if do_plain:
         hp, ms_p, st_p = time_form(g4gpu, torch, g4gpu.PLAIN, beam, cur, lat, psteps, args.warmup)
         ms_p = max_over_ranks(ws, ms_p)
-    # error of the mixed form against the plain one after the same steps
-    err = None
+    # error of the mixed form against the plain one after the same steps, and after
+    # the whole lattice (both handles run on to its end)
+    err = err_full = err_res = None
     if do_plain and psteps == args.steps:
-        bm, fm = hm.diag(1)
-        bp, fp = hp.diag(1)
-        pw_m, pw_p = fm[0][:, 0], fp[0][:, 0]
-        err = {"power_max_rel": float(np.max(np.abs(pw_m - pw_p)) / max(np.max(np.abs(pw_p)), 1e-300)),
-               "energy_rel": float(abs(pw_m.sum() / pw_p.sum() - 1)) if pw_p.sum() > 0 else None,
-               "bunching_max_rel": float(np.max(np.abs(bm[:, 24] - bp[:, 24])) / np.max(np.abs(bp[:, 24]))),
-               "after_steps": args.warmup + args.steps}
+        err = mixed_error(hm, hp, args.warmup + args.steps)
+        if not args.no_full_lattice:
+            done = args.warmup + args.steps
+            nlat = lat.shape[0]
+            if done < nlat:
+                hm.run(done, nlat - done)
+                hp.run(done, nlat - done)
+            err_full = mixed_error(hm, hp, max(nlat, done))
     hm.close()
     if do_plain:
         hp.close()
+    if do_plain and not args.no_full_lattice:
+        err_res = resonant_companion(g4gpu, torch, shapes)
 
     value = job_value(ws, NS, args.steps, ms_m)
     plain_value = job_value(ws, NS, psteps, ms_p) if do_plain else None
@@ -839,6 +932,7 @@ def main():
 
     kernels = kernel_table(st_m, True)
     kernels_plain = kernel_table(st_p, False) if do_plain else None
+    fp64_g, fp64_src = fp64_peak(g4gpu, torch.cuda.current_device())
     dom = max(kernels, key=lambda k: kernels[k]["ms_total"])
     dk = kernels[dom]
 
@@ -846,8 +940,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_m / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
             "data": "synthetic",
-            "config": {"workload": "time-dependent SASE, 4096 slices x 8192 particles, ngrid 151, "
-                                   "ADI, 4x110-period planar undulator with FODO, shot noise seed 7",
+            "config": {"workload": WORKLOAD,
                        "form": "mixed (FP32 field/solver/deposition, phase as a 64-bit fixed-point turn count)",
                        "cache": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{ws}",
                        "launch_shapes": ({"push_block": shapes[0], "field_threads": shapes[1],
@@ -857,8 +950,12 @@ def main():
             "forms": {"mixed": {"value": value, "ms_per_step": ms_m / args.steps},
                       "plain_fp64": ({"value": plain_value, "ms_per_step": ms_p / psteps,
                                       "steps": psteps, "kernels": kernels_plain,
-                                      "fp64": fp64_roofline(kernels_plain)} if do_plain else None)},
+                                      "fp64": fp64_roofline(kernels_plain, fp64_g, fp64_src)} if do_plain
+                                     else None)},
+            "value_plain_fp64": plain_value,
             "mixed_error_vs_plain": err,
+            "mixed_error_vs_plain_full_lattice": err_full,
+            "mixed_error_vs_plain_resonant": err_res,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": dk.get("achieved_gbs"), "peak": peak,
                          "unit": "GB/s", "frac": dk.get("frac_hbm"),
                          "traffic": (TRAFFIC_PER_SLICE[dom] * NS if dom in TRAFFIC_PER_SLICE else None),
@@ -892,12 +989,16 @@ def main():
         del beam_q
     if rank == 0 and not args.no_e2e:
         field_pinned = torch.zeros((NS, NGRID * NGRID, 2), dtype=torch.float64).pin_memory()
-        t, h2d, d2h, phases = e2e_window(g4gpu, torch, g4gpu.MIXED, beam_pinned, cur, field_pinned, lat,
-                                         args.steps, 2, shapes=shapes)
+        times, h2d, d2h, phases = e2e_window(g4gpu, torch, g4gpu.MIXED, beam_pinned, cur, field_pinned, lat,
+                                             args.steps, E2E_WINDOWS, shapes=shapes)
+        t = statistics.median(times)
         line["e2e"] = {"value": NS * args.steps / t, "unit": "slice-steps/s",
                        "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-                       "window": f"upload beam+field, {args.steps} steps with every step's diagnostics (g4gpu_run_diag), download",
-                       "window_s": t, "phases_of_one_window": phases}
+                       "window": f"upload beam+field, {args.steps} steps with every step's diagnostics "
+                                 f"(g4gpu_run_diag), download; median of {len(times)} windows after one warm-up window",
+                       "window_s": t, "windows_s": times,
+                       "spread": (max(times) - min(times)) / t,
+                       "phases_of_one_window": phases}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1)
     if rank == 0:

@@ -944,12 +944,21 @@ __device__ __forceinline__ void bulk_load_issue(float2 *s, const float2 *g, int 
   if (head && threadIdx.x == 32) s[0] = g[0];
   if (tail && threadIdx.x == 64) s[count - 1] = g[count - 1];
 }
-// Waits for bulk_load_issue's copy (bounded) and makes it visible to the CTA.
-__device__ __forceinline__ bool bulk_load_wait(uint32_t bar, int *err) {
-  bool ok = mbar_wait(bar, 0, err);
-  __syncthreads();
+// The CTA's verdict on a bounded wait for a bulk copy: false for every thread if the
+// phase timed out for any of them (so that all threads leave together and none is
+// left at a later barrier). A copy that timed out gets one more bounded wait before
+// the CTA leaves, so that it is not still writing shared memory that the SM hands to
+// another CTA.
+__device__ __forceinline__ bool bulk_wait_uniform(uint32_t bar, uint32_t parity, int *err) {
+  const bool ok = __syncthreads_and(mbar_wait(bar, parity, err)) != 0;
+  if (!ok) {
+    mbar_wait(bar, parity, nullptr);
+    __syncthreads();
+  }
   return ok;
 }
+// Waits for bulk_load_issue's copy (bounded) and makes it visible to the CTA.
+__device__ __forceinline__ bool bulk_load_wait(uint32_t bar, int *err) { return bulk_wait_uniform(bar, 0, err); }
 __device__ __forceinline__ bool bulk_load(float2 *s, const float2 *g, int count, uint32_t bar, int *err) {
   bulk_load_issue(s, g, count, bar);
   return bulk_load_wait(bar, err);
@@ -1788,9 +1797,7 @@ __device__ __forceinline__ bool bulk_load_parity(float2 *s, const float2 *g, int
   }
   if (head && threadIdx.x == 32) s[0] = g[0];
   if (tail && threadIdx.x == 64) s[count - 1] = g[count - 1];
-  bool ok = mbar_wait(bar, parity, err);
-  __syncthreads();
-  return ok;
+  return bulk_wait_uniform(bar, parity, err);
 }
 
 // The ADI half steps of k_field_fused_f with the source read from a caller's array

@@ -8,7 +8,10 @@
 // by that many slice lengths. Every slice then holds its staying particles, in their
 // previous order, followed by the arrivals; the reference's removal by swapping with
 // the last element orders them differently, which changes only the summation order of
-// later per-slice sums.
+// later per-slice sums. The arrivals take their slots by atomic increments, so their
+// order behind the staying particles varies from run to run (and with it the
+// summation order); when a slice overflows its capacity, which arrivals are lost
+// varies too. The set of particles in a slice without overflow does not.
 //
 // Three kernels, one CTA per slice: (1) count each slice's staying particles and every
 // slice's arrivals; (2) compact the staying particles in order into the scratch arrays

@@ -150,3 +150,56 @@ void launch_convert_field(void *stream, const void *in, void *out, size_t n, int
 }
 
 }  // namespace g4
+
+// ---- FP64 instruction rate of the device (the roofline of the plain form) ----------
+
+namespace {
+
+// Eight independent chains of FP64 fused multiply-adds per thread: the FP64 pipe, not
+// the dependent latency, bounds the rate. x -> a x + b with |a| < 1 stays bounded.
+__global__ void k_dfma_chains(double *out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) x[k] = 1e-3 * (threadIdx.x + 1) + k;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = fma(x[k], a, b);
+  }
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += x[k];
+  out[blockIdx.x * (size_t)blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" int g4gpu_measure_fp64_rate(int device, double *instr_per_s) {
+  if (!instr_per_s) return G4GPU_ERR_ARG;
+  *instr_per_s = 0;
+  if (cudaSetDevice(device) != cudaSuccess) return G4GPU_ERR_CUDA;
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return G4GPU_ERR_CUDA;
+  const int threads = 256, blocks = nsm * 8, iters = 4096;
+  double *out = nullptr;
+  if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return G4GPU_ERR_NOMEM;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 0;
+  for (int rep = 0; rep < 4; rep++) {  // the first launch warms up; the best of the others
+    cudaEventRecord(e0);
+    k_dfma_chains<<<blocks, threads>>>(out, iters, 0.9999999, 1e-7);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && (best == 0 || ms < best)) best = ms;
+  }
+  const cudaError_t err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (err != cudaSuccess || best <= 0) return G4GPU_ERR_CUDA;
+  *instr_per_s = (double)blocks * threads * 8.0 * iters / (best * 1e-3);
+  return G4GPU_OK;
+}

@@ -54,6 +54,7 @@ ABI_SYMBOLS = [
     "g4gpu_dpi_info", "g4gpu_dpi_field", "g4gpu_dpi_beam", "g4gpu_dpi_field_from", "g4gpu_dpi_beam_from",
     "g4gpu_dpi_close", "g4gpu_get_stream",
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
+    "g4gpu_measure_fp64_rate",
     "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc", "g4gpu_host_single_wakes",
     "g4gpu_set_wake", "g4gpu_set_chicanes", "g4gpu_load_beam_counts", "g4gpu_get_counts", "g4gpu_sort",
     "g4gpu_apply_slippage", "g4gpu_set_incoherent", "g4gpu_h5_create", "g4gpu_h5_dataset", "g4gpu_h5_dataset_int",
@@ -142,6 +143,7 @@ def load_library(path=None):
     L.g4gpu_diag.argtypes = [vp, i, vp, vp]
     L.g4gpu_run_diag.argtypes = [vp, i, i, i, vp, vp]
     L.g4gpu_diag_fft.argtypes = [vp, vp]
+    L.g4gpu_measure_fp64_rate.argtypes = [i, pd]
     L.g4gpu_diag_global.argtypes = [P(Config), i, vp, vp, vp, vp, vp, vp]
     L.g4gpu_get_config.argtypes = [vp, P(Config)]
     L.g4gpu_dpi_open.argtypes = [ctypes.c_char_p, ctypes.c_char_p, i, P(vp), ctypes.c_char_p, i]

@@ -165,6 +165,9 @@ int g4gpu_get_counts(g4gpu_handle h, int *counts);
  * the reference returns, always 0 (its centre shift is off). Synchronous. A full window
  * (no counts) is left alone, as the reference skips sorting outside one4one runs.
  * G4GPU_ERR_STATE when a slice would exceed npart (the particles without room are lost).
+ * Arrivals are placed behind a slice's staying particles in an order that varies from
+ * run to run (atomic slot assignment), and so does which of them are lost on overflow;
+ * the particles of a slice that does not overflow are the same set every run.
  * The reference sorts at marker steps between the push and the field solve
  * (Gencore.cpp:121-132): g4gpu_run(h, i, 1, G4GPU_STAGE_PUSH), g4gpu_sort, then
  * g4gpu_run(h, i, 1, G4GPU_STAGE_FIELD | G4GPU_STAGE_SLIP). */
@@ -305,7 +308,8 @@ int g4gpu_diag_global(const g4gpu_config *cfg, int nharm, const double *current,
  * same way (Diagnostic::calc after every output step in Gencore::run,
  * src/Core/Gencore.cpp:102-160; written by Output::writeGroup at the end).
  * Synchronous: returns when the steps and all records are done; a device error raised
- * during any step fails the call. */
+ * during any step fails the call with G4GPU_ERR_DEVICE, and beam_out and field_out
+ * are then undefined (records of every step may already have been written). */
 int g4gpu_run_diag(g4gpu_handle h, int istep0, int nsteps, int nharm, double *beam_out, double *field_out);
 
 /* The CUDA stream (cudaStream_t) every kernel of h is queued on. */
@@ -323,6 +327,15 @@ int g4gpu_reset_stats(g4gpu_handle h);
 
 /* Bytes of device memory held by h. */
 size_t g4gpu_device_bytes(g4gpu_handle h);
+
+/* The FP64 instruction rate of a device, measured: a kernel of independent FP64
+ * fused multiply-add chains (eight per thread, eight CTAs of 256 threads per SM)
+ * timed by CUDA events, best of three launches after one warm-up. *instr_per_s
+ * receives FP64 instructions per second (an FMA counts once; DADD and DMUL issue
+ * at the same rate). This is the peak of the plain FP64 form's roofline: its push
+ * and ADI sweeps are bound by the FP64 pipe. Synchronous; allocates and frees a
+ * small output buffer. No reference counterpart. */
+int g4gpu_measure_fp64_rate(int device, double *instr_per_s);
 
 /* ---- CUDA graphs, launch-shape tuning, batched ensembles ------------------- */
 

@@ -165,3 +165,45 @@ def test_cluster_pair_field_kernel_matches_single_cta(lib, ng):
     assert rel_err(F1, F0) < (tol if ng <= 168 else 1e-2)
     assert np.max(np.abs(b1[:, 24] - b0[:, 24])) <= tol * np.max(np.abs(b0[:, 24])) + 1e-4
 
+
+
+def test_ensemble_members_match_oracle(lib, oracle):
+    """Members shaped like the uneven ensemble's draws, run as one batch in the mixed
+    form (captured graphs, launch shapes from the autotuner), each against the FP64
+    oracle (bit-exact with the reference): linear aw tapers over four modules, ngrid
+    201 (cluster-pair field kernel) and 255 (tiled two-pass ADI), npart 2048 and 16384,
+    a 1 kW seed over shot noise. Slice power within 1 % of the largest slice power,
+    bunching within 1 % of the largest plus 1e-3 (far below the shot-noise level
+    1/sqrt(npart) of these beams)."""
+    import g4gpu
+    import g4cases as T
+    specs = [(8, 2048, 201, 11, -0.015), (4, 16384, 255, 12, -0.007), (6, 4096, 101, 13, -0.02)]
+    cases, cfgs = [], []
+    for ns, npart, ngrid, seed, taper in specs:
+        cur = T.flat_top_current(ns, 1e-10, 1.0, 3000.0, ns * 1e-10 / 8)
+        sp = T.slice_params(ns, 11357.8, 2.0, 0.4e-6, 15.0, currents=cur)
+        beam = g4gpu.host_load_beam(sp, 0, npart, 4, seed, 1, 1e-10, 1.0)
+        lat = T.undulator_lattice(1.7, 0.015, 10, 4, 1e-10, 11357.8, quad_k1=1.5, quad_l=0.08, taper=taper)
+        gh = g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e3, 30e-6), 1e-4, ngrid)
+        fld = np.repeat(gh[None, :], ns, axis=0)
+        cases.append((lat, beam, cur, fld))
+        cfgs.append(g4gpu.Config(nslice=ns, npart=npart, ngrid=ngrid, gridmax=1e-4, lambda0=1e-10, sample=1.0,
+                                 gammaref=11357.8, precision=1, time_run=1))
+    with g4gpu.Batch(cfgs) as b:
+        for m, (lat, beam, cur, fld) in zip(b.members, cases):
+            m.set_lattice(lat)
+            m.load_beam(beam, cur)
+            m.load_field(0, fld)
+            m.autotune()
+        b.run(0, max(c[0].shape[0] for c in cases))
+        b.synchronize()
+        got = [m.diag(1) for m in b.members]
+    for (lat, beam, cur, fld), (bd, fd), (ns, npart, ngrid, _, taper) in zip(cases, got, specs):
+        assert abs(lat[-1, 0] / lat[0, 0] - 1 - taper) < 1e-12  # the taper spans the lattice
+        rp, rf, rfirst, _ = oracle.run_steps(lat, 11357.8, beam, cur, 1e-10, 1.0, [1], [1e-4], fld[None], [0],
+                                             nthreads=8)
+        of = oracle.diag_field(rf[0], 1e-4, 1e-10, 1, int(rfirst[0]))
+        ob = oracle.diag_beam(rp, 1)
+        assert of[:, 0].max() > 0
+        assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-2, (ngrid, npart)
+        assert np.max(np.abs(bd[:, 24] - ob[:, 24])) <= 1e-2 * np.max(ob[:, 24]) + 1e-3, (ngrid, npart)

@@ -719,3 +719,53 @@ def test_plugins_fed_from_the_device(lib, test_plugins, prec):
         with g4gpu.Plugin(test_plugins["beam"]) as p:
             out = p.beam_from(h, iz=3)
         assert np.allclose(out["mean_gamma"], beam[..., 0].mean(axis=1), rtol=1e-14)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_lasing_time_dependent_window_matches_oracle(lib, oracle, prec):
+    """A time-dependent window that lases: the first 550 steps of the reference's
+    Example1 lattice (helical, resonant at 1e-10 m, 2.99 slices of slippage per step;
+    tests/golden/example1.npz) on a periodic window of 16 slices of 2048 particles
+    (nbins 8, shot noise from seed 7, delgam 1.0), ngrid 101 over 2e-4 m, a 5 kW seed.
+    Against the FP64 oracle (bit-exact with the reference) every 110 steps: the plain
+    form within 1e-9, the mixed form within 1 % on slice power (of the largest slice
+    power) and bunching (of the largest bunching, plus an absolute 1e-3, below the
+    shot-noise level 1/sqrt(2048) = 0.022). The window energy grows 60-fold and the
+    bunching from 0.02 to 0.15 over the run (exponential gain in the last 220 steps)."""
+    import g4gpu
+    import g4cases as T
+    ns, npart, ng, gm, g0 = 16, 2048, 101, 2e-4, 11357.82
+    lat = golden("example1.npz")["lat"][:550]
+    cur = np.full(ns, 3000.0)
+    part = g4gpu.host_load_beam(T.slice_params(ns, g0, 1.0, 0.4e-6, 15.0, currents=cur), 0, npart, 8, 7, 1, 1e-10,
+                                1.0)
+    seed = g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 5e3, 30e-6), gm, ng)
+    fld = np.repeat(seed[None, :], ns, axis=0)
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, gridmax=gm, lambda0=1e-10, sample=1.0, gammaref=g0,
+                       precision=prec, time_run=1, periodic=1)
+    energies, bunch = [], []
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam(part, cur)
+        h.load_field(0, fld)
+        state = (part, fld[None], [0], None)
+        done = 0
+        for e in range(110, 551, 110):
+            h.run(done, e - done)
+            bd, fd = h.diag(1)
+            p, f, first, acc = oracle.run_steps(lat[done:e], g0, state[0], cur, 1e-10, 1.0, [1], [gm], state[1],
+                                                state[2], nthreads=8, accuslip=state[3], periodic=1)
+            state = (p, f, first, acc)
+            done = e
+            assert h.get_field(0)[1] == first[0]
+            of = oracle.diag_field(f[0], gm, 1e-10, 1, int(first[0]))
+            ob = oracle.diag_beam(p, 1)
+            energies.append(of[:, 0].sum())
+            bunch.append(ob[:, 24].max())
+            if prec == 0:
+                assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-9, e
+                assert rel_err(bd[:, 24], ob[:, 24]) < 1e-9, e
+            else:
+                assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-2, e
+                assert np.max(np.abs(bd[:, 24] - ob[:, 24])) <= 1e-2 * np.max(ob[:, 24]) + 1e-3, e
+    assert energies[-1] > 30 * energies[0] and bunch[-1] > 0.1, (energies, bunch)
