@@ -246,7 +246,10 @@ def kernel_alg_bytes(kernel, mixed, ns=None):
       adi_y       intermediate + source read, field written: same
       field       (fused mixed kernel) field read + written (16 B per cell) and the
                   particle coordinates the deposition needs (x, y, gamma FP32, theta
-                  FP64: 20 B per particle)"""
+                  FP64: 20 B per particle)
+      step        (the whole step of a slice in one kernel) particles read + written
+                  (56 B per particle) and the field read + written (16 B per cell): the
+                  step's algorithmic bytes"""
     ns = ns or NS
     ncell = NGRID * NGRID
     if kernel == "push":
@@ -255,6 +258,8 @@ def kernel_alg_bytes(kernel, mixed, ns=None):
         per = (24 if mixed else 48) * ncell
     elif kernel == "field":
         per = 16 * ncell + 20 * NPART
+    elif kernel == "step":
+        per = 56 * NPART + 16 * ncell
     else:
         return None
     return ns * per
@@ -711,33 +716,45 @@ def e2e_window(g4gpu, torch, precision, beam_pinned, cur, field_pinned, lat, ste
     cur_np = np.ascontiguousarray(cur)
     diag_out = (np.zeros((steps, NS, len(g4gpu.DB_COLS) + 2)), np.zeros((steps, 1, NS, len(g4gpu.DF_COLS))))
     times = []
+    gpu_phases = []
     d2h_diag = 0
+    stream = torch.cuda.ExternalStream(h.stream())
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     for rep in range(reps + 2):
         # the first window is the warm-up; the last one is split into its phases
         split = rep == reps + 1
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        ev[0].record(stream)
         h.load_beam_ptr(beam_pinned.data_ptr(), cur_np.ctypes.data)
         h.load_field_ptr(0, field_pinned.data_ptr())
+        ev[1].record(stream)
         if split:
             h.synchronize()
             t_up = time.perf_counter()
         # the steps, with the per-slice diagnostics of every step recorded on the
         # device and read back once (g4gpu_run_diag)
         bd, fd = h.run_diag(0, steps, 1, out=diag_out)
+        ev[2].record(stream)
         d2h_diag = bd.nbytes + fd.nbytes
         if split:
             t_steps = time.perf_counter()
         h.get_beam(out_beam.numpy())
         h.get_field(0, out_field.numpy().view(np.complex128).reshape(NS, NGRID * NGRID))
+        ev[3].record(stream)
         t1 = time.perf_counter()
         if split:
             phases = {"upload_s": t_up - t0, "steps_with_diag_s": t_steps - t_up, "download_s": t1 - t_steps}
         elif rep > 0:
             times.append(t1 - t0)
+            ev[3].synchronize()
+            # device time between the phase boundaries on the handle's stream (no
+            # synchronisation added inside the window)
+            gpu_phases.append([ev[k].elapsed_time(ev[k + 1]) / 1e3 for k in range(3)])
     h.close()
     h2d = beam_pinned.numel() * 8 + cur_np.nbytes + field_pinned.numel() * 8
     d2h = d2h_diag + out_beam.numel() * 8 + out_field.numel() * 8
+    phases["device_phases_s_per_window"] = gpu_phases
     return times, h2d, d2h, phases
 
 
@@ -751,7 +768,7 @@ def cpu_sample(lib, ns):
     return beam, cur, np.zeros((1, ns, NGRID * NGRID), dtype=np.complex128)
 
 
-def cpu_baseline(nthreads, target_seconds=15.0):
+def cpu_baseline(nthreads, target_seconds=20.0):
     """Times the oracle port (oracle/g4oracle.c, bit-exact with the reference) on a
     bounded sample of the workload: full-size slices (8192 particles, ngrid 151), as
     many steps of the lattice as fit and then as many slices (a multiple of the
@@ -944,7 +961,8 @@ def main():
                        "form": "mixed (FP32 field/solver/deposition, phase as a 64-bit fixed-point turn count)",
                        "cache": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{ws}",
                        "launch_shapes": ({"push_block": shapes[0], "field_threads": shapes[1],
-                                          "field_kernel": ["one CTA per slice", "cluster pair"][shapes[2]],
+                                          "field_kernel": ["one CTA per slice", "cluster pair",
+                                                           "whole step per CTA"][shapes[2]],
                                           "source": "--launch-shapes" if fixed else "g4gpu_autotune"}
                                          if shapes else "defaults")},
             "forms": {"mixed": {"value": value, "ms_per_step": ms_m / args.steps},

@@ -1084,7 +1084,23 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
     bool pair_ok = h->mixed && c.solver == G4GPU_SOLVER_ADI && ng <= g4::pair_max_ngrid();
     for (int k = 0; k < c.nfield; k++) pair_ok = pair_ok && sc.f[k].tw > 0;
     bool pair = pair_ok && (h->field_kernel == 1 || !fused);
-    if (fused || pair) {
+    // the whole step in one kernel (push, deposition, ADI; one CTA per slice): chosen
+    // by the autotuner (field_kernel 2) for one-field windows without space charge
+    const bool rec_ok = h->diag_rec && g4::fused_diag_fits(ng, h->field_threads, h->diag_nharm);
+    const bool step_fused = fused && h->field_kernel == 2 && do_push && do_field && !h->sc_on &&
+                            g4::step_fused_ok(c.nfield, ng, h->field_threads, rec_ok, rec_ok, h->diag_nharm);
+    if (step_fused) {
+      const char *cb = (const char *)h->coef + (size_t)sc.f[0].coef * 3 * ng * h->csize;
+      const int bw = g4::beam_diag_width(h->diag_nharm);
+      {
+        Timed t(h, G4GPU_K_STEP);
+        g4::launch_step_fused_mixed(L, scf_push, h->beam, h->field[0], cb, ns, np, ng, sc.f[0].dep_on,
+                                    h->field_threads, wake, isr, rec_ok ? h->diag_rec : nullptr,
+                                    rec_ok ? h->diag_rec + (size_t)ns * bw : nullptr, h->diag_nharm, c.gammaref);
+      }
+      if (isr.ctr) g4::launch_isr_advance(h->stream, h->isr_ctr);
+      if (rec_ok) h->diag_fields_in_step = h->diag_beam_in_step = true;
+    } else if (fused || pair) {
       g4::StepConstF scf = scf_push;
       if (do_push) push(nullptr, 0);
       if (do_field) {
@@ -1217,7 +1233,7 @@ int g4gpu_set_launch_shapes(g4gpu_handle h, int push_block, int field_threads, i
     return fail(h, G4GPU_ERR_ARG, "push_block must be a multiple of 32 in [32, 512]");
   if (field_threads < 2 * h->cfg.ngrid || field_threads > 1024 || field_threads % 32)
     return fail(h, G4GPU_ERR_ARG, "field_threads must be a multiple of 32 in [2 ngrid, 1024]");
-  if (field_kernel != 0 && field_kernel != 1) return fail(h, G4GPU_ERR_ARG, "field_kernel must be 0 or 1");
+  if (field_kernel < 0 || field_kernel > 2) return fail(h, G4GPU_ERR_ARG, "field_kernel must be 0, 1 or 2");
   h->push_block = push_block;
   h->field_threads = field_threads;
   h->field_kernel = field_kernel;
@@ -1560,14 +1576,15 @@ int g4gpu_run_diag(g4gpu_handle h, int istep0, int nsteps, int nharm, double *be
     // from the diagnostic kernels after the step
     h->diag_rec = h->ddiag + (size_t)s * rec;
     h->diag_nharm = nharm;
-    h->diag_fields_in_step = false;
+    h->diag_fields_in_step = h->diag_beam_in_step = false;
     rc = enqueue_steps(h, istep0 + s, 1, G4GPU_STAGE_ALL);
-    const bool fields_done = h->diag_fields_in_step;
+    const bool fields_done = h->diag_fields_in_step, beam_done = h->diag_beam_in_step;
     h->diag_rec = nullptr;
-    h->diag_fields_in_step = false;
+    h->diag_fields_in_step = h->diag_beam_in_step = false;
     if (rc) return rc;
     for (int k = 0; k < c.nfield; k++) firsts[(size_t)s * G4GPU_MAX_FIELDS + k] = h->first[k];
-    enqueue_diag(h, nharm, h->ddiag + (size_t)s * rec, beam_out != nullptr, field_out != nullptr && !fields_done);
+    enqueue_diag(h, nharm, h->ddiag + (size_t)s * rec, beam_out != nullptr && !beam_done,
+                 field_out != nullptr && !fields_done);
     G4_CUDA(h, cudaGetLastError());
     G4_CUDA(h, cudaMemcpyAsync(h->hdiag + (size_t)s * rec, h->ddiag + (size_t)s * rec, rec * sizeof(double),
                                cudaMemcpyDeviceToHost, h->stream));
@@ -1731,10 +1748,10 @@ extern "C" int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_thread
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  auto time_step = [&](int pb, int ft, float *ms) -> int {
+  auto time_step = [&](int pb, int ft, float *ms, int fk = 0) -> int {
     h->push_block = pb;
     h->field_threads = ft;
-    h->field_kernel = 0;
+    h->field_kernel = fk;
     float best = 1e30f;
     for (int rep = 0; rep < 3; rep++) {  // first repetition warms up
       restore_state(h, b, false);
@@ -1793,6 +1810,28 @@ extern "C" int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_thread
       }
       h->field_kernel = 0;
       if (!rc && pms < single) best_fk = 1;
+    }
+  }
+  // the whole step in one kernel, over its CTA sizes (each with its own particles per
+  // lane), against the best of the above
+  if (!rc && fused && c.nfield == 1 && !h->sc_on) {
+    float cur = 1e30f;
+    if (!(rc = time_step(best_pb, best_ft, &cur, best_fk))) {
+      int step_ft = 0;
+      float step_ms = 1e30f;
+      for (int ft : fields) {
+        if (ft != (2 * c.ngrid + 31) / 32 * 32 && ft < 512) continue;
+        float ms;
+        if ((rc = time_step(best_pb, ft, &ms, 2))) break;
+        if (ms < step_ms) {
+          step_ms = ms;
+          step_ft = ft;
+        }
+      }
+      if (!rc && step_ms < cur) {
+        best_fk = 2;
+        best_ft = step_ft;
+      }
     }
   }
   cudaEventDestroy(e0);

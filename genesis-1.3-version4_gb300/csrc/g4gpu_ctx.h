@@ -39,10 +39,12 @@ struct g4gpu_ctx {
   size_t ddiag_bytes = 0;
   double *hdiag = nullptr;  // pinned host copy of ddiag (the per-step read-back)
   // g4gpu_run_diag: the record of the step being queued (null otherwise), its
-  // harmonics, and whether the step's kernels formed the fields' part of it
+  // harmonics, and whether the step's kernels formed the fields' (and the beam's) part
+  // of it
   double *diag_rec = nullptr;
   int diag_nharm = 0;
   bool diag_fields_in_step = false;
+  bool diag_beam_in_step = false;
   // space charge (g4gpu_set_efield): its parameters and device state
   bool sc_on = false;
   int sc_ngrid = 0, sc_nz = 0, sc_nphi = 0, sc_longrange = 0;

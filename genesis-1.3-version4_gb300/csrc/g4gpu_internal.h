@@ -165,6 +165,16 @@ struct IsrStream {
 };
 void launch_isr_advance(void *stream, unsigned long long *ctr);
 
+// The whole step of a one-field window in one kernel, one CTA per slice: push,
+// deposition and ADI (mixed form, slice in shared memory, no space charge). Usable
+// where step_fused_ok; threads, dbeam, dfield as launch_field_fused_mixed's; wake and
+// isr as the push's.
+bool step_fused_ok(int nfield, int ngrid, int threads, bool dbeam, bool dfield, int nharm);
+void launch_step_fused_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b, void *field,
+                             const void *coef, int ns, int np, int ngrid, int deposit, int threads,
+                             const void *wake, const IsrStream &isr, double *dbeam, double *dfield, int nharm,
+                             double gref);
+
 // Space charge (&efield, EFieldSolver.cpp), sc_kernels.cuh, instantiated in
 // kernels_plain.cu (FP64) and kernels_mixed.cu (FP32).
 struct ScConst {

@@ -301,33 +301,16 @@ __device__ __forceinline__ void deposit_f(const StepConstF &sc, const PtrsF &p, 
   }
 }
 
+// Beam::track of one particle of slice `is` after its first transverse half step
+// (Beam.cpp:97-112): the field gather of BeamSolver::advance (BeamSolver.cpp:48-86)
+// from fslice[k], the storage slice of field k this beam slice sees, RK4 of the
+// energy offset and phase, incoherent radiation, wakes, R56, the second transverse
+// half step. th already holds the autophase shift.
 template <int NF>
-__global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, int np, int ng,
-                                                int deposit) {
-  int is = blockIdx.y;
-  int ip = blockIdx.x * blockDim.x + threadIdx.x;
-  // lanes past the slice's particles stay for the deposition's warp shuffles
-  const bool valid = ip < slice_np_f(p, is, np);
-  if (!valid && !deposit) return;
-  size_t o = (size_t)is * np + (valid ? ip : 0);
+__device__ __forceinline__ void push_rest_f(const StepConstF &sc, const PtrsF &p, const float2 *const *fslice,
+                                            int is, int ip, int ng, float ez, float &dg, long long &th, float &x,
+                                            float &y, float &px, float &py) {
   const float g0 = (float)sc.gammaref;
-  float dg = p.dg[o], x = p.x[o], y = p.y[o], px = p.px[o], py = p.py[o];
-  long long th = p.theta[o] + sc.autophase_q;
-  size_t ncell = (size_t)ng * ng;
-
-  if (p.mode != 2) transverse_f(sc, false, g0 + dg, x, y, px, py);
-  if (p.mode == 1) {
-    if (valid) {
-      p.x[o] = x;
-      p.y[o] = y;
-      p.px[o] = px;
-      p.py[o] = py;
-    }
-    return;
-  }
-  // BeamSolver.cpp:50, 61: ez = the particle's short-range field + the slice's loss
-  const float ez = (p.ez ? p.ez[o] : 0.f) + (p.eloss ? (float)p.eloss[is] : 0.f);
-
   // the step works on FP32 offsets from the reduced phase
   float a0 = phase_of(th);
 
@@ -339,8 +322,7 @@ __global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, 
   for (int k = 0; k < NF; k++) {
     if (k >= sc.nfld) break;
     const FieldStepF &fs = sc.f[k];
-    int islice = (is + fs.first) % ns;
-    const float2 *f = p.field[k] + (size_t)islice * ncell;
+    const float2 *f = fslice[k];
     CellF c;
     if (ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x, y, c)) {
       float2 v00 = f[c.i00], v10 = f[c.i10], v01 = f[c.i01], v11 = f[c.i11];
@@ -376,9 +358,41 @@ __global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, 
   th = add_phase(th, dth);
   // TrackBeam::applyR56 (TrackBeam.cpp:260-277): gamma - gamma0 is the stored offset
   if (sc.chic) th = add_phase(th, sc.r56 * dg);
-  float g = g0 + dg;
+  transverse_f(sc, true, g0 + dg, x, y, px, py);
+}
 
-  transverse_f(sc, true, g, x, y, px, py);
+template <int NF>
+__global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, int np, int ng,
+                                                int deposit) {
+  int is = blockIdx.y;
+  int ip = blockIdx.x * blockDim.x + threadIdx.x;
+  // lanes past the slice's particles stay for the deposition's warp shuffles
+  const bool valid = ip < slice_np_f(p, is, np);
+  if (!valid && !deposit) return;
+  size_t o = (size_t)is * np + (valid ? ip : 0);
+  const float g0 = (float)sc.gammaref;
+  float dg = p.dg[o], x = p.x[o], y = p.y[o], px = p.px[o], py = p.py[o];
+  long long th = p.theta[o] + sc.autophase_q;
+  size_t ncell = (size_t)ng * ng;
+
+  if (p.mode != 2) transverse_f(sc, false, g0 + dg, x, y, px, py);
+  if (p.mode == 1) {
+    if (valid) {
+      p.x[o] = x;
+      p.y[o] = y;
+      p.px[o] = px;
+      p.py[o] = py;
+    }
+    return;
+  }
+  // BeamSolver.cpp:50, 61: ez = the particle's short-range field + the slice's loss
+  const float ez = (p.ez ? p.ez[o] : 0.f) + (p.eloss ? (float)p.eloss[is] : 0.f);
+  const float2 *fslice[NF];
+#pragma unroll
+  for (int k = 0; k < NF; k++) fslice[k] = k < sc.nfld ? p.field[k] + (size_t)((is + sc.f[k].first) % ns) * ncell
+                                                       : nullptr;
+  push_rest_f<NF>(sc, p, fslice, is, ip, ng, ez, dg, th, x, y, px, py);
+  const float g = g0 + dg;
 
   if (valid) {
     p.dg[o] = dg;
@@ -1201,6 +1215,141 @@ __global__ void __launch_bounds__(kFusedMaxThreads, 1)
   __syncthreads();
   bulk_store(u, S, ncell);
   // the field record of storage slice i, read from S alongside the store
+  if (dfield) slice_field_sums(S, ng, dsh, dres, dfield + (size_t)i * (kFieldSums + 2));
+  if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
+// ---- the whole step of one slice in one CTA: push, deposition and ADI -----------
+//
+// One CTA per slice of a one-field window (mixed form, slice in shared memory, no
+// space charge). Beam slice `is` sees only field storage slot (is + first) % ns in its
+// push, and that slot's solve uses only beam slice `is` (BeamSolver.cpp:66,
+// FieldSolverADI.cpp:11-55), so the slice's whole step runs on chip:
+//   S = u                                   bulk load of the field slice
+//   S = (I + c Dy) S = S1                    column pass
+//   push every particle of the slice        gathering from u, still unmodified in
+//                                           global memory (and in L2 from the load),
+//                                           storing it and depositing it at once:
+//                                           S = S1 + src
+//   row sweeps, 2 u' - S1, column sweeps, bulk store, as k_field_fused_f.
+// Against the push kernel followed by k_field_fused_f, the particles are read and
+// written once and never read again for the deposition, the push's field gather
+// and the second right-hand side hit L2, and one launch replaces two. Each lane
+// takes U particles per round (their loads issued together); the 32 lanes of a warp
+// hold consecutive particles, so deposit_lanes sums the beamlets that share a cell.
+template <int U, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1)
+    k_step_fused_f(StepConstF sc, PtrsF p, float2 *__restrict__ field, const float2 *__restrict__ coef,
+                   int ns, int np, int ng, int deposit, int *err, double *dbeam, double *dfield, int nharm,
+                   double gref) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ncell = ng * ng;
+  const FieldStepF &fs = sc.f[0];
+  const int is = blockIdx.x;
+  const int i = (is + fs.first) % ns;
+  float2 *u = field + (size_t)i * ncell;
+  // shared layout as k_field_fused_f's
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);
+  float2 *K = reinterpret_cast<float2 *>(smem_raw + 8);
+  float2 *C = reinterpret_cast<float2 *>(smem_raw + 16);
+  float2 *CB = C + ng, *CW = CB + ng;
+  size_t soff = (16 + 3 * (size_t)ng * 8 + 15) & ~(size_t)15;
+  soff += reinterpret_cast<uintptr_t>(u) & 15;
+  float2 *S = reinterpret_cast<float2 *>(smem_raw + soff);
+  const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int t = threadIdx.x; t < 3 * ng; t += blockDim.x) C[t] = coef[t];
+  __syncthreads();
+  const float2 a = C[1];
+  if (threadIdx.x == 0) {
+    const int m = ng / 2;
+    float2 bm = make_float2(CB[0].x, -CB[0].y);
+    const float n0 = CB[0].x * CB[0].x + CB[0].y * CB[0].y;
+    bm.x /= n0;
+    bm.y /= n0;
+    const float2 t1 = cmulf(a, CW[m]), t2 = cmulf(a, CW[ng - 1 - m]);
+    const float2 den = make_float2(bm.x - t1.x - t2.x, bm.y - t1.y - t2.y);
+    const float nd = den.x * den.x + den.y * den.y;
+    K[0] = make_float2(den.x / nd, -den.y / nd);
+  }
+  double *dsh = reinterpret_cast<double *>(smem_raw + ((soff + (size_t)ncell * 8 + 15) & ~(size_t)15));
+  double *dres = dsh + (blockDim.x >> 5) * kFusedDiagValues;
+  bulk_load_issue(S, u, ncell, bar_s);
+  if (!bulk_load_wait(bar_s, err)) return;
+  const float cs = fs.cstep;
+  const int tid = threadIdx.x;
+  const int nseg = max(1, min((int)blockDim.x / ng, 8));
+  stencil_cols_seg(S, ng, cs, nseg);  // S1 = (I + c Dy) u
+  __syncthreads();
+
+  // push and deposit: S = S1 + src
+  {
+    const int n = slice_np_f(p, is, np);
+    const float scl = fs.dep_scl * slice_cur_f(p, is, np);
+    const float2 *fslice[1] = {u};
+    const size_t base = (size_t)is * np;
+    const int lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+    const float g0 = (float)sc.gammaref;
+    const float ez = p.eloss ? (float)p.eloss[is] : 0.f;
+    for (int w0 = warp * 32 * U; w0 < n; w0 += nwarp * 32 * U) {
+      float dg[U], x[U], y[U], px[U], py[U];
+      long long th[U];
+#pragma unroll
+      for (int v = 0; v < U; v++) {
+        const int ip = w0 + v * 32 + lane;
+        const bool in = ip < n;
+        const size_t o = base + (in ? ip : 0);
+        dg[v] = p.dg[o];
+        x[v] = p.x[o];
+        y[v] = p.y[o];
+        px[v] = p.px[o];
+        py[v] = p.py[o];
+        th[v] = p.theta[o];
+      }
+#pragma unroll
+      for (int v = 0; v < U; v++) {
+        const int ip = w0 + v * 32 + lane;
+        const bool in = ip < n;
+        if (in) {
+          th[v] += sc.autophase_q;
+          transverse_f(sc, false, g0 + dg[v], x[v], y[v], px[v], py[v]);
+          push_rest_f<1>(sc, p, fslice, is, ip, ng, ez, dg[v], th[v], x[v], y[v], px[v], py[v]);
+          const size_t o = base + ip;
+          p.dg[o] = dg[v];
+          p.theta[o] = th[v];
+          p.x[o] = x[v];
+          p.y[o] = y[v];
+          p.px[o] = px[v];
+          p.py[o] = py[v];
+        }
+        if (deposit)
+          deposit_lanes(sc, fs, scl, S, ng, in ? x[v] : 1e30f, in ? y[v] : 1e30f, th[v], dg[v]);
+      }
+    }
+  }
+  __syncthreads();
+  // the beam record of this slice, from the pushed particles (read back from L2)
+  if (dbeam) slice_beam_sums(p, gref, is, np, nharm, dsh, dres, dbeam + (size_t)is * beam_diag_width(nharm));
+  const float2 invden = K[0];
+  const int line = tid >> 1, up = tid & 1;
+  const bool segmented = fs.tw > 0 && nseg >= 2;
+  const unsigned mask = __ballot_sync(0xffffffffu, line < ng);
+  if (segmented)
+    thomas_seg(S, ng, 1, ng, nseg, fs.tw, C, CB, CW);  // rows: u'
+  else if (line < ng)
+    thomas2(S + line * ng, 1, ng, up, CB, CW, a, invden, mask);
+  __syncthreads();
+  r2_cols_seg(S, u, ng, cs, nseg);  // 2 u' - S1
+  __syncthreads();
+  if (segmented)
+    thomas_seg(S, 1, ng, ng, nseg, fs.tw, C, CB, CW);  // columns
+  else if (line < ng)
+    thomas2(S + line, ng, ng, up, CB, CW, a, invden, mask);
+  __syncthreads();
+  bulk_store(u, S, ncell);
   if (dfield) slice_field_sums(S, ng, dsh, dres, dfield + (size_t)i * (kFieldSums + 2));
   if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
@@ -2073,6 +2222,55 @@ void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, cons
   PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
   k_field_fused_f<<<ns, threads, smem, (cudaStream_t)L.stream>>>(
       sc, k, p, (float2 *)field, (const float2 *)coef, ns, np, ngrid, deposit, L.err, dbeam, dfield, nharm, gref);
+}
+
+// k_step_fused_f's particles per lane and round (their loads in flight together) by
+// CTA size: the register cap of 1024 threads (64) holds one particle's push, that of
+// 768 threads (85) two, of 512 threads (128) four.
+template <int U, int MAXT>
+void launch_step_variant(cudaStream_t st, int threads, size_t smem, const StepConstF &sc, const PtrsF &p,
+                         float2 *field, const float2 *coef, int ns, int np, int ng, int deposit, int *err,
+                         double *dbeam, double *dfield, int nharm, double gref) {
+  static std::atomic<unsigned long long> configured{0};  // one bit per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !(configured.load() & (1ull << dev))) {
+    cudaFuncSetAttribute(k_step_fused_f<U, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    configured.fetch_or(1ull << dev);
+  }
+  k_step_fused_f<U, MAXT><<<ns, threads, smem, st>>>(sc, p, field, coef, ns, np, ng, deposit, err, dbeam, dfield,
+                                                       nharm, gref);
+}
+
+bool step_fused_ok(int nfield, int ngrid, int threads, bool dbeam, bool dfield, int nharm) {
+  if (nfield != 1 || ngrid > fused_max_ngrid()) return false;
+  if ((dbeam || dfield) && !fused_diag_fits(ngrid, threads, nharm)) return false;
+  return true;
+}
+
+void launch_step_fused_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b, void *field,
+                             const void *coef, int ns, int np, int ngrid, int deposit, int threads,
+                             const void *wake, const IsrStream &isr, double *dbeam, double *dfield, int nharm,
+                             double gref) {
+  threads = fused_threads(ngrid, threads);
+  const size_t smem = (dbeam || dfield) ? fused_diag_smem_bytes(ngrid, threads) : fused_smem_bytes(ngrid);
+  void *const fld[1] = {field};
+  PtrsF p = make_ptrs_f(b, fld, nullptr, 1);
+  if (isr.ctr && (sc.isr_avg != 0 || sc.isr_sig != 0)) p.isr = isr;
+  p.mode = 0;
+  p.wake = (const float *)wake;
+  cudaStream_t st = (cudaStream_t)L.stream;
+  float2 *f = (float2 *)field;
+  const float2 *cf = (const float2 *)coef;
+  if (threads <= 512)
+    launch_step_variant<4, 512>(st, threads, smem, sc, p, f, cf, ns, np, ngrid, deposit, L.err, dbeam, dfield,
+                                nharm, gref);
+  else if (threads <= 768)
+    launch_step_variant<2, 768>(st, threads, smem, sc, p, f, cf, ns, np, ngrid, deposit, L.err, dbeam, dfield,
+                                nharm, gref);
+  else
+    launch_step_variant<1, kFusedMaxThreads>(st, threads, smem, sc, p, f, cf, ns, np, ngrid, deposit, L.err,
+                                             dbeam, dfield, nharm, gref);
 }
 
 int pair_max_ngrid() {

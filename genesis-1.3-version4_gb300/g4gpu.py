@@ -43,7 +43,7 @@ G4GPU_DPI_FIELD, G4GPU_DPI_BEAM = 0, 1
 DBG_COLS = ["energy", "energyspread", "xposition", "xsize", "yposition", "ysize"]
 DFG_COLS = ["energy", "xposition", "xsize", "yposition", "ysize", "intensity-nearfield",
             "intensity-farfield", "xpointing", "xdivergence", "ypointing", "ydivergence"]
-KERNEL_CLASSES = ["push", "adi_x", "adi_y", "fft", "slip", "diag", "misc", "sc", "sc_field"]
+KERNEL_CLASSES = ["push", "adi_x", "adi_y", "fft", "slip", "diag", "misc", "sc", "sc_field", "step"]
 
 # exported symbols of include/g4gpu.h
 ABI_SYMBOLS = [

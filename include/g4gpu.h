@@ -320,7 +320,9 @@ int g4gpu_get_stream(g4gpu_handle h, void **stream);
  * (G4GPU_K_*) the launch count and the summed device time in milliseconds of the
  * launches since the last reset. The launch counter runs always. */
 enum { G4GPU_K_PUSH, G4GPU_K_ADI_X, G4GPU_K_ADI_Y, G4GPU_K_FFT, G4GPU_K_SLIP, G4GPU_K_DIAG,
-       G4GPU_K_MISC, G4GPU_K_SC, G4GPU_K_SC_FIELD, G4GPU_K_NCLASS };
+       G4GPU_K_MISC, G4GPU_K_SC, G4GPU_K_SC_FIELD,
+       G4GPU_K_STEP, /* the whole step of a slice in one kernel (launch shape field_kernel 2) */
+       G4GPU_K_NCLASS };
 int g4gpu_set_profiling(g4gpu_handle h, int on);
 int g4gpu_kernel_stats(g4gpu_handle h, long long *launches, double *ms);
 int g4gpu_reset_stats(g4gpu_handle h);
@@ -351,15 +353,18 @@ int g4gpu_set_graph_mode(g4gpu_handle h, int on);
  * (one step per candidate; beam and field are restored afterwards) and keeps the
  * fastest: threads per block of the push, threads per CTA of the fused field
  * kernel, and the fused field kernel itself (0: one CTA per slice, 1: a cluster of
- * two CTAs per slice, each holding half the rows). Choices are cached per
+ * two CTAs per slice, each holding half the rows, 2: the whole step of a slice in
+ * one CTA, push, deposition and ADI, for one-field windows without space charge;
+ * steps it does not apply to run kernel 0). Choices are cached per
  * (precision, npart, ngrid, nfield, solver) for the life of the process. Requires
  * the lattice, beam and fields to be loaded. *push_block, *field_threads and
  * *field_kernel (each may be NULL) receive the choice. No reference counterpart. */
 int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_threads, int *field_kernel);
 /* Sets the launch shapes g4gpu_autotune would choose: push_block a multiple of 32 in
  * [32, 512], field_threads a multiple of 32 in [2 ngrid, 1024] (mixed ADI form), and
- * field_kernel 0 or 1; other values are rejected with G4GPU_ERR_ARG. The pair kernel
- * runs only where its segmented solves apply; elsewhere the single-CTA kernel does. No
+ * field_kernel 0, 1 or 2; other values are rejected with G4GPU_ERR_ARG. The pair kernel
+ * runs only where its segmented solves apply, the whole-step kernel only on one-field
+ * windows without space charge; elsewhere the single-CTA field kernel does. No
  * reference counterpart. */
 int g4gpu_set_launch_shapes(g4gpu_handle h, int push_block, int field_threads, int field_kernel);
 
