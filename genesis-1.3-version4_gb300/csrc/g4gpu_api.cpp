@@ -974,6 +974,75 @@ static int apply_slippage(g4gpu_handle h, int k, double slippage) {
   return G4GPU_OK;
 }
 
+// ---- sharded windows: the slippage exchange between ranks --------------------------
+
+extern "C" int g4gpu_slip_shifts(double *accuslip, double slippage, double sample, int *direction) {
+  if (!accuslip || !direction || !std::isfinite(slippage) || !(sample > 0)) return -1;
+  // Control::applySlippage (Control.cpp:161-186): the shifts the accumulated slippage
+  // yields, each moving it by one sample towards zero
+  *accuslip += slippage;
+  int n = 0, dir = 1;
+  while (std::fabs(*accuslip) > (sample * 0.8)) {
+    if (*accuslip < 0) dir = -1;
+    *accuslip -= sample * dir;
+    n++;
+  }
+  *direction = dir;
+  return n;
+}
+
+int g4gpu_slip_count(g4gpu_handle h, int ifld, double slippage, int *nshift, int *direction) {
+  if (!h || !nshift || !direction) return fail(h, G4GPU_ERR_ARG, "null argument");
+  if (ifld < 0 || ifld >= h->cfg.nfield) return fail(h, G4GPU_ERR_ARG, "field index out of range");
+  if (!std::isfinite(slippage)) return fail(h, G4GPU_ERR_ARG, "slippage must be finite");
+  *nshift = 0;
+  *direction = 1;
+  if (!h->cfg.time_run) return G4GPU_OK;  // Control.cpp:159
+  *nshift = g4gpu_slip_shifts(&h->accuslip[ifld], slippage, h->cfg.sample, direction);
+  return G4GPU_OK;
+}
+
+size_t g4gpu_slice_bytes(g4gpu_handle h) {
+  return h ? (size_t)h->cfg.ngrid * h->cfg.ngrid * h->csize : 0;
+}
+
+int g4gpu_shift_out(g4gpu_handle h, int ifld, int direction, void *send) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (ifld < 0 || ifld >= h->cfg.nfield) return fail(h, G4GPU_ERR_ARG, "field index out of range");
+  if (direction != 1 && direction != -1) return fail(h, G4GPU_ERR_ARG, "direction must be +1 or -1");
+  if (h->shift_slot[ifld] >= 0) return fail(h, G4GPU_ERR_STATE, "g4gpu_shift_in of the previous shift is missing");
+  cudaSetDevice(h->cfg.device);
+  const int ns = h->cfg.nslice;
+  const size_t bytes = g4gpu_slice_bytes(h);
+  // the slice leaving the block: the head (window slice ns - 1) forwards, the tail
+  // (window slice 0) backwards (Control.cpp:199-204)
+  int last = (h->first[ifld] + ns - 1) % ns;
+  if (direction < 0) last = (last + 1) % ns;
+  if (send)
+    G4_CUDA(h, cudaMemcpyAsync(send, (char *)h->field[ifld] + (size_t)last * bytes, bytes, cudaMemcpyDeviceToDevice,
+                               h->stream));
+  // its slot becomes the entering slice (Control.cpp:268-272)
+  h->first[ifld] = direction > 0 ? last : (last + 1) % ns;
+  h->shift_slot[ifld] = last;
+  return G4GPU_OK;
+}
+
+int g4gpu_shift_in(g4gpu_handle h, int ifld, const void *recv) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (ifld < 0 || ifld >= h->cfg.nfield) return fail(h, G4GPU_ERR_ARG, "field index out of range");
+  const int slot = h->shift_slot[ifld];
+  if (slot < 0) return fail(h, G4GPU_ERR_STATE, "no g4gpu_shift_out before g4gpu_shift_in");
+  cudaSetDevice(h->cfg.device);
+  const size_t bytes = g4gpu_slice_bytes(h);
+  char *dst = (char *)h->field[ifld] + (size_t)slot * bytes;
+  if (recv)
+    G4_CUDA(h, cudaMemcpyAsync(dst, recv, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  else
+    G4_CUDA(h, cudaMemsetAsync(dst, 0, bytes, h->stream));
+  h->shift_slot[ifld] = -1;
+  return G4GPU_OK;
+}
+
 int g4gpu_apply_slippage(g4gpu_handle h, int ifld, double slippage) {
   if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
   if (ifld < 0 || ifld >= h->cfg.nfield) return fail(h, G4GPU_ERR_ARG, "field index out of range");

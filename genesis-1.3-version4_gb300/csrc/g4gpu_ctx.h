@@ -80,6 +80,9 @@ struct g4gpu_ctx {
   std::vector<double> slip;
   int first[G4GPU_MAX_FIELDS] = {};
   double accuslip[G4GPU_MAX_FIELDS] = {};
+  // sharded windows: the storage slot g4gpu_shift_out freed for the entering slice
+  // (-1: none pending)
+  int shift_slot[G4GPU_MAX_FIELDS] = {-1, -1, -1, -1, -1, -1, -1, -1};
   bool beam_loaded = false;
   bool field_loaded[G4GPU_MAX_FIELDS] = {};
 

@@ -54,7 +54,8 @@ ABI_SYMBOLS = [
     "g4gpu_dpi_info", "g4gpu_dpi_field", "g4gpu_dpi_beam", "g4gpu_dpi_field_from", "g4gpu_dpi_beam_from",
     "g4gpu_dpi_close", "g4gpu_get_stream",
     "g4gpu_set_profiling", "g4gpu_kernel_stats", "g4gpu_reset_stats", "g4gpu_device_bytes",
-    "g4gpu_measure_fp64_rate",
+    "g4gpu_measure_fp64_rate", "g4gpu_slip_shifts", "g4gpu_slip_count", "g4gpu_slice_bytes",
+    "g4gpu_shift_out", "g4gpu_shift_in",
     "g4gpu_host_load_beam", "g4gpu_host_gauss_hermite", "g4gpu_host_fc", "g4gpu_host_single_wakes",
     "g4gpu_set_wake", "g4gpu_set_chicanes", "g4gpu_load_beam_counts", "g4gpu_get_counts", "g4gpu_sort",
     "g4gpu_apply_slippage", "g4gpu_set_incoherent", "g4gpu_h5_create", "g4gpu_h5_dataset", "g4gpu_h5_dataset_int",
@@ -144,6 +145,12 @@ def load_library(path=None):
     L.g4gpu_run_diag.argtypes = [vp, i, i, i, vp, vp]
     L.g4gpu_diag_fft.argtypes = [vp, vp]
     L.g4gpu_measure_fp64_rate.argtypes = [i, pd]
+    L.g4gpu_slip_shifts.argtypes = [pd, d, d, P(i)]
+    L.g4gpu_slip_count.argtypes = [vp, i, d, P(i), P(i)]
+    L.g4gpu_slice_bytes.argtypes = [vp]
+    L.g4gpu_slice_bytes.restype = ctypes.c_size_t
+    L.g4gpu_shift_out.argtypes = [vp, i, i, vp]
+    L.g4gpu_shift_in.argtypes = [vp, i, vp]
     L.g4gpu_diag_global.argtypes = [P(Config), i, vp, vp, vp, vp, vp, vp]
     L.g4gpu_get_config.argtypes = [vp, P(Config)]
     L.g4gpu_dpi_open.argtypes = [ctypes.c_char_p, ctypes.c_char_p, i, P(vp), ctypes.c_char_p, i]
@@ -251,6 +258,17 @@ def host_gauss_hermite(par, gridmax, ngrid):
     if rc:
         raise G4Error(rc, "host_gauss_hermite: invalid arguments")
     return out[:, 0] + 1j * out[:, 1]
+
+
+def slip_shifts(accuslip, slippage, sample):
+    """Control::applySlippage's bookkeeping on the host (g4gpu_slip_shifts): returns
+    (shifts, direction, new accumulated slippage)."""
+    acc = ctypes.c_double(float(accuslip))
+    dr = ctypes.c_int()
+    n = _lib().g4gpu_slip_shifts(ctypes.byref(acc), float(slippage), float(sample), ctypes.byref(dr))
+    if n < 0:
+        raise ValueError("invalid slippage arguments")
+    return n, dr.value, acc.value
 
 
 def host_fc(aw, helical, h):
@@ -384,6 +402,27 @@ class Handle:
     def apply_slippage(self, ifld, slippage):
         """Control::applySlippage of field ifld outside the step loop."""
         self._check(self.L.g4gpu_apply_slippage(self.h, int(ifld), float(slippage)))
+
+    # ---- a window sharded over ranks (one handle per rank) ----
+    def slip_count(self, ifld, slippage):
+        """(shifts, direction) the step's slippage yields for field ifld
+        (g4gpu_slip_count: Control::applySlippage's bookkeeping)."""
+        n, dr = ctypes.c_int(), ctypes.c_int()
+        self._check(self.L.g4gpu_slip_count(self.h, int(ifld), float(slippage), ctypes.byref(n), ctypes.byref(dr)))
+        return n.value, dr.value
+
+    def slice_bytes(self):
+        return int(self.L.g4gpu_slice_bytes(self.h))
+
+    def shift_out(self, ifld, direction, send_ptr):
+        """Copies the slice leaving this block to the device address send_ptr (0: none)
+        and frees its slot for the entering slice."""
+        self._check(self.L.g4gpu_shift_out(self.h, int(ifld), int(direction),
+                                           ctypes.c_void_p(send_ptr) if send_ptr else None))
+
+    def shift_in(self, ifld, recv_ptr):
+        """Fills the entering slice from the device address recv_ptr (0: zeros)."""
+        self._check(self.L.g4gpu_shift_in(self.h, int(ifld), ctypes.c_void_p(recv_ptr) if recv_ptr else None))
 
     def sort(self):
         """Beam::sort for the window (one4one); returns the field shift (0)."""

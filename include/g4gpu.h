@@ -179,6 +179,40 @@ int g4gpu_sort(g4gpu_handle h, int *shift);
  * unless the window is periodic; nothing for a steady-state run. Asynchronous. */
 int g4gpu_apply_slippage(g4gpu_handle h, int ifld, double slippage);
 
+/* ---- a window sharded over ranks -----------------------------------------------
+ * The reference splits the time window into contiguous blocks of slices, one block per
+ * MPI rank (Time::finishInit, src/Main/GenTime.cpp:74-77). The step's only exchange is
+ * the slippage (Control::applySlippage, src/Core/Control.cpp:183-275): per slice shift
+ * every rank sends the slice leaving its block to the next rank (the previous one when
+ * the slippage runs backwards) and receives the entering slice from the other
+ * neighbour; rank 0 (the last rank, backwards) fills it with zeros unless the window
+ * is periodic, when the ring closes. A handle per rank holds its block (cfg.nslice of
+ * its slices, its part of the currents and particles); its steps run with the stages
+ * PUSH | FIELD, and each step's slippage of field ifld is g4gpu_slip_count, then per
+ * shift g4gpu_shift_out, the caller's transfer between the ranks (NCCL, MPI, a peer
+ * copy: the engine takes no part in it), g4gpu_shift_in. The transfers must be ordered
+ * after g4gpu_shift_out and before g4gpu_shift_in on the handle's stream. */
+
+/* The accumulated-slippage bookkeeping of Control::applySlippage (Control.cpp:161-186)
+ * on the host, without a handle: adds `slippage` to *accuslip, takes one `sample` off
+ * it per shift while |*accuslip| > 0.8 sample, and returns the number of shifts, with
+ * *direction = +1 (towards the head of the window) or -1. -1 for invalid arguments. */
+int g4gpu_slip_shifts(double *accuslip, double slippage, double sample, int *direction);
+/* The same on field ifld of h (its accumulated slippage); *nshift = 0 for a steady-
+ * state run. No device work. */
+int g4gpu_slip_count(g4gpu_handle h, int ifld, double slippage, int *nshift, int *direction);
+/* Bytes of one field slice on the device: ngrid^2 complex values of the handle's
+ * precision (16 B plain, 8 B mixed). */
+size_t g4gpu_slice_bytes(g4gpu_handle h);
+/* One slice shift of field ifld, first half: copies the slice leaving the block
+ * (window slice nslice - 1 for direction +1, window slice 0 for -1) to `send` (device,
+ * g4gpu_slice_bytes; may be NULL) and moves the ring start so that its storage slot
+ * becomes the entering slice. Asynchronous on the handle's stream. */
+int g4gpu_shift_out(g4gpu_handle h, int ifld, int direction, void *send);
+/* Second half: fills the entering slice from `recv` (device, as `send`), or with
+ * zeros when recv is NULL. Asynchronous. G4GPU_ERR_STATE without a g4gpu_shift_out. */
+int g4gpu_shift_in(g4gpu_handle h, int ifld, const void *recv);
+
 /* Copies field ifld (host, storage order) to the device with ring start `first`
  * and accumulated slippage `accuslip` (Field::first, Field::accuslip). */
 int g4gpu_load_field(g4gpu_handle h, int ifld, const double *field, int first, double accuslip);
