@@ -1019,7 +1019,7 @@ int g4gpu_shift_out(g4gpu_handle h, int ifld, int direction, void *send) {
   int last = (h->first[ifld] + ns - 1) % ns;
   if (direction < 0) last = (last + 1) % ns;
   if (send)
-    G4_CUDA(h, cudaMemcpyAsync(send, (char *)h->field[ifld] + (size_t)last * bytes, bytes, cudaMemcpyDeviceToDevice,
+    G4_CUDA(h, cudaMemcpyAsync(send, (char *)h->field[ifld] + (size_t)last * bytes, bytes, cudaMemcpyDefault,
                                h->stream));
   // its slot becomes the entering slice (Control.cpp:268-272)
   h->first[ifld] = direction > 0 ? last : (last + 1) % ns;
@@ -1036,7 +1036,7 @@ int g4gpu_shift_in(g4gpu_handle h, int ifld, const void *recv) {
   const size_t bytes = g4gpu_slice_bytes(h);
   char *dst = (char *)h->field[ifld] + (size_t)slot * bytes;
   if (recv)
-    G4_CUDA(h, cudaMemcpyAsync(dst, recv, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    G4_CUDA(h, cudaMemcpyAsync(dst, recv, bytes, cudaMemcpyDefault, h->stream));
   else
     G4_CUDA(h, cudaMemsetAsync(dst, 0, bytes, h->stream));
   h->shift_slot[ifld] = -1;

@@ -205,12 +205,15 @@ int g4gpu_slip_count(g4gpu_handle h, int ifld, double slippage, int *nshift, int
  * precision (16 B plain, 8 B mixed). */
 size_t g4gpu_slice_bytes(g4gpu_handle h);
 /* One slice shift of field ifld, first half: copies the slice leaving the block
- * (window slice nslice - 1 for direction +1, window slice 0 for -1) to `send` (device,
- * g4gpu_slice_bytes; may be NULL) and moves the ring start so that its storage slot
- * becomes the entering slice. Asynchronous on the handle's stream. */
+ * (window slice nslice - 1 for direction +1, window slice 0 for -1) to `send`
+ * (g4gpu_slice_bytes of device or host memory; may be NULL) and moves the ring start
+ * so that its storage slot becomes the entering slice. Asynchronous on the handle's
+ * stream (synchronise before a host buffer is read). */
 int g4gpu_shift_out(g4gpu_handle h, int ifld, int direction, void *send);
-/* Second half: fills the entering slice from `recv` (device, as `send`), or with
- * zeros when recv is NULL. Asynchronous. G4GPU_ERR_STATE without a g4gpu_shift_out. */
+/* Second half: fills the entering slice from `recv` (device or host memory, as
+ * `send`), or with zeros when recv is NULL. Asynchronous (a host buffer must stay
+ * unchanged until the handle's stream has passed the copy). G4GPU_ERR_STATE without a
+ * g4gpu_shift_out. */
 int g4gpu_shift_in(g4gpu_handle h, int ifld, const void *recv);
 
 /* Copies field ifld (host, storage order) to the device with ring start `first`
