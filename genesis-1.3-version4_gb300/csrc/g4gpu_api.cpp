@@ -517,6 +517,22 @@ int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *tab) {
     s.xks = xks;
     s.xku = r[G4GPU_LAT_KU];
     if (s.xku == 0) s.xku = xks * 0.5 / gamma0 / gamma0;  // BeamSolver.cpp:34-38
+    s.ztemp1 = -2. / s.xks;
+    {
+      // dtheta/dz of the ODE (BeamSolver.cpp:144-163) at gammaref, on axis, no field
+      const double bpar = std::sqrt(1. - (1. + aw * aw) / (gamma0 * gamma0));
+      const double rate = s.xks * (1. - 1. / bpar) + s.xku;
+      s.dnom_half = 0.5 * s.delz * rate;
+      s.dnom_full = s.delz * rate;
+      for (int k = 0; k < c.nfield; k++) {
+        g4::FieldStep &f = s.f[k];
+        f.idgrid = 1. / f.dgrid;
+        f.rot_half[0] = std::cos(f.rharm * s.dnom_half);
+        f.rot_half[1] = std::sin(f.rharm * s.dnom_half);
+        f.rot_full[0] = std::cos(f.rharm * s.dnom_full);
+        f.rot_full[1] = std::sin(f.rharm * s.dnom_full);
+      }
+    }
     h->slip[i] = r[G4GPU_LAT_SLIP];
   }
   h->nsteps = nsteps;

@@ -30,6 +30,12 @@ struct FieldStep {
   int coef;       // index of the ADI coefficient set of this (field, delz)
   int first;      // ring start of the field when the step runs (filled at launch)
   int tw;         // warm-up length of the segmented FP32 tridiagonal solves, 0: not applicable
+  double idgrid;  // 1 / dgrid: the FP64 push's cell lookup multiplies
+  // The FP64 push forms e^{i h theta} at its RK4 stages by rotating e^{i h theta0}: by
+  // e^{i h D} for the step's nominal phase advance D (StepConst::dnom_half over half a
+  // step, dnom_full over the step) and by a short series for the small remainder.
+  // rot_half / rot_full: cos and sin of rharm * dnom_half / dnom_full.
+  double rot_half[2], rot_full[2];
 };
 
 // Per integration step constants (Undulator accessors, Undulator.h:82-204).
@@ -50,6 +56,10 @@ struct StepConst {
   double xku;         // undulator wavenumber, or xks/(2 gamma0^2) in drifts
   double delz;
   double gammaref;
+  double ztemp1;      // -2 / xks (BeamSolver.cpp:147), the same value the ODE computes
+  // nominal phase advance over half a step and over the step: delz / 2 and delz times
+  // dtheta/dz of a particle at gammaref on axis without field (BeamSolver.cpp:144-163)
+  double dnom_half, dnom_full;
   // chicane of the step (g4gpu_set_chicanes): its transfer matrix, applied before the
   // first half step (TrackBeam::applyChicane, TrackBeam.cpp:131-244), elements
   // m00 m01 m10 m11 m22 m23 m32 m33, and the phase shift R56 2 pi / (lambda0 gamma0)

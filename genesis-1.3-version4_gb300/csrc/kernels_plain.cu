@@ -35,28 +35,30 @@ __device__ __forceinline__ C2 rmul(double s, C2 a) { return {s * a.x, s * a.y}; 
 // complex * real
 __device__ __forceinline__ C2 mulr(C2 a, double s) { return {a.x * s, a.y * s}; }
 
-// TrackBeam::applyDrift / applyFQuad / applyDQuad (TrackBeam.cpp:84-116)
+// TrackBeam::applyDrift / applyFQuad / applyDQuad (TrackBeam.cpp:84-116). The
+// divisions by gammaz are multiplications by igz = 1 / gammaz (one division per half
+// step instead of up to three; the products differ from the quotients in the last bit).
 __device__ __forceinline__ void plane_step(int kind, double q, double off, double delz, double &x,
-                                           double &p, double gammaz) {
+                                           double &p, double gammaz, double igz) {
   if (kind == 0) {
-    x += p * delz / gammaz;
+    x += p * delz * igz;
   } else if (kind == 1) {
-    double foc = sqrt(q / gammaz);
+    double foc = sqrt(q * igz);
     double omg = foc * delz;
     double a1 = cos(omg);
     double a2 = sin(omg) / foc;
     double a3 = -a2 * foc * foc;
     double xtmp = x - off;
-    x = a1 * xtmp + a2 * p / gammaz + off;
+    x = a1 * xtmp + a2 * p * igz + off;
     p = a3 * xtmp * gammaz + a1 * p;
   } else {
-    double foc = sqrt(-q / gammaz);
+    double foc = sqrt(-q * igz);
     double omg = foc * delz;
     double a1 = cosh(omg);
     double a2 = sinh(omg) / foc;
     double a3 = a2 * foc * foc;
     double xtmp = x - off;
-    x = a1 * xtmp + a2 * p / gammaz + off;
+    x = a1 * xtmp + a2 * p * igz + off;
     p = a3 * xtmp * gammaz + a1 * p;
   }
 }
@@ -81,8 +83,9 @@ __device__ __forceinline__ void transverse(const StepConst &sc, bool last, doubl
   }
   double delz = sc.delz * 0.5;
   double gammaz = sqrt(g * g - 1 - sc.aw_t * sc.aw_t - px * px - py * py);
-  plane_step(sc.kindx, sc.qx, sc.xoff, delz, x, px, gammaz);
-  plane_step(sc.kindy, sc.qy, sc.yoff, delz, y, py, gammaz);
+  const double igz = 1. / gammaz;
+  plane_step(sc.kindx, sc.qx, sc.xoff, delz, x, px, gammaz, igz);
+  plane_step(sc.kindy, sc.qy, sc.yoff, delz, y, py, gammaz, igz);
 }
 
 // Field::getLLGridpoint (Field.cpp:160-174). Returns the lower-left cell and the
@@ -93,11 +96,15 @@ struct Cell {
   int i00, i10, i01, i11;
   double wx, wy;
 };
-__device__ __forceinline__ bool ll_gridpoint(double gm, double dg, int ng, double x, double y,
+// The reference divides by the spacing; the push multiplies by its host-computed
+// inverse idg (the weights then differ in the last bit, and a particle within rounding
+// of a cell boundary may take the neighbouring cell, where the bilinear weights give
+// the same value).
+__device__ __forceinline__ bool ll_gridpoint(double gm, double idg, int ng, double x, double y,
                                              Cell &c) {
   if ((x > -gm) && (x < gm) && (y > -gm) && (y < gm)) {
-    double wx = (x + gm) / dg;
-    double wy = (y + gm) / dg;
+    double wx = (x + gm) * idg;
+    double wy = (y + gm) * idg;
     double fx = floor(wx), fy = floor(wy);
     int ix = (int)fx, iy = (int)fy;
     c.wx = 1 + fx - wx;
@@ -113,46 +120,86 @@ __device__ __forceinline__ bool ll_gridpoint(double gm, double dg, int ng, doubl
   return false;
 }
 
-// BeamSolver::ODE (BeamSolver.cpp:144-163) for NF fields
+// BeamSolver::ODE (BeamSolver.cpp:144-163) for NF fields, given cs[i] = (cos, sin) of
+// rharm_i * tthet. Two of the reference's four divisions become products with the
+// reciprocals 1 / tgam and 1 / btpar0 (the latter computed as the reference computes
+// it, so that xks (1 - 1/btpar0), which xks ~ 1e11 amplifies, is the reference's
+// value); ztemp1 = -2 / xks comes with the step constants.
 template <int NF>
-__device__ __forceinline__ void ode(const StepConst &sc, const C2 *rpart, double btpar, double ez,
-                                    double tgam, double tthet, double &k2gg, double &k2pp) {
-  double ztemp1 = -2. / sc.xks;
+__device__ __forceinline__ void ode(const StepConst &sc, const C2 *rpart, const C2 *cs, double btpar, double ez,
+                                    double tgam, double &k2gg, double &k2pp) {
   C2 ctmp = {0, 0};
 #pragma unroll
   for (int i = 0; i < NF; i++) {
     if (i >= sc.nfld) break;
-    double s, c;
-    sincos(sc.f[i].rharm * tthet, &s, &c);
-    ctmp = cadd(ctmp, cmul(rpart[i], C2{c, -s}));
+    ctmp = cadd(ctmp, cmul(rpart[i], C2{cs[i].x, -cs[i].y}));
   }
-  double btper0 = btpar + ztemp1 * ctmp.x;
-  double btpar0 = sqrt(1. - btper0 / (tgam * tgam));
-  k2pp += sc.xks * (1. - 1. / btpar0) + sc.xku;
-  k2gg += ctmp.y / btpar0 / tgam - ez;
+  const double itg = 1. / tgam;
+  double btper0 = btpar + sc.ztemp1 * ctmp.x;
+  double btpar0 = sqrt(1. - btper0 * (itg * itg));
+  const double ib = 1. / btpar0;
+  k2pp += sc.xks * (1. - ib) + sc.xku;
+  k2gg += ctmp.y * ib * itg - ez;
+}
+
+// e^{i eps} by its Taylor series, for |eps| <= kRotMax: the first omitted terms are
+// eps^14 / 14! (cosine) and eps^13 / 13! (sine), below 1e-19 at kRotMax = 0.25.
+constexpr double kRotMax = 0.25;
+__device__ __forceinline__ C2 expi_small(double e) {
+  const double z = e * e;
+  double c = fma(z, 1. / 479001600., -1. / 3628800.);
+  c = fma(z, c, 1. / 40320.);
+  c = fma(z, c, -1. / 720.);
+  c = fma(z, c, 1. / 24.);
+  c = fma(z, c, -0.5);
+  c = fma(z, c, 1.);
+  double sn = fma(z, -1. / 39916800., 1. / 362880.);
+  sn = fma(z, sn, -1. / 5040.);
+  sn = fma(z, sn, 1. / 120.);
+  sn = fma(z, sn, -1. / 6.);
+  sn = fma(z, sn, 1.);
+  return {c, sn * e};
+}
+
+// (cos, sin) of h theta for a phase theta = theta0 + dth near theta0 + dnom: the
+// particle's e^{i h theta0} rotated by e^{i h dnom} (brot: their product, formed once
+// per particle and harmonic) and by e^{i h (dth - dnom)}; sincos of h theta where the
+// remainder is not small.
+__device__ __forceinline__ C2 rotated(C2 brot, double h, double theta, double dth, double dnom) {
+  const double e = h * (dth - dnom);
+  if (fabs(e) <= kRotMax) return cmul(brot, expi_small(e));
+  double sn, c;
+  sincos(h * theta, &sn, &c);
+  return {c, sn};
 }
 
 // Deposition of one particle into the source of every field
 // (FieldSolverADI.cpp:19-51; FieldSolverFFT.cpp:19-51 is identical).
+// cs: (cos, sin) of rharm_k * theta of every field, or null (computed here).
 template <int NF>
 __device__ __forceinline__ void deposit_particle(const StepConst &sc, double2 *const *src,
                                                  size_t slice_off, int ng, double cur,
                                                  double npd, double g, double th, double x,
-                                                 double y) {
+                                                 double y, const C2 *cs = nullptr) {
 #pragma unroll
   for (int k = 0; k < NF; k++) {
     if (k >= sc.nfld) break;
     const FieldStep &fs = sc.f[k];
     if (!fs.dep_on) continue;
     Cell c;
-    if (!ll_gridpoint(fs.gridmax, fs.dgrid, ng, x, y, c)) continue;
+    if (!ll_gridpoint(fs.gridmax, fs.idgrid, ng, x, y, c)) continue;
     double scl = fs.fc * kVacimp * cur * fs.xks * sc.delz;
     scl /= 4 * kEev * npd * fs.dgrid * fs.dgrid;
     double dx = x - sc.ax, dy = y - sc.ay;
     double faw2 = (1 + sc.kx * dx * dx + sc.ky * dy * dy + 2 * (sc.gradx * dx + sc.grady * dy));
     double part = sqrt(faw2) * scl / g;
     double s, co;
-    sincos(fs.rharm * th, &s, &co);
+    if (cs) {
+      co = cs[k].x;
+      s = cs[k].y;
+    } else {
+      sincos(fs.rharm * th, &s, &co);
+    }
     C2 cpart = mulr(C2{s, co}, part);
     double2 *d = src[k] + slice_off;
     double w = c.wx * c.wy;
@@ -232,7 +279,7 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
     int islice = (is + fs.first) % ns;
     const double2 *f = p.field[k] + (size_t)islice * ncell;
     Cell c;
-    if (ll_gridpoint(fs.gridmax, fs.dgrid, ng, x, y, c)) {
+    if (ll_gridpoint(fs.gridmax, fs.idgrid, ng, x, y, c)) {
       C2 cpart = mulr(mulr(ld(f + c.i00), c.wx), c.wy);
       cpart = cadd(cpart, mulr(mulr(ld(f + c.i10), 1 - c.wx), c.wy));
       cpart = cadd(cpart, mulr(mulr(ld(f + c.i01), c.wx), 1 - c.wy));
@@ -243,9 +290,30 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
     }
   }
 
+  // e^{i h theta} of every field at the start, and rotated towards the stages: one
+  // sincos per harmonic and particle instead of one per stage
+  const double theta0 = theta;
+  C2 bhalf[NF], bfull[NF], cs[NF];
+#pragma unroll
+  for (int k = 0; k < NF; k++) {
+    if (k >= sc.nfld) break;
+    double sn, c;
+    sincos(sc.f[k].rharm * theta0, &sn, &c);
+    cs[k] = C2{c, sn};
+    bhalf[k] = cmul(cs[k], C2{sc.f[k].rot_half[0], sc.f[k].rot_half[1]});
+    bfull[k] = cmul(cs[k], C2{sc.f[k].rot_full[0], sc.f[k].rot_full[1]});
+  }
+  auto stage = [&](const C2 *b, double dnom) {
+#pragma unroll
+    for (int k = 0; k < NF; k++) {
+      if (k >= sc.nfld) break;
+      cs[k] = rotated(b[k], sc.f[k].rharm, theta, theta - theta0, dnom);
+    }
+  };
+
   // BeamSolver::RungeKutta, BeamSolver.cpp:89-141
   double k2gg = 0, k2pp = 0, k3gg, k3pp;
-  ode<NF>(sc, rpart, btpar, ez, gamma, theta, k2gg, k2pp);
+  ode<NF>(sc, rpart, cs, btpar, ez, gamma, k2gg, k2pp);
   double stpz = 0.5 * sc.delz;
   gamma += stpz * k2gg;
   theta += stpz * k2pp;
@@ -253,14 +321,16 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   k3pp = k2pp;
   k2gg = 0;
   k2pp = 0;
-  ode<NF>(sc, rpart, btpar, ez, gamma, theta, k2gg, k2pp);
+  stage(bhalf, sc.dnom_half);
+  ode<NF>(sc, rpart, cs, btpar, ez, gamma, k2gg, k2pp);
   gamma += stpz * (k2gg - k3gg);
   theta += stpz * (k2pp - k3pp);
   k3gg /= 6;
   k3pp /= 6;
   k2gg *= -0.5;
   k2pp *= -0.5;
-  ode<NF>(sc, rpart, btpar, ez, gamma, theta, k2gg, k2pp);
+  stage(bhalf, sc.dnom_half);
+  ode<NF>(sc, rpart, cs, btpar, ez, gamma, k2gg, k2pp);
   stpz = sc.delz;
   gamma += stpz * k2gg;
   theta += stpz * k2pp;
@@ -268,7 +338,8 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   k3pp -= k2pp;
   k2gg *= 2;
   k2pp *= 2;
-  ode<NF>(sc, rpart, btpar, ez, gamma, theta, k2gg, k2pp);
+  stage(bfull, sc.dnom_full);
+  ode<NF>(sc, rpart, cs, btpar, ez, gamma, k2gg, k2pp);
   gamma += stpz * (k3gg + k2gg / 6.0);
   theta += stpz * (k3pp + k2pp / 6.0);
 
@@ -291,9 +362,12 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   p.px[o] = px;
   p.py[o] = py;
 
-  if (deposit)
+  if (deposit) {
+    // the deposition's phases, rotated from the start of the step like the stages'
+    stage(bfull, sc.dnom_full);
     deposit_particle<NF>(sc, p.src, (size_t)is * ncell, ng, p.current[is], (double)n, gamma,
-                         theta, x, y);
+                         theta, x, y, cs);
+  }
 }
 
 // Deposition alone, for a Field::track without a preceding push.
