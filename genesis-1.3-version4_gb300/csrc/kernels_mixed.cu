@@ -1781,18 +1781,21 @@ __device__ __forceinline__ bool cell_rc(float gm, float dg, int ng, float x, flo
 // four particles (deposit_quads' grouping); each weighted contribution goes to the
 // CTA that holds its row: T[0], T[1] are the two bands (one local, one the peer's
 // through distributed shared memory), starting at global rows 0 and h.
-__device__ __forceinline__ void pair_add(float2 *const *T, int h, int ng, int ix, int iy, float w, float cpx,
+// The contribution to cell (ix, iy) if row iy is one of this CTA's rows [r0, r0 + nrow)
+// (its band S): every CTA of the pair deposits into its own shared memory only.
+__device__ __forceinline__ void pair_add(float2 *S, int r0, int nrow, int ng, int ix, int iy, float w, float cpx,
                                          float cpy) {
-  const int o = iy >= h;
-  float2 *t = T[o] + (size_t)(iy - (o ? h : 0)) * ng + ix;
+  if (iy < r0 || iy >= r0 + nrow) return;
+  float2 *t = S + (size_t)(iy - r0) * ng + ix;
   atomicAdd(&t->x, w * cpx);
   atomicAdd(&t->y, w * cpy);
 }
-__device__ __forceinline__ void pair_group(const StepConstF &sc, const FieldStepF &fs, float scl, float2 *const *T,
-                                           int h, int ng, float x, float y, const long long *th, const float *dgam,
-                                           int n) {
+__device__ __forceinline__ void pair_group(const StepConstF &sc, const FieldStepF &fs, float scl, float2 *S,
+                                           int r0, int nrow, int ng, float x, float y, const long long *th,
+                                           const float *dgam, int n) {
   CellRC c;
   if (!cell_rc(fs.gridmax, fs.dgrid, ng, x, y, c)) return;
+  if (c.iy1 < r0 || c.iy >= r0 + nrow) return;  // the particle's rows are the peer's
   float dx = x - sc.ax, dy = y - sc.ay;
   float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
   float a = sqrtf(faw2) * scl;
@@ -1804,51 +1807,56 @@ __device__ __forceinline__ void pair_group(const StepConstF &sc, const FieldStep
     cpx += sn * part;
     cpy += co * part;
   }
-  pair_add(T, h, ng, c.ix, c.iy, c.wx * c.wy, cpx, cpy);
-  pair_add(T, h, ng, c.ix1, c.iy, (1.f - c.wx) * c.wy, cpx, cpy);
-  pair_add(T, h, ng, c.ix, c.iy1, c.wx * (1.f - c.wy), cpx, cpy);
-  pair_add(T, h, ng, c.ix1, c.iy1, (1.f - c.wx) * (1.f - c.wy), cpx, cpy);
+  pair_add(S, r0, nrow, ng, c.ix, c.iy, c.wx * c.wy, cpx, cpy);
+  pair_add(S, r0, nrow, ng, c.ix1, c.iy, (1.f - c.wx) * c.wy, cpx, cpy);
+  pair_add(S, r0, nrow, ng, c.ix, c.iy1, c.wx * (1.f - c.wy), cpx, cpy);
+  pair_add(S, r0, nrow, ng, c.ix1, c.iy1, (1.f - c.wx) * (1.f - c.wy), cpx, cpy);
 }
-__device__ __forceinline__ void deposit_pair(const StepConstF &sc, const FieldStepF &fs, const PtrsF &p,
-                                             float2 *const *T, int h, int is, int np, int ng, int q) {
+// The pair's deposition: each CTA reads every particle of the slice and deposits the
+// contributions to its own rows into its own band, with shared-memory atomics only. A
+// particle whose footprint straddles the two bands is deposited by both, each into its
+// rows. (Splitting the particles between the CTAs instead sends half of every CTA's
+// contributions to the peer as distributed-shared-memory atomics, which took 2.8 times
+// as long as the single CTA's whole deposition.)
+__device__ __forceinline__ void deposit_pair(const StepConstF &sc, const FieldStepF &fs, const PtrsF &p, float2 *S,
+                                             int r0, int nrow, int is, int np, int ng) {
   const float scl = fs.dep_scl * slice_cur_f(p, is, np);
   const size_t base = (size_t)is * np;
   if ((np & 3) == 0 && !p.count) {
-    const int nq = np >> 2, q0 = q ? nq / 2 : 0, q1 = q ? nq : nq / 2;
+    const int nq = np >> 2;
     const float4 *X = reinterpret_cast<const float4 *>(p.x + base);
     const float4 *Y = reinterpret_cast<const float4 *>(p.y + base);
     const float4 *G = reinterpret_cast<const float4 *>(p.dg + base);
     const longlong2 *TH = reinterpret_cast<const longlong2 *>(p.theta + base);
-    for (int g = q0 + threadIdx.x; g < q1; g += blockDim.x) {
+    for (int g = threadIdx.x; g < nq; g += blockDim.x) {
       const float4 x = X[g], y = Y[g], gg = G[g];
       const longlong2 t01 = TH[2 * g], t23 = TH[2 * g + 1];
       const long long th[4] = {t01.x, t01.y, t23.x, t23.y};
       const float dg[4] = {gg.x, gg.y, gg.z, gg.w};
       const bool p01 = x.x == x.y && y.x == y.y, p23 = x.z == x.w && y.z == y.w;
       if (p01 && p23 && x.x == x.z && y.x == y.z) {
-        pair_group(sc, fs, scl, T, h, ng, x.x, y.x, th, dg, 4);
+        pair_group(sc, fs, scl, S, r0, nrow, ng, x.x, y.x, th, dg, 4);
       } else {
         if (p01) {
-          pair_group(sc, fs, scl, T, h, ng, x.x, y.x, th, dg, 2);
+          pair_group(sc, fs, scl, S, r0, nrow, ng, x.x, y.x, th, dg, 2);
         } else {
-          pair_group(sc, fs, scl, T, h, ng, x.x, y.x, th, dg, 1);
-          pair_group(sc, fs, scl, T, h, ng, x.y, y.y, th + 1, dg + 1, 1);
+          pair_group(sc, fs, scl, S, r0, nrow, ng, x.x, y.x, th, dg, 1);
+          pair_group(sc, fs, scl, S, r0, nrow, ng, x.y, y.y, th + 1, dg + 1, 1);
         }
         if (p23) {
-          pair_group(sc, fs, scl, T, h, ng, x.z, y.z, th + 2, dg + 2, 2);
+          pair_group(sc, fs, scl, S, r0, nrow, ng, x.z, y.z, th + 2, dg + 2, 2);
         } else {
-          pair_group(sc, fs, scl, T, h, ng, x.z, y.z, th + 2, dg + 2, 1);
-          pair_group(sc, fs, scl, T, h, ng, x.w, y.w, th + 3, dg + 3, 1);
+          pair_group(sc, fs, scl, S, r0, nrow, ng, x.z, y.z, th + 2, dg + 2, 1);
+          pair_group(sc, fs, scl, S, r0, nrow, ng, x.w, y.w, th + 3, dg + 3, 1);
         }
       }
     }
   } else {
     const int n = slice_np_f(p, is, np);
-    const int i0 = q ? n / 2 : 0, i1 = q ? n : n / 2;
-    for (int ip = i0 + threadIdx.x; ip < i1; ip += blockDim.x) {
+    for (int ip = threadIdx.x; ip < n; ip += blockDim.x) {
       const long long th = p.theta[base + ip];
       const float dg = p.dg[base + ip];
-      pair_group(sc, fs, scl, T, h, ng, p.x[base + ip], p.y[base + ip], &th, &dg, 1);
+      pair_group(sc, fs, scl, S, r0, nrow, ng, p.x[base + ip], p.y[base + ip], &th, &dg, 1);
     }
   }
 }
@@ -1896,14 +1904,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 2)
   const float cs = fs.cstep;
   const int nseg = max(1, min((int)blockDim.x / ng, 8));
   stencil_cols_band(S, u, ng, r0, nrow, cs, nseg);  // S1 on this band
-  cl.sync();                                        // both bands hold S1 before any deposit
-  if (deposit) {
-    float2 *T[2];
-    T[q] = S;
-    T[1 - q] = P;
-    deposit_pair(sc, fs, p, T, (ng + 1) / 2, is, np, ng, q);
-  }
-  cl.sync();  // every contribution, local or remote, has landed
+  __syncthreads();  // the band holds S1 before any deposit
+  if (deposit) deposit_pair(sc, fs, p, S, r0, nrow, is, np, ng);
+  cl.sync();  // both bands are complete before the solves read across the pair
   thomas_lines(S, nrow, ng, 1, ng, max(1, min((int)blockDim.x / nrow, 32)), fs.tw, C, CB, CW);  // rows
   r2_cols_band(S, u, ng, r0, nrow, cs, nseg);
   __syncthreads();
