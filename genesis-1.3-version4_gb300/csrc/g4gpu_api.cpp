@@ -540,6 +540,7 @@ int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *tab) {
   for (auto &g : h->graphs)
     if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
   h->graphs.clear();
+  h->graph_gen++;
   if (h->coef) {
     cudaFree(h->coef);
     h->bytes -= h->coef_bytes;
@@ -628,6 +629,7 @@ int g4gpu_set_incoherent(g4gpu_handle h, int seed, int do_loss, int do_spread, i
   for (auto &g : h->graphs)
     if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
   h->graphs.clear();
+  h->graph_gen++;
   return G4GPU_OK;
 }
 
@@ -655,6 +657,7 @@ int g4gpu_set_chicanes(g4gpu_handle h, int nsteps, const double *table) {
   for (auto &g : h->graphs)
     if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
   h->graphs.clear();
+  h->graph_gen++;
   return G4GPU_OK;
 }
 
@@ -689,6 +692,7 @@ static void drop_graphs(g4gpu_handle h) {
   for (auto &g : h->graphs)
     if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
   h->graphs.clear();
+  h->graph_gen++;
 }
 
 int g4gpu_load_beam(g4gpu_handle h, const double *particles, const double *current) {
@@ -888,6 +892,7 @@ int g4gpu_set_efield(g4gpu_handle h, double rmax, int ngrid, int nz, int nphi, i
   for (auto &g : h->graphs)
     if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
   h->graphs.clear();
+  h->graph_gen++;
   return G4GPU_OK;
 }
 
@@ -1941,8 +1946,31 @@ extern "C" int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_thread
 
 // ---- batched ensembles ---------------------------------------------------------
 
+// A batch: the members' handles, and the ensemble's step ranges as single CUDA graphs.
+// One graph holds every member's steps of a range as parallel branches (forked from and
+// joined into the batch's own stream), so the whole ensemble advances with one graph
+// launch. Like a handle's own graphs it is valid for exactly the ring states (and launch
+// shapes) it was captured from, which key it.
 struct g4gpu_batch_ctx {
   std::vector<g4gpu_handle> members;
+  cudaStream_t origin = nullptr;
+  cudaEvent_t fork = nullptr, post = nullptr;
+  std::vector<cudaEvent_t> pre, join;
+  struct Key {
+    int istep0, nsteps, stages;
+    std::vector<long long> state;  // per member: steps, launch shapes, first[], accuslip[] bits
+    bool operator<(const Key &o) const {
+      return std::tie(istep0, nsteps, stages, state) < std::tie(o.istep0, o.nsteps, o.stages, o.state);
+    }
+  };
+  struct Entry {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<std::vector<int>> end_first;
+    std::vector<std::vector<double>> end_accuslip;
+    std::vector<std::vector<long long>> launches;
+  };
+  std::map<Key, Entry> graphs;
+  bool single_device = true;
 };
 
 extern "C" int g4gpu_batch_create(int nrun, const g4gpu_config *cfgs, g4gpu_batch *out) {
@@ -1959,6 +1987,22 @@ extern "C" int g4gpu_batch_create(int nrun, const g4gpu_config *cfgs, g4gpu_batc
     }
     h->graph_mode = true;
     b->members.push_back(h);
+    if (cfgs[i].device != cfgs[0].device) b->single_device = false;
+  }
+  if (b->single_device) {
+    cudaSetDevice(cfgs[0].device);
+    bool ok = cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&b->post, cudaEventDisableTiming) == cudaSuccess;
+    b->pre.assign(nrun, nullptr);
+    b->join.assign(nrun, nullptr);
+    for (int i = 0; i < nrun && ok; i++)
+      ok = cudaEventCreateWithFlags(&b->pre[i], cudaEventDisableTiming) == cudaSuccess &&
+           cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+      g4gpu_batch_destroy(b);
+      return fail(nullptr, G4GPU_ERR_CUDA, "batch stream and events");
+    }
   }
   *out = b;
   return G4GPU_OK;
@@ -1966,6 +2010,16 @@ extern "C" int g4gpu_batch_create(int nrun, const g4gpu_config *cfgs, g4gpu_batc
 
 extern "C" void g4gpu_batch_destroy(g4gpu_batch b) {
   if (!b) return;
+  if (!b->members.empty()) cudaSetDevice(b->members[0]->cfg.device);
+  for (auto &g : b->graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+  for (cudaEvent_t e : b->pre)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : b->join)
+    if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->post) cudaEventDestroy(b->post);
+  if (b->origin) cudaStreamDestroy(b->origin);
   for (auto m : b->members) g4gpu_destroy(m);
   delete b;
 }
@@ -1977,14 +2031,106 @@ extern "C" g4gpu_handle g4gpu_batch_member(g4gpu_batch b, int i) {
 
 extern "C" int g4gpu_batch_run(g4gpu_batch b, int istep0, int nsteps, int stages) {
   if (!b || istep0 < 0 || nsteps < 0) return fail(nullptr, G4GPU_ERR_ARG, "bad batch arguments");
-  for (auto m : b->members) {
-    int n = std::min(nsteps, m->nsteps - istep0);
-    if (n <= 0) continue;
-    int rc = g4gpu_run(m, istep0, n, stages);
-    if (rc) {
-      fail(nullptr, rc, std::string("batch member: ") + m->err);
-      return rc;
+  const int nrun = (int)b->members.size();
+  std::vector<int> nm(nrun);
+  bool graph = b->single_device;
+  for (int i = 0; i < nrun; i++) {
+    g4gpu_handle m = b->members[i];
+    nm[i] = std::max(0, std::min(nsteps, m->nsteps - istep0));
+    graph = graph && m->graph_mode;
+    if (nm[i] > 0) {
+      if (!m->beam_loaded) return fail(nullptr, G4GPU_ERR_STATE, "batch member: no beam loaded");
+      for (int k = 0; k < m->cfg.nfield; k++)
+        if (!m->field_loaded[k]) return fail(nullptr, G4GPU_ERR_STATE, "batch member: a field is not loaded");
     }
+  }
+  if (!graph) {  // members on several devices, or graph mode off: one launch sequence per member
+    for (int i = 0; i < nrun; i++) {
+      if (nm[i] <= 0) continue;
+      int rc = g4gpu_run(b->members[i], istep0, nm[i], stages);
+      if (rc) {
+        fail(nullptr, rc, std::string("batch member: ") + b->members[i]->err);
+        return rc;
+      }
+    }
+    return G4GPU_OK;
+  }
+  cudaSetDevice(b->members[0]->cfg.device);
+  g4gpu_batch_ctx::Key key{istep0, nsteps, stages, {}};
+  for (int i = 0; i < nrun; i++) {
+    g4gpu_handle m = b->members[i];
+    key.state.push_back(nm[i]);
+    key.state.push_back(m->push_block);
+    key.state.push_back(m->field_threads);
+    key.state.push_back(m->field_kernel);
+    key.state.push_back(m->graph_gen);  // the member's lattice and set-up the graph was captured with
+    for (int k = 0; k < m->cfg.nfield; k++) {
+      long long bits;
+      std::memcpy(&bits, &m->accuslip[k], sizeof(bits));
+      key.state.push_back(m->first[k]);
+      key.state.push_back(bits);
+    }
+  }
+  auto bfail = [&](cudaError_t e, const char *what) {
+    return fail(nullptr, G4GPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  };
+  auto it = b->graphs.find(key);
+  if (it == b->graphs.end()) {
+    g4gpu_batch_ctx::Entry ent;
+    std::vector<std::vector<long long>> before(nrun);
+    for (int i = 0; i < nrun; i++) before[i].assign(b->members[i]->launches, b->members[i]->launches + G4GPU_K_NCLASS);
+    cudaError_t e = cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return bfail(e, "cudaStreamBeginCapture");
+    cudaEventRecord(b->fork, b->origin);
+    int rc = G4GPU_OK;
+    for (int i = 0; i < nrun && !rc; i++) {
+      g4gpu_handle m = b->members[i];
+      if (nm[i] <= 0) continue;
+      cudaStreamWaitEvent(m->stream, b->fork, 0);
+      m->capturing = true;
+      rc = enqueue_steps(m, istep0, nm[i], stages);
+      m->capturing = false;
+      cudaEventRecord(b->join[i], m->stream);
+      cudaStreamWaitEvent(b->origin, b->join[i], 0);
+    }
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(b->origin, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return fail(nullptr, rc, "batch member: capture of its steps failed");
+    }
+    if (e != cudaSuccess) return bfail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&ent.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return bfail(e, "cudaGraphInstantiate");
+    for (int i = 0; i < nrun; i++) {
+      g4gpu_handle m = b->members[i];
+      ent.end_first.emplace_back(m->first, m->first + m->cfg.nfield);
+      ent.end_accuslip.emplace_back(m->accuslip, m->accuslip + m->cfg.nfield);
+      std::vector<long long> d(G4GPU_K_NCLASS);
+      for (int c = 0; c < G4GPU_K_NCLASS; c++) d[c] = m->launches[c] - before[i][c];
+      ent.launches.push_back(d);
+      // the capture advanced the counters without running anything
+      std::memcpy(m->launches, before[i].data(), sizeof(long long) * G4GPU_K_NCLASS);
+    }
+    it = b->graphs.emplace(key, std::move(ent)).first;
+  }
+  // the graph follows the members' earlier work and their later work follows it
+  for (int i = 0; i < nrun; i++) {
+    cudaEventRecord(b->pre[i], b->members[i]->stream);
+    cudaStreamWaitEvent(b->origin, b->pre[i], 0);
+  }
+  cudaError_t e = cudaGraphLaunch(it->second.exec, b->origin);
+  if (e != cudaSuccess) return bfail(e, "cudaGraphLaunch");
+  cudaEventRecord(b->post, b->origin);
+  for (int i = 0; i < nrun; i++) {
+    g4gpu_handle m = b->members[i];
+    cudaStreamWaitEvent(m->stream, b->post, 0);
+    for (int k = 0; k < m->cfg.nfield; k++) {
+      m->first[k] = it->second.end_first[i][k];
+      m->accuslip[k] = it->second.end_accuslip[i][k];
+    }
+    for (int c = 0; c < G4GPU_K_NCLASS; c++) m->launches[c] += it->second.launches[i][c];
   }
   return G4GPU_OK;
 }

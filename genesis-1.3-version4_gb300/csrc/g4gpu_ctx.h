@@ -108,6 +108,9 @@ struct g4gpu_ctx {
     long long launches[G4GPU_K_NCLASS] = {};
   };
   std::map<GraphKey, GraphEntry> graphs;
+  // advanced whenever the captured graphs are dropped (a new lattice, chicanes, beam
+  // layout, set-up), so that a batch's ensemble graphs of this member are not reused
+  long long graph_gen = 0;
   bool capturing = false;
 
   // learned closure (g4gpu_learned.cpp)
