@@ -460,25 +460,6 @@ __device__ __forceinline__ void phase_sincos(float a, float *sn, float *cs) {
   __sincosf(a, sn, cs);
 }
 
-// One factor of the separable propagator: P[k] = exp(i d^2 k2dz) at FFT index k of a
-// line, d = ((k + n - (n+1)/2) mod n) - (n-1)/2 on the reference's shifted frequency
-// map; the product of the row's and the column's factor is exp(K2 dz). The caller
-// synchronises before reading P.
-template <typename T2>
-__device__ __forceinline__ void prop_factors(T2 *P, int n, double k2dz) {
-  typedef typename Real<T2>::T R;
-  const R kdz = (R)k2dz, half = (R)(0.5 * (n - 1));
-  const int off = n - (n + 1) / 2;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    int ix = k + off;
-    ix -= ix >= n ? n : 0;
-    const R d = (R)ix - half;
-    R sn, cs;
-    phase_sincos(d * d * kdz, &sn, &cs);
-    P[k] = mk<T2>(cs, sn);
-  }
-}
-
 // Transposed load of columns c0 .. c0 + lines - 1 of slice `g` (rows of n) into
 // lines of `dst` (line c = column c0 + c): thread t takes column t mod 16 of rows
 // t / 16, t / 16 + blockDim / 16, ... (lines <= 16)
@@ -513,7 +494,6 @@ __global__ void __launch_bounds__(256, sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTA
   const int n = pl.n;
   T2 *Abuf = W + 2 * n;
   T2 *SA = Abuf + 2 * L * n;  // filtered source columns (only with srcf)
-  T2 *Py = SA;                // separable: the propagator's column factor by column frequency
   const int nblk = (n + L - 1) / L, ntiles = ns * nblk;
   const size_t ncell = (size_t)n * n;
   const R kdz = (R)k2dz, half = (R)(0.5 * (n - 1));
@@ -522,7 +502,6 @@ __global__ void __launch_bounds__(256, sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTA
   const int c_init = fdiv(threadIdx.x, n, pl.mn), ky_init = threadIdx.x - c_init * n;
   const int dc = fdiv(blockDim.x, n, pl.mn), dky = blockDim.x - dc * n;
   for (int t = threadIdx.x; t < 2 * n - 1; t += blockDim.x) cp_elem(W + t, roots + t);
-  if (sep) prop_factors(Py, n, k2dz);
   int tile = blockIdx.x;
   if (tile < ntiles) {
     const int ii = tile / nblk, c0 = (tile - ii * nblk) * L;
@@ -558,18 +537,13 @@ __global__ void __launch_bounds__(256, sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTA
         const R *st = sigt + (size_t)c0 * n;
         int c = c_init, ky = ky_init;
         for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-          T2 v;
-          if (sep) {
-            v = cm(A[t], Py[ky]);
-          } else {
-            int ix = c0 + c + off, iy = ky + off;
-            ix -= ix >= n ? n : 0;
-            iy -= iy >= n ? n : 0;
-            const R dx = (R)ix - half, dy = (R)iy - half;
-            R sn, cs;
-            phase_sincos((dx * dx + dy * dy) * kdz, &sn, &cs);
-            v = cm(A[t], mk<T2>(cs, sn));
-          }
+          int ix = c0 + c + off, iy = ky + off;
+          ix -= ix >= n ? n : 0;
+          iy -= iy >= n ? n : 0;
+          const R dx = (R)ix - half, dy = (R)iy - half;
+          R sn, cs;
+          phase_sincos((sep ? dy * dy : dx * dx + dy * dy) * kdz, &sn, &cs);
+          T2 v = cm(A[t], mk<T2>(cs, sn));
           if (srcf) v = axpy((R)2 * st[t], SA[t], v);
           A[t] = v;
           c += dc;
@@ -618,15 +592,13 @@ __global__ void __launch_bounds__(256, sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTA
   T2 *W = reinterpret_cast<T2 *>(smem_raw);
   const int n = pl.n;
   T2 *Abuf = W + 2 * n;
-  T2 *Px = Abuf + 2 * L * n;  // the propagator's row factor by row frequency
   const int nblk = (n + L - 1) / L, ntiles = ns * nblk;
   const size_t ncell = (size_t)n * n;
-  // row frequency of tile element t = threadIdx.x + m blockDim.x: t mod n, advanced by
-  // blockDim.x mod n per step
-  const int kx_init = threadIdx.x - fdiv(threadIdx.x, n, pl.mn) * n;
-  const int dkx = blockDim.x - fdiv(blockDim.x, n, pl.mn) * n;
+  const R kdz = (R)k2dz, half = (R)(0.5 * (n - 1));
+  const int off = n - (n + 1) / 2;
+  const int l_init = fdiv(threadIdx.x, n, pl.mn), kx_init = threadIdx.x - l_init * n;
+  const int dl = fdiv(blockDim.x, n, pl.mn), dkx = blockDim.x - dl * n;
   for (int t = threadIdx.x; t < 2 * n - 1; t += blockDim.x) cp_elem(W + t, roots + t);
-  prop_factors(Px, n, k2dz);
   int tile = blockIdx.x;
   if (tile < ntiles) {
     const int ii = tile / nblk, r0 = (tile - ii * nblk) * L, cnt = min(L, n - r0) * n;
@@ -651,11 +623,20 @@ __global__ void __launch_bounds__(256, sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTA
     for (int job = 0; job < 2; job++) {
       const bool inverse = job == 1;
       if (inverse) {
-        int kx = kx_init;
+        int l = l_init, kx = kx_init;
         for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-          A[t] = cm(A[t], Px[kx]);
+          int ix = kx + off;
+          ix -= ix >= n ? n : 0;
+          const R dx = (R)ix - half;
+          R sn, cs;
+          phase_sincos(dx * dx * kdz, &sn, &cs);
+          A[t] = cm(A[t], mk<T2>(cs, sn));
+          l += dl;
           kx += dkx;
-          if (kx >= n) kx -= n;
+          if (kx >= n) {
+            kx -= n;
+            l++;
+          }
         }
         __syncthreads();
       }
@@ -808,13 +789,12 @@ void launch_fft(void *stream, void *field, const void *src, void *work, const vo
   typedef typename Real<T2>::T R;
   if (!filtered) {
     // two passes: rows with their propagator factor, columns with theirs and the source
-    // (each pass holds its propagator factors, n elements, beside the tile buffers)
     const int Lr = fft_lines_per_cta(pl, es, 2, 32, rows_ctas);
-    const size_t mr = fft_smem(n, Lr, 2, (size_t)es) + (size_t)n * es;
+    const size_t mr = fft_smem(n, Lr, 2, (size_t)es);
     k_fft_rows_prop<T2><<<grid(Lr, mr, rows_ctas), FFT_THREADS, mr, s>>>(f, rt, k2c * delz, pl, ns, first,
                                                                         1.0 / n, Lr);
     const int Lc = fft_lines_per_cta(pl, es, 2, 16, cols_ctas);
-    const size_t mc = fft_smem(n, Lc, 2, (size_t)es) + (size_t)n * es;
+    const size_t mc = fft_smem(n, Lc, 2, (size_t)es);
     k_fft_cols<T2><<<grid(Lc, mc, cols_ctas), FFT_THREADS, mc, s>>>(f, nullptr, rt, k2c * delz, (const R *)sig, pl,
                                                                    ns, first, Lc, 1, sr, 1.0 / n);
     return;
