@@ -587,9 +587,8 @@ def harmonic_fft_form(g4gpu, torch, steps, warmup, peak, nsub=256, ns=None):
     tot = max(sum(x[1] for x in st.values()), 1e-12)
     kern = {k: {"launches": n, "ms_total": t, "ms_avg": t / n, "share": t / tot} for k, (n, t) in st.items() if n}
     # FFT solve of one field over the window: at least the field read and written and
-    # the source read once (FP32 complex: 24 B per cell); the separable two-pass solve
-    # (rows with their propagator factor, columns with theirs and the source) moves 40 B
-    # per cell
+    # the source read once (FP32 complex: 24 B per cell); the three-pass transform
+    # (rows, columns, rows through global memory) moves 56 B per cell
     fft_alg = len(HARM_H) * ns * ncell * 24.0 * steps
     fft_ms = st["fft"][1]
     out = {"value": ns * steps / (ms / 1e3), "unit": "slice-steps/s", "ms_per_step": ms / steps,
@@ -598,7 +597,7 @@ def harmonic_fft_form(g4gpu, torch, steps, warmup, peak, nsub=256, ns=None):
            "kernels": kern}
     if fft_ms > 0:
         a = fft_alg / (fft_ms / 1e3) / 1e9
-        out["fft_roofline"] = {"bound": "hbm", "alg_bytes_per_cell": 24, "design_bytes_per_cell": 40,
+        out["fft_roofline"] = {"bound": "hbm", "alg_bytes_per_cell": 24, "design_bytes_per_cell": 56,
                                "achieved_gbs": a, "peak": peak, "frac": a / peak,
                                "ms_per_field_solve": fft_ms / (steps * len(HARM_H))}
     pw = {}

@@ -1231,9 +1231,7 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
         const void *srck = any_dep ? h->src[k] : nullptr;
         // a zero source makes the filtered term vanish (FieldSolverFFT.cpp:74-90)
         int filtered = c.source_filter && srck && c.sigmoid > 0 && c.xcut > 0 && c.ycut > 0;
-        // filtered: rows of the field and of the source, columns, inverse rows; else the
-        // separable solve's row and column passes
-        Timed t(h, G4GPU_K_FFT, filtered ? 4 : 2);
+        Timed t(h, G4GPU_K_FFT, 3);
         g4::launch_fft_solve(h->stream, h->mixed, h->field[k], srck, h->tmp, h->fft_roots[k], h->fft_k2c[k],
                              h->fft_sig[k], filtered, sc.delz, h->fft_plan, ns, sc.f[k].first);
       }

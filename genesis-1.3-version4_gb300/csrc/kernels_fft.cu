@@ -5,18 +5,12 @@
 // unnormalised) and K2 = -i (dx^2 + dy^2) dk^2 / (2 xks) on the reference's
 // shifted frequency map (FieldSolverFFT.cpp:131-145).
 //
-// Unfiltered, the propagator exp(K2 dz) = exp(-i (dx^2 + dy^2) c) is the product of a
-// factor of the row frequency and one of the column frequency, and the 2-D transform
-// is the row transforms followed by the column transforms; so the step separates into
-// two passes over global memory, each on tiles of whole lines in shared memory:
-//   rows:    forward FFT of every row, exp(-i dx^2 c), inverse FFT, 1/n
-//   columns: forward FFT of every column, exp(-i dy^2 c), inverse FFT, 1/n, + 2 src
-// (40 bytes of global traffic per cell in FP32 instead of the 56 of a 2-D transform
-// and back). Filtered, the sigmoid does not separate, and the solve is three passes:
-//   rows:    forward FFT of every row (and of the source rows)
-//   columns: forward FFT of every column, the k-space propagator and filtered
-//            source, inverse FFT of every column
-//   rows:    inverse FFT of every row, 1/n^2
+// The 2-D transform of each ngrid x ngrid slice is done as three passes over
+// global memory, each on tiles of whole lines in shared memory:
+//   rows:    forward FFT of every row (and, filtered, of the source rows)
+//   columns: forward FFT of every column, the k-space propagator (and filtered
+//            source), inverse FFT of every column
+//   rows:    inverse FFT of every row, 1/n^2, + 2 src when unfiltered
 // The passes are persistent CTAs whose next tile's loads, issued at once as
 // asynchronous copies, are in flight while the current tile is transformed.
 // Every 1-D transform is a Stockham autosort mixed-radix FFT over the factors of
@@ -479,15 +473,10 @@ __device__ __forceinline__ void load_cols(T2 *dst, const T2 *g, int n, int c0, i
 // likewise dy; sigt holds the sigmoid transposed, sigt[kx n + ky], so that the
 // reads of a column are contiguous; srcf (filtered) holds the row-transformed
 // source of slice ii, staged in a third tile buffer.
-// Separable mode (sep): the propagator's column factor exp(i dy^2 k2dz) only (the row
-// factor was applied by k_fft_rows_prop), and the columns are written back times
-// `scale` plus 2 src (src: beam slice ii, null for none): the last pass of the
-// unfiltered solve.
 template <typename T2>
 __global__ void __launch_bounds__(256, sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTAS_FP64)
     k_fft_cols(T2 *__restrict__ field, const T2 *__restrict__ srcf, const T2 *__restrict__ roots, double k2dz,
-               const typename Real<T2>::T *__restrict__ sigt, FFTPlan pl, int ns, int first, int L, int sep,
-               const T2 *__restrict__ src, double scale) {
+               const typename Real<T2>::T *__restrict__ sigt, FFTPlan pl, int ns, int first, int L) {
   typedef typename Real<T2>::T R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T2 *W = reinterpret_cast<T2 *>(smem_raw);
@@ -542,7 +531,7 @@ __global__ void __launch_bounds__(256, sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTA
           iy -= iy >= n ? n : 0;
           const R dx = (R)ix - half, dy = (R)iy - half;
           R sn, cs;
-          phase_sincos((sep ? dy * dy : dx * dx + dy * dy) * kdz, &sn, &cs);
+          phase_sincos((dx * dx + dy * dy) * kdz, &sn, &cs);
           T2 v = cm(A[t], mk<T2>(cs, sn));
           if (srcf) v = axpy((R)2 * st[t], SA[t], v);
           A[t] = v;
@@ -558,93 +547,10 @@ __global__ void __launch_bounds__(256, sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTA
       fft_lines(job == 1 && srcf ? SA : A, n, lines, pl, W, inverse);
     }
     const int tc = threadIdx.x & 15;
-    if (tc < lines) {
-      if (sep) {
-        const R sc = (R)scale;
-        const T2 *sv = src ? src + (size_t)ii * ncell : nullptr;
-        for (int row = threadIdx.x >> 4; row < n; row += blockDim.x >> 4) {
-          const size_t g = (size_t)row * n + c0 + tc;
-          T2 v = axpy(sc, A[tc * n + row], mk<T2>(0, 0));
-          if (sv) v = axpy((R)2, sv[g], v);
-          u[g] = v;
-        }
-      } else {
-        for (int row = threadIdx.x >> 4; row < n; row += blockDim.x >> 4)
-          u[(size_t)row * n + c0 + tc] = A[tc * n + row];
-      }
-    }
+    if (tc < lines)
+      for (int row = threadIdx.x >> 4; row < n; row += blockDim.x >> 4)
+        u[(size_t)row * n + c0 + tc] = A[tc * n + row];
     __syncthreads();
-  }
-  cp_wait<0>();
-}
-
-// Row pass of the separable (unfiltered) solve over tiles of L rows: forward FFT of
-// the rows, the row factor exp(i dx^2 k2dz) of the propagator at the row frequency kx
-// (dx from the shifted map as in k_fft_cols), inverse FFT, times `scale`, written back
-// in place. The two transforms run in one loop so that the kernel holds one copy of
-// their code.
-template <typename T2>
-__global__ void __launch_bounds__(256, sizeof(T2) == 8 ? FFT_CTAS_FP32 : FFT_CTAS_FP64)
-    k_fft_rows_prop(T2 *__restrict__ field, const T2 *__restrict__ roots, double k2dz, FFTPlan pl, int ns,
-                    int first, double scale, int L) {
-  typedef typename Real<T2>::T R;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T2 *W = reinterpret_cast<T2 *>(smem_raw);
-  const int n = pl.n;
-  T2 *Abuf = W + 2 * n;
-  const int nblk = (n + L - 1) / L, ntiles = ns * nblk;
-  const size_t ncell = (size_t)n * n;
-  const R kdz = (R)k2dz, half = (R)(0.5 * (n - 1));
-  const int off = n - (n + 1) / 2;
-  const int l_init = fdiv(threadIdx.x, n, pl.mn), kx_init = threadIdx.x - l_init * n;
-  const int dl = fdiv(blockDim.x, n, pl.mn), dkx = blockDim.x - dl * n;
-  for (int t = threadIdx.x; t < 2 * n - 1; t += blockDim.x) cp_elem(W + t, roots + t);
-  int tile = blockIdx.x;
-  if (tile < ntiles) {
-    const int ii = tile / nblk, r0 = (tile - ii * nblk) * L, cnt = min(L, n - r0) * n;
-    const T2 *g = field + (size_t)((ii + first) % ns) * ncell + (size_t)r0 * n;
-    for (int t = threadIdx.x; t < cnt; t += blockDim.x) cp_elem(Abuf + t, g + t);
-  }
-  cp_commit();
-  for (int it = 0; tile < ntiles; tile += gridDim.x, it++) {
-    T2 *A = Abuf + (it & 1) * L * n;
-    const int ii = tile / nblk, r0 = (tile - ii * nblk) * L, lines = min(L, n - r0);
-    const int nx = tile + gridDim.x;
-    if (nx < ntiles) {
-      const int jj = nx / nblk, q0 = (nx - jj * nblk) * L, qc = min(L, n - q0) * n;
-      const T2 *g = field + (size_t)((jj + first) % ns) * ncell + (size_t)q0 * n;
-      T2 *dst = Abuf + ((it + 1) & 1) * L * n;
-      for (int t = threadIdx.x; t < qc; t += blockDim.x) cp_elem(dst + t, g + t);
-    }
-    cp_commit();
-    cp_wait<1>();  // this tile's rows (committed one iteration earlier)
-    __syncthreads();
-    T2 *o = field + (size_t)((ii + first) % ns) * ncell + (size_t)r0 * n;
-    for (int job = 0; job < 2; job++) {
-      const bool inverse = job == 1;
-      if (inverse) {
-        int l = l_init, kx = kx_init;
-        for (int t = threadIdx.x; t < lines * n; t += blockDim.x) {
-          int ix = kx + off;
-          ix -= ix >= n ? n : 0;
-          const R dx = (R)ix - half;
-          R sn, cs;
-          phase_sincos(dx * dx * kdz, &sn, &cs);
-          A[t] = cm(A[t], mk<T2>(cs, sn));
-          l += dl;
-          kx += dkx;
-          if (kx >= n) {
-            kx -= n;
-            l++;
-          }
-        }
-        __syncthreads();
-      }
-      // the inverse's last stage writes the rows to global memory, scaled
-      fft_lines(A, n, lines, pl, W, inverse, inverse ? o : (T2 *)nullptr,
-                Epilogue<T2>{(R)(inverse ? scale : 1.0), nullptr}, false);
-    }
-    __syncthreads();  // A is free for the copies of the next iteration
   }
   cp_wait<0>();
 }
@@ -771,7 +677,6 @@ void launch_fft(void *stream, void *field, const void *src, void *work, const vo
   if (dev < 64 && !(configured.load() & (1ull << dev))) {
     cudaFuncSetAttribute(k_fft_rows<T2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_fft_rows<T2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(k_fft_rows_prop<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(k_fft_cols<T2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     configured.fetch_or(1ull << dev);
   }
@@ -787,18 +692,6 @@ void launch_fft(void *stream, void *field, const void *src, void *work, const vo
   T2 *sfw = filtered ? (T2 *)work : nullptr;
   const T2 *rt = (const T2 *)roots;
   typedef typename Real<T2>::T R;
-  if (!filtered) {
-    // two passes: rows with their propagator factor, columns with theirs and the source
-    const int Lr = fft_lines_per_cta(pl, es, 2, 32, rows_ctas);
-    const size_t mr = fft_smem(n, Lr, 2, (size_t)es);
-    k_fft_rows_prop<T2><<<grid(Lr, mr, rows_ctas), FFT_THREADS, mr, s>>>(f, rt, k2c * delz, pl, ns, first,
-                                                                        1.0 / n, Lr);
-    const int Lc = fft_lines_per_cta(pl, es, 2, 16, cols_ctas);
-    const size_t mc = fft_smem(n, Lc, 2, (size_t)es);
-    k_fft_cols<T2><<<grid(Lc, mc, cols_ctas), FFT_THREADS, mc, s>>>(f, nullptr, rt, k2c * delz, (const R *)sig, pl,
-                                                                   ns, first, Lc, 1, sr, 1.0 / n);
-    return;
-  }
   // forward rows of the field (and, filtered, of the source into the work array)
   const int Lr = fft_lines_per_cta(pl, es, 2, 32, rows_ctas);
   const size_t mr = fft_smem(n, Lr, 2, (size_t)es);
@@ -810,7 +703,7 @@ void launch_fft(void *stream, void *field, const void *src, void *work, const vo
   const int Lc = fft_lines_per_cta(pl, es, bc, 16, cols_ctas);
   const size_t mc = fft_smem(n, Lc, bc, (size_t)es);
   k_fft_cols<T2><<<grid(Lc, mc, cols_ctas), FFT_THREADS, mc, s>>>(f, sfw, rt, k2c * delz, (const R *)sig, pl,
-                                                                 ns, first, Lc, 0, nullptr, 1.0);
+                                                                 ns, first, Lc);
   // inverse rows, 1/n^2, + 2 src when unfiltered (the source rows in a third tile
   // buffer, at one CTA per SM fewer)
   const T2 *s1 = filtered ? nullptr : sr;

@@ -335,11 +335,7 @@ def test_fft_solver_plain_matches_oracle(lib, oracle, solver, filt, n):
         p = h.get_beam()
         f0, first0, _ = h.get_field(0)
         f1, _, _ = h.get_field(1)
-        # per field and step: the separable solve's two passes, or the filtered solve's
-        # four where a source is deposited (undulator steps)
-        und = int(np.count_nonzero(lat[:, T.C["aw"]] > 0))
-        per_field = 2 * lat.shape[0] + (2 * und if solver == 2 else 0)
-        assert h.kernel_stats()["fft"][0] == 2 * per_field
+        assert h.kernel_stats()["fft"][0] == 3 * 2 * lat.shape[0]
     rp, rf, rfirst, _ = oracle.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, [1, 3], [6e-5, 4e-5], fld, [0, 0],
                                          solver=solver, filt=filt, periodic=1)
     assert first0 == rfirst[0]
