@@ -699,7 +699,7 @@ def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_s
                          "generate_s": t_gen, "train_s": t_train}}
 
 
-E2E_WINDOWS = 7
+E2E_WINDOWS = 11
 
 
 def e2e_window(g4gpu, torch, precision, beam_pinned, cur, field_pinned, lat, steps, reps, shapes=None):
