@@ -47,6 +47,7 @@ struct g4gpu_mlp_ctx {
   float *dA = nullptr, *dZ = nullptr;
   __nv_bfloat16 *dZb = nullptr, *dZt = nullptr;
   float *xin = nullptr, *tgt = nullptr, *loss = nullptr;
+  int *derr = nullptr;  // device flag: a tensor-core GEMM's bounded wait ran out
   int adam_t = 0;
   std::string err;
 };
@@ -62,6 +63,15 @@ int mfail(g4gpu_mlp m, int code, const std::string &msg) {
     cudaError_t e_ = (call);                                                       \
     if (e_ != cudaSuccess) return mfail(m, G4GPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
+
+// G4GPU_ERR_DEVICE if a GEMM of the network raised the device flag; called after
+// the stream has been synchronised
+int mlp_device_status(g4gpu_mlp m) {
+  int v = 0;
+  M_CUDA(m, cudaMemcpy(&v, m->derr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v) return mfail(m, G4GPU_ERR_DEVICE, "mlp: a tensor-core GEMM did not complete within its bounded wait");
+  return G4GPU_OK;
+}
 
 int ensure_cap(g4gpu_mlp m, int rows) {
   if (rows <= m->cap) return G4GPU_OK;
@@ -105,7 +115,7 @@ void forward(g4gpu_mlp m, int rows) {
   for (int l = 0; l < kLayers; l++) {
     int K = m->dims[l], N = m->dims[l + 1];
     g4::mlp_gemm_nt(m->stream, m->actb[l], m->wb + m->wboff[l], m->params + m->boff[l], m->act[l + 1],
-                    m->actb[l + 1], rows, N, K, l < kLayers - 1, 0);
+                    m->actb[l + 1], rows, N, K, l < kLayers - 1, 0, m->derr);
   }
 }
 
@@ -120,11 +130,13 @@ void backward(g4gpu_mlp m, int rows) {
     // dW [N][K] = dZ^T A_l
     g4::mlp_transpose_bf16(m->stream, m->dZb, m->dZt, rows, N);
     g4::mlp_transpose_bf16(m->stream, m->actb[l], m->actt, rows, K);
-    g4::mlp_gemm_nt(m->stream, m->dZt, m->actt, nullptr, m->grads + m->woff[l], nullptr, N, K, rows, 0, 0);
+    g4::mlp_gemm_nt(m->stream, m->dZt, m->actt, nullptr, m->grads + m->woff[l], nullptr, N, K, rows, 0, 0,
+                    m->derr);
     g4::mlp_colsum(m->stream, m->dZ, m->grads + m->boff[l], rows, N);
     // dA_l [rows][K] = dZ W_l
     if (l > 0)
-      g4::mlp_gemm_nt(m->stream, m->dZb, m->wbt + m->wboff[l], nullptr, m->dA, nullptr, rows, K, N, 0, 0);
+      g4::mlp_gemm_nt(m->stream, m->dZb, m->wbt + m->wboff[l], nullptr, m->dA, nullptr, rows, K, N, 0, 0,
+                      m->derr);
   }
 }
 
@@ -201,7 +213,7 @@ int g4gpu_mlp_create(int nin, int width, int nout, int seed, int device, g4gpu_m
             cudaMalloc(&m->wb, nw * 2) == cudaSuccess && cudaMalloc(&m->wbt, nw * 2) == cudaSuccess &&
             cudaMalloc(&m->fmean, nin * 4) == cudaSuccess && cudaMalloc(&m->fstd, nin * 4) == cudaSuccess &&
             cudaMalloc(&m->oscale, nout * 4) == cudaSuccess && cudaMalloc(&m->oshift, nout * 4) == cudaSuccess &&
-            cudaMalloc(&m->loss, 4) == cudaSuccess;
+            cudaMalloc(&m->loss, 4) == cudaSuccess && cudaMalloc(&m->derr, 4) == cudaSuccess;
   if (!ok) {
     g4gpu_mlp_destroy(m);
     return g4_fail(nullptr, G4GPU_ERR_NOMEM, "mlp: allocation failed");
@@ -209,6 +221,7 @@ int g4gpu_mlp_create(int nin, int width, int nout, int seed, int device, g4gpu_m
   cudaMemcpy(m->params, p.data(), m->nparam * 4, cudaMemcpyHostToDevice);
   cudaMemset(m->m, 0, m->nparam * 4);
   cudaMemset(m->v, 0, m->nparam * 4);
+  cudaMemset(m->derr, 0, 4);
   m->h_fmean.assign(nin, 0.f);
   m->h_fstd.assign(nin, 1.f);
   m->h_oshift.assign(nout, 0.f);
@@ -225,7 +238,8 @@ void g4gpu_mlp_destroy(g4gpu_mlp m) {
   cudaSetDevice(m->device);
   if (m->stream) cudaStreamSynchronize(m->stream);
   void *ptrs[] = {m->params, m->grads, m->m,  m->v,   m->wb,  m->wbt,  m->fmean, m->fstd, m->oscale,
-                  m->oshift, m->actt,  m->dA, m->dZ,  m->dZb, m->dZt,  m->xin,   m->tgt,  m->loss};
+                  m->oshift, m->actt,  m->dA, m->dZ,  m->dZb, m->dZt,  m->xin,   m->tgt,  m->loss,
+                  m->derr};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (int l = 0; l <= kLayers; l++) {
@@ -285,7 +299,7 @@ int g4gpu_mlp_forward(g4gpu_mlp m, const float *X, int n, float *Y) {
   g4::closure_denormalize(m->stream, m->act[kLayers], m->oscale, m->oshift, yd, n, m->nout, m->dims[kLayers]);
   M_CUDA(m, cudaMemcpyAsync(Y, yd, (size_t)n * m->nout * 4, cudaMemcpyDeviceToHost, m->stream));
   M_CUDA(m, cudaStreamSynchronize(m->stream));
-  return G4GPU_OK;
+  return mlp_device_status(m);
 }
 
 // Gradients of the MSE loss of normalised outputs over n rows (one batch, no update).
@@ -301,7 +315,7 @@ int g4gpu_mlp_gradients(g4gpu_mlp m, const float *X, const float *T, int n, floa
   M_CUDA(m, cudaMemcpyAsync(grads, m->grads, m->nparam * 4, cudaMemcpyDeviceToHost, m->stream));
   if (loss) M_CUDA(m, cudaMemcpyAsync(loss, m->loss, 4, cudaMemcpyDeviceToHost, m->stream));
   M_CUDA(m, cudaStreamSynchronize(m->stream));
-  return G4GPU_OK;
+  return mlp_device_status(m);
 }
 
 // Adam training on n rows of raw features X [n][nin] and targets T [n][nout].
@@ -365,6 +379,7 @@ int g4gpu_mlp_train(g4gpu_mlp m, const float *X, const float *T, int n, int epoc
     float l = 0;
     M_CUDA(m, cudaMemcpyAsync(&l, m->loss, 4, cudaMemcpyDeviceToHost, m->stream));
     M_CUDA(m, cudaStreamSynchronize(m->stream));
+    if ((rc = mlp_device_status(m))) return rc;
     if (loss_per_epoch) loss_per_epoch[ep] = nb ? l / nb : 0.f;
   }
   return G4GPU_OK;
@@ -470,8 +485,11 @@ static int closure_correct(g4gpu_handle h) {
   int ns = c.nslice;
   int rc = ensure_cap(m, ns);
   if (rc) return g4_fail(h, rc, m->err);
+  // the network runs on the handle's stream and raises the handle's device flag
   cudaStream_t saved = m->stream;
+  int *saved_err = m->derr;
   m->stream = h->stream;
+  m->derr = h->derr;
   g4::closure_normalize(h->stream, h->closure_feat, m->fmean, m->fstd, m->actb[0], ns, m->nin, m->dims[0]);
   forward(m, ns);
   g4::closure_denormalize(h->stream, m->act[kLayers], m->oscale, m->oshift, h->closure_corr, ns, m->nout,
@@ -479,6 +497,7 @@ static int closure_correct(g4gpu_handle h) {
   g4::closure_apply(h->stream, h->beam.theta, h->beam.gamma, h->field[0], h->closure_corr, h->mixed, ns,
                     c.npart, c.ngrid, h->first[0]);
   m->stream = saved;
+  m->derr = saved_err;
   h->launches[G4GPU_K_MISC] += 3 + kLayers;
   return G4GPU_OK;
 }

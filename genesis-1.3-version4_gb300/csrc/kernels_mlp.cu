@@ -2,12 +2,18 @@
 // (inputs -> 256 -> 256 -> 256 -> outputs) evaluated and trained on the GPU.
 //
 // GEMM: C[M][N] = sum_k A[M][k] B[N][k] ("NT": both operands row-major with the
-// reduction index last), BF16 operands, FP32 accumulation, with mma.sync
-// m16n8k16. The GEMMs of this network are small (M = slices, N, K <= 256) and
-// latency-bound; the warp-level MMA needs no tensor-memory allocation or
-// descriptor set-up per launch, which at these sizes costs more than it saves.
-// Each CTA computes a 64 x 64 tile with 4 warps (32 x 32 each); K is staged through
-// shared memory in chunks of 32.
+// reduction index last), BF16 operands, FP32 accumulation. Two kernels:
+//
+//   k_gemm_tc   the 5th-generation tensor cores (tcgen05): a CTA computes a 128 x BN
+//               tile (BN <= 128) with its accumulator in tensor memory. The whole
+//               reduction (K <= 256) is staged in shared memory at once, one thread
+//               issues the K / 16 MMAs, their completion arrives on an mbarrier, and
+//               the four warps read the accumulator back (tcgen05.ld) for the bias /
+//               ReLU epilogue. Every GEMM of the forward pass and the dA = dZ W
+//               products of the backward pass take it.
+//   k_gemm_nt   warp-level mma.sync m16n8k16, 64 x 64 tiles, K staged in chunks of 32:
+//               the weight gradients dW = dZ^T A, whose reduction runs over the batch
+//               rows (thousands), beyond what k_gemm_tc stages.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -106,6 +112,174 @@ __global__ void __launch_bounds__(128) k_gemm_nt(const __nv_bfloat16 *__restrict
       }
 }
 
+// ---- k_gemm_tc: tcgen05 MMA with the accumulator in tensor memory --------------
+constexpr int kTcM = 128;     // tile rows: the accumulator's 128 TMEM lanes
+constexpr int kTcMaxK = 256;  // the reduction is staged whole
+constexpr int kTcMaxN = 128;  // tile columns (TMEM columns of FP32 accumulator)
+// Shared memory of a CTA at least this large keeps at most 3 CTAs on an SM, so their
+// accumulators (<= 128 TMEM columns each) always fit the SM's 512 columns and no
+// allocation has to wait for another CTA.
+constexpr size_t kTcMinSmem = 60 * 1024;
+constexpr long long kTcSpin = 1LL << 22;  // bounded mbarrier polls
+
+// Operand tiles in shared memory are K-major without swizzle: 8 x 16-byte core
+// matrices (8 rows of 8 BF16 along K). The core matrix of row group g and K chunk c
+// (k / 8) sits at byte (g * K / 8 + c) * 128, its row r % 8 at + 16 (r % 8). In the
+// MMA's shared-memory descriptors, core matrices adjacent in K are 128 B apart (the
+// leading byte offset) and row groups K * 16 B apart (the stride byte offset).
+__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);  // version 1; no swizzle, base offset 0
+}
+
+// Instruction descriptor of tcgen05.mma kind::f16: D in F32 (bits 4-5 = 1), A and B
+// BF16 (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N / 8 at bit 17,
+// M / 16 at bit 24.
+__device__ __forceinline__ uint32_t tc_idesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// Stages rows [r0, r0 + rows) x [0, K) of the row-major matrix X (K columns, nrow
+// valid rows; zero past them) into the tile at shared address T with 16-byte
+// cp.async copies. Copy idx takes row (idx / (8 K/8)) * 8 + idx % 8 and chunk
+// (idx / 8) % (K / 8), which is the tile's byte idx * 16: consecutive threads write
+// consecutive 16 bytes.
+__device__ __forceinline__ void tc_stage(uint32_t T, const __nv_bfloat16 *__restrict__ X, int r0, int rows, int nrow,
+                                         int K) {
+  const int ck = K >> 3;
+  const int total = rows * ck;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int r = ((idx >> 3) / ck) * 8 + (idx & 7), c = (idx >> 3) % ck;
+    const bool ok = r0 + r < nrow;
+    const __nv_bfloat16 *src = ok ? X + (size_t)(r0 + r) * K + c * 8 : X;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(T + (uint32_t)idx * 16u), "l"(src),
+                 "r"(ok ? 16 : 0)
+                 : "memory");
+  }
+}
+
+// two FP32 values rounded to BF16, the first in the low half (the lower address)
+__device__ __forceinline__ uint32_t pack_bf2(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t *>(&h);
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
+  for (long long it = 0; it < kTcSpin; it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// C = A B^T (+ bias[n]) with optional ReLU, as k_gemm_nt, for K a multiple of 16 up
+// to kTcMaxK and a tile width BN (a multiple of 16 up to kTcMaxN) dividing N. 128
+// threads; CTA (bx, by) computes rows [128 bx, 128 bx + 128) and columns
+// [BN by, BN by + BN). Shared memory: A tile (128 x K), B tile (BN x K), the MMA
+// mbarrier, the TMEM address. If the MMAs do not complete within the bounded wait,
+// *err is set, the CTA waits once more (bounded) so that no MMA still writes the
+// accumulator, frees its tensor memory and writes nothing.
+__global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict__ A,
+                                                 const __nv_bfloat16 *__restrict__ B,
+                                                 const float *__restrict__ bias, float *C, __nv_bfloat16 *Cb,
+                                                 int M, int N, int K, int BN, int relu, int accumulate, int *err) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  const uint32_t sA = (uint32_t)__cvta_generic_to_shared(tc_smem);
+  const uint32_t sB = sA + (uint32_t)(kTcM * K * 2);
+  const uint32_t sbar = sB + (uint32_t)(BN * K * 2), sadr = sbar + 8;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kTcM, n0 = blockIdx.y * BN;
+  uint32_t ncols = 32;  // TMEM columns: a power of two >= 32
+  while ((int)ncols < BN) ncols <<= 1;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sadr), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_stage(sA, A, m0, kTcM, M, K);
+  tc_stage(sB, B, n0, BN, N, K);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  // the staged tiles, written through the generic proxy, made visible to the MMAs
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  uint32_t tmem;
+  asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(sadr) : "memory");
+  if (threadIdx.x == 0) {
+    const uint32_t idesc = tc_idesc(kTcM, BN);
+    const uint32_t sbo = (uint32_t)K * 16u;
+    for (int s = 0; s < K / 16; s++) {
+      // K step s: core-matrix chunks 2s and 2s + 1 of every row group
+      const uint64_t ad = tc_smem_desc(sA + (uint32_t)s * 256u, 128u, sbo);
+      const uint64_t bd = tc_smem_desc(sB + (uint32_t)s * 256u, 128u, sbo);
+      asm volatile(
+          "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+          " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+          "l"(ad), "l"(bd), "r"(idesc), "r"(s)
+          : "memory");
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(sbar)
+                 : "memory");
+  }
+  const bool done = __syncthreads_and(tc_wait(sbar, 0)) != 0;
+  if (!done) {
+    if (threadIdx.x == 0) {
+      atomicExch(err, 1);
+      tc_wait(sbar, 0);
+    }
+  } else {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // warp w reads TMEM lanes [32 w, 32 w + 32): the rows of the tile it owns
+    const int r = m0 + warp * 32 + lane;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int c0 = 0; c0 < BN; c0 += 8) {
+      uint32_t v[8];
+      // the load and its wait in one statement: no use of v can be placed between them
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+          "tcgen05.wait::ld.sync.aligned;\n"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+          : "r"(trow + (uint32_t)c0)
+          : "memory");
+      if (r < M) {
+        const int c = n0 + c0;
+        float o[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          float x = __uint_as_float(v[j]);
+          if (accumulate && C) x += C[(size_t)r * N + c + j];
+          if (bias) x += bias[c + j];
+          if (relu) x = fmaxf(x, 0.f);
+          o[j] = x;
+        }
+        if (C) {
+          float4 *d = reinterpret_cast<float4 *>(C + (size_t)r * N + c);
+          d[0] = make_float4(o[0], o[1], o[2], o[3]);
+          d[1] = make_float4(o[4], o[5], o[6], o[7]);
+        }
+        if (Cb)
+          *reinterpret_cast<uint4 *>(Cb + (size_t)r * N + c) =
+              make_uint4(pack_bf2(o[0], o[1]), pack_bf2(o[2], o[3]), pack_bf2(o[4], o[5]), pack_bf2(o[6], o[7]));
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+}
+
 // out[c][r] = in[r][c] for a rows x cols bf16 matrix
 __global__ void k_transpose_bf16(const __nv_bfloat16 *in, __nv_bfloat16 *out, int rows, int cols) {
   __shared__ __nv_bfloat16 tile[32][33];
@@ -186,8 +360,29 @@ unsigned blocks_for(size_t n) {
 
 }  // namespace
 
+int mlp_tile_n(int N, int K) {
+  if (K < 16 || K > kTcMaxK || K % 16) return 0;
+  const int bn = N <= kTcMaxN ? N : (N % kTcMaxN == 0 ? kTcMaxN : 0);
+  return bn >= 16 && bn % 16 == 0 ? bn : 0;
+}
+
 void mlp_gemm_nt(void *stream, const void *A, const void *B, const float *bias, float *C, void *Cb, int M,
-                 int N, int K, int relu, int accumulate) {
+                 int N, int K, int relu, int accumulate, int *err) {
+  if (M <= 0 || N <= 0) return;
+  const int bn = mlp_tile_n(N, K);
+  if (bn) {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+      attr = true;
+    }
+    size_t smem = (size_t)(kTcM + bn) * K * 2 + 16;
+    if (smem < kTcMinSmem) smem = kTcMinSmem;
+    dim3 grid((M + kTcM - 1) / kTcM, N / bn);
+    k_gemm_tc<<<grid, 128, smem, (cudaStream_t)stream>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, bias,
+                                                        C, (__nv_bfloat16 *)Cb, M, N, K, bn, relu, accumulate, err);
+    return;
+  }
   dim3 grid((M + TM - 1) / TM, (N + TN - 1) / TN);
   k_gemm_nt<<<grid, 128, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, bias,
                                                      C, (__nv_bfloat16 *)Cb, M, N, K, relu, accumulate);

@@ -44,6 +44,32 @@ def test_mlp_gradients_match_cpu_oracle(lib, n):
             o += size
 
 
+@pytest.mark.parametrize("n,width", [(4096, 256), (1000, 96), (333, 48), (700, 512)])
+def test_mlp_forward_matches_cpu_oracle(lib, n, width):
+    """The forward pass over a window's worth of rows: the tcgen05 GEMM (K <= 256, tile
+    width 128, or the whole N up to 128: 96 and 48 here) and, at width 512, the
+    mma.sync GEMM for the K = 512 layers beside it. Ragged row counts leave the last
+    128-row tile partly empty."""
+    import g4gpu
+    import mlp_oracle
+    rng = np.random.default_rng(n + width)
+    m = g4gpu.MLP(32, width, 4, seed=5)
+    p = m.get_params()
+    p = p + (rng.standard_normal(p.size).astype(np.float32) * 0.01) * (p == 0)
+    m.set_params(p)
+    m.set_normalization(np.zeros(32), np.ones(32), np.zeros(4), np.ones(4))
+    X = rng.standard_normal((n, 32)).astype(np.float32)
+    Y = m.forward(X)
+    Y0 = mlp_oracle.forward_backward(m.get_params(), X.astype(np.float64), np.zeros((n, 4)), 32, width, 4,
+                                     bf16=True)[0]
+    m.close()
+    # BF16 activations rounded from FP32 sums taken in another order: a value near a
+    # rounding boundary may round the other way (2^-8 relative) and carry that on
+    scale = np.max(np.abs(Y0))
+    assert np.max(np.abs(Y - Y0)) < 3e-3 * scale
+    assert np.mean(np.abs(Y - Y0)) < 3e-4 * scale
+
+
 def test_mlp_training_lowers_the_loss(lib):
     import g4gpu
     rng = np.random.default_rng(0)
