@@ -271,14 +271,15 @@ void launch_fft_solve(void *stream, int mixed, void *field, const void *src, voi
                       double k2c, const void *sig, int filtered, double delz, const FFTPlan &pl, int ns,
                       int first);
 
-// kernels_mlp.cu: BF16 tensor-core MLP (FP32 accumulation). mlp_gemm_nt takes the
-// tcgen05 kernel when mlp_tile_n(N, K) gives a tile width (K a multiple of 16 up to
-// 256, N up to 128 or a multiple of 128), else the mma.sync kernel; *err (device)
-// is set if the tcgen05 kernel's bounded wait for its MMAs runs out.
+// kernels_mlp.cu: BF16 tensor-core MLP (tcgen05, FP32 accumulation in tensor
+// memory). mlp_gemm_nt needs N and K multiples of 16 (mlp_tile_n gives the tile
+// width, 0 if unsupported) and returns -1 otherwise; *err (device) is set if a
+// bounded wait for the MMAs runs out. mlp_transpose_bf16 writes ldo >= rows
+// columns, zero past rows.
 int mlp_tile_n(int N, int K);
-void mlp_gemm_nt(void *stream, const void *A, const void *B, const float *bias, float *C, void *Cb, int M,
-                 int N, int K, int relu, int accumulate, int *err);
-void mlp_transpose_bf16(void *stream, const void *in, void *out, int rows, int cols);
+int mlp_gemm_nt(void *stream, const void *A, const void *B, const float *bias, float *C, void *Cb, int M, int N,
+                int K, int relu, int accumulate, int *err);
+void mlp_transpose_bf16(void *stream, const void *in, void *out, int rows, int cols, int ldo);
 void mlp_to_bf16(void *stream, const float *in, void *out, size_t n);
 void mlp_relu_backward(void *stream, const float *dA, const float *Z, float *dZ, void *dZb, size_t n);
 void mlp_colsum(void *stream, const float *dZ, float *db, int rows, int cols);

@@ -90,11 +90,12 @@ int ensure_cap(g4gpu_mlp m, int rows) {
   cudaFree(m->dZt);
   cudaFree(m->xin);
   cudaFree(m->tgt);
-  M_CUDA(m, cudaMalloc(&m->actt, (size_t)cap * wmax * sizeof(__nv_bfloat16)));
+  // transposed operands of the weight gradients: rows padded to a multiple of 16
+  M_CUDA(m, cudaMalloc(&m->actt, (size_t)round16(cap) * wmax * sizeof(__nv_bfloat16)));
   M_CUDA(m, cudaMalloc(&m->dA, (size_t)cap * wmax * sizeof(float)));
   M_CUDA(m, cudaMalloc(&m->dZ, (size_t)cap * wmax * sizeof(float)));
   M_CUDA(m, cudaMalloc(&m->dZb, (size_t)cap * wmax * sizeof(__nv_bfloat16)));
-  M_CUDA(m, cudaMalloc(&m->dZt, (size_t)cap * wmax * sizeof(__nv_bfloat16)));
+  M_CUDA(m, cudaMalloc(&m->dZt, (size_t)round16(cap) * wmax * sizeof(__nv_bfloat16)));
   M_CUDA(m, cudaMalloc(&m->xin, (size_t)cap * m->nin * sizeof(float)));
   M_CUDA(m, cudaMalloc(&m->tgt, (size_t)cap * m->nout * sizeof(float)));
   m->cap = cap;
@@ -106,38 +107,43 @@ void refresh_bf16(g4gpu_mlp m) {
   for (int l = 0; l < kLayers; l++) {
     int K = m->dims[l], N = m->dims[l + 1];
     g4::mlp_to_bf16(m->stream, m->params + m->woff[l], m->wb + m->wboff[l], (size_t)N * K);
-    g4::mlp_transpose_bf16(m->stream, m->wb + m->wboff[l], m->wbt + m->wboff[l], N, K);
+    g4::mlp_transpose_bf16(m->stream, m->wb + m->wboff[l], m->wbt + m->wboff[l], N, K, N);
   }
 }
 
 // forward pass over `rows` rows of normalised BF16 input already in actb[0]
-void forward(g4gpu_mlp m, int rows) {
+int forward(g4gpu_mlp m, int rows) {
   for (int l = 0; l < kLayers; l++) {
     int K = m->dims[l], N = m->dims[l + 1];
-    g4::mlp_gemm_nt(m->stream, m->actb[l], m->wb + m->wboff[l], m->params + m->boff[l], m->act[l + 1],
-                    m->actb[l + 1], rows, N, K, l < kLayers - 1, 0, m->derr);
+    if (g4::mlp_gemm_nt(m->stream, m->actb[l], m->wb + m->wboff[l], m->params + m->boff[l], m->act[l + 1],
+                        m->actb[l + 1], rows, N, K, l < kLayers - 1, 0, m->derr))
+      return mfail(m, G4GPU_ERR_ARG, "mlp: a layer's widths are not multiples of 16");
   }
+  return G4GPU_OK;
 }
 
 // backward pass of the MSE loss against normalised targets tgt [rows][nout];
 // gradients into m->grads, loss into m->loss (accumulated)
-void backward(g4gpu_mlp m, int rows) {
+int backward(g4gpu_mlp m, int rows) {
   int L = kLayers;
+  const int rows16 = round16(rows);  // the weight gradients' reduction, zero-padded
   g4::mlp_mse(m->stream, m->act[L], m->tgt, m->dZ, m->dZb, rows, m->nout, m->dims[L], m->loss);
   for (int l = L - 1; l >= 0; l--) {
     int K = m->dims[l], N = m->dims[l + 1];
     if (l < L - 1) g4::mlp_relu_backward(m->stream, m->dA, m->act[l + 1], m->dZ, m->dZb, (size_t)rows * N);
     // dW [N][K] = dZ^T A_l
-    g4::mlp_transpose_bf16(m->stream, m->dZb, m->dZt, rows, N);
-    g4::mlp_transpose_bf16(m->stream, m->actb[l], m->actt, rows, K);
-    g4::mlp_gemm_nt(m->stream, m->dZt, m->actt, nullptr, m->grads + m->woff[l], nullptr, N, K, rows, 0, 0,
-                    m->derr);
+    g4::mlp_transpose_bf16(m->stream, m->dZb, m->dZt, rows, N, rows16);
+    g4::mlp_transpose_bf16(m->stream, m->actb[l], m->actt, rows, K, rows16);
+    int rc = g4::mlp_gemm_nt(m->stream, m->dZt, m->actt, nullptr, m->grads + m->woff[l], nullptr, N, K, rows16, 0, 0,
+                             m->derr);
     g4::mlp_colsum(m->stream, m->dZ, m->grads + m->boff[l], rows, N);
     // dA_l [rows][K] = dZ W_l
-    if (l > 0)
-      g4::mlp_gemm_nt(m->stream, m->dZb, m->wbt + m->wboff[l], nullptr, m->dA, nullptr, rows, K, N, 0, 0,
-                      m->derr);
+    if (l > 0 && !rc)
+      rc = g4::mlp_gemm_nt(m->stream, m->dZb, m->wbt + m->wboff[l], nullptr, m->dA, nullptr, rows, K, N, 0, 0,
+                           m->derr);
+    if (rc) return mfail(m, G4GPU_ERR_ARG, "mlp: a layer's widths are not multiples of 16");
   }
+  return G4GPU_OK;
 }
 
 int upload_norm(g4gpu_mlp m) {
@@ -294,7 +300,7 @@ int g4gpu_mlp_forward(g4gpu_mlp m, const float *X, int n, float *Y) {
   cudaSetDevice(m->device);
   int rc = load_rows(m, X, nullptr, n);
   if (rc) return rc;
-  forward(m, n);
+  if ((rc = forward(m, n))) return rc;
   float *yd = m->dZ;  // scratch for the de-normalised outputs
   g4::closure_denormalize(m->stream, m->act[kLayers], m->oscale, m->oshift, yd, n, m->nout, m->dims[kLayers]);
   M_CUDA(m, cudaMemcpyAsync(Y, yd, (size_t)n * m->nout * 4, cudaMemcpyDeviceToHost, m->stream));
@@ -310,8 +316,7 @@ int g4gpu_mlp_gradients(g4gpu_mlp m, const float *X, const float *T, int n, floa
   if (rc) return rc;
   M_CUDA(m, cudaMemsetAsync(m->loss, 0, 4, m->stream));
   M_CUDA(m, cudaMemsetAsync(m->grads, 0, m->nparam * 4, m->stream));
-  forward(m, n);
-  backward(m, n);
+  if ((rc = forward(m, n)) || (rc = backward(m, n))) return rc;
   M_CUDA(m, cudaMemcpyAsync(grads, m->grads, m->nparam * 4, cudaMemcpyDeviceToHost, m->stream));
   if (loss) M_CUDA(m, cudaMemcpyAsync(loss, m->loss, 4, cudaMemcpyDeviceToHost, m->stream));
   M_CUDA(m, cudaStreamSynchronize(m->stream));
@@ -370,8 +375,7 @@ int g4gpu_mlp_train(g4gpu_mlp m, const float *X, const float *T, int n, int epoc
         std::memcpy(&tb[(size_t)r * m->nout], &T[(size_t)idx[b0 + r] * m->nout], m->nout * 4);
       }
       if ((rc = load_rows(m, xb.data(), tb.data(), batch))) return rc;
-      forward(m, batch);
-      backward(m, batch);
+      if ((rc = forward(m, batch)) || (rc = backward(m, batch))) return rc;
       m->adam_t++;
       g4::mlp_adam(m->stream, m->params, m->grads, m->m, m->v, m->nparam, lr, 0.9f, 0.999f, 1e-8f, m->adam_t);
       refresh_bf16(m);
@@ -491,7 +495,12 @@ static int closure_correct(g4gpu_handle h) {
   m->stream = h->stream;
   m->derr = h->derr;
   g4::closure_normalize(h->stream, h->closure_feat, m->fmean, m->fstd, m->actb[0], ns, m->nin, m->dims[0]);
-  forward(m, ns);
+  rc = forward(m, ns);
+  if (rc) {
+    m->stream = saved;
+    m->derr = saved_err;
+    return g4_fail(h, rc, m->err);
+  }
   g4::closure_denormalize(h->stream, m->act[kLayers], m->oscale, m->oshift, h->closure_corr, ns, m->nout,
                           m->dims[kLayers]);
   g4::closure_apply(h->stream, h->beam.theta, h->beam.gamma, h->field[0], h->closure_corr, h->mixed, ns,

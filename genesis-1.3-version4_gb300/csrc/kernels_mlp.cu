@@ -2,18 +2,17 @@
 // (inputs -> 256 -> 256 -> 256 -> outputs) evaluated and trained on the GPU.
 //
 // GEMM: C[M][N] = sum_k A[M][k] B[N][k] ("NT": both operands row-major with the
-// reduction index last), BF16 operands, FP32 accumulation. Two kernels:
-//
-//   k_gemm_tc   the 5th-generation tensor cores (tcgen05): a CTA computes a 128 x BN
-//               tile (BN <= 128) with its accumulator in tensor memory. The whole
-//               reduction (K <= 256) is staged in shared memory at once, one thread
-//               issues the K / 16 MMAs, their completion arrives on an mbarrier, and
-//               the four warps read the accumulator back (tcgen05.ld) for the bias /
-//               ReLU epilogue. Every GEMM of the forward pass and the dA = dZ W
-//               products of the backward pass take it.
-//   k_gemm_nt   warp-level mma.sync m16n8k16, 64 x 64 tiles, K staged in chunks of 32:
-//               the weight gradients dW = dZ^T A, whose reduction runs over the batch
-//               rows (thousands), beyond what k_gemm_tc stages.
+// reduction index last), BF16 operands, FP32 accumulation, on the 5th-generation
+// tensor cores (k_gemm_tc): a CTA computes a 128 x BN tile (BN <= 128, a multiple of
+// 16 dividing N) with its accumulator in tensor memory (TMEM). The reduction runs in
+// stages of 64: while one thread issues the MMAs of stage k (tcgen05.mma, 4 per
+// stage, K = 16 each), the CTA's copies of stage k + 2 are in flight (cp.async into
+// a ring of three stage buffers), and a stage buffer is refilled only after the
+// MMAs that read it have completed (tcgen05.commit to the buffer's mbarrier). The
+// eight warps then read the accumulator back (tcgen05.ld), a quarter of the rows and
+// half of the columns each, for the bias / ReLU epilogue. Every GEMM of the network takes it: the forward layers, dA = dZ W, and
+// the weight gradients dW = dZ^T A, whose reduction runs over the batch rows (the
+// transposed operands are zero-padded to a multiple of 16 rows).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -24,112 +23,29 @@
 namespace g4 {
 namespace {
 
-constexpr int TM = 64, TN = 64, TK = 32;
-
-__device__ __forceinline__ uint32_t pack2(const __nv_bfloat16 *p) {
-  return *reinterpret_cast<const uint32_t *>(p);
-}
-
-// mma.sync m16n8k16, row.col, bf16 x bf16 -> f32
-__device__ __forceinline__ void mma16816(float *d, const uint32_t *a, const uint32_t *b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// C = A B^T (+ bias[n]) with optional ReLU; writes FP32 C and/or BF16 Cb.
-// A: [M][K] bf16, B: [N][K] bf16, K a multiple of 16 (callers pad).
-__global__ void __launch_bounds__(128) k_gemm_nt(const __nv_bfloat16 *__restrict__ A,
-                                                 const __nv_bfloat16 *__restrict__ B,
-                                                 const float *__restrict__ bias, float *C,
-                                                 __nv_bfloat16 *Cb, int M, int N, int K, int relu,
-                                                 int accumulate) {
-  __shared__ __align__(16) __nv_bfloat16 As[TM][TK + 8];
-  __shared__ __align__(16) __nv_bfloat16 Bs[TN][TK + 8];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-  const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN;
-  const int g = lane >> 2, t = lane & 3;
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; i++)
-#pragma unroll
-    for (int j = 0; j < 4; j++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
-  for (int k0 = 0; k0 < K; k0 += TK) {
-    // stage the 64 x 32 tiles of A and B (zero outside the matrices)
-    for (int e = threadIdx.x; e < TM * TK; e += blockDim.x) {
-      int r = e / TK, c = e % TK;
-      int gm = m0 + r, gk = k0 + c;
-      As[r][c] = (gm < M && gk < K) ? A[(size_t)gm * K + gk] : __float2bfloat16(0.f);
-      int gn = n0 + r;
-      Bs[r][c] = (gn < N && gk < K) ? B[(size_t)gn * K + gk] : __float2bfloat16(0.f);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < TK; kk += 16) {
-      uint32_t af[2][4], bf[4][2];
-#pragma unroll
-      for (int i = 0; i < 2; i++) {
-        int r = wm + i * 16 + g;
-        af[i][0] = pack2(&As[r][kk + 2 * t]);
-        af[i][1] = pack2(&As[r + 8][kk + 2 * t]);
-        af[i][2] = pack2(&As[r][kk + 8 + 2 * t]);
-        af[i][3] = pack2(&As[r + 8][kk + 8 + 2 * t]);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        int c = wn + j * 8 + g;
-        bf[j][0] = pack2(&Bs[c][kk + 2 * t]);
-        bf[j][1] = pack2(&Bs[c][kk + 8 + 2 * t]);
-      }
-#pragma unroll
-      for (int i = 0; i < 2; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++) mma16816(acc[i][j], af[i], bf[j]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int i = 0; i < 2; i++)
-#pragma unroll
-    for (int j = 0; j < 4; j++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        int r = m0 + wm + i * 16 + g + (q >= 2 ? 8 : 0);
-        int c = n0 + wn + j * 8 + 2 * t + (q & 1);
-        if (r < M && c < N) {
-          float v = acc[i][j][q];
-          if (accumulate && C) v += C[(size_t)r * N + c];
-          if (bias) v += bias[c];
-          if (relu) v = fmaxf(v, 0.f);
-          if (C) C[(size_t)r * N + c] = v;
-          if (Cb) Cb[(size_t)r * N + c] = __float2bfloat16(v);
-        }
-      }
-}
-
 // ---- k_gemm_tc: tcgen05 MMA with the accumulator in tensor memory --------------
-constexpr int kTcM = 128;     // tile rows: the accumulator's 128 TMEM lanes
-constexpr int kTcMaxK = 256;  // the reduction is staged whole
-constexpr int kTcMaxN = 128;  // tile columns (TMEM columns of FP32 accumulator)
-// Shared memory of a CTA at least this large keeps at most 3 CTAs on an SM, so their
-// accumulators (<= 128 TMEM columns each) always fit the SM's 512 columns and no
-// allocation has to wait for another CTA.
-constexpr size_t kTcMinSmem = 60 * 1024;
+constexpr int kTcM = 128;      // tile rows: the accumulator's 128 TMEM lanes
+constexpr int kTcKC = 64;      // reduction elements per stage (128 bytes of a row)
+constexpr int kTcStages = 3;   // stage buffers in the ring
+constexpr int kTcMaxN = 128;   // tile columns (TMEM columns of the FP32 accumulator)
+constexpr int kTcThreads = 256;  // two warpgroups: both stage; each reads half the columns
 constexpr long long kTcSpin = 1LL << 22;  // bounded mbarrier polls
+// Shared memory of a CTA: kTcStages x (A stage 16 KB + B stage BN x 128 B), one
+// mbarrier per stage, the TMEM address. At BN = 128 that is 96 KB, so at most two
+// CTAs share an SM and their accumulators (<= 128 TMEM columns each) always fit
+// its 512 columns; smaller tiles are padded to kTcMinSmem for the same bound
+// (at most 3 CTAs per SM), so no TMEM allocation waits for another CTA.
+constexpr size_t kTcMinSmem = 60 * 1024;
 
-// Operand tiles in shared memory are K-major without swizzle: 8 x 16-byte core
-// matrices (8 rows of 8 BF16 along K). The core matrix of row group g and K chunk c
-// (k / 8) sits at byte (g * K / 8 + c) * 128, its row r % 8 at + 16 (r % 8). In the
-// MMA's shared-memory descriptors, core matrices adjacent in K are 128 B apart (the
-// leading byte offset) and row groups K * 16 B apart (the stride byte offset).
-__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);  // version 1; no swizzle, base offset 0
+// A stage buffer holds its rows K-major without swizzle, in 8 x 16-byte core
+// matrices (8 rows of 8 BF16 along K): row group g, K chunk c (8 elements) at byte
+// g * 1024 + c * 128, row r % 8 of it at + 16 (r % 8). In the MMA's shared-memory
+// descriptors, core matrices adjacent in K are 128 B apart (the leading byte
+// offset) and row groups 1024 B apart (the stride byte offset).
+constexpr uint32_t kTcLBO = 128, kTcSBO = 1024;
+__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(kTcLBO >> 4) << 16) | ((uint64_t)(kTcSBO >> 4) << 32) |
+         (1ull << 46);  // descriptor version 1 (bits 46-48 = 0b001); no swizzle, base offset 0
 }
 
 // Instruction descriptor of tcgen05.mma kind::f16: D in F32 (bits 4-5 = 1), A and B
@@ -139,22 +55,30 @@ __device__ __forceinline__ uint32_t tc_idesc(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-// Stages rows [r0, r0 + rows) x [0, K) of the row-major matrix X (K columns, nrow
-// valid rows; zero past them) into the tile at shared address T with 16-byte
-// cp.async copies. Copy idx takes row (idx / (8 K/8)) * 8 + idx % 8 and chunk
-// (idx / 8) % (K / 8), which is the tile's byte idx * 16: consecutive threads write
-// consecutive 16 bytes.
+// Copies stage [k0, k0 + kw) of rows [r0, r0 + rows) of the row-major matrix X (K
+// columns, nrow valid rows) into the stage buffer at shared address T with 16-byte
+// cp.async copies; rows past nrow read as zero. Copy idx takes row group
+// idx / (8 ck), chunk (idx / 8) % ck and row idx % 8 of the group, so that 8
+// consecutive threads fill one 128-byte core matrix; in a full stage (ck = 8) that
+// is byte idx * 16 of the buffer.
+__device__ __forceinline__ void tc_copy(uint32_t dst, const __nv_bfloat16 *src, bool ok) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(ok ? 16 : 0) : "memory");
+}
 __device__ __forceinline__ void tc_stage(uint32_t T, const __nv_bfloat16 *__restrict__ X, int r0, int rows, int nrow,
-                                         int K) {
-  const int ck = K >> 3;
-  const int total = rows * ck;
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int r = ((idx >> 3) / ck) * 8 + (idx & 7), c = (idx >> 3) % ck;
-    const bool ok = r0 + r < nrow;
-    const __nv_bfloat16 *src = ok ? X + (size_t)(r0 + r) * K + c * 8 : X;
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(T + (uint32_t)idx * 16u), "l"(src),
-                 "r"(ok ? 16 : 0)
-                 : "memory");
+                                         int K, int k0, int kw) {
+  if (kw == kTcKC) {
+    for (int idx = threadIdx.x; idx < rows * 8; idx += blockDim.x) {
+      const int r = r0 + ((idx >> 6) << 3) + (idx & 7), k = k0 + (((idx >> 3) & 7) << 3);
+      const bool ok = r < nrow;
+      tc_copy(T + (uint32_t)idx * 16u, ok ? X + (size_t)r * K + k : X, ok);
+    }
+    return;
+  }
+  const int ck = kw >> 3;
+  for (int idx = threadIdx.x; idx < rows * ck; idx += blockDim.x) {
+    const int q = idx >> 3, c = q % ck, g = q / ck, r = r0 + g * 8 + (idx & 7);
+    const bool ok = r < nrow;
+    tc_copy(T + (uint32_t)(g * 1024 + c * 128 + (idx & 7) * 16), ok ? X + (size_t)r * K + k0 + c * 8 : X, ok);
   }
 }
 
@@ -177,27 +101,27 @@ __device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
   return false;
 }
 
-// C = A B^T (+ bias[n]) with optional ReLU, as k_gemm_nt, for K a multiple of 16 up
-// to kTcMaxK and a tile width BN (a multiple of 16 up to kTcMaxN) dividing N. 128
-// threads; CTA (bx, by) computes rows [128 bx, 128 bx + 128) and columns
-// [BN by, BN by + BN). Shared memory: A tile (128 x K), B tile (BN x K), the MMA
-// mbarrier, the TMEM address. If the MMAs do not complete within the bounded wait,
-// *err is set, the CTA waits once more (bounded) so that no MMA still writes the
-// accumulator, frees its tensor memory and writes nothing.
-__global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict__ A,
+// C = A B^T (+ bias[n]) with optional ReLU (and optionally added to C); writes FP32
+// C and/or BF16 Cb. A: [M][K], B: [N][K], K a multiple of 16, BN (a multiple of 16 up
+// to kTcMaxN) dividing N. kTcThreads threads (two warpgroups); CTA (bx, by) computes
+// rows [128 bx, 128 bx + 128) and columns [BN by, BN by + BN). If an MMA completion is not seen within the
+// bounded wait, *err is set, the CTA waits once more (bounded) for the MMAs it
+// issued and for its copies, frees its tensor memory and writes nothing.
+__global__ void __launch_bounds__(kTcThreads) k_gemm_tc(const __nv_bfloat16 *__restrict__ A,
                                                  const __nv_bfloat16 *__restrict__ B,
                                                  const float *__restrict__ bias, float *C, __nv_bfloat16 *Cb,
                                                  int M, int N, int K, int BN, int relu, int accumulate, int *err) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
-  const uint32_t sA = (uint32_t)__cvta_generic_to_shared(tc_smem);
-  const uint32_t sB = sA + (uint32_t)(kTcM * K * 2);
-  const uint32_t sbar = sB + (uint32_t)(BN * K * 2), sadr = sbar + 8;
+  const uint32_t base = (uint32_t)__cvta_generic_to_shared(tc_smem);
+  const uint32_t stage_bytes = (uint32_t)(kTcM + BN) * kTcKC * 2;
+  const uint32_t sbar = base + kTcStages * stage_bytes, sadr = sbar + 8 * kTcStages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * kTcM, n0 = blockIdx.y * BN;
   uint32_t ncols = 32;  // TMEM columns: a power of two >= 32
   while ((int)ncols < BN) ncols <<= 1;
   if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+    for (int b = 0; b < kTcStages; b++)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar + 8 * b) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -205,45 +129,78 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  tc_stage(sA, A, m0, kTcM, M, K);
-  tc_stage(sB, B, n0, BN, N, K);
-  asm volatile("cp.async.commit_group;" ::: "memory");
-  asm volatile("cp.async.wait_group 0;" ::: "memory");
-  // the staged tiles, written through the generic proxy, made visible to the MMAs
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  const int nk = (K + kTcKC - 1) / kTcKC;
+  auto stage = [&](int j) {
+    const uint32_t sa = base + (uint32_t)(j % kTcStages) * stage_bytes;
+    const int k0 = j * kTcKC, kw = min(kTcKC, K - k0);
+    tc_stage(sa, A, m0, kTcM, M, K, k0, kw);
+    tc_stage(sa + kTcM * kTcKC * 2, B, n0, BN, N, K, k0, kw);
+  };
+  // prologue: stages 0 .. kTcStages - 2, one copy group each (empty past the end),
+  // so that at step kc the group of stage kc is the oldest but kTcStages - 1
+  for (int j = 0; j < kTcStages - 1; j++) {
+    if (j < nk) stage(j);
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   uint32_t tmem;
   asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(sadr) : "memory");
-  if (threadIdx.x == 0) {
-    const uint32_t idesc = tc_idesc(kTcM, BN);
-    const uint32_t sbo = (uint32_t)K * 16u;
-    for (int s = 0; s < K / 16; s++) {
-      // K step s: core-matrix chunks 2s and 2s + 1 of every row group
-      const uint64_t ad = tc_smem_desc(sA + (uint32_t)s * 256u, 128u, sbo);
-      const uint64_t bd = tc_smem_desc(sB + (uint32_t)s * 256u, 128u, sbo);
-      asm volatile(
-          "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-          " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-          "l"(ad), "l"(bd), "r"(idesc), "r"(s)
-          : "memory");
+  const uint32_t idesc = tc_idesc(kTcM, BN);
+  bool ok = true;
+  int last = -1;  // the last stage whose MMAs were committed
+  for (int kc = 0; kc < nk; kc++) {
+    const int nx = kc + kTcStages - 1;
+    if (nx < nk) {
+      // stage nx refills the buffer of stage kc - 1: its MMAs must have completed
+      if (kc >= 1) {
+        ok = __syncthreads_and(tc_wait(sbar + 8 * ((kc - 1) % kTcStages), ((kc - 1) / kTcStages) & 1)) != 0;
+        if (!ok) break;
+      }
+      stage(nx);
     }
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(sbar)
-                 : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group %0;" ::"n"(kTcStages - 1) : "memory");
+    // the stage's tiles, written through the generic proxy, made visible to the MMAs
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (threadIdx.x == 0) {
+      const uint32_t sa = base + (uint32_t)(kc % kTcStages) * stage_bytes, sb = sa + kTcM * kTcKC * 2;
+      const int ks = min(kTcKC, K - kc * kTcKC) / 16;
+      for (int s = 0; s < ks; s++) {
+        // K step s of the stage: core-matrix chunks 2s and 2s + 1 of every row group
+        const uint64_t ad = tc_smem_desc(sa + (uint32_t)s * 256u), bd = tc_smem_desc(sb + (uint32_t)s * 256u);
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(kc | s)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       sbar + 8 * (kc % kTcStages))
+                   : "memory");
+    }
+    last = kc;
   }
-  const bool done = __syncthreads_and(tc_wait(sbar, 0)) != 0;
-  if (!done) {
+  if (ok && last >= 0)
+    ok = __syncthreads_and(tc_wait(sbar + 8 * (last % kTcStages), (last / kTcStages) & 1)) != 0;
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  if (!ok) {
     if (threadIdx.x == 0) {
       atomicExch(err, 1);
-      tc_wait(sbar, 0);
+      if (last >= 0) tc_wait(sbar + 8 * (last % kTcStages), (last / kTcStages) & 1);
     }
   } else {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    // warp w reads TMEM lanes [32 w, 32 w + 32): the rows of the tile it owns
-    const int r = m0 + warp * 32 + lane;
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int c0 = 0; c0 < BN; c0 += 8) {
+    // warp w reads TMEM lanes [32 (w % 4), 32 (w % 4) + 32), the rows of the tile its
+    // position in the warpgroup gives it access to, and the columns of half w / 4
+    const int quarter = warp & 3, half = warp >> 2;
+    const int r = m0 + quarter * 32 + lane;
+    const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16);
+    for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 8) {
       uint32_t v[8];
       // the load and its wait in one statement: no use of v can be placed between them
       asm volatile(
@@ -280,8 +237,9 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const __nv_bfloat16 *__restrict
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
 }
 
-// out[c][r] = in[r][c] for a rows x cols bf16 matrix
-__global__ void k_transpose_bf16(const __nv_bfloat16 *in, __nv_bfloat16 *out, int rows, int cols) {
+// out[c][r] = in[r][c] for a rows x cols bf16 matrix; out has ldo >= rows columns,
+// the ones past rows set to zero (the zero padding of a reduction over rows)
+__global__ void k_transpose_bf16(const __nv_bfloat16 *in, __nv_bfloat16 *out, int rows, int cols, int ldo) {
   __shared__ __nv_bfloat16 tile[32][33];
   int bx = blockIdx.x * 32, by = blockIdx.y * 32;
   for (int j = threadIdx.y; j < 32; j += blockDim.y) {
@@ -291,7 +249,7 @@ __global__ void k_transpose_bf16(const __nv_bfloat16 *in, __nv_bfloat16 *out, in
   __syncthreads();
   for (int j = threadIdx.y; j < 32; j += blockDim.y) {
     int c = bx + j, r = by + threadIdx.x;
-    if (r < rows && c < cols) out[(size_t)c * rows + r] = tile[threadIdx.x][j];
+    if (r < ldo && c < cols) out[(size_t)c * ldo + r] = r < rows ? tile[threadIdx.x][j] : __float2bfloat16(0.f);
   }
 }
 
@@ -361,37 +319,33 @@ unsigned blocks_for(size_t n) {
 }  // namespace
 
 int mlp_tile_n(int N, int K) {
-  if (K < 16 || K > kTcMaxK || K % 16) return 0;
-  const int bn = N <= kTcMaxN ? N : (N % kTcMaxN == 0 ? kTcMaxN : 0);
-  return bn >= 16 && bn % 16 == 0 ? bn : 0;
+  if (K < 16 || K % 16 || N < 16 || N % 16) return 0;
+  for (int bn = kTcMaxN; bn >= 16; bn -= 16)
+    if (N % bn == 0) return bn;
+  return 0;
 }
 
-void mlp_gemm_nt(void *stream, const void *A, const void *B, const float *bias, float *C, void *Cb, int M,
-                 int N, int K, int relu, int accumulate, int *err) {
-  if (M <= 0 || N <= 0) return;
+int mlp_gemm_nt(void *stream, const void *A, const void *B, const float *bias, float *C, void *Cb, int M, int N,
+                int K, int relu, int accumulate, int *err) {
   const int bn = mlp_tile_n(N, K);
-  if (bn) {
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-      attr = true;
-    }
-    size_t smem = (size_t)(kTcM + bn) * K * 2 + 16;
-    if (smem < kTcMinSmem) smem = kTcMinSmem;
-    dim3 grid((M + kTcM - 1) / kTcM, N / bn);
-    k_gemm_tc<<<grid, 128, smem, (cudaStream_t)stream>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, bias,
-                                                        C, (__nv_bfloat16 *)Cb, M, N, K, bn, relu, accumulate, err);
-    return;
+  if (M <= 0 || !bn) return -1;
+  size_t smem = (size_t)kTcStages * (kTcM + bn) * kTcKC * 2 + 8 * kTcStages + 8;
+  if (smem < kTcMinSmem) smem = kTcMinSmem;
+  static size_t smem_set = 0;  // the largest dynamic shared memory granted so far
+  if (smem > smem_set) {
+    cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    smem_set = smem;
   }
-  dim3 grid((M + TM - 1) / TM, (N + TN - 1) / TN);
-  k_gemm_nt<<<grid, 128, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, bias,
-                                                     C, (__nv_bfloat16 *)Cb, M, N, K, relu, accumulate);
+  dim3 grid((M + kTcM - 1) / kTcM, N / bn);
+  k_gemm_tc<<<grid, kTcThreads, smem, (cudaStream_t)stream>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, bias, C,
+                                                      (__nv_bfloat16 *)Cb, M, N, K, bn, relu, accumulate, err);
+  return 0;
 }
 
-void mlp_transpose_bf16(void *stream, const void *in, void *out, int rows, int cols) {
-  dim3 grid((cols + 31) / 32, (rows + 31) / 32);
+void mlp_transpose_bf16(void *stream, const void *in, void *out, int rows, int cols, int ldo) {
+  dim3 grid((cols + 31) / 32, (ldo + 31) / 32);
   k_transpose_bf16<<<grid, dim3(32, 8), 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)in,
-                                                                  (__nv_bfloat16 *)out, rows, cols);
+                                                                  (__nv_bfloat16 *)out, rows, cols, ldo);
 }
 
 void mlp_to_bf16(void *stream, const float *in, void *out, size_t n) {

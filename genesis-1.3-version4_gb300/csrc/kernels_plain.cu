@@ -36,8 +36,8 @@ __device__ __forceinline__ C2 rmul(double s, C2 a) { return {s * a.x, s * a.y}; 
 __device__ __forceinline__ C2 mulr(C2 a, double s) { return {a.x * s, a.y * s}; }
 
 // TrackBeam::applyDrift / applyFQuad / applyDQuad (TrackBeam.cpp:84-116). The
-// divisions by gammaz are multiplications by igz = 1 / gammaz (one division per half
-// step instead of up to three; the products differ from the quotients in the last bit).
+// divisions by gammaz are multiplications by igz = 1 / gammaz (the products differ
+// from the quotients in the last bit).
 __device__ __forceinline__ void plane_step(int kind, double q, double off, double delz, double &x,
                                            double &p, double gammaz, double igz) {
   if (kind == 0) {
@@ -82,8 +82,11 @@ __device__ __forceinline__ void transverse(const StepConst &sc, bool last, doubl
     py = sc.cm[6] * tmp * gz + sc.cm[7] * py;
   }
   double delz = sc.delz * 0.5;
-  double gammaz = sqrt(g * g - 1 - sc.aw_t * sc.aw_t - px * px - py * py);
-  const double igz = 1. / gammaz;
+  // 1 / gammaz by one reciprocal square root, gammaz (the quadrupoles' only) as
+  // gammaz^2 / gammaz; both within an ulp or two of the reference's sqrt and quotients
+  const double gz2 = g * g - 1 - sc.aw_t * sc.aw_t - px * px - py * py;
+  const double igz = rsqrt(gz2);
+  const double gammaz = gz2 * igz;
   plane_step(sc.kindx, sc.qx, sc.xoff, delz, x, px, gammaz, igz);
   plane_step(sc.kindy, sc.qy, sc.yoff, delz, y, py, gammaz, igz);
 }
@@ -120,21 +123,33 @@ __device__ __forceinline__ bool ll_gridpoint(double gm, double idg, int ng, doub
   return false;
 }
 
+// 1 / x given r, the reciprocal of a nearby value: two Newton steps, each squaring
+// the relative error e = 1 - x r, when |e| <= 1e-5 (then the error is below 1e-20
+// before rounding), else the division. The RK4 stages of a step change gamma by far
+// less than that, so each stage's 1 / gamma follows from the previous one.
+__device__ __forceinline__ double recip_near(double x, double r) {
+  double e = fma(-x, r, 1.);
+  if (!(fabs(e) <= 1e-5)) return 1. / x;
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.);
+  return fma(r, e, r);
+}
+
 // BeamSolver::ODE (BeamSolver.cpp:144-163) for NF fields, given cs[i] = (cos, sin) of
-// rharm_i * tthet. Two of the reference's four divisions become products with the
-// reciprocals 1 / tgam and 1 / btpar0 (the latter computed as the reference computes
-// it, so that xks (1 - 1/btpar0), which xks ~ 1e11 amplifies, is the reference's
-// value); ztemp1 = -2 / xks comes with the step constants.
+// rharm_i * tthet and itg = 1 / tgam. Two of the reference's four divisions become
+// products with the reciprocals 1 / tgam and 1 / btpar0 (the latter computed as the
+// reference computes it, so that xks (1 - 1/btpar0), which xks ~ 1e11 amplifies, is
+// the reference's value; a last-bit change of 1 / tgam changes btper0 / tgam^2 ~ 1e-8
+// far below the last bit of btpar0); ztemp1 = -2 / xks comes with the step constants.
 template <int NF>
 __device__ __forceinline__ void ode(const StepConst &sc, const C2 *rpart, const C2 *cs, double btpar, double ez,
-                                    double tgam, double &k2gg, double &k2pp) {
+                                    double itg, double &k2gg, double &k2pp) {
   C2 ctmp = {0, 0};
 #pragma unroll
   for (int i = 0; i < NF; i++) {
     if (i >= sc.nfld) break;
     ctmp = cadd(ctmp, cmul(rpart[i], C2{cs[i].x, -cs[i].y}));
   }
-  const double itg = 1. / tgam;
   double btper0 = btpar + sc.ztemp1 * ctmp.x;
   double btpar0 = sqrt(1. - btper0 * (itg * itg));
   const double ib = 1. / btpar0;
@@ -176,11 +191,22 @@ __device__ __forceinline__ C2 rotated(C2 brot, double h, double theta, double dt
 // Deposition of one particle into the source of every field
 // (FieldSolverADI.cpp:19-51; FieldSolverFFT.cpp:19-51 is identical).
 // cs: (cos, sin) of rharm_k * theta of every field, or null (computed here).
+// The source scale of field k for a slice of current cur and npd particles
+// (FieldSolverADI.cpp:21-22), in the reference's operation order.
+__device__ __forceinline__ double deposit_scale(const StepConst &sc, const FieldStep &fs, double cur, double npd) {
+  double scl = fs.fc * kVacimp * cur * fs.xks * sc.delz;
+  scl /= 4 * kEev * npd * fs.dgrid * fs.dgrid;
+  return scl;
+}
+
+// scls: every field's deposit_scale for this slice, or null (computed here). ig: 1 / g,
+// or 0 (divided here).
 template <int NF>
 __device__ __forceinline__ void deposit_particle(const StepConst &sc, double2 *const *src,
                                                  size_t slice_off, int ng, double cur,
                                                  double npd, double g, double th, double x,
-                                                 double y, const C2 *cs = nullptr) {
+                                                 double y, const C2 *cs = nullptr, const double *scls = nullptr,
+                                                 double ig = 0.) {
 #pragma unroll
   for (int k = 0; k < NF; k++) {
     if (k >= sc.nfld) break;
@@ -188,11 +214,10 @@ __device__ __forceinline__ void deposit_particle(const StepConst &sc, double2 *c
     if (!fs.dep_on) continue;
     Cell c;
     if (!ll_gridpoint(fs.gridmax, fs.idgrid, ng, x, y, c)) continue;
-    double scl = fs.fc * kVacimp * cur * fs.xks * sc.delz;
-    scl /= 4 * kEev * npd * fs.dgrid * fs.dgrid;
+    const double scl = scls ? scls[k] : deposit_scale(sc, fs, cur, npd);
     double dx = x - sc.ax, dy = y - sc.ay;
     double faw2 = (1 + sc.kx * dx * dx + sc.ky * dy * dy + 2 * (sc.gradx * dx + sc.grady * dy));
-    double part = sqrt(faw2) * scl / g;
+    double part = ig != 0. ? sqrt(faw2) * scl * ig : sqrt(faw2) * scl / g;
     double s, co;
     if (cs) {
       co = cs[k].x;
@@ -250,6 +275,11 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   int is = blockIdx.y;
   int ip = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = slice_np(p, is, np);
+  // the slice's source scales, one thread per field (the block is one slice)
+  __shared__ double scls[NF];
+  if (deposit && threadIdx.x < NF && (int)threadIdx.x < sc.nfld)
+    scls[threadIdx.x] = deposit_scale(sc, sc.f[threadIdx.x], p.current[is], (double)n);
+  __syncthreads();
   if (ip >= n) return;
   size_t o = (size_t)is * np + ip;
   double g = p.gamma[o], th = p.theta[o], x = p.x[o], y = p.y[o], px = p.px[o], py = p.py[o];
@@ -313,7 +343,8 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
 
   // BeamSolver::RungeKutta, BeamSolver.cpp:89-141
   double k2gg = 0, k2pp = 0, k3gg, k3pp;
-  ode<NF>(sc, rpart, cs, btpar, ez, gamma, k2gg, k2pp);
+  double itg = 1. / gamma;  // 1 / gamma of the stage, each stage's from the previous one
+  ode<NF>(sc, rpart, cs, btpar, ez, itg, k2gg, k2pp);
   double stpz = 0.5 * sc.delz;
   gamma += stpz * k2gg;
   theta += stpz * k2pp;
@@ -322,7 +353,8 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   k2gg = 0;
   k2pp = 0;
   stage(bhalf, sc.dnom_half);
-  ode<NF>(sc, rpart, cs, btpar, ez, gamma, k2gg, k2pp);
+  itg = recip_near(gamma, itg);
+  ode<NF>(sc, rpart, cs, btpar, ez, itg, k2gg, k2pp);
   gamma += stpz * (k2gg - k3gg);
   theta += stpz * (k2pp - k3pp);
   k3gg /= 6;
@@ -330,7 +362,8 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   k2gg *= -0.5;
   k2pp *= -0.5;
   stage(bhalf, sc.dnom_half);
-  ode<NF>(sc, rpart, cs, btpar, ez, gamma, k2gg, k2pp);
+  itg = recip_near(gamma, itg);
+  ode<NF>(sc, rpart, cs, btpar, ez, itg, k2gg, k2pp);
   stpz = sc.delz;
   gamma += stpz * k2gg;
   theta += stpz * k2pp;
@@ -339,7 +372,8 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   k2gg *= 2;
   k2pp *= 2;
   stage(bfull, sc.dnom_full);
-  ode<NF>(sc, rpart, cs, btpar, ez, gamma, k2gg, k2pp);
+  itg = recip_near(gamma, itg);
+  ode<NF>(sc, rpart, cs, btpar, ez, itg, k2gg, k2pp);
   gamma += stpz * (k3gg + k2gg / 6.0);
   theta += stpz * (k3pp + k2pp / 6.0);
 
@@ -366,7 +400,7 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
     // the deposition's phases, rotated from the start of the step like the stages'
     stage(bfull, sc.dnom_full);
     deposit_particle<NF>(sc, p.src, (size_t)is * ncell, ng, p.current[is], (double)n, gamma,
-                         theta, x, y, cs);
+                         theta, x, y, cs, scls, recip_near(gamma, itg));
   }
 }
 

@@ -46,10 +46,10 @@ def test_mlp_gradients_match_cpu_oracle(lib, n):
 
 @pytest.mark.parametrize("n,width", [(4096, 256), (1000, 96), (333, 48), (700, 512)])
 def test_mlp_forward_matches_cpu_oracle(lib, n, width):
-    """The forward pass over a window's worth of rows: the tcgen05 GEMM (K <= 256, tile
-    width 128, or the whole N up to 128: 96 and 48 here) and, at width 512, the
-    mma.sync GEMM for the K = 512 layers beside it. Ragged row counts leave the last
-    128-row tile partly empty."""
+    """The forward pass over a window's worth of rows through the tcgen05 GEMM: tile
+    widths 128 (N = 256, 512) and the whole N below that (96, 48); reductions of
+    32, 48, 96, 256 and 512 (one to eight 64-element stages, the last one partial
+    at 48 and 96). Ragged row counts leave the last 128-row tile partly empty."""
     import g4gpu
     import mlp_oracle
     rng = np.random.default_rng(n + width)
