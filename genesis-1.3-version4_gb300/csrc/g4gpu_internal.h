@@ -271,10 +271,11 @@ void launch_fft_solve(void *stream, int mixed, void *field, const void *src, voi
                       double k2c, const void *sig, int filtered, double delz, const FFTPlan &pl, int ns,
                       int first);
 
-// kernels_mlp.cu: BF16 tensor-core MLP (tcgen05, FP32 accumulation in tensor
-// memory). mlp_gemm_nt needs N and K multiples of 16 (mlp_tile_n gives the tile
-// width, 0 if unsupported) and returns -1 otherwise; *err (device) is set if a
-// bounded wait for the MMAs runs out. mlp_transpose_bf16 writes ldo >= rows
+// kernels_mlp.cu: BF16 tensor-core MLP (tcgen05 fed by TMA, FP32 accumulation in
+// tensor memory). mlp_gemm_nt needs N and K multiples of 16 (mlp_tile_n gives the
+// tile width, 0 if unsupported) and returns -1 otherwise, -2 if the driver gives no
+// tensor map for an operand (16-byte aligned operands only); *err (device) is set
+// if a bounded wait for the copies or MMAs runs out. mlp_transpose_bf16 writes ldo >= rows
 // columns, zero past rows.
 int mlp_tile_n(int N, int K);
 int mlp_gemm_nt(void *stream, const void *A, const void *B, const float *bias, float *C, void *Cb, int M, int N,

@@ -117,7 +117,7 @@ int forward(g4gpu_mlp m, int rows) {
     int K = m->dims[l], N = m->dims[l + 1];
     if (g4::mlp_gemm_nt(m->stream, m->actb[l], m->wb + m->wboff[l], m->params + m->boff[l], m->act[l + 1],
                         m->actb[l + 1], rows, N, K, l < kLayers - 1, 0, m->derr))
-      return mfail(m, G4GPU_ERR_ARG, "mlp: a layer's widths are not multiples of 16");
+      return mfail(m, G4GPU_ERR_ARG, "mlp: a GEMM could not be launched (widths not multiples of 16, or no tensor map for an operand)");
   }
   return G4GPU_OK;
 }
@@ -141,7 +141,7 @@ int backward(g4gpu_mlp m, int rows) {
     if (l > 0 && !rc)
       rc = g4::mlp_gemm_nt(m->stream, m->dZb, m->wbt + m->wboff[l], nullptr, m->dA, nullptr, rows, K, N, 0, 0,
                            m->derr);
-    if (rc) return mfail(m, G4GPU_ERR_ARG, "mlp: a layer's widths are not multiples of 16");
+    if (rc) return mfail(m, G4GPU_ERR_ARG, "mlp: a GEMM could not be launched (widths not multiples of 16, or no tensor map for an operand)");
   }
   return G4GPU_OK;
 }

@@ -5,14 +5,18 @@
 // reduction index last), BF16 operands, FP32 accumulation, on the 5th-generation
 // tensor cores (k_gemm_tc): a CTA computes a 128 x BN tile (BN <= 128, a multiple of
 // 16 dividing N) with its accumulator in tensor memory (TMEM). The reduction runs in
-// stages of 64: while one thread issues the MMAs of stage k (tcgen05.mma, 4 per
-// stage, K = 16 each), the CTA's copies of stage k + 2 are in flight (cp.async into
-// a ring of three stage buffers), and a stage buffer is refilled only after the
-// MMAs that read it have completed (tcgen05.commit to the buffer's mbarrier). The
+// stages of 64 through a ring of three stage buffers. One thread drives the ring: it
+// loads a stage's tiles with TMA tensor copies (cp.async.bulk.tensor, completing on
+// the buffer's "full" mbarrier), issues the stage's four MMAs (tcgen05.mma, K = 16
+// each) once they have landed, commits them to the buffer's "empty" mbarrier
+// (tcgen05.commit), and refills a buffer only after its MMAs have completed. The
 // eight warps then read the accumulator back (tcgen05.ld), a quarter of the rows and
-// half of the columns each, for the bias / ReLU epilogue. Every GEMM of the network takes it: the forward layers, dA = dZ W, and
-// the weight gradients dW = dZ^T A, whose reduction runs over the batch rows (the
-// transposed operands are zero-padded to a multiple of 16 rows).
+// half of the columns each, for the bias / ReLU epilogue. Every GEMM of the network
+// takes it: the forward layers, dA = dZ W, and the weight gradients dW = dZ^T A,
+// whose reduction runs over the batch rows (the transposed operands are zero-padded
+// to a multiple of 16 rows).
+#include <cuda.h>          // CUtensorMap and its enumerations
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled_v12000
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -24,28 +28,29 @@ namespace g4 {
 namespace {
 
 // ---- k_gemm_tc: tcgen05 MMA with the accumulator in tensor memory --------------
-constexpr int kTcM = 128;      // tile rows: the accumulator's 128 TMEM lanes
-constexpr int kTcKC = 64;      // reduction elements per stage (128 bytes of a row)
-constexpr int kTcStages = 3;   // stage buffers in the ring
-constexpr int kTcMaxN = 128;   // tile columns (TMEM columns of the FP32 accumulator)
-constexpr int kTcThreads = 256;  // two warpgroups: both stage; each reads half the columns
+constexpr int kTcM = 128;        // tile rows: the accumulator's 128 TMEM lanes
+constexpr int kTcKC = 64;        // reduction elements per stage (8 chunks of 16 bytes)
+constexpr int kTcStages = 3;     // stage buffers in the ring
+constexpr int kTcMaxN = 128;     // tile columns (TMEM columns of the FP32 accumulator)
+constexpr int kTcThreads = 256;  // two warpgroups; each reads half the columns back
 constexpr long long kTcSpin = 1LL << 22;  // bounded mbarrier polls
-// Shared memory of a CTA: kTcStages x (A stage 16 KB + B stage BN x 128 B), one
-// mbarrier per stage, the TMEM address. At BN = 128 that is 96 KB, so at most two
-// CTAs share an SM and their accumulators (<= 128 TMEM columns each) always fit
-// its 512 columns; smaller tiles are padded to kTcMinSmem for the same bound
-// (at most 3 CTAs per SM), so no TMEM allocation waits for another CTA.
+// Shared memory of a CTA: 1 KB of alignment slack, kTcStages x (A stage 16 KB + B
+// stage BN x 128 B), a full and an empty mbarrier per stage, the TMEM address, the
+// verdict of the driving thread and the tile's BN biases. At BN = 128 that is 97 KB, so at most two CTAs
+// share an SM and their accumulators (<= 128 TMEM columns each) always fit its 512
+// columns; smaller tiles are padded to kTcMinSmem for the same bound (at most 3 CTAs
+// per SM), so no TMEM allocation waits for another CTA.
 constexpr size_t kTcMinSmem = 60 * 1024;
 
-// A stage buffer holds its rows K-major without swizzle, in 8 x 16-byte core
-// matrices (8 rows of 8 BF16 along K): row group g, K chunk c (8 elements) at byte
-// g * 1024 + c * 128, row r % 8 of it at + 16 (r % 8). In the MMA's shared-memory
-// descriptors, core matrices adjacent in K are 128 B apart (the leading byte
-// offset) and row groups 1024 B apart (the stride byte offset).
-constexpr uint32_t kTcLBO = 128, kTcSBO = 1024;
-__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t addr) {
-  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(kTcLBO >> 4) << 16) | ((uint64_t)(kTcSBO >> 4) << 32) |
-         (1ull << 46);  // descriptor version 1 (bits 46-48 = 0b001); no swizzle, base offset 0
+// A stage buffer holds each operand chunk-major: the 16-byte chunk c (elements
+// 8c .. 8c + 7 of the stage's reduction range) of all R rows of the tile lies in
+// R x 16 contiguous bytes at c R 16, row r at + 16 r, which is what one TMA copy of a
+// box of 8 elements x R rows writes. Its 8 x 16-byte core matrices (8 rows of one
+// chunk) are therefore 128 B apart along the rows (the descriptors' stride byte
+// offset) and R x 16 B apart along the reduction (the leading byte offset).
+__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t addr, uint32_t lbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)(128u >> 4) << 32) | (1ull << 46);  // version 1 (bits 46-48 = 0b001); no swizzle
 }
 
 // Instruction descriptor of tcgen05.mma kind::f16: D in F32 (bits 4-5 = 1), A and B
@@ -55,31 +60,15 @@ __device__ __forceinline__ uint32_t tc_idesc(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-// Copies stage [k0, k0 + kw) of rows [r0, r0 + rows) of the row-major matrix X (K
-// columns, nrow valid rows) into the stage buffer at shared address T with 16-byte
-// cp.async copies; rows past nrow read as zero. Copy idx takes row group
-// idx / (8 ck), chunk (idx / 8) % ck and row idx % 8 of the group, so that 8
-// consecutive threads fill one 128-byte core matrix; in a full stage (ck = 8) that
-// is byte idx * 16 of the buffer.
-__device__ __forceinline__ void tc_copy(uint32_t dst, const __nv_bfloat16 *src, bool ok) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(ok ? 16 : 0) : "memory");
-}
-__device__ __forceinline__ void tc_stage(uint32_t T, const __nv_bfloat16 *__restrict__ X, int r0, int rows, int nrow,
-                                         int K, int k0, int kw) {
-  if (kw == kTcKC) {
-    for (int idx = threadIdx.x; idx < rows * 8; idx += blockDim.x) {
-      const int r = r0 + ((idx >> 6) << 3) + (idx & 7), k = k0 + (((idx >> 3) & 7) << 3);
-      const bool ok = r < nrow;
-      tc_copy(T + (uint32_t)idx * 16u, ok ? X + (size_t)r * K + k : X, ok);
-    }
-    return;
-  }
-  const int ck = kw >> 3;
-  for (int idx = threadIdx.x; idx < rows * ck; idx += blockDim.x) {
-    const int q = idx >> 3, c = q % ck, g = q / ck, r = r0 + g * 8 + (idx & 7);
-    const bool ok = r < nrow;
-    tc_copy(T + (uint32_t)(g * 1024 + c * 128 + (idx & 7) * 16), ok ? X + (size_t)r * K + k0 + c * 8 : X, ok);
-  }
+// TMA tensor copy of the box at (x, y) of the 2-D map (x: element along the
+// reduction, a multiple of 8, so 16-byte aligned; y: row) into shared memory at dst,
+// completing on the mbarrier bar. Rows past the matrix read as zero.
+__device__ __forceinline__ void tc_tma(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
 }
 
 // two FP32 values rounded to BF16, the first in the low half (the lower address)
@@ -102,26 +91,35 @@ __device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
 }
 
 // C = A B^T (+ bias[n]) with optional ReLU (and optionally added to C); writes FP32
-// C and/or BF16 Cb. A: [M][K], B: [N][K], K a multiple of 16, BN (a multiple of 16 up
-// to kTcMaxN) dividing N. kTcThreads threads (two warpgroups); CTA (bx, by) computes
-// rows [128 bx, 128 bx + 128) and columns [BN by, BN by + BN). If an MMA completion is not seen within the
-// bounded wait, *err is set, the CTA waits once more (bounded) for the MMAs it
-// issued and for its copies, frees its tensor memory and writes nothing.
-__global__ void __launch_bounds__(kTcThreads) k_gemm_tc(const __nv_bfloat16 *__restrict__ A,
-                                                 const __nv_bfloat16 *__restrict__ B,
-                                                 const float *__restrict__ bias, float *C, __nv_bfloat16 *Cb,
-                                                 int M, int N, int K, int BN, int relu, int accumulate, int *err) {
+// C and/or BF16 Cb. A: [M][K] through the tensor map tmA (box 8 x arows, arows 128 or
+// M rounded up to 8 when M < 128), B: [N][K] through tmB (box 8 x BN); K a multiple of 16, BN (a multiple of 16 up to kTcMaxN)
+// dividing N. kTcThreads threads; CTA (bx, by) computes rows [128 bx, 128 bx + 128)
+// and columns [BN by, BN by + BN). If an mbarrier phase is not seen within the
+// bounded wait, *err is set, the driving thread waits once more (bounded) for the
+// copies and MMAs it issued, the CTA frees its tensor memory and writes nothing.
+__global__ void __launch_bounds__(kTcThreads) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
+                                                        const __grid_constant__ CUtensorMap tmB,
+                                                        const float *__restrict__ bias, float *C, __nv_bfloat16 *Cb,
+                                                        int M, int N, int K, int BN, int arows, int relu,
+                                                        int accumulate, int *err) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
-  const uint32_t base = (uint32_t)__cvta_generic_to_shared(tc_smem);
-  const uint32_t stage_bytes = (uint32_t)(kTcM + BN) * kTcKC * 2;
-  const uint32_t sbar = base + kTcStages * stage_bytes, sadr = sbar + 8 * kTcStages;
+  const uint32_t base = ((uint32_t)__cvta_generic_to_shared(tc_smem) + 1023u) & ~1023u;
+  const uint32_t a_bytes = kTcM * kTcKC * 2, stage_bytes = a_bytes + (uint32_t)BN * kTcKC * 2;
+  const uint32_t sfull = base + kTcStages * stage_bytes, sempty = sfull + 8 * kTcStages;
+  const uint32_t sadr = sempty + 8 * kTcStages, sok = sadr + 4;
+  // the tile's bias, staged while the reduction runs: the epilogue then reads shared
+  // memory instead of waiting on a global load per group of columns
+  float *sbias = reinterpret_cast<float *>(tc_smem + (sok + 4 - (uint32_t)__cvta_generic_to_shared(tc_smem)));
+  for (int t = threadIdx.x; t < BN; t += blockDim.x) sbias[t] = bias ? bias[n0 + t] : 0.f;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * kTcM, n0 = blockIdx.y * BN;
   uint32_t ncols = 32;  // TMEM columns: a power of two >= 32
   while ((int)ncols < BN) ncols <<= 1;
   if (threadIdx.x == 0) {
-    for (int b = 0; b < kTcStages; b++)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar + 8 * b) : "memory");
+    for (int b = 0; b < kTcStages; b++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sfull + 8 * b) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sempty + 8 * b) : "memory");
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -129,50 +127,42 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(const __nv_bfloat16 *__r
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  const int nk = (K + kTcKC - 1) / kTcKC;
-  auto stage = [&](int j) {
-    const uint32_t sa = base + (uint32_t)(j % kTcStages) * stage_bytes;
-    const int k0 = j * kTcKC, kw = min(kTcKC, K - k0);
-    tc_stage(sa, A, m0, kTcM, M, K, k0, kw);
-    tc_stage(sa + kTcM * kTcKC * 2, B, n0, BN, N, K, k0, kw);
-  };
-  // prologue: stages 0 .. kTcStages - 2, one copy group each (empty past the end),
-  // so that at step kc the group of stage kc is the oldest but kTcStages - 1
-  for (int j = 0; j < kTcStages - 1; j++) {
-    if (j < nk) stage(j);
-    asm volatile("cp.async.commit_group;" ::: "memory");
-  }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   uint32_t tmem;
   asm volatile("ld.shared.b32 %0, [%1];" : "=r"(tmem) : "r"(sadr) : "memory");
-  const uint32_t idesc = tc_idesc(kTcM, BN);
-  bool ok = true;
-  int last = -1;  // the last stage whose MMAs were committed
-  for (int kc = 0; kc < nk; kc++) {
-    const int nx = kc + kTcStages - 1;
-    if (nx < nk) {
-      // stage nx refills the buffer of stage kc - 1: its MMAs must have completed
-      if (kc >= 1) {
-        ok = __syncthreads_and(tc_wait(sbar + 8 * ((kc - 1) % kTcStages), ((kc - 1) / kTcStages) & 1)) != 0;
-        if (!ok) break;
+  if (threadIdx.x == 0) {
+    const int nk = (K + kTcKC - 1) / kTcKC;
+    const uint32_t idesc = tc_idesc(kTcM, BN);
+    int issued = 0;    // stages whose copies were issued
+    int consumed = 0;  // stages whose copies were seen to land
+    int last = -1;     // the last stage whose MMAs were committed
+    auto issue = [&](int j) {
+      const uint32_t sa = base + (uint32_t)(j % kTcStages) * stage_bytes, sb = sa + a_bytes;
+      const uint32_t bar = sfull + 8 * (j % kTcStages);
+      const int k0 = j * kTcKC, nc = min(kTcKC, K - k0) / 8;
+      const uint32_t bytes = (uint32_t)nc * (uint32_t)(arows + BN) * 16u;
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+      for (int c = 0; c < nc; c++) {
+        tc_tma(sa + (uint32_t)c * (kTcM * 16), &tmA, k0 + 8 * c, m0, bar);
+        tc_tma(sb + (uint32_t)c * (uint32_t)(BN * 16), &tmB, k0 + 8 * c, n0, bar);
       }
-      stage(nx);
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    asm volatile("cp.async.wait_group %0;" ::"n"(kTcStages - 1) : "memory");
-    // the stage's tiles, written through the generic proxy, made visible to the MMAs
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (threadIdx.x == 0) {
-      const uint32_t sa = base + (uint32_t)(kc % kTcStages) * stage_bytes, sb = sa + kTcM * kTcKC * 2;
+      issued = j + 1;
+    };
+    bool ok = true;
+    for (int j = 0; j < kTcStages && j < nk; j++) issue(j);
+    for (int kc = 0; kc < nk; kc++) {
+      const int b = kc % kTcStages;
+      if (!(ok = tc_wait(sfull + 8 * b, (kc / kTcStages) & 1))) break;
+      consumed = kc + 1;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sa = base + (uint32_t)b * stage_bytes, sb = sa + a_bytes;
       const int ks = min(kTcKC, K - kc * kTcKC) / 16;
       for (int s = 0; s < ks; s++) {
-        // K step s of the stage: core-matrix chunks 2s and 2s + 1 of every row group
-        const uint64_t ad = tc_smem_desc(sa + (uint32_t)s * 256u), bd = tc_smem_desc(sb + (uint32_t)s * 256u);
+        // K step s: chunks 2s and 2s + 1 of every row
+        const uint64_t ad = tc_smem_desc(sa + (uint32_t)(2 * s) * (kTcM * 16), kTcM * 16);
+        const uint64_t bd = tc_smem_desc(sb + (uint32_t)(2 * s) * (uint32_t)(BN * 16), (uint32_t)BN * 16u);
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
             " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
@@ -180,21 +170,31 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(const __nv_bfloat16 *__r
             : "memory");
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       sbar + 8 * (kc % kTcStages))
+                       sempty + 8 * b)
                    : "memory");
+      last = kc;
+      // refill the buffer of stage kc - 1 once its MMAs have completed
+      const int nx = kc - 1 + kTcStages;
+      if (kc >= 1 && nx < nk) {
+        if (!(ok = tc_wait(sempty + 8 * ((kc - 1) % kTcStages), ((kc - 1) / kTcStages) & 1))) break;
+        issue(nx);
+      }
     }
-    last = kc;
-  }
-  if (ok && last >= 0)
-    ok = __syncthreads_and(tc_wait(sbar + 8 * (last % kTcStages), (last / kTcStages) & 1)) != 0;
-  asm volatile("cp.async.wait_group 0;" ::: "memory");
-  if (!ok) {
-    if (threadIdx.x == 0) {
+    if (ok && last >= 0) ok = tc_wait(sempty + 8 * (last % kTcStages), (last / kTcStages) & 1);
+    if (!ok) {
       atomicExch(err, 1);
-      if (last >= 0) tc_wait(sbar + 8 * (last % kTcStages), (last / kTcStages) & 1);
+      // the copies still in flight and the MMAs issued finish before the CTA leaves
+      for (int j = consumed; j < issued; j++) tc_wait(sfull + 8 * (j % kTcStages), (j / kTcStages) & 1);
+      if (last >= 0) tc_wait(sempty + 8 * (last % kTcStages), (last / kTcStages) & 1);
     }
-  } else {
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("st.shared.b32 [%0], %1;" ::"r"(sok), "r"(ok ? 1 : 0) : "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  uint32_t ok;
+  asm volatile("ld.shared.b32 %0, [%1];" : "=r"(ok) : "r"(sok) : "memory");
+  if (ok) {
     // warp w reads TMEM lanes [32 (w % 4), 32 (w % 4) + 32), the rows of the tile its
     // position in the warpgroup gives it access to, and the columns of half w / 4
     const int quarter = warp & 3, half = warp >> 2;
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(const __nv_bfloat16 *__r
         for (int j = 0; j < 8; j++) {
           float x = __uint_as_float(v[j]);
           if (accumulate && C) x += C[(size_t)r * N + c + j];
-          if (bias) x += bias[c + j];
+          if (bias) x += sbias[c0 + j];
           if (relu) x = fmaxf(x, 0.f);
           o[j] = x;
         }
@@ -325,11 +325,49 @@ int mlp_tile_n(int N, int K) {
   return 0;
 }
 
+// cuTensorMapEncodeTiled from the driver, through the runtime (no link against
+// libcuda); null if the driver does not provide it
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// The 2-D tensor map of a row-major BF16 matrix of `rows` rows of K elements (K a
+// multiple of 8: 16-byte aligned rows), read in boxes of 8 elements x box_rows rows,
+// zero outside the matrix.
+bool bf16_map(CUtensorMap *map, const void *ptr, int K, int rows, int box_rows) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc || (reinterpret_cast<uintptr_t>(ptr) & 15)) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+  cuuint32_t box[2] = {8, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 int mlp_gemm_nt(void *stream, const void *A, const void *B, const float *bias, float *C, void *Cb, int M, int N,
                 int K, int relu, int accumulate, int *err) {
   const int bn = mlp_tile_n(N, K);
   if (M <= 0 || !bn) return -1;
-  size_t smem = (size_t)kTcStages * (kTcM + bn) * kTcKC * 2 + 8 * kTcStages + 8;
+  // A's box spans the tile's 128 rows (rows past M read as zero), or, for fewer rows
+  // than a tile, those rows rounded up to 8 (the tile's other accumulator rows then
+  // hold whatever the stage buffers held and are not written out)
+  const int arows = M >= kTcM ? kTcM : (M + 7) / 8 * 8;
+  CUtensorMap ma, mb;
+  if (!bf16_map(&ma, A, K, M, arows) || !bf16_map(&mb, B, K, N, bn)) return -2;
+  size_t smem = 1024 + (size_t)kTcStages * (kTcM + bn) * kTcKC * 2 + 16 * kTcStages + 8 + 4 * (size_t)bn;
   if (smem < kTcMinSmem) smem = kTcMinSmem;
   static size_t smem_set = 0;  // the largest dynamic shared memory granted so far
   if (smem > smem_set) {
@@ -337,8 +375,8 @@ int mlp_gemm_nt(void *stream, const void *A, const void *B, const float *bias, f
     smem_set = smem;
   }
   dim3 grid((M + kTcM - 1) / kTcM, N / bn);
-  k_gemm_tc<<<grid, kTcThreads, smem, (cudaStream_t)stream>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, bias, C,
-                                                      (__nv_bfloat16 *)Cb, M, N, K, bn, relu, accumulate, err);
+  k_gemm_tc<<<grid, kTcThreads, smem, (cudaStream_t)stream>>>(ma, mb, bias, C, (__nv_bfloat16 *)Cb, M, N, K, bn,
+                                                             arows, relu, accumulate, err);
   return 0;
 }
 
