@@ -107,12 +107,12 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(const __grid_constant__ 
   const uint32_t a_bytes = kTcM * kTcKC * 2, stage_bytes = a_bytes + (uint32_t)BN * kTcKC * 2;
   const uint32_t sfull = base + kTcStages * stage_bytes, sempty = sfull + 8 * kTcStages;
   const uint32_t sadr = sempty + 8 * kTcStages, sok = sadr + 4;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kTcM, n0 = blockIdx.y * BN;
   // the tile's bias, staged while the reduction runs: the epilogue then reads shared
   // memory instead of waiting on a global load per group of columns
   float *sbias = reinterpret_cast<float *>(tc_smem + (sok + 4 - (uint32_t)__cvta_generic_to_shared(tc_smem)));
   for (int t = threadIdx.x; t < BN; t += blockDim.x) sbias[t] = bias ? bias[n0 + t] : 0.f;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * kTcM, n0 = blockIdx.y * BN;
   uint32_t ncols = 32;  // TMEM columns: a power of two >= 32
   while ((int)ncols < BN) ncols <<= 1;
   if (threadIdx.x == 0) {
@@ -359,8 +359,18 @@ bool bf16_map(CUtensorMap *map, const void *ptr, int K, int rows, int box_rows) 
 
 int mlp_gemm_nt(void *stream, const void *A, const void *B, const float *bias, float *C, void *Cb, int M, int N,
                 int K, int relu, int accumulate, int *err) {
-  const int bn = mlp_tile_n(N, K);
+  int bn = mlp_tile_n(N, K);
   if (M <= 0 || !bn) return -1;
+  // narrower tiles while the grid would leave most SMs idle: these GEMMs are
+  // latency-bound, and a narrower tile stages less of B per CTA
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 1;
+  }
+  const long long mtiles = (M + kTcM - 1) / kTcM;
+  while (bn % 32 == 0 && bn >= 64 && mtiles * (N / bn) < nsm) bn /= 2;
   // A's box spans the tile's 128 rows (rows past M read as zero), or, for fewer rows
   // than a tile, those rows rounded up to 8 (the tile's other accumulator rows then
   // hold whatever the stage buffers held and are not written out)
