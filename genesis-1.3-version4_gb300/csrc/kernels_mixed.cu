@@ -1777,10 +1777,6 @@ __device__ __forceinline__ bool cell_rc(float gm, float dg, int ng, float x, flo
   return false;
 }
 
-// The deposition of the pair: this CTA (rank q) takes half of the slice's groups of
-// four particles (deposit_quads' grouping); each weighted contribution goes to the
-// CTA that holds its row: T[0], T[1] are the two bands (one local, one the peer's
-// through distributed shared memory), starting at global rows 0 and h.
 // The contribution to cell (ix, iy) if row iy is one of this CTA's rows [r0, r0 + nrow)
 // (its band S): every CTA of the pair deposits into its own shared memory only.
 __device__ __forceinline__ void pair_add(float2 *S, int r0, int nrow, int ng, int ix, int iy, float w, float cpx,
