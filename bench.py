@@ -17,10 +17,12 @@ Arms:
   default             the engine through its C ABI: the mixed form (FP32 field,
                       FP64 phase) is the headline `value`; the plain FP64 form is
                       timed beside it, and the mixed form's error against it is
-                      reported. `e2e` times a whole track window through the ABI
-                      with host buffers: upload of beam and field from pinned
-                      memory, K steps each followed by the per-slice power /
-                      bunching read-back, download of the final beam and field.
+                      reported. `e2e` times whole runs through the ABI with host
+                      buffers, as Gencore::run tracks a beam through the whole
+                      lattice: upload of beam and field from pinned memory, every
+                      step of the 443-step lattice with its per-slice diagnostics
+                      read back, download of the final beam and field.
+                      `e2e_short_window` does the same over K steps only.
   --impl reference    the CPU implementation of the step on the host cores, all
                       threads: the reference compiled from its own sources where
                       it is built (oracle/_ref), else the C restatement of it
@@ -198,7 +200,7 @@ TRAFFIC_SOURCE = "ncu capture of a 608-slice window, scaled to the launch's slic
 # per cell of each plain ADI sweep, from ncu captures of a 152-slice window
 # (profiles/ncu_fp64_k_push_k_adi_plain_sase152.md); nominal GB300 FP64 rate: 1.25 TFLOP/s
 # with FMA counted as two operations, i.e. 625 G FP64 instructions/s.
-FP64_INSTR = {"push_per_particle": 486.1, "adi_per_cell": 29.9}
+FP64_INSTR = {"push_per_particle": 477.1, "adi_per_cell": 19.9}
 FP64_NOMINAL_GINSTR = 625.0
 
 
@@ -699,7 +701,8 @@ def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_s
                          "generate_s": t_gen, "train_s": t_train}}
 
 
-E2E_WINDOWS = 11
+E2E_WINDOWS = 11       # timed windows of K steps
+E2E_RUNS = 5           # timed whole-lattice runs
 
 
 def e2e_window(g4gpu, torch, precision, beam_pinned, cur, field_pinned, lat, steps, reps, shapes=None):
@@ -859,6 +862,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=None, help="timed steps of the plain form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=None,
+                    help="steps of a timed e2e run (default: the whole lattice)")
     ap.add_argument("--no-full-lattice", action="store_true",
                     help="skip the mixed form's error after the whole 443-step lattice and its resonant companion")
     ap.add_argument("--nslice", type=int, default=None,
@@ -1011,16 +1016,23 @@ def main():
         del beam_q
     if rank == 0 and not args.no_e2e:
         field_pinned = torch.zeros((NS, NGRID * NGRID, 2), dtype=torch.float64).pin_memory()
-        times, h2d, d2h, phases = e2e_window(g4gpu, torch, g4gpu.MIXED, beam_pinned, cur, field_pinned, lat,
-                                             args.steps, E2E_WINDOWS, shapes=shapes)
-        t = statistics.median(times)
-        line["e2e"] = {"value": NS * args.steps / t, "unit": "slice-steps/s",
-                       "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-                       "window": f"upload beam+field, {args.steps} steps with every step's diagnostics "
-                                 f"(g4gpu_run_diag), download; median of {len(times)} windows after one warm-up window",
-                       "window_s": t, "windows_s": times,
-                       "spread": (max(times) - min(times)) / t,
-                       "phases_of_one_window": phases}
+        nrun = min(args.e2e_steps or lat.shape[0], lat.shape[0])
+        for key, steps, reps, what in (
+                ("e2e", nrun, E2E_RUNS, f"one whole run: upload beam+field, all {nrun} steps of the lattice with "
+                                        "every step's diagnostics (g4gpu_run_diag), download"),
+                ("e2e_short_window", args.steps, E2E_WINDOWS,
+                 f"upload beam+field, {args.steps} steps with every step's diagnostics (g4gpu_run_diag), "
+                 "download")):
+            times, h2d, d2h, phases = e2e_window(g4gpu, torch, g4gpu.MIXED, beam_pinned, cur, field_pinned, lat,
+                                                 steps, reps, shapes=shapes)
+            t = statistics.median(times)
+            line[key] = {"value": NS * steps / t, "unit": "slice-steps/s",
+                         "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
+                         "steps_per_window": steps,
+                         "window": what + f"; median of {len(times)} windows after one warm-up window",
+                         "window_s": t, "windows_s": times,
+                         "spread": (max(times) - min(times)) / t,
+                         "phases_of_one_window": phases}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1)
     if rank == 0:

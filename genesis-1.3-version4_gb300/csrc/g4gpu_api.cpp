@@ -1168,12 +1168,18 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
     bool any_dep = false;
     for (int k = 0; k < c.nfield; k++) any_dep = any_dep || sc.f[k].dep_on;
     // mixed form with the slice in shared memory: deposition and ADI in one kernel,
-    // one CTA per slice or a cluster pair (chosen by the autotuner; the pair also
-    // serves grids too large for one CTA when its segmented solves apply)
+    // one CTA per slice or a cluster pair (chosen by the autotuner); grids too large
+    // for one CTA take the smallest cluster whose bands fit (2 to 4 CTAs) when the
+    // segmented solves apply
     bool fused = h->mixed && c.solver == G4GPU_SOLVER_ADI && ng <= g4::fused_max_ngrid();
-    bool pair_ok = h->mixed && c.solver == G4GPU_SOLVER_ADI && ng <= g4::pair_max_ngrid();
-    for (int k = 0; k < c.nfield; k++) pair_ok = pair_ok && sc.f[k].tw > 0;
-    bool pair = pair_ok && (h->field_kernel == 1 || !fused);
+    int band_w = 0;
+    bool pair_ok = h->mixed && c.solver == G4GPU_SOLVER_ADI;
+    for (int k = 0; k < c.nfield; k++) {
+      pair_ok = pair_ok && sc.f[k].tw > 0;
+      band_w = std::max(band_w, sc.f[k].tw);
+    }
+    const int band_cl = pair_ok ? g4::band_cluster(ng, band_w) : 0;
+    bool pair = band_cl > 0 && (h->field_kernel == 1 || !fused);
     // the whole step in one kernel (push, deposition, ADI; one CTA per slice): chosen
     // by the autotuner (field_kernel 2) for one-field windows without space charge
     const bool rec_ok = h->diag_rec && g4::fused_diag_fits(ng, h->field_threads, h->diag_nharm);
@@ -1202,7 +1208,8 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
           const char *cb = (const char *)h->coef + (size_t)sc.f[k].coef * 3 * ng * h->csize;
           Timed t(h, G4GPU_K_ADI_X);
           if (pair)
-            g4::launch_field_pair_mixed(L, scf, k, h->beam, h->field[k], cb, ns, np, ng, sc.f[k].dep_on);
+            g4::launch_field_band_mixed(L, scf, k, h->beam, h->field[k], cb, ns, np, ng, sc.f[k].dep_on,
+                                        band_cl);
           else
             g4::launch_field_fused_mixed(L, scf, k, h->beam, h->field[k], cb, ns, np, ng, sc.f[k].dep_on,
                                          h->field_threads, nullptr,
@@ -1880,8 +1887,13 @@ extern "C" int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_thread
   }
   // the cluster-pair field kernel, where the step's segmented solves apply
   int best_fk = 0;
-  bool pairable = fused && c.ngrid <= g4::pair_max_ngrid();
-  for (int k = 0; k < c.nfield; k++) pairable = pairable && h->steps[istep].f[k].tw > 0;
+  bool pairable = fused;
+  int band_w = 0;
+  for (int k = 0; k < c.nfield; k++) {
+    pairable = pairable && h->steps[istep].f[k].tw > 0;
+    band_w = std::max(band_w, h->steps[istep].f[k].tw);
+  }
+  pairable = pairable && g4::band_cluster(c.ngrid, band_w) == 2;
   if (!rc && pairable) {
     float ms;
     if (!(rc = time_step(best_pb, best_ft, &ms))) {

@@ -89,7 +89,9 @@ struct g4gpu_ctx {
   // launch shapes (chosen by g4gpu_autotune, defaults otherwise)
   int push_block = 256;
   int field_threads = 512;
-  int field_kernel = 0;  // mixed ADI: 0 one CTA per slice (k_field_fused_f), 1 a cluster pair (k_field_pair_f)
+  // mixed ADI with the slice in shared memory: 0 one CTA per slice (k_field_fused_f),
+  // 1 a cluster pair (k_field_band_f<2>), 2 the whole step per CTA (k_step_fused_f)
+  int field_kernel = 0;
 
   // captured step sequences, keyed by the step range and the ring state they start from
   bool graph_mode = false;

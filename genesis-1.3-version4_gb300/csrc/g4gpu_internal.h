@@ -144,12 +144,15 @@ void launch_diag_field_mixed(const Launch &L, const void *field, int ns, int ngr
 // Fused deposition + ADI of one field in shared memory, one CTA per slice; usable
 // for ngrid <= fused_max_ngrid() (168: the FP32 slice must fit in 227 KB).
 int fused_max_ngrid();
-// The same step on a thread-block cluster of two CTAs per slice, each holding half the
-// rows; usable for ngrid <= pair_max_ngrid() when the step's segmented solves apply
-// (FieldStep::tw > 0).
-int pair_max_ngrid();
-void launch_field_pair_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b, void *field,
-                             const void *coef, int ns, int np, int ngrid, int deposit);
+// The same step on a thread-block cluster of cl CTAs per slice (2 <= cl <=
+// kMaxBandCluster), each holding a band of the rows; usable when the step's segmented
+// solves apply (FieldStep::tw > 0). band_cluster(ngrid, W) gives the smallest cluster
+// whose bands fit shared memory with the last band at least W rows (the segments'
+// warm-up), or 0 if none does.
+constexpr int kMaxBandCluster = 4;
+int band_cluster(int ngrid, int W);
+void launch_field_band_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b, void *field,
+                             const void *coef, int ns, int np, int ngrid, int deposit, int cl);
 // threads: CTA size, a multiple of 32 in [2 ngrid, 1024]. dbeam / dfield (may be
 // null): the step's diagnostic record, beam [nslice][beam_diag_width(nharm)] (formed by
 // the launch of field 0) and this field's [nslice][kFieldSums + 2] in storage order.

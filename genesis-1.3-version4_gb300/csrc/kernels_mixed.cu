@@ -119,6 +119,17 @@ constexpr float kInvTwoPiF = 0.159154943f;
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+// r - c d for a coefficient c = (0, cy) with zero real part: the ADI's off-diagonal
+// coefficients c[k] = (0, -mlow[k]) and cstep are purely imaginary
+// (FieldSolverADI.cpp:139, 161-165), so c d = (-cy d.y, cy d.x): two FMAs instead of
+// a complex product and a difference
+__device__ __forceinline__ float2 sub_imulf(float2 r, float cy, float2 d) {
+  return make_float2(fmaf(cy, d.y, r.x), fmaf(-cy, d.x, r.y));
+}
+// v - w x for complex w, both products fused into the difference
+__device__ __forceinline__ float2 sub_cmulf(float2 v, float2 w, float2 x) {
+  return make_float2(fmaf(-w.x, x.x, fmaf(w.y, x.y, v.x)), fmaf(-w.x, x.y, fmaf(-w.y, x.x, v.y)));
+}
 // reduces an FP32 angle of moderate size (|a| < ~1e3) to [-pi, pi]
 __device__ __forceinline__ float wrapf(float a) { return fmaf(-kTwoPiF, rintf(a * kInvTwoPiF), a); }
 
@@ -459,18 +470,14 @@ __global__ void __launch_bounds__(128) k_adi_x_f(const float2 *__restrict__ fiel
     if (k == 0) {
       v = cmulf(r, cf.cbet[0]);
     } else {
-      float2 cp = cmulf(cf.c[k], prev);
-      v = cmulf(make_float2(r.x - cp.x, r.y - cp.y), cf.cbet[k]);
+      v = cmulf(sub_imulf(r, cf.c[k].y, prev), cf.cbet[k]);
     }
     w[k] = v;
     prev = v;
   }
   float2 next = prev;
   for (int k = ng - 2; k >= 0; k--) {
-    float2 cw = cmulf(cf.cwet[k + 1], next);
-    float2 v = w[k];
-    v.x -= cw.x;
-    v.y -= cw.y;
+    float2 v = sub_cmulf(w[k], cf.cwet[k + 1], next);
     w[k] = v;
     next = v;
   }
@@ -503,8 +510,7 @@ __global__ void __launch_bounds__(128) k_adi_y_f(float2 *__restrict__ field,
     if (k == 0) {
       v = cmulf(r, cf.cbet[0]);
     } else {
-      float2 cp = cmulf(cf.c[k], prev);
-      v = cmulf(make_float2(r.x - cp.x, r.y - cp.y), cf.cbet[k]);
+      v = cmulf(sub_imulf(r, cf.c[k].y, prev), cf.cbet[k]);
     }
     u[o] = v;
     prev = v;
@@ -512,10 +518,7 @@ __global__ void __launch_bounds__(128) k_adi_y_f(float2 *__restrict__ field,
   float2 next = prev;
   for (int k = ng - 2; k >= 0; k--) {
     size_t o = (size_t)k * ng;
-    float2 cw = cmulf(cf.cwet[k + 1], next);
-    float2 v = u[o];
-    v.x -= cw.x;
-    v.y -= cw.y;
+    float2 v = sub_cmulf(u[o], cf.cwet[k + 1], next);
     u[o] = v;
     next = v;
   }
@@ -569,8 +572,7 @@ __device__ __forceinline__ void thomas2(float2 *S, int stride, int ng, int up, c
   for (int t = 0; t < len; t++) {
     float2 r = rn;
     if (t + 1 < len) rn = L[(t + 1) * step];
-    float2 ad = cmulf(a, d);
-    d = cmulf(make_float2(r.x - ad.x, r.y - ad.y), CB[t]);
+    d = cmulf(sub_imulf(r, a.y, d), CB[t]);
     L[t * step] = d;
   }
   // meet at row m
@@ -579,14 +581,11 @@ __device__ __forceinline__ void thomas2(float2 *S, int stride, int ng, int up, c
   d_other.y = __shfl_xor_sync(mask, d.y, 1);
   float2 dsum = make_float2(d.x + d_other.x, d.y + d_other.y);
   float2 rm = S[m * stride];
-  float2 ads = cmulf(a, dsum);
-  float2 xm = cmulf(make_float2(rm.x - ads.x, rm.y - ads.y), invden);
+  float2 xm = cmulf(sub_imulf(rm, a.y, dsum), invden);
   // back substitution outward from m
   float2 x = xm;
   for (int t = len - 1; t >= 0; t--) {
-    float2 v = L[t * step];
-    float2 cw = cmulf(CW[t + 1], x);
-    x = make_float2(v.x - cw.x, v.y - cw.y);
+    x = sub_cmulf(L[t * step], CW[t + 1], x);
     L[t * step] = x;
   }
   if (!up) S[m * stride] = xm;
@@ -615,14 +614,14 @@ __device__ __forceinline__ void thomas_seg(float2 *S, int lstride, int estride, 
   float2 d = make_float2(0.f, 0.f);
   if (act)
     for (int k = max(0, b - W); k < b; k++) {
-      float2 r = L[k * estride], cd = cmulf(Cc[k], d);
-      d = cmulf(make_float2(r.x - cd.x, r.y - cd.y), CB[k]);
+      float2 r = L[k * estride];
+      d = cmulf(sub_imulf(r, Cc[k].y, d), CB[k]);
     }
   __syncthreads();
   if (act)
     for (int k = b; k < e; k++) {
-      float2 r = L[k * estride], cd = cmulf(Cc[k], d);
-      d = cmulf(make_float2(r.x - cd.x, r.y - cd.y), CB[k]);
+      float2 r = L[k * estride];
+      d = cmulf(sub_imulf(r, Cc[k].y, d), CB[k]);
       L[k * estride] = d;
     }
   __syncthreads();
@@ -632,8 +631,7 @@ __device__ __forceinline__ void thomas_seg(float2 *S, int lstride, int estride, 
   if (act && k1 >= e) {
     x = L[k1 * estride];
     for (int k = k1 - 1; k >= e; k--) {
-      float2 v = L[k * estride], cw = cmulf(CW[k + 1], x);
-      x = make_float2(v.x - cw.x, v.y - cw.y);
+      x = sub_cmulf(L[k * estride], CW[k + 1], x);
     }
   }
   __syncthreads();
@@ -641,8 +639,7 @@ __device__ __forceinline__ void thomas_seg(float2 *S, int lstride, int estride, 
     for (int k = e - 1; k >= b; k--) {
       float2 v = L[k * estride];
       if (k < ng - 1) {
-        float2 cw = cmulf(CW[k + 1], x);
-        v = make_float2(v.x - cw.x, v.y - cw.y);
+        v = sub_cmulf(v, CW[k + 1], x);
       }
       x = v;
       L[k * estride] = x;
@@ -1569,31 +1566,40 @@ PtrsF make_ptrs_f(const DeviceBeam &b, void *const *field, void *const *src, int
   return p;
 }
 
-// ---- fused field step on a pair of CTAs (a thread-block cluster of two) -------
+// ---- fused field step on a cluster of CTAs (2, 3 or 4 per slice) ---------------
 //
-// The slice's rows are split between the two CTAs of a cluster: rows [0, h) and
-// [h, ng), h = ceil(ng / 2). Each CTA holds its ~half slice (92 KB at ngrid 151), so
-// two CTAs fit an SM and one CTA's bulk copies, barriers and latency overlap the
-// other's arithmetic, which a single 182 KB CTA per SM cannot do. The phases are those
-// of k_field_fused_f, with what crosses the split done as follows:
+// The slice's rows are split between the CL CTAs of a thread-block cluster: CTA q
+// holds the band of rows [q h, min((q + 1) h, ng)), h = ceil(ng / CL). A band is a
+// fraction of the slice (92 KB at ngrid 151 for a pair, 131 KB at ngrid 255 for four),
+// so grids too large for one CTA still take the one-pass step with the field read and
+// written once, and a pair's two CTAs share an SM, one CTA's bulk copies, barriers and
+// latency overlapping the other's arithmetic. The phases are those of k_field_fused_f,
+// with what crosses a band boundary done as follows:
 //  * the column stencils take the rows just outside a CTA's band from the slice in
 //    global memory, which stays unmodified until the final stores;
-//  * the deposition splits the particles between the two CTAs, and a contribution to
-//    the other CTA's rows is a shared-memory atomic through the cluster's distributed
-//    shared memory;
-//  * the column solves' segments next to the split take their warm-up values from
-//    the other CTA's shared memory, read between cluster barriers that order them
-//    against that CTA's in-place writes.
-// Every thread of both CTAs passes every cluster barrier (no early exit), and the
+//  * the deposition: every CTA reads every particle of the slice and deposits the
+//    contributions to its own rows (deposit_pair);
+//  * the column solves' segments next to a boundary take their warm-up values from
+//    the neighbouring CTA's shared memory (distributed shared memory), read between
+//    cluster barriers that order them against that CTA's in-place writes. A warm-up
+//    spans W <= 21 rows, so only the adjacent bands are read, and the host requires
+//    the last band to hold at least W rows.
+// Every thread of every CTA passes every cluster barrier (no early exit), and the
 // last distributed-shared-memory access precedes the last cluster barrier.
 namespace cg = cooperative_groups;
 
-constexpr int kPairThreads = 512;
+// CTA size: a pair shares an SM (two CTAs of 512 threads); larger clusters take one
+// CTA of 1024 threads per SM
+template <int CL>
+constexpr int band_threads() {
+  return CL == 2 ? 512 : 1024;
+}
 
-__device__ __forceinline__ void pair_rows(int ng, int q, int &r0, int &nrow) {
-  const int h = (ng + 1) / 2;
-  r0 = q ? h : 0;
-  nrow = q ? ng - h : h;
+template <int CL>
+__device__ __forceinline__ void band_rows(int ng, int q, int &r0, int &nrow) {
+  const int h = (ng + CL - 1) / CL;
+  r0 = q * h;
+  nrow = min(h, ng - r0);
 }
 
 // thomas_seg for nline lines of n elements (the rows of a band)
@@ -1608,14 +1614,14 @@ __device__ __forceinline__ void thomas_lines(float2 *S, int nline, int lstride, 
   float2 d = make_float2(0.f, 0.f);
   if (act)
     for (int k = max(0, b - W); k < b; k++) {
-      float2 r = L[k * estride], cd = cmulf(Cc[k], d);
-      d = cmulf(make_float2(r.x - cd.x, r.y - cd.y), CB[k]);
+      float2 r = L[k * estride];
+      d = cmulf(sub_imulf(r, Cc[k].y, d), CB[k]);
     }
   __syncthreads();
   if (act)
     for (int k = b; k < e; k++) {
-      float2 r = L[k * estride], cd = cmulf(Cc[k], d);
-      d = cmulf(make_float2(r.x - cd.x, r.y - cd.y), CB[k]);
+      float2 r = L[k * estride];
+      d = cmulf(sub_imulf(r, Cc[k].y, d), CB[k]);
       L[k * estride] = d;
     }
   __syncthreads();
@@ -1624,8 +1630,7 @@ __device__ __forceinline__ void thomas_lines(float2 *S, int nline, int lstride, 
   if (act && k1 >= e) {
     x = L[k1 * estride];
     for (int k = k1 - 1; k >= e; k--) {
-      float2 v = L[k * estride], cw = cmulf(CW[k + 1], x);
-      x = make_float2(v.x - cw.x, v.y - cw.y);
+      x = sub_cmulf(L[k * estride], CW[k + 1], x);
     }
   }
   __syncthreads();
@@ -1633,8 +1638,7 @@ __device__ __forceinline__ void thomas_lines(float2 *S, int nline, int lstride, 
     for (int k = e - 1; k >= b; k--) {
       float2 v = L[k * estride];
       if (k < n - 1) {
-        float2 cw = cmulf(CW[k + 1], x);
-        v = make_float2(v.x - cw.x, v.y - cw.y);
+        v = sub_cmulf(v, CW[k + 1], x);
       }
       x = v;
       L[k * estride] = x;
@@ -1701,35 +1705,39 @@ __device__ __forceinline__ void r2_cols_band(float2 *S, const float2 *__restrict
   }
 }
 
-// Column solve of the pair (thomas_seg along the columns, rows split between the
+// Column solve of a cluster (thomas_seg along the columns, rows split between the
 // CTAs): band row k of this CTA is global row r0 + k; the warm-ups of the segments
-// next to the split read the peer's band P (distributed shared memory).
-__device__ __forceinline__ void thomas_cols_pair(cg::cluster_group &cl, float2 *S, const float2 *P, int ng, int r0,
-                                                 int nrow, int nrow_peer, int q, int nseg, int W, const float2 *Cc,
-                                                 const float2 *CB, const float2 *CW) {
+// next to a boundary read the band above (Pa, nrow_above rows) or below (Pb) in the
+// neighbouring CTA's shared memory (distributed shared memory).
+__device__ __forceinline__ void thomas_cols_band(cg::cluster_group &cl, float2 *S, const float2 *Pa,
+                                                 const float2 *Pb, int ng, int r0, int nrow, int nrow_above,
+                                                 int nseg, int W, const float2 *Cc, const float2 *CB,
+                                                 const float2 *CW) {
   const int tid = threadIdx.x;
   const int col = tid % ng, seg = tid / ng;
   const int len = (nrow + nseg - 1) / nseg;
   const int b = seg * len, e = min(b + len, nrow);
   const bool act = seg < nseg && b < e;
-  // band row k, k < 0 or k >= nrow meaning the peer's rows (above for q = 1, below for q = 0)
+  // band row k, k < 0 or k >= nrow meaning the rows of the band above or below (k
+  // stays within W rows of the band, and only the first band has none above, the
+  // last none below: their sweeps start and end at the grid's edge)
   auto at = [&](int k) -> float2 {
     if (k >= 0 && k < nrow) return S[k * ng + col];
-    return q ? P[(nrow_peer + k) * ng + col] : P[(k - nrow) * ng + col];
+    return k < 0 ? Pa[(nrow_above + k) * ng + col] : Pb[(k - nrow) * ng + col];
   };
   float2 d = make_float2(0.f, 0.f);
   if (act)
     for (int k = max(-r0, b - W); k < b; k++) {
       const int g = r0 + k;
-      float2 r = at(k), cd = cmulf(Cc[g], d);
-      d = cmulf(make_float2(r.x - cd.x, r.y - cd.y), CB[g]);
+      float2 r = at(k);
+      d = cmulf(sub_imulf(r, Cc[g].y, d), CB[g]);
     }
   cl.sync();
   if (act)
     for (int k = b; k < e; k++) {
       const int g = r0 + k;
-      float2 r = S[k * ng + col], cd = cmulf(Cc[g], d);
-      d = cmulf(make_float2(r.x - cd.x, r.y - cd.y), CB[g]);
+      float2 r = S[k * ng + col];
+      d = cmulf(sub_imulf(r, Cc[g].y, d), CB[g]);
       S[k * ng + col] = d;
     }
   cl.sync();
@@ -1738,8 +1746,7 @@ __device__ __forceinline__ void thomas_cols_pair(cg::cluster_group &cl, float2 *
   if (act && k1 >= e) {
     x = at(k1);
     for (int k = k1 - 1; k >= e; k--) {
-      float2 v = at(k), cw = cmulf(CW[r0 + k + 1], x);
-      x = make_float2(v.x - cw.x, v.y - cw.y);
+      x = sub_cmulf(at(k), CW[r0 + k + 1], x);
     }
   }
   cl.sync();
@@ -1748,8 +1755,7 @@ __device__ __forceinline__ void thomas_cols_pair(cg::cluster_group &cl, float2 *
       const int g = r0 + k;
       float2 v = S[k * ng + col];
       if (g < ng - 1) {
-        float2 cw = cmulf(CW[g + 1], x);
-        v = make_float2(v.x - cw.x, v.y - cw.y);
+        v = sub_cmulf(v, CW[g + 1], x);
       }
       x = v;
       S[k * ng + col] = x;
@@ -1778,7 +1784,7 @@ __device__ __forceinline__ bool cell_rc(float gm, float dg, int ng, float x, flo
 }
 
 // The contribution to cell (ix, iy) if row iy is one of this CTA's rows [r0, r0 + nrow)
-// (its band S): every CTA of the pair deposits into its own shared memory only.
+// (its band S): every CTA of a cluster deposits into its own shared memory only.
 __device__ __forceinline__ void pair_add(float2 *S, int r0, int nrow, int ng, int ix, int iy, float w, float cpx,
                                          float cpy) {
   if (iy < r0 || iy >= r0 + nrow) return;
@@ -1791,7 +1797,7 @@ __device__ __forceinline__ void pair_group(const StepConstF &sc, const FieldStep
                                            const float *dgam, int n) {
   CellRC c;
   if (!cell_rc(fs.gridmax, fs.dgrid, ng, x, y, c)) return;
-  if (c.iy1 < r0 || c.iy >= r0 + nrow) return;  // the particle's rows are the peer's
+  if (c.iy1 < r0 || c.iy >= r0 + nrow) return;  // the particle's rows are another band's
   float dx = x - sc.ax, dy = y - sc.ay;
   float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
   float a = sqrtf(faw2) * scl;
@@ -1808,12 +1814,12 @@ __device__ __forceinline__ void pair_group(const StepConstF &sc, const FieldStep
   pair_add(S, r0, nrow, ng, c.ix, c.iy1, c.wx * (1.f - c.wy), cpx, cpy);
   pair_add(S, r0, nrow, ng, c.ix1, c.iy1, (1.f - c.wx) * (1.f - c.wy), cpx, cpy);
 }
-// The pair's deposition: each CTA reads every particle of the slice and deposits the
+// A cluster's deposition: each CTA reads every particle of the slice and deposits the
 // contributions to its own rows into its own band, with shared-memory atomics only. A
-// particle whose footprint straddles the two bands is deposited by both, each into its
-// rows. (Splitting the particles between the CTAs instead sends half of every CTA's
-// contributions to the peer as distributed-shared-memory atomics, which took 2.8 times
-// as long as the single CTA's whole deposition.)
+// particle whose footprint straddles two bands is deposited by both, each into its
+// rows. (Splitting the particles between the CTAs of a pair instead sends half of
+// every CTA's contributions to the peer as distributed-shared-memory atomics, which
+// took 2.8 times as long as the single CTA's whole deposition.)
 __device__ __forceinline__ void deposit_pair(const StepConstF &sc, const FieldStepF &fs, const PtrsF &p, float2 *S,
                                              int r0, int nrow, int is, int np, int ng) {
   const float scl = fs.dep_scl * slice_cur_f(p, is, np);
@@ -1857,36 +1863,44 @@ __device__ __forceinline__ void deposit_pair(const StepConstF &sc, const FieldSt
   }
 }
 
-// shared memory of one CTA of the pair: mbarrier, coefficients, slack, its band
-size_t pair_smem_bytes(int ng) {
-  return ((16 + 3 * (size_t)ng * 8 + 15) & ~(size_t)15) + 8 + (size_t)((ng + 1) / 2) * ng * 8;
+// shared memory of one CTA of a cluster of CL: mbarrier, coefficients, slack, its band
+size_t band_smem_bytes(int ng, int CL) {
+  return ((16 + 3 * (size_t)ng * 8 + 15) & ~(size_t)15) + 8 + (size_t)((ng + CL - 1) / CL) * ng * 8;
 }
 
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 2)
-    k_field_pair_f(StepConstF sc, int k, PtrsF p, float2 *__restrict__ field, const float2 *__restrict__ coef,
+template <int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(band_threads<CL>(), CL == 2 ? 2 : 1)
+    k_field_band_f(StepConstF sc, int k, PtrsF p, float2 *__restrict__ field, const float2 *__restrict__ coef,
                    int ns, int np, int ng, int deposit, int *err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cl = cg::this_cluster();
   const int q = (int)cl.block_rank();
   const int ncell = ng * ng;
   const FieldStepF &fs = sc.f[k];
-  const int is = blockIdx.x >> 1;
+  const int is = blockIdx.x / CL;
   const int i = (is + fs.first) % ns;
   float2 *u = field + (size_t)i * ncell;
-  int r0, nrow, r0p, nrowp;
-  pair_rows(ng, q, r0, nrow);
-  pair_rows(ng, 1 - q, r0p, nrowp);
+  int r0, nrow, r0a, nrowa, r0b, nrowb;
+  band_rows<CL>(ng, q, r0, nrow);
+  band_rows<CL>(ng, q > 0 ? q - 1 : q, r0a, nrowa);
+  band_rows<CL>(ng, q < CL - 1 ? q + 1 : q, r0b, nrowb);
   float2 *ub = u + (size_t)r0 * ng;  // this CTA's band in global memory
   // layout as k_field_fused_f: [mbarrier][8 B][coefficients 3 ng][pad][band], the band
-  // congruent to its global rows mod 16; the peer's band at its own offset
+  // congruent to its global rows mod 16; a neighbour's band at its own offset
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);
   float2 *C = reinterpret_cast<float2 *>(smem_raw + 16);
   float2 *CB = C + ng, *CW = CB + ng;
   const size_t soff = (16 + 3 * (size_t)ng * 8 + 15) & ~(size_t)15;
   float2 *S = reinterpret_cast<float2 *>(smem_raw + soff + (reinterpret_cast<uintptr_t>(ub) & 15));
-  float2 *Sp_local = reinterpret_cast<float2 *>(
-      smem_raw + soff + (reinterpret_cast<uintptr_t>(u + (size_t)r0p * ng) & 15));
-  float2 *P = cl.map_shared_rank(Sp_local, 1 - q);
+  auto band_of = [&](int r0n, int rank) -> float2 * {
+    float2 *local = reinterpret_cast<float2 *>(
+        smem_raw + soff + (reinterpret_cast<uintptr_t>(u + (size_t)r0n * ng) & 15));
+    return cl.map_shared_rank(local, rank);
+  };
+  // the bands above and below (a CTA's own band stands in at the grid's edges, where
+  // the column solve reads no neighbour)
+  const float2 *Pa = band_of(r0a, q > 0 ? q - 1 : q);
+  const float2 *Pb = band_of(r0b, q < CL - 1 ? q + 1 : q);
   uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(bar);
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s) : "memory");
@@ -1902,11 +1916,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 2)
   stencil_cols_band(S, u, ng, r0, nrow, cs, nseg);  // S1 on this band
   __syncthreads();  // the band holds S1 before any deposit
   if (deposit) deposit_pair(sc, fs, p, S, r0, nrow, is, np, ng);
-  cl.sync();  // both bands are complete before the solves read across the pair
+  cl.sync();  // every band is complete before the solves read across the cluster
   thomas_lines(S, nrow, ng, 1, ng, max(1, min((int)blockDim.x / nrow, 32)), fs.tw, C, CB, CW);  // rows
   r2_cols_band(S, u, ng, r0, nrow, cs, nseg);
   __syncthreads();
-  thomas_cols_pair(cl, S, P, ng, r0, nrow, nrowp, q, nseg, fs.tw, C, CB, CW);  // columns
+  thomas_cols_band(cl, S, Pa, Pb, ng, r0, nrow, nrowa, nseg, fs.tw, C, CB, CW);  // columns
   bulk_store(ub, S, nrow * ng);
   if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
@@ -2272,24 +2286,37 @@ void launch_step_fused_mixed(const Launch &L, const StepConstF &sc, const Device
                                              dbeam, dfield, nharm, gref);
 }
 
-int pair_max_ngrid() {
-  int ng = 3;
-  while (pair_smem_bytes(ng + 1) <= 227u * 1024u) ng++;
-  return ng;
+int band_cluster(int ngrid, int W) {
+  for (int cl = 2; cl <= kMaxBandCluster; cl++) {
+    const int h = (ngrid + cl - 1) / cl, last = ngrid - (cl - 1) * h;
+    if (band_smem_bytes(ngrid, cl) <= 227u * 1024u && last >= max(W, 2)) return cl;
+  }
+  return 0;
 }
 
-void launch_field_pair_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b, void *field,
-                             const void *coef, int ns, int np, int ngrid, int deposit) {
+template <int CL>
+static void launch_band(const Launch &L, const StepConstF &sc, int k, const PtrsF &p, void *field, const void *coef,
+                        int ns, int np, int ngrid, int deposit) {
   static std::atomic<unsigned long long> configured{0};  // one bit per device
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 64 && !(configured.load() & (1ull << dev))) {
-    cudaFuncSetAttribute(k_field_pair_f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(k_field_band_f<CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     configured.fetch_or(1ull << dev);
   }
-  PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
-  k_field_pair_f<<<2 * ns, kPairThreads, pair_smem_bytes(ngrid), (cudaStream_t)L.stream>>>(
+  k_field_band_f<CL><<<CL * ns, band_threads<CL>(), band_smem_bytes(ngrid, CL), (cudaStream_t)L.stream>>>(
       sc, k, p, (float2 *)field, (const float2 *)coef, ns, np, ngrid, deposit, L.err);
+}
+
+void launch_field_band_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b, void *field,
+                             const void *coef, int ns, int np, int ngrid, int deposit, int cl) {
+  PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
+  if (cl == 2)
+    launch_band<2>(L, sc, k, p, field, coef, ns, np, ngrid, deposit);
+  else if (cl == 3)
+    launch_band<3>(L, sc, k, p, field, coef, ns, np, ngrid, deposit);
+  else
+    launch_band<4>(L, sc, k, p, field, coef, ns, np, ngrid, deposit);
 }
 
 namespace {

@@ -32,6 +32,16 @@ __device__ __forceinline__ C2 csub(C2 a, C2 b) { return {a.x - b.x, a.y - b.y}; 
 // product fused into its sum: one rounding fewer per component than GCC's evaluation
 // (a last-bit difference), and two FP64 instructions instead of three
 __device__ __forceinline__ C2 cmul_fma(C2 a, C2 b) { return {fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x)}; }
+// a + i b l for real b. The ADI's cstep and off-diagonal coefficients c[k] are purely
+// imaginary (FieldSolverADI.cpp:139, 161-165: real part exactly 0), so the reference's
+// complex product i b l is exactly (-b l.y, b l.x); here it is fused into the sum (a
+// last-bit difference, two FP64 instructions instead of four).
+__device__ __forceinline__ C2 add_imul(C2 a, double b, C2 l) { return {fma(-b, l.y, a.x), fma(b, l.x, a.y)}; }
+// d - w n for complex w, both products fused into the difference (four FP64
+// instructions instead of six)
+__device__ __forceinline__ C2 sub_cmul(C2 d, C2 w, C2 n) {
+  return {fma(-w.x, n.x, fma(w.y, n.y, d.x)), fma(-w.x, n.y, fma(-w.y, n.x, d.y))};
+}
 // real * complex
 __device__ __forceinline__ C2 rmul(double s, C2 a) { return {s * a.x, s * a.y}; }
 // complex * real
@@ -105,9 +115,15 @@ struct Cell {
 // inverse idg (the weights then differ in the last bit, and a particle within rounding
 // of a cell boundary may take the neighbouring cell, where the bilinear weights give
 // the same value).
+// |v| < gm for gm > 0 as an integer comparison of the magnitudes' bit patterns: the
+// same verdict as -gm < v < gm for every v (NaN fails both), without the FP64 pipe.
+__device__ __forceinline__ bool inside(double v, double gm) {
+  return (unsigned long long)(__double_as_longlong(v) & 0x7fffffffffffffffLL) <
+         (unsigned long long)__double_as_longlong(gm);
+}
 __device__ __forceinline__ bool ll_gridpoint(double gm, double idg, int ng, double x, double y,
                                              Cell &c) {
-  if ((x > -gm) && (x < gm) && (y > -gm) && (y < gm)) {
+  if (inside(x, gm) && inside(y, gm)) {
     double wx = (x + gm) * idg;
     double wy = (y + gm) * idg;
     double fx = floor(wx), fy = floor(wy);
@@ -125,13 +141,18 @@ __device__ __forceinline__ bool ll_gridpoint(double gm, double idg, int ng, doub
   return false;
 }
 
+// |v| < 2^-k for the exponent field ek = 1023 - k: a comparison of the high word's
+// magnitude bits (integer pipe; NaN and infinities fail)
+__device__ __forceinline__ bool below_pow2(double v, int ek) {
+  return (__double2hiint(v) & 0x7fffffff) < (ek << 20);
+}
 // 1 / x given r, the reciprocal of a nearby value: two Newton steps, each squaring
-// the relative error e = 1 - x r, when |e| <= 1e-5 (then the error is below 1e-20
+// the relative error e = 1 - x r, when |e| < 2^-17 (then the error is below 1e-20
 // before rounding), else the division. The RK4 stages of a step change gamma by far
 // less than that, so each stage's 1 / gamma follows from the previous one.
 __device__ __forceinline__ double recip_near(double x, double r) {
   double e = fma(-x, r, 1.);
-  if (!(fabs(e) <= 1e-5)) return 1. / x;
+  if (!below_pow2(e, 1023 - 17)) return 1. / x;
   r = fma(r, e, r);
   e = fma(-x, r, 1.);
   return fma(r, e, r);
@@ -161,9 +182,8 @@ __device__ __forceinline__ void ode(const StepConst &sc, const C2 *rpart, const 
   k2gg += fma(ctmp.y * ib, itg, -ez);
 }
 
-// e^{i eps} by its Taylor series, for |eps| <= kRotMax: the first omitted terms are
-// eps^14 / 14! (cosine) and eps^13 / 13! (sine), below 1e-19 at kRotMax = 0.25.
-constexpr double kRotMax = 0.25;
+// e^{i eps} by its Taylor series, for |eps| < 1/4: the first omitted terms are
+// eps^14 / 14! (cosine) and eps^13 / 13! (sine), below 1e-19 at 1/4.
 // the RK4 weights' divisions by 6 as products with 1 / 6 (a last-bit difference)
 constexpr double kSixth = 1. / 6.;
 __device__ __forceinline__ C2 expi_small(double e) {
@@ -181,6 +201,22 @@ __device__ __forceinline__ C2 expi_small(double e) {
   sn = fma(z, sn, 1.);
   return {c, sn * e};
 }
+// The same for |eps| < 1/16, the usual case (the remainder is the phase slip of the
+// particle's energy and angle offsets over a stage, ~1e-2 rad at 3 sigma of the
+// benchmark beam): the first omitted terms, eps^10 / 10! and eps^11 / 11!, are below
+// 2.6e-19. Ten FP64 instructions instead of thirteen.
+__device__ __forceinline__ C2 expi_tiny(double e) {
+  const double z = e * e;
+  double c = fma(z, 1. / 40320., -1. / 720.);
+  c = fma(z, c, 1. / 24.);
+  c = fma(z, c, -0.5);
+  c = fma(z, c, 1.);
+  double sn = fma(z, 1. / 362880., -1. / 5040.);
+  sn = fma(z, sn, 1. / 120.);
+  sn = fma(z, sn, -1. / 6.);
+  sn = fma(z, sn, 1.);
+  return {c, sn * e};
+}
 
 // (cos, sin) of h theta for a phase theta = theta0 + dth near theta0 + dnom: the
 // particle's e^{i h theta0} rotated by e^{i h dnom} (brot: their product, formed once
@@ -188,7 +224,8 @@ __device__ __forceinline__ C2 expi_small(double e) {
 // remainder is not small.
 __device__ __forceinline__ C2 rotated(C2 brot, double h, double theta, double dth, double dnom) {
   const double e = h * (dth - dnom);
-  if (fabs(e) <= kRotMax) return cmul_fma(brot, expi_small(e));
+  if (below_pow2(e, 1023 - 4)) return cmul_fma(brot, expi_tiny(e));
+  if (below_pow2(e, 1023 - 2)) return cmul_fma(brot, expi_small(e));
   double sn, c;
   sincos(h * theta, &sn, &c);
   return {c, sn};
@@ -456,21 +493,21 @@ __global__ void __launch_bounds__(128) k_adi_x(const double2 *__restrict__ field
   const double2 *s = src ? src + (size_t)ii * ncell + (size_t)iy * ng : nullptr;
   double2 *w = tmp + (size_t)i * ncell + (size_t)iy * ng;
   bool hp = iy > 0, hn = iy < ng - 1;
-  C2 cs = {0.0, cstep};
   C2 prev = {0, 0};
   for (int k = 0; k < ng; k++) {
     C2 uc = ld(u + k);
     C2 un = hn ? ld(u + k + ng) : C2{0, 0};
     C2 us = hp ? ld(u + k - ng) : C2{0, 0};
     C2 sv = s ? ld(s + k) : C2{0, 0};
-    C2 r = cadd(cadd(sv, uc), cmul_fma(cs, lap(hp, hn, us, uc, un)));
-    C2 v = (k == 0) ? cmul_fma(r, ld(cf.cbet)) : cmul_fma(csub(r, cmul_fma(ld(cf.c + k), prev)), ld(cf.cbet + k));
+    C2 r = add_imul(cadd(sv, uc), cstep, lap(hp, hn, us, uc, un));
+    // r - c[k] u_{k-1} with c[k] = (0, -mlow[k]); c[0] = 0
+    C2 v = (k == 0) ? cmul_fma(r, ld(cf.cbet)) : cmul_fma(add_imul(r, -cf.c[k].y, prev), ld(cf.cbet + k));
     st(w + k, v);
     prev = v;
   }
   C2 next = prev;
   for (int k = ng - 2; k >= 0; k--) {
-    C2 v = csub(ld(w + k), cmul_fma(ld(cf.cwet + k + 1), next));
+    C2 v = sub_cmul(ld(w + k), ld(cf.cwet + k + 1), next);
     st(w + k, v);
     next = v;
   }
@@ -491,7 +528,6 @@ __global__ void __launch_bounds__(128) k_adi_y(double2 *__restrict__ field,
   const double2 *s = src ? src + (size_t)ii * ncell + ix : nullptr;
   const double2 *w = tmp + (size_t)i * ncell + ix;
   bool hp = ix > 0, hn = ix < ng - 1;
-  C2 cs = {0.0, cstep};
   C2 prev = {0, 0};
   for (int k = 0; k < ng; k++) {
     size_t o = (size_t)k * ng;
@@ -499,15 +535,15 @@ __global__ void __launch_bounds__(128) k_adi_y(double2 *__restrict__ field,
     C2 wn = hn ? ld(w + o + 1) : C2{0, 0};
     C2 wp = hp ? ld(w + o - 1) : C2{0, 0};
     C2 sv = s ? ld(s + o) : C2{0, 0};
-    C2 r = cadd(cadd(sv, wc), cmul_fma(cs, lap(hp, hn, wp, wc, wn)));
-    C2 v = (k == 0) ? cmul_fma(r, ld(cf.cbet)) : cmul_fma(csub(r, cmul_fma(ld(cf.c + k), prev)), ld(cf.cbet + k));
+    C2 r = add_imul(cadd(sv, wc), cstep, lap(hp, hn, wp, wc, wn));
+    C2 v = (k == 0) ? cmul_fma(r, ld(cf.cbet)) : cmul_fma(add_imul(r, -cf.c[k].y, prev), ld(cf.cbet + k));
     st(u + o, v);
     prev = v;
   }
   C2 next = prev;
   for (int k = ng - 2; k >= 0; k--) {
     size_t o = (size_t)k * ng;
-    C2 v = csub(ld(u + o), cmul_fma(ld(cf.cwet + k + 1), next));
+    C2 v = sub_cmul(ld(u + o), ld(cf.cwet + k + 1), next);
     st(u + o, v);
     next = v;
   }

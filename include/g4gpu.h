@@ -392,7 +392,9 @@ int g4gpu_set_graph_mode(g4gpu_handle h, int on);
  * kernel, and the fused field kernel itself (0: one CTA per slice, 1: a cluster of
  * two CTAs per slice, each holding half the rows, 2: the whole step of a slice in
  * one CTA, push, deposition and ADI, for one-field windows without space charge;
- * steps it does not apply to run kernel 0). Choices are cached per
+ * steps it does not apply to run kernel 0). Grids too large for one CTA (ngrid > 168)
+ * run on the smallest cluster of 2 to 4 CTAs whose bands of rows fit shared memory
+ * (up to ngrid 333), beyond that on the tiled two-pass ADI. Choices are cached per
  * (precision, npart, ngrid, nfield, solver) for the life of the process. Requires
  * the lattice, beam and fields to be loaded. *push_block, *field_threads and
  * *field_kernel (each may be NULL) receive the choice. No reference counterpart. */

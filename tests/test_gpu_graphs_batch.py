@@ -126,13 +126,13 @@ def test_batch_of_uneven_runs_matches_single_runs(lib):
         assert np.max(np.abs(bd[:, 24] - bd0[:, 24])) < 1e-4
 
 
-@pytest.mark.parametrize("ng", [51, 151, 201])
+@pytest.mark.parametrize("ng", [51, 151, 201, 255])
 def test_cluster_pair_field_kernel_matches_single_cta(lib, ng):
-    """The mixed form's field step on a cluster of two CTAs per slice (rows split,
-    deposition and column solves across the pair through distributed shared memory)
-    against the one-CTA-per-slice kernel (ngrid <= 168) or the tiled two-pass ADI
-    (ngrid 201, which the pair replaces by default): a lasing window over whole
-    undulator steps with slippage."""
+    """The mixed form's field step on a cluster of CTAs per slice (rows split into
+    bands, column solves across the bands through distributed shared memory): a pair
+    against the one-CTA-per-slice kernel (ngrid <= 168), and the pair (ngrid 201) or a
+    cluster of three (ngrid 255), the default for grids too large for one CTA, against
+    the FP64 form: a lasing window over whole undulator steps with slippage."""
     import g4gpu
     import g4cases as T
     ns, npart = 24, 1024
@@ -181,7 +181,7 @@ def test_ensemble_members_match_oracle(lib, oracle):
     """Members shaped like the uneven ensemble's draws, run as one batch in the mixed
     form (captured graphs, launch shapes from the autotuner), each against the FP64
     oracle (bit-exact with the reference): linear aw tapers over four modules, ngrid
-    201 (cluster-pair field kernel) and 255 (tiled two-pass ADI), npart 2048 and 16384,
+    201 (cluster-pair field kernel) and 255 (a cluster of three), npart 2048 and 16384,
     a 1 kW seed over shot noise, periodic windows (at 2.26 slices of slippage per step
     a zero-filled window of a few slices would be emptied within two steps). Slice
     power within 1 % of the largest slice power, bunching within 1 % of the largest

@@ -258,11 +258,12 @@ def test_mixed_full_slices_with_split_beamlets_match_plain(lib, nbins, split):
     assert bunching_ok(bm[:, 24], bp[:, 24])
 
 
-@pytest.mark.parametrize("ng", [181, 255])
+@pytest.mark.parametrize("ng", [181, 255, 331, 341])
 def test_mixed_large_grid_close_to_oracle(lib, oracle, ng):
-    """Mixed form on grids too large for the fused kernel (tiled two-pass ADI, FP32):
-    slice power and bunching within 1 % of the FP64 oracle after 12 steps with a
-    seeded field."""
+    """Mixed form on grids too large for one CTA's shared memory: the one-pass step on
+    clusters of 2 (ngrid 181), 3 (255) and 4 (331) CTAs per slice, each holding a band
+    of rows, and the tiled two-pass ADI beyond them (341): slice power and bunching
+    within 1 % of the FP64 oracle after 12 steps with a seeded field."""
     import g4gpu
     import g4cases as T
     ns, npart, gm, g0 = 8, 512, 1e-4, 17081.0
@@ -278,6 +279,10 @@ def test_mixed_large_grid_close_to_oracle(lib, oracle, ng):
         h.load_field(0, fld)
         h.run(0, lat.shape[0])
         bd, fd = h.diag(1)
+        # the one-pass kernels are accounted as the first ADI pass alone; the tiled
+        # path runs both passes
+        two_pass = h.kernel_stats()["adi_y"][0] > 0
+    assert two_pass == (ng > 333), ng
     p, f, ofirst, _ = oracle.run_steps(lat, g0, beam, cur, 1e-10, 1.0, [1], [gm], fld[None], [0], time_run=1,
                                        nthreads=8)
     ob = oracle.diag_beam(p, 1)
