@@ -616,7 +616,8 @@ def harmonic_fft_form(g4gpu, torch, steps, warmup, peak, nsub=256, ns=None):
 
 
 def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_slices=64, max_coarse=63,
-                 check_every=8, tol=0.01, gamma0=GAMMA0, seed_power=0.0, time_run=1, shotnoise=1):
+                 check_every=8, tol=0.01, gamma0=GAMMA0, seed_power=0.0, time_run=1, shotnoise=1,
+                 substeps=True):
     """The coarse-step closure on the full window. Training data: fine (one-period)
     runs of a train_slices-slice window of the same beam over seeds 100..100+nseeds-1
     for the first max_coarse coarse steps (4 periods each), mixed form; the network
@@ -624,7 +625,10 @@ def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_s
     trained with Adam on the GPU. Timed: `steps` coarse steps with the closure after
     `warmup`, with the fine solve judging every check_every coarse steps (fallback
     above tol relative slice-power error). Throughput counts the fine slice-steps
-    the coarse steps cover. Error: against the plain FP64 fine run."""
+    the coarse steps cover. Error: against the plain FP64 fine run. substeps: a
+    coarse step pushes once over its 4 periods, then deposits and slips period by
+    period from interpolated phases, then diffracts once (g4gpu_set_field_substeps);
+    else it is one whole step of 4 periods."""
     import learned
     dev = torch.cuda.current_device()
     waist, u0, c0 = 30e-6, 1.0, 1.0
@@ -640,7 +644,7 @@ def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_s
     X, Tg, clat, fs, fc = learned.generate_training_data(
         dict(base, nslice=train_slices), lat, range(100, 100 + nseeds), sp, NPART, 4,
         np.repeat(slice_field[None, :], train_slices, axis=0), waist, u0, c0, max_coarse=max_coarse,
-        shotnoise=shotnoise)
+        shotnoise=shotnoise, substeps=substeps)
     t_gen = time.perf_counter() - t0
     fine_slice_steps = int(nseeds * train_slices * int(fs[max_coarse - 1] + fc[max_coarse - 1]))
     t0 = time.perf_counter()
@@ -648,7 +652,8 @@ def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_s
     curve = m.train(X, Tg, epochs=8, batch=512, lr=1e-3, seed=0)
     t_train = time.perf_counter() - t0
     fld = np.repeat(slice_field[None, :], NS, axis=0)
-    hf, hc = learned.make_pair(dict(base, nslice=NS), lat, clat, beam, cur, fld, m, waist, u0, c0)
+    hf, hc = learned.make_pair(dict(base, nslice=NS), lat, clat, beam, cur, fld, m, waist, u0, c0,
+                               fc if substeps else None)
     hc.run_learned(hf, 0, warmup, fs, fc, check_every=check_every, tol=tol)
     hc.synchronize()
     hf.synchronize()
@@ -675,6 +680,8 @@ def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_s
         bp, fp = hp.diag(1)
     with g4gpu.Handle(g4gpu.Config(**dict(base, nslice=NS))) as hcn:
         hcn.set_lattice(clat)
+        if substeps:
+            hcn.set_field_substeps(fc)
         hcn.load_beam(beam, cur)
         hcn.load_field(0, fld)
         hcn.run(0, warmup + steps)
@@ -690,6 +697,9 @@ def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_s
                                                  "absolute terms against the shot-noise level "
                                                  "1/sqrt(npart) of the beam"),
             "coarse_without_closure_error_vs_plain": diag_error(bn, fn, bp, fp),
+            "coarse_step": ("push over 4 periods; per period the deposition from interpolated phases and "
+                            "positions and the slippage; one diffraction over 4 periods" if substeps
+                            else "one whole step of 4 periods (push, field solve and slippage)"),
             "beam": f"gamma0 {gamma0}, 4096 slices x {NPART} particles, the config-0 lattice, "
                     + (f"{seed_power:g} W Gaussian seed (waist 30 um) in every slice, " if seed_power > 0
                        else "no seed, ")
@@ -1004,15 +1014,15 @@ def main():
     if "learned" in args.forms:
         line["forms"]["learned"] = learned_form(g4gpu, torch, lat, beam, cur, args.steps, args.warmup)
         # the same closure in steady state (config 0: quiet loading, 1 kW seed, no
-        # slippage), 4096 independent slices: there 4-period steps are physically valid.
-        # In a time-dependent window sampled every wavelength they are not: one coarse step
-        # slips the field 4 slices at once, so each slice's source adds coherently over 4
-        # periods (about 4x the fine run's power, in the oracle as on the GPU), which no
-        # per-slice correction represents, and the judge rejects the coarse steps.
+        # slippage), 4096 independent slices, with whole 4-period steps: valid there. In
+        # the time-dependent window above a whole coarse step would slip the field 4
+        # slices at once and add each slice's source coherently over 4 periods (about 4x
+        # the fine run's power, in the oracle as on the GPU); its coarse steps therefore
+        # push once and deposit and slip period by period.
         beam_q = g4gpu.host_load_beam(sp, 0, NPART, 4, 7, 0, LAMBDA0, 1.0)
         line["forms"]["learned_steady_state"] = learned_form(g4gpu, torch, lat, beam_q, cur, args.steps,
                                                              args.warmup, seed_power=1e3, time_run=0,
-                                                             shotnoise=0)
+                                                             shotnoise=0, substeps=False)
         del beam_q
     if rank == 0 and not args.no_e2e:
         field_pinned = torch.zeros((NS, NGRID * NGRID, 2), dtype=torch.float64).pin_memory()

@@ -394,7 +394,7 @@ void g4gpu_destroy(g4gpu_handle h) {
                   h->closure_basis, h->closure_feat, h->closure_corr, h->sc.st, h->sc.state, h->sc.ez,
                   h->wake_tab, h->wake_loss, h->wake_lossf, h->wake_scratch, h->count_buf, h->sort_iscratch,
                   h->sort_scratch[0], h->sort_scratch[1], h->sort_scratch[2], h->sort_scratch[3],
-                  h->sort_scratch[4], h->sort_scratch[5], h->isr_ctr};
+                  h->sort_scratch[4], h->sort_scratch[5], h->isr_ctr, h->sub_theta, h->sub_x, h->sub_y};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
@@ -422,6 +422,7 @@ int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *tab) {
   int ng = c.ngrid;
   h->steps.assign(nsteps, StepConst{});
   h->slip.assign(nsteps, 0.0);
+  h->substeps.clear();
   typedef std::complex<double> cd;
   std::map<std::pair<int, double>, int> sets;  // (field, delz) -> set
   std::vector<cd> coefs;                       // [nset][3][ng]
@@ -626,6 +627,34 @@ int g4gpu_set_incoherent(g4gpu_handle h, int seed, int do_loss, int do_spread, i
   h->isr_spread = do_spread != 0;
   h->isr_seed = (unsigned)seed;
   h->isr_nbins = nbins;
+  for (auto &g : h->graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+  h->graphs.clear();
+  h->graph_gen++;
+  return G4GPU_OK;
+}
+
+int g4gpu_set_field_substeps(g4gpu_handle h, int nsteps, const int *counts) {
+  if (!h) return fail(nullptr, G4GPU_ERR_ARG, "null handle");
+  if (nsteps != h->nsteps || (nsteps > 0 && !counts))
+    return fail(h, G4GPU_ERR_ARG, "the sub-step counts need one entry per lattice step");
+  const g4gpu_config &c = h->cfg;
+  bool any = false;
+  for (int i = 0; i < nsteps; i++) any = any || counts[i] > 1;
+  if (any && !(h->mixed && c.nfield == 1 && c.solver == G4GPU_SOLVER_ADI && c.ngrid <= g4::fused_max_ngrid() &&
+               c.npart % 4 == 0 && !h->beam.count && !h->sc_on))
+    return fail(h, G4GPU_ERR_ARG,
+                "coarse steps need the mixed form, one field, the ADI solver, ngrid <= 168, npart a multiple "
+                "of 4, full slices and no space charge");
+  cudaSetDevice(c.device);
+  const size_t n = (size_t)c.nslice * c.npart;
+  if (any && !h->sub_theta) {
+    int rc = alloc(h, &h->sub_theta, n * 8);
+    if (!rc) rc = alloc(h, &h->sub_x, n * 4);
+    if (!rc) rc = alloc(h, &h->sub_y, n * 4);
+    if (rc) return rc;
+  }
+  h->substeps.assign(counts, counts + nsteps);
   for (auto &g : h->graphs)
     if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
   h->graphs.clear();
@@ -1073,6 +1102,52 @@ int g4gpu_apply_slippage(g4gpu_handle h, int ifld, double slippage) {
   return apply_slippage(h, ifld, slippage);
 }
 
+// A coarse step of g4gpu_set_field_substeps: the push over the whole step, c source
+// sub-steps with their slippage, and the diffraction over the whole step.
+static int enqueue_coarse_step(g4gpu_handle h, int istep, int cnt) {
+  const g4gpu_config &c = h->cfg;
+  const int ns = c.nslice, np = c.npart, ng = c.ngrid;
+  g4::Launch L{h->stream, h->derr};
+  StepConst sc = h->steps[istep];
+  sc.f[0].first = h->first[0];
+  g4::StepConstF scf = g4::to_float(sc, np);
+  const size_t n = (size_t)ns * np;
+  // the phases and positions at the start of the push
+  G4_CUDA(h, cudaMemcpyAsync(h->sub_theta, h->beam.theta, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+  G4_CUDA(h, cudaMemcpyAsync(h->sub_x, h->beam.x, n * 4, cudaMemcpyDeviceToDevice, h->stream));
+  G4_CUDA(h, cudaMemcpyAsync(h->sub_y, h->beam.y, n * 4, cudaMemcpyDeviceToDevice, h->stream));
+  const void *wake = h->wake_on ? (const void *)h->wake_lossf : nullptr;
+  {
+    Timed t(h, G4GPU_K_PUSH);
+    g4::launch_push_mixed_sc(L, scf, h->beam, h->field, nullptr, ns, np, ng, 0, h->push_block, 0, nullptr, nullptr,
+                             wake, g4::IsrStream{});
+  }
+  // the sources of the c periods, each followed by its slippage
+  for (int j = 0; j < cnt; j++) {
+    scf.f[0].first = h->first[0];
+    {
+      Timed t(h, G4GPU_K_MISC);
+      if (sc.f[0].dep_on)
+        g4::launch_source_substep_mixed(L, scf, h->beam, h->sub_theta, h->sub_x, h->sub_y,
+                                        (float)(j + 1) / (float)cnt, 2.f / (float)cnt, h->field[0], ns, np, ng);
+    }
+    if (c.time_run) {
+      int rc = apply_slippage(h, 0, h->slip[istep] / cnt);
+      if (rc) return rc;
+    }
+  }
+  // the diffraction of the c periods: the ADI over the whole step without a source
+  scf.f[0].first = h->first[0];
+  const char *cb = (const char *)h->coef + (size_t)sc.f[0].coef * 3 * ng * h->csize;
+  {
+    Timed t(h, G4GPU_K_ADI_X);
+    g4::launch_field_fused_mixed(L, scf, 0, h->beam, h->field[0], cb, ns, np, ng, 0, h->field_threads, nullptr,
+                                 nullptr, 1, c.gammaref);
+  }
+  G4_CUDA(h, cudaGetLastError());
+  return G4GPU_OK;
+}
+
 static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
   const g4gpu_config &c = h->cfg;
   int ns = c.nslice, np = c.npart, ng = c.ngrid;
@@ -1082,6 +1157,15 @@ static int enqueue_steps(g4gpu_handle h, int istep0, int nsteps, int stages) {
   bool do_slip = (stages & G4GPU_STAGE_SLIP) && c.time_run;
   for (int istep = istep0; istep < istep0 + nsteps; istep++) {
     StepConst sc = h->steps[istep];
+    // a coarse step (g4gpu_set_field_substeps) with every stage; with space charge,
+    // one4one counts or incoherent radiation switched on since, the step runs whole
+    if (istep < (int)h->substeps.size() && h->substeps[istep] > 1 && do_push && do_field &&
+        (stages & G4GPU_STAGE_SLIP) && !sc.chic && !h->sc_on && !h->beam.count && !h->isr_loss &&
+        !h->isr_spread) {
+      int rc = enqueue_coarse_step(h, istep, h->substeps[istep]);
+      if (rc) return rc;
+      continue;
+    }
     for (int k = 0; k < c.nfield; k++) sc.f[k].first = h->first[k];
     // Incoherent::apply (Incoherent.cpp:31-63): the step's loss and spread of gamma, in
     // undulators

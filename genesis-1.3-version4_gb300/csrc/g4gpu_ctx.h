@@ -78,6 +78,10 @@ struct g4gpu_ctx {
   int nsteps = 0;
   std::vector<g4::StepConst> steps;
   std::vector<double> slip;
+  // g4gpu_set_field_substeps: periods per lattice step (empty: none), and the beam's
+  // phases and positions at the start of a coarse push
+  std::vector<int> substeps;
+  void *sub_theta = nullptr, *sub_x = nullptr, *sub_y = nullptr;
   int first[G4GPU_MAX_FIELDS] = {};
   double accuslip[G4GPU_MAX_FIELDS] = {};
   // sharded windows: the storage slot g4gpu_shift_out freed for the entering slice

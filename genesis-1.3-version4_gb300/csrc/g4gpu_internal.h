@@ -159,6 +159,13 @@ void launch_field_band_mixed(const Launch &L, const StepConstF &sc, int k, const
 void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, const DeviceBeam &b,
                               void *field, const void *coef, int ns, int np, int ngrid, int deposit,
                               int threads, double *dbeam, double *dfield, int nharm, double gref);
+// One source sub-step of a coarse step (g4gpu_set_field_substeps; k_source_f): the
+// deposition of every beam slice into field 0's slot (is + sc.f[0].first) % ns, u +=
+// scale * src, from phases and positions interpolated at frac between tp, xp, yp (the
+// beam before the push) and the beam's arrays. npart % 4 == 0, full slices.
+void launch_source_substep_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b, const void *tp,
+                                 const void *xp, const void *yp, float frac, float scale, void *field, int ns,
+                                 int np, int ngrid);
 // whether the fused kernel can record the diagnostics (nharm bunching harmonics) too
 bool fused_diag_fits(int ngrid, int threads, int nharm);
 // One ADI step of ns float2 field slices with an optional source, all scratch in the

@@ -601,9 +601,14 @@ __device__ __forceinline__ void thomas2(float2 *S, int stride, int ng, int up, c
 // alpha^W <= 2^-32. Each warm-up runs on values its neighbour has not yet overwritten
 // (a barrier separates it from the in-place pass). The first segment's forward pass
 // and the last segment's backward pass are the exact sweeps. Every thread of the
-// block must call it.
+// block must call it. With SUMS (a column solve: lstride 1, estride ng), the final pass
+// also sums the record terms of k_diag_field_f over the thread's solved elements into
+// fsum[kFieldSums] (power, its first and second moments in x and y, the field's sum):
+// the slice's diagnostics without another pass over it.
+template <bool SUMS = false>
 __device__ __forceinline__ void thomas_seg(float2 *S, int lstride, int estride, int ng, int nseg, int W,
-                                           const float2 *Cc, const float2 *CB, const float2 *CW) {
+                                           const float2 *Cc, const float2 *CB, const float2 *CW,
+                                           float *fsum = nullptr) {
   const int tid = threadIdx.x;
   const int line = tid % ng, seg = tid / ng;
   const int len = (ng + nseg - 1) / nseg;
@@ -635,6 +640,8 @@ __device__ __forceinline__ void thomas_seg(float2 *S, int lstride, int estride, 
     }
   }
   __syncthreads();
+  const float shift = -0.5f * (float)(ng - 1);
+  float sw = 0.f, swy = 0.f, swyy = 0.f, sre = 0.f, sim = 0.f;
   if (act)
     for (int k = e - 1; k >= b; k--) {
       float2 v = L[k * estride];
@@ -643,7 +650,25 @@ __device__ __forceinline__ void thomas_seg(float2 *S, int lstride, int estride, 
       }
       x = v;
       L[k * estride] = x;
+      if (SUMS) {
+        const float dy = (float)k + shift, wei = x.x * x.x + x.y * x.y;
+        sw += wei;
+        swy += dy * wei;
+        swyy += dy * dy * wei;
+        sre += x.x;
+        sim += x.y;
+      }
     }
+  if (SUMS) {
+    const float dx = act ? (float)line + shift : 0.f;
+    fsum[0] = sw;
+    fsum[1] = dx * sw;
+    fsum[2] = dx * dx * sw;
+    fsum[3] = swy;
+    fsum[4] = swyy;
+    fsum[5] = sre;
+    fsum[6] = sim;
+  }
   __syncthreads();
 }
 
@@ -917,6 +942,65 @@ __device__ __forceinline__ void deposit_quads(const StepConstF &sc, const FieldS
 }
 
 
+// One source sub-step of a coarse step (g4gpu_set_field_substeps): the deposition of
+// beam slice `is` (FieldSolverADI.cpp:19-51) added to its field storage slot
+// (is + first) % ns as the Crank-Nicolson step adds a source without diffraction, u +=
+// 2 src, with float atomics in global memory. Every particle's phase, x and y are
+// interpolated at `frac` of the coarse push, between the start (tp, xp, yp: copies
+// taken before the push) and the end (the beam's arrays): exact for the free drift
+// of the phase and the straight transverse path over a few periods. `scale` is 2 / c
+// for a coarse step of c periods (the step constants hold the whole step's dz). One
+// thread per four consecutive particles, grouped as deposit_quads groups them; needs
+// npart % 4 == 0 and full slices.
+__global__ void __launch_bounds__(128) k_source_f(StepConstF sc, PtrsF p, const long long *__restrict__ tp,
+                                                  const float *__restrict__ xp, const float *__restrict__ yp,
+                                                  float frac, float scale, float2 *field, int ns, int np,
+                                                  int ng) {
+  const int is = blockIdx.y;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (np >> 2)) return;
+  const FieldStepF &fs = sc.f[0];
+  const float scl = scale * fs.dep_scl * (float)p.current[is];
+  float2 *S = field + (size_t)((is + fs.first) % ns) * ng * ng;
+  const size_t base = (size_t)is * np;
+  const float4 x1 = reinterpret_cast<const float4 *>(p.x + base)[q];
+  const float4 y1 = reinterpret_cast<const float4 *>(p.y + base)[q];
+  const float4 x0 = reinterpret_cast<const float4 *>(xp + base)[q];
+  const float4 y0 = reinterpret_cast<const float4 *>(yp + base)[q];
+  const float4 g = reinterpret_cast<const float4 *>(p.dg + base)[q];
+  const longlong2 *T1 = reinterpret_cast<const longlong2 *>(p.theta + base);
+  const longlong2 *T0 = reinterpret_cast<const longlong2 *>(tp + base);
+  const longlong2 a01 = T1[2 * q], a23 = T1[2 * q + 1], b01 = T0[2 * q], b23 = T0[2 * q + 1];
+  // the phase advance over the coarse push is a few turns: (float)(t1 - t0) keeps it to
+  // ~1e-7 of itself, ~1e-6 rad
+  const long long t1[4] = {a01.x, a01.y, a23.x, a23.y}, t0[4] = {b01.x, b01.y, b23.x, b23.y};
+  long long th[4];
+#pragma unroll
+  for (int m = 0; m < 4; m++) th[m] = t0[m] + (long long)llrintf((float)(t1[m] - t0[m]) * frac);
+  const float x[4] = {fmaf(frac, x1.x - x0.x, x0.x), fmaf(frac, x1.y - x0.y, x0.y), fmaf(frac, x1.z - x0.z, x0.z),
+                      fmaf(frac, x1.w - x0.w, x0.w)};
+  const float y[4] = {fmaf(frac, y1.x - y0.x, y0.x), fmaf(frac, y1.y - y0.y, y0.y), fmaf(frac, y1.z - y0.z, y0.z),
+                      fmaf(frac, y1.w - y0.w, y0.w)};
+  const float dg[4] = {g.x, g.y, g.z, g.w};
+  const bool p01 = x[0] == x[1] && y[0] == y[1], p23 = x[2] == x[3] && y[2] == y[3];
+  if (p01 && p23 && x[0] == x[2] && y[0] == y[2]) {
+    deposit_group<4>(sc, fs, scl, S, ng, x[0], y[0], th, dg);
+    return;
+  }
+  if (p01) {
+    deposit_group<2>(sc, fs, scl, S, ng, x[0], y[0], th, dg);
+  } else {
+    deposit_one(sc, fs, scl, S, ng, x[0], y[0], th[0], dg[0]);
+    deposit_one(sc, fs, scl, S, ng, x[1], y[1], th[1], dg[1]);
+  }
+  if (p23) {
+    deposit_group<2>(sc, fs, scl, S, ng, x[2], y[2], th + 2, dg + 2);
+  } else {
+    deposit_one(sc, fs, scl, S, ng, x[2], y[2], th[2], dg[2]);
+    deposit_one(sc, fs, scl, S, ng, x[3], y[3], th[3], dg[3]);
+  }
+}
+
 // Bounded wait on an mbarrier phase; returns false (and raises the device error
 // flag) if the phase does not complete within the iteration limit.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err) {
@@ -1097,6 +1181,19 @@ __device__ __forceinline__ void slice_beam_sums(const PtrsF &p, double gref, int
   if (k < 10) o[kBeamSums + k] = (k >= 8 ? gref : 0.0) + res[NSUM + k];
 }
 
+// The field record o[kFieldSums + 2] of the slice S from every thread's partial sums c
+// (slice_field_sums, or the column sweep of thomas_seg<true>) and the on-axis value.
+__device__ __forceinline__ void finish_field_sums(const float2 *S, int ng, const float *c, double *sh, double *res,
+                                                  double *o) {
+  cta_reduce<kFieldSums, 0>(c, nullptr, nullptr, sh, res);
+  if (threadIdx.x < kFieldSums) o[threadIdx.x] = res[threadIdx.x];
+  if (threadIdx.x == 0) {
+    const float2 v = S[(ng / 2) * ng + ng / 2];
+    o[7] = v.x;
+    o[8] = v.y;
+  }
+}
+
 // Field sums of the slice S (ng x ng, in shared memory) into o[kFieldSums + 2]
 // (k_diag_field_f's record).
 __device__ __forceinline__ void slice_field_sums(const float2 *S, int ng, double *sh, double *res, double *o) {
@@ -1120,13 +1217,7 @@ __device__ __forceinline__ void slice_field_sums(const float2 *S, int ng, double
       row++;
     }
   }
-  cta_reduce<kFieldSums, 0>(c, nullptr, nullptr, sh, res);
-  if (threadIdx.x < kFieldSums) o[threadIdx.x] = res[threadIdx.x];
-  if (threadIdx.x == 0) {
-    const float2 v = S[(ng / 2) * ng + ng / 2];
-    o[7] = v.x;
-    o[8] = v.y;
-  }
+  finish_field_sums(S, ng, c, sh, res, o);
 }
 
 __global__ void __launch_bounds__(kFusedMaxThreads, 1)
@@ -1205,14 +1296,24 @@ __global__ void __launch_bounds__(kFusedMaxThreads, 1)
   // right-hand side needs neither a second deposition nor a stored S1
   r2_cols_seg(S, u, ng, cs, nseg);
   __syncthreads();
-  if (segmented)
+  // the field record's sums are formed by the segmented column sweep itself
+  float fsum[kFieldSums];
+  if (segmented && dfield)
+    thomas_seg<true>(S, 1, ng, ng, nseg, fs.tw, C, CB, CW, fsum);  // columns
+  else if (segmented)
     thomas_seg(S, 1, ng, ng, nseg, fs.tw, C, CB, CW);  // columns
   else if (line < ng)
     thomas2(S + line, ng, ng, up, CB, CW, a, invden, mask);
   __syncthreads();
   bulk_store(u, S, ncell);
-  // the field record of storage slice i, read from S alongside the store
-  if (dfield) slice_field_sums(S, ng, dsh, dres, dfield + (size_t)i * (kFieldSums + 2));
+  // the field record of storage slice i (from S alongside the store where the sweep
+  // did not form its sums)
+  if (dfield) {
+    if (segmented)
+      finish_field_sums(S, ng, fsum, dsh, dres, dfield + (size_t)i * (kFieldSums + 2));
+    else
+      slice_field_sums(S, ng, dsh, dres, dfield + (size_t)i * (kFieldSums + 2));
+  }
   if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
@@ -1341,13 +1442,21 @@ __global__ void __launch_bounds__(MAXT, 1)
   __syncthreads();
   r2_cols_seg(S, u, ng, cs, nseg);  // 2 u' - S1
   __syncthreads();
-  if (segmented)
+  float fsum[kFieldSums];
+  if (segmented && dfield)
+    thomas_seg<true>(S, 1, ng, ng, nseg, fs.tw, C, CB, CW, fsum);  // columns, with the record's sums
+  else if (segmented)
     thomas_seg(S, 1, ng, ng, nseg, fs.tw, C, CB, CW);  // columns
   else if (line < ng)
     thomas2(S + line, ng, ng, up, CB, CW, a, invden, mask);
   __syncthreads();
   bulk_store(u, S, ncell);
-  if (dfield) slice_field_sums(S, ng, dsh, dres, dfield + (size_t)i * (kFieldSums + 2));
+  if (dfield) {
+    if (segmented)
+      finish_field_sums(S, ng, fsum, dsh, dres, dfield + (size_t)i * (kFieldSums + 2));
+    else
+      slice_field_sums(S, ng, dsh, dres, dfield + (size_t)i * (kFieldSums + 2));
+  }
   if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
@@ -2235,6 +2344,16 @@ void launch_field_fused_mixed(const Launch &L, const StepConstF &sc, int k, cons
   PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
   k_field_fused_f<<<ns, threads, smem, (cudaStream_t)L.stream>>>(
       sc, k, p, (float2 *)field, (const float2 *)coef, ns, np, ngrid, deposit, L.err, dbeam, dfield, nharm, gref);
+}
+
+void launch_source_substep_mixed(const Launch &L, const StepConstF &sc, const DeviceBeam &b, const void *tp,
+                                 const void *xp, const void *yp, float frac, float scale, void *field, int ns,
+                                 int np, int ngrid) {
+  PtrsF p = make_ptrs_f(b, nullptr, nullptr, 0);
+  dim3 grid((np / 4 + 127) / 128, ns);
+  k_source_f<<<grid, 128, 0, (cudaStream_t)L.stream>>>(sc, p, (const long long *)tp, (const float *)xp,
+                                                        (const float *)yp, frac, scale, (float2 *)field, ns, np,
+                                                        ngrid);
 }
 
 // k_step_fused_f's particles per lane and round (their loads in flight together) by

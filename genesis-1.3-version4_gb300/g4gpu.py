@@ -66,6 +66,7 @@ ABI_SYMBOLS = [
     "g4gpu_mlp_get_params", "g4gpu_mlp_set_params", "g4gpu_mlp_set_normalization", "g4gpu_mlp_forward",
     "g4gpu_mlp_gradients", "g4gpu_mlp_train", "g4gpu_closure_attach", "g4gpu_closure_features",
     "g4gpu_closure_apply", "g4gpu_closure_targets", "g4gpu_copy_state", "g4gpu_run_learned",
+    "g4gpu_set_field_substeps",
     "g4gpu_adi_advance_noalloc", "g4gpu_set_launch_shapes",
 ]
 CLOSURE_NIN, CLOSURE_NOUT = 32, 4
@@ -177,6 +178,7 @@ def load_library(path=None):
     L.g4gpu_host_single_wakes.argtypes = [i, d, d, d, d, i, d, d, d, d, pd, pd, pd]
     L.g4gpu_set_wake.argtypes = [vp, i, d, pd, pd, pd, pd, d, d, i]
     L.g4gpu_set_chicanes.argtypes = [vp, i, pd]
+    L.g4gpu_set_field_substeps.argtypes = [vp, i, ctypes.POINTER(ctypes.c_int)]
     L.g4gpu_load_beam_counts.argtypes = [vp, vp, vp, P(i)]
     L.g4gpu_get_counts.argtypes = [vp, P(i)]
     L.g4gpu_sort.argtypes = [vp, P(i)]
@@ -520,6 +522,14 @@ class Handle:
 
     def device_bytes(self):
         return int(self.L.g4gpu_device_bytes(self.h))
+
+    def set_field_substeps(self, counts):
+        """Periods per lattice step (g4gpu_set_field_substeps): a step of c > 1 periods
+        pushes once over its length and deposits and slips period by period, then
+        diffracts once."""
+        cnt = np.ascontiguousarray(counts, dtype=np.int32).ravel()
+        self._check(self.L.g4gpu_set_field_substeps(self.h, int(cnt.size),
+                                                    cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
 
     def set_chicanes(self, table):
         """Chicanes of the lattice steps: [nsteps][4] angle, lb, ld, lt (zero angle: none)."""

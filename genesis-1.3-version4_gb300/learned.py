@@ -4,7 +4,14 @@ coarse-step run with the fine-step judge.
 The steps:
   1. coarsen_lattice(): merges runs of up to `factor` identical undulator steps
      (one period each) into one coarse step; other steps stay as they are. Returns
-     the coarse table and, per coarse step, the fine steps it covers.
+     the coarse table and, per coarse step, the fine steps it covers. With
+     `substeps`, the coarse handle runs a coarse step as a coarse push under the
+     fine source and slippage (g4gpu_set_field_substeps): the push over the whole
+     step, then period by period the deposition from interpolated phases and the
+     slippage, then the diffraction of the whole step. A time-dependent window
+     sampled every wavelength needs it: a whole coarse step would slip the field
+     `factor` slices at once and add each slice's source coherently over the
+     `factor` periods.
   2. generate_training_data(): for every seed, a window is integrated with fine
      steps; at every coarse step the state is copied to a second handle that takes
      the coarse step. The per-slice features of the starting state and the
@@ -48,13 +55,17 @@ def coarsen_lattice(fine, factor=4, cols=g4gpu.LAT_COLS):
     return np.array(rows), np.array(start, dtype=np.int32), np.array(count, dtype=np.int32)
 
 
-def make_pair(cfg_kwargs, fine_lat, coarse_lat, beam, current, field, mlp_for_targets, waist, u0, c0):
+def make_pair(cfg_kwargs, fine_lat, coarse_lat, beam, current, field, mlp_for_targets, waist, u0, c0,
+              counts=None):
     """A fine and a coarse handle on the same window (the coarse one with a closure
-    attached, which the target kernel needs for its buffers)."""
+    attached, which the target kernel needs for its buffers). counts: the periods of
+    every coarse step, for coarse pushes under the fine source and slippage."""
     hf = g4gpu.Handle(g4gpu.Config(**cfg_kwargs))
     hc = g4gpu.Handle(g4gpu.Config(**cfg_kwargs))
     hf.set_lattice(fine_lat)
     hc.set_lattice(coarse_lat)
+    if counts is not None:
+        hc.set_field_substeps(counts)
     for h in (hf, hc):
         h.load_beam(beam, current)
         h.load_field(0, field)
@@ -63,9 +74,10 @@ def make_pair(cfg_kwargs, fine_lat, coarse_lat, beam, current, field, mlp_for_ta
 
 
 def generate_training_data(cfg_kwargs, fine_lat, seeds, slice_params, npart, nbins, field, waist, u0, c0,
-                           factor=4, max_coarse=None, shotnoise=1):
+                           factor=4, max_coarse=None, shotnoise=1, substeps=False):
     """Features X [n][32] and targets T [n][4] from fine runs over `seeds` (the loading
-    seed of each run; shotnoise 0 loads quiet beams)."""
+    seed of each run; shotnoise 0 loads quiet beams); substeps: coarse pushes under the
+    fine source and slippage."""
     coarse_lat, fstart, fcount = coarsen_lattice(fine_lat, factor)
     ncoarse = coarse_lat.shape[0] if max_coarse is None else min(max_coarse, coarse_lat.shape[0])
     scratch = g4gpu.MLP()
@@ -74,7 +86,7 @@ def generate_training_data(cfg_kwargs, fine_lat, seeds, slice_params, npart, nbi
     for seed in seeds:
         beam = g4gpu.host_load_beam(slice_params, 0, npart, nbins, seed, shotnoise, lam, sample)
         hf, hc = make_pair(cfg_kwargs, fine_lat, coarse_lat, beam, slice_params[:, 16], field, scratch, waist,
-                           u0, c0)
+                           u0, c0, fcount if substeps else None)
         with hf, hc:
             for i in range(ncoarse):
                 X.append(hf.closure_features())
@@ -87,13 +99,14 @@ def generate_training_data(cfg_kwargs, fine_lat, seeds, slice_params, npart, nbi
 
 
 def evaluate(cfg_kwargs, fine_lat, coarse_lat, fstart, fcount, beam, current, field, mlp, waist, u0, c0,
-             ncoarse=None):
+             ncoarse=None, substeps=False):
     """Slice power and bunching after the same distance by (fine, coarse, coarse +
     closure). Returns dict of arrays."""
     ncoarse = coarse_lat.shape[0] if ncoarse is None else ncoarse
     nfine = int(fstart[ncoarse - 1] + fcount[ncoarse - 1])
+    counts = fcount if substeps else None
     out = {}
-    hf, hc = make_pair(cfg_kwargs, fine_lat, coarse_lat, beam, current, field, mlp, waist, u0, c0)
+    hf, hc = make_pair(cfg_kwargs, fine_lat, coarse_lat, beam, current, field, mlp, waist, u0, c0, counts)
     with hf, hc:
         hf.run(0, nfine)
         bd, fd = hf.diag(1)
@@ -102,7 +115,7 @@ def evaluate(cfg_kwargs, fine_lat, coarse_lat, fstart, fcount, beam, current, fi
         bd, fd = hc.diag(1)
         out["coarse"] = (fd[0][:, 0].copy(), bd[:, 24].copy())
     # coarse + closure through the driver, with no check inside the run
-    hf, hc = make_pair(cfg_kwargs, fine_lat, coarse_lat, beam, current, field, mlp, waist, u0, c0)
+    hf, hc = make_pair(cfg_kwargs, fine_lat, coarse_lat, beam, current, field, mlp, waist, u0, c0, counts)
     with hf, hc:
         hc.run_learned(hf, 0, ncoarse, fstart, fcount, check_every=10 ** 9, tol=1e9)
         bd, fd = hc.diag(1)

@@ -459,6 +459,30 @@ int g4gpu_closure_apply(g4gpu_handle h, const float *corr); /* [nslice][4] */
 int g4gpu_closure_targets(g4gpu_handle hc, g4gpu_handle hf, float *out);
 /* device copy of beam, fields and ring state between handles of the same shape */
 int g4gpu_copy_state(g4gpu_handle dst, g4gpu_handle src);
+/* Coarse pushes under a fine source and slippage, for the closure's coarse steps.
+ * counts[nsteps] (nsteps the lattice's): a lattice step i with counts[i] = c > 1 is a
+ * coarse step standing for c identical undulator periods of length dz/c (its dz and
+ * slippage are the c periods' sums, as a coarsened lattice table gives them). It runs:
+ *   1. the push of Beam::track over the whole dz (one RK4 step, BeamSolver.cpp:89-141);
+ *   2. c source sub-steps: the deposition of FieldSolverADI::advance for a period
+ *      (FieldSolverADI.cpp:19-51, scaled to dz/c), from every particle's phase and
+ *      position interpolated linearly between the start and the end of the push at
+ *      the end of period j, added to the field as the Crank-Nicolson step adds it
+ *      without diffraction (twice the source), each followed by Control::applySlippage
+ *      of dz/c (Control.cpp:158-276);
+ *   3. one FieldSolverADI::ADI step (FieldSolverADI.cpp:60-122) over dz with no source:
+ *      the diffraction of the c periods. The transverse diffraction acts alike on every
+ *      slice, so it commutes with the slippage; splitting it from the sources errs by
+ *      the diffraction of a source over c periods, (c dz / Rayleigh length) relative.
+ * So the pusher takes coarse steps while the source and the slippage keep the period's
+ * resolution: a time-dependent window sampled every wavelength keeps each slice's
+ * source spread over the c slices it slips across. Mixed form, one field, ADI solver,
+ * ngrid <= 168 (the fused field kernel), no space charge, full slices (npart a
+ * multiple of 4, no one4one counts); other handles are rejected with G4GPU_ERR_ARG.
+ * Steps with counts[i] <= 1, chicane steps and partial stages run as before. Calling
+ * it again replaces the counts; g4gpu_set_lattice clears them. No reference
+ * counterpart (the reference integrates every period, src/Core/Gencore.cpp:102-160). */
+int g4gpu_set_field_substeps(g4gpu_handle h, int nsteps, const int *counts);
 /* coarse steps istep0 .. istep0+ncoarse-1 of hc with the closure; every check_every
  * steps the fine handle hf integrates the same interval (fine steps fine_start[i],
  * fine_count[i]) from the same state; above tol relative slice-power error the fine

@@ -581,17 +581,20 @@ def test_pinned_host_buffers_round_trip_like_pageable(lib, prec):
         assert rel_err(ref_beam, part) < 1e-6 and rel_err(ref_field, fld[1]) < 1e-6
 
 
-@pytest.mark.parametrize("prec,nh", [(0, 3), (1, 2), (1, 3)])
-def test_run_diag_records_every_step_like_diag(lib, prec, nh):
+@pytest.mark.parametrize("prec,nh,npart,shapes", [(0, 3, 128, None), (1, 2, 128, None), (1, 3, 128, None),
+                                                  (1, 2, 1024, (128, 512, 0))])
+def test_run_diag_records_every_step_like_diag(lib, prec, nh, npart, shapes):
     """g4gpu_run_diag records after every step what g4gpu_diag gives after that step
     of g4gpu_run (time-dependent window with slippage, two fields). A second run gives
     the records to 1e-6 of each column's scale (the deposition's atomic adds make two
     runs differ in the last bits; phases of small amplitudes are not compared). The
-    mixed window (ngrid 25) takes the fused field kernel, which forms the records
-    itself for up to 2 harmonics: nharm 2 there, 3 (the separate kernels) as well."""
+    mixed window (ngrid 25) takes the fused field kernel, which forms the field
+    records itself for up to 2 harmonics (their sums in its column sweep): nharm 2
+    there, 3 (the separate kernels) as well, and a window of 1024 particles per slice
+    pushed in blocks of 128 threads."""
     import g4gpu
     import g4cases as T
-    ns, npart, ng = 8, 128, 25
+    ns, ng = 8, 25
     lat = T.undulator_lattice(1.7, 0.015, 5, 2, 1e-10, 11357.8, quad_k1=1.5, quad_l=0.08)
     part = g4gpu.host_load_beam(T.slice_params(ns, 11357.8, 1.0, 0.4e-6, 15.0), 0, npart, 4, 3, 1, 1e-10, 1.0)
     cur = np.full(ns, 3000.0)
@@ -607,6 +610,8 @@ def test_run_diag_records_every_step_like_diag(lib, prec, nh):
         h.load_beam(part, cur)
         h.load_field(0, fld[0])
         h.load_field(1, fld[1])
+        if shapes:
+            h.set_launch_shapes(*shapes)
         return h
 
     with handle() as h:
