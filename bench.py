@@ -878,6 +878,8 @@ def main():
                     help="skip the mixed form's error after the whole 443-step lattice and its resonant companion")
     ap.add_argument("--nslice", type=int, default=None,
                     help="slices of the window (default 4096); smaller values are for profiling only")
+    ap.add_argument("--ngrid", type=int, default=None,
+                    help="grid points of the window (default 151); other values are for profiling only")
     ap.add_argument("--forms", default="mixed,plain,batched,harmonic,learned,spacecharge",
                     help="forms to time besides the mixed headline: plain, batched, harmonic, learned, "
                          "spacecharge")
@@ -889,9 +891,11 @@ def main():
                     help="push_block,field_threads,field_kernel for the mixed form instead of autotuning "
                          "(for profiling captures without the tuner's trial launches)")
     args = ap.parse_args()
-    global NS
+    global NS, NGRID
     if args.nslice:
         NS = args.nslice
+    if args.ngrid:
+        NGRID = args.ngrid
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -948,8 +952,9 @@ def main():
 
     def kernel_table(st, mixed):
         # the mixed form's deposition + ADI runs as one fused kernel when the slice
-        # fits in shared memory; it is accounted under the adi_x class
-        fused = mixed and NGRID <= 168
+        # fits in shared memory, or in the shared memory of a cluster of up to four CTAs
+        # (ngrid <= 333); it is accounted under the adi_x class
+        fused = mixed and NGRID <= 333
         tot = max(sum(x[1] for x in st.values()), 1e-12)
         out = {}
         for k, (n, ms) in st.items():
