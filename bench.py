@@ -617,7 +617,7 @@ def harmonic_fft_form(g4gpu, torch, steps, warmup, peak, nsub=256, ns=None):
 
 def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_slices=64, max_coarse=63,
                  check_every=8, tol=0.01, gamma0=GAMMA0, seed_power=0.0, time_run=1, shotnoise=1,
-                 substeps=True):
+                 substeps=True, factor=4):
     """The coarse-step closure on the full window. Training data: fine (one-period)
     runs of a train_slices-slice window of the same beam over seeds 100..100+nseeds-1
     for the first max_coarse coarse steps (4 periods each), mixed form; the network
@@ -628,7 +628,7 @@ def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_s
     the coarse steps cover. Error: against the plain FP64 fine run. substeps: a
     coarse step pushes once over its 4 periods, then deposits and slips period by
     period from interpolated phases, then diffracts once (g4gpu_set_field_substeps);
-    else it is one whole step of 4 periods."""
+    else it is one whole step of 4 periods. factor: the periods of a coarse step."""
     import learned
     dev = torch.cuda.current_device()
     waist, u0, c0 = 30e-6, 1.0, 1.0
@@ -643,8 +643,8 @@ def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_s
     t0 = time.perf_counter()
     X, Tg, clat, fs, fc = learned.generate_training_data(
         dict(base, nslice=train_slices), lat, range(100, 100 + nseeds), sp, NPART, 4,
-        np.repeat(slice_field[None, :], train_slices, axis=0), waist, u0, c0, max_coarse=max_coarse,
-        shotnoise=shotnoise, substeps=substeps)
+        np.repeat(slice_field[None, :], train_slices, axis=0), waist, u0, c0, factor=factor,
+        max_coarse=max_coarse, shotnoise=shotnoise, substeps=substeps)
     t_gen = time.perf_counter() - t0
     fine_slice_steps = int(nseeds * train_slices * int(fs[max_coarse - 1] + fc[max_coarse - 1]))
     t0 = time.perf_counter()
@@ -697,9 +697,9 @@ def learned_form(g4gpu, torch, lat, beam, cur, steps, warmup, nseeds=64, train_s
                                                  "absolute terms against the shot-noise level "
                                                  "1/sqrt(npart) of the beam"),
             "coarse_without_closure_error_vs_plain": diag_error(bn, fn, bp, fp),
-            "coarse_step": ("push over 4 periods; per period the deposition from interpolated phases and "
-                            "positions and the slippage; one diffraction over 4 periods" if substeps
-                            else "one whole step of 4 periods (push, field solve and slippage)"),
+            "coarse_step": (f"push over {factor} periods; per period the deposition from interpolated phases "
+                            f"and positions and the slippage; one diffraction over {factor} periods" if substeps
+                            else f"one whole step of {factor} periods (push, field solve and slippage)"),
             "beam": f"gamma0 {gamma0}, 4096 slices x {NPART} particles, the config-0 lattice, "
                     + (f"{seed_power:g} W Gaussian seed (waist 30 um) in every slice, " if seed_power > 0
                        else "no seed, ")
