@@ -1744,13 +1744,25 @@ int g4gpu_run_diag(g4gpu_handle h, int istep0, int nsteps, int nharm, double *be
   std::vector<int> firsts((size_t)nsteps * G4GPU_MAX_FIELDS);
   // each step's record is copied back as soon as it is formed and finished on the host
   // while the device runs the later steps
+  // the records are copied on a stream of their own, so that a copy over the host link
+  // runs beside the next step instead of in front of it (each step's record has its own
+  // slot of ddiag)
   struct Events {
     std::vector<cudaEvent_t> ev;
+    cudaEvent_t formed = nullptr;
+    cudaStream_t copy = nullptr;
     ~Events() {
       for (cudaEvent_t e : ev) cudaEventDestroy(e);
+      if (formed) cudaEventDestroy(formed);
+      if (copy) {
+        cudaStreamSynchronize(copy);
+        cudaStreamDestroy(copy);
+      }
     }
   } done;
   done.ev.reserve(nsteps);
+  G4_CUDA(h, cudaStreamCreateWithFlags(&done.copy, cudaStreamNonBlocking));
+  G4_CUDA(h, cudaEventCreateWithFlags(&done.formed, cudaEventDisableTiming));
   for (int s = 0; s < nsteps; s++) {
     // the fused field kernel forms the fields' record during the step where it can
     // (the slice is in its shared memory); the beam's, and the fields' elsewhere, come
@@ -1767,12 +1779,14 @@ int g4gpu_run_diag(g4gpu_handle h, int istep0, int nsteps, int nharm, double *be
     enqueue_diag(h, nharm, h->ddiag + (size_t)s * rec, beam_out != nullptr && !beam_done,
                  field_out != nullptr && !fields_done);
     G4_CUDA(h, cudaGetLastError());
+    G4_CUDA(h, cudaEventRecord(done.formed, h->stream));
+    G4_CUDA(h, cudaStreamWaitEvent(done.copy, done.formed, 0));
     G4_CUDA(h, cudaMemcpyAsync(h->hdiag + (size_t)s * rec, h->ddiag + (size_t)s * rec, rec * sizeof(double),
-                               cudaMemcpyDeviceToHost, h->stream));
+                               cudaMemcpyDeviceToHost, done.copy));
     cudaEvent_t e;
     G4_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     done.ev.push_back(e);
-    G4_CUDA(h, cudaEventRecord(e, h->stream));
+    G4_CUDA(h, cudaEventRecord(e, done.copy));
   }
   const size_t bstride = (size_t)c.nslice * (G4GPU_DB_NCOL + 2 * nharm);
   const size_t fstride = (size_t)c.nfield * c.nslice * G4GPU_DF_NCOL;
