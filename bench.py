@@ -194,7 +194,7 @@ def job_value(ws, slices_per_rank, steps, ms_max):
 # (profiles/ncu_full_k_push_f_k_field_fused_f_sase608.md); the traffic of these kernels
 # grows in proportion to the slices of a launch, so a full launch's is the per-slice
 # figure times the slices.
-TRAFFIC_PER_SLICE = {"field": 448487.0, "push": 432237.0}
+TRAFFIC_PER_SLICE = {"field": 447986.0, "push": 431960.0}
 TRAFFIC_SOURCE = "ncu capture of a 608-slice window, scaled to the launch's slices"
 # FP64 instructions (DFMA + DMUL + DADD, thread level) per particle of the plain push and
 # per cell of each plain ADI sweep, from ncu captures of a 152-slice window
