@@ -267,17 +267,31 @@ def kernel_alg_bytes(kernel, mixed, ns=None):
     return ns * per
 
 
+def far_field_spectrum(fd):
+    """The window's spectrum as the reference's post-processing forms it
+    (examples/Example3-TimeDependent/Example3.py:129-136): |FFT over the slices of
+    sqrt(I_ff) exp(i phi_ff)|^2, from each slice's far-field intensity and phase
+    (a field record [nslice][cols] in window order)."""
+    import g4gpu
+    i_ff = fd[:, g4gpu.DF_COLS.index("intensity-farfield")]
+    phi = fd[:, g4gpu.DF_COLS.index("phase-farfield")]
+    return np.abs(np.fft.fftshift(np.fft.fft(np.sqrt(np.maximum(i_ff, 0.0)) * np.exp(1j * phi)))) ** 2
+
+
 def mixed_error(hm, hp, after_steps):
     """The mixed handle's slice power and bunching against the plain FP64 handle's
     (both at the same step): the largest slice-power difference over the largest
-    slice power, the window energy, the largest bunching difference over the largest
+    slice power, the largest difference of the window's spectrum over its largest
+    value, the window energy, the largest bunching difference over the largest
     bunching and absolute. The absolute bunching floor that matters is the shot-noise
     level of the beam, 1/sqrt(npart) = 0.011 for 8192 particles."""
     bm, fm = hm.diag(1)
     bp, fp = hp.diag(1)
     pw_m, pw_p = fm[0][:, 0], fp[0][:, 0]
     db = float(np.max(np.abs(bm[:, 24] - bp[:, 24])))
+    sm, sp = far_field_spectrum(fm[0]), far_field_spectrum(fp[0])
     return {"power_max_rel": float(np.max(np.abs(pw_m - pw_p)) / max(np.max(np.abs(pw_p)), 1e-300)),
+            "spectrum_max_rel": float(np.max(np.abs(sm - sp)) / max(np.max(sp), 1e-300)),
             "energy_rel": float(abs(pw_m.sum() / pw_p.sum() - 1)) if pw_p.sum() > 0 else None,
             "bunching_max_rel": db / max(float(np.max(np.abs(bp[:, 24]))), 1e-300),
             "bunching_max_abs": db, "bunching_floor_1_over_sqrt_npart": 1.0 / np.sqrt(NPART),
@@ -322,6 +336,7 @@ def resonant_companion(g4gpu, torch, shapes):
     e0 = out["modules"][0]["window_energy_plain"]
     out["energy_growth_module1_to_end"] = out["modules"][-1]["window_energy_plain"] / max(e0, 1e-300)
     out["power_max_rel"] = max(m["power_max_rel"] for m in out["modules"])
+    out["spectrum_max_rel"] = max(m["spectrum_max_rel"] for m in out["modules"])
     out["bunching_max_rel"] = max(m["bunching_max_rel"] for m in out["modules"])
     return out
 
@@ -456,13 +471,16 @@ def ensemble_member(r, ns, npart, ngrid, taper, g4gpu):
 
 
 def diag_error(b, f, b0, f0):
-    """Slice-power error relative to the largest slice power, and bunching error
+    """Slice-power error relative to the largest slice power, the window spectrum's
+    error relative to its largest value (far_field_spectrum), and bunching error
     relative to the largest bunching and absolute (bunching |<exp(i theta)>| lies in
     [0, 1]; near the shot-noise level of a quiet beam only the absolute error means
     anything), of (b, f) against (b0, f0)."""
     p, p0 = f[0][:, 0], f0[0][:, 0]
     db = float(np.max(np.abs(b[:, 24] - b0[:, 24])))
+    s, s0 = far_field_spectrum(f[0]), far_field_spectrum(f0[0])
     return {"power_max_rel": float(np.max(np.abs(p - p0)) / max(np.max(np.abs(p0)), 1e-300)),
+            "spectrum_max_rel": float(np.max(np.abs(s - s0)) / max(np.max(s0), 1e-300)),
             "bunching_max_rel": db / max(float(np.max(np.abs(b0[:, 24]))), 1e-300),
             "bunching_max_abs": db}
 
@@ -528,6 +546,7 @@ def batched_form(g4gpu, torch, steps, warmup, peak, nrun=ENSEMBLE_RUNS, nerr=4):
                               "frac": achieved / peak},
             "error_vs_plain": {"runs": errs, "after_steps": warmup + steps,
                                "power_max_rel": max(e["power_max_rel"] for e in errs),
+                               "spectrum_max_rel": max(e["spectrum_max_rel"] for e in errs),
                                "bunching_max_rel": max(e["bunching_max_rel"] for e in errs)}}
 
 
@@ -602,16 +621,18 @@ def harmonic_fft_form(g4gpu, torch, steps, warmup, peak, nsub=256, ns=None):
         out["fft_roofline"] = {"bound": "hbm", "alg_bytes_per_cell": 24, "design_bytes_per_cell": 56,
                                "achieved_gbs": a, "peak": peak, "frac": a / peak,
                                "ms_per_field_solve": fft_ms / (steps * len(HARM_H))}
-    pw = {}
+    pw, spec = {}, {}
     for k, hk in enumerate(HARM_H):
         a, b = fm[k][:nsub, 0], fp[k][:, 0]
         pw[f"h{hk}"] = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+        sa, sb = far_field_spectrum(fm[k][:nsub]), far_field_spectrum(fp[k])
+        spec[f"h{hk}"] = float(np.max(np.abs(sa - sb)) / max(np.max(sb), 1e-300))
     bun = {}
     for j in range(nh):
         a, b = bm[:nsub, 24 + 2 * j], bp[:, 24 + 2 * j]
         bun[f"h{j + 1}"] = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
     out["error_vs_plain"] = {"slices": nsub, "after_steps": warmup + steps, "power_max_rel": pw,
-                             "bunching_max_rel": bun}
+                             "spectrum_max_rel": spec, "bunching_max_rel": bun}
     return out
 
 
