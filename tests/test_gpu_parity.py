@@ -752,8 +752,8 @@ def test_lasing_time_dependent_window_matches_oracle(lib, oracle, prec):
     an absolute 1e-3, below the shot-noise level 1/sqrt(2048) = 0.022). The window energy
     grows 60-fold and the bunching from 0.02 to 0.15 over the run (exponential gain in
     the last 220 steps). The spectrum formed from every slice's far-field intensity and
-    phase, as the reference's examples form it, agrees within 1e-8 (plain) and 2 %
-    (mixed) of its largest value.
+    phase, as the reference's examples form it, agrees within 1e-8 (plain; measured up to
+    1.1e-10) and 1 % (mixed; measured up to 1.7e-3) of its largest value.
 
     The plain bunching bound: the push rounds 1/beta_par as the reference does, but its
     argument can differ from the reference's in the last bit (fused products, the
@@ -797,6 +797,7 @@ def test_lasing_time_dependent_window_matches_oracle(lib, oracle, prec):
             # Example3.py:129-136), against its largest value
             spec, ospec = far_field_spectrum(fd[0]), far_field_spectrum(of)
             spec_err = np.max(np.abs(spec - ospec)) / np.max(ospec)
+            print(f"step {e}: spectrum error {spec_err:.3e}")
             if prec == 0:
                 assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-9, e
                 assert rel_err(bd[:, 24], ob[:, 24]) < 5e-9, e
@@ -804,5 +805,5 @@ def test_lasing_time_dependent_window_matches_oracle(lib, oracle, prec):
             else:
                 assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-2, e
                 assert np.max(np.abs(bd[:, 24] - ob[:, 24])) <= 1e-2 * np.max(ob[:, 24]) + 1e-3, e
-                assert spec_err < 2e-2, (e, spec_err)
+                assert spec_err < 1e-2, (e, spec_err)
     assert energies[-1] > 30 * energies[0] and bunch[-1] > 0.1, (energies, bunch)
