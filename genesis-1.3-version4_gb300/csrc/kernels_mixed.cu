@@ -236,6 +236,13 @@ struct PtrsF {
   IsrStream isr;
 };
 
+// the field storage slot (is + first) % ns of beam slice is, for is and first in
+// [0, ns): a compare instead of an integer division per thread
+__device__ __forceinline__ int ring_slot(int is, int first, int ns) {
+  const int t = is + first;
+  return t >= ns ? t - ns : t;
+}
+
 // particles of slice is: np, or the slice's own count
 __device__ __forceinline__ int slice_np_f(const PtrsF &p, int is, int np) {
   return p.count ? min(p.count[is], np) : np;
@@ -400,7 +407,7 @@ __global__ void __launch_bounds__(512) k_push_f(StepConstF sc, PtrsF p, int ns, 
   const float ez = (p.ez ? p.ez[o] : 0.f) + (p.eloss ? (float)p.eloss[is] : 0.f);
   const float2 *fslice[NF];
 #pragma unroll
-  for (int k = 0; k < NF; k++) fslice[k] = k < sc.nfld ? p.field[k] + (size_t)((is + sc.f[k].first) % ns) * ncell
+  for (int k = 0; k < NF; k++) fslice[k] = k < sc.nfld ? p.field[k] + (size_t)ring_slot(is, sc.f[k].first, ns) * ncell
                                                        : nullptr;
   push_rest_f<NF>(sc, p, fslice, is, ip, ng, ez, dg, th, x, y, px, py);
   const float g = g0 + dg;
@@ -961,7 +968,7 @@ __global__ void __launch_bounds__(128) k_source_f(StepConstF sc, PtrsF p, const 
   if (q >= (np >> 2)) return;
   const FieldStepF &fs = sc.f[0];
   const float scl = scale * fs.dep_scl * (float)p.current[is];
-  float2 *S = field + (size_t)((is + fs.first) % ns) * ng * ng;
+  float2 *S = field + (size_t)ring_slot(is, fs.first, ns) * ng * ng;
   const size_t base = (size_t)is * np;
   const float4 x1 = reinterpret_cast<const float4 *>(p.x + base)[q];
   const float4 y1 = reinterpret_cast<const float4 *>(p.y + base)[q];
