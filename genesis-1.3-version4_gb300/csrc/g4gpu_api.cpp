@@ -519,6 +519,9 @@ int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *tab) {
     s.xku = r[G4GPU_LAT_KU];
     if (s.xku == 0) s.xku = xks * 0.5 / gamma0 / gamma0;  // BeamSolver.cpp:34-38
     s.ztemp1 = -2. / s.xks;
+    s.half_delz = s.delz * 0.5;
+    s.aw_t2 = s.aw_t * s.aw_t;
+    s.aw2 = s.aw * s.aw;
     {
       // dtheta/dz of the ODE (BeamSolver.cpp:144-163) at gammaref, on axis, no field
       const double bpar = std::sqrt(1. - (1. + aw * aw) / (gamma0 * gamma0));

@@ -57,6 +57,9 @@ struct StepConst {
   double delz;
   double gammaref;
   double ztemp1;      // -2 / xks (BeamSolver.cpp:147), the same value the ODE computes
+  // exact products of the step's constants the FP64 push would otherwise form per
+  // particle: delz / 2, aw_t^2, aw^2 (each the same IEEE product on the host)
+  double half_delz, aw_t2, aw2;
   // nominal phase advance over half a step and over the step: delz / 2 and delz times
   // dtheta/dz of a particle at gammaref on axis without field (BeamSolver.cpp:144-163)
   double dnom_half, dnom_full;

@@ -93,10 +93,10 @@ __device__ __forceinline__ void transverse(const StepConst &sc, bool last, doubl
     y = sc.cm[4] * tmp + sc.cm[5] * py / gz;
     py = sc.cm[6] * tmp * gz + sc.cm[7] * py;
   }
-  double delz = sc.delz * 0.5;
+  const double delz = sc.half_delz;
   // 1 / gammaz by one reciprocal square root, gammaz (the quadrupoles' only) as
   // gammaz^2 / gammaz; both within an ulp or two of the reference's sqrt and quotients
-  const double gz2 = fma(-py, py, fma(-px, px, fma(g, g, -1.) - sc.aw_t * sc.aw_t));
+  const double gz2 = fma(-py, py, fma(-px, px, fma(g, g, -1.) - sc.aw_t2));
   const double igz = rsqrt(gz2);
   const double gammaz = gz2 * igz;
   plane_step(sc.kindx, sc.qx, sc.xoff, delz, x, px, gammaz, igz);
@@ -164,7 +164,11 @@ __device__ __forceinline__ double recip_near(double x, double r) {
 // reference computes it, so that xks (1 - 1/btpar0), which xks ~ 1e11 amplifies, is
 // the reference's value; a last-bit change of 1 / tgam changes btper0 / tgam^2 ~ 1e-8
 // far below the last bit of btpar0); ztemp1 = -2 / xks comes with the step constants.
-template <int NF>
+// ACC: how the stage's derivative f enters the RK4 accumulators k2: 0 k2 = f (the first
+// two stages, where the reference adds f to zero), 1 k2 = -k2 / 2 + f and 2 k2 = 2 k2 + f
+// (the third and fourth, where the reference scales k2 by -0.5 or 2 first): each one
+// fma, exact as the reference's product (a scaling by a power of two) and rounded sum.
+template <int NF, int ACC>
 __device__ __forceinline__ void ode(const StepConst &sc, const C2 *rpart, const C2 *cs, double btpar, double ez,
                                     double itg, double &k2gg, double &k2pp) {
   // sum of rpart_i conj(cs_i), products fused into the sums
@@ -178,8 +182,15 @@ __device__ __forceinline__ void ode(const StepConst &sc, const C2 *rpart, const 
   double btper0 = fma(sc.ztemp1, ctmp.x, btpar);
   double btpar0 = sqrt(fma(-btper0, itg * itg, 1.));
   const double ib = 1. / btpar0;
-  k2pp += fma(sc.xks, 1. - ib, sc.xku);
-  k2gg += fma(ctmp.y * ib, itg, -ez);
+  const double fpp = fma(sc.xks, 1. - ib, sc.xku), fgg = fma(ctmp.y * ib, itg, -ez);
+  if (ACC == 0) {
+    k2pp = fpp;
+    k2gg = fgg;
+  } else {
+    const double scale = ACC == 1 ? -0.5 : 2.0;
+    k2pp = fma(scale, k2pp, fpp);
+    k2gg = fma(scale, k2gg, fgg);
+  }
 }
 
 // e^{i eps} by its Taylor series, for |eps| < 1/4: the first omitted terms are
@@ -343,7 +354,7 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   double gamma = g, theta = th + sc.autophase;
   double dx = x - sc.ax, dy = y - sc.ay;
   const double awloc = fma(sc.grady, dy, fma(sc.gradx, dx, fma(0.5, fma(sc.ky * dy, dy, sc.kx * dx * dx), 1.)));
-  const double btpar = fma(sc.aw * sc.aw * awloc, awloc, fma(py, py, fma(px, px, 1.)));
+  const double btpar = fma(sc.aw2 * awloc, awloc, fma(py, py, fma(px, px, 1.)));
   C2 rpart[NF];
 #pragma unroll
   for (int k = 0; k < NF; k++) {
@@ -388,38 +399,32 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   };
 
   // BeamSolver::RungeKutta, BeamSolver.cpp:89-141
-  double k2gg = 0, k2pp = 0, k3gg, k3pp;
+  double k2gg, k2pp, k3gg, k3pp;
   double itg = 1. / gamma;  // 1 / gamma of the stage, each stage's from the previous one
-  ode<NF>(sc, rpart, cs, btpar, ez, itg, k2gg, k2pp);
-  double stpz = 0.5 * sc.delz;
+  ode<NF, 0>(sc, rpart, cs, btpar, ez, itg, k2gg, k2pp);
+  double stpz = sc.half_delz;
   gamma = fma(stpz, k2gg, gamma);
   theta = fma(stpz, k2pp, theta);
   k3gg = k2gg;
   k3pp = k2pp;
-  k2gg = 0;
-  k2pp = 0;
   stage(bhalf, sc.dnom_half);
   itg = recip_near(gamma, itg);
-  ode<NF>(sc, rpart, cs, btpar, ez, itg, k2gg, k2pp);
+  ode<NF, 0>(sc, rpart, cs, btpar, ez, itg, k2gg, k2pp);
   gamma = fma(stpz, k2gg - k3gg, gamma);
   theta = fma(stpz, k2pp - k3pp, theta);
   k3gg *= kSixth;
   k3pp *= kSixth;
-  k2gg *= -0.5;
-  k2pp *= -0.5;
   stage(bhalf, sc.dnom_half);
   itg = recip_near(gamma, itg);
-  ode<NF>(sc, rpart, cs, btpar, ez, itg, k2gg, k2pp);
+  ode<NF, 1>(sc, rpart, cs, btpar, ez, itg, k2gg, k2pp);  // k2 = -k2 / 2 + f
   stpz = sc.delz;
   gamma = fma(stpz, k2gg, gamma);
   theta = fma(stpz, k2pp, theta);
   k3gg -= k2gg;
   k3pp -= k2pp;
-  k2gg *= 2;
-  k2pp *= 2;
   stage(bfull, sc.dnom_full);
   itg = recip_near(gamma, itg);
-  ode<NF>(sc, rpart, cs, btpar, ez, itg, k2gg, k2pp);
+  ode<NF, 2>(sc, rpart, cs, btpar, ez, itg, k2gg, k2pp);  // k2 = 2 k2 + f
   gamma = fma(stpz, fma(k2gg, kSixth, k3gg), gamma);
   theta = fma(stpz, fma(k2pp, kSixth, k3pp), theta);
 
