@@ -517,7 +517,7 @@ int g4gpu_run_learned(g4gpu_handle hc, g4gpu_handle hf, int istep0, int ncoarse,
  * gives the message. Any nslice: slices are taken in turns by at most one CTA per
  * SM, each with one scratch slot of ngrid^2 complex floats.
  * The first call on a device looks up the array's device address and sets the
- * kernel's shared-memory limit; make that first call before any stream capture.
+ * kernel's shared-memory limit.
  * Every call on a device shares the one array, which keeps the last call's
  * contents (the call clears its error flag and rewrites its coefficients, and every
  * slot is written before it is read): calls that overlap on the GPU, from two host
