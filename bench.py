@@ -200,7 +200,7 @@ TRAFFIC_SOURCE = "ncu capture of a 608-slice window, scaled to the launch's slic
 # per cell of each plain ADI sweep, from ncu captures of a 152-slice window
 # (profiles/ncu_fp64_k_push_k_adi_plain_sase152.md); nominal GB300 FP64 rate: 1.25 TFLOP/s
 # with FMA counted as two operations, i.e. 625 G FP64 instructions/s.
-FP64_INSTR = {"push_per_particle": 463.1, "adi_per_cell": 17.9}
+FP64_INSTR = {"push_per_particle": 458.1, "adi_per_cell": 17.9}
 FP64_NOMINAL_GINSTR = 625.0
 
 
@@ -736,7 +736,7 @@ E2E_WINDOWS = 11       # timed windows of K steps
 E2E_RUNS = 5           # timed whole-lattice runs
 
 
-def e2e_window(g4gpu, torch, precision, beam_pinned, cur, field_pinned, lat, steps, reps, shapes=None):
+def e2e_window(g4gpu, torch, precision, beam_pinned, cur, field_pinned, lat, steps, reps, outs, shapes=None):
     """Track windows through the ABI with host buffers: upload, `steps` steps with the
     per-slice diagnostics of every step (recorded on the device, each step's record
     read back while the later steps run), download of beam and field. One warm-up
@@ -749,8 +749,7 @@ def e2e_window(g4gpu, torch, precision, beam_pinned, cur, field_pinned, lat, ste
     h.set_lattice(lat)
     if shapes is not None:  # the launch shapes of the headline form (its autotuner's)
         h.set_launch_shapes(*shapes)
-    out_beam = torch.empty_like(beam_pinned).pin_memory()
-    out_field = torch.empty_like(field_pinned).pin_memory()
+    out_beam, out_field = outs
     cur_np = np.ascontiguousarray(cur)
     diag_out = (np.zeros((steps, NS, len(g4gpu.DB_COLS) + 2)), np.zeros((steps, 1, NS, len(g4gpu.DF_COLS))))
     times = []
@@ -930,6 +929,11 @@ def main():
     beam_pinned = torch.empty((NS, NPART, 6), dtype=torch.float64).pin_memory()
     beam = beam_pinned.numpy()
     g4gpu.host_load_beam(sp, 0, NPART, 4, 7, 1, LAMBDA0, 1.0, out=beam)
+    # the end-to-end windows' host buffers, pinned once at start-up as an application
+    # allocates its I/O buffers
+    if rank == 0 and not args.no_e2e:
+        field_pinned = torch.zeros((NS, NGRID * NGRID, 2), dtype=torch.float64).pin_memory()
+        e2e_out = (torch.empty_like(beam_pinned).pin_memory(), torch.empty_like(field_pinned).pin_memory())
 
     peak, peak_kind = measured_peaks()
     sampler = ClockSampler(local)
@@ -943,6 +947,29 @@ def main():
     barrier(ws)
     clocks = sampler.stop()
     ms_m = max_over_ranks(ws, ms_m)
+    # end to end through the ABI, right after the headline: in the process state of a
+    # single run, before the comparison runs and the other forms allocate and free their
+    # handles and host buffers (after them, the same copies ran up to six times slower)
+    e2e_res = {}
+    if rank == 0 and not args.no_e2e:
+        nrun = min(args.e2e_steps or lat.shape[0], lat.shape[0])
+        for key, steps, reps, what in (
+                ("e2e", nrun, E2E_RUNS, f"one whole run: upload beam+field, all {nrun} steps of the lattice with "
+                                        "every step's diagnostics (g4gpu_run_diag), download"),
+                ("e2e_short_window", args.steps, E2E_WINDOWS,
+                 f"upload beam+field, {args.steps} steps with every step's diagnostics (g4gpu_run_diag), "
+                 "download")):
+            times, h2d, d2h, phases = e2e_window(g4gpu, torch, g4gpu.MIXED, beam_pinned, cur, field_pinned, lat,
+                                                 steps, reps, e2e_out, shapes=shapes)
+            t = statistics.median(times)
+            e2e_res[key] = {"value": NS * steps / t, "unit": "slice-steps/s",
+                            "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
+                            "steps_per_window": steps,
+                            "window": what + f"; median of {len(times)} windows after one warm-up window",
+                            "window_s": t, "windows_s": times,
+                            "spread": (max(times) - min(times)) / t,
+                            "phases_of_one_window": phases}
+        del e2e_out, field_pinned
     # plain FP64 form, same initial state and steps
     psteps = args.plain_steps if args.plain_steps is not None else args.steps
     do_plain = "plain" in args.forms
@@ -1026,6 +1053,7 @@ def main():
                          "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                          "alg_bytes_per_launch": dk.get("alg_bytes"), "ms_per_launch": dk["ms_avg"]},
             "kernels": kernels, "gpu_launches": launches, "clocks": clocks}
+    line.update(e2e_res)
 
     if "batched" in args.forms:
         line["forms"]["batched"] = batched_form(g4gpu, torch, args.steps, args.warmup, peak)
@@ -1050,25 +1078,6 @@ def main():
                                                              args.warmup, seed_power=1e3, time_run=0,
                                                              shotnoise=0, substeps=False)
         del beam_q
-    if rank == 0 and not args.no_e2e:
-        field_pinned = torch.zeros((NS, NGRID * NGRID, 2), dtype=torch.float64).pin_memory()
-        nrun = min(args.e2e_steps or lat.shape[0], lat.shape[0])
-        for key, steps, reps, what in (
-                ("e2e", nrun, E2E_RUNS, f"one whole run: upload beam+field, all {nrun} steps of the lattice with "
-                                        "every step's diagnostics (g4gpu_run_diag), download"),
-                ("e2e_short_window", args.steps, E2E_WINDOWS,
-                 f"upload beam+field, {args.steps} steps with every step's diagnostics (g4gpu_run_diag), "
-                 "download")):
-            times, h2d, d2h, phases = e2e_window(g4gpu, torch, g4gpu.MIXED, beam_pinned, cur, field_pinned, lat,
-                                                 steps, reps, shapes=shapes)
-            t = statistics.median(times)
-            line[key] = {"value": NS * steps / t, "unit": "slice-steps/s",
-                         "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
-                         "steps_per_window": steps,
-                         "window": what + f"; median of {len(times)} windows after one warm-up window",
-                         "window_s": t, "windows_s": times,
-                         "spread": (max(times) - min(times)) / t,
-                         "phases_of_one_window": phases}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1)
     if rank == 0:

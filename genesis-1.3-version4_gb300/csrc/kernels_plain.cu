@@ -158,11 +158,44 @@ __device__ __forceinline__ double recip_near(double x, double r) {
   return fma(r, e, r);
 }
 
+// 1 / sqrt(a) as the correctly rounded quotient of 1 by the correctly rounded square
+// root (BeamSolver::ODE's btpar0 = sqrt(...), 1 / btpar0), without the square root and
+// the division when a = 1 - d, |d| < 2^-14 (btpar0 is 1 - O(1 / gamma^2)):
+//  - s0 = 1 - d/2 - d^2/8 - d^3/16 (Taylor series of sqrt(1 - d); the omitted terms
+//    are below 2^-60) is within an ulp of sqrt(a). Tuckerman's rounding test picks
+//    RN(sqrt(a)) among s0 and its neighbours: with u = next(s0) - s0, sqrt(a) lies above
+//    s0 + u/2 iff a > s0 next(s0), the sign of fma(s0, next(s0), -a) (exact: a and
+//    s0 next(s0) are multiples of a spacing above u^2 / 4), and the same below.
+//  - q0 = 1 + e + e^2 + e^3 for e = 1 - s (exact) is within an ulp of 1 / s. The residual
+//    1 - s q0 is exact, and q0 is RN(1 / s) iff it is smaller in magnitude than s g / 2,
+//    g the spacing of the doubles on its side of q0 (2^-52 in [1, 2), 2^-53 below 1);
+//    1 / s is never a midpoint, as s is a double.
+// Both tests run on the integer pipe but the three residuals. Bit-identical to
+// 1. / sqrt(a) (checked against IEEE sqrt and division on 1.5e8 arguments either side
+// of 1); outside the range, sqrt and the division.
+__device__ __forceinline__ double recip_sqrt_near1(double a) {
+  const double d = 1. - a;
+  if (!below_pow2(d, 1023 - 14)) return 1. / sqrt(a);
+  double s = fma(d, fma(d, fma(d, -1. / 16., -1. / 8.), -0.5), 1.);
+  const long long sb = __double_as_longlong(s);
+  const double su = __longlong_as_double(sb + 1), sd = __longlong_as_double(sb - 1);
+  if (__double2hiint(fma(s, su, -a)) < 0) s = su;
+  else if (__double2hiint(fma(s, sd, -a)) >= 0) s = sd;
+  const double e = 1. - s;
+  double q = 1. + fma(fma(e, e, e), e, e);
+  const long long qb = __double_as_longlong(q), rb = __double_as_longlong(fma(-s, q, 1.));
+  const bool up = rb > 0;  // 1 / s > q
+  const bool wide = up ? qb >= 0x3FF0000000000000LL : qb > 0x3FF0000000000000LL;
+  const long long hb = __double_as_longlong(s) - ((wide ? 53LL : 54LL) << 52);  // s g / 2
+  if ((rb & 0x7fffffffffffffffLL) > hb) q = __longlong_as_double(qb + (up ? 1 : -1));
+  return q;
+}
+
 // BeamSolver::ODE (BeamSolver.cpp:144-163) for NF fields, given cs[i] = (cos, sin) of
 // rharm_i * tthet and itg = 1 / tgam. Two of the reference's four divisions become
-// products with the reciprocals 1 / tgam and 1 / btpar0 (the latter computed as the
-// reference computes it, so that xks (1 - 1/btpar0), which xks ~ 1e11 amplifies, is
-// the reference's value; a last-bit change of 1 / tgam changes btper0 / tgam^2 ~ 1e-8
+// products with the reciprocals 1 / tgam and 1 / btpar0 (the latter rounded as the
+// reference's sqrt and quotient round it, by recip_sqrt_near1, so that xks (1 - 1/btpar0),
+// which xks ~ 1e11 amplifies, is the reference's value; a last-bit change of 1 / tgam changes btper0 / tgam^2 ~ 1e-8
 // far below the last bit of btpar0); ztemp1 = -2 / xks comes with the step constants.
 // ACC: how the stage's derivative f enters the RK4 accumulators k2: 0 k2 = f (the first
 // two stages, where the reference adds f to zero), 1 k2 = -k2 / 2 + f and 2 k2 = 2 k2 + f
@@ -180,8 +213,7 @@ __device__ __forceinline__ void ode(const StepConst &sc, const C2 *rpart, const 
     ctmp.y = fma(rpart[i].y, cs[i].x, fma(-rpart[i].x, cs[i].y, ctmp.y));
   }
   double btper0 = fma(sc.ztemp1, ctmp.x, btpar);
-  double btpar0 = sqrt(fma(-btper0, itg * itg, 1.));
-  const double ib = 1. / btpar0;
+  const double ib = recip_sqrt_near1(fma(-btper0, itg * itg, 1.));
   const double fpp = fma(sc.xks, 1. - ib, sc.xku), fgg = fma(ctmp.y * ib, itg, -ez);
   if (ACC == 0) {
     k2pp = fpp;
