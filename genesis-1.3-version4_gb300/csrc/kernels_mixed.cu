@@ -908,11 +908,54 @@ __device__ __forceinline__ void deposit_group(const StepConstF &sc, const FieldS
   atomicAdd(&S[c.i11].y, w11 * cpy);
 }
 
+// Four particles that lie in one cell without sharing x and y exactly: a beamlet's
+// mirrored members once their energies, and with them their transverse steps, differ in
+// the last bits. Each particle's own weights and phasor are summed in registers, then
+// one set of eight atomics (exact up to FP32 summation order). Returns false, having
+// deposited nothing, unless all four lie inside the grid in the same cell.
+__device__ __forceinline__ bool deposit_cell4(const StepConstF &sc, const FieldStepF &fs, float scl, float2 *S,
+                                              int ng, const float *x, const float *y, const long long *th,
+                                              const float *dgam) {
+  CellF c;
+  if (!ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x[0], y[0], c)) return false;
+#pragma unroll
+  for (int m = 1; m < 4; m++) {
+    CellF cm;
+    if (!ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x[m], y[m], cm) || cm.i00 != c.i00) return false;
+  }
+  float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int m = 0; m < 4; m++) {
+    CellF cm;
+    ll_gridpoint_f(fs.gridmax, fs.dgrid, ng, x[m], y[m], cm);
+    const float dx = x[m] - sc.ax, dy = y[m] - sc.ay;
+    const float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
+    const float part = sqrtf(faw2) * scl / ((float)sc.gammaref + dgam[m]);
+    float sn, co;
+    __sincosf(phase_of(th[m], (unsigned)fs.harm), &sn, &co);
+    const float cpx = sn * part, cpy = co * part;
+    const float w00 = cm.wx * cm.wy, w10 = (1.f - cm.wx) * cm.wy, w01 = cm.wx * (1.f - cm.wy),
+                w11 = (1.f - cm.wx) * (1.f - cm.wy);
+    v[0] += w00 * cpx; v[1] += w00 * cpy; v[2] += w10 * cpx; v[3] += w10 * cpy;
+    v[4] += w01 * cpx; v[5] += w01 * cpy; v[6] += w11 * cpx; v[7] += w11 * cpy;
+  }
+  atomicAdd(&S[c.i00].x, v[0]);
+  atomicAdd(&S[c.i00].y, v[1]);
+  atomicAdd(&S[c.i10].x, v[2]);
+  atomicAdd(&S[c.i10].y, v[3]);
+  atomicAdd(&S[c.i01].x, v[4]);
+  atomicAdd(&S[c.i01].y, v[5]);
+  atomicAdd(&S[c.i11].x, v[6]);
+  atomicAdd(&S[c.i11].y, v[7]);
+  return true;
+}
+
 // Adds the deposited source of beam slice `is` to S with one thread per four
 // consecutive particles. Quiet loading stores the nbins mirrored members of a
 // beamlet consecutively (nbins a multiple of 4 gives aligned groups of four sharing
 // x and y; nbins = 2, pairs): a group that shares x and y is deposited once with the
-// sum of its members' phasors, pairs likewise, anything else particle by particle.
+// sum of its members' phasors, a group in one cell with the sum of its members' weighted
+// phasors, pairs that share x and y like the first, anything else particle by particle.
 // No warp-level exchange is needed, and the loads are 16-byte vectors. Needs
 // npart % 4 == 0.
 __device__ __forceinline__ void deposit_quads(const StepConstF &sc, const FieldStepF &fs, const PtrsF &p,
@@ -929,9 +972,10 @@ __device__ __forceinline__ void deposit_quads(const StepConstF &sc, const FieldS
     const long long th[4] = {t01.x, t01.y, t23.x, t23.y};
     const float dg[4] = {g.x, g.y, g.z, g.w};
     const bool p01 = x.x == x.y && y.x == y.y, p23 = x.z == x.w && y.z == y.w;
+    const float xs[4] = {x.x, x.y, x.z, x.w}, ys[4] = {y.x, y.y, y.z, y.w};
     if (p01 && p23 && x.x == x.z && y.x == y.z) {
       deposit_group<4>(sc, fs, scl, S, ng, x.x, y.x, th, dg);
-    } else {
+    } else if (!deposit_cell4(sc, fs, scl, S, ng, xs, ys, th, dg)) {
       if (p01) {
         deposit_group<2>(sc, fs, scl, S, ng, x.x, y.x, th, dg);
       } else {
@@ -994,6 +1038,7 @@ __global__ void __launch_bounds__(128) k_source_f(StepConstF sc, PtrsF p, const 
     deposit_group<4>(sc, fs, scl, S, ng, x[0], y[0], th, dg);
     return;
   }
+  if (deposit_cell4(sc, fs, scl, S, ng, x, y, th, dg)) return;
   if (p01) {
     deposit_group<2>(sc, fs, scl, S, ng, x[0], y[0], th, dg);
   } else {
