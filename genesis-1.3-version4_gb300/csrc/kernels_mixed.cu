@@ -1975,6 +1975,43 @@ __device__ __forceinline__ void pair_group(const StepConstF &sc, const FieldStep
   pair_add(S, r0, nrow, ng, c.ix, c.iy1, c.wx * (1.f - c.wy), cpx, cpy);
   pair_add(S, r0, nrow, ng, c.ix1, c.iy1, (1.f - c.wx) * (1.f - c.wy), cpx, cpy);
 }
+// Four particles in one cell that do not share x and y exactly (deposit_cell4's case),
+// into the rows [r0, r0 + nrow) of a band: each particle's weighted phasor summed in
+// registers, then one atomic pair per corner in the band. Returns false, having
+// deposited nothing, unless all four lie inside the grid in the same cell.
+__device__ __forceinline__ bool pair_cell4(const StepConstF &sc, const FieldStepF &fs, float scl, float2 *S,
+                                           int r0, int nrow, int ng, const float *x, const float *y,
+                                           const long long *th, const float *dgam) {
+  CellRC c;
+  if (!cell_rc(fs.gridmax, fs.dgrid, ng, x[0], y[0], c)) return false;
+#pragma unroll
+  for (int m = 1; m < 4; m++) {
+    CellRC cm;
+    if (!cell_rc(fs.gridmax, fs.dgrid, ng, x[m], y[m], cm) || cm.ix != c.ix || cm.iy != c.iy) return false;
+  }
+  if (c.iy1 < r0 || c.iy >= r0 + nrow) return true;  // the four particles' rows are another band's
+  float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int m = 0; m < 4; m++) {
+    CellRC cm;
+    cell_rc(fs.gridmax, fs.dgrid, ng, x[m], y[m], cm);
+    const float dx = x[m] - sc.ax, dy = y[m] - sc.ay;
+    const float faw2 = 1.f + sc.kx * dx * dx + sc.ky * dy * dy + 2.f * (sc.gradx * dx + sc.grady * dy);
+    const float part = sqrtf(faw2) * scl / ((float)sc.gammaref + dgam[m]);
+    float sn, co;
+    __sincosf(phase_of(th[m], (unsigned)fs.harm), &sn, &co);
+    const float cpx = sn * part, cpy = co * part;
+    const float w00 = cm.wx * cm.wy, w10 = (1.f - cm.wx) * cm.wy, w01 = cm.wx * (1.f - cm.wy),
+                w11 = (1.f - cm.wx) * (1.f - cm.wy);
+    v[0] += w00 * cpx; v[1] += w00 * cpy; v[2] += w10 * cpx; v[3] += w10 * cpy;
+    v[4] += w01 * cpx; v[5] += w01 * cpy; v[6] += w11 * cpx; v[7] += w11 * cpy;
+  }
+  pair_add(S, r0, nrow, ng, c.ix, c.iy, 1.f, v[0], v[1]);
+  pair_add(S, r0, nrow, ng, c.ix1, c.iy, 1.f, v[2], v[3]);
+  pair_add(S, r0, nrow, ng, c.ix, c.iy1, 1.f, v[4], v[5]);
+  pair_add(S, r0, nrow, ng, c.ix1, c.iy1, 1.f, v[6], v[7]);
+  return true;
+}
 // A cluster's deposition: each CTA reads every particle of the slice and deposits the
 // contributions to its own rows into its own band, with shared-memory atomics only. A
 // particle whose footprint straddles two bands is deposited by both, each into its
@@ -1997,9 +2034,10 @@ __device__ __forceinline__ void deposit_pair(const StepConstF &sc, const FieldSt
       const long long th[4] = {t01.x, t01.y, t23.x, t23.y};
       const float dg[4] = {gg.x, gg.y, gg.z, gg.w};
       const bool p01 = x.x == x.y && y.x == y.y, p23 = x.z == x.w && y.z == y.w;
+      const float xs[4] = {x.x, x.y, x.z, x.w}, ys[4] = {y.x, y.y, y.z, y.w};
       if (p01 && p23 && x.x == x.z && y.x == y.z) {
         pair_group(sc, fs, scl, S, r0, nrow, ng, x.x, y.x, th, dg, 4);
-      } else {
+      } else if (!pair_cell4(sc, fs, scl, S, r0, nrow, ng, xs, ys, th, dg)) {
         if (p01) {
           pair_group(sc, fs, scl, S, r0, nrow, ng, x.x, y.x, th, dg, 2);
         } else {
