@@ -551,6 +551,40 @@ def test_mixed_global_deposit_groups_match_oracle(lib, oracle, nbins, npart, spl
     assert bunching_ok(bd[:, 24], ob[:, 24])
 
 
+@pytest.mark.parametrize("ng", [45, 201])
+def test_mixed_deposit_same_cell_quads_match_oracle(lib, oracle, ng):
+    """Quiet loading's groups of four mirrored beamlet members share x and y until their
+    energies part; then their positions differ in the last bits while the four still lie
+    in one cell. The mixed deposition sums such a group's weighted phasors before one set
+    of atomics (ngrid 45: the one-CTA field kernel; 201: the cluster bands). Members here
+    get x and y scaled by 1 + k 2^-20 (k = 0..3, kept by FP32), so no group shares them
+    bitwise: slice power and bunching within 1 % of the oracle."""
+    import g4gpu
+    import g4cases as T
+    ns, npart, gm = 4, 1024, 1e-4
+    lat = T.undulator_lattice(1.7, 0.015, 8, 1, 1e-10, 11357.8)
+    part = g4gpu.host_load_beam(T.slice_params(ns, 11357.8, 1.0, 0.4e-6, 15.0), 0, npart, 4, 5, 1, 1e-10, 1.0)
+    scale = 1 + np.tile(np.arange(4), npart // 4) * 2.0 ** -20
+    part[:, :, 2] *= scale
+    part[:, :, 3] *= scale
+    cur = np.full(ns, 3000.0)
+    g1 = g4gpu.host_gauss_hermite(T.gauss_field_par(1e-10, 1e6, 20e-6), gm, ng)
+    fld = np.stack([g1 * (1 + 0.3j * k) for k in range(ns)])
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, gridmax=gm, lambda0=1e-10, sample=1.0,
+                       gammaref=11357.8, precision=1, time_run=1)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam(part, cur)
+        h.load_field(0, fld)
+        h.run(0, lat.shape[0])
+        bd, fd = h.diag(1)
+    rp, rf, rfirst, _ = oracle.run_steps(lat, 11357.8, part, cur, 1e-10, 1.0, [1], [gm], fld[None], [0])
+    of = oracle.diag_field(rf[0], gm, 1e-10, 1, int(rfirst[0]))
+    ob = oracle.diag_beam(rp, 1)
+    assert rel_err(fd[0][:, 0], of[:, 0]) < 1e-2
+    assert bunching_ok(bd[:, 24], ob[:, 24])
+
+
 @pytest.mark.parametrize("prec", [0, 1])
 def test_pinned_host_buffers_round_trip_like_pageable(lib, prec):
     """Loading from and storing to pinned host arrays (through raw pointers, as the
