@@ -531,6 +531,7 @@ int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *tab) {
       for (int k = 0; k < c.nfield; k++) {
         g4::FieldStep &f = s.f[k];
         f.idgrid = 1. / f.dgrid;
+        f.gm_idg = f.gridmax * f.idgrid;
         f.rot_half[0] = std::cos(f.rharm * s.dnom_half);
         f.rot_half[1] = std::sin(f.rharm * s.dnom_half);
         f.rot_full[0] = std::cos(f.rharm * s.dnom_full);

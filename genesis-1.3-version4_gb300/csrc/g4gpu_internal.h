@@ -31,6 +31,7 @@ struct FieldStep {
   int first;      // ring start of the field when the step runs (filled at launch)
   int tw;         // warm-up length of the segmented FP32 tridiagonal solves, 0: not applicable
   double idgrid;  // 1 / dgrid: the FP64 push's cell lookup multiplies
+  double gm_idg;  // gridmax / dgrid: the FP64 cell coordinate is fma(x, idgrid, gm_idg)
   // The FP64 push forms e^{i h theta} at its RK4 stages by rotating e^{i h theta0}: by
   // e^{i h D} for the step's nominal phase advance D (StepConst::dnom_half over half a
   // step, dnom_full over the step) and by a short series for the small remainder.

@@ -109,27 +109,50 @@ __device__ __forceinline__ void transverse(const StepConst &sc, bool last, doubl
 // the neighbour index is then clamped so that no access leaves the grid.
 struct Cell {
   int i00, i10, i01, i11;
-  double wx, wy;
+  double wx, wy;  // the lower-left weights, 1 - ux and 1 - uy
+  double ux, uy;  // the cell coordinates' fractions: the upper/right neighbours' weights
 };
-// The reference divides by the spacing; the push multiplies by its host-computed
-// inverse idg (the weights then differ in the last bit, and a particle within rounding
-// of a cell boundary may take the neighbouring cell, where the bilinear weights give
-// the same value).
+// The reference divides x + gridmax by the spacing; the push forms the cell coordinate
+// as fma(x, 1 / dgrid, gridmax / dgrid) with host-computed factors (the weights then
+// differ in the last bit, and a particle within rounding of a cell boundary may take the
+// neighbouring cell, where the bilinear weights give the same value).
 // |v| < gm for gm > 0 as an integer comparison of the magnitudes' bit patterns: the
 // same verdict as -gm < v < gm for every v (NaN fails both), without the FP64 pipe.
 __device__ __forceinline__ bool inside(double v, double gm) {
   return (unsigned long long)(__double_as_longlong(v) & 0x7fffffffffffffffLL) <
          (unsigned long long)__double_as_longlong(gm);
 }
-__device__ __forceinline__ bool ll_gridpoint(double gm, double idg, int ng, double x, double y,
+// floor(t) and the fraction t - floor(t), both exact, for 0 <= t < 2^31, from the bit
+// pattern on the integer pipe (no FP64 rounding, conversion or subtraction): the
+// significand's bits below the binary point, shifted up to a normalised significand,
+// are the fraction.
+__device__ __forceinline__ int floor_frac(double t, double &frac) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+  const int e = (int)(b >> 52) - 1023;
+  if (e < 0) {  // t < 1
+    frac = t;
+    return 0;
+  }
+  const int sh = 52 - e;  // bits below the binary point
+  const unsigned long long m = (b & ((1ULL << 52) - 1)) | (1ULL << 52);
+  const unsigned long long fb = m & ((1ULL << sh) - 1);
+  const int ip = (int)(m >> sh);
+  if (fb == 0) {
+    frac = 0.;
+    return ip;
+  }
+  const int lz = __clzll((long long)fb);  // fb < 2^52: lz >= 12; its leading one at bit 63 - lz
+  const unsigned long long mant = (fb << (lz - 11)) & ((1ULL << 52) - 1);
+  frac = __longlong_as_double((long long)(((unsigned long long)(1023 + 63 - lz - sh) << 52) | mant));
+  return ip;
+}
+__device__ __forceinline__ bool ll_gridpoint(double gm, double idg, double gmi, int ng, double x, double y,
                                              Cell &c) {
   if (inside(x, gm) && inside(y, gm)) {
-    double wx = (x + gm) * idg;
-    double wy = (y + gm) * idg;
-    double fx = floor(wx), fy = floor(wy);
-    int ix = (int)fx, iy = (int)fy;
-    c.wx = 1 + fx - wx;
-    c.wy = 1 + fy - wy;
+    // x > -gm, so the coordinate is positive
+    const int ix = floor_frac(fma(x, idg, gmi), c.ux), iy = floor_frac(fma(y, idg, gmi), c.uy);
+    c.wx = 1. - c.ux;
+    c.wy = 1. - c.uy;
     int ix1 = ix + 1 < ng ? ix + 1 : ix;
     int iy1 = iy + 1 < ng ? iy + 1 : iy;
     c.i00 = ix + iy * ng;
@@ -299,7 +322,7 @@ __device__ __forceinline__ void deposit_particle(const StepConst &sc, double2 *c
     const FieldStep &fs = sc.f[k];
     if (!fs.dep_on) continue;
     Cell c;
-    if (!ll_gridpoint(fs.gridmax, fs.idgrid, ng, x, y, c)) continue;
+    if (!ll_gridpoint(fs.gridmax, fs.idgrid, fs.gm_idg, ng, x, y, c)) continue;
     const double scl = scls ? scls[k] : deposit_scale(sc, fs, cur, npd);
     double dx = x - sc.ax, dy = y - sc.ay;
     double faw2 = fma(2., fma(sc.grady, dy, sc.gradx * dx), fma(sc.ky * dy, dy, fma(sc.kx * dx, dx, 1.)));
@@ -316,13 +339,13 @@ __device__ __forceinline__ void deposit_particle(const StepConst &sc, double2 *c
     double w = c.wx * c.wy;
     atomicAdd(&d[c.i00].x, w * cpart.x);
     atomicAdd(&d[c.i00].y, w * cpart.y);
-    w = (1 - c.wx) * c.wy;
+    w = c.ux * c.wy;
     atomicAdd(&d[c.i10].x, w * cpart.x);
     atomicAdd(&d[c.i10].y, w * cpart.y);
-    w = c.wx * (1 - c.wy);
+    w = c.wx * c.uy;
     atomicAdd(&d[c.i01].x, w * cpart.x);
     atomicAdd(&d[c.i01].y, w * cpart.y);
-    w = (1 - c.wx) * (1 - c.wy);
+    w = c.ux * c.uy;
     atomicAdd(&d[c.i11].x, w * cpart.x);
     atomicAdd(&d[c.i11].y, w * cpart.y);
   }
@@ -395,10 +418,9 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
     int islice = (is + fs.first) % ns;
     const double2 *f = p.field[k] + (size_t)islice * ncell;
     Cell c;
-    if (ll_gridpoint(fs.gridmax, fs.idgrid, ng, x, y, c)) {
+    if (ll_gridpoint(fs.gridmax, fs.idgrid, fs.gm_idg, ng, x, y, c)) {
       // bilinear weights formed once, the four terms fused into their sum
-      const double w00 = c.wx * c.wy, w10 = (1 - c.wx) * c.wy, w01 = c.wx * (1 - c.wy),
-                   w11 = (1 - c.wx) * (1 - c.wy);
+      const double w00 = c.wx * c.wy, w10 = c.ux * c.wy, w01 = c.wx * c.uy, w11 = c.ux * c.uy;
       const C2 f00 = ld(f + c.i00), f10 = ld(f + c.i10), f01 = ld(f + c.i01), f11 = ld(f + c.i11);
       C2 cpart;
       cpart.x = fma(f11.x, w11, fma(f01.x, w01, fma(f10.x, w10, f00.x * w00)));
