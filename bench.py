@@ -795,6 +795,34 @@ def e2e_window(g4gpu, torch, precision, beam_pinned, cur, field_pinned, lat, ste
     return times, h2d, d2h, phases
 
 
+def lattice_step_times(g4gpu, torch, beam, cur, lat, shapes):
+    """Device time of every step of the whole lattice (CUDA events on the handle's stream
+    between single-step calls), mixed form with the headline's launch shapes: how a step's
+    cost moves over a run as the beam bunches and its energies part."""
+    cfg = g4gpu.Config(nslice=NS, npart=NPART, ngrid=NGRID, gridmax=GRIDMAX, lambda0=LAMBDA0,
+                       sample=1.0, gammaref=GAMMA0, precision=g4gpu.MIXED, time_run=1,
+                       device=torch.cuda.current_device())
+    nlat = lat.shape[0]
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        if shapes is not None:
+            h.set_launch_shapes(*shapes)
+        h.load_beam(beam, cur)
+        h.load_field(0, np.zeros((NS, NGRID * NGRID), dtype=np.complex128))
+        h.synchronize()
+        stream = torch.cuda.ExternalStream(h.stream())
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(nlat + 1)]
+        ev[0].record(stream)
+        for i in range(nlat):
+            h.run(i, 1)
+            ev[i + 1].record(stream)
+        h.synchronize()
+        ms = np.array([ev[i].elapsed_time(ev[i + 1]) for i in range(nlat)])
+    return {"steps": nlat, "total_s": float(ms.sum() / 1e3), "mean_ms": float(ms.mean()),
+            "first_step_ms": float(ms[0]), "steps_2_to_21_mean_ms": float(ms[1:21].mean()),
+            "last_20_mean_ms": float(ms[-20:].mean()), "max_ms_after_first": float(ms[1:].max())}
+
+
 def cpu_sample(lib, ns):
     """ns full-size slices (8192 particles, ngrid 151) from the middle of the
     workload's window, loaded by the checker library's own bit-exact loader (the
@@ -970,6 +998,7 @@ def main():
                             "spread": (max(times) - min(times)) / t,
                             "phases_of_one_window": phases}
         del e2e_out, field_pinned
+        e2e_res["mixed_step_times_over_lattice"] = lattice_step_times(g4gpu, torch, beam, cur, lat, shapes)
     # plain FP64 form, same initial state and steps
     psteps = args.plain_steps if args.plain_steps is not None else args.steps
     do_plain = "plain" in args.forms
