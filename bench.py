@@ -200,7 +200,7 @@ TRAFFIC_SOURCE = "ncu capture of a 608-slice window, scaled to the launch's slic
 # per cell of each plain ADI sweep, from ncu captures of a 152-slice window
 # (profiles/ncu_fp64_k_push_k_adi_plain_sase152.md); nominal GB300 FP64 rate: 1.25 TFLOP/s
 # with FMA counted as two operations, i.e. 625 G FP64 instructions/s.
-FP64_INSTR = {"push_per_particle": 434.1, "adi_per_cell": 17.9}
+FP64_INSTR = {"push_per_particle": 414.1, "adi_per_cell": 17.9}
 FP64_NOMINAL_GINSTR = 625.0
 
 

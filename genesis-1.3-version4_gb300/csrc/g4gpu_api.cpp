@@ -357,6 +357,11 @@ int g4gpu_create(const g4gpu_config *cfg, g4gpu_handle *out) {
   for (auto p : coords)
     if ((rc = alloc(h, p, np * h->rsize))) return bail(rc);
   if ((rc = alloc(h, &h->beam.theta, np * sizeof(double)))) return bail(rc);
+  if (!h->mixed) {
+    if ((rc = alloc(h, &h->beam.phasor, (size_t)c.nfield * np * 16))) return bail(rc);
+    if ((rc = alloc(h, (void **)&h->beam.phasor_ok, sizeof(int)))) return bail(rc);
+    cudaMemsetAsync(h->beam.phasor_ok, 0, sizeof(int), h->stream);
+  }
   if ((rc = alloc(h, (void **)&h->beam.current, c.nslice * sizeof(double)))) return bail(rc);
   // the fused mixed ADI kernel keeps the source and the intermediate on chip: no
   // source or intermediate arrays
@@ -394,7 +399,8 @@ void g4gpu_destroy(g4gpu_handle h) {
                   h->closure_basis, h->closure_feat, h->closure_corr, h->sc.st, h->sc.state, h->sc.ez,
                   h->wake_tab, h->wake_loss, h->wake_lossf, h->wake_scratch, h->count_buf, h->sort_iscratch,
                   h->sort_scratch[0], h->sort_scratch[1], h->sort_scratch[2], h->sort_scratch[3],
-                  h->sort_scratch[4], h->sort_scratch[5], h->isr_ctr, h->sub_theta, h->sub_x, h->sub_y};
+                  h->sort_scratch[4], h->sort_scratch[5], h->isr_ctr, h->sub_theta, h->sub_x, h->sub_y,
+                  h->beam.phasor, h->beam.phasor_ok};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int k = 0; k < G4GPU_MAX_FIELDS; k++) {
@@ -536,6 +542,8 @@ int g4gpu_set_lattice(g4gpu_handle h, int nsteps, const double *tab) {
         f.rot_half[1] = std::sin(f.rharm * s.dnom_half);
         f.rot_full[0] = std::cos(f.rharm * s.dnom_full);
         f.rot_full[1] = std::sin(f.rharm * s.dnom_full);
+        f.rot_auto[0] = std::cos(f.rharm * s.autophase);
+        f.rot_auto[1] = std::sin(f.rharm * s.autophase);
       }
     }
     h->slip[i] = r[G4GPU_LAT_SLIP];
@@ -694,6 +702,11 @@ int g4gpu_set_chicanes(g4gpu_handle h, int nsteps, const double *table) {
   return G4GPU_OK;
 }
 
+// The FP64 push's cached phasors no longer match theta (a load, a sort, a restored state)
+static void phasor_stale(g4gpu_handle h) {
+  if (h->beam.phasor_ok) cudaMemsetAsync(h->beam.phasor_ok, 0, sizeof(int), h->stream);
+}
+
 static int ensure_stage(g4gpu_handle h, size_t n) {
   if (h->stage_bytes >= n) return G4GPU_OK;
   if (h->stage) {
@@ -750,6 +763,7 @@ int g4gpu_load_beam(g4gpu_handle h, const double *particles, const double *curre
     Timed t(h, G4GPU_K_MISC);
     g4::launch_aos_to_soa(h->stream, (const double *)h->stage, soa, h->mixed, h->cfg.gammaref, n);
   }
+  phasor_stale(h);
   G4_CUDA(h, cudaGetLastError());
   h->beam_loaded = true;
   // the wake of every slice follows the window's current
@@ -814,6 +828,7 @@ int g4gpu_sort(g4gpu_handle h, int *shift) {
   for (int k = 0; k < 6; k++)
     G4_CUDA(h, cudaMemcpyAsync(dst[k], h->sort_scratch[k], (size_t)ns * cap * es[k], cudaMemcpyDeviceToDevice,
                                h->stream));
+  phasor_stale(h);
   int over = 0;
   G4_CUDA(h, cudaMemcpyAsync(&over, h->sort_iscratch + 3 * ns, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   G4_CUDA(h, cudaMemcpyAsync(h->hcount.data(), h->count_buf, ns * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -1899,6 +1914,7 @@ static void restore_state(g4gpu_handle h, StateBackup &b, bool release) {
   }
   std::memcpy(h->first, b.first, sizeof(b.first));
   std::memcpy(h->accuslip, b.accuslip, sizeof(b.accuslip));
+  phasor_stale(h);
 }
 
 extern "C" int g4gpu_autotune(g4gpu_handle h, int *push_block, int *field_threads, int *field_kernel) {

@@ -37,6 +37,8 @@ struct FieldStep {
   // step, dnom_full over the step) and by a short series for the small remainder.
   // rot_half / rot_full: cos and sin of rharm * dnom_half / dnom_full.
   double rot_half[2], rot_full[2];
+  // cos and sin of rharm * autophase: the step's phase offset applied to a cached phasor
+  double rot_auto[2];
 };
 
 // Per integration step constants (Undulator accessors, Undulator.h:82-204).
@@ -111,6 +113,11 @@ struct DeviceBeam {
   // particles of every slice when they differ (one4one windows: npart is then the
   // capacity of a slice), null when every slice holds npart
   int *count;
+  // FP64 form: e^{i rharm theta} of every field and particle as the last push left it
+  // ([nfield][nslice * npart] double2), and a device flag, nonzero while it matches theta
+  // (cleared wherever theta is written outside the push); null in the mixed form
+  void *phasor = nullptr;
+  int *phasor_ok = nullptr;
 };
 
 struct Launch {

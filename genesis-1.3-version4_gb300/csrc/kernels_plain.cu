@@ -382,6 +382,11 @@ struct Ptrs {
   const int *count;
   // incoherent radiation: the stream of the step (ctr null: off)
   IsrStream isr;
+  // the cached e^{i rharm theta} of every field ([nfield][pstride]) and its validity flag
+  // (DeviceBeam::phasor), null: none
+  double2 *phasor;
+  const int *phasor_ok;
+  size_t pstride;
 };
 
 // particles of slice is: np, or the slice's own count
@@ -447,15 +452,22 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   }
 
   // e^{i h theta} of every field at the start, and rotated towards the stages: one
-  // sincos per harmonic and particle instead of one per stage
+  // sincos per harmonic and particle instead of one per stage, or none where the last
+  // push left it (the phasor of the stored phase, turned by the step's phase offset)
   const double theta0 = theta;
+  const bool cached = p.phasor && *p.phasor_ok;
   C2 bhalf[NF], bfull[NF], cs[NF];
 #pragma unroll
   for (int k = 0; k < NF; k++) {
     if (k >= sc.nfld) break;
-    double sn, c;
-    sincos(sc.f[k].rharm * theta0, &sn, &c);
-    cs[k] = C2{c, sn};
+    if (cached) {
+      const C2 c = ld(p.phasor + k * p.pstride + o);
+      cs[k] = sc.autophase != 0. ? cmul_fma(c, C2{sc.f[k].rot_auto[0], sc.f[k].rot_auto[1]}) : c;
+    } else {
+      double sn, c;
+      sincos(sc.f[k].rharm * theta0, &sn, &c);
+      cs[k] = C2{c, sn};
+    }
     bhalf[k] = cmul_fma(cs[k], C2{sc.f[k].rot_half[0], sc.f[k].rot_half[1]});
     bfull[k] = cmul_fma(cs[k], C2{sc.f[k].rot_full[0], sc.f[k].rot_full[1]});
   }
@@ -522,13 +534,16 @@ __global__ void __launch_bounds__(512) k_push(StepConst sc, Ptrs p, int ns, int 
   p.px[o] = px;
   p.py[o] = py;
 
-  if (deposit) {
-    // the deposition's phases, rotated on from stage 4's
+  if (deposit || p.phasor) {
+    // the deposition's phases, rotated on from stage 4's, kept for the next push
 #pragma unroll
     for (int k = 0; k < NF; k++) {
       if (k >= sc.nfld) break;
       cs[k] = rotated_on(cs[k], theta - theta3, bfull[k], sc.f[k].rharm, theta, theta0, sc.dnom_full);
+      if (p.phasor) st(p.phasor + k * p.pstride + o, cs[k]);
     }
+  }
+  if (deposit) {
     deposit_particle<NF>(sc, p.src, (size_t)is * ncell, ng, p.current[is], (double)n, gamma,
                          theta, x, y, cs, scls, recip_near(gamma, itg));
   }
@@ -756,6 +771,8 @@ Ptrs make_ptrs(const DeviceBeam &b, void *const *field, void *const *src, int nf
   p.py = (double *)b.py;
   p.current = b.current;
   p.count = b.count;
+  p.phasor = (double2 *)b.phasor;
+  p.phasor_ok = b.phasor_ok;
   for (int k = 0; k < nfld && k < G4GPU_MAX_FIELDS; k++) {
     p.field[k] = field ? (const double2 *)field[k] : nullptr;
     p.src[k] = src ? (double2 *)src[k] : nullptr;
@@ -886,6 +903,10 @@ void launch_push_plain_sc(const Launch &L, const StepConst &sc, const DeviceBeam
   p.eloss = eloss;
   p.wake = (const double *)wake;
   if (mode == 1) deposit = 0;
+  p.pstride = (size_t)ns * np;
+  // a launch that only moves the particles transversely leaves theta and the cache as
+  // they are
+  if (mode == 1) p.phasor = nullptr;
   dim3 grid((np + block - 1) / block, ns);
   cudaStream_t s = (cudaStream_t)L.stream;
   switch (sc.nfld) {
@@ -894,6 +915,8 @@ void launch_push_plain_sc(const Launch &L, const StepConst &sc, const DeviceBeam
     case 3: k_push<3><<<grid, block, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
     default: k_push<G4GPU_MAX_FIELDS><<<grid, block, 0, s>>>(sc, p, ns, np, ngrid, deposit); break;
   }
+  // every particle's phasor now matches its phase (bytes of 1: a nonzero flag)
+  if (p.phasor) cudaMemsetAsync((void *)p.phasor_ok, 1, sizeof(int), s);
 }
 
 void launch_deposit_plain(const Launch &L, const StepConst &sc, const DeviceBeam &b,
