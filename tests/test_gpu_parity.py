@@ -585,6 +585,41 @@ def test_mixed_deposit_same_cell_quads_match_oracle(lib, oracle, ng):
     assert bunching_ok(bd[:, 24], ob[:, 24])
 
 
+def test_plain_phasor_cache_follows_beam_loads(lib):
+    """The FP64 push starts each step from the phasor the previous push left per
+    particle. A beam loaded into a handle that already ran steps must not meet the earlier
+    beam's phasors: after a second load, the steps give what a fresh handle gives (up to the
+    summation order of the deposition's atomics; stale phasors would move the phases by
+    order one)."""
+    import g4gpu
+    import g4cases as T
+    ns, npart, ng, gm = 4, 512, 45, 1e-4
+    lat = T.undulator_lattice(1.7, 0.015, 6, 1, 1e-10, 11357.8)
+    sp = T.slice_params(ns, 11357.8, 1.0, 0.4e-6, 15.0)
+    beam_a = g4gpu.host_load_beam(sp, 0, npart, 4, 5, 1, 1e-10, 1.0)
+    beam_b = g4gpu.host_load_beam(sp, 0, npart, 4, 9, 1, 1e-10, 1.0)
+    cur = np.full(ns, 3000.0)
+    fld = np.zeros((ns, ng * ng), dtype=np.complex128)
+    cfg = g4gpu.Config(nslice=ns, npart=npart, ngrid=ng, gridmax=gm, lambda0=1e-10, sample=1.0,
+                       gammaref=11357.8, precision=0, time_run=1)
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam(beam_a, cur)
+        h.load_field(0, fld)
+        h.run(0, 3)
+        h.load_beam(beam_b, cur)
+        h.load_field(0, fld)
+        h.run(0, lat.shape[0])
+        got = h.get_beam()
+    with g4gpu.Handle(cfg) as h:
+        h.set_lattice(lat)
+        h.load_beam(beam_b, cur)
+        h.load_field(0, fld)
+        h.run(0, lat.shape[0])
+        want = h.get_beam()
+    assert np.allclose(got, want, rtol=1e-9, atol=1e-12)
+
+
 @pytest.mark.parametrize("prec", [0, 1])
 def test_pinned_host_buffers_round_trip_like_pageable(lib, prec):
     """Loading from and storing to pinned host arrays (through raw pointers, as the
